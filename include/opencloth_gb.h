@@ -1,0 +1,167 @@
+/*
+ * opencloth_gb.h — C ABI of the GB300 implicit mass-spring cloth step.
+ *
+ * Drop-in for the step of OpenCloth_Implicit (OpenCloth_Implicit/OpenCloth_Implicit/
+ * main.cpp, cited below as IMP).  The reference step is a set of free functions on
+ * globals:
+ *
+ *   ComputeForces()            IMP:698   -> oc_step (force gather) / oc_compute_forces
+ *   CalcForceDerivatives()     IMP:737   -> oc_step (Jacobians)    / oc_assemble
+ *   IntegrateImplicit(dt)      IMP:775   -> oc_step (assembly, PCG, update)
+ *   StepPhysics(dt)            IMP:873   -> oc_step + oc_provot_ellipsoid (optional passes)
+ *   AddSpring(a,b,ks,kd,type)  IMP:370   -> oc_spring records in oc_cloth_desc
+ *   globals X, V, dV           IMP:80-81, IMP:361 -> oc_set_state / oc_get_state
+ *
+ * Conventions
+ *   - Every entry point returns an oc_status (0 = OC_OK); no C++ exception crosses the
+ *     ABI.  oc_last_error() gives a message for the last failing call on a handle.
+ *   - Host buffers passed in are copied; the library owns all device memory.
+ *   - One CUDA stream per handle (library-owned unless the caller supplies one).  A
+ *     handle is not thread-safe; different handles are independent.
+ *   - Vectors are packed AoS float triples (x, y, z) over all instances of a handle,
+ *     instance k occupying vertices [vertex_offset(k), vertex_offset(k) + n_vertices).
+ *   - Device-side waits are bounded; a wait that gives up surfaces as
+ *     OC_ERR_DEVICE_TIMEOUT.
+ */
+#ifndef OPENCLOTH_GB_H
+#define OPENCLOTH_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------ */
+typedef int32_t oc_status;
+#define OC_OK 0
+#define OC_ERR_INVALID_ARGUMENT 1 /* NULL handle/pointer, non-positive size, bad enum */
+#define OC_ERR_BAD_INDEX 2        /* spring endpoint or pinned index outside [0, n_vertices) */
+#define OC_ERR_NON_FINITE 3       /* NaN or Inf in positions, velocities or parameters */
+#define OC_ERR_DEGENERATE 4       /* zero-length spring (the reference divides by it, IMP:720-727) */
+#define OC_ERR_CUDA 5             /* a CUDA runtime call failed; see oc_last_error */
+#define OC_ERR_OUT_OF_MEMORY 6
+#define OC_ERR_UNSUPPORTED 7      /* option not available for this configuration */
+#define OC_ERR_DEVICE_TIMEOUT 8   /* a bounded device-side wait gave up */
+
+/* ---- per-instance result flags (oc_get_stats) -------------------------------------- */
+#define OC_FLAG_NOT_CONVERGED 1u /* CG stopped at cg_max_iter (normal for the reference's i_max=10) */
+#define OC_FLAG_BREAKDOWN 2u     /* CG direction with d.(A d) <= 0 or non-finite: system not SPD */
+#define OC_FLAG_NON_FINITE 4u    /* a non-finite value appeared in the step */
+
+/* ---- spring: mirrors `struct Spring` IMP:70-75 ------------------------------------ */
+#define OC_STRUCTURAL_SPRING 0 /* IMP:98 */
+#define OC_SHEAR_SPRING 1      /* IMP:99 */
+#define OC_BEND_SPRING 2       /* IMP:100 */
+
+typedef struct oc_spring {
+    int32_t p1, p2;    /* vertex indices within the instance */
+    float rest_length; /* IMP:378: length at creation */
+    float ks, kd;      /* stiffness and damping (kd negative by the reference's convention) */
+    int32_t type;      /* OC_*_SPRING, informational */
+} oc_spring;
+
+/* ---- Jacobian modes -------------------------------------------------------------- */
+/* REFERENCE: vertex i takes spring i's df/dx, df/dv (IMP:782-783 index the per-spring
+ * arrays by vertex), giving a block-diagonal system solved by the reference's PCG. */
+#define OC_JAC_REFERENCE 0
+/* COUPLED: the same per-spring blocks assembled at (p1,p1),(p1,p2),(p2,p1),(p2,p2)
+ * into a 3x3 block-CSR matrix (Baraff-Witkin coupling; no counterpart in the reference). */
+#define OC_JAC_COUPLED 1
+
+/* ---- one cloth (one instance) ----------------------------------------------------- */
+typedef struct oc_cloth_desc {
+    int32_t n_vertices;
+    int32_t n_springs;
+    const oc_spring* springs;  /* n_springs records, in the reference's creation order */
+    const float* mass;         /* n_vertices, or NULL for 1.0 (the reference: M = I, IMP:363) */
+    const int32_t* pinned;     /* indices of pinned vertices (the reference pins 0 and numX) */
+    int32_t n_pinned;
+    const float* ext_force;    /* 3*n_vertices constant external force, or NULL */
+    float gravity[3];          /* IMP:108, added as m*g to unpinned vertices */
+    float velocity_damping;    /* DEFAULT_DAMPING, IMP:104 (-0.125) */
+    int32_t cg_max_iter;       /* i_max, IMP:128 */
+    float cg_tol;              /* EPS, IMP:126; the CG stops when r.r <= EPS^2 * delta0 */
+    int32_t jacobian_mode;     /* OC_JAC_* */
+} oc_cloth_desc;
+
+/* ---- executors ---------------------------------------------------------------------- */
+#define OC_EXEC_AUTO 0     /* resident kernels for instances that fit on chip, streamed otherwise */
+#define OC_EXEC_STREAMED 1 /* multi-kernel step, CG loop in a CUDA-graph WHILE node */
+#define OC_EXEC_RESIDENT 2 /* one cluster of CTAs per instance, the whole step on chip */
+#define OC_EXEC_PLAIN 3    /* one launch sequence per cloth, CG loop driven from the host */
+
+typedef struct oc_options {
+    int32_t executor;        /* OC_EXEC_* */
+    int32_t device;          /* CUDA device ordinal */
+    void* stream;            /* cudaStream_t to use, or NULL for a library-owned stream */
+    int32_t use_graph;       /* 1: replay the step as a CUDA graph (default) */
+    int32_t block_threads;   /* 0: tuned default */
+    int32_t vertices_per_thread; /* 0: tuned default (streamed executor) */
+    int32_t resident_max_vertices; /* 0: tuned default; larger instances are streamed */
+} oc_options;
+
+typedef struct oc_solver oc_solver;
+
+void oc_default_options(oc_options* opts);
+
+/* Validate, pack and upload n_instances cloths.  Positions and velocities start at 0;
+ * set them with oc_set_state.  Fails with OC_ERR_BAD_INDEX / OC_ERR_NON_FINITE /
+ * OC_ERR_DEGENERATE on bad input, without allocating device memory. */
+oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_options* opts, oc_solver** out);
+void oc_destroy(oc_solver* s);
+const char* oc_last_error(const oc_solver* s);
+const char* oc_status_string(oc_status status);
+
+/* Sizes of a handle. */
+oc_status oc_get_counts(const oc_solver* s, int64_t* total_vertices, int64_t* total_springs, int32_t* n_instances);
+oc_status oc_get_vertex_offsets(const oc_solver* s, int64_t* offsets /* n_instances + 1 */);
+
+/* State = X, V and the CG warm start dV (IMP:361, reused as the initial guess at
+ * IMP:788).  Host pointers; any may be NULL to leave that array unchanged/unread.
+ * Synchronous with respect to the handle's stream. */
+oc_status oc_set_state(oc_solver* s, const float* X, const float* V, const float* dV);
+oc_status oc_get_state(oc_solver* s, float* X, float* V, float* dV);
+/* Same with device pointers (packed float triples); enqueued on the handle's stream. */
+oc_status oc_set_state_device(oc_solver* s, const float* X, const float* V, const float* dV);
+oc_status oc_get_state_device(oc_solver* s, float* X, float* V, float* dV);
+
+/* n_steps x { ComputeForces(); IntegrateImplicit(dt); } for every instance.
+ * Asynchronous: enqueued on the handle's stream. */
+oc_status oc_step(oc_solver* s, float dt, int32_t n_steps);
+oc_status oc_synchronize(oc_solver* s);
+
+/* Per-instance results of the last step: CG iterations, relative residual
+ * sqrt(delta_new / delta0), OC_FLAG_* bits.  Any pointer may be NULL. */
+oc_status oc_get_stats(oc_solver* s, int32_t* cg_iters, double* rel_residual, uint32_t* flags);
+
+/* ComputeForces alone on the current state (IMP:698-735): F, packed float triples. */
+oc_status oc_compute_forces(oc_solver* s, float* F);
+/* ComputeForces + CalcForceDerivatives + assembly on the current state (IMP:737-786):
+ * A as 9 floats per vertex (glm column-major) and b as float triples. */
+oc_status oc_assemble(oc_solver* s, float dt, float* A9, float* b);
+
+/* Per-kernel timing of n_steps un-graphed steps (CUDA events on the handle's stream).
+ * names: up to max_kernels kernel names (each <= 31 chars + NUL, 32-byte slots);
+ * ms_total / launches: per kernel.  Returns the number of kernels in *n_kernels. */
+oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_kernels, char* names,
+                           double* ms_total, int64_t* launches, int32_t* n_kernels);
+
+/* ---- reference topology builder (IMP:497-565) ------------------------------------ */
+/* Number of springs InitGL() creates for a cols x rows vertex grid (cols, rows >= 3):
+ * rows*(cols-1) + cols*(rows-1) + 2*(rows-1)*(cols-1) + rows*(cols-1) + cols*(rows-1),
+ * which includes the reference's one duplicate bend spring per row and column. */
+oc_status oc_grid_spring_count(int32_t cols, int32_t rows, int32_t* n_springs);
+/* Springs in the reference's creation order with rest lengths from the exact lattice,
+ * then positions with i.i.d. N(0, (jitter * spacing)^2) noise per coordinate (seeded).
+ * Lattice: x = ((i/(cols-1))*2 - 1) * size/2, y = size + 1 - (j/(rows-1)) * size, z = 0,
+ * vertex j*cols + i; row 0 at the top, so the reference's pins 0 and cols-1 are the two
+ * top corners.  ks/kd are indexed by spring type. */
+oc_status oc_grid_build(int32_t cols, int32_t rows, float size, const float ks[3], const float kd[3],
+                        float jitter, uint64_t seed, float* X, oc_spring* springs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OPENCLOTH_GB_H */

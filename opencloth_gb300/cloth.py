@@ -1,0 +1,280 @@
+"""Host-side interface of the GB300 implicit cloth step.
+
+Two layers over the C ABI (include/opencloth_gb.h):
+
+* ``ClothSolver`` — a handle over one or many cloths (a ragged batch), with state
+  transfer, stepping, statistics and the debug entry points.
+* ``ImplicitCloth`` — the reference's own interface for one cloth
+  (OpenCloth_Implicit/OpenCloth_Implicit/main.cpp): arrays ``X``, ``V``, ``springs``
+  and the functions ``AddSpring`` (IMP:370), ``ComputeForces`` (IMP:698),
+  ``IntegrateImplicit`` (IMP:775) and ``StepPhysics`` (IMP:873), operating on host
+  arrays the caller may edit between steps (IMP:439-444).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Sequence
+
+import numpy as np
+
+from . import _native as N
+from ._native import SPRING_DTYPE, OcError, ptr
+
+STRUCTURAL_SPRING, SHEAR_SPRING, BEND_SPRING = 0, 1, 2
+DEFAULT_DAMPING = -0.125  # IMP:104
+DEFAULT_GRAVITY = (0.0, -0.00981, 0.0)  # IMP:108
+
+_EXECUTORS = {"auto": N.EXEC_AUTO, "streamed": N.EXEC_STREAMED, "resident": N.EXEC_RESIDENT,
+              "plain": N.EXEC_PLAIN}
+
+
+def _check(lib, status: int, handle=None, what: str = "") -> None:
+    if status != N.OC_OK:
+        msg = lib.oc_last_error(handle).decode() if handle else what
+        raise OcError(status, msg or what)
+
+
+@dataclass
+class ClothDesc:
+    """One cloth: springs (``SPRING_DTYPE`` records) over ``n_vertices`` vertices."""
+
+    n_vertices: int
+    springs: np.ndarray
+    mass: np.ndarray | None = None
+    pinned: np.ndarray | None = None
+    ext_force: np.ndarray | None = None
+    gravity: tuple = DEFAULT_GRAVITY
+    velocity_damping: float = DEFAULT_DAMPING
+    cg_max_iter: int = 10  # IMP:128
+    cg_tol: float = 1e-3  # IMP:126
+    jacobian_mode: int = N.JAC_REFERENCE
+    _keep: list = field(default_factory=list, repr=False)
+
+    def to_c(self) -> N.ClothDescC:
+        sp = np.ascontiguousarray(self.springs, dtype=SPRING_DTYPE)
+        mass = None if self.mass is None else np.ascontiguousarray(self.mass, dtype=np.float32)
+        pinned = None if self.pinned is None else np.ascontiguousarray(self.pinned, dtype=np.int32)
+        ext = None if self.ext_force is None else np.ascontiguousarray(self.ext_force, dtype=np.float32)
+        self._keep = [sp, mass, pinned, ext]
+        d = N.ClothDescC()
+        d.n_vertices = int(self.n_vertices)
+        d.n_springs = int(sp.shape[0])
+        d.springs = ptr(sp) if sp.size else None
+        d.mass = ptr(mass)
+        d.pinned = ptr(pinned) if pinned is not None and pinned.size else None
+        d.n_pinned = 0 if pinned is None else int(pinned.size)
+        d.ext_force = ptr(ext)
+        d.gravity[:] = [float(g) for g in self.gravity]
+        d.velocity_damping = float(self.velocity_damping)
+        d.cg_max_iter = int(self.cg_max_iter)
+        d.cg_tol = float(self.cg_tol)
+        d.jacobian_mode = int(self.jacobian_mode)
+        return d
+
+
+def grid_spring_count(cols: int, rows: int) -> int:
+    lib = N.load()
+    n = C.c_int32()
+    _check(lib, lib.oc_grid_spring_count(cols, rows, C.byref(n)), what="oc_grid_spring_count")
+    return int(n.value)
+
+
+def grid_cloth(cols: int, rows: int, size: float = 4.0, ks=(0.75, 0.75, 0.95), kd=(-0.25, -0.25, -0.25),
+               jitter: float = 0.0, seed: int = 0):
+    """The reference's cloth (InitGL, IMP:497-565) on the x-y plane, row 0 on top.
+
+    Returns ``(X, springs)``: positions (cols*rows, 3) float32 and spring records in
+    the reference's creation order.  ``jitter`` is the position noise sigma as a
+    fraction of the grid spacing, applied after rest lengths are taken.
+    """
+    lib = N.load()
+    ns = grid_spring_count(cols, rows)
+    X = np.zeros((cols * rows, 3), np.float32)
+    springs = np.zeros(ns, SPRING_DTYPE)
+    ks_a = np.asarray(ks, np.float32)
+    kd_a = np.asarray(kd, np.float32)
+    _check(lib, lib.oc_grid_build(cols, rows, float(size), ptr(ks_a), ptr(kd_a), float(jitter),
+                                  C.c_uint64(seed & (2**64 - 1)), ptr(X), ptr(springs)), what="oc_grid_build")
+    return X, springs
+
+
+def grid_pins(cols: int) -> np.ndarray:
+    """The reference's hard-coded pins, vertices 0 and numX (IMP:705, IMP:730-732)."""
+    return np.array([0, cols - 1], np.int32)
+
+
+class ClothSolver:
+    """A solver handle over one cloth or a ragged batch of cloths."""
+
+    def __init__(self, descs: ClothDesc | Sequence[ClothDesc], executor: str = "auto", device: int = 0,
+                 use_graph: bool = True, stream: int | None = None, vertices_per_thread: int = 0):
+        self._lib = N.load()
+        if isinstance(descs, ClothDesc):
+            descs = [descs]
+        self.descs = list(descs)
+        arr = (N.ClothDescC * len(self.descs))(*[d.to_c() for d in self.descs])
+        opts = N.OptionsC()
+        self._lib.oc_default_options(C.byref(opts))
+        opts.executor = _EXECUTORS[executor]
+        opts.device = device
+        opts.stream = stream
+        opts.use_graph = 1 if use_graph else 0
+        opts.vertices_per_thread = vertices_per_thread
+        h = C.c_void_p()
+        st = self._lib.oc_create(arr, len(self.descs), C.byref(opts), C.byref(h))
+        if st != N.OC_OK:
+            raise OcError(st, "oc_create failed (details on stderr)")
+        self._h = h
+        nv, ns, ni = C.c_int64(), C.c_int64(), C.c_int32()
+        self._call(self._lib.oc_get_counts(self._h, C.byref(nv), C.byref(ns), C.byref(ni)))
+        self.n_vertices, self.n_springs, self.n_instances = nv.value, ns.value, ni.value
+        self.offsets = np.zeros(self.n_instances + 1, np.int64)
+        self._call(self._lib.oc_get_vertex_offsets(self._h, ptr(self.offsets)))
+
+    def _call(self, status: int) -> None:
+        _check(self._lib, status, self._h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.oc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _vec(self, a) -> np.ndarray | None:
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+        if a.size != 3 * self.n_vertices:
+            raise ValueError(f"expected {3 * self.n_vertices} floats, got {a.size}")
+        return a
+
+    def set_state(self, X=None, V=None, dV=None) -> None:
+        X, V, dV = self._vec(X), self._vec(V), self._vec(dV)
+        self._call(self._lib.oc_set_state(self._h, ptr(X), ptr(V), ptr(dV)))
+
+    def get_state(self):
+        X = np.empty((self.n_vertices, 3), np.float32)
+        V = np.empty_like(X)
+        dV = np.empty_like(X)
+        self._call(self._lib.oc_get_state(self._h, ptr(X), ptr(V), ptr(dV)))
+        return X, V, dV
+
+    def set_state_device(self, X=0, V=0, dV=0) -> None:
+        """Device pointers (ints) to packed float triples; 0 leaves an array unchanged."""
+        self._call(self._lib.oc_set_state_device(self._h, X or None, V or None, dV or None))
+
+    def get_state_device(self, X=0, V=0, dV=0) -> None:
+        self._call(self._lib.oc_get_state_device(self._h, X or None, V or None, dV or None))
+
+    def step(self, dt: float, n_steps: int = 1) -> None:
+        self._call(self._lib.oc_step(self._h, float(dt), int(n_steps)))
+
+    def synchronize(self) -> None:
+        self._call(self._lib.oc_synchronize(self._h))
+
+    def stats(self):
+        it = np.zeros(self.n_instances, np.int32)
+        rr = np.zeros(self.n_instances, np.float64)
+        fl = np.zeros(self.n_instances, np.uint32)
+        self._call(self._lib.oc_get_stats(self._h, ptr(it), ptr(rr), ptr(fl)))
+        return it, rr, fl
+
+    def compute_forces(self) -> np.ndarray:
+        F = np.empty((self.n_vertices, 3), np.float32)
+        self._call(self._lib.oc_compute_forces(self._h, ptr(F)))
+        return F
+
+    def assemble(self, dt: float):
+        """A_i as (N, 3, 3) indexed [column][row] like glm, and b_i as (N, 3)."""
+        A9 = np.empty((self.n_vertices, 3, 3), np.float32)
+        b = np.empty((self.n_vertices, 3), np.float32)
+        self._call(self._lib.oc_assemble(self._h, float(dt), ptr(A9), ptr(b)))
+        return A9, b
+
+    def profile(self, dt: float, n_steps: int) -> dict:
+        names = C.create_string_buffer(32 * 8)
+        ms = np.zeros(8, np.float64)
+        launches = np.zeros(8, np.int64)
+        n = C.c_int32()
+        self._call(self._lib.oc_profile_steps(self._h, float(dt), int(n_steps), 8, names, ptr(ms), ptr(launches),
+                                              C.byref(n)))
+        raw = names.raw
+        out = {}
+        for k in range(n.value):
+            name = raw[32 * k: 32 * (k + 1)].split(b"\0", 1)[0].decode()
+            out[name] = {"ms_total": float(ms[k]), "launches": int(launches[k])}
+        return out
+
+
+class ImplicitCloth:
+    """The reference's step interface for one cloth, on host arrays.
+
+    ``X``, ``V`` (and the warm start ``dV``) are float32 (N, 3) arrays the caller may
+    read and edit between steps.  ``springs`` starts empty; ``AddSpring`` appends a
+    spring whose rest length is the current distance of its endpoints (IMP:370-380).
+    The device handle is created on the first step and rebuilt if springs change.
+    """
+
+    def __init__(self, X: np.ndarray, V: np.ndarray | None = None, pinned: Sequence[int] | None = None,
+                 gravity=DEFAULT_GRAVITY, velocity_damping: float = DEFAULT_DAMPING, mass=None,
+                 cg_max_iter: int = 10, cg_tol: float = 1e-3, executor: str = "auto"):
+        self.X = np.ascontiguousarray(X, np.float32).reshape(-1, 3).copy()
+        self.V = np.zeros_like(self.X) if V is None else np.ascontiguousarray(V, np.float32).reshape(-1, 3).copy()
+        self.dV = np.zeros_like(self.X)
+        self.F = np.zeros_like(self.X)
+        self.springs = np.zeros(0, SPRING_DTYPE)
+        self.pinned = None if pinned is None else np.asarray(pinned, np.int32)
+        self.gravity = tuple(gravity)
+        self.velocity_damping = float(velocity_damping)
+        self.mass = mass
+        self.cg_max_iter = int(cg_max_iter)
+        self.cg_tol = float(cg_tol)
+        self.executor = executor
+        self._solver: ClothSolver | None = None
+        self._springs_seen = None
+
+    def AddSpring(self, a: int, b: int, ks: float, kd: float, type: int) -> None:  # noqa: N802 (reference name)
+        d = self.X[a] - self.X[b]
+        rest = np.sqrt(np.float32(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]), dtype=np.float32)
+        rec = np.array([(a, b, rest, ks, kd, type)], SPRING_DTYPE)
+        self.springs = np.concatenate([self.springs, rec])
+
+    def _handle(self) -> ClothSolver:
+        key = (self.springs.tobytes(), None if self.pinned is None else self.pinned.tobytes())
+        if self._solver is None or self._springs_seen != key:
+            if self._solver is not None:
+                self._solver.close()
+            desc = ClothDesc(n_vertices=self.X.shape[0], springs=self.springs, pinned=self.pinned,
+                             mass=self.mass, gravity=self.gravity, velocity_damping=self.velocity_damping,
+                             cg_max_iter=self.cg_max_iter, cg_tol=self.cg_tol)
+            self._solver = ClothSolver(desc, executor=self.executor)
+            self._springs_seen = key
+        return self._solver
+
+    def ComputeForces(self) -> np.ndarray:  # noqa: N802
+        s = self._handle()
+        s.set_state(self.X, self.V, self.dV)
+        self.F = s.compute_forces()
+        return self.F
+
+    def IntegrateImplicit(self, dt: float) -> None:  # noqa: N802
+        s = self._handle()
+        s.set_state(self.X, self.V, self.dV)
+        s.step(dt, 1)
+        self.X, self.V, self.dV = s.get_state()
+
+    def StepPhysics(self, dt: float) -> None:  # noqa: N802
+        """ComputeForces(); IntegrateImplicit(dt); (IMP:873-876)."""
+        self.IntegrateImplicit(dt)

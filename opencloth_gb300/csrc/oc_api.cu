@@ -1,0 +1,519 @@
+// C ABI (include/opencloth_gb.h): handle lifetime, state transfer, and the three ways
+// of running a step — a CUDA graph whose CG loop is a device-driven WHILE node, the
+// same kernels launched directly with the loop driven from the host, and the plain
+// one-cloth-per-launch sequence.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "oc_internal.h"
+
+using namespace oc;
+
+struct oc_solver {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int32_t executor = OC_EXEC_STREAMED;
+    bool use_graph = true;
+    int32_t n_inst = 0;
+    int64_t nv = 0, ns = 0;
+    int32_t n_blocks = 0;
+    int32_t vertices_per_block = 0;
+    std::vector<int64_t> v_off;
+    std::vector<InstParams> inst_host;
+    std::vector<void*> allocs;
+    StepArgs args{};
+    float* stage = nullptr;         // device staging: 3 x 3 * nv floats
+    int32_t* d_err = nullptr;       // device validation flag
+    InstState* h_state = nullptr;   // pinned host mirror of the instance states
+    int32_t* h_scalar = nullptr;    // pinned host scalar for loop control
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    float graph_dt = 0.0f;
+    std::string err;
+};
+
+namespace {
+
+oc_status fail(oc_solver* s, oc_status code, const std::string& msg) {
+    if (s) s->err = msg;
+    return code;
+}
+
+oc_status fail_cuda(oc_solver* s, cudaError_t e, const char* what) {
+    const oc_status code = (e == cudaErrorMemoryAllocation) ? OC_ERR_OUT_OF_MEMORY : OC_ERR_CUDA;
+    return fail(s, code, std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+#define OC_TRY(call)                                          \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return fail_cuda(s, e_, #call); \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(oc_solver* s, T** p, size_t count) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess) s->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return e;
+}
+
+template <class T>
+cudaError_t upload(oc_solver* s, T** p, const std::vector<T>& v) {
+    cudaError_t e = dalloc(s, p, v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+void release(oc_solver* s) {
+    if (!s) return;
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    for (void* p : s->allocs) cudaFree(p);
+    s->allocs.clear();
+    if (s->h_state) cudaFreeHost(s->h_state);
+    if (s->h_scalar) cudaFreeHost(s->h_scalar);
+    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+}
+
+// One step with the CG loop driven from the host.  per_cloth: launch each instance's
+// blocks separately (the plain one-cloth-per-launch baseline).  timer: optional
+// per-kernel timing callback around every launch.
+struct KernelTimer {
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    double ms[K_COUNT] = {0};
+    int64_t launches[K_COUNT] = {0};
+};
+
+oc_status launch_timed(oc_solver* s, KernelKind k, const StepArgs& a, int nblocks, KernelTimer* t) {
+    if (t) OC_TRY(cudaEventRecord(t->ev[0], s->stream));
+    OC_TRY(launch_kernel(k, a, nblocks, s->stream));
+    if (t) {
+        OC_TRY(cudaEventRecord(t->ev[1], s->stream));
+        OC_TRY(cudaEventSynchronize(t->ev[1]));
+        float ms = 0.0f;
+        OC_TRY(cudaEventElapsedTime(&ms, t->ev[0], t->ev[1]));
+        t->ms[k] += ms;
+        t->launches[k] += 1;
+    }
+    return OC_OK;
+}
+
+oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* t) {
+    StepArgs a = s->args;
+    a.dt = dt;
+    a.use_cond = 0;
+    a.cond = 0;
+    OC_TRY(cudaMemsetAsync(a.unconverged, 0, sizeof(int32_t), s->stream));
+    const int n_groups = per_cloth ? s->n_inst : 1;
+    for (int grp = 0; grp < n_groups; ++grp) {
+        a.blk_base = per_cloth ? s->inst_host[grp].blk0 : 0;
+        const int nb = per_cloth ? s->inst_host[grp].nblk : s->n_blocks;
+        oc_status st = launch_timed(s, K_ASSEMBLE, a, nb, t);
+        if (st != OC_OK) return st;
+        for (;;) {
+            if (per_cloth)
+                OC_TRY(cudaMemcpyAsync(s->h_scalar, &s->args.state[grp].active, sizeof(int32_t),
+                                       cudaMemcpyDeviceToHost, s->stream));
+            else
+                OC_TRY(cudaMemcpyAsync(s->h_scalar, a.unconverged, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                       s->stream));
+            OC_TRY(cudaStreamSynchronize(s->stream));
+            if (*s->h_scalar <= 0) break;
+            if ((st = launch_timed(s, K_CG_DIR, a, nb, t)) != OC_OK) return st;
+            if ((st = launch_timed(s, K_CG_UPDATE, a, nb, t)) != OC_OK) return st;
+        }
+        if ((st = launch_timed(s, K_INTEGRATE, a, nb, t)) != OC_OK) return st;
+    }
+    return OC_OK;
+}
+
+oc_status build_graph(oc_solver* s, float dt) {
+    if (s->exec) {
+        cudaGraphExecDestroy(s->exec);
+        s->exec = nullptr;
+    }
+    if (s->graph) {
+        cudaGraphDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    OC_TRY(cudaGraphCreate(&g, 0));
+    s->graph = g;
+    cudaGraphConditionalHandle handle;
+    OC_TRY(cudaGraphConditionalHandleCreate(&handle, g, 0, 0));
+
+    StepArgs a = s->args;
+    a.dt = dt;
+    a.blk_base = 0;
+    a.use_cond = 1;
+    a.cond = (unsigned long long)handle;
+    void* params[] = {&a};
+    auto kparams = [&](KernelKind k) {
+        cudaKernelNodeParams kp{};
+        kp.func = const_cast<void*>(kernel_fn(k));
+        kp.gridDim = dim3((unsigned)s->n_blocks);
+        kp.blockDim = dim3((unsigned)kernel_block_threads());
+        kp.sharedMemBytes = 0;
+        kp.kernelParams = params;
+        kp.extra = nullptr;
+        return kp;
+    };
+
+    cudaGraphNode_t n_reset, n_asm, n_loop, n_dir, n_upd, n_int;
+    cudaMemsetParams mp{};
+    mp.dst = a.unconverged;
+    mp.value = 0;
+    mp.elementSize = sizeof(int32_t);
+    mp.width = 1;
+    mp.height = 1;
+    mp.pitch = sizeof(int32_t);
+    OC_TRY(cudaGraphAddMemsetNode(&n_reset, g, nullptr, 0, &mp));
+    cudaKernelNodeParams kp = kparams(K_ASSEMBLE);
+    OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &n_reset, 1, &kp));
+
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    OC_TRY(cudaGraphAddNode(&n_loop, g, &n_asm, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    kp = kparams(K_CG_DIR);
+    OC_TRY(cudaGraphAddKernelNode(&n_dir, body, nullptr, 0, &kp));
+    kp = kparams(K_CG_UPDATE);
+    OC_TRY(cudaGraphAddKernelNode(&n_upd, body, &n_dir, 1, &kp));
+
+    kp = kparams(K_INTEGRATE);
+    OC_TRY(cudaGraphAddKernelNode(&n_int, g, &n_loop, 1, &kp));
+    OC_TRY(cudaGraphInstantiate(&s->exec, g, 0));
+    s->graph_dt = dt;
+    return OC_OK;
+}
+
+bool valid_solver(const oc_solver* s) { return s != nullptr && s->nv > 0; }
+
+}  // namespace
+
+extern "C" {
+
+void oc_default_options(oc_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->executor = OC_EXEC_AUTO;
+    o->device = 0;
+    o->stream = nullptr;
+    o->use_graph = 1;
+}
+
+const char* oc_status_string(oc_status st) {
+    switch (st) {
+        case OC_OK: return "OC_OK";
+        case OC_ERR_INVALID_ARGUMENT: return "OC_ERR_INVALID_ARGUMENT";
+        case OC_ERR_BAD_INDEX: return "OC_ERR_BAD_INDEX";
+        case OC_ERR_NON_FINITE: return "OC_ERR_NON_FINITE";
+        case OC_ERR_DEGENERATE: return "OC_ERR_DEGENERATE";
+        case OC_ERR_CUDA: return "OC_ERR_CUDA";
+        case OC_ERR_OUT_OF_MEMORY: return "OC_ERR_OUT_OF_MEMORY";
+        case OC_ERR_UNSUPPORTED: return "OC_ERR_UNSUPPORTED";
+        case OC_ERR_DEVICE_TIMEOUT: return "OC_ERR_DEVICE_TIMEOUT";
+        default: return "OC_ERR_UNKNOWN";
+    }
+}
+
+const char* oc_last_error(const oc_solver* s) { return s ? s->err.c_str() : "NULL solver"; }
+
+oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_options* opts, oc_solver** out) {
+    if (!out) return OC_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    oc_options o;
+    oc_default_options(&o);
+    if (opts) o = *opts;
+    if (o.executor < OC_EXEC_AUTO || o.executor > OC_EXEC_PLAIN) return OC_ERR_INVALID_ARGUMENT;
+    if (o.executor == OC_EXEC_RESIDENT) return OC_ERR_UNSUPPORTED;
+    if (o.vertices_per_thread < 0 || o.vertices_per_thread > 64 || o.block_threads < 0) return OC_ERR_INVALID_ARGUMENT;
+    if (o.block_threads != 0 && o.block_threads != kernel_block_threads()) return OC_ERR_UNSUPPORTED;
+
+    oc_solver* s = new (std::nothrow) oc_solver();
+    if (!s) return OC_ERR_OUT_OF_MEMORY;
+    const int vpt = o.vertices_per_thread > 0 ? o.vertices_per_thread : 1;
+    PackedHost P;
+    oc_status st = pack_instances(descs, n_instances, kernel_block_threads() * vpt, &P, &s->err);
+    if (st != OC_OK) {
+        // The message is only reachable through a handle; print it for the caller.
+        std::fprintf(stderr, "oc_create: %s\n", s->err.c_str());
+        delete s;
+        return st;
+    }
+    auto bail = [&](oc_status code) {
+        std::fprintf(stderr, "oc_create: %s\n", s->err.c_str());
+        release(s);
+        delete s;
+        return code;
+    };
+#define OC_CREATE_TRY(call)                                           \
+    do {                                                              \
+        cudaError_t e_ = (call);                                      \
+        if (e_ != cudaSuccess) return bail(fail_cuda(s, e_, #call));  \
+    } while (0)
+
+    s->device = o.device;
+    s->executor = (o.executor == OC_EXEC_PLAIN) ? OC_EXEC_PLAIN : OC_EXEC_STREAMED;
+    s->use_graph = o.use_graph != 0;
+    s->n_inst = P.n_inst;
+    s->nv = P.nv;
+    s->ns = P.ns;
+    s->v_off = P.v_off;
+    s->inst_host = P.inst;
+    s->n_blocks = (int32_t)P.blocks.size();
+    s->vertices_per_block = P.vertices_per_block;
+    OC_CREATE_TRY(cudaSetDevice(o.device));
+    if (o.stream) {
+        s->stream = static_cast<cudaStream_t>(o.stream);
+    } else {
+        OC_CREATE_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        s->own_stream = true;
+    }
+
+    StepArgs& a = s->args;
+    OC_CREATE_TRY(upload(s, &a.X, P.X0));
+    OC_CREATE_TRY(upload(s, &a.V, P.V0));
+    float4* fext = nullptr;
+    if (!P.fext.empty()) OC_CREATE_TRY(upload(s, &fext, P.fext));
+    a.fext = fext;
+    int32_t* rowptr = nullptr;
+    int4* inc = nullptr;
+    int2* own_ends = nullptr;
+    float4* own_par = nullptr;
+    OC_CREATE_TRY(upload(s, &rowptr, P.rowptr));
+    OC_CREATE_TRY(upload(s, &inc, P.inc));
+    OC_CREATE_TRY(upload(s, &own_ends, P.own_ends));
+    OC_CREATE_TRY(upload(s, &own_par, P.own_par));
+    a.rowptr = rowptr;
+    a.inc = inc;
+    a.own_ends = own_ends;
+    a.own_par = own_par;
+    const size_t stride = (size_t)((P.nv + 63) / 64) * 64;
+    float* planes = nullptr;
+    OC_CREATE_TRY(dalloc(s, &planes, 15 * stride));
+    OC_CREATE_TRY(cudaMemset(planes, 0, 15 * stride * sizeof(float)));
+    for (int k = 0; k < 6; ++k) a.A[k] = planes + k * stride;
+    for (int k = 0; k < 3; ++k) {
+        a.x[k] = planes + (6 + k) * stride;
+        a.r[k] = planes + (9 + k) * stride;
+        a.d[k] = planes + (12 + k) * stride;
+    }
+    OC_CREATE_TRY(dalloc(s, &a.partials, P.blocks.size()));
+    InstParams* inst = nullptr;
+    OC_CREATE_TRY(upload(s, &inst, P.inst));
+    a.inst = inst;
+    OC_CREATE_TRY(dalloc(s, &a.state, (size_t)P.n_inst));
+    OC_CREATE_TRY(cudaMemset(a.state, 0, sizeof(InstState) * P.n_inst));
+    BlockInfo* blocks = nullptr;
+    OC_CREATE_TRY(upload(s, &blocks, P.blocks));
+    a.blocks = blocks;
+    OC_CREATE_TRY(dalloc(s, &a.unconverged, 1));
+    OC_CREATE_TRY(dalloc(s, &a.grid_ticket, 1));
+    OC_CREATE_TRY(cudaMemset(a.unconverged, 0, sizeof(int32_t)));
+    OC_CREATE_TRY(cudaMemset(a.grid_ticket, 0, sizeof(uint32_t)));
+    OC_CREATE_TRY(dalloc(s, &s->stage, 9 * (size_t)P.nv));
+    OC_CREATE_TRY(dalloc(s, &s->d_err, 1));
+    OC_CREATE_TRY(cudaMallocHost(&s->h_state, sizeof(InstState) * P.n_inst));
+    OC_CREATE_TRY(cudaMallocHost(&s->h_scalar, sizeof(int32_t)));
+    a.vpt = vpt;
+    OC_CREATE_TRY(cudaDeviceSynchronize());
+#undef OC_CREATE_TRY
+    *out = s;
+    return OC_OK;
+}
+
+void oc_destroy(oc_solver* s) {
+    if (!s) return;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    release(s);
+    delete s;
+}
+
+oc_status oc_get_counts(const oc_solver* s, int64_t* total_vertices, int64_t* total_springs, int32_t* n_instances) {
+    if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
+    if (total_vertices) *total_vertices = s->nv;
+    if (total_springs) *total_springs = s->ns;
+    if (n_instances) *n_instances = s->n_inst;
+    return OC_OK;
+}
+
+oc_status oc_get_vertex_offsets(const oc_solver* s, int64_t* offsets) {
+    if (!valid_solver(s) || !offsets) return OC_ERR_INVALID_ARGUMENT;
+    std::memcpy(offsets, s->v_off.data(), sizeof(int64_t) * s->v_off.size());
+    return OC_OK;
+}
+
+oc_status oc_set_state_device(oc_solver* s, const float* X, const float* V, const float* dV) {
+    if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    OC_TRY(cudaMemsetAsync(s->d_err, 0, sizeof(int32_t), s->stream));
+    OC_TRY(launch_state_in(s->args, X, V, dV, s->nv, s->d_err, s->stream));
+    return OC_OK;
+}
+
+oc_status oc_get_state_device(oc_solver* s, float* X, float* V, float* dV) {
+    if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    OC_TRY(launch_state_out(s->args, X, V, dV, s->nv, s->stream));
+    return OC_OK;
+}
+
+oc_status oc_set_state(oc_solver* s, const float* X, const float* V, const float* dV) {
+    if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    const size_t n3 = 3 * (size_t)s->nv;
+    float* sx = X ? s->stage : nullptr;
+    float* sv = V ? s->stage + n3 : nullptr;
+    float* sd = dV ? s->stage + 2 * n3 : nullptr;
+    if (X) OC_TRY(cudaMemcpyAsync(sx, X, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    if (V) OC_TRY(cudaMemcpyAsync(sv, V, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    if (dV) OC_TRY(cudaMemcpyAsync(sd, dV, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    OC_TRY(cudaMemsetAsync(s->d_err, 0, sizeof(int32_t), s->stream));
+    OC_TRY(launch_state_in(s->args, sx, sv, sd, s->nv, s->d_err, s->stream));
+    OC_TRY(cudaMemcpyAsync(s->h_scalar, s->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    if (*s->h_scalar != 0) return fail(s, OC_ERR_NON_FINITE, "oc_set_state: non-finite value in the new state");
+    return OC_OK;
+}
+
+oc_status oc_get_state(oc_solver* s, float* X, float* V, float* dV) {
+    if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    const size_t n3 = 3 * (size_t)s->nv;
+    float* sx = X ? s->stage : nullptr;
+    float* sv = V ? s->stage + n3 : nullptr;
+    float* sd = dV ? s->stage + 2 * n3 : nullptr;
+    OC_TRY(launch_state_out(s->args, sx, sv, sd, s->nv, s->stream));
+    if (X) OC_TRY(cudaMemcpyAsync(X, sx, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    if (V) OC_TRY(cudaMemcpyAsync(V, sv, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    if (dV) OC_TRY(cudaMemcpyAsync(dV, sd, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    return OC_OK;
+}
+
+oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
+    if (!valid_solver(s) || n_steps < 0 || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    if (s->executor == OC_EXEC_PLAIN) {
+        for (int32_t i = 0; i < n_steps; ++i) {
+            oc_status st = step_host_driven(s, dt, true, nullptr);
+            if (st != OC_OK) return st;
+        }
+        return OC_OK;
+    }
+    if (!s->use_graph) {
+        for (int32_t i = 0; i < n_steps; ++i) {
+            oc_status st = step_host_driven(s, dt, false, nullptr);
+            if (st != OC_OK) return st;
+        }
+        return OC_OK;
+    }
+    if (!s->exec || s->graph_dt != dt) {
+        oc_status st = build_graph(s, dt);
+        if (st != OC_OK) return st;
+    }
+    for (int32_t i = 0; i < n_steps; ++i) OC_TRY(cudaGraphLaunch(s->exec, s->stream));
+    return OC_OK;
+}
+
+oc_status oc_synchronize(oc_solver* s) {
+    if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    return OC_OK;
+}
+
+oc_status oc_get_stats(oc_solver* s, int32_t* cg_iters, double* rel_residual, uint32_t* flags) {
+    if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    OC_TRY(cudaMemcpyAsync(s->h_state, s->args.state, sizeof(InstState) * s->n_inst, cudaMemcpyDeviceToHost,
+                           s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    for (int32_t k = 0; k < s->n_inst; ++k) {
+        const InstState& st = s->h_state[k];
+        if (cg_iters) cg_iters[k] = st.iter;
+        if (rel_residual) rel_residual[k] = st.delta0 > 0.0 ? std::sqrt(st.delta_new / st.delta0) : 0.0;
+        if (flags) flags[k] = st.flags;
+    }
+    return OC_OK;
+}
+
+oc_status oc_compute_forces(oc_solver* s, float* F) {
+    if (!valid_solver(s) || !F) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    StepArgs a = s->args;
+    a.dbg_F = s->stage;
+    a.blk_base = 0;
+    OC_TRY(launch_kernel(K_FORCES, a, s->n_blocks, s->stream));
+    OC_TRY(cudaMemcpyAsync(F, s->stage, 3 * (size_t)s->nv * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    return OC_OK;
+}
+
+oc_status oc_assemble(oc_solver* s, float dt, float* A9, float* b) {
+    if (!valid_solver(s) || !A9 || !b || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    float* dA9 = nullptr;
+    OC_TRY(cudaMallocAsync(&dA9, 9 * (size_t)s->nv * sizeof(float), s->stream));
+    StepArgs a = s->args;
+    a.dt = dt;
+    a.blk_base = 0;
+    a.use_cond = 0;
+    a.dbg_A9 = dA9;
+    a.dbg_b = s->stage;
+    cudaError_t e = launch_kernel(K_ASSEMBLE, a, s->n_blocks, s->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(A9, dA9, 9 * (size_t)s->nv * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b, s->stage, 3 * (size_t)s->nv * sizeof(float), cudaMemcpyDeviceToHost, s->stream);
+    // The assembly pass also primed the CG loop; leave no instance marked running.
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->args.unconverged, 0, sizeof(int32_t), s->stream);
+    cudaFreeAsync(dA9, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return fail_cuda(s, e, "oc_assemble");
+    return OC_OK;
+}
+
+oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_kernels, char* names,
+                           double* ms_total, int64_t* launches, int32_t* n_kernels) {
+    if (!valid_solver(s) || n_steps < 0 || max_kernels < 0 || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    KernelTimer t;
+    OC_TRY(cudaEventCreate(&t.ev[0]));
+    OC_TRY(cudaEventCreate(&t.ev[1]));
+    oc_status st = OC_OK;
+    for (int32_t i = 0; i < n_steps && st == OC_OK; ++i)
+        st = step_host_driven(s, dt, s->executor == OC_EXEC_PLAIN, &t);
+    cudaEventDestroy(t.ev[0]);
+    cudaEventDestroy(t.ev[1]);
+    if (st != OC_OK) return st;
+    const KernelKind kinds[] = {K_ASSEMBLE, K_CG_DIR, K_CG_UPDATE, K_INTEGRATE};
+    int32_t n = 0;
+    for (KernelKind k : kinds) {
+        if (n >= max_kernels) break;
+        if (names) {
+            std::memset(names + 32 * n, 0, 32);
+            std::strncpy(names + 32 * n, kernel_name(k), 31);
+        }
+        if (ms_total) ms_total[n] = t.ms[k];
+        if (launches) launches[n] = t.launches[k];
+        ++n;
+    }
+    if (n_kernels) *n_kernels = n;
+    return OC_OK;
+}
+
+}  // extern "C"

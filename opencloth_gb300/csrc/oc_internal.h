@@ -1,0 +1,108 @@
+// Internal types shared by the C-ABI layer and the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "opencloth_gb.h"
+
+namespace oc {
+
+// Per-instance constants, device resident, read by every kernel of a step.
+struct InstParams {
+    float gravity[3];
+    float damping;  // DEFAULT_DAMPING, IMP:104
+    float eps2;     // EPS*EPS rounded to float, IMP:127
+    int32_t imax;   // i_max, IMP:128
+    int32_t blk0;   // first streamed block of the instance
+    int32_t nblk;   // streamed blocks of the instance
+    int64_t v_off;  // first vertex (global index)
+    int32_t nv;
+    int32_t has_ext;
+};
+
+// Per-instance CG scalars, device resident, written by the last block of each
+// instance (deterministic fixed-order reduction of per-block FP64 partials).
+struct InstState {
+    double delta_new;  // r.r (first: r.(P r)), IMP:317/325
+    double delta0;
+    double dq;         // d.(A d), IMP:321
+    float alpha, beta;
+    int32_t iter;
+    int32_t active;    // 1 while the CG loop runs for this instance
+    uint32_t flags;    // OC_FLAG_*
+    uint32_t ticket;   // arrivals of this instance's blocks in the current kernel
+};
+
+// One streamed block: a contiguous vertex range of one instance.
+struct BlockInfo {
+    int32_t inst;
+    int32_t local_blk;  // index of this block within its instance
+    int64_t v_begin;    // global vertex range [v_begin, v_end)
+    int64_t v_end;
+};
+
+// Everything a streamed kernel needs, passed by value.
+struct StepArgs {
+    float4* X;               // x, y, z, mass
+    float4* V;               // x, y, z, pinned (0 or 1)
+    const float4* fext;      // external force or nullptr
+    const int32_t* rowptr;   // vertex -> incidence range (global), n_vertices + 1
+    const int4* inc;         // {other | is_p2 << 31, rest, ks, kd} in spring order
+    const int2* own_ends;    // vertex i -> endpoints of spring i (global), or -1
+    const float4* own_par;   // vertex i -> rest, ks, kd of spring i
+    float* A[6];             // symmetric A: a00 a01 a02 a11 a12 a22 planes
+    float* x[3];             // CG solution = persistent warm start dV
+    float* r[3];
+    float* d[3];
+    double* partials;        // one per streamed block
+    const InstParams* inst;
+    InstState* state;
+    const BlockInfo* blocks;
+    int32_t* unconverged;    // number of instances whose CG is running
+    uint32_t* grid_ticket;   // arrivals of all blocks in the current kernel
+    float dt;
+    int32_t blk_base;        // first block of this launch (per-cloth launches)
+    int32_t vpt;             // vertices per thread
+    int32_t use_cond;        // 1: set the graph WHILE condition
+    unsigned long long cond; // cudaGraphConditionalHandle
+    float* dbg_F;            // optional debug outputs (float triples) or nullptr
+    float* dbg_A9;
+    float* dbg_b;
+};
+
+enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3, K_FORCES = 4, K_COUNT = 5 };
+
+const char* kernel_name(KernelKind k);
+const void* kernel_fn(KernelKind k);
+int kernel_block_threads();
+
+// Host-side launch of one kernel kind over [blk_base, blk_base + nblocks).
+cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStream_t stream);
+
+cudaError_t launch_state_in(const StepArgs& a, const float* X3, const float* V3, const float* dV3, int64_t nv,
+                            int32_t* err, cudaStream_t stream);
+cudaError_t launch_state_out(const StepArgs& a, float* X3, float* V3, float* dV3, int64_t nv, cudaStream_t stream);
+
+// Topology / validation helpers (oc_topology.cpp).
+struct PackedHost {
+    int32_t n_inst = 0;
+    int64_t nv = 0, ns = 0;
+    std::vector<int64_t> v_off, s_off;
+    std::vector<InstParams> inst;
+    std::vector<float4> X0, V0, fext;  // fext empty when no instance has one
+    std::vector<int32_t> rowptr;
+    std::vector<int4> inc;
+    std::vector<int2> own_ends;
+    std::vector<float4> own_par;
+    std::vector<BlockInfo> blocks;
+    int32_t vertices_per_block = 0;
+};
+
+oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vertices_per_block, PackedHost* out,
+                         std::string* err);
+
+}  // namespace oc

@@ -1,0 +1,512 @@
+// Streamed executor: the implicit step as four kernels over a ragged batch.
+//
+//   k_assemble   ComputeForces (IMP:698-735) as a per-vertex gather over the
+//                incidence CSR, CalcForceDerivatives for spring i (IMP:737-772),
+//                the assembly of A_i, b_i, P_i (IMP:781-786) and the CG set-up
+//                r = b - A x, d = P^-1 r, delta0 = r.(P r) (IMP:310-318).
+//   k_cg_dir     [d = r + beta d]; alpha = delta_new / d.(A d)    (IMP:320-321, 327)
+//   k_cg_update  x += alpha d; r -= alpha A d; delta_new = r.r     (IMP:322-326)
+//   k_integrate  V += dV dt; X += dt V; ground clamp               (IMP:790-797)
+//
+// Compiled with --fmad=false and IEEE division / square root so every FP32 operation
+// rounds exactly as the reference's scalar code does; the CG dot products alone
+// accumulate in FP64 (per-vertex FP32 dot terms, summed in double).
+//
+// Reductions are deterministic: each block writes one FP64 partial; the last block of
+// an instance to finish (atomic ticket) sums that instance's partials in a fixed order
+// and updates the instance's CG scalars.  The last block of the whole grid sets the
+// CUDA-graph WHILE condition to "some instance still iterating".
+#include <cuda_runtime.h>
+
+#include "oc_internal.h"
+
+namespace oc {
+namespace {
+
+constexpr int kThreads = 256;
+
+struct SpringEval {
+    float C, Cdot;
+    float n[3];  // dc_dp
+    float q[3];  // deltaP2
+};
+
+// Spring force on p1, IMP:717-728 (glm length / normalize rounding order).
+__device__ __forceinline__ float3 spring_force(const float4 p1, const float4 p2, const float4 v1, const float4 v2,
+                                               float rest, float ks, float kd) {
+    const float dPx = p1.x - p2.x, dPy = p1.y - p2.y, dPz = p1.z - p2.z;
+    const float dVx = v1.x - v2.x, dVy = v1.y - v2.y, dVz = v1.z - v2.z;
+    const float sqr = dPx * dPx + dPy * dPy + dPz * dPz;
+    const float dist = sqrtf(sqr);
+    const float left = (-ks) * (dist - rest);
+    const float right = kd * ((dVx * dPx + dVy * dPy + dVz * dPz) / dist);
+    const float inv = 1.0f / sqrtf(sqr);
+    const float mag = left + right;
+    return make_float3(mag * (dPx * inv), mag * (dPy * inv), mag * (dPz * inv));
+}
+
+// The per-spring quantities CalcForceDerivatives reads, IMP:719-724.
+__device__ __forceinline__ void spring_state(const float4 p1, const float4 p2, const float4 v1, const float4 v2,
+                                             float rest, SpringEval& e) {
+    const float dPx = p1.x - p2.x, dPy = p1.y - p2.y, dPz = p1.z - p2.z;
+    const float sqr = dPx * dPx + dPy * dPy + dPz * dPz;
+    const float dist = sqrtf(sqr);
+    e.C = dist - rest;
+    e.n[0] = dPx / dist;
+    e.n[1] = dPy / dist;
+    e.n[2] = dPz / dist;
+    e.Cdot = (v1.x * (-e.n[0]) + v1.y * (-e.n[1]) + v1.z * (-e.n[2])) +
+             (v2.x * e.n[0] + v2.y * e.n[1] + v2.z * e.n[2]);
+    e.q[0] = dPx * dPx;
+    e.q[1] = dPy * dPy;
+    e.q[2] = dPz * dPz;
+}
+
+// One element m[c][r] of df_dx and df_dv for one spring, IMP:744-770.  d2C_dp2 has
+// zeros off the diagonal (identity initialisation, IMP:744).
+__device__ __forceinline__ void jac_element(const SpringEval& e, float ks, float kd, int c, int r, float& j,
+                                            float& jv) {
+    const float zero = 0.0f;
+    const float d00 = (c == r) ? ((-e.C) * e.q[c] + e.C) : zero;
+    const float d01 = (c == r) ? (e.C * e.q[c] - e.C) : zero;
+    const float dp1 = e.n[r] * e.n[c];
+    const float dp2 = e.n[r] * (-e.n[c]);
+    const float dp3 = (-e.n[r]) * (-e.n[c]);
+    const float t1 = (-ks) * (dp1 + d00 * e.C) - kd * (d00 * e.Cdot);
+    const float t2 = (-ks) * (dp2 + d01 * e.C) - kd * (d01 * e.Cdot);
+    const float t3 = (-ks) * (dp2 + d00 * e.C) - kd * (d00 * e.Cdot);
+    j = ((zero + t1) + t2) + t3;
+    jv = ((zero + (-kd) * dp1) + (-kd) * dp2) + (-kd) * dp3;
+}
+
+// F_i: zero, gravity (m g) unless pinned, damping on all, optional external force,
+// then every incident spring in spring-id order (the reference's scatter order).
+__device__ __forceinline__ float3 gather_force(const StepArgs& a, const InstParams& ip, int64_t g, const float4 Xg,
+                                               const float4 Vg, bool pinned) {
+    float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
+    if (!pinned) {
+        Fx += Xg.w * ip.gravity[0];
+        Fy += Xg.w * ip.gravity[1];
+        Fz += Xg.w * ip.gravity[2];
+    }
+    Fx += ip.damping * Vg.x;
+    Fy += ip.damping * Vg.y;
+    Fz += ip.damping * Vg.z;
+    if (!pinned) {
+        if (ip.has_ext) {
+            const float4 e = __ldg(a.fext + g);
+            Fx += e.x;
+            Fy += e.y;
+            Fz += e.z;
+        }
+        const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
+        for (int32_t k = k0; k < k1; ++k) {
+            const int4 rec = __ldg(a.inc + k);
+            const bool as_p2 = rec.x < 0;
+            const int32_t o = rec.x & 0x7fffffff;
+            const float4 Xo = __ldg(a.X + o), Vo = __ldg(a.V + o);
+            const float3 f = as_p2 ? spring_force(Xo, Xg, Vo, Vg, __int_as_float(rec.y), __int_as_float(rec.z),
+                                                  __int_as_float(rec.w))
+                                   : spring_force(Xg, Xo, Vg, Vo, __int_as_float(rec.y), __int_as_float(rec.z),
+                                                  __int_as_float(rec.w));
+            if (as_p2) {
+                Fx -= f.x;
+                Fy -= f.y;
+                Fz -= f.z;
+            } else {
+                Fx += f.x;
+                Fy += f.y;
+                Fz += f.z;
+            }
+        }
+    }
+    return make_float3(Fx, Fy, Fz);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Fixed-order block sum; the result is valid in thread 0.
+__device__ double block_sum(double v) {
+    __shared__ double warp_part[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) warp_part[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (w == 0) {
+        t = (lane < (int)(blockDim.x >> 5)) ? warp_part[lane] : 0.0;
+        t = warp_sum(t);
+    }
+    return t;
+}
+
+// Last-block epilogue shared by the reducing kernels.
+template <int KIND>
+__device__ void finish(const StepArgs& a, int blk, int inst, bool participates, double part) {
+    __shared__ int s_last;
+    if (participates) {
+        const double bsum = block_sum(part);
+        if (threadIdx.x == 0) {
+            a.partials[blk] = bsum;
+            __threadfence();
+            const unsigned t = atomicAdd(&a.state[inst].ticket, 1u);
+            s_last = (t == (unsigned)(a.inst[inst].nblk - 1));
+        }
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            const InstParams& ip = a.inst[inst];
+            double acc = 0.0;
+            for (int j = threadIdx.x; j < ip.nblk; j += blockDim.x) acc += __ldcg(a.partials + ip.blk0 + j);
+            const double total = block_sum(acc);
+            if (threadIdx.x == 0) {
+                InstState& st = a.state[inst];
+                st.ticket = 0;
+                if (KIND == K_ASSEMBLE) {
+                    st.delta0 = total;
+                    st.delta_new = total;
+                    st.dq = 0.0;
+                    st.alpha = 0.0f;
+                    st.beta = 0.0f;
+                    st.iter = 0;
+                    st.flags = 0u;
+                    bool run = (0 < ip.imax) && (total > (double)ip.eps2 * total);
+                    if (!isfinite(total)) {
+                        st.flags |= OC_FLAG_NON_FINITE;
+                        run = false;
+                    }
+                    st.active = run ? 1 : 0;
+                    if (run) atomicAdd(a.unconverged, 1);
+                } else if (KIND == K_CG_DIR) {
+                    st.dq = total;
+                    if (!(total > 0.0) || !isfinite(total)) {
+                        st.flags |= isfinite(total) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
+                        st.active = 0;
+                        atomicSub(a.unconverged, 1);
+                    } else {
+                        st.alpha = (float)(st.delta_new / total);
+                    }
+                } else {  // K_CG_UPDATE
+                    const double old = st.delta_new;
+                    st.delta_new = total;
+                    st.beta = (float)(total / old);
+                    st.iter += 1;
+                    const bool more = st.iter < ip.imax && total > (double)ip.eps2 * st.delta0;
+                    if (!isfinite(total)) st.flags |= OC_FLAG_NON_FINITE;
+                    if (!more || !isfinite(total)) {
+                        if (isfinite(total) && total > (double)ip.eps2 * st.delta0) st.flags |= OC_FLAG_NOT_CONVERGED;
+                        st.active = 0;
+                        atomicSub(a.unconverged, 1);
+                    }
+                }
+                __threadfence();
+            }
+        }
+    }
+    if (KIND != K_CG_DIR && threadIdx.x == 0) {
+        __threadfence();
+        const unsigned t = atomicAdd(a.grid_ticket, 1u);
+        if (t == gridDim.x - 1) {
+            *a.grid_ticket = 0u;
+            __threadfence();
+            if (a.use_cond) {
+                const int u = atomicAdd(a.unconverged, 0);
+                cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, u > 0 ? 1u : 0u);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void matvec(const float A[6], float x0, float x1, float x2, float& y0, float& y1,
+                                       float& y2) {
+    // glm mat3 * vec3 (GLM/core/type_mat3x3.inl:511-518) on a symmetric matrix.
+    y0 = A[0] * x0 + A[1] * x1 + A[2] * x2;
+    y1 = A[1] * x0 + A[3] * x1 + A[4] * x2;
+    y2 = A[2] * x0 + A[4] * x1 + A[5] * x2;
+}
+
+__global__ void __launch_bounds__(kThreads) k_assemble(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const InstParams& ip = a.inst[bi.inst];
+    const float h = a.dt;
+    double part = 0.0;
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
+        const bool pinned = Vg.w != 0.0f;
+        const float3 F = gather_force(a, ip, g, Xg, Vg, pinned);
+
+        float J[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, Jv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const int2 ends = __ldg(a.own_ends + g);
+        if (ends.x >= 0) {
+            const float4 par = __ldg(a.own_par + g);
+            SpringEval e;
+            spring_state(__ldg(a.X + ends.x), __ldg(a.X + ends.y), __ldg(a.V + ends.x), __ldg(a.V + ends.y), par.x,
+                         e);
+            jac_element(e, par.y, par.z, 0, 0, J[0], Jv[0]);
+            jac_element(e, par.y, par.z, 0, 1, J[1], Jv[1]);
+            jac_element(e, par.y, par.z, 0, 2, J[2], Jv[2]);
+            jac_element(e, par.y, par.z, 1, 1, J[3], Jv[3]);
+            jac_element(e, par.y, par.z, 1, 2, J[4], Jv[4]);
+            jac_element(e, par.y, par.z, 2, 2, J[5], Jv[5]);
+        }
+        // A = M - h (df_dv + h df_dx), b = h (F + (h df_dx)(V + y)), IMP:782-783.
+        float A[6], hJ[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float Mk = (k == 0 || k == 3 || k == 5) ? Xg.w : 0.0f;
+            A[k] = Mk - h * (Jv[k] + h * J[k]);
+            hJ[k] = h * J[k];
+        }
+        const float y = 0.0f;
+        const float vx = Vg.x + y, vy = Vg.y + y, vz = Vg.z + y;
+        float wx, wy, wz;
+        matvec(hJ, vx, vy, vz, wx, wy, wz);
+        const float bx = h * (F.x + wx), by = h * (F.y + wy), bz = h * (F.z + wz);
+
+        // CG set-up, IMP:310-318, with pinned rows filtered out.
+        float x0 = a.x[0][g], x1 = a.x[1][g], x2 = a.x[2][g];
+        if (pinned) {
+            x0 = x1 = x2 = 0.0f;
+            a.x[0][g] = 0.0f;
+            a.x[1][g] = 0.0f;
+            a.x[2][g] = 0.0f;
+        }
+        float ax, ay, az;
+        matvec(A, x0, x1, x2, ax, ay, az);
+        float r0 = bx - ax, r1 = by - ay, r2 = bz - az;
+        if (pinned) r0 = r1 = r2 = 0.0f;
+        const float pi0 = 1.0f / A[0], pi1 = 1.0f / A[3], pi2 = 1.0f / A[5];
+        const float d0 = pi0 * r0, d1 = pi1 * r1, d2 = pi2 * r2;
+        const float pr0 = A[0] * r0, pr1 = A[3] * r1, pr2 = A[5] * r2;
+        part += (double)(r0 * pr0 + r1 * pr1 + r2 * pr2);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.A[k][g] = A[k];
+        a.r[0][g] = r0;
+        a.r[1][g] = r1;
+        a.r[2][g] = r2;
+        a.d[0][g] = d0;
+        a.d[1][g] = d1;
+        a.d[2][g] = d2;
+        if (a.dbg_A9) {
+            float* o = a.dbg_A9 + 9 * g;
+            o[0] = A[0]; o[1] = A[1]; o[2] = A[2];
+            o[3] = A[1]; o[4] = A[3]; o[5] = A[4];
+            o[6] = A[2]; o[7] = A[4]; o[8] = A[5];
+        }
+        if (a.dbg_b) {
+            a.dbg_b[3 * g] = bx;
+            a.dbg_b[3 * g + 1] = by;
+            a.dbg_b[3 * g + 2] = bz;
+        }
+    }
+    finish<K_ASSEMBLE>(a, blk, bi.inst, true, part);
+}
+
+__global__ void __launch_bounds__(kThreads) k_cg_dir(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const InstState& st = a.state[bi.inst];
+    const bool active = st.active != 0;
+    double part = 0.0;
+    if (active) {
+        const bool first = st.iter == 0;
+        const float beta = st.beta;
+        for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+            float d0 = a.d[0][g], d1 = a.d[1][g], d2 = a.d[2][g];
+            if (!first) {  // d = r + beta d, IMP:327
+                d0 = a.r[0][g] + d0 * beta;
+                d1 = a.r[1][g] + d1 * beta;
+                d2 = a.r[2][g] + d2 * beta;
+                a.d[0][g] = d0;
+                a.d[1][g] = d1;
+                a.d[2][g] = d2;
+            }
+            float A[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) A[k] = a.A[k][g];
+            float q0, q1, q2;
+            matvec(A, d0, d1, d2, q0, q1, q2);
+            part += (double)(d0 * q0 + d1 * q1 + d2 * q2);
+        }
+    }
+    finish<K_CG_DIR>(a, blk, bi.inst, active, part);
+}
+
+__global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const InstState& st = a.state[bi.inst];
+    const bool active = st.active != 0;
+    double part = 0.0;
+    if (active) {
+        const float alpha = st.alpha;
+        for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+            const float d0 = a.d[0][g], d1 = a.d[1][g], d2 = a.d[2][g];
+            float A[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) A[k] = a.A[k][g];
+            float q0, q1, q2;
+            matvec(A, d0, d1, d2, q0, q1, q2);
+            a.x[0][g] = a.x[0][g] + d0 * alpha;  // x = x + alpha d, IMP:322
+            a.x[1][g] = a.x[1][g] + d1 * alpha;
+            a.x[2][g] = a.x[2][g] + d2 * alpha;
+            const float r0 = a.r[0][g] - q0 * alpha;  // r = r - alpha q, IMP:323
+            const float r1 = a.r[1][g] - q1 * alpha;
+            const float r2 = a.r[2][g] - q2 * alpha;
+            a.r[0][g] = r0;
+            a.r[1][g] = r1;
+            a.r[2][g] = r2;
+            part += (double)(r0 * r0 + r1 * r1 + r2 * r2);
+        }
+    }
+    finish<K_CG_UPDATE>(a, blk, bi.inst, active, part);
+}
+
+__global__ void __launch_bounds__(kThreads) k_integrate(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const float dt = a.dt;
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        float4 Xg = a.X[g], Vg = a.V[g];
+        Vg.x = Vg.x + a.x[0][g] * dt;  // V += dV dt, IMP:791
+        Vg.y = Vg.y + a.x[1][g] * dt;
+        Vg.z = Vg.z + a.x[2][g] * dt;
+        Xg.x = Xg.x + dt * Vg.x;  // X += dt V, IMP:792
+        Xg.y = Xg.y + dt * Vg.y;
+        Xg.z = Xg.z + dt * Vg.z;
+        if (Xg.y < 0.0f) Xg.y = 0.0f;  // IMP:794-796
+        a.X[g] = Xg;
+        a.V[g] = Vg;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_forces(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const InstParams& ip = a.inst[bi.inst];
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
+        const float3 F = gather_force(a, ip, g, Xg, Vg, Vg.w != 0.0f);
+        a.dbg_F[3 * g] = F.x;
+        a.dbg_F[3 * g + 1] = F.y;
+        a.dbg_F[3 * g + 2] = F.z;
+    }
+}
+
+// Packed float triples <-> the device layout (X/V float4, dV planes).  Flags a
+// non-finite input in *err.
+__global__ void k_state_in(const StepArgs a, const float* X3, const float* V3, const float* dV3, int64_t nv,
+                           int32_t* err) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nv; g += (int64_t)gridDim.x * blockDim.x) {
+        bool bad = false;
+        if (X3) {
+            float4 v = a.X[g];
+            v.x = X3[3 * g];
+            v.y = X3[3 * g + 1];
+            v.z = X3[3 * g + 2];
+            bad |= !isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z);
+            a.X[g] = v;
+        }
+        if (V3) {
+            float4 v = a.V[g];
+            v.x = V3[3 * g];
+            v.y = V3[3 * g + 1];
+            v.z = V3[3 * g + 2];
+            bad |= !isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z);
+            a.V[g] = v;
+        }
+        if (dV3) {
+            const float x0 = dV3[3 * g], x1 = dV3[3 * g + 1], x2 = dV3[3 * g + 2];
+            bad |= !isfinite(x0) || !isfinite(x1) || !isfinite(x2);
+            a.x[0][g] = x0;
+            a.x[1][g] = x1;
+            a.x[2][g] = x2;
+        }
+        if (bad) atomicOr(err, 1);
+    }
+}
+
+__global__ void k_state_out(const StepArgs a, float* X3, float* V3, float* dV3, int64_t nv) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nv; g += (int64_t)gridDim.x * blockDim.x) {
+        if (X3) {
+            const float4 v = a.X[g];
+            X3[3 * g] = v.x;
+            X3[3 * g + 1] = v.y;
+            X3[3 * g + 2] = v.z;
+        }
+        if (V3) {
+            const float4 v = a.V[g];
+            V3[3 * g] = v.x;
+            V3[3 * g + 1] = v.y;
+            V3[3 * g + 2] = v.z;
+        }
+        if (dV3) {
+            dV3[3 * g] = a.x[0][g];
+            dV3[3 * g + 1] = a.x[1][g];
+            dV3[3 * g + 2] = a.x[2][g];
+        }
+    }
+}
+
+}  // namespace
+
+const char* kernel_name(KernelKind k) {
+    switch (k) {
+        case K_ASSEMBLE: return "k_assemble";
+        case K_CG_DIR: return "k_cg_dir";
+        case K_CG_UPDATE: return "k_cg_update";
+        case K_INTEGRATE: return "k_integrate";
+        case K_FORCES: return "k_forces";
+        default: return "?";
+    }
+}
+
+const void* kernel_fn(KernelKind k) {
+    switch (k) {
+        case K_ASSEMBLE: return (const void*)k_assemble;
+        case K_CG_DIR: return (const void*)k_cg_dir;
+        case K_CG_UPDATE: return (const void*)k_cg_update;
+        case K_INTEGRATE: return (const void*)k_integrate;
+        case K_FORCES: return (const void*)k_forces;
+        default: return nullptr;
+    }
+}
+
+int kernel_block_threads() { return kThreads; }
+
+static int state_blocks(int64_t nv) {
+    const int64_t b = (nv + kThreads - 1) / kThreads;
+    return (int)(b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
+}
+
+cudaError_t launch_state_in(const StepArgs& a, const float* X3, const float* V3, const float* dV3, int64_t nv,
+                            int32_t* err, cudaStream_t stream) {
+    k_state_in<<<state_blocks(nv), kThreads, 0, stream>>>(a, X3, V3, dV3, nv, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_state_out(const StepArgs& a, float* X3, float* V3, float* dV3, int64_t nv, cudaStream_t stream) {
+    k_state_out<<<state_blocks(nv), kThreads, 0, stream>>>(a, X3, V3, dV3, nv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStream_t stream) {
+    if (nblocks <= 0) return cudaSuccess;
+    switch (k) {
+        case K_ASSEMBLE: k_assemble<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_CG_DIR: k_cg_dir<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_CG_UPDATE: k_cg_update<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_INTEGRATE: k_integrate<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_FORCES: k_forces<<<nblocks, kThreads, 0, stream>>>(a); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace oc

@@ -1,0 +1,267 @@
+// Host-side topology: the reference grid builder, input validation, and packing of
+// many cloths into one ragged structure-of-arrays batch with a vertex->spring
+// incidence (CSR) ordered by spring id.
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+#include "oc_internal.h"
+
+namespace oc {
+namespace {
+
+inline int32_t float_bits(float f) {
+    int32_t i;
+    std::memcpy(&i, &f, sizeof(i));
+    return i;
+}
+
+inline bool finite3(const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+// splitmix64 (Steele, Lea, Flood 2014) and Box-Muller: a portable seeded normal stream.
+inline uint64_t splitmix64(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+inline double uniform_open01(uint64_t& s) { return ((double)(splitmix64(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+
+}  // namespace
+
+oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, PackedHost* out, std::string* err) {
+    if (!descs || n < 1 || !out || vpb < 1) {
+        *err = "oc_create: descs must hold n_instances >= 1 cloths";
+        return OC_ERR_INVALID_ARGUMENT;
+    }
+    int64_t nv = 0, ns = 0;
+    bool any_ext = false;
+    for (int32_t k = 0; k < n; ++k) {
+        const oc_cloth_desc& d = descs[k];
+        const std::string who = "instance " + std::to_string(k) + ": ";
+        if (d.n_vertices < 1 || d.n_springs < 0 || (d.n_springs > 0 && !d.springs) || d.n_pinned < 0 ||
+            (d.n_pinned > 0 && !d.pinned)) {
+            *err = who + "bad sizes or NULL arrays";
+            return OC_ERR_INVALID_ARGUMENT;
+        }
+        if (d.jacobian_mode != OC_JAC_REFERENCE) {
+            *err = who + "jacobian_mode " + std::to_string(d.jacobian_mode) + " is not available";
+            return OC_ERR_UNSUPPORTED;
+        }
+        if (d.cg_max_iter < 0 || !std::isfinite(d.cg_tol) || d.cg_tol < 0.0f) {
+            *err = who + "cg_max_iter must be >= 0 and cg_tol finite and >= 0";
+            return OC_ERR_INVALID_ARGUMENT;
+        }
+        if (!finite3(d.gravity) || !std::isfinite(d.velocity_damping)) {
+            *err = who + "gravity / velocity_damping not finite";
+            return OC_ERR_NON_FINITE;
+        }
+        for (int32_t s = 0; s < d.n_springs; ++s) {
+            const oc_spring& sp = d.springs[s];
+            if (sp.p1 < 0 || sp.p1 >= d.n_vertices || sp.p2 < 0 || sp.p2 >= d.n_vertices) {
+                *err = who + "spring " + std::to_string(s) + " endpoint out of range";
+                return OC_ERR_BAD_INDEX;
+            }
+            if (sp.p1 == sp.p2) {
+                *err = who + "spring " + std::to_string(s) + " joins a vertex to itself";
+                return OC_ERR_DEGENERATE;
+            }
+            if (!std::isfinite(sp.rest_length) || !std::isfinite(sp.ks) || !std::isfinite(sp.kd)) {
+                *err = who + "spring " + std::to_string(s) + " has a non-finite parameter";
+                return OC_ERR_NON_FINITE;
+            }
+            if (sp.rest_length < 0.0f) {
+                *err = who + "spring " + std::to_string(s) + " has a negative rest length";
+                return OC_ERR_INVALID_ARGUMENT;
+            }
+        }
+        for (int32_t p = 0; p < d.n_pinned; ++p) {
+            if (d.pinned[p] < 0 || d.pinned[p] >= d.n_vertices) {
+                *err = who + "pinned index " + std::to_string(d.pinned[p]) + " out of range";
+                return OC_ERR_BAD_INDEX;
+            }
+        }
+        if (d.mass) {
+            for (int32_t i = 0; i < d.n_vertices; ++i) {
+                if (!std::isfinite(d.mass[i])) {
+                    *err = who + "mass not finite";
+                    return OC_ERR_NON_FINITE;
+                }
+                if (!(d.mass[i] > 0.0f)) {
+                    *err = who + "mass must be > 0";
+                    return OC_ERR_INVALID_ARGUMENT;
+                }
+            }
+        }
+        if (d.ext_force) {
+            any_ext = true;
+            for (int32_t i = 0; i < d.n_vertices; ++i) {
+                if (!finite3(d.ext_force + 3 * (size_t)i)) {
+                    *err = who + "ext_force not finite";
+                    return OC_ERR_NON_FINITE;
+                }
+            }
+        }
+        nv += d.n_vertices;
+        ns += d.n_springs;
+    }
+    const int64_t int_max = std::numeric_limits<int32_t>::max();
+    if (nv >= int_max || 2 * ns >= int_max) {
+        *err = "batch too large: total vertices and 2 x total springs must stay below 2^31";
+        return OC_ERR_UNSUPPORTED;
+    }
+
+    PackedHost& P = *out;
+    P.n_inst = n;
+    P.nv = nv;
+    P.ns = ns;
+    P.vertices_per_block = vpb;
+    P.v_off.assign(n + 1, 0);
+    P.s_off.assign(n + 1, 0);
+    P.inst.resize(n);
+    P.X0.assign(nv, make_float4(0.f, 0.f, 0.f, 1.f));
+    P.V0.assign(nv, make_float4(0.f, 0.f, 0.f, 0.f));
+    P.fext.clear();
+    if (any_ext) P.fext.assign(nv, make_float4(0.f, 0.f, 0.f, 0.f));
+    P.own_ends.assign(nv, make_int2(-1, -1));
+    P.own_par.assign(nv, make_float4(0.f, 0.f, 0.f, 0.f));
+    P.blocks.clear();
+
+    std::vector<int32_t> deg(nv, 0);
+    for (int32_t k = 0; k < n; ++k) {
+        const oc_cloth_desc& d = descs[k];
+        P.v_off[k + 1] = P.v_off[k] + d.n_vertices;
+        P.s_off[k + 1] = P.s_off[k] + d.n_springs;
+        const int64_t vo = P.v_off[k];
+        for (int32_t s = 0; s < d.n_springs; ++s) {
+            ++deg[vo + d.springs[s].p1];
+            ++deg[vo + d.springs[s].p2];
+        }
+    }
+    P.rowptr.assign(nv + 1, 0);
+    for (int64_t g = 0; g < nv; ++g) P.rowptr[g + 1] = P.rowptr[g] + deg[g];
+    P.inc.assign((size_t)P.rowptr[nv], make_int4(0, 0, 0, 0));
+    std::vector<int32_t> cursor(P.rowptr.begin(), P.rowptr.end() - 1);
+
+    for (int32_t k = 0; k < n; ++k) {
+        const oc_cloth_desc& d = descs[k];
+        const int64_t vo = P.v_off[k];
+        InstParams& ip = P.inst[k];
+        ip.gravity[0] = d.gravity[0];
+        ip.gravity[1] = d.gravity[1];
+        ip.gravity[2] = d.gravity[2];
+        ip.damping = d.velocity_damping;
+        const float eps = d.cg_tol;
+        ip.eps2 = eps * eps;
+        ip.imax = d.cg_max_iter;
+        ip.v_off = vo;
+        ip.nv = d.n_vertices;
+        ip.has_ext = d.ext_force ? 1 : 0;
+        ip.blk0 = (int32_t)P.blocks.size();
+        ip.nblk = (d.n_vertices + vpb - 1) / vpb;
+        for (int32_t b = 0; b < ip.nblk; ++b) {
+            BlockInfo bi;
+            bi.inst = k;
+            bi.local_blk = b;
+            bi.v_begin = vo + (int64_t)b * vpb;
+            bi.v_end = std::min<int64_t>(vo + d.n_vertices, bi.v_begin + vpb);
+            P.blocks.push_back(bi);
+        }
+        for (int32_t i = 0; i < d.n_vertices; ++i) {
+            P.X0[vo + i].w = d.mass ? d.mass[i] : 1.0f;
+            if (d.ext_force)
+                P.fext[vo + i] = make_float4(d.ext_force[3 * (size_t)i], d.ext_force[3 * (size_t)i + 1],
+                                             d.ext_force[3 * (size_t)i + 2], 0.f);
+        }
+        for (int32_t p = 0; p < d.n_pinned; ++p) P.V0[vo + d.pinned[p]].w = 1.0f;
+        for (int32_t s = 0; s < d.n_springs; ++s) {
+            const oc_spring& sp = d.springs[s];
+            const int32_t g1 = (int32_t)(vo + sp.p1), g2 = (int32_t)(vo + sp.p2);
+            const int32_t rb = float_bits(sp.rest_length), kb = float_bits(sp.ks), db = float_bits(sp.kd);
+            P.inc[cursor[g1]++] = make_int4(g2, rb, kb, db);
+            P.inc[cursor[g2]++] = make_int4((int32_t)((uint32_t)g1 | 0x80000000u), rb, kb, db);
+            if (s < d.n_vertices) {
+                P.own_ends[vo + s] = make_int2(g1, g2);
+                P.own_par[vo + s] = make_float4(sp.rest_length, sp.ks, sp.kd, 0.f);
+            }
+        }
+    }
+    return OC_OK;
+}
+
+}  // namespace oc
+
+extern "C" {
+
+oc_status oc_grid_spring_count(int32_t cols, int32_t rows, int32_t* n_springs) {
+    if (!n_springs || cols < 3 || rows < 3) return OC_ERR_INVALID_ARGUMENT;
+    const int64_t u = cols, v = rows;
+    const int64_t s = v * (u - 1) + u * (v - 1) + 2 * (v - 1) * (u - 1) + v * (u - 1) + u * (v - 1);
+    if (s >= std::numeric_limits<int32_t>::max()) return OC_ERR_UNSUPPORTED;
+    *n_springs = (int32_t)s;
+    return OC_OK;
+}
+
+// Mirrors InitGL's lattice and spring loops, IMP:497-565 (AddSpring IMP:370-380 takes
+// the rest length from the positions at creation, before any jitter).
+oc_status oc_grid_build(int32_t cols, int32_t rows, float size, const float ks[3], const float kd[3], float jitter,
+                        uint64_t seed, float* X, oc_spring* springs) {
+    int32_t ns = 0;
+    if (oc_grid_spring_count(cols, rows, &ns) != OC_OK || !ks || !kd || !X || !springs ||
+        !(size > 0.0f) || !std::isfinite(size) || !std::isfinite(jitter) || jitter < 0.0f)
+        return OC_ERR_INVALID_ARGUMENT;
+    const int32_t u = cols, v = rows;
+    const float halfsize = size / 2.0f;
+    for (int32_t j = 0; j < v; ++j) {
+        for (int32_t i = 0; i < u; ++i) {
+            float* p = X + 3 * ((size_t)j * u + i);
+            p[0] = (((float)i / (float)(u - 1)) * 2.0f - 1.0f) * halfsize;
+            p[1] = (size + 1.0f) - ((float)j / (float)(v - 1)) * size;
+            p[2] = 0.0f;
+        }
+    }
+    int32_t c = 0;
+    auto add = [&](int32_t a, int32_t b, int32_t type) {
+        oc_spring& sp = springs[c++];
+        sp.p1 = a;
+        sp.p2 = b;
+        sp.ks = ks[type];
+        sp.kd = kd[type];
+        sp.type = type;
+        const float dx = X[3 * (size_t)a] - X[3 * (size_t)b];
+        const float dy = X[3 * (size_t)a + 1] - X[3 * (size_t)b + 1];
+        const float dz = X[3 * (size_t)a + 2] - X[3 * (size_t)b + 2];
+        sp.rest_length = std::sqrt(dx * dx + dy * dy + dz * dz);
+    };
+    for (int32_t l1 = 0; l1 < v; ++l1)  // horizontal structural
+        for (int32_t l2 = 0; l2 < u - 1; ++l2) add(l1 * u + l2, l1 * u + l2 + 1, OC_STRUCTURAL_SPRING);
+    for (int32_t l1 = 0; l1 < u; ++l1)  // vertical structural
+        for (int32_t l2 = 0; l2 < v - 1; ++l2) add(l2 * u + l1, (l2 + 1) * u + l1, OC_STRUCTURAL_SPRING);
+    for (int32_t l1 = 0; l1 < v - 1; ++l1)  // shear, two per quad
+        for (int32_t l2 = 0; l2 < u - 1; ++l2) {
+            add(l1 * u + l2, (l1 + 1) * u + l2 + 1, OC_SHEAR_SPRING);
+            add((l1 + 1) * u + l2, l1 * u + l2 + 1, OC_SHEAR_SPRING);
+        }
+    for (int32_t l1 = 0; l1 < v; ++l1) {  // bend along rows, plus the reference's repeat of the last one
+        for (int32_t l2 = 0; l2 < u - 2; ++l2) add(l1 * u + l2, l1 * u + l2 + 2, OC_BEND_SPRING);
+        add(l1 * u + (u - 3), l1 * u + (u - 1), OC_BEND_SPRING);
+    }
+    for (int32_t l1 = 0; l1 < u; ++l1) {  // bend along columns, same repeat
+        for (int32_t l2 = 0; l2 < v - 2; ++l2) add(l2 * u + l1, (l2 + 2) * u + l1, OC_BEND_SPRING);
+        add((v - 3) * u + l1, (v - 1) * u + l1, OC_BEND_SPRING);
+    }
+    if (jitter > 0.0f) {
+        const double sigma = (double)jitter * (double)size / (double)(u - 1);
+        uint64_t state = seed;
+        const size_t n3 = 3 * (size_t)u * v;
+        for (size_t k = 0; k < n3; k += 2) {
+            const double r = std::sqrt(-2.0 * std::log(oc::uniform_open01(state)));
+            const double t = 6.283185307179586 * oc::uniform_open01(state);
+            X[k] += (float)(sigma * r * std::cos(t));
+            if (k + 1 < n3) X[k + 1] += (float)(sigma * r * std::sin(t));
+        }
+    }
+    return c == ns ? OC_OK : OC_ERR_INVALID_ARGUMENT;
+}
+
+}  // extern "C"

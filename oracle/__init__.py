@@ -1,0 +1,256 @@
+"""Test infrastructure: the oracle for the implicit cloth step.
+
+Only ``tests/``, ``bench.py`` (its CPU-baseline leg and reference arm) and
+``__graft_entry__.smoke()`` may use this package, and only as the checker or the timed
+CPU baseline.  The product (``opencloth_gb300``) never imports it.
+
+Two oracles:
+
+* the *port* — ``oc_oracle.c``, a C restatement of the reference step
+  (OpenCloth_Implicit/OpenCloth_Implicit/main.cpp:698-798, :308-330) in FP32 and FP64,
+  built here and on any host with gcc;
+* the *reference itself* — ``_ref/ref_step_f32`` / ``_ref/ref_step_f64``, the
+  reference's own source compiled headless by ``build_ref.sh`` where the reference tree
+  is present.  Tests pin the port to it bit for bit, and committed golden fixtures
+  (``tests/golden/``) carry its outputs to hosts without it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import struct
+import subprocess
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+REF = HERE / "_ref"
+PORT_LIB = BUILD / "liboc_oracle.so"
+
+SPRING_DTYPE = np.dtype(
+    [("p1", "<i4"), ("p2", "<i4"), ("rest_length", "<f4"), ("ks", "<f4"), ("kd", "<f4"), ("type", "<i4")]
+)
+
+
+def build(reference: bool = True) -> None:
+    """Compile the port (always) and the reference harness (when the tree is present)."""
+    BUILD.mkdir(exist_ok=True)
+    srcs = [HERE / "oc_oracle.c", HERE / "oc_oracle_impl.h", HERE / "oc_oracle.h"]
+    if not PORT_LIB.exists() or any(s.stat().st_mtime > PORT_LIB.stat().st_mtime for s in srcs):
+        tmp = PORT_LIB.with_suffix(".so.tmp")
+        subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
+                        str(HERE / "oc_oracle.c"), "-o", str(tmp), "-lm"], check=True)
+        os.replace(tmp, PORT_LIB)
+    if reference:
+        subprocess.run(["bash", str(HERE / "build_ref.sh")], check=True, capture_output=True)
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("n_vertices", C.c_int32), ("n_springs", C.c_int32), ("springs", C.c_void_p), ("pinned", C.c_void_p),
+        ("num_x", C.c_int32), ("mass", C.c_void_p), ("ext_force", C.c_void_p), ("gravity", C.c_float * 3),
+        ("damping", C.c_float), ("i_max", C.c_int32), ("eps", C.c_float), ("dot_fp64", C.c_int32),
+        ("filter_pinned", C.c_int32),
+    ]
+
+
+_port = None
+
+
+def port() -> C.CDLL:
+    global _port
+    if _port is None:
+        if not PORT_LIB.exists():
+            build(reference=False)
+        lib = C.CDLL(str(PORT_LIB))
+        P = C.POINTER(Params)
+        for sfx, real in (("f32", C.c_float), ("f64", C.c_double)):
+            getattr(lib, f"ocr_compute_forces_{sfx}").argtypes = [P, C.c_void_p, C.c_void_p, C.c_void_p]
+            getattr(lib, f"ocr_assemble_{sfx}").argtypes = [P, real, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                            C.c_void_p, C.c_void_p]
+            f = getattr(lib, f"ocr_step_{sfx}")
+            f.argtypes = [P, real, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+            f.restype = C.c_int
+        _port = lib
+    return _port
+
+
+class Cloth:
+    """Inputs of one cloth for the oracle (mirrors oc_cloth_desc)."""
+
+    def __init__(self, n_vertices, springs, pinned=None, num_x=None, mass=None, ext_force=None,
+                 gravity=(0.0, -0.00981, 0.0), damping=-0.125, i_max=10, eps=1e-3):
+        self.n_vertices = int(n_vertices)
+        self.springs = np.ascontiguousarray(springs, SPRING_DTYPE)
+        self.pinned = pinned  # index array or None (then the reference pins {0, num_x})
+        self.num_x = num_x
+        self.mass = mass
+        self.ext_force = ext_force
+        self.gravity = tuple(float(g) for g in gravity)
+        self.damping = float(damping)
+        self.i_max = int(i_max)
+        self.eps = float(eps)
+
+    def params(self, dot_fp64: bool, filter_pinned: bool):
+        keep = []
+        p = Params()
+        p.n_vertices = self.n_vertices
+        p.n_springs = int(self.springs.shape[0])
+        p.springs = self.springs.ctypes.data if self.springs.size else None
+        keep.append(self.springs)
+        if self.pinned is not None:
+            mask = np.zeros(self.n_vertices, np.uint8)
+            mask[np.asarray(self.pinned, np.int64)] = 1
+            keep.append(mask)
+            p.pinned = mask.ctypes.data
+        else:
+            p.pinned = None
+        p.num_x = -1 if self.num_x is None else int(self.num_x)
+        if self.mass is not None:
+            m = np.ascontiguousarray(self.mass, np.float32)
+            keep.append(m)
+            p.mass = m.ctypes.data
+        if self.ext_force is not None:
+            e = np.ascontiguousarray(self.ext_force, np.float32).reshape(-1)
+            keep.append(e)
+            p.ext_force = e.ctypes.data
+        p.gravity[:] = self.gravity
+        p.damping = self.damping
+        p.i_max = self.i_max
+        p.eps = self.eps
+        p.dot_fp64 = 1 if dot_fp64 else 0
+        p.filter_pinned = 1 if filter_pinned else 0
+        return p, keep
+
+
+def port_step(cloth: Cloth, X, V, dV=None, dt=1.0 / 60.0, n_steps=1, fp64=False, dot_fp64=False,
+              filter_pinned=False):
+    """Run the port; returns (X, V, dV, iters[n_steps], rel_residual[n_steps])."""
+    lib = port()
+    real = np.float64 if fp64 else np.float32
+    X = np.array(X, real).reshape(-1)
+    V = np.array(V, real).reshape(-1)
+    dV = np.zeros_like(X) if dV is None else np.array(dV, real).reshape(-1)
+    iters = np.zeros(max(n_steps, 1), np.int32)
+    rr = np.zeros(max(n_steps, 1), np.float64)
+    p, keep = cloth.params(dot_fp64, filter_pinned)
+    fn = lib.ocr_step_f64 if fp64 else lib.ocr_step_f32
+    dtv = float(np.float32(dt))
+    rc = fn(C.byref(p), dtv, int(n_steps), X.ctypes.data, V.ctypes.data, dV.ctypes.data, iters.ctypes.data,
+            rr.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("oracle port step failed")
+    del keep
+    return X.reshape(-1, 3), V.reshape(-1, 3), dV.reshape(-1, 3), iters[:n_steps], rr[:n_steps]
+
+
+def port_forces(cloth: Cloth, X, V, fp64=False):
+    lib = port()
+    real = np.float64 if fp64 else np.float32
+    X = np.ascontiguousarray(X, real).reshape(-1)
+    V = np.ascontiguousarray(V, real).reshape(-1)
+    F = np.zeros_like(X)
+    p, keep = cloth.params(False, False)
+    (lib.ocr_compute_forces_f64 if fp64 else lib.ocr_compute_forces_f32)(C.byref(p), X.ctypes.data,
+                                                                         V.ctypes.data, F.ctypes.data)
+    del keep
+    return F.reshape(-1, 3)
+
+
+def port_assemble(cloth: Cloth, X, V, dt, fp64=False):
+    """(F, A as (N,3,3) [column][row], b)."""
+    lib = port()
+    real = np.float64 if fp64 else np.float32
+    X = np.ascontiguousarray(X, real).reshape(-1)
+    V = np.ascontiguousarray(V, real).reshape(-1)
+    F = port_forces(cloth, X, V, fp64).reshape(-1).astype(real)
+    A9 = np.zeros(9 * cloth.n_vertices, real)
+    b = np.zeros(3 * cloth.n_vertices, real)
+    p, keep = cloth.params(False, False)
+    (lib.ocr_assemble_f64 if fp64 else lib.ocr_assemble_f32)(C.byref(p), float(np.float32(dt)), X.ctypes.data,
+                                                             V.ctypes.data, F.ctypes.data, A9.ctypes.data,
+                                                             b.ctypes.data)
+    del keep
+    return F.reshape(-1, 3), A9.reshape(-1, 3, 3), b.reshape(-1, 3)
+
+
+# ---- the reference itself, built headless --------------------------------------------
+
+def ref_binary(fp64: bool = False) -> Path:
+    return REF / ("ref_step_f64" if fp64 else "ref_step_f32")
+
+
+def ref_available() -> bool:
+    b = ref_binary()
+    if not b.exists():
+        return False
+    try:
+        env = dict(os.environ, OC_NUMX="2", OC_NUMY="2")
+        with tempfile.TemporaryDirectory() as td:
+            r = subprocess.run([str(b), "--topology", os.path.join(td, "t.bin")], env=env, capture_output=True,
+                               timeout=30)
+        return r.returncode == 0
+    except OSError:
+        return False
+
+
+def _ref_env(num_x, num_y, i_max, eps):
+    return dict(os.environ, OC_NUMX=str(num_x), OC_NUMY=str(num_y), OC_IMAX=str(int(i_max)),
+                OC_EPS="%.17g" % float(np.float32(eps)))
+
+
+def ref_topology(num_x: int, num_y: int):
+    """InitGL()'s springs and positions for a (num_x+1) x (num_y+1) grid."""
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "topo.bin")
+        subprocess.run([str(ref_binary()), "--topology", out], env=_ref_env(num_x, num_y, 10, 1e-3), check=True,
+                       capture_output=True)
+        b = open(out, "rb").read()
+    n, s = struct.unpack_from("<ii", b, 0)
+    X = np.frombuffer(b, np.float32, 3 * n, 8).reshape(n, 3).copy()
+    sp = np.frombuffer(b, SPRING_DTYPE, s, 8 + 12 * n).copy()
+    return X, sp
+
+
+def ref_run(cloth: Cloth, num_x: int, num_y: int, X, V, dV=None, dt=1.0 / 60.0, snaps=(1,), fp64=False,
+            timed=False):
+    """Step the reference itself; returns {step: (X, V, dV)} (and seconds if timed)."""
+    n = cloth.n_vertices
+    assert n == (num_x + 1) * (num_y + 1)
+    X = np.ascontiguousarray(X, np.float32).reshape(-1)
+    V = np.ascontiguousarray(V, np.float32).reshape(-1)
+    dV = np.zeros_like(X) if dV is None else np.ascontiguousarray(dV, np.float32).reshape(-1)
+    snaps = sorted(int(s) for s in snaps)
+    g = cloth.gravity
+    hdr = b"OCI1" + struct.pack("<5i", n, cloth.springs.shape[0], num_x, num_y, cloth.i_max)
+    hdr += struct.pack("<5f", cloth.eps, dt, g[0], g[1], g[2]) + struct.pack("<i", len(snaps))
+    blob = hdr + np.asarray(snaps, np.int32).tobytes() + X.tobytes() + V.tobytes() + dV.tobytes()
+    blob += cloth.springs.tobytes()
+    with tempfile.TemporaryDirectory() as td:
+        inp, out = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        open(inp, "wb").write(blob)
+        cmd = [str(ref_binary(fp64)), inp, out] + (["--time"] if timed else [])
+        r = subprocess.run(cmd, env=_ref_env(num_x, num_y, cloth.i_max, cloth.eps), capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference run failed: {r.stderr}")
+        b = open(out, "rb").read()
+    assert b[:4] == b"OCO1"
+    rsize, nsnap = struct.unpack_from("<ii", b, 4)
+    dtype = np.float64 if rsize == 8 else np.float32
+    off = 12
+    res = {}
+    for _ in range(nsnap):
+        (step,) = struct.unpack_from("<i", b, off)
+        off += 4
+        arrs = []
+        for _k in range(3):
+            arrs.append(np.frombuffer(b, dtype, 3 * n, off).reshape(n, 3).copy())
+            off += 3 * n * rsize
+        res[step] = tuple(arrs)
+    if timed:
+        import json
+        return res, json.loads(r.stdout.strip().splitlines()[-1])["seconds"]
+    return res

@@ -1,0 +1,46 @@
+#!/usr/bin/env bash
+# Test infrastructure: builds the reference's own implicit step headless, from the
+# reference sources where they lie, into oracle/_ref/ (git-ignored; never committed).
+#
+#   OpenCloth_Implicit/OpenCloth_Implicit/main.cpp  -> _ref/imp_f32.cpp (generated copy)
+#                                                  -> _ref/imp_f64.cpp (FP64 copy)
+#   ref_harness.cpp + shim/GL/*.h + dep/glm          -> _ref/ref_step_f32, _ref/ref_step_f64
+#
+# The generated copies differ from the reference only where a compile-time constant
+# has to become a run-time value (grid size main.cpp:60, CG EPS main.cpp:126 and i_max
+# main.cpp:128, read from OC_NUMX/OC_NUMY/OC_EPS/OC_IMAX at start-up).  The FP64 copy
+# additionally maps glm::vecN/matN -> glm::dvecN/dmatN, float -> double and strips the
+# f suffix from floating literals.
+#
+# Exits 0 without building when the reference tree is absent.
+set -euo pipefail
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+REF="${OC_REFERENCE_DIR:-/root/reference}"
+SRC="$REF/OpenCloth_Implicit/OpenCloth_Implicit/main.cpp"
+OUT="$HERE/_ref"
+if [ ! -f "$SRC" ]; then
+    echo "build_ref: reference source not present ($SRC); skipping"
+    exit 0
+fi
+mkdir -p "$OUT"
+
+sed -E \
+    -e 's/^int numX = 20, numY=20;/int numX = oc_env_int("OC_NUMX", 20), numY = oc_env_int("OC_NUMY", 20);/' \
+    -e 's/^const float EPS = 0\.001f;/const float EPS = oc_env_real("OC_EPS", 0.001f);/' \
+    -e 's/^const int i_max = 10;/const int i_max = oc_env_int("OC_IMAX", 10);/' \
+    "$SRC" > "$OUT/imp_f32.cpp"
+for pat in 'oc_env_int("OC_NUMX"' 'oc_env_real("OC_EPS"' 'oc_env_int("OC_IMAX"'; do
+    grep -qF "$pat" "$OUT/imp_f32.cpp" || { echo "build_ref: substitution failed: $pat" >&2; exit 1; }
+done
+
+sed -E \
+    -e 's/glm::(vec|mat)([234])/glm::d\1\2/g' \
+    -e 's/\bfloat\b/double/g' \
+    -e 's/\b([0-9]+\.[0-9]*|[0-9]*\.[0-9]+)f\b/\1/g' \
+    "$OUT/imp_f32.cpp" > "$OUT/imp_f64.cpp"
+
+CXXFLAGS="-std=c++14 -O2 -ffp-contract=off -w -I$HERE/shim -I$REF/dep/glm -I$OUT -Dglm_core_func_integer"
+g++ $CXXFLAGS -DOC_REAL=float '-DOC_REF_SOURCE="imp_f32.cpp"' "$HERE/ref_harness.cpp" -o "$OUT/ref_step_f32" &
+g++ $CXXFLAGS -DOC_REAL=double '-DOC_REF_SOURCE="imp_f64.cpp"' "$HERE/ref_harness.cpp" -o "$OUT/ref_step_f64" &
+wait %1 && wait %2
+echo "build_ref: built $OUT/ref_step_f32 $OUT/ref_step_f64"

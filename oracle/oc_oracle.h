@@ -1,0 +1,71 @@
+/* Test infrastructure: CPU restatement of the reference's implicit mass-spring step.
+ *
+ * Only tests/, bench.py's cpu_baseline / reference arm and __graft_entry__.smoke()
+ * use this, and only as the checker.  The library (opencloth_gb300/) never links it.
+ *
+ * It restates, operation for operation and in the same rounding order (compile with
+ * -ffp-contract=off), the reference's
+ *   ComputeForces                          OpenCloth_Implicit/.../main.cpp:698-735
+ *   CalcForceDerivatives                   main.cpp:737-772
+ *   IntegrateImplicit (assembly + update)  main.cpp:775-798
+ *   SolveConjugateGradientPreconditioned   main.cpp:308-330
+ * with the glm 0.9.0 primitives those use (length, normalize = x * (1/sqrt(x.x)),
+ * outerProduct, column-major mat3 * vec3).  Parity is pinned by tests that compare it
+ * bit for bit with the reference itself built headless (oracle/build_ref.sh).
+ *
+ * Generalisations (each reduces to the reference when left at its default):
+ *   pinned mask      NULL -> the reference's hard-coded pins {0, num_x}
+ *   mass             NULL -> 1 (the reference's M = I, gravity added as a force)
+ *   ext_force        NULL -> none (added after damping)
+ *   dot_fp64         0 -> FP32 sequential dots as the reference; 1 -> per-vertex FP32
+ *                    dot terms summed in FP64 (what the GPU solver does)
+ *   filter_pinned    0 -> no filter (the reference); 1 -> pinned rows of the warm start
+ *                    and of the residual are zeroed before the CG (the GPU solver)
+ */
+#ifndef OC_ORACLE_H
+#define OC_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ocr_spring {
+    int32_t p1, p2;
+    float rest, ks, kd;
+    int32_t type;
+} ocr_spring;
+
+typedef struct ocr_params {
+    int32_t n_vertices, n_springs;
+    const ocr_spring* springs;
+    const uint8_t* pinned; /* n_vertices flags, or NULL for {0, num_x} */
+    int32_t num_x;
+    const float* mass;      /* n_vertices, or NULL */
+    const float* ext_force; /* 3 * n_vertices, or NULL */
+    float gravity[3];
+    float damping;
+    int32_t i_max;
+    float eps;
+    int32_t dot_fp64;
+    int32_t filter_pinned;
+} ocr_params;
+
+/* FP32 flavour: state arrays are 3 * n_vertices floats, AoS (x, y, z). */
+void ocr_compute_forces_f32(const ocr_params* p, const float* X, const float* V, float* F);
+void ocr_assemble_f32(const ocr_params* p, float dt, const float* X, const float* V, const float* F, float* A9,
+                      float* b);
+int ocr_step_f32(const ocr_params* p, float dt, int32_t n_steps, float* X, float* V, float* dV, int32_t* iters,
+                 double* rel_residual);
+
+/* FP64 flavour of the same method (the reference built with double everywhere). */
+void ocr_compute_forces_f64(const ocr_params* p, const double* X, const double* V, double* F);
+void ocr_assemble_f64(const ocr_params* p, double dt, const double* X, const double* V, const double* F,
+                      double* A9, double* b);
+int ocr_step_f64(const ocr_params* p, double dt, int32_t n_steps, double* X, double* V, double* dV,
+                 int32_t* iters, double* rel_residual);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
