@@ -1,0 +1,375 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 implicit cloth step, in vertex-steps/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload grid1025|batch4096]
+    python bench.py --impl reference ...     # the reference's CPU step on the host cores
+
+A step is ComputeForces + IntegrateImplicit (forces, Jacobians, assembly, PCG to the
+configured tolerance, update) over every cloth of the workload.
+
+Workloads (synthetic, seeded):
+  grid1025   one 1025 x 1025 cloth (1,050,625 vertices, 6,295,552 springs including the
+             reference's duplicate bend springs), 4.0 x 4.0 square, Ks 50.75/50.75/50.95,
+             Kd -0.25, mass 1, gravity (0,-0.00981,0), dt 1/60, top corners pinned,
+             N(0,(1e-3 spacing)^2) position jitter, CG <= 200 iterations to 1e-5.
+  batch4096  4096 cloths, side uniform in [8,128], per-type Ks log-uniform [10,500],
+             Kd uniform [-0.5,-0.05], same jitter, CG <= 200 iterations to 1e-5.
+
+The timed region replays the step's CUDA graph K times on the solver's stream with
+inputs resident in HBM; the per-step working set (grid1025: ~0.75 GB) exceeds the 129 MB
+L2, so no explicit flush is done.  Multi-GPU runs are replicas (one workload per rank,
+no collective on the data path): weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+DT = 1.0 / 60.0
+METRIC = "vertex-steps/s"
+
+
+# ---- workloads ------------------------------------------------------------------------
+
+def grid1025(seed: int):
+    from opencloth_gb300 import ClothDesc, grid_cloth
+
+    cols = 1025
+    X, sp = grid_cloth(cols, cols, ks=(50.75, 50.75, 50.95), kd=(-0.25, -0.25, -0.25), jitter=1e-3, seed=seed)
+    desc = ClothDesc(n_vertices=cols * cols, springs=sp, pinned=np.array([0, cols - 1], np.int32),
+                     cg_max_iter=200, cg_tol=1e-5)
+    return [desc], [(cols, cols)], X, np.zeros_like(X)
+
+
+def batch4096(seed: int, count: int = 4096):
+    from opencloth_gb300 import ClothDesc, grid_cloth
+
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(8, 129, count)
+    descs, shapes, Xs = [], [], []
+    for k, n in enumerate(sides):
+        n = int(n)
+        ks = np.exp(rng.uniform(np.log(10.0), np.log(500.0), 3))
+        kd = rng.uniform(-0.5, -0.05, 3)
+        X, sp = grid_cloth(n, n, ks=tuple(ks), kd=tuple(kd), jitter=1e-3, seed=seed * 100003 + k)
+        descs.append(ClothDesc(n_vertices=n * n, springs=sp, pinned=np.array([0, n - 1], np.int32),
+                               cg_max_iter=200, cg_tol=1e-5))
+        shapes.append((n, n))
+        Xs.append(X)
+    X = np.concatenate(Xs)
+    return descs, shapes, X, np.zeros_like(X)
+
+
+WORKLOADS = {"grid1025": grid1025, "batch4096": batch4096}
+
+
+def algorithmic_bytes(kernel: str, n_vertices: int, n_springs: int, first_dir: bool = False) -> int:
+    """Bytes a launch must move, each array element counted once (device layout:
+    X/V float4 with mass / pin flag in w, 16-byte incidence records, FP32 planes)."""
+    N, S = n_vertices, n_springs
+    if kernel == "k_assemble":
+        # X, V 32 + rowptr 4 + own spring ends/params 24 + warm start 12 + A 24 + r 12 + d 12
+        # per vertex, plus two 16-byte incidence records per spring.
+        return 120 * N + 32 * S
+    if kernel == "k_cg_dir":
+        return (36 if first_dir else 60) * N  # A 24 + d 12 (+ r 12, d write 12)
+    if kernel == "k_cg_update":
+        return 84 * N  # A 24 + d 12 + x 12 + r 12, write x 12 + r 12
+    if kernel == "k_integrate":
+        return 76 * N  # X, V 32 + dV 12 in, X, V 32 out
+    raise KeyError(kernel)
+
+
+# ---- clocks -----------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for name, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        finally:
+            os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- CPU side (oracle) ------------------------------------------------------------------
+
+def _cpu_worker(args):
+    """One process: the oracle port on a list of cloths for a number of steps."""
+    import oracle
+
+    items, steps, use_ref = args
+    vsteps, secs = 0, 0.0
+    for springs, cols, rows, X, i_max, eps in items:
+        n = cols * rows
+        if use_ref:
+            cl = oracle.Cloth(n, springs, num_x=cols - 1, i_max=i_max, eps=eps)
+            _, s = oracle.ref_run(cl, cols - 1, rows - 1, X, np.zeros_like(X), snaps=(steps,), timed=True)
+        else:
+            cl = oracle.Cloth(n, springs, pinned=[0, cols - 1], i_max=i_max, eps=eps)
+            t0 = time.perf_counter()
+            oracle.port_step(cl, X, np.zeros_like(X), n_steps=steps, filter_pinned=True)
+            s = time.perf_counter() - t0
+        vsteps += n * steps
+        secs += s
+    return vsteps, secs
+
+
+def cpu_throughput(workload: str, descs, shapes, X, budget_s: float, processes: int):
+    """The reference step (or its port) on a bounded sample of the same workload.
+    Returns (vertex-steps/s, cores, kind, sample description)."""
+    import oracle
+
+    oracle.build(reference=True)
+    use_ref = oracle.ref_available()
+    kind = "reference" if use_ref else "port"
+    offs = np.cumsum([0] + [d.n_vertices for d in descs])
+    items = [(d.springs, c, r, X[offs[k]:offs[k + 1]], d.cg_max_iter, d.cg_tol)
+             for k, (d, (c, r)) in enumerate(zip(descs, shapes))]
+    if len(items) == 1:
+        # One cloth: the reference is serial.  Time single steps until the budget is spent.
+        t0, steps, vs, secs = time.perf_counter(), 0, 0, 0.0
+        Xc = items[0][3]
+        while True:
+            v, s = _cpu_worker(([items[0][:3] + (Xc,) + items[0][4:]], 1, use_ref))
+            vs, secs, steps = vs + v, secs + s, steps + 1
+            if time.perf_counter() - t0 >= budget_s:
+                break
+        c, r = shapes[0]
+        return vs / secs, 1, kind, f"{steps} step(s) of the full {c}x{r} cloth from its initial state, 1 thread"
+    # Batch: a size-spanning subset of cloths, one process per core, 3 steps each.
+    order = np.argsort([it[1] * it[2] for it in items])
+    pick = order[np.linspace(0, len(order) - 1, min(len(order), 8 * processes)).astype(int)]
+    chunks = [[items[i] for i in pick[j::processes]] for j in range(processes)]
+    import multiprocessing as mp
+
+    steps = 3
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(processes) as pool:
+        res = pool.map(_cpu_worker, [(c, steps, use_ref) for c in chunks if c])
+    wall = time.perf_counter() - t0
+    vs = sum(r[0] for r in res)
+    return vs / wall, processes, kind, (f"{len(pick)} cloths spanning the size range x {steps} steps, "
+                                        f"{processes} processes (one per core)")
+
+
+# ---- arms -------------------------------------------------------------------------------
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_reference(args) -> None:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    descs, shapes, X, _ = WORKLOADS[args.workload](args.seed)
+    nv = sum(d.n_vertices for d in descs)
+    procs = max(1, os.cpu_count() or 1)
+    budget = min(120.0, 2.0 * max(args.steps, 1))
+    value, cores, kind, sample = cpu_throughput(args.workload, descs, shapes, X, budget, procs)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * nv / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "vertices": nv, "instances": len(descs)},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+
+    from opencloth_gb300 import ClothSolver
+    from opencloth_gb300.build import build
+
+    rank, world, local = dist_env()
+    build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    descs, shapes, X0, V0 = WORKLOADS[args.workload](args.seed + 7919 * rank)
+    nv = sum(d.n_vertices for d in descs)
+    ns = sum(len(d.springs) for d in descs)
+    stream = torch.cuda.Stream()
+    solver = ClothSolver(descs, device=local, stream=stream.cuda_stream)
+    solver.set_state(X0, V0)
+    solver.step(DT, args.warmup)
+    solver.synchronize()
+    l0 = solver.launch_count()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        solver.step(DT, args.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    launches = solver.launch_count() - l0
+    iters, rr, flags = solver.stats()
+    value = nv * args.steps * world / (ms / 1e3)
+
+    # Per-kernel durations (CUDA events around each launch, same stream) for the roofline.
+    prof = solver.profile(DT, 3)
+    dom = max(prof, key=lambda k: prof[k]["ms_total"])
+    launches_dom = prof[dom]["launches"]
+    avg_s = prof[dom]["ms_total"] / 1e3 / max(launches_dom, 1)
+    if dom == "k_cg_dir":
+        n_first = prof["k_assemble"]["launches"]
+        tot = (n_first * algorithmic_bytes(dom, nv, ns, True)
+               + (launches_dom - n_first) * algorithmic_bytes(dom, nv, ns, False))
+        per_launch = tot / max(launches_dom, 1)
+    else:
+        per_launch = algorithmic_bytes(dom, nv, ns)
+    achieved = per_launch / avg_s / 1e9
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    if peaks_path.exists():
+        peak, peak_src = float(json.loads(peaks_path.read_text())["hbm_gbs"]), "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    traffic = None
+    tpath = ROOT / "profiles" / f"{dom}_{args.workload}.traffic.json"
+    if tpath.exists():
+        traffic = json.loads(tpath.read_text()).get("dram_bytes_per_launch")
+
+    # End to end through the public API with host buffers: per step, pinned host X, V
+    # in, one step, X, V back out.
+    e2e_steps = max(5, min(args.steps, 50))
+    Xh = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True).numpy()
+    Vh = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True).numpy()
+    solver.get_state_into(Xh, Vh, None)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        solver.set_state(Xh, Vh)
+        solver.step(DT, 1)
+        solver.get_state_into(Xh, Vh, None)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": nv * e2e_steps * world / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 24 * nv,
+           "d2h_bytes_per_step": 24 * nv, "steps": e2e_steps}
+
+    if rank == 0:
+        cpu_v, cores, kind, sample = cpu_throughput(args.workload, descs, shapes, X0, 12.0,
+                                                    max(1, os.cpu_count() or 1))
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "vertices": nv, "springs": ns, "instances": len(descs),
+                       "dt": DT, "cg_max_iter": 200, "cg_tol": 1e-5, "parallelism": f"replicas x{world}",
+                       "l2": "per-step working set larger than the 129 MB L2; no flush"},
+            "cg": {"iters_last_step_max": int(iters.max()), "iters_last_step_mean": float(iters.mean()),
+                   "rel_residual_max": float(rr.max()), "flags_any": int(np.bitwise_or.reduce(flags))},
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(),
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": per_launch, "avg_launch_us": avg_s * 1e6},
+            "kernels": {k: {"avg_us": 1e3 * v["ms_total"] / max(v["launches"], 1), "launches": v["launches"]}
+                        for k, v in prof.items()},
+            "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cores, "kind": kind, "sample": sample},
+        }
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="grid1025")
+    ap.add_argument("--seed", type=int, default=20261203)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

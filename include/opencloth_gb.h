@@ -8,7 +8,7 @@
  *   ComputeForces()            IMP:698   -> oc_step (force gather) / oc_compute_forces
  *   CalcForceDerivatives()     IMP:737   -> oc_step (Jacobians)    / oc_assemble
  *   IntegrateImplicit(dt)      IMP:775   -> oc_step (assembly, PCG, update)
- *   StepPhysics(dt)            IMP:873   -> oc_step + oc_provot_ellipsoid (optional passes)
+ *   StepPhysics(dt)            IMP:873   -> oc_step (ComputeForces + IntegrateImplicit)
  *   AddSpring(a,b,ks,kd,type)  IMP:370   -> oc_spring records in oc_cloth_desc
  *   globals X, V, dV           IMP:80-81, IMP:361 -> oc_set_state / oc_get_state
  *
@@ -70,6 +70,10 @@ typedef struct oc_spring {
  * into a 3x3 block-CSR matrix (Baraff-Witkin coupling; no counterpart in the reference). */
 #define OC_JAC_COUPLED 1
 
+/* Upper bound on cg_max_iter: the device-driven CG loop of a step runs at most this
+ * many passes, so every step ends. */
+#define OC_MAX_CG_ITER 100000
+
 /* ---- one cloth (one instance) ----------------------------------------------------- */
 typedef struct oc_cloth_desc {
     int32_t n_vertices;
@@ -81,7 +85,7 @@ typedef struct oc_cloth_desc {
     const float* ext_force;    /* 3*n_vertices constant external force, or NULL */
     float gravity[3];          /* IMP:108, added as m*g to unpinned vertices */
     float velocity_damping;    /* DEFAULT_DAMPING, IMP:104 (-0.125) */
-    int32_t cg_max_iter;       /* i_max, IMP:128 */
+    int32_t cg_max_iter;       /* i_max, IMP:128; at most OC_MAX_CG_ITER */
     float cg_tol;              /* EPS, IMP:126; the CG stops when r.r <= EPS^2 * delta0 */
     int32_t jacobian_mode;     /* OC_JAC_* */
 } oc_cloth_desc;
@@ -135,6 +139,10 @@ oc_status oc_synchronize(oc_solver* s);
 /* Per-instance results of the last step: CG iterations, relative residual
  * sqrt(delta_new / delta0), OC_FLAG_* bits.  Any pointer may be NULL. */
 oc_status oc_get_stats(oc_solver* s, int32_t* cg_iters, double* rel_residual, uint32_t* flags);
+
+/* Kernels of the step (force/assembly, CG direction, CG update, integration)
+ * launched by this handle so far, counted on the device for the graph's CG loop. */
+oc_status oc_get_launch_count(oc_solver* s, int64_t* kernels_launched);
 
 /* ComputeForces alone on the current state (IMP:698-735): F, packed float triples. */
 oc_status oc_compute_forces(oc_solver* s, float* F);

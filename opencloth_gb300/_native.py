@@ -87,6 +87,7 @@ SIGNATURES = {
     "oc_step": (C.c_int32, [_P, C.c_float, C.c_int32]),
     "oc_synchronize": (C.c_int32, [_P]),
     "oc_get_stats": (C.c_int32, [_P, _P, _P, _P]),
+    "oc_get_launch_count": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
     "oc_compute_forces": (C.c_int32, [_P, _P]),
     "oc_assemble": (C.c_int32, [_P, C.c_float, _P, _P]),
     "oc_profile_steps": (C.c_int32, [_P, C.c_float, C.c_int32, C.c_int32, _P, _P, _P, _P]),

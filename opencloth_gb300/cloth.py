@@ -171,6 +171,13 @@ class ClothSolver:
         self._call(self._lib.oc_get_state(self._h, ptr(X), ptr(V), ptr(dV)))
         return X, V, dV
 
+    def get_state_into(self, X=None, V=None, dV=None) -> None:
+        """Read the state into caller-owned contiguous float32 arrays (any may be None)."""
+        for a in (X, V, dV):
+            if a is not None and (a.dtype != np.float32 or not a.flags.c_contiguous or a.size != 3 * self.n_vertices):
+                raise ValueError("get_state_into needs contiguous float32 arrays of 3 * n_vertices")
+        self._call(self._lib.oc_get_state(self._h, ptr(X), ptr(V), ptr(dV)))
+
     def set_state_device(self, X=0, V=0, dV=0) -> None:
         """Device pointers (ints) to packed float triples; 0 leaves an array unchanged."""
         self._call(self._lib.oc_set_state_device(self._h, X or None, V or None, dV or None))
@@ -190,6 +197,11 @@ class ClothSolver:
         fl = np.zeros(self.n_instances, np.uint32)
         self._call(self._lib.oc_get_stats(self._h, ptr(it), ptr(rr), ptr(fl)))
         return it, rr, fl
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._call(self._lib.oc_get_launch_count(self._h, C.byref(n)))
+        return int(n.value)
 
     def compute_forces(self) -> np.ndarray:
         F = np.empty((self.n_vertices, 3), np.float32)

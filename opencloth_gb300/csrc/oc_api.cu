@@ -37,6 +37,8 @@ struct oc_solver {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     float graph_dt = 0.0f;
+    int64_t host_launches = 0;  // k_assemble + k_integrate launches enqueued
+    unsigned long long* h_loop = nullptr;
     std::string err;
 };
 
@@ -82,6 +84,7 @@ void release(oc_solver* s) {
     s->allocs.clear();
     if (s->h_state) cudaFreeHost(s->h_state);
     if (s->h_scalar) cudaFreeHost(s->h_scalar);
+    if (s->h_loop) cudaFreeHost(s->h_loop);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -120,6 +123,7 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
         const int nb = per_cloth ? s->inst_host[grp].nblk : s->n_blocks;
         oc_status st = launch_timed(s, K_ASSEMBLE, a, nb, t);
         if (st != OC_OK) return st;
+        s->host_launches += 2;
         for (;;) {
             if (per_cloth)
                 OC_TRY(cudaMemcpyAsync(s->h_scalar, &s->args.state[grp].active, sizeof(int32_t),
@@ -323,6 +327,9 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     a.blocks = blocks;
     OC_CREATE_TRY(dalloc(s, &a.unconverged, 1));
     OC_CREATE_TRY(dalloc(s, &a.grid_ticket, 1));
+    OC_CREATE_TRY(dalloc(s, &a.loop_count, 1));
+    OC_CREATE_TRY(cudaMemset(a.loop_count, 0, sizeof(unsigned long long)));
+    OC_CREATE_TRY(cudaMallocHost(&s->h_loop, sizeof(unsigned long long)));
     OC_CREATE_TRY(cudaMemset(a.unconverged, 0, sizeof(int32_t)));
     OC_CREATE_TRY(cudaMemset(a.grid_ticket, 0, sizeof(uint32_t)));
     OC_CREATE_TRY(dalloc(s, &s->stage, 9 * (size_t)P.nv));
@@ -427,6 +434,7 @@ oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
         if (st != OC_OK) return st;
     }
     for (int32_t i = 0; i < n_steps; ++i) OC_TRY(cudaGraphLaunch(s->exec, s->stream));
+    s->host_launches += 2 * (int64_t)n_steps;
     return OC_OK;
 }
 
@@ -448,6 +456,16 @@ oc_status oc_get_stats(oc_solver* s, int32_t* cg_iters, double* rel_residual, ui
         if (rel_residual) rel_residual[k] = st.delta0 > 0.0 ? std::sqrt(st.delta_new / st.delta0) : 0.0;
         if (flags) flags[k] = st.flags;
     }
+    return OC_OK;
+}
+
+oc_status oc_get_launch_count(oc_solver* s, int64_t* kernels_launched) {
+    if (!valid_solver(s) || !kernels_launched) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    OC_TRY(cudaMemcpyAsync(s->h_loop, s->args.loop_count, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    *kernels_launched = s->host_launches + 2 * (int64_t)*s->h_loop;
     return OC_OK;
 }
 

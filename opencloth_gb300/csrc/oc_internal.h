@@ -64,6 +64,7 @@ struct StepArgs {
     const BlockInfo* blocks;
     int32_t* unconverged;    // number of instances whose CG is running
     uint32_t* grid_ticket;   // arrivals of all blocks in the current kernel
+    unsigned long long* loop_count;  // completed (k_cg_dir, k_cg_update) launch pairs
     float dt;
     int32_t blk_base;        // first block of this launch (per-cloth launches)
     int32_t vpt;             // vertices per thread

@@ -213,6 +213,7 @@ __device__ void finish(const StepArgs& a, int blk, int inst, bool participates, 
         const unsigned t = atomicAdd(a.grid_ticket, 1u);
         if (t == gridDim.x - 1) {
             *a.grid_ticket = 0u;
+            if (KIND == K_CG_UPDATE) atomicAdd(a.loop_count, 1ull);
             __threadfence();
             if (a.use_cond) {
                 const int u = atomicAdd(a.unconverged, 0);

@@ -48,8 +48,8 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
             *err = who + "jacobian_mode " + std::to_string(d.jacobian_mode) + " is not available";
             return OC_ERR_UNSUPPORTED;
         }
-        if (d.cg_max_iter < 0 || !std::isfinite(d.cg_tol) || d.cg_tol < 0.0f) {
-            *err = who + "cg_max_iter must be >= 0 and cg_tol finite and >= 0";
+        if (d.cg_max_iter < 0 || d.cg_max_iter > OC_MAX_CG_ITER || !std::isfinite(d.cg_tol) || d.cg_tol < 0.0f) {
+            *err = who + "cg_max_iter must be in [0, OC_MAX_CG_ITER] and cg_tol finite and >= 0";
             return OC_ERR_INVALID_ARGUMENT;
         }
         if (!finite3(d.gravity) || !std::isfinite(d.velocity_damping)) {
