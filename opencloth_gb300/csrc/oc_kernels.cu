@@ -162,6 +162,7 @@ __device__ void finish(const StepArgs& a, int blk, int inst, bool participates, 
             __threadfence();
             const InstParams& ip = a.inst[inst];
             double acc = 0.0;
+#pragma unroll 8
             for (int j = threadIdx.x; j < ip.nblk; j += blockDim.x) acc += __ldcg(a.partials + ip.blk0 + j);
             const double total = block_sum(acc);
             if (threadIdx.x == 0) {

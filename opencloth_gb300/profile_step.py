@@ -1,0 +1,74 @@
+"""Run a few implicit steps of a synthetic workload, for profilers and launch-shape sweeps.
+
+    python -m opencloth_gb300.profile_step --cols 1025 --steps 3 [--vpt 4] [--instances 1]
+
+Prints one JSON line: graph-replayed ms/step (CUDA events on the solver's stream) and
+the per-kernel average durations of an un-graphed pass.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import ClothDesc, ClothSolver, grid_cloth
+
+
+def workload(cols: int, instances: int, seed: int, random_sides: bool):
+    rng = np.random.default_rng(seed)
+    descs, Xs = [], []
+    for k in range(instances):
+        n = int(rng.integers(8, 129)) if random_sides else cols
+        ks = np.exp(rng.uniform(np.log(10.0), np.log(500.0), 3)) if random_sides else (50.75, 50.75, 50.95)
+        kd = rng.uniform(-0.5, -0.05, 3) if random_sides else (-0.25, -0.25, -0.25)
+        X, sp = grid_cloth(n, n, ks=tuple(ks), kd=tuple(kd), jitter=1e-3, seed=seed + k)
+        descs.append(ClothDesc(n_vertices=n * n, springs=sp, pinned=np.array([0, n - 1], np.int32),
+                               cg_max_iter=200, cg_tol=1e-5))
+        Xs.append(X)
+    return descs, np.concatenate(Xs)
+
+
+def main() -> None:
+    import torch
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--cols", type=int, default=1025)
+    ap.add_argument("--instances", type=int, default=1)
+    ap.add_argument("--random-sides", action="store_true", help="sides uniform in [8,128], random Ks/Kd")
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--vpt", type=int, default=0)
+    ap.add_argument("--executor", default="auto")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-profile", action="store_true")
+    a = ap.parse_args()
+    t0 = time.perf_counter()
+    descs, X = workload(a.cols, a.instances, a.seed, a.random_sides)
+    stream = torch.cuda.Stream()
+    s = ClothSolver(descs, stream=stream.cuda_stream, vertices_per_thread=a.vpt, executor=a.executor)
+    s.set_state(X, np.zeros_like(X))
+    setup = time.perf_counter() - t0
+    s.step(1.0 / 60.0, a.warmup)
+    s.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.step(1.0 / 60.0, a.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / max(a.steps, 1)
+    it, rr, fl = s.stats()
+    out = {"vertices": s.n_vertices, "springs": s.n_springs, "instances": s.n_instances, "vpt": a.vpt,
+           "executor": a.executor, "ms_per_step": ms, "vertex_steps_per_s": s.n_vertices / (ms / 1e3),
+           "iters_max": int(it.max()), "residual_max": float(rr.max()), "flags": int(np.bitwise_or.reduce(fl)),
+           "setup_s": setup}
+    if not a.no_profile:
+        prof = s.profile(1.0 / 60.0, 2)
+        out["kernels_us"] = {k: 1e3 * v["ms_total"] / max(v["launches"], 1) for k, v in prof.items()}
+    print(json.dumps(out), flush=True)
+    s.close()
+
+
+if __name__ == "__main__":
+    main()
