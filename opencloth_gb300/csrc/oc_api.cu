@@ -249,7 +249,9 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
 
     oc_solver* s = new (std::nothrow) oc_solver();
     if (!s) return OC_ERR_OUT_OF_MEMORY;
-    const int vpt = o.vertices_per_thread > 0 ? o.vertices_per_thread : 1;
+    // Eight vertices per thread: fewer, longer-lived blocks (one wave for a 1M-vertex
+    // cloth) amortise the per-block reduction epilogue.
+    const int vpt = o.vertices_per_thread > 0 ? o.vertices_per_thread : 8;
     PackedHost P;
     oc_status st = pack_instances(descs, n_instances, kernel_block_threads() * vpt, &P, &s->err);
     if (st != OC_OK) {
