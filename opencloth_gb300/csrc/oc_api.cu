@@ -167,7 +167,7 @@ oc_status build_graph(oc_solver* s, float dt) {
         kp.func = const_cast<void*>(kernel_fn(k));
         kp.gridDim = dim3((unsigned)s->n_blocks);
         kp.blockDim = dim3((unsigned)kernel_block_threads());
-        kp.sharedMemBytes = 0;
+        kp.sharedMemBytes = (unsigned)kernel_smem_bytes(k);
         kp.kernelParams = params;
         kp.extra = nullptr;
         return kp;
@@ -283,6 +283,7 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     s->n_blocks = (int32_t)P.blocks.size();
     s->vertices_per_block = P.vertices_per_block;
     OC_CREATE_TRY(cudaSetDevice(o.device));
+    OC_CREATE_TRY(prepare_kernels());
     if (o.stream) {
         s->stream = static_cast<cudaStream_t>(o.stream);
     } else {

@@ -80,6 +80,8 @@ enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3
 const char* kernel_name(KernelKind k);
 const void* kernel_fn(KernelKind k);
 int kernel_block_threads();
+size_t kernel_smem_bytes(KernelKind k);  // dynamic shared memory of a launch
+cudaError_t prepare_kernels();           // function attributes (once per device)
 
 // Host-side launch of one kernel kind over [blk_base, blk_base + nblocks).
 cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStream_t stream);

@@ -79,44 +79,92 @@ __device__ __forceinline__ void jac_element(const SpringEval& e, float ks, float
     jv = ((zero + (-kd) * dp1) + (-kd) * dp2) + (-kd) * dp3;
 }
 
-// F_i: zero, gravity (m g) unless pinned, damping on all, optional external force,
-// then every incident spring in spring-id order (the reference's scatter order).
-__device__ __forceinline__ float3 gather_force(const StepArgs& a, const InstParams& ip, int64_t g, const float4 Xg,
-                                               const float4 Vg, bool pinned) {
-    float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
-    if (!pinned) {
-        Fx += Xg.w * ip.gravity[0];
-        Fy += Xg.w * ip.gravity[1];
-        Fz += Xg.w * ip.gravity[2];
+// Shared-memory staging of one chunk (blockDim consecutive vertices of a block) for
+// the cooperative force gather.
+constexpr int kIncCap = 3328;  // incidence records staged per round (13 per thread)
+
+struct GatherSmem {
+    float4 X[kThreads];
+    float4 V[kThreads];
+    float fx[kIncCap], fy[kIncCap], fz[kIncCap];
+    uint8_t owner[kIncCap];  // chunk-local vertex of each staged record
+};
+constexpr size_t kGatherSmem = sizeof(GatherSmem);
+
+// F_i for the chunk [c0, c1): zero, gravity (m g) unless pinned, damping on all,
+// optional external force, then every incident spring in spring-id order — the
+// reference's scatter order (IMP:701-734).  The records of the chunk are contiguous;
+// lanes evaluate them in parallel (coalesced record loads, independent neighbour
+// gathers) into shared memory, and each vertex then adds its own forces sequentially,
+// so the FP32 sum is the reference's.  Every thread of the block must call this.
+__device__ float3 chunk_gather(const StepArgs& a, const InstParams& ip, int64_t c0, int64_t c1, GatherSmem& sm,
+                               float4& Xg, float4& Vg) {
+    const int t = threadIdx.x;
+    const int64_t g = c0 + t;
+    const bool valid = g < c1;
+    Xg = make_float4(0.f, 0.f, 0.f, 1.f);
+    Vg = make_float4(0.f, 0.f, 0.f, 0.f);
+    int32_t k0 = 0, k1 = 0;
+    if (valid) {
+        Xg = __ldg(a.X + g);
+        Vg = __ldg(a.V + g);
+        k0 = __ldg(a.rowptr + g);
+        k1 = __ldg(a.rowptr + g + 1);
     }
-    Fx += ip.damping * Vg.x;
-    Fy += ip.damping * Vg.y;
-    Fz += ip.damping * Vg.z;
-    if (!pinned) {
-        if (ip.has_ext) {
+    sm.X[t] = Xg;
+    sm.V[t] = Vg;
+    const bool pinned = Vg.w != 0.0f;
+    float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
+    if (valid) {
+        if (!pinned) {
+            Fx += Xg.w * ip.gravity[0];
+            Fy += Xg.w * ip.gravity[1];
+            Fz += Xg.w * ip.gravity[2];
+        }
+        Fx += ip.damping * Vg.x;
+        Fy += ip.damping * Vg.y;
+        Fz += ip.damping * Vg.z;
+        if (!pinned && ip.has_ext) {
             const float4 e = __ldg(a.fext + g);
             Fx += e.x;
             Fy += e.y;
             Fz += e.z;
         }
-        const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
-        for (int32_t k = k0; k < k1; ++k) {
+    }
+    const int32_t kb = __ldg(a.rowptr + c0), ke = __ldg(a.rowptr + c1);
+    for (int32_t rb = kb; rb < ke; rb += kIncCap) {
+        const int32_t re = min(ke, rb + kIncCap);
+        __syncthreads();
+        for (int32_t k = max(k0, rb); k < min(k1, re); ++k) sm.owner[k - rb] = (uint8_t)t;
+        __syncthreads();
+#pragma unroll 4
+        for (int32_t k = rb + t; k < re; k += blockDim.x) {
             const int4 rec = __ldg(a.inc + k);
-            const bool as_p2 = rec.x < 0;
-            const int32_t o = rec.x & 0x7fffffff;
-            const float4 Xo = __ldg(a.X + o), Vo = __ldg(a.V + o);
-            const float3 f = as_p2 ? spring_force(Xo, Xg, Vo, Vg, __int_as_float(rec.y), __int_as_float(rec.z),
-                                                  __int_as_float(rec.w))
-                                   : spring_force(Xg, Xo, Vg, Vo, __int_as_float(rec.y), __int_as_float(rec.z),
-                                                  __int_as_float(rec.w));
-            if (as_p2) {
-                Fx -= f.x;
-                Fy -= f.y;
-                Fz -= f.z;
-            } else {
-                Fx += f.x;
-                Fy += f.y;
-                Fz += f.z;
+            const int self = sm.owner[k - rb];
+            const float4 Xs = sm.X[self], Vs = sm.V[self];
+            float3 f = make_float3(0.f, 0.f, 0.f);
+            if (Vs.w == 0.0f) {  // pinned vertices take no spring force (IMP:730-733)
+                const bool as_p2 = rec.x < 0;
+                const int32_t o = rec.x & 0x7fffffff;
+                const float4 Xo = __ldg(a.X + o), Vo = __ldg(a.V + o);
+                const float rest = __int_as_float(rec.y), ks = __int_as_float(rec.z), kd = __int_as_float(rec.w);
+                if (as_p2) {  // F[p2] -= f, IMP:733
+                    f = spring_force(Xo, Xs, Vo, Vs, rest, ks, kd);
+                    f = make_float3(-f.x, -f.y, -f.z);
+                } else {  // F[p1] += f, IMP:731
+                    f = spring_force(Xs, Xo, Vs, Vo, rest, ks, kd);
+                }
+            }
+            sm.fx[k - rb] = f.x;
+            sm.fy[k - rb] = f.y;
+            sm.fz[k - rb] = f.z;
+        }
+        __syncthreads();
+        if (valid && !pinned) {
+            for (int32_t k = max(k0, rb); k < min(k1, re); ++k) {
+                Fx += sm.fx[k - rb];
+                Fy += sm.fy[k - rb];
+                Fz += sm.fz[k - rb];
             }
         }
     }
@@ -233,15 +281,19 @@ __device__ __forceinline__ void matvec(const float A[6], float x0, float x1, flo
 }
 
 __global__ void __launch_bounds__(kThreads) k_assemble(const StepArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    GatherSmem& sm = *reinterpret_cast<GatherSmem*>(smem_raw);
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstParams& ip = a.inst[bi.inst];
     const float h = a.dt;
     double part = 0.0;
-    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
-        const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
+    for (int64_t c0 = bi.v_begin; c0 < bi.v_end; c0 += blockDim.x) {
+        const int64_t g = c0 + threadIdx.x;
+        float4 Xg, Vg;
+        const float3 F = chunk_gather(a, ip, c0, min(c0 + (int64_t)blockDim.x, bi.v_end), sm, Xg, Vg);
+        if (g >= bi.v_end) continue;
         const bool pinned = Vg.w != 0.0f;
-        const float3 F = gather_force(a, ip, g, Xg, Vg, pinned);
 
         float J[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, Jv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const int2 ends = __ldg(a.own_ends + g);
@@ -310,6 +362,10 @@ __global__ void __launch_bounds__(kThreads) k_assemble(const StepArgs a) {
     finish<K_ASSEMBLE>(a, blk, bi.inst, true, part);
 }
 
+// The CG passes stream fifteen FP32 planes.  Each thread keeps two vertices' loads in
+// flight (g and g + blockDim) before computing; __restrict__ lets the loads of the
+// next pair be issued ahead of this pair's stores.  The per-thread FP64 partial still
+// adds vertices in the order g, g + blockDim, g + 2 blockDim, ...
 __global__ void __launch_bounds__(kThreads) k_cg_dir(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
@@ -319,22 +375,52 @@ __global__ void __launch_bounds__(kThreads) k_cg_dir(const StepArgs a) {
     if (active) {
         const bool first = st.iter == 0;
         const float beta = st.beta;
-        for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
-            float d0 = a.d[0][g], d1 = a.d[1][g], d2 = a.d[2][g];
-            if (!first) {  // d = r + beta d, IMP:327
-                d0 = a.r[0][g] + d0 * beta;
-                d1 = a.r[1][g] + d1 * beta;
-                d2 = a.r[2][g] + d2 * beta;
-                a.d[0][g] = d0;
-                a.d[1][g] = d1;
-                a.d[2][g] = d2;
-            }
-            float A[6];
+        const float* __restrict__ A0 = a.A[0];
+        const float* __restrict__ A1 = a.A[1];
+        const float* __restrict__ A2 = a.A[2];
+        const float* __restrict__ A3 = a.A[3];
+        const float* __restrict__ A4 = a.A[4];
+        const float* __restrict__ A5 = a.A[5];
+        const float* __restrict__ R0 = a.r[0];
+        const float* __restrict__ R1 = a.r[1];
+        const float* __restrict__ R2 = a.r[2];
+        float* __restrict__ D0 = a.d[0];
+        float* __restrict__ D1 = a.d[1];
+        float* __restrict__ D2 = a.d[2];
+        const int64_t T = blockDim.x;
+        for (int64_t base = bi.v_begin + threadIdx.x; base < bi.v_end; base += 2 * T) {
+            float A[2][6], d[2][3], r[2][3];
+            bool ok[2];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) A[k] = a.A[k][g];
-            float q0, q1, q2;
-            matvec(A, d0, d1, d2, q0, q1, q2);
-            part += (double)(d0 * q0 + d1 * q1 + d2 * q2);
+            for (int u = 0; u < 2; ++u) {
+                const int64_t g = base + u * T;
+                ok[u] = g < bi.v_end;
+                const int64_t q = ok[u] ? g : base;
+                A[u][0] = A0[q]; A[u][1] = A1[q]; A[u][2] = A2[q];
+                A[u][3] = A3[q]; A[u][4] = A4[q]; A[u][5] = A5[q];
+                d[u][0] = D0[q]; d[u][1] = D1[q]; d[u][2] = D2[q];
+                r[u][0] = 0.f; r[u][1] = 0.f; r[u][2] = 0.f;
+                if (!first) {
+                    r[u][0] = R0[q]; r[u][1] = R1[q]; r[u][2] = R2[q];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (!ok[u]) continue;
+                const int64_t g = base + u * T;
+                float d0 = d[u][0], d1 = d[u][1], d2 = d[u][2];
+                if (!first) {  // d = r + beta d, IMP:327
+                    d0 = r[u][0] + d0 * beta;
+                    d1 = r[u][1] + d1 * beta;
+                    d2 = r[u][2] + d2 * beta;
+                    D0[g] = d0;
+                    D1[g] = d1;
+                    D2[g] = d2;
+                }
+                float q0, q1, q2;
+                matvec(A[u], d0, d1, d2, q0, q1, q2);
+                part += (double)(d0 * q0 + d1 * q1 + d2 * q2);
+            }
         }
     }
     finish<K_CG_DIR>(a, blk, bi.inst, active, part);
@@ -348,23 +434,53 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
     double part = 0.0;
     if (active) {
         const float alpha = st.alpha;
-        for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
-            const float d0 = a.d[0][g], d1 = a.d[1][g], d2 = a.d[2][g];
-            float A[6];
+        const float* __restrict__ A0 = a.A[0];
+        const float* __restrict__ A1 = a.A[1];
+        const float* __restrict__ A2 = a.A[2];
+        const float* __restrict__ A3 = a.A[3];
+        const float* __restrict__ A4 = a.A[4];
+        const float* __restrict__ A5 = a.A[5];
+        const float* __restrict__ D0 = a.d[0];
+        const float* __restrict__ D1 = a.d[1];
+        const float* __restrict__ D2 = a.d[2];
+        float* __restrict__ X0 = a.x[0];
+        float* __restrict__ X1 = a.x[1];
+        float* __restrict__ X2 = a.x[2];
+        float* __restrict__ R0 = a.r[0];
+        float* __restrict__ R1 = a.r[1];
+        float* __restrict__ R2 = a.r[2];
+        const int64_t T = blockDim.x;
+        for (int64_t base = bi.v_begin + threadIdx.x; base < bi.v_end; base += 2 * T) {
+            float A[2][6], d[2][3], x[2][3], r[2][3];
+            bool ok[2];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) A[k] = a.A[k][g];
-            float q0, q1, q2;
-            matvec(A, d0, d1, d2, q0, q1, q2);
-            a.x[0][g] = a.x[0][g] + d0 * alpha;  // x = x + alpha d, IMP:322
-            a.x[1][g] = a.x[1][g] + d1 * alpha;
-            a.x[2][g] = a.x[2][g] + d2 * alpha;
-            const float r0 = a.r[0][g] - q0 * alpha;  // r = r - alpha q, IMP:323
-            const float r1 = a.r[1][g] - q1 * alpha;
-            const float r2 = a.r[2][g] - q2 * alpha;
-            a.r[0][g] = r0;
-            a.r[1][g] = r1;
-            a.r[2][g] = r2;
-            part += (double)(r0 * r0 + r1 * r1 + r2 * r2);
+            for (int u = 0; u < 2; ++u) {
+                const int64_t g = base + u * T;
+                ok[u] = g < bi.v_end;
+                const int64_t q = ok[u] ? g : base;
+                A[u][0] = A0[q]; A[u][1] = A1[q]; A[u][2] = A2[q];
+                A[u][3] = A3[q]; A[u][4] = A4[q]; A[u][5] = A5[q];
+                d[u][0] = D0[q]; d[u][1] = D1[q]; d[u][2] = D2[q];
+                x[u][0] = X0[q]; x[u][1] = X1[q]; x[u][2] = X2[q];
+                r[u][0] = R0[q]; r[u][1] = R1[q]; r[u][2] = R2[q];
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (!ok[u]) continue;
+                const int64_t g = base + u * T;
+                float q0, q1, q2;
+                matvec(A[u], d[u][0], d[u][1], d[u][2], q0, q1, q2);
+                X0[g] = x[u][0] + d[u][0] * alpha;  // x = x + alpha d, IMP:322
+                X1[g] = x[u][1] + d[u][1] * alpha;
+                X2[g] = x[u][2] + d[u][2] * alpha;
+                const float r0 = r[u][0] - q0 * alpha;  // r = r - alpha q, IMP:323
+                const float r1 = r[u][1] - q1 * alpha;
+                const float r2 = r[u][2] - q2 * alpha;
+                R0[g] = r0;
+                R1[g] = r1;
+                R2[g] = r2;
+                part += (double)(r0 * r0 + r1 * r1 + r2 * r2);
+            }
         }
     }
     finish<K_CG_UPDATE>(a, blk, bi.inst, active, part);
@@ -389,12 +505,16 @@ __global__ void __launch_bounds__(kThreads) k_integrate(const StepArgs a) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_forces(const StepArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    GatherSmem& sm = *reinterpret_cast<GatherSmem*>(smem_raw);
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstParams& ip = a.inst[bi.inst];
-    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
-        const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
-        const float3 F = gather_force(a, ip, g, Xg, Vg, Vg.w != 0.0f);
+    for (int64_t c0 = bi.v_begin; c0 < bi.v_end; c0 += blockDim.x) {
+        const int64_t g = c0 + threadIdx.x;
+        float4 Xg, Vg;
+        const float3 F = chunk_gather(a, ip, c0, min(c0 + (int64_t)blockDim.x, bi.v_end), sm, Xg, Vg);
+        if (g >= bi.v_end) continue;
         a.dbg_F[3 * g] = F.x;
         a.dbg_F[3 * g + 1] = F.y;
         a.dbg_F[3 * g + 2] = F.z;
@@ -482,6 +602,15 @@ const void* kernel_fn(KernelKind k) {
 
 int kernel_block_threads() { return kThreads; }
 
+size_t kernel_smem_bytes(KernelKind k) { return (k == K_ASSEMBLE || k == K_FORCES) ? kGatherSmem : 0; }
+
+cudaError_t prepare_kernels() {
+    cudaError_t e = cudaFuncSetAttribute(k_assemble, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGatherSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_forces, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGatherSmem);
+    return e;
+}
+
 static int state_blocks(int64_t nv) {
     const int64_t b = (nv + kThreads - 1) / kThreads;
     return (int)(b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
@@ -501,11 +630,11 @@ cudaError_t launch_state_out(const StepArgs& a, float* X3, float* V3, float* dV3
 cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStream_t stream) {
     if (nblocks <= 0) return cudaSuccess;
     switch (k) {
-        case K_ASSEMBLE: k_assemble<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_ASSEMBLE: k_assemble<<<nblocks, kThreads, kGatherSmem, stream>>>(a); break;
         case K_CG_DIR: k_cg_dir<<<nblocks, kThreads, 0, stream>>>(a); break;
         case K_CG_UPDATE: k_cg_update<<<nblocks, kThreads, 0, stream>>>(a); break;
         case K_INTEGRATE: k_integrate<<<nblocks, kThreads, 0, stream>>>(a); break;
-        case K_FORCES: k_forces<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_FORCES: k_forces<<<nblocks, kThreads, kGatherSmem, stream>>>(a); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
