@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -283,7 +284,11 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     s->n_blocks = (int32_t)P.blocks.size();
     s->vertices_per_block = P.vertices_per_block;
     OC_CREATE_TRY(cudaSetDevice(o.device));
-    OC_CREATE_TRY(prepare_kernels());
+    {
+        // Force-gather variant (a tuning knob; OC_GATHER_VARIANT overrides the default).
+        const char* gv = std::getenv("OC_GATHER_VARIANT");
+        OC_CREATE_TRY(prepare_kernels(gv ? std::atoi(gv) : 3));
+    }
     if (o.stream) {
         s->stream = static_cast<cudaStream_t>(o.stream);
     } else {

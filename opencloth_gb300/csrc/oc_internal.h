@@ -81,7 +81,9 @@ const char* kernel_name(KernelKind k);
 const void* kernel_fn(KernelKind k);
 int kernel_block_threads();
 size_t kernel_smem_bytes(KernelKind k);  // dynamic shared memory of a launch
-cudaError_t prepare_kernels();           // function attributes (once per device)
+// Function attributes and the force-gather variant of k_assemble (0 block-cooperative,
+// 1/2/3 one thread per vertex with 1/2/4 incidences in flight).
+cudaError_t prepare_kernels(int gather_variant);
 
 // Host-side launch of one kernel kind over [blk_base, blk_base + nblocks).
 cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStream_t stream);

@@ -280,84 +280,183 @@ __device__ __forceinline__ void matvec(const float A[6], float x0, float x1, flo
     y2 = A[2] * x0 + A[4] * x1 + A[5] * x2;
 }
 
-__global__ void __launch_bounds__(kThreads) k_assemble(const StepArgs a) {
+// Per-vertex part of the assembly after the force gather: Jacobians of spring i
+// (CalcForceDerivatives, IMP:744-770), A_i and b_i (IMP:782-783), and the CG set-up
+// r = b - A x, d = P^-1 r, r.(P r) (IMP:310-318) with pinned rows filtered out.
+// Returns the vertex's FP32 term of delta0.
+__device__ __forceinline__ double assemble_vertex(const StepArgs& a, int64_t g, const float4 Xg, const float4 Vg,
+                                                  const float3 F, const int2 ends, const float4 par,
+                                                  const float4 E1, const float4 E2, const float4 W1,
+                                                  const float4 W2) {
+    const float h = a.dt;
+    const bool pinned = Vg.w != 0.0f;
+    float J[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, Jv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (ends.x >= 0) {
+        SpringEval e;
+        spring_state(E1, E2, W1, W2, par.x, e);
+        jac_element(e, par.y, par.z, 0, 0, J[0], Jv[0]);
+        jac_element(e, par.y, par.z, 0, 1, J[1], Jv[1]);
+        jac_element(e, par.y, par.z, 0, 2, J[2], Jv[2]);
+        jac_element(e, par.y, par.z, 1, 1, J[3], Jv[3]);
+        jac_element(e, par.y, par.z, 1, 2, J[4], Jv[4]);
+        jac_element(e, par.y, par.z, 2, 2, J[5], Jv[5]);
+    }
+    // A = M - h (df_dv + h df_dx), b = h (F + (h df_dx)(V + y)), IMP:782-783.
+    float A[6], hJ[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const float Mk = (k == 0 || k == 3 || k == 5) ? Xg.w : 0.0f;
+        A[k] = Mk - h * (Jv[k] + h * J[k]);
+        hJ[k] = h * J[k];
+    }
+    const float y = 0.0f;
+    const float vx = Vg.x + y, vy = Vg.y + y, vz = Vg.z + y;
+    float wx, wy, wz;
+    matvec(hJ, vx, vy, vz, wx, wy, wz);
+    const float bx = h * (F.x + wx), by = h * (F.y + wy), bz = h * (F.z + wz);
+
+    float x0 = a.x[0][g], x1 = a.x[1][g], x2 = a.x[2][g];
+    if (pinned) {
+        x0 = x1 = x2 = 0.0f;
+        a.x[0][g] = 0.0f;
+        a.x[1][g] = 0.0f;
+        a.x[2][g] = 0.0f;
+    }
+    float ax, ay, az;
+    matvec(A, x0, x1, x2, ax, ay, az);
+    float r0 = bx - ax, r1 = by - ay, r2 = bz - az;
+    if (pinned) r0 = r1 = r2 = 0.0f;
+    const float pi0 = 1.0f / A[0], pi1 = 1.0f / A[3], pi2 = 1.0f / A[5];
+    const float d0 = pi0 * r0, d1 = pi1 * r1, d2 = pi2 * r2;
+    const float pr0 = A[0] * r0, pr1 = A[3] * r1, pr2 = A[5] * r2;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) a.A[k][g] = A[k];
+    a.r[0][g] = r0;
+    a.r[1][g] = r1;
+    a.r[2][g] = r2;
+    a.d[0][g] = d0;
+    a.d[1][g] = d1;
+    a.d[2][g] = d2;
+    if (a.dbg_A9) {
+        float* o = a.dbg_A9 + 9 * g;
+        o[0] = A[0]; o[1] = A[1]; o[2] = A[2];
+        o[3] = A[1]; o[4] = A[3]; o[5] = A[4];
+        o[6] = A[2]; o[7] = A[4]; o[8] = A[5];
+    }
+    if (a.dbg_b) {
+        a.dbg_b[3 * g] = bx;
+        a.dbg_b[3 * g + 1] = by;
+        a.dbg_b[3 * g + 2] = bz;
+    }
+    return (double)(r0 * pr0 + r1 * pr1 + r2 * pr2);
+}
+
+struct OwnSpring {
+    int2 ends;
+    float4 par, E1, E2, W1, W2;
+};
+
+// Spring i's record and endpoint states for vertex i (loaded early to overlap).
+__device__ __forceinline__ OwnSpring load_own(const StepArgs& a, int64_t g) {
+    OwnSpring o;
+    o.ends = __ldg(a.own_ends + g);
+    o.par = make_float4(0.f, 0.f, 0.f, 0.f);
+    o.E1 = o.E2 = o.W1 = o.W2 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (o.ends.x >= 0) {
+        o.par = __ldg(a.own_par + g);
+        o.E1 = __ldg(a.X + o.ends.x);
+        o.E2 = __ldg(a.X + o.ends.y);
+        o.W1 = __ldg(a.V + o.ends.x);
+        o.W2 = __ldg(a.V + o.ends.y);
+    }
+    return o;
+}
+
+// F_i gathered by the vertex's own thread: B incidence records and their neighbour
+// states are fetched ahead of use, then added in spring-id order (IMP:701-734).
+template <int B>
+__device__ __forceinline__ float3 thread_gather(const StepArgs& a, const InstParams& ip, int64_t g, const float4 Xg,
+                                                const float4 Vg) {
+    const bool pinned = Vg.w != 0.0f;
+    float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
+    if (!pinned) {
+        Fx += Xg.w * ip.gravity[0];
+        Fy += Xg.w * ip.gravity[1];
+        Fz += Xg.w * ip.gravity[2];
+    }
+    Fx += ip.damping * Vg.x;
+    Fy += ip.damping * Vg.y;
+    Fz += ip.damping * Vg.z;
+    if (pinned) return make_float3(Fx, Fy, Fz);
+    if (ip.has_ext) {
+        const float4 e = __ldg(a.fext + g);
+        Fx += e.x;
+        Fy += e.y;
+        Fz += e.z;
+    }
+    const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
+    for (int32_t k = k0; k < k1; k += B) {
+        int4 rec[B];
+        float4 Xo[B], Vo[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) rec[u] = (k + u < k1) ? __ldg(a.inc + k + u) : make_int4((int)g, 0, 0, 0);
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int32_t o = rec[u].x & 0x7fffffff;
+            Xo[u] = __ldg(a.X + o);
+            Vo[u] = __ldg(a.V + o);
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            if (k + u >= k1) break;
+            const float rest = __int_as_float(rec[u].y), ks = __int_as_float(rec[u].z), kd = __int_as_float(rec[u].w);
+            if (rec[u].x < 0) {  // F[p2] -= f, IMP:733
+                const float3 f = spring_force(Xo[u], Xg, Vo[u], Vg, rest, ks, kd);
+                Fx -= f.x;
+                Fy -= f.y;
+                Fz -= f.z;
+            } else {  // F[p1] += f, IMP:731
+                const float3 f = spring_force(Xg, Xo[u], Vg, Vo[u], rest, ks, kd);
+                Fx += f.x;
+                Fy += f.y;
+                Fz += f.z;
+            }
+        }
+    }
+    return make_float3(Fx, Fy, Fz);
+}
+
+// Assembly with one thread per vertex.
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_assemble_thread(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const InstParams& ip = a.inst[bi.inst];
+    double part = 0.0;
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
+        const OwnSpring os = load_own(a, g);
+        const float3 F = thread_gather<B>(a, ip, g, Xg, Vg);
+        part += assemble_vertex(a, g, Xg, Vg, F, os.ends, os.par, os.E1, os.E2, os.W1, os.W2);
+    }
+    finish<K_ASSEMBLE>(a, blk, bi.inst, true, part);
+}
+
+// Assembly with the block-cooperative gather (shared-memory staging).
+__global__ void __launch_bounds__(kThreads) k_assemble_coop(const StepArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     GatherSmem& sm = *reinterpret_cast<GatherSmem*>(smem_raw);
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstParams& ip = a.inst[bi.inst];
-    const float h = a.dt;
     double part = 0.0;
     for (int64_t c0 = bi.v_begin; c0 < bi.v_end; c0 += blockDim.x) {
         const int64_t g = c0 + threadIdx.x;
         float4 Xg, Vg;
+        const OwnSpring os = load_own(a, g < bi.v_end ? g : bi.v_begin);
         const float3 F = chunk_gather(a, ip, c0, min(c0 + (int64_t)blockDim.x, bi.v_end), sm, Xg, Vg);
         if (g >= bi.v_end) continue;
-        const bool pinned = Vg.w != 0.0f;
-
-        float J[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, Jv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        const int2 ends = __ldg(a.own_ends + g);
-        if (ends.x >= 0) {
-            const float4 par = __ldg(a.own_par + g);
-            SpringEval e;
-            spring_state(__ldg(a.X + ends.x), __ldg(a.X + ends.y), __ldg(a.V + ends.x), __ldg(a.V + ends.y), par.x,
-                         e);
-            jac_element(e, par.y, par.z, 0, 0, J[0], Jv[0]);
-            jac_element(e, par.y, par.z, 0, 1, J[1], Jv[1]);
-            jac_element(e, par.y, par.z, 0, 2, J[2], Jv[2]);
-            jac_element(e, par.y, par.z, 1, 1, J[3], Jv[3]);
-            jac_element(e, par.y, par.z, 1, 2, J[4], Jv[4]);
-            jac_element(e, par.y, par.z, 2, 2, J[5], Jv[5]);
-        }
-        // A = M - h (df_dv + h df_dx), b = h (F + (h df_dx)(V + y)), IMP:782-783.
-        float A[6], hJ[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            const float Mk = (k == 0 || k == 3 || k == 5) ? Xg.w : 0.0f;
-            A[k] = Mk - h * (Jv[k] + h * J[k]);
-            hJ[k] = h * J[k];
-        }
-        const float y = 0.0f;
-        const float vx = Vg.x + y, vy = Vg.y + y, vz = Vg.z + y;
-        float wx, wy, wz;
-        matvec(hJ, vx, vy, vz, wx, wy, wz);
-        const float bx = h * (F.x + wx), by = h * (F.y + wy), bz = h * (F.z + wz);
-
-        // CG set-up, IMP:310-318, with pinned rows filtered out.
-        float x0 = a.x[0][g], x1 = a.x[1][g], x2 = a.x[2][g];
-        if (pinned) {
-            x0 = x1 = x2 = 0.0f;
-            a.x[0][g] = 0.0f;
-            a.x[1][g] = 0.0f;
-            a.x[2][g] = 0.0f;
-        }
-        float ax, ay, az;
-        matvec(A, x0, x1, x2, ax, ay, az);
-        float r0 = bx - ax, r1 = by - ay, r2 = bz - az;
-        if (pinned) r0 = r1 = r2 = 0.0f;
-        const float pi0 = 1.0f / A[0], pi1 = 1.0f / A[3], pi2 = 1.0f / A[5];
-        const float d0 = pi0 * r0, d1 = pi1 * r1, d2 = pi2 * r2;
-        const float pr0 = A[0] * r0, pr1 = A[3] * r1, pr2 = A[5] * r2;
-        part += (double)(r0 * pr0 + r1 * pr1 + r2 * pr2);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) a.A[k][g] = A[k];
-        a.r[0][g] = r0;
-        a.r[1][g] = r1;
-        a.r[2][g] = r2;
-        a.d[0][g] = d0;
-        a.d[1][g] = d1;
-        a.d[2][g] = d2;
-        if (a.dbg_A9) {
-            float* o = a.dbg_A9 + 9 * g;
-            o[0] = A[0]; o[1] = A[1]; o[2] = A[2];
-            o[3] = A[1]; o[4] = A[3]; o[5] = A[4];
-            o[6] = A[2]; o[7] = A[4]; o[8] = A[5];
-        }
-        if (a.dbg_b) {
-            a.dbg_b[3 * g] = bx;
-            a.dbg_b[3 * g + 1] = by;
-            a.dbg_b[3 * g + 2] = bz;
-        }
+        part += assemble_vertex(a, g, Xg, Vg, F, os.ends, os.par, os.E1, os.E2, os.W1, os.W2);
     }
     finish<K_ASSEMBLE>(a, blk, bi.inst, true, part);
 }
@@ -505,16 +604,12 @@ __global__ void __launch_bounds__(kThreads) k_integrate(const StepArgs a) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_forces(const StepArgs a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    GatherSmem& sm = *reinterpret_cast<GatherSmem*>(smem_raw);
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstParams& ip = a.inst[bi.inst];
-    for (int64_t c0 = bi.v_begin; c0 < bi.v_end; c0 += blockDim.x) {
-        const int64_t g = c0 + threadIdx.x;
-        float4 Xg, Vg;
-        const float3 F = chunk_gather(a, ip, c0, min(c0 + (int64_t)blockDim.x, bi.v_end), sm, Xg, Vg);
-        if (g >= bi.v_end) continue;
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
+        const float3 F = thread_gather<1>(a, ip, g, Xg, Vg);
         a.dbg_F[3 * g] = F.x;
         a.dbg_F[3 * g + 1] = F.y;
         a.dbg_F[3 * g + 2] = F.z;
@@ -576,6 +671,19 @@ __global__ void k_state_out(const StepArgs a, float* X3, float* V3, float* dV3, 
     }
 }
 
+// Force-gather variant of k_assemble: 0 block-cooperative, 1/2/3 one thread per
+// vertex fetching 1/2/4 incidences ahead.
+int kGatherVariant = 3;
+
+const void* assemble_fn(int v) {
+    switch (v) {
+        case 0: return (const void*)k_assemble_coop;
+        case 1: return (const void*)k_assemble_thread<1>;
+        case 2: return (const void*)k_assemble_thread<2>;
+        default: return (const void*)k_assemble_thread<4>;
+    }
+}
+
 }  // namespace
 
 const char* kernel_name(KernelKind k) {
@@ -591,7 +699,7 @@ const char* kernel_name(KernelKind k) {
 
 const void* kernel_fn(KernelKind k) {
     switch (k) {
-        case K_ASSEMBLE: return (const void*)k_assemble;
+        case K_ASSEMBLE: return assemble_fn(kGatherVariant);
         case K_CG_DIR: return (const void*)k_cg_dir;
         case K_CG_UPDATE: return (const void*)k_cg_update;
         case K_INTEGRATE: return (const void*)k_integrate;
@@ -602,13 +710,12 @@ const void* kernel_fn(KernelKind k) {
 
 int kernel_block_threads() { return kThreads; }
 
-size_t kernel_smem_bytes(KernelKind k) { return (k == K_ASSEMBLE || k == K_FORCES) ? kGatherSmem : 0; }
+size_t kernel_smem_bytes(KernelKind k) { return (k == K_ASSEMBLE && kGatherVariant == 0) ? kGatherSmem : 0; }
 
-cudaError_t prepare_kernels() {
-    cudaError_t e = cudaFuncSetAttribute(k_assemble, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGatherSmem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_forces, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGatherSmem);
-    return e;
+cudaError_t prepare_kernels(int gather_variant) {
+    if (gather_variant < 0 || gather_variant > 3) return cudaErrorInvalidValue;
+    kGatherVariant = gather_variant;
+    return cudaFuncSetAttribute(k_assemble_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGatherSmem);
 }
 
 static int state_blocks(int64_t nv) {
@@ -630,11 +737,20 @@ cudaError_t launch_state_out(const StepArgs& a, float* X3, float* V3, float* dV3
 cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStream_t stream) {
     if (nblocks <= 0) return cudaSuccess;
     switch (k) {
-        case K_ASSEMBLE: k_assemble<<<nblocks, kThreads, kGatherSmem, stream>>>(a); break;
+        case K_ASSEMBLE:
+            if (kGatherVariant == 0)
+                k_assemble_coop<<<nblocks, kThreads, kGatherSmem, stream>>>(a);
+            else if (kGatherVariant == 1)
+                k_assemble_thread<1><<<nblocks, kThreads, 0, stream>>>(a);
+            else if (kGatherVariant == 2)
+                k_assemble_thread<2><<<nblocks, kThreads, 0, stream>>>(a);
+            else
+                k_assemble_thread<4><<<nblocks, kThreads, 0, stream>>>(a);
+            break;
         case K_CG_DIR: k_cg_dir<<<nblocks, kThreads, 0, stream>>>(a); break;
         case K_CG_UPDATE: k_cg_update<<<nblocks, kThreads, 0, stream>>>(a); break;
         case K_INTEGRATE: k_integrate<<<nblocks, kThreads, 0, stream>>>(a); break;
-        case K_FORCES: k_forces<<<nblocks, kThreads, kGatherSmem, stream>>>(a); break;
+        case K_FORCES: k_forces<<<nblocks, kThreads, 0, stream>>>(a); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
