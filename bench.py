@@ -110,7 +110,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
             time.sleep(0.3)
         except OSError:
             self.proc = None
@@ -222,36 +222,63 @@ def run_reference(args) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    descs, shapes, X, _ = WORKLOADS[args.workload](args.seed)
+    name = "grid1025" if args.workload == "all" else args.workload
+    descs, shapes, X, _ = WORKLOADS[name](args.seed)
     nv = sum(d.n_vertices for d in descs)
     procs = max(1, os.cpu_count() or 1)
     budget = min(120.0, 2.0 * max(args.steps, 1))
-    value, cores, kind, sample = cpu_throughput(args.workload, descs, shapes, X, budget, procs)
+    value, cores, kind, sample = cpu_throughput(name, descs, shapes, X, budget, procs)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * nv / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "vertices": nv, "instances": len(descs)},
+        "config": {"workload": name, "vertices": nv, "instances": len(descs)},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args) -> None:
+def _dominant_roofline(prof: dict, nv: int, ns: int, peak: float, workload: str) -> dict:
+    """Roofline of the kernel with the largest share of the step (CUDA-event durations)."""
+    dom = max(prof, key=lambda k: prof[k]["ms_total"])
+    n = max(prof[dom]["launches"], 1)
+    avg_s = prof[dom]["ms_total"] / 1e3 / n
+    if dom == "k_cg_dir":
+        first = prof["k_assemble"]["launches"]
+        per_launch = (first * algorithmic_bytes(dom, nv, ns, True)
+                      + (n - first) * algorithmic_bytes(dom, nv, ns, False)) / n
+    else:
+        per_launch = algorithmic_bytes(dom, nv, ns)
+    achieved = per_launch / avg_s / 1e9
+    traffic = None
+    tpath = ROOT / "profiles" / f"{dom}_{workload}.traffic.json"
+    if tpath.exists():
+        traffic = json.loads(tpath.read_text()).get("dram_bytes_per_launch")
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_launch": per_launch,
+            "avg_launch_us": avg_s * 1e6}
+
+
+def _cg_roofline(prof: dict, nv: int, ns: int, peak: float) -> dict:
+    """The two SpMV-bound CG passes together (bytes and time summed over their launches)."""
+    first = prof["k_assemble"]["launches"]
+    nd, nu = prof["k_cg_dir"]["launches"], prof["k_cg_update"]["launches"]
+    byts = (first * algorithmic_bytes("k_cg_dir", nv, ns, True) + (nd - first) * algorithmic_bytes("k_cg_dir", nv, ns)
+            + nu * algorithmic_bytes("k_cg_update", nv, ns))
+    secs = (prof["k_cg_dir"]["ms_total"] + prof["k_cg_update"]["ms_total"]) / 1e3
+    achieved = byts / secs / 1e9 if secs > 0 else 0.0
+    return {"bound": "hbm", "kernels": ["k_cg_dir", "k_cg_update"], "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak}
+
+
+def measure(name: str, args, steps: int, rank: int, world: int, local: int, plain_steps: int) -> dict:
+    """Time one workload on this rank; returns the figures rank 0 reports."""
     import torch
 
     from opencloth_gb300 import ClothSolver
-    from opencloth_gb300.build import build
 
-    rank, world, local = dist_env()
-    build()
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    descs, shapes, X0, V0 = WORKLOADS[args.workload](args.seed + 7919 * rank)
+    descs, shapes, X0, V0 = WORKLOADS[name](args.seed + 7919 * rank)
     nv = sum(d.n_vertices for d in descs)
     ns = sum(len(d.springs) for d in descs)
     stream = torch.cuda.Stream()
@@ -266,90 +293,123 @@ def run_ours(args) -> None:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    def max_over_ranks(v: float) -> float:
+        if world == 1:
+            return v
+        t = torch.tensor([v], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
     barrier()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
         ev0.record(stream)
-        solver.step(DT, args.steps)
+        solver.step(DT, steps)
         ev1.record(stream)
         ev1.synchronize()
     barrier()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1))
     launches = solver.launch_count() - l0
     iters, rr, flags = solver.stats()
-    value = nv * args.steps * world / (ms / 1e3)
+    value = nv * steps * world / (ms / 1e3)
 
-    # Per-kernel durations (CUDA events around each launch, same stream) for the roofline.
     prof = solver.profile(DT, 3)
-    dom = max(prof, key=lambda k: prof[k]["ms_total"])
-    launches_dom = prof[dom]["launches"]
-    avg_s = prof[dom]["ms_total"] / 1e3 / max(launches_dom, 1)
-    if dom == "k_cg_dir":
-        n_first = prof["k_assemble"]["launches"]
-        tot = (n_first * algorithmic_bytes(dom, nv, ns, True)
-               + (launches_dom - n_first) * algorithmic_bytes(dom, nv, ns, False))
-        per_launch = tot / max(launches_dom, 1)
-    else:
-        per_launch = algorithmic_bytes(dom, nv, ns)
-    achieved = per_launch / avg_s / 1e9
     peaks_path = ROOT / "MEASURED_PEAKS.json"
-    if peaks_path.exists():
-        peak, peak_src = float(json.loads(peaks_path.read_text())["hbm_gbs"]), "measured"
-    else:
-        peak, peak_src = 6800.0, "fallback"
-    traffic = None
-    tpath = ROOT / "profiles" / f"{dom}_{args.workload}.traffic.json"
-    if tpath.exists():
-        traffic = json.loads(tpath.read_text()).get("dram_bytes_per_launch")
+    peak = float(json.loads(peaks_path.read_text())["hbm_gbs"]) if peaks_path.exists() else 6800.0
+    roof = _dominant_roofline(prof, nv, ns, peak, name)
+    roof["peak_source"] = "measured" if peaks_path.exists() else "fallback"
+    cg_roof = _cg_roofline(prof, nv, ns, peak)
 
-    # End to end through the public API with host buffers: per step, pinned host X, V
-    # in, one step, X, V back out.
-    e2e_steps = max(5, min(args.steps, 50))
+    # End to end through the public API with host buffers: each step copies pinned
+    # host X, V in, runs the step and reads X, V back.
+    e2e_steps = max(5, min(steps, 50 if nv < 4_000_000 else 10))
     Xh = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True).numpy()
     Vh = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True).numpy()
     solver.get_state_into(Xh, Vh, None)
+    barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         solver.set_state(Xh, Vh)
         solver.step(DT, 1)
         solver.get_state_into(Xh, Vh, None)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = {"value": nv * e2e_steps * world / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 24 * nv,
            "d2h_bytes_per_step": 24 * nv, "steps": e2e_steps}
+    solver.close()
 
+    # The plain GPU step on the same inputs: the same kernels, one launch sequence per
+    # cloth, the CG loop driven from the host.
+    plain = ClothSolver(descs, device=local, stream=stream.cuda_stream, executor="plain")
+    plain.set_state(X0, V0)
+    plain.step(DT, 1)
+    plain.synchronize()
+    barrier()
+    ev0.record(stream)
+    plain.step(DT, plain_steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    pms = max_over_ranks(ev0.elapsed_time(ev1))
+    plain_value = nv * plain_steps * world / (pms / 1e3)
+    plain.close()
+
+    return {
+        "name": name, "descs": descs, "shapes": shapes, "X0": X0, "nv": nv, "ns": ns, "value": value,
+        "ms_per_step": ms / steps, "steps": steps, "launches": launches, "clocks": clocks.summary(),
+        "cg": {"iters_last_step_max": int(iters.max()), "iters_last_step_mean": float(iters.mean()),
+               "rel_residual_max": float(rr.max()), "flags_any": int(np.bitwise_or.reduce(flags))},
+        "roofline": roof, "cg_roofline": cg_roof, "e2e": e2e,
+        "kernels": {k: {"avg_us": 1e3 * v["ms_total"] / max(v["launches"], 1), "launches": v["launches"]}
+                    for k, v in prof.items()},
+        "plain_gpu": {"value": plain_value, "unit": METRIC, "ms_per_step": pms / plain_steps,
+                      "steps": plain_steps, "speedup": value / plain_value},
+    }
+
+
+def run_ours(args) -> None:
+    import torch
+
+    from opencloth_gb300.build import build
+
+    rank, world, local = dist_env()
+    build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    names = ["grid1025", "batch4096"] if args.workload == "all" else [args.workload]
+    results = []
+    for name in names:
+        steps = args.steps if name == names[0] else max(10, args.steps // 20)
+        plain_steps = 20 if name == "grid1025" else 2
+        results.append(measure(name, args, steps, rank, world, local, plain_steps))
     if rank == 0:
-        cpu_v, cores, kind, sample = cpu_throughput(args.workload, descs, shapes, X0, 12.0,
+        r = results[0]
+        cpu_v, cores, kind, sample = cpu_throughput(r["name"], r["descs"], r["shapes"], r["X0"], 12.0,
                                                     max(1, os.cpu_count() or 1))
         line = {
-            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": world, "steps": r["steps"],
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "vertices": nv, "springs": ns, "instances": len(descs),
-                       "dt": DT, "cg_max_iter": 200, "cg_tol": 1e-5, "parallelism": f"replicas x{world}",
+            "config": {"workload": r["name"], "vertices": r["nv"], "springs": r["ns"],
+                       "instances": len(r["descs"]), "dt": DT, "cg_max_iter": 200, "cg_tol": 1e-5,
+                       "parallelism": f"replicas x{world}",
                        "l2": "per-step working set larger than the 129 MB L2; no flush"},
-            "cg": {"iters_last_step_max": int(iters.max()), "iters_last_step_mean": float(iters.mean()),
-                   "rel_residual_max": float(rr.max()), "flags_any": int(np.bitwise_or.reduce(flags))},
-            "gpu_launches": int(launches),
-            "clocks": clocks.summary(),
-            "e2e": e2e,
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
-                         "algorithmic_bytes_per_launch": per_launch, "avg_launch_us": avg_s * 1e6},
-            "kernels": {k: {"avg_us": 1e3 * v["ms_total"] / max(v["launches"], 1), "launches": v["launches"]}
-                        for k, v in prof.items()},
+            "cg": r["cg"], "gpu_launches": int(r["launches"]), "clocks": r["clocks"], "e2e": r["e2e"],
+            "roofline": r["roofline"], "cg_roofline": r["cg_roofline"], "kernels": r["kernels"],
+            "plain_gpu": r["plain_gpu"],
             "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cores, "kind": kind, "sample": sample},
         }
+        for b in results[1:]:
+            line[b["name"]] = {
+                "value": b["value"], "unit": METRIC, "ms_per_step": b["ms_per_step"], "steps": b["steps"],
+                "vertices": b["nv"], "springs": b["ns"], "instances": len(b["descs"]), "cg": b["cg"],
+                "gpu_launches": int(b["launches"]), "clocks": b["clocks"], "e2e": b["e2e"],
+                "roofline": b["roofline"], "cg_roofline": b["cg_roofline"], "kernels": b["kernels"],
+                "plain_gpu": b["plain_gpu"],
+            }
         print(json.dumps(line), flush=True)
-    solver.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
@@ -357,10 +417,11 @@ def run_ours(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="grid1025")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["all"], default="all",
+                    help="all: the 1M-vertex cloth (headline value) and the 4096-cloth batch")
     ap.add_argument("--seed", type=int, default=20261203)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -672,8 +672,9 @@ __global__ void k_state_out(const StepArgs a, float* X3, float* V3, float* dV3, 
 }
 
 // Force-gather variant of k_assemble: 0 block-cooperative, 1/2/3 one thread per
-// vertex fetching 1/2/4 incidences ahead.
-int kGatherVariant = 3;
+// vertex fetching 1/2/4 incidences ahead.  Measured on GB300 (1025 x 1025 cloth and the
+// 4096-cloth batch): variant 1 is fastest; wider prefetch costs occupancy.
+int kGatherVariant = 1;
 
 const void* assemble_fn(int v) {
     switch (v) {
