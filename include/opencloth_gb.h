@@ -150,11 +150,15 @@ oc_status oc_compute_forces(oc_solver* s, float* F);
  * A as 9 floats per vertex (glm column-major) and b as float triples. */
 oc_status oc_assemble(oc_solver* s, float dt, float* A9, float* b);
 
-/* Per-kernel timing of n_steps un-graphed steps (CUDA events on the handle's stream).
- * names: up to max_kernels kernel names (each <= 31 chars + NUL, 32-byte slots);
- * ms_total / launches: per kernel.  Returns the number of kernels in *n_kernels. */
+/* Per-kernel timing of n_steps un-graphed steps (CUDA events around every launch on the
+ * handle's stream; the CG loop is driven from the host).  Per kernel: its name in a
+ * 32-byte slot of names (up to max_kernels), total ms, launches, and the algorithmic
+ * bytes it moved — each array element it must read or write counted once, for the
+ * instances still iterating: per vertex k_assemble 120 B + 32 B per spring, k_cg_dir
+ * 36 B on the first pass of a step and 60 B after, k_cg_update 84 B, k_integrate 76 B.
+ * *n_kernels receives the number of kernels reported. */
 oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_kernels, char* names,
-                           double* ms_total, int64_t* launches, int32_t* n_kernels);
+                           double* ms_total, int64_t* launches, double* algorithmic_bytes, int32_t* n_kernels);
 
 /* ---- reference topology builder (IMP:497-565) ------------------------------------ */
 /* Number of springs InitGL() creates for a cols x rows vertex grid (cols, rows >= 3):

@@ -90,7 +90,7 @@ SIGNATURES = {
     "oc_get_launch_count": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
     "oc_compute_forces": (C.c_int32, [_P, _P]),
     "oc_assemble": (C.c_int32, [_P, C.c_float, _P, _P]),
-    "oc_profile_steps": (C.c_int32, [_P, C.c_float, C.c_int32, C.c_int32, _P, _P, _P, _P]),
+    "oc_profile_steps": (C.c_int32, [_P, C.c_float, C.c_int32, C.c_int32, _P, _P, _P, _P, _P]),
     "oc_grid_spring_count": (C.c_int32, [C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
     "oc_grid_build": (C.c_int32, [C.c_int32, C.c_int32, C.c_float, _P, _P, C.c_float, C.c_uint64, _P, _P]),
 }

@@ -219,14 +219,15 @@ class ClothSolver:
         names = C.create_string_buffer(32 * 8)
         ms = np.zeros(8, np.float64)
         launches = np.zeros(8, np.int64)
+        byts = np.zeros(8, np.float64)
         n = C.c_int32()
         self._call(self._lib.oc_profile_steps(self._h, float(dt), int(n_steps), 8, names, ptr(ms), ptr(launches),
-                                              C.byref(n)))
+                                              ptr(byts), C.byref(n)))
         raw = names.raw
         out = {}
         for k in range(n.value):
             name = raw[32 * k: 32 * (k + 1)].split(b"\0", 1)[0].decode()
-            out[name] = {"ms_total": float(ms[k]), "launches": int(launches[k])}
+            out[name] = {"ms_total": float(ms[k]), "launches": int(launches[k]), "bytes": float(byts[k])}
         return out
 
 

@@ -29,6 +29,7 @@ struct oc_solver {
     int32_t vertices_per_block = 0;
     std::vector<int64_t> v_off;
     std::vector<InstParams> inst_host;
+    std::vector<int64_t> ns_inst;  // springs per instance
     std::vector<void*> allocs;
     StepArgs args{};
     float* stage = nullptr;         // device staging: 3 x 3 * nv floats
@@ -96,7 +97,26 @@ struct KernelTimer {
     cudaEvent_t ev[2] = {nullptr, nullptr};
     double ms[K_COUNT] = {0};
     int64_t launches[K_COUNT] = {0};
+    double bytes[K_COUNT] = {0};  // algorithmic bytes moved (active instances only)
 };
+
+// Algorithmic bytes of one step, from each instance's CG iteration count: every array
+// element a kernel must read or write counted once, in the device layout (X/V float4,
+// 16-byte incidence records, FP32 planes).  Per vertex: k_assemble 120 B plus 32 B per
+// spring, first k_cg_dir pass 36 B, later passes 60 B, k_cg_update 84 B, k_integrate 76 B.
+void account_step_bytes(const oc_solver* s, KernelTimer* t) {
+    for (int32_t k = 0; k < s->n_inst; ++k) {
+        const double nv = (double)s->inst_host[k].nv, ns = (double)s->ns_inst[k];
+        const InstState& st = s->h_state[k];
+        const double it = (double)st.iter;
+        t->bytes[K_ASSEMBLE] += 120.0 * nv + 32.0 * ns;
+        t->bytes[K_INTEGRATE] += 76.0 * nv;
+        t->bytes[K_CG_UPDATE] += 84.0 * nv * it;
+        double dirs = it > 0 ? 36.0 * nv + 60.0 * nv * (it - 1.0) : 0.0;
+        if (st.flags & OC_FLAG_BREAKDOWN) dirs += (it > 0 ? 60.0 : 36.0) * nv;
+        t->bytes[K_CG_DIR] += dirs;
+    }
+}
 
 oc_status launch_timed(oc_solver* s, KernelKind k, const StepArgs& a, int nblocks, KernelTimer* t) {
     if (t) OC_TRY(cudaEventRecord(t->ev[0], s->stream));
@@ -138,6 +158,12 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
             if ((st = launch_timed(s, K_CG_UPDATE, a, nb, t)) != OC_OK) return st;
         }
         if ((st = launch_timed(s, K_INTEGRATE, a, nb, t)) != OC_OK) return st;
+    }
+    if (t) {
+        OC_TRY(cudaMemcpyAsync(s->h_state, s->args.state, sizeof(InstState) * s->n_inst, cudaMemcpyDeviceToHost,
+                               s->stream));
+        OC_TRY(cudaStreamSynchronize(s->stream));
+        account_step_bytes(s, t);
     }
     return OC_OK;
 }
@@ -281,6 +307,8 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     s->ns = P.ns;
     s->v_off = P.v_off;
     s->inst_host = P.inst;
+    s->ns_inst.resize(P.n_inst);
+    for (int32_t k = 0; k < P.n_inst; ++k) s->ns_inst[k] = P.s_off[k + 1] - P.s_off[k];
     s->n_blocks = (int32_t)P.blocks.size();
     s->vertices_per_block = P.vertices_per_block;
     OC_CREATE_TRY(cudaSetDevice(o.device));
@@ -514,7 +542,7 @@ oc_status oc_assemble(oc_solver* s, float dt, float* A9, float* b) {
 }
 
 oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_kernels, char* names,
-                           double* ms_total, int64_t* launches, int32_t* n_kernels) {
+                           double* ms_total, int64_t* launches, double* algorithmic_bytes, int32_t* n_kernels) {
     if (!valid_solver(s) || n_steps < 0 || max_kernels < 0 || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
     OC_TRY(cudaSetDevice(s->device));
     KernelTimer t;
@@ -536,6 +564,7 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
         }
         if (ms_total) ms_total[n] = t.ms[k];
         if (launches) launches[n] = t.launches[k];
+        if (algorithmic_bytes) algorithmic_bytes[n] = t.bytes[k];
         ++n;
     }
     if (n_kernels) *n_kernels = n;
