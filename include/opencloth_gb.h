@@ -160,6 +160,26 @@ oc_status oc_assemble(oc_solver* s, float dt, float* A9, float* b);
 oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_kernels, char* names,
                            double* ms_total, int64_t* launches, double* algorithmic_bytes, int32_t* n_kernels);
 
+/* ---- allocation-free solve -------------------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device memory
+ * around a solve — an engine that manages a fixed device-memory budget itself, or a
+ * real-time frame loop where a cudaMalloc/cudaFree (which may synchronise the device)
+ * is not acceptable.  Runs the step's preconditioned CG (first iteration
+ * preconditioned, FP64 dot accumulation, pinned rows filtered out) on a block-diagonal
+ * system the caller assembled, such as the A and b that oc_assemble returns.
+ *   A9      device, 9 floats per vertex (glm column-major, symmetric)
+ *   b, x    device float triples; x holds the warm start on entry, the solution on return
+ *   pinned  device, one byte per vertex (non-zero = pinned), or NULL
+ *   stream  cudaStream_t, or NULL for the default stream; the call is synchronous
+ * Scratch is a fixed static device array sized for OC_NOALLOC_MAX_VERTICES vertices
+ * (about 3.8 MB, held by every GPU that loads the library until exit); larger systems
+ * return OC_ERR_UNSUPPORTED.  All calls on a device share that array: calls whose GPU
+ * work overlaps race.  The first call on a device looks up the array's address; make
+ * that call before any stream capture. */
+#define OC_NOALLOC_MAX_VERTICES 65536
+oc_status oc_pcg_solve_noalloc(const float* A9, const float* b, float* x, const uint8_t* pinned, int32_t n_vertices,
+                               int32_t cg_max_iter, float cg_tol, int32_t* cg_iters, uint32_t* flags, void* stream);
+
 /* ---- reference topology builder (IMP:497-565) ------------------------------------ */
 /* Number of springs InitGL() creates for a cols x rows vertex grid (cols, rows >= 3):
  * rows*(cols-1) + cols*(rows-1) + 2*(rows-1)*(cols-1) + rows*(cols-1) + cols*(rows-1),

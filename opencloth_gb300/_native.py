@@ -91,6 +91,8 @@ SIGNATURES = {
     "oc_compute_forces": (C.c_int32, [_P, _P]),
     "oc_assemble": (C.c_int32, [_P, C.c_float, _P, _P]),
     "oc_profile_steps": (C.c_int32, [_P, C.c_float, C.c_int32, C.c_int32, _P, _P, _P, _P, _P]),
+    "oc_pcg_solve_noalloc": (C.c_int32, [_P, _P, _P, _P, C.c_int32, C.c_int32, C.c_float, C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_uint32), _P]),
     "oc_grid_spring_count": (C.c_int32, [C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
     "oc_grid_build": (C.c_int32, [C.c_int32, C.c_int32, C.c_float, _P, _P, C.c_float, C.c_uint64, _P, _P]),
 }
