@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <tuple>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -30,6 +32,16 @@ struct oc_solver {
     std::vector<int64_t> v_off;
     std::vector<InstParams> inst_host;
     std::vector<int64_t> ns_inst;  // springs per instance
+    // Resident executor: cloths grouped by launch shape; the streamed kernels of a step
+    // run over the blocks of the remaining (streamed) cloths only.
+    struct Bucket {
+        int threads, cluster, vcta, n;
+        int32_t* d_ids;
+    };
+    std::vector<Bucket> buckets;
+    std::vector<uint8_t> resident;  // per instance
+    BlockInfo* d_streamed_blocks = nullptr;
+    int32_t n_streamed_blocks = 0;
     std::vector<void*> allocs;
     StepArgs args{};
     float* stage = nullptr;         // device staging: 3 x 3 * nv floats
@@ -108,6 +120,12 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
     for (int32_t k = 0; k < s->n_inst; ++k) {
         const double nv = (double)s->inst_host[k].nv, ns = (double)s->ns_inst[k];
         const InstState& st = s->h_state[k];
+        if (s->resident[k]) {
+            // Inputs X, V 32 + rowptr 4 + spring i 24 + warm start 12 and 32 B per spring;
+            // outputs X, V 32 + dV 12.  The CG runs in shared memory.
+            t->bytes[K_RESIDENT] += 116.0 * nv + 32.0 * ns;
+            continue;
+        }
         const double it = (double)st.iter;
         t->bytes[K_ASSEMBLE] += 120.0 * nv + 32.0 * ns;
         t->bytes[K_INTEGRATE] += 76.0 * nv;
@@ -132,16 +150,39 @@ oc_status launch_timed(oc_solver* s, KernelKind k, const StepArgs& a, int nblock
     return OC_OK;
 }
 
+oc_status launch_resident_all(oc_solver* s, const StepArgs& a, KernelTimer* t) {
+    for (const auto& b : s->buckets) {
+        if (t) OC_TRY(cudaEventRecord(t->ev[0], s->stream));
+        ResidentLaunch L{b.d_ids, b.cluster, b.vcta};
+        OC_TRY(launch_resident(a, L, b.threads, b.n, s->stream));
+        s->host_launches += 1;
+        if (t) {
+            OC_TRY(cudaEventRecord(t->ev[1], s->stream));
+            OC_TRY(cudaEventSynchronize(t->ev[1]));
+            float ms = 0.0f;
+            OC_TRY(cudaEventElapsedTime(&ms, t->ev[0], t->ev[1]));
+            t->ms[K_RESIDENT] += ms;
+            t->launches[K_RESIDENT] += 1;
+        }
+    }
+    return OC_OK;
+}
+
 oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* t) {
     StepArgs a = s->args;
     a.dt = dt;
     a.use_cond = 0;
     a.cond = 0;
     OC_TRY(cudaMemsetAsync(a.unconverged, 0, sizeof(int32_t), s->stream));
-    const int n_groups = per_cloth ? s->n_inst : 1;
+    if (!per_cloth) {
+        oc_status st = launch_resident_all(s, a, t);
+        if (st != OC_OK) return st;
+        a.blocks = s->d_streamed_blocks;
+    }
+    const int n_groups = per_cloth ? s->n_inst : (s->n_streamed_blocks > 0 ? 1 : 0);
     for (int grp = 0; grp < n_groups; ++grp) {
         a.blk_base = per_cloth ? s->inst_host[grp].blk0 : 0;
-        const int nb = per_cloth ? s->inst_host[grp].nblk : s->n_blocks;
+        const int nb = per_cloth ? s->inst_host[grp].nblk : s->n_streamed_blocks;
         oc_status st = launch_timed(s, K_ASSEMBLE, a, nb, t);
         if (st != OC_OK) return st;
         s->host_launches += 2;
@@ -188,11 +229,39 @@ oc_status build_graph(oc_solver* s, float dt) {
     a.blk_base = 0;
     a.use_cond = 1;
     a.cond = (unsigned long long)handle;
+    a.blocks = s->d_streamed_blocks;
+    if (!s->buckets.empty()) {
+        // The resident launches, captured into a child graph that runs beside the
+        // streamed part (the two touch disjoint cloths).
+        cudaGraph_t rg = nullptr;
+        OC_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        StepArgs ra = a;
+        ra.use_cond = 0;
+        for (const auto& b : s->buckets) {
+            ResidentLaunch L{b.d_ids, b.cluster, b.vcta};
+            cudaError_t e = launch_resident(ra, L, b.threads, b.n, s->stream);
+            if (e != cudaSuccess) {
+                cudaStreamEndCapture(s->stream, &rg);
+                if (rg) cudaGraphDestroy(rg);
+                return fail_cuda(s, e, "launch_resident (capture)");
+            }
+        }
+        OC_TRY(cudaStreamEndCapture(s->stream, &rg));
+        cudaGraphNode_t n_res;
+        cudaError_t e = cudaGraphAddChildGraphNode(&n_res, g, nullptr, 0, rg);
+        cudaGraphDestroy(rg);
+        if (e != cudaSuccess) return fail_cuda(s, e, "cudaGraphAddChildGraphNode");
+    }
+    if (s->n_streamed_blocks == 0) {
+        OC_TRY(cudaGraphInstantiate(&s->exec, g, 0));
+        s->graph_dt = dt;
+        return OC_OK;
+    }
     void* params[] = {&a};
     auto kparams = [&](KernelKind k) {
         cudaKernelNodeParams kp{};
         kp.func = const_cast<void*>(kernel_fn(k));
-        kp.gridDim = dim3((unsigned)s->n_blocks);
+        kp.gridDim = dim3((unsigned)s->n_streamed_blocks);
         kp.blockDim = dim3((unsigned)kernel_block_threads());
         kp.sharedMemBytes = (unsigned)kernel_smem_bytes(k);
         kp.kernelParams = params;
@@ -229,6 +298,36 @@ oc_status build_graph(oc_solver* s, float dt) {
     OC_TRY(cudaGraphInstantiate(&s->exec, g, 0));
     s->graph_dt = dt;
     return OC_OK;
+}
+
+// Launch shape of a resident cloth: up to 1024 vertices one CTA (vertex capacity the
+// next power of two, at least 128); beyond, clusters of CTAs of 1024 vertices each, up
+// to max_vertices and kResidentMaxCluster CTAs.
+constexpr int kResidentDefaultVcta = 1024;
+
+bool resident_shape(int nv, int max_vertices, int* threads, int* cluster, int* vcta) {
+    if (nv < 1 || nv > max_vertices) return false;
+    if (nv <= kResidentDefaultVcta) {
+        int v = 128;
+        while (v < nv) v <<= 1;
+        *cluster = 1;
+        *vcta = v;
+        *threads = v < 256 ? v : 256;
+        return true;
+    }
+    const int c = (nv + kResidentDefaultVcta - 1) / kResidentDefaultVcta;
+    if (c > kResidentMaxCluster) {
+        const int c2 = (nv + kResidentMaxVcta - 1) / kResidentMaxVcta;
+        if (c2 > kResidentMaxCluster) return false;
+        *cluster = c2;
+        *vcta = kResidentMaxVcta;
+        *threads = 512;
+        return true;
+    }
+    *cluster = c;
+    *vcta = kResidentDefaultVcta;
+    *threads = 256;
+    return true;
 }
 
 bool valid_solver(const oc_solver* s) { return s != nullptr && s->nv > 0; }
@@ -270,7 +369,6 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     oc_default_options(&o);
     if (opts) o = *opts;
     if (o.executor < OC_EXEC_AUTO || o.executor > OC_EXEC_PLAIN) return OC_ERR_INVALID_ARGUMENT;
-    if (o.executor == OC_EXEC_RESIDENT) return OC_ERR_UNSUPPORTED;
     if (o.vertices_per_thread < 0 || o.vertices_per_thread > 64 || o.block_threads < 0) return OC_ERR_INVALID_ARGUMENT;
     if (o.block_threads != 0 && o.block_threads != kernel_block_threads()) return OC_ERR_UNSUPPORTED;
 
@@ -300,7 +398,7 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     } while (0)
 
     s->device = o.device;
-    s->executor = (o.executor == OC_EXEC_PLAIN) ? OC_EXEC_PLAIN : OC_EXEC_STREAMED;
+    s->executor = o.executor;
     s->use_graph = o.use_graph != 0;
     s->n_inst = P.n_inst;
     s->nv = P.nv;
@@ -361,6 +459,44 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     BlockInfo* blocks = nullptr;
     OC_CREATE_TRY(upload(s, &blocks, P.blocks));
     a.blocks = blocks;
+
+    // Which cloths run resident (one cluster per cloth, the whole step on chip) and
+    // which run streamed; resident cloths are grouped by launch shape.
+    {
+        const int max_res = o.resident_max_vertices > 0 ? o.resident_max_vertices
+                                                        : kResidentMaxCluster * kResidentDefaultVcta;
+        s->resident.assign(P.n_inst, 0);
+        std::vector<BlockInfo> streamed;
+        std::map<std::tuple<int, int, int>, std::vector<int32_t>> groups;
+        for (int32_t k = 0; k < P.n_inst; ++k) {
+            int threads = 0, cluster = 0, vcta = 0;
+            const bool want = (s->executor == OC_EXEC_RESIDENT || s->executor == OC_EXEC_AUTO) &&
+                              resident_shape(P.inst[k].nv, max_res, &threads, &cluster, &vcta);
+            if (s->executor == OC_EXEC_RESIDENT && !want) {
+                s->err = "instance " + std::to_string(k) + " (" + std::to_string(P.inst[k].nv) +
+                         " vertices) is too large for the resident executor";
+                return bail(OC_ERR_UNSUPPORTED);
+            }
+            if (want) {
+                s->resident[k] = 1;
+                groups[std::make_tuple(threads, cluster, vcta)].push_back(k);
+            } else {
+                for (int32_t b = 0; b < P.inst[k].nblk; ++b) streamed.push_back(P.blocks[P.inst[k].blk0 + b]);
+            }
+        }
+        for (auto& kv : groups) {
+            oc_solver::Bucket b;
+            b.threads = std::get<0>(kv.first);
+            b.cluster = std::get<1>(kv.first);
+            b.vcta = std::get<2>(kv.first);
+            b.n = (int)kv.second.size();
+            OC_CREATE_TRY(upload(s, &b.d_ids, kv.second));
+            s->buckets.push_back(b);
+        }
+        s->n_streamed_blocks = (int32_t)streamed.size();
+        OC_CREATE_TRY(upload(s, &s->d_streamed_blocks, streamed));
+        if (!s->buckets.empty()) OC_CREATE_TRY(prepare_resident());
+    }
     OC_CREATE_TRY(dalloc(s, &a.unconverged, 1));
     OC_CREATE_TRY(dalloc(s, &a.grid_ticket, 1));
     OC_CREATE_TRY(dalloc(s, &a.loop_count, 1));
@@ -470,7 +606,7 @@ oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
         if (st != OC_OK) return st;
     }
     for (int32_t i = 0; i < n_steps; ++i) OC_TRY(cudaGraphLaunch(s->exec, s->stream));
-    s->host_launches += 2 * (int64_t)n_steps;
+    s->host_launches += ((s->n_streamed_blocks > 0 ? 2 : 0) + (int64_t)s->buckets.size()) * (int64_t)n_steps;
     return OC_OK;
 }
 
@@ -554,7 +690,7 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
     cudaEventDestroy(t.ev[0]);
     cudaEventDestroy(t.ev[1]);
     if (st != OC_OK) return st;
-    const KernelKind kinds[] = {K_ASSEMBLE, K_CG_DIR, K_CG_UPDATE, K_INTEGRATE};
+    const KernelKind kinds[] = {K_ASSEMBLE, K_CG_DIR, K_CG_UPDATE, K_INTEGRATE, K_RESIDENT};
     int32_t n = 0;
     for (KernelKind k : kinds) {
         if (n >= max_kernels) break;

@@ -40,8 +40,8 @@ struct InstState {
 // One streamed block: a contiguous vertex range of one instance.
 struct BlockInfo {
     int32_t inst;
-    int32_t local_blk;  // index of this block within its instance
-    int64_t v_begin;    // global vertex range [v_begin, v_end)
+    int32_t gblk;     // index of this block in the handle's full block table (partials slot)
+    int64_t v_begin;  // global vertex range [v_begin, v_end)
     int64_t v_end;
 };
 
@@ -75,7 +75,8 @@ struct StepArgs {
     float* dbg_b;
 };
 
-enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3, K_FORCES = 4, K_COUNT = 5 };
+enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3, K_FORCES = 4, K_RESIDENT = 5,
+                  K_COUNT = 6 };
 
 const char* kernel_name(KernelKind k);
 const void* kernel_fn(KernelKind k);
@@ -87,6 +88,20 @@ cudaError_t prepare_kernels(int gather_variant);
 
 // Host-side launch of one kernel kind over [blk_base, blk_base + nblocks).
 cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStream_t stream);
+
+// Resident executor (oc_resident.cu): one launch runs whole steps for n_clusters cloths,
+// cluster CTAs of `threads` threads per cloth, at most vcta vertices per CTA.
+struct ResidentLaunch {
+    const int32_t* inst_ids;  // the cloth of each cluster
+    int32_t cluster;
+    int32_t vcta;
+};
+constexpr int kResidentMaxVcta = 2048;
+constexpr int kResidentMaxCluster = 16;
+size_t resident_smem_bytes(int vcta);
+cudaError_t prepare_resident();  // function attributes (once per device)
+cudaError_t launch_resident(const StepArgs& a, const ResidentLaunch& L, int threads, int n_clusters,
+                            cudaStream_t stream);
 
 cudaError_t launch_state_in(const StepArgs& a, const float* X3, const float* V3, const float* dV3, int64_t nv,
                             int32_t* err, cudaStream_t stream);

@@ -18,66 +18,13 @@
 // CUDA-graph WHILE condition to "some instance still iterating".
 #include <cuda_runtime.h>
 
+#include "oc_device.cuh"
 #include "oc_internal.h"
 
 namespace oc {
 namespace {
 
 constexpr int kThreads = 256;
-
-struct SpringEval {
-    float C, Cdot;
-    float n[3];  // dc_dp
-    float q[3];  // deltaP2
-};
-
-// Spring force on p1, IMP:717-728 (glm length / normalize rounding order).
-__device__ __forceinline__ float3 spring_force(const float4 p1, const float4 p2, const float4 v1, const float4 v2,
-                                               float rest, float ks, float kd) {
-    const float dPx = p1.x - p2.x, dPy = p1.y - p2.y, dPz = p1.z - p2.z;
-    const float dVx = v1.x - v2.x, dVy = v1.y - v2.y, dVz = v1.z - v2.z;
-    const float sqr = dPx * dPx + dPy * dPy + dPz * dPz;
-    const float dist = sqrtf(sqr);
-    const float left = (-ks) * (dist - rest);
-    const float right = kd * ((dVx * dPx + dVy * dPy + dVz * dPz) / dist);
-    const float inv = 1.0f / sqrtf(sqr);
-    const float mag = left + right;
-    return make_float3(mag * (dPx * inv), mag * (dPy * inv), mag * (dPz * inv));
-}
-
-// The per-spring quantities CalcForceDerivatives reads, IMP:719-724.
-__device__ __forceinline__ void spring_state(const float4 p1, const float4 p2, const float4 v1, const float4 v2,
-                                             float rest, SpringEval& e) {
-    const float dPx = p1.x - p2.x, dPy = p1.y - p2.y, dPz = p1.z - p2.z;
-    const float sqr = dPx * dPx + dPy * dPy + dPz * dPz;
-    const float dist = sqrtf(sqr);
-    e.C = dist - rest;
-    e.n[0] = dPx / dist;
-    e.n[1] = dPy / dist;
-    e.n[2] = dPz / dist;
-    e.Cdot = (v1.x * (-e.n[0]) + v1.y * (-e.n[1]) + v1.z * (-e.n[2])) +
-             (v2.x * e.n[0] + v2.y * e.n[1] + v2.z * e.n[2]);
-    e.q[0] = dPx * dPx;
-    e.q[1] = dPy * dPy;
-    e.q[2] = dPz * dPz;
-}
-
-// One element m[c][r] of df_dx and df_dv for one spring, IMP:744-770.  d2C_dp2 has
-// zeros off the diagonal (identity initialisation, IMP:744).
-__device__ __forceinline__ void jac_element(const SpringEval& e, float ks, float kd, int c, int r, float& j,
-                                            float& jv) {
-    const float zero = 0.0f;
-    const float d00 = (c == r) ? ((-e.C) * e.q[c] + e.C) : zero;
-    const float d01 = (c == r) ? (e.C * e.q[c] - e.C) : zero;
-    const float dp1 = e.n[r] * e.n[c];
-    const float dp2 = e.n[r] * (-e.n[c]);
-    const float dp3 = (-e.n[r]) * (-e.n[c]);
-    const float t1 = (-ks) * (dp1 + d00 * e.C) - kd * (d00 * e.Cdot);
-    const float t2 = (-ks) * (dp2 + d01 * e.C) - kd * (d01 * e.Cdot);
-    const float t3 = (-ks) * (dp2 + d00 * e.C) - kd * (d00 * e.Cdot);
-    j = ((zero + t1) + t2) + t3;
-    jv = ((zero + (-kd) * dp1) + (-kd) * dp2) + (-kd) * dp3;
-}
 
 // Shared-memory staging of one chunk (blockDim consecutive vertices of a block) for
 // the cooperative force gather.
@@ -171,28 +118,6 @@ __device__ float3 chunk_gather(const StepArgs& a, const InstParams& ip, int64_t 
     return make_float3(Fx, Fy, Fz);
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Fixed-order block sum; the result is valid in thread 0.
-__device__ double block_sum(double v) {
-    __shared__ double warp_part[32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    v = warp_sum(v);
-    __syncthreads();
-    if (lane == 0) warp_part[w] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (w == 0) {
-        t = (lane < (int)(blockDim.x >> 5)) ? warp_part[lane] : 0.0;
-        t = warp_sum(t);
-    }
-    return t;
-}
-
 // Last-block epilogue shared by the reducing kernels.
 template <int KIND>
 __device__ void finish(const StepArgs& a, int blk, int inst, bool participates, double part) {
@@ -272,158 +197,39 @@ __device__ void finish(const StepArgs& a, int blk, int inst, bool participates, 
     }
 }
 
-__device__ __forceinline__ void matvec(const float A[6], float x0, float x1, float x2, float& y0, float& y1,
-                                       float& y2) {
-    // glm mat3 * vec3 (GLM/core/type_mat3x3.inl:511-518) on a symmetric matrix.
-    y0 = A[0] * x0 + A[1] * x1 + A[2] * x2;
-    y1 = A[1] * x0 + A[3] * x1 + A[4] * x2;
-    y2 = A[2] * x0 + A[4] * x1 + A[5] * x2;
-}
-
-// Per-vertex part of the assembly after the force gather: Jacobians of spring i
-// (CalcForceDerivatives, IMP:744-770), A_i and b_i (IMP:782-783), and the CG set-up
-// r = b - A x, d = P^-1 r, r.(P r) (IMP:310-318) with pinned rows filtered out.
-// Returns the vertex's FP32 term of delta0.
+// Per-vertex part of the assembly after the force gather: the vertex's system and CG
+// set-up (pinned rows filtered out), stored to the SoA planes.  Returns the vertex's
+// term of delta0.
 __device__ __forceinline__ double assemble_vertex(const StepArgs& a, int64_t g, const float4 Xg, const float4 Vg,
-                                                  const float3 F, const int2 ends, const float4 par,
-                                                  const float4 E1, const float4 E2, const float4 W1,
-                                                  const float4 W2) {
-    const float h = a.dt;
+                                                  const float3 F, const OwnSpring& os) {
     const bool pinned = Vg.w != 0.0f;
-    float J[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, Jv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (ends.x >= 0) {
-        SpringEval e;
-        spring_state(E1, E2, W1, W2, par.x, e);
-        jac_element(e, par.y, par.z, 0, 0, J[0], Jv[0]);
-        jac_element(e, par.y, par.z, 0, 1, J[1], Jv[1]);
-        jac_element(e, par.y, par.z, 0, 2, J[2], Jv[2]);
-        jac_element(e, par.y, par.z, 1, 1, J[3], Jv[3]);
-        jac_element(e, par.y, par.z, 1, 2, J[4], Jv[4]);
-        jac_element(e, par.y, par.z, 2, 2, J[5], Jv[5]);
-    }
-    // A = M - h (df_dv + h df_dx), b = h (F + (h df_dx)(V + y)), IMP:782-783.
-    float A[6], hJ[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        const float Mk = (k == 0 || k == 3 || k == 5) ? Xg.w : 0.0f;
-        A[k] = Mk - h * (Jv[k] + h * J[k]);
-        hJ[k] = h * J[k];
-    }
-    const float y = 0.0f;
-    const float vx = Vg.x + y, vy = Vg.y + y, vz = Vg.z + y;
-    float wx, wy, wz;
-    matvec(hJ, vx, vy, vz, wx, wy, wz);
-    const float bx = h * (F.x + wx), by = h * (F.y + wy), bz = h * (F.z + wz);
-
-    float x0 = a.x[0][g], x1 = a.x[1][g], x2 = a.x[2][g];
+    const VertexSystem sys = vertex_system(a.dt, Xg, Vg, F, os);
+    const CgInit c = cg_init(sys, a.x[0][g], a.x[1][g], a.x[2][g], pinned);
     if (pinned) {
-        x0 = x1 = x2 = 0.0f;
         a.x[0][g] = 0.0f;
         a.x[1][g] = 0.0f;
         a.x[2][g] = 0.0f;
     }
-    float ax, ay, az;
-    matvec(A, x0, x1, x2, ax, ay, az);
-    float r0 = bx - ax, r1 = by - ay, r2 = bz - az;
-    if (pinned) r0 = r1 = r2 = 0.0f;
-    const float pi0 = 1.0f / A[0], pi1 = 1.0f / A[3], pi2 = 1.0f / A[5];
-    const float d0 = pi0 * r0, d1 = pi1 * r1, d2 = pi2 * r2;
-    const float pr0 = A[0] * r0, pr1 = A[3] * r1, pr2 = A[5] * r2;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) a.A[k][g] = A[k];
-    a.r[0][g] = r0;
-    a.r[1][g] = r1;
-    a.r[2][g] = r2;
-    a.d[0][g] = d0;
-    a.d[1][g] = d1;
-    a.d[2][g] = d2;
+    for (int k = 0; k < 6; ++k) a.A[k][g] = sys.A[k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        a.r[k][g] = c.r[k];
+        a.d[k][g] = c.d[k];
+    }
     if (a.dbg_A9) {
+        const float* A = sys.A;
         float* o = a.dbg_A9 + 9 * g;
         o[0] = A[0]; o[1] = A[1]; o[2] = A[2];
         o[3] = A[1]; o[4] = A[3]; o[5] = A[4];
         o[6] = A[2]; o[7] = A[4]; o[8] = A[5];
     }
     if (a.dbg_b) {
-        a.dbg_b[3 * g] = bx;
-        a.dbg_b[3 * g + 1] = by;
-        a.dbg_b[3 * g + 2] = bz;
+        a.dbg_b[3 * g] = sys.b[0];
+        a.dbg_b[3 * g + 1] = sys.b[1];
+        a.dbg_b[3 * g + 2] = sys.b[2];
     }
-    return (double)(r0 * pr0 + r1 * pr1 + r2 * pr2);
-}
-
-struct OwnSpring {
-    int2 ends;
-    float4 par, E1, E2, W1, W2;
-};
-
-// Spring i's record and endpoint states for vertex i (loaded early to overlap).
-__device__ __forceinline__ OwnSpring load_own(const StepArgs& a, int64_t g) {
-    OwnSpring o;
-    o.ends = __ldg(a.own_ends + g);
-    o.par = make_float4(0.f, 0.f, 0.f, 0.f);
-    o.E1 = o.E2 = o.W1 = o.W2 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (o.ends.x >= 0) {
-        o.par = __ldg(a.own_par + g);
-        o.E1 = __ldg(a.X + o.ends.x);
-        o.E2 = __ldg(a.X + o.ends.y);
-        o.W1 = __ldg(a.V + o.ends.x);
-        o.W2 = __ldg(a.V + o.ends.y);
-    }
-    return o;
-}
-
-// F_i gathered by the vertex's own thread: B incidence records and their neighbour
-// states are fetched ahead of use, then added in spring-id order (IMP:701-734).
-template <int B>
-__device__ __forceinline__ float3 thread_gather(const StepArgs& a, const InstParams& ip, int64_t g, const float4 Xg,
-                                                const float4 Vg) {
-    const bool pinned = Vg.w != 0.0f;
-    float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
-    if (!pinned) {
-        Fx += Xg.w * ip.gravity[0];
-        Fy += Xg.w * ip.gravity[1];
-        Fz += Xg.w * ip.gravity[2];
-    }
-    Fx += ip.damping * Vg.x;
-    Fy += ip.damping * Vg.y;
-    Fz += ip.damping * Vg.z;
-    if (pinned) return make_float3(Fx, Fy, Fz);
-    if (ip.has_ext) {
-        const float4 e = __ldg(a.fext + g);
-        Fx += e.x;
-        Fy += e.y;
-        Fz += e.z;
-    }
-    const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
-    for (int32_t k = k0; k < k1; k += B) {
-        int4 rec[B];
-        float4 Xo[B], Vo[B];
-#pragma unroll
-        for (int u = 0; u < B; ++u) rec[u] = (k + u < k1) ? __ldg(a.inc + k + u) : make_int4((int)g, 0, 0, 0);
-#pragma unroll
-        for (int u = 0; u < B; ++u) {
-            const int32_t o = rec[u].x & 0x7fffffff;
-            Xo[u] = __ldg(a.X + o);
-            Vo[u] = __ldg(a.V + o);
-        }
-#pragma unroll
-        for (int u = 0; u < B; ++u) {
-            if (k + u >= k1) break;
-            const float rest = __int_as_float(rec[u].y), ks = __int_as_float(rec[u].z), kd = __int_as_float(rec[u].w);
-            if (rec[u].x < 0) {  // F[p2] -= f, IMP:733
-                const float3 f = spring_force(Xo[u], Xg, Vo[u], Vg, rest, ks, kd);
-                Fx -= f.x;
-                Fy -= f.y;
-                Fz -= f.z;
-            } else {  // F[p1] += f, IMP:731
-                const float3 f = spring_force(Xg, Xo[u], Vg, Vo[u], rest, ks, kd);
-                Fx += f.x;
-                Fy += f.y;
-                Fz += f.z;
-            }
-        }
-    }
-    return make_float3(Fx, Fy, Fz);
+    return (double)c.term;
 }
 
 // Assembly with one thread per vertex.
@@ -437,9 +243,9 @@ __global__ void __launch_bounds__(kThreads) k_assemble_thread(const StepArgs a) 
         const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
         const OwnSpring os = load_own(a, g);
         const float3 F = thread_gather<B>(a, ip, g, Xg, Vg);
-        part += assemble_vertex(a, g, Xg, Vg, F, os.ends, os.par, os.E1, os.E2, os.W1, os.W2);
+        part += assemble_vertex(a, g, Xg, Vg, F, os);
     }
-    finish<K_ASSEMBLE>(a, blk, bi.inst, true, part);
+    finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
 }
 
 // Assembly with the block-cooperative gather (shared-memory staging).
@@ -456,9 +262,9 @@ __global__ void __launch_bounds__(kThreads) k_assemble_coop(const StepArgs a) {
         const OwnSpring os = load_own(a, g < bi.v_end ? g : bi.v_begin);
         const float3 F = chunk_gather(a, ip, c0, min(c0 + (int64_t)blockDim.x, bi.v_end), sm, Xg, Vg);
         if (g >= bi.v_end) continue;
-        part += assemble_vertex(a, g, Xg, Vg, F, os.ends, os.par, os.E1, os.E2, os.W1, os.W2);
+        part += assemble_vertex(a, g, Xg, Vg, F, os);
     }
-    finish<K_ASSEMBLE>(a, blk, bi.inst, true, part);
+    finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
 }
 
 // The CG passes stream fifteen FP32 planes.  Each thread keeps two vertices' loads in
@@ -522,7 +328,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_dir(const StepArgs a) {
             }
         }
     }
-    finish<K_CG_DIR>(a, blk, bi.inst, active, part);
+    finish<K_CG_DIR>(a, bi.gblk, bi.inst, active, part);
 }
 
 __global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
@@ -582,7 +388,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
             }
         }
     }
-    finish<K_CG_UPDATE>(a, blk, bi.inst, active, part);
+    finish<K_CG_UPDATE>(a, bi.gblk, bi.inst, active, part);
 }
 
 __global__ void __launch_bounds__(kThreads) k_integrate(const StepArgs a) {
@@ -694,6 +500,7 @@ const char* kernel_name(KernelKind k) {
         case K_CG_UPDATE: return "k_cg_update";
         case K_INTEGRATE: return "k_integrate";
         case K_FORCES: return "k_forces";
+        case K_RESIDENT: return "k_resident";
         default: return "?";
     }
 }

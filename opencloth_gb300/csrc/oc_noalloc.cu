@@ -200,7 +200,7 @@ extern "C" oc_status oc_pcg_solve_noalloc(const float* A9, const float* b, float
     BlockInfo blocks[kNaMaxBlocks];
     for (int k = 0; k < nblk; ++k) {
         blocks[k].inst = 0;
-        blocks[k].local_blk = k;
+        blocks[k].gblk = k;
         blocks[k].v_begin = (int64_t)k * kNaVertsPerBlock;
         blocks[k].v_end = std::min<int64_t>(n_vertices, (int64_t)(k + 1) * kNaVertsPerBlock);
     }

@@ -1,0 +1,238 @@
+// Resident executor: one cluster of CTAs per cloth runs the whole implicit step in one
+// launch — force gather, Jacobians and assembly (IMP:698-786), the complete
+// preconditioned CG to the cloth's own tolerance (IMP:308-330), and the update
+// (IMP:790-797).  The CG state (A, x, r, d: 60 B per vertex) lives in shared memory,
+// so the CG loop touches no HBM.  Dot products reduce per CTA in FP64, then across
+// the cluster through distributed shared memory after a hardware cluster barrier; every
+// CTA sums the CTAs' partials in rank order, so all of them take identical
+// decisions.  There are no spin-waits.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "oc_device.cuh"
+#include "oc_internal.h"
+
+namespace cgx = cooperative_groups;
+
+namespace oc {
+namespace {
+
+// FP64 sum over the CTA, then over the cluster (C CTAs), identical in every CTA.
+// slots[2] (double-buffered per call) and bcast live in shared memory.
+__device__ double cluster_sum(double part, int C, double* slots, double* bcast, int& phase) {
+    const double bs = block_sum(part);
+    if (C == 1) {
+        if (threadIdx.x == 0) *bcast = bs;
+        __syncthreads();
+        return *bcast;
+    }
+    cgx::cluster_group cl = cgx::this_cluster();
+    double* slot = slots + (phase & 1);
+    ++phase;
+    if (threadIdx.x == 0) *slot = bs;
+    cl.sync();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int r = 0; r < C; ++r) t += *cl.map_shared_rank(slot, r);
+        *bcast = t;
+    }
+    __syncthreads();
+    return *bcast;
+}
+
+template <int T>
+__global__ void __launch_bounds__(T) k_resident(const StepArgs a, const ResidentLaunch L) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ double slots[2];
+    __shared__ double bcast;
+    const int C = L.cluster;
+    const int rank = (C > 1) ? (int)cgx::this_cluster().block_rank() : 0;
+    const int inst = L.inst_ids[blockIdx.x / C];
+    const InstParams& ip = a.inst[inst];
+    const int chunk = (ip.nv + C - 1) / C;
+    const int lb = rank * chunk;
+    const int n_local = max(0, min(ip.nv, lb + chunk) - lb);
+    const int64_t base = ip.v_off + lb;
+    const int cap = L.vcta;
+    float* sA[6];
+    float* sx[3];
+    float* sr[3];
+    float* sd[3];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) sA[k] = smem + k * cap;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        sx[k] = smem + (6 + k) * cap;
+        sr[k] = smem + (9 + k) * cap;
+        sd[k] = smem + (12 + k) * cap;
+    }
+
+    // Assembly and CG set-up.
+    double part = 0.0;
+    for (int j = threadIdx.x; j < n_local; j += T) {
+        const int64_t g = base + j;
+        const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
+        const OwnSpring os = load_own(a, g);
+        const float3 F = thread_gather<1>(a, ip, g, Xg, Vg);
+        const VertexSystem sys = vertex_system(a.dt, Xg, Vg, F, os);
+        const CgInit c = cg_init(sys, a.x[0][g], a.x[1][g], a.x[2][g], Vg.w != 0.0f);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) sA[k][j] = sys.A[k];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            sx[k][j] = c.x[k];
+            sr[k][j] = c.r[k];
+            sd[k][j] = c.d[k];
+        }
+        part += (double)c.term;
+    }
+    int phase = 0;
+    const double delta0 = cluster_sum(part, C, slots, &bcast, phase);
+    double delta = delta0;
+    const double thresh = (double)ip.eps2 * delta0;
+    uint32_t flags = 0u;
+    int it = 0;
+    bool run = (0 < ip.imax) && (delta0 > thresh);
+    if (!isfinite(delta0)) {
+        flags |= OC_FLAG_NON_FINITE;
+        run = false;
+    }
+    float beta = 0.0f;
+    while (run) {
+        // d = r + beta d (after the first iteration), d.(A d), IMP:320-321, 327.
+        part = 0.0;
+        for (int j = threadIdx.x; j < n_local; j += T) {
+            float d0 = sd[0][j], d1 = sd[1][j], d2 = sd[2][j];
+            if (it > 0) {
+                d0 = sr[0][j] + d0 * beta;
+                d1 = sr[1][j] + d1 * beta;
+                d2 = sr[2][j] + d2 * beta;
+                sd[0][j] = d0;
+                sd[1][j] = d1;
+                sd[2][j] = d2;
+            }
+            const float A[6] = {sA[0][j], sA[1][j], sA[2][j], sA[3][j], sA[4][j], sA[5][j]};
+            float q0, q1, q2;
+            matvec(A, d0, d1, d2, q0, q1, q2);
+            part += (double)(d0 * q0 + d1 * q1 + d2 * q2);
+        }
+        const double dq = cluster_sum(part, C, slots, &bcast, phase);
+        if (!(dq > 0.0) || !isfinite(dq)) {
+            flags |= isfinite(dq) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
+            break;
+        }
+        const float alpha = (float)(delta / dq);
+        // x += alpha d; r -= alpha A d; r.r, IMP:322-325.
+        part = 0.0;
+        for (int j = threadIdx.x; j < n_local; j += T) {
+            const float d0 = sd[0][j], d1 = sd[1][j], d2 = sd[2][j];
+            const float A[6] = {sA[0][j], sA[1][j], sA[2][j], sA[3][j], sA[4][j], sA[5][j]};
+            float q0, q1, q2;
+            matvec(A, d0, d1, d2, q0, q1, q2);
+            sx[0][j] = sx[0][j] + d0 * alpha;
+            sx[1][j] = sx[1][j] + d1 * alpha;
+            sx[2][j] = sx[2][j] + d2 * alpha;
+            const float r0 = sr[0][j] - q0 * alpha;
+            const float r1 = sr[1][j] - q1 * alpha;
+            const float r2 = sr[2][j] - q2 * alpha;
+            sr[0][j] = r0;
+            sr[1][j] = r1;
+            sr[2][j] = r2;
+            part += (double)(r0 * r0 + r1 * r1 + r2 * r2);
+        }
+        const double old = delta;
+        delta = cluster_sum(part, C, slots, &bcast, phase);
+        beta = (float)(delta / old);
+        ++it;
+        if (!isfinite(delta)) {
+            flags |= OC_FLAG_NON_FINITE;
+            break;
+        }
+        if (!(it < ip.imax && delta > thresh)) {
+            if (delta > thresh) flags |= OC_FLAG_NOT_CONVERGED;
+            break;
+        }
+    }
+    // V += dV dt; X += dt V; ground clamp (IMP:790-797); dV stays as the warm start.
+    const float dt = a.dt;
+    __syncthreads();
+    for (int j = threadIdx.x; j < n_local; j += T) {
+        const int64_t g = base + j;
+        float4 Xg = a.X[g], Vg = a.V[g];
+        const float x0 = sx[0][j], x1 = sx[1][j], x2 = sx[2][j];
+        Vg.x = Vg.x + x0 * dt;
+        Vg.y = Vg.y + x1 * dt;
+        Vg.z = Vg.z + x2 * dt;
+        Xg.x = Xg.x + dt * Vg.x;
+        Xg.y = Xg.y + dt * Vg.y;
+        Xg.z = Xg.z + dt * Vg.z;
+        if (Xg.y < 0.0f) Xg.y = 0.0f;
+        a.X[g] = Xg;
+        a.V[g] = Vg;
+        a.x[0][g] = x0;
+        a.x[1][g] = x1;
+        a.x[2][g] = x2;
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+        InstState& st = a.state[inst];
+        st.delta0 = delta0;
+        st.delta_new = delta;
+        st.iter = it;
+        st.flags = flags;
+        st.active = 0;
+        st.alpha = 0.0f;
+        st.beta = beta;
+    }
+    // A CTA's shared memory must outlive the other CTAs' reads of it.
+    if (C > 1) cgx::this_cluster().sync();
+}
+
+template <int T>
+cudaError_t prepare_t() {
+    cudaError_t e = cudaFuncSetAttribute(k_resident<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(15 * kResidentMaxVcta * sizeof(float)));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_resident<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+}
+
+template <int T>
+cudaError_t launch_t(const StepArgs& a, const ResidentLaunch& L, int n_clusters, cudaStream_t stream) {
+    const size_t smem = resident_smem_bytes(L.vcta);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(n_clusters * L.cluster));
+    cfg.blockDim = dim3(T);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)L.cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = L.cluster > 1 ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_resident<T>, a, L);
+}
+
+}  // namespace
+
+size_t resident_smem_bytes(int vcta) { return (size_t)15 * vcta * sizeof(float); }
+
+cudaError_t prepare_resident() {
+    cudaError_t e = prepare_t<128>();
+    if (e == cudaSuccess) e = prepare_t<256>();
+    if (e == cudaSuccess) e = prepare_t<512>();
+    return e;
+}
+
+cudaError_t launch_resident(const StepArgs& a, const ResidentLaunch& L, int threads, int n_clusters,
+                            cudaStream_t stream) {
+    if (n_clusters <= 0) return cudaSuccess;
+    switch (threads) {
+        case 128: return launch_t<128>(a, L, n_clusters, stream);
+        case 256: return launch_t<256>(a, L, n_clusters, stream);
+        case 512: return launch_t<512>(a, L, n_clusters, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace oc

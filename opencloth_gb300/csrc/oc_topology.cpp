@@ -162,7 +162,7 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
         for (int32_t b = 0; b < ip.nblk; ++b) {
             BlockInfo bi;
             bi.inst = k;
-            bi.local_blk = b;
+            bi.gblk = (int32_t)P.blocks.size();
             bi.v_begin = vo + (int64_t)b * vpb;
             bi.v_end = std::min<int64_t>(vo + d.n_vertices, bi.v_begin + vpb);
             P.blocks.push_back(bi);

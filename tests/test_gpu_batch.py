@@ -27,7 +27,7 @@ def make_batch(n, seed, lo=4, hi=40):
     return items
 
 
-@pytest.mark.parametrize("executor", ["streamed", "plain"])
+@pytest.mark.parametrize("executor", ["streamed", "plain", "resident", "auto"])
 def test_batch_equals_solo_runs(executor):
     items = make_batch(12, seed=1)
     descs = [it[0] for it in items]
@@ -40,7 +40,7 @@ def test_batch_equals_solo_runs(executor):
         itb, rrb, flb = s.stats()
         off = s.offsets
     for k, (desc, _, X, V) in enumerate(items):
-        with ClothSolver(desc) as solo:
+        with ClothSolver(desc, executor=executor) as solo:
             solo.set_state(X, V)
             solo.step(DT, 7)
             Xs, Vs, dVs = solo.get_state()
@@ -95,3 +95,66 @@ def test_single_vertex_and_springless_instances():
                                        filter_pinned=True)
     assert rel(Xg[:1], Xo) <= 1e-6 and Xg[0, 1] < 3.0
     assert np.array_equal(Xg[2], X[2])  # the pinned vertex stays
+
+
+def large_batch(seed):
+    """Sizes that exercise every resident launch shape: one CTA (<= 1024 vertices) and
+    clusters of 2..16 CTAs (up to 128 x 128 = 16384 vertices)."""
+    sides = [8, 11, 16, 23, 32, 40, 45, 64, 90, 100, 127, 128]
+    return [seeded_cloth(n, n, seed=100 * seed + k, velocity=0.01) for k, n in enumerate(sides)]
+
+
+def run_batch(items, executor, steps=6):
+    with ClothSolver([it[0] for it in items], executor=executor) as s:
+        s.set_state(np.concatenate([it[2] for it in items]), np.concatenate([it[3] for it in items]))
+        s.step(DT, steps)
+        X, V, dV = s.get_state()
+        it, rr, fl = s.stats()
+        return X, V, dV, it, rr, fl, s.offsets
+
+
+def test_resident_matches_streamed():
+    """Same arithmetic, different FP64 summation order across CTAs: within 1e-6."""
+    items = large_batch(1)
+    Xr, Vr, dVr, itr, rrr, flr, off = run_batch(items, "resident")
+    Xs, Vs, dVs, its, rrs, fls, _ = run_batch(items, "streamed")
+    for k in range(len(items)):
+        sl = slice(off[k], off[k + 1])
+        assert rel(Xr[sl], Xs[sl]) <= 1e-6 and rel(Vr[sl], Vs[sl]) <= 1e-5, k
+        assert abs(int(itr[k]) - int(its[k])) <= 1 and flr[k] == fls[k] == 0, k
+        assert rrr[k] <= 1e-5
+
+
+def test_resident_tracks_oracle():
+    items = large_batch(2)[::3]
+    Xb, Vb, _, itb, _, _, off = run_batch(items, "resident", steps=4)
+    for k, (_, ocl, X, V) in enumerate(items):
+        Xo, Vo, _, ito, _ = oracle.port_step(ocl, X, V, n_steps=4, dot_fp64=True, filter_pinned=True)
+        sl = slice(off[k], off[k + 1])
+        assert rel(Xb[sl], Xo) <= 1e-6 and rel(Vb[sl], Vo) <= 1e-5, k
+        assert abs(int(itb[k]) - int(ito[-1])) <= 1, k
+
+
+def test_auto_mixes_resident_and_streamed_cloths():
+    """A cloth above the resident size limit runs streamed beside resident cloths in one
+    graph; each matches its solo run bit for bit."""
+    items = [seeded_cloth(20, 20, seed=31), seeded_cloth(140, 140, seed=32), seeded_cloth(50, 50, seed=33)]
+    Xb, Vb, dVb, itb, _, _, off = run_batch(items, "auto", steps=5)
+    for k, (desc, _, X, V) in enumerate(items):
+        with ClothSolver(desc) as solo:
+            solo.set_state(X, V)
+            solo.step(DT, 5)
+            Xs, Vs, dVs = solo.get_state()
+            its = solo.stats()[0]
+        sl = slice(off[k], off[k + 1])
+        assert np.array_equal(Xb[sl], Xs) and np.array_equal(Vb[sl], Vs) and np.array_equal(dVb[sl], dVs), k
+        assert itb[k] == its[0]
+
+
+def test_resident_rejects_oversize_cloth():
+    from opencloth_gb300 import OcError
+
+    big = seeded_cloth(200, 200, seed=5)[0]
+    with pytest.raises(OcError) as e:
+        ClothSolver(big, executor="resident")
+    assert e.value.status == 7

@@ -94,7 +94,8 @@ def test_error_against_fp64_reference():
     assert rel(X, g["X64_600"]) <= TOL_FP64_X
 
 
-@pytest.mark.parametrize("executor,graph", [("streamed", True), ("streamed", False), ("plain", False)])
+@pytest.mark.parametrize("executor,graph", [("streamed", True), ("streamed", False), ("plain", False),
+                                            ("resident", True), ("resident", False)])
 def test_executors_agree_bit_for_bit(executor, graph):
     g = golden("random7x5_ref")
     with solver_for(g) as base:
