@@ -221,8 +221,10 @@ oc_status build_graph(oc_solver* s, float dt) {
     cudaGraph_t g = nullptr;
     OC_TRY(cudaGraphCreate(&g, 0));
     s->graph = g;
-    cudaGraphConditionalHandle handle;
-    OC_TRY(cudaGraphConditionalHandleCreate(&handle, g, 0, 0));
+    // The WHILE loop's handle exists only when there are streamed cloths (a handle that
+    // no conditional node uses makes the graph fail to instantiate).
+    cudaGraphConditionalHandle handle = 0;
+    if (s->n_streamed_blocks > 0) OC_TRY(cudaGraphConditionalHandleCreate(&handle, g, 0, 0));
 
     StepArgs a = s->args;
     a.dt = dt;
