@@ -42,6 +42,10 @@ struct oc_solver {
     std::vector<uint8_t> resident;  // per instance
     BlockInfo* d_streamed_blocks = nullptr;
     int32_t n_streamed_blocks = 0;
+    // Resident buckets run concurrently: forked from the handle's stream onto these.
+    std::vector<cudaStream_t> aux;
+    std::vector<cudaEvent_t> aux_done;
+    cudaEvent_t fork_ev = nullptr;
     std::vector<void*> allocs;
     StepArgs args{};
     float* stage = nullptr;         // device staging: 3 x 3 * nv floats
@@ -99,6 +103,9 @@ void release(oc_solver* s) {
     if (s->h_state) cudaFreeHost(s->h_state);
     if (s->h_scalar) cudaFreeHost(s->h_scalar);
     if (s->h_loop) cudaFreeHost(s->h_loop);
+    for (cudaStream_t x : s->aux) cudaStreamDestroy(x);
+    for (cudaEvent_t e : s->aux_done) cudaEventDestroy(e);
+    if (s->fork_ev) cudaEventDestroy(s->fork_ev);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -151,6 +158,22 @@ oc_status launch_timed(oc_solver* s, KernelKind k, const StepArgs& a, int nblock
 }
 
 oc_status launch_resident_all(oc_solver* s, const StepArgs& a, KernelTimer* t) {
+    if (!t && !s->aux.empty()) {
+        // Fork: every bucket on its own stream, joined back into the handle's stream.
+        OC_TRY(cudaEventRecord(s->fork_ev, s->stream));
+        for (size_t i = 0; i < s->aux.size(); ++i) OC_TRY(cudaStreamWaitEvent(s->aux[i], s->fork_ev, 0));
+        for (size_t i = 0; i < s->buckets.size(); ++i) {
+            const auto& b = s->buckets[i];
+            ResidentLaunch L{b.d_ids, b.cluster, b.vcta};
+            OC_TRY(launch_resident(a, L, b.threads, b.n, s->aux[i % s->aux.size()]));
+            s->host_launches += 1;
+        }
+        for (size_t i = 0; i < s->aux.size(); ++i) {
+            OC_TRY(cudaEventRecord(s->aux_done[i], s->aux[i]));
+            OC_TRY(cudaStreamWaitEvent(s->stream, s->aux_done[i], 0));
+        }
+        return OC_OK;
+    }
     for (const auto& b : s->buckets) {
         if (t) OC_TRY(cudaEventRecord(t->ev[0], s->stream));
         ResidentLaunch L{b.d_ids, b.cluster, b.vcta};
@@ -239,16 +262,15 @@ oc_status build_graph(oc_solver* s, float dt) {
         OC_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
         StepArgs ra = a;
         ra.use_cond = 0;
-        for (const auto& b : s->buckets) {
-            ResidentLaunch L{b.d_ids, b.cluster, b.vcta};
-            cudaError_t e = launch_resident(ra, L, b.threads, b.n, s->stream);
-            if (e != cudaSuccess) {
-                cudaStreamEndCapture(s->stream, &rg);
-                if (rg) cudaGraphDestroy(rg);
-                return fail_cuda(s, e, "launch_resident (capture)");
-            }
+        const int64_t launches_before = s->host_launches;
+        oc_status rs = launch_resident_all(s, ra, nullptr);
+        s->host_launches = launches_before;
+        cudaError_t ce = cudaStreamEndCapture(s->stream, &rg);
+        if (rs != OC_OK) {
+            if (rg) cudaGraphDestroy(rg);
+            return rs;
         }
-        OC_TRY(cudaStreamEndCapture(s->stream, &rg));
+        if (ce != cudaSuccess) return fail_cuda(s, ce, "cudaStreamEndCapture");
         cudaGraphNode_t n_res;
         cudaError_t e = cudaGraphAddChildGraphNode(&n_res, g, nullptr, 0, rg);
         cudaGraphDestroy(rg);
@@ -486,7 +508,14 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
                 for (int32_t b = 0; b < P.inst[k].nblk; ++b) streamed.push_back(P.blocks[P.inst[k].blk0 + b]);
             }
         }
-        for (auto& kv : groups) {
+        std::vector<std::pair<std::tuple<int, int, int>, std::vector<int32_t>>> ordered(groups.begin(), groups.end());
+        // Largest buckets first, so their clusters start before the small ones fill in.
+        std::stable_sort(ordered.begin(), ordered.end(), [](const auto& x, const auto& y) {
+            const double wx = (double)x.second.size() * std::get<1>(x.first) * std::get<2>(x.first);
+            const double wy = (double)y.second.size() * std::get<1>(y.first) * std::get<2>(y.first);
+            return wx > wy;
+        });
+        for (auto& kv : ordered) {
             oc_solver::Bucket b;
             b.threads = std::get<0>(kv.first);
             b.cluster = std::get<1>(kv.first);
@@ -497,7 +526,19 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
         }
         s->n_streamed_blocks = (int32_t)streamed.size();
         OC_CREATE_TRY(upload(s, &s->d_streamed_blocks, streamed));
-        if (!s->buckets.empty()) OC_CREATE_TRY(prepare_resident());
+        if (!s->buckets.empty()) {
+            OC_CREATE_TRY(prepare_resident());
+            const size_t naux = std::min<size_t>(s->buckets.size(), 8);
+            OC_CREATE_TRY(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming));
+            for (size_t i = 0; i < naux; ++i) {
+                cudaStream_t x = nullptr;
+                cudaEvent_t e = nullptr;
+                OC_CREATE_TRY(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+                s->aux.push_back(x);
+                OC_CREATE_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+                s->aux_done.push_back(e);
+            }
+        }
     }
     OC_CREATE_TRY(dalloc(s, &a.unconverged, 1));
     OC_CREATE_TRY(dalloc(s, &a.grid_ticket, 1));

@@ -9,8 +9,9 @@
 //   k_integrate  V += dV dt; X += dt V; ground clamp               (IMP:790-797)
 //
 // Compiled with --fmad=false and IEEE division / square root so every FP32 operation
-// rounds exactly as the reference's scalar code does; the CG dot products alone
-// accumulate in FP64 (per-vertex FP32 dot terms, summed in double).
+// rounds exactly as the reference's scalar code does.  The CG dot products are summed
+// in extended precision: per-vertex FP32 terms, error-free float pairs within a warp,
+// FP64 above (see Acc in oc_device.cuh).
 //
 // Reductions are deterministic: each block writes one FP64 partial; the last block of
 // an instance to finish (atomic ticket) sums that instance's partials in a fixed order
@@ -120,10 +121,10 @@ __device__ float3 chunk_gather(const StepArgs& a, const InstParams& ip, int64_t 
 
 // Last-block epilogue shared by the reducing kernels.
 template <int KIND>
-__device__ void finish(const StepArgs& a, int blk, int inst, bool participates, double part) {
+__device__ void finish(const StepArgs& a, int blk, int inst, bool participates, Acc part) {
     __shared__ int s_last;
     if (participates) {
-        const double bsum = block_sum(part);
+        const double bsum = block_sum_acc(part);
         if (threadIdx.x == 0) {
             a.partials[blk] = bsum;
             __threadfence();
@@ -200,8 +201,8 @@ __device__ void finish(const StepArgs& a, int blk, int inst, bool participates, 
 // Per-vertex part of the assembly after the force gather: the vertex's system and CG
 // set-up (pinned rows filtered out), stored to the SoA planes.  Returns the vertex's
 // term of delta0.
-__device__ __forceinline__ double assemble_vertex(const StepArgs& a, int64_t g, const float4 Xg, const float4 Vg,
-                                                  const float3 F, const OwnSpring& os) {
+__device__ __forceinline__ float assemble_vertex(const StepArgs& a, int64_t g, const float4 Xg, const float4 Vg,
+                                                 const float3 F, const OwnSpring& os) {
     const bool pinned = Vg.w != 0.0f;
     const VertexSystem sys = vertex_system(a.dt, Xg, Vg, F, os);
     const CgInit c = cg_init(sys, a.x[0][g], a.x[1][g], a.x[2][g], pinned);
@@ -229,7 +230,7 @@ __device__ __forceinline__ double assemble_vertex(const StepArgs& a, int64_t g, 
         a.dbg_b[3 * g + 1] = sys.b[1];
         a.dbg_b[3 * g + 2] = sys.b[2];
     }
-    return (double)c.term;
+    return c.term;
 }
 
 // Assembly with one thread per vertex.
@@ -238,12 +239,12 @@ __global__ void __launch_bounds__(kThreads) k_assemble_thread(const StepArgs a) 
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstParams& ip = a.inst[bi.inst];
-    double part = 0.0;
+    Acc part = acc_zero();
     for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
         const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
         const OwnSpring os = load_own(a, g);
         const float3 F = thread_gather<B>(a, ip, g, Xg, Vg);
-        part += assemble_vertex(a, g, Xg, Vg, F, os);
+        acc_add(part, assemble_vertex(a, g, Xg, Vg, F, os));
     }
     finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
 }
@@ -255,14 +256,14 @@ __global__ void __launch_bounds__(kThreads) k_assemble_coop(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstParams& ip = a.inst[bi.inst];
-    double part = 0.0;
+    Acc part = acc_zero();
     for (int64_t c0 = bi.v_begin; c0 < bi.v_end; c0 += blockDim.x) {
         const int64_t g = c0 + threadIdx.x;
         float4 Xg, Vg;
         const OwnSpring os = load_own(a, g < bi.v_end ? g : bi.v_begin);
         const float3 F = chunk_gather(a, ip, c0, min(c0 + (int64_t)blockDim.x, bi.v_end), sm, Xg, Vg);
         if (g >= bi.v_end) continue;
-        part += assemble_vertex(a, g, Xg, Vg, F, os);
+        acc_add(part, assemble_vertex(a, g, Xg, Vg, F, os));
     }
     finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
 }
@@ -276,7 +277,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_dir(const StepArgs a) {
     const BlockInfo bi = a.blocks[blk];
     const InstState& st = a.state[bi.inst];
     const bool active = st.active != 0;
-    double part = 0.0;
+    Acc part = acc_zero();
     if (active) {
         const bool first = st.iter == 0;
         const float beta = st.beta;
@@ -324,7 +325,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_dir(const StepArgs a) {
                 }
                 float q0, q1, q2;
                 matvec(A[u], d0, d1, d2, q0, q1, q2);
-                part += (double)(d0 * q0 + d1 * q1 + d2 * q2);
+                acc_add(part, d0 * q0 + d1 * q1 + d2 * q2);
             }
         }
     }
@@ -336,7 +337,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
     const BlockInfo bi = a.blocks[blk];
     const InstState& st = a.state[bi.inst];
     const bool active = st.active != 0;
-    double part = 0.0;
+    Acc part = acc_zero();
     if (active) {
         const float alpha = st.alpha;
         const float* __restrict__ A0 = a.A[0];
@@ -384,7 +385,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
                 R0[g] = r0;
                 R1[g] = r1;
                 R2[g] = r2;
-                part += (double)(r0 * r0 + r1 * r1 + r2 * r2);
+                acc_add(part, r0 * r0 + r1 * r1 + r2 * r2);
             }
         }
     }

@@ -2,8 +2,9 @@
 // launch — force gather, Jacobians and assembly (IMP:698-786), the complete
 // preconditioned CG to the cloth's own tolerance (IMP:308-330), and the update
 // (IMP:790-797).  The CG state (A, x, r, d: 60 B per vertex) lives in shared memory,
-// so the CG loop touches no HBM.  Dot products reduce per CTA in FP64, then across
-// the cluster through distributed shared memory after a hardware cluster barrier; every
+// so the CG loop touches no HBM.  Dot products reduce per CTA (Acc pairs within warps,
+// FP64 above), then in FP64 across the cluster through distributed shared memory
+// after a hardware cluster barrier; every
 // CTA sums the CTAs' partials in rank order, so all of them take identical
 // decisions.  There are no spin-waits.
 #include <cooperative_groups.h>
@@ -19,8 +20,8 @@ namespace {
 
 // FP64 sum over the CTA, then over the cluster (C CTAs), identical in every CTA.
 // slots[2] (double-buffered per call) and bcast live in shared memory.
-__device__ double cluster_sum(double part, int C, double* slots, double* bcast, int& phase) {
-    const double bs = block_sum(part);
+__device__ double cluster_sum(Acc part, int C, double* slots, double* bcast, int& phase) {
+    const double bs = block_sum_acc(part);
     if (C == 1) {
         if (threadIdx.x == 0) *bcast = bs;
         __syncthreads();
@@ -68,7 +69,7 @@ __global__ void __launch_bounds__(T) k_resident(const StepArgs a, const Resident
     }
 
     // Assembly and CG set-up.
-    double part = 0.0;
+    Acc part = acc_zero();
     for (int j = threadIdx.x; j < n_local; j += T) {
         const int64_t g = base + j;
         const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
@@ -84,7 +85,7 @@ __global__ void __launch_bounds__(T) k_resident(const StepArgs a, const Resident
             sr[k][j] = c.r[k];
             sd[k][j] = c.d[k];
         }
-        part += (double)c.term;
+        acc_add(part, c.term);
     }
     int phase = 0;
     const double delta0 = cluster_sum(part, C, slots, &bcast, phase);
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(T) k_resident(const StepArgs a, const Resident
     float beta = 0.0f;
     while (run) {
         // d = r + beta d (after the first iteration), d.(A d), IMP:320-321, 327.
-        part = 0.0;
+        part = acc_zero();
         for (int j = threadIdx.x; j < n_local; j += T) {
             float d0 = sd[0][j], d1 = sd[1][j], d2 = sd[2][j];
             if (it > 0) {
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(T) k_resident(const StepArgs a, const Resident
             const float A[6] = {sA[0][j], sA[1][j], sA[2][j], sA[3][j], sA[4][j], sA[5][j]};
             float q0, q1, q2;
             matvec(A, d0, d1, d2, q0, q1, q2);
-            part += (double)(d0 * q0 + d1 * q1 + d2 * q2);
+            acc_add(part, d0 * q0 + d1 * q1 + d2 * q2);
         }
         const double dq = cluster_sum(part, C, slots, &bcast, phase);
         if (!(dq > 0.0) || !isfinite(dq)) {
@@ -123,7 +124,7 @@ __global__ void __launch_bounds__(T) k_resident(const StepArgs a, const Resident
         }
         const float alpha = (float)(delta / dq);
         // x += alpha d; r -= alpha A d; r.r, IMP:322-325.
-        part = 0.0;
+        part = acc_zero();
         for (int j = threadIdx.x; j < n_local; j += T) {
             const float d0 = sd[0][j], d1 = sd[1][j], d2 = sd[2][j];
             const float A[6] = {sA[0][j], sA[1][j], sA[2][j], sA[3][j], sA[4][j], sA[5][j]};
@@ -138,7 +139,7 @@ __global__ void __launch_bounds__(T) k_resident(const StepArgs a, const Resident
             sr[0][j] = r0;
             sr[1][j] = r1;
             sr[2][j] = r2;
-            part += (double)(r0 * r0 + r1 * r1 + r2 * r2);
+            acc_add(part, r0 * r0 + r1 * r1 + r2 * r2);
         }
         const double old = delta;
         delta = cluster_sum(part, C, slots, &bcast, phase);
