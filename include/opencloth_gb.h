@@ -155,7 +155,8 @@ oc_status oc_assemble(oc_solver* s, float dt, float* A9, float* b);
  * 32-byte slot of names (up to max_kernels), total ms, launches, and the algorithmic
  * bytes it moved — each array element it must read or write counted once, for the
  * instances still iterating: per vertex k_assemble 120 B + 32 B per spring, k_cg_dir
- * 36 B on the first pass of a step and 60 B after, k_cg_update 84 B, k_integrate 76 B.
+ * 36 B on the first pass of a step and 60 B after, k_cg_update 84 B, k_integrate 76 B,
+ * k_resident (the whole CG of a cloth in shared memory, plus the update) 136 B.
  * *n_kernels receives the number of kernels reported. */
 oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_kernels, char* names,
                            double* ms_total, int64_t* launches, double* algorithmic_bytes, int32_t* n_kernels);

@@ -127,14 +127,14 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
     for (int32_t k = 0; k < s->n_inst; ++k) {
         const double nv = (double)s->inst_host[k].nv, ns = (double)s->ns_inst[k];
         const InstState& st = s->h_state[k];
+        t->bytes[K_ASSEMBLE] += 120.0 * nv + 32.0 * ns;
         if (s->resident[k]) {
-            // Inputs X, V 32 + rowptr 4 + spring i 24 + warm start 12 and 32 B per spring;
-            // outputs X, V 32 + dV 12.  The CG runs in shared memory.
-            t->bytes[K_RESIDENT] += 116.0 * nv + 32.0 * ns;
+            // CG state in (A 24 + x, r, d 36), X, V 32 in and out, dV 12 out; the CG
+            // iterations run in shared memory.
+            t->bytes[K_RESIDENT] += 136.0 * nv;
             continue;
         }
         const double it = (double)st.iter;
-        t->bytes[K_ASSEMBLE] += 120.0 * nv + 32.0 * ns;
         t->bytes[K_INTEGRATE] += 76.0 * nv;
         t->bytes[K_CG_UPDATE] += 84.0 * nv * it;
         double dirs = it > 0 ? 36.0 * nv + 60.0 * nv * (it - 1.0) : 0.0;
@@ -197,31 +197,45 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
     a.use_cond = 0;
     a.cond = 0;
     OC_TRY(cudaMemsetAsync(a.unconverged, 0, sizeof(int32_t), s->stream));
-    if (!per_cloth) {
-        oc_status st = launch_resident_all(s, a, t);
-        if (st != OC_OK) return st;
-        a.blocks = s->d_streamed_blocks;
-    }
-    const int n_groups = per_cloth ? s->n_inst : (s->n_streamed_blocks > 0 ? 1 : 0);
-    for (int grp = 0; grp < n_groups; ++grp) {
-        a.blk_base = per_cloth ? s->inst_host[grp].blk0 : 0;
-        const int nb = per_cloth ? s->inst_host[grp].nblk : s->n_streamed_blocks;
-        oc_status st = launch_timed(s, K_ASSEMBLE, a, nb, t);
-        if (st != OC_OK) return st;
-        s->host_launches += 2;
-        for (;;) {
-            if (per_cloth)
+    oc_status st = OC_OK;
+    if (per_cloth) {
+        // The plain baseline: every cloth on its own, streamed kernels, host-driven loop.
+        for (int grp = 0; grp < s->n_inst; ++grp) {
+            a.blk_base = s->inst_host[grp].blk0;
+            const int nb = s->inst_host[grp].nblk;
+            if ((st = launch_timed(s, K_ASSEMBLE, a, nb, t)) != OC_OK) return st;
+            s->host_launches += 2;
+            for (;;) {
                 OC_TRY(cudaMemcpyAsync(s->h_scalar, &s->args.state[grp].active, sizeof(int32_t),
                                        cudaMemcpyDeviceToHost, s->stream));
-            else
+                OC_TRY(cudaStreamSynchronize(s->stream));
+                if (*s->h_scalar <= 0) break;
+                if ((st = launch_timed(s, K_CG_DIR, a, nb, t)) != OC_OK) return st;
+                if ((st = launch_timed(s, K_CG_UPDATE, a, nb, t)) != OC_OK) return st;
+            }
+            if ((st = launch_timed(s, K_INTEGRATE, a, nb, t)) != OC_OK) return st;
+        }
+    } else {
+        // Assembly over every cloth, then the resident CG launches and the streamed loop.
+        a.blk_base = 0;
+        if ((st = launch_timed(s, K_ASSEMBLE, a, s->n_blocks, t)) != OC_OK) return st;
+        s->host_launches += 1;
+        if ((st = launch_resident_all(s, a, t)) != OC_OK) return st;
+        StepArgs sa = a;
+        sa.blocks = s->d_streamed_blocks;
+        const int nb = s->n_streamed_blocks;
+        if (nb > 0) {
+            for (;;) {
                 OC_TRY(cudaMemcpyAsync(s->h_scalar, a.unconverged, sizeof(int32_t), cudaMemcpyDeviceToHost,
                                        s->stream));
-            OC_TRY(cudaStreamSynchronize(s->stream));
-            if (*s->h_scalar <= 0) break;
-            if ((st = launch_timed(s, K_CG_DIR, a, nb, t)) != OC_OK) return st;
-            if ((st = launch_timed(s, K_CG_UPDATE, a, nb, t)) != OC_OK) return st;
+                OC_TRY(cudaStreamSynchronize(s->stream));
+                if (*s->h_scalar <= 0) break;
+                if ((st = launch_timed(s, K_CG_DIR, sa, nb, t)) != OC_OK) return st;
+                if ((st = launch_timed(s, K_CG_UPDATE, sa, nb, t)) != OC_OK) return st;
+            }
+            if ((st = launch_timed(s, K_INTEGRATE, sa, nb, t)) != OC_OK) return st;
+            s->host_launches += 1;
         }
-        if ((st = launch_timed(s, K_INTEGRATE, a, nb, t)) != OC_OK) return st;
     }
     if (t) {
         OC_TRY(cudaMemcpyAsync(s->h_state, s->args.state, sizeof(InstState) * s->n_inst, cudaMemcpyDeviceToHost,
@@ -244,20 +258,63 @@ oc_status build_graph(oc_solver* s, float dt) {
     cudaGraph_t g = nullptr;
     OC_TRY(cudaGraphCreate(&g, 0));
     s->graph = g;
+    const bool streamed = s->n_streamed_blocks > 0;
     // The WHILE loop's handle exists only when there are streamed cloths (a handle that
     // no conditional node uses makes the graph fail to instantiate).
     cudaGraphConditionalHandle handle = 0;
-    if (s->n_streamed_blocks > 0) OC_TRY(cudaGraphConditionalHandleCreate(&handle, g, 0, 0));
+    if (streamed) OC_TRY(cudaGraphConditionalHandleCreate(&handle, g, 0, 0));
 
-    StepArgs a = s->args;
+    StepArgs a = s->args;  // full block table: the assembly covers every cloth
     a.dt = dt;
     a.blk_base = 0;
-    a.use_cond = 1;
+    a.use_cond = streamed ? 1 : 0;
     a.cond = (unsigned long long)handle;
-    a.blocks = s->d_streamed_blocks;
+    StepArgs sa = a;  // streamed cloths only
+    sa.blocks = s->d_streamed_blocks;
+    void* params_all[] = {&a};
+    void* params_str[] = {&sa};
+    auto kparams = [&](KernelKind k, bool all) {
+        cudaKernelNodeParams kp{};
+        kp.func = const_cast<void*>(kernel_fn(k));
+        kp.gridDim = dim3((unsigned)(all ? s->n_blocks : s->n_streamed_blocks));
+        kp.blockDim = dim3((unsigned)kernel_block_threads());
+        kp.sharedMemBytes = (unsigned)kernel_smem_bytes(k);
+        kp.kernelParams = all ? params_all : params_str;
+        kp.extra = nullptr;
+        return kp;
+    };
+
+    cudaGraphNode_t n_reset, n_asm;
+    cudaMemsetParams mp{};
+    mp.dst = a.unconverged;
+    mp.value = 0;
+    mp.elementSize = sizeof(int32_t);
+    mp.width = 1;
+    mp.height = 1;
+    mp.pitch = sizeof(int32_t);
+    OC_TRY(cudaGraphAddMemsetNode(&n_reset, g, nullptr, 0, &mp));
+    cudaKernelNodeParams kp = kparams(K_ASSEMBLE, true);
+    OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &n_reset, 1, &kp));
+
+    if (streamed) {
+        cudaGraphNode_t n_loop, n_dir, n_upd, n_int;
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        OC_TRY(cudaGraphAddNode(&n_loop, g, &n_asm, nullptr, 1, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        kp = kparams(K_CG_DIR, false);
+        OC_TRY(cudaGraphAddKernelNode(&n_dir, body, nullptr, 0, &kp));
+        kp = kparams(K_CG_UPDATE, false);
+        OC_TRY(cudaGraphAddKernelNode(&n_upd, body, &n_dir, 1, &kp));
+        kp = kparams(K_INTEGRATE, false);
+        OC_TRY(cudaGraphAddKernelNode(&n_int, g, &n_loop, 1, &kp));
+    }
     if (!s->buckets.empty()) {
-        // The resident launches, captured into a child graph that runs beside the
-        // streamed part (the two touch disjoint cloths).
+        // The resident CG launches (concurrent, fork/join) captured into a child graph that
+        // runs after the assembly, beside the streamed loop (they touch disjoint cloths).
         cudaGraph_t rg = nullptr;
         OC_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
         StepArgs ra = a;
@@ -272,53 +329,10 @@ oc_status build_graph(oc_solver* s, float dt) {
         }
         if (ce != cudaSuccess) return fail_cuda(s, ce, "cudaStreamEndCapture");
         cudaGraphNode_t n_res;
-        cudaError_t e = cudaGraphAddChildGraphNode(&n_res, g, nullptr, 0, rg);
+        cudaError_t e = cudaGraphAddChildGraphNode(&n_res, g, &n_asm, 1, rg);
         cudaGraphDestroy(rg);
         if (e != cudaSuccess) return fail_cuda(s, e, "cudaGraphAddChildGraphNode");
     }
-    if (s->n_streamed_blocks == 0) {
-        OC_TRY(cudaGraphInstantiate(&s->exec, g, 0));
-        s->graph_dt = dt;
-        return OC_OK;
-    }
-    void* params[] = {&a};
-    auto kparams = [&](KernelKind k) {
-        cudaKernelNodeParams kp{};
-        kp.func = const_cast<void*>(kernel_fn(k));
-        kp.gridDim = dim3((unsigned)s->n_streamed_blocks);
-        kp.blockDim = dim3((unsigned)kernel_block_threads());
-        kp.sharedMemBytes = (unsigned)kernel_smem_bytes(k);
-        kp.kernelParams = params;
-        kp.extra = nullptr;
-        return kp;
-    };
-
-    cudaGraphNode_t n_reset, n_asm, n_loop, n_dir, n_upd, n_int;
-    cudaMemsetParams mp{};
-    mp.dst = a.unconverged;
-    mp.value = 0;
-    mp.elementSize = sizeof(int32_t);
-    mp.width = 1;
-    mp.height = 1;
-    mp.pitch = sizeof(int32_t);
-    OC_TRY(cudaGraphAddMemsetNode(&n_reset, g, nullptr, 0, &mp));
-    cudaKernelNodeParams kp = kparams(K_ASSEMBLE);
-    OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &n_reset, 1, &kp));
-
-    cudaGraphNodeParams cp{};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = handle;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    OC_TRY(cudaGraphAddNode(&n_loop, g, &n_asm, nullptr, 1, &cp));
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    kp = kparams(K_CG_DIR);
-    OC_TRY(cudaGraphAddKernelNode(&n_dir, body, nullptr, 0, &kp));
-    kp = kparams(K_CG_UPDATE);
-    OC_TRY(cudaGraphAddKernelNode(&n_upd, body, &n_dir, 1, &kp));
-
-    kp = kparams(K_INTEGRATE);
-    OC_TRY(cudaGraphAddKernelNode(&n_int, g, &n_loop, 1, &kp));
     OC_TRY(cudaGraphInstantiate(&s->exec, g, 0));
     s->graph_dt = dt;
     return OC_OK;
@@ -524,6 +538,9 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
             OC_CREATE_TRY(upload(s, &b.d_ids, kv.second));
             s->buckets.push_back(b);
         }
+        for (int32_t k = 0; k < P.n_inst; ++k) P.inst[k].resident = s->resident[k];
+        s->inst_host = P.inst;
+        OC_CREATE_TRY(cudaMemcpy(inst, P.inst.data(), sizeof(InstParams) * P.n_inst, cudaMemcpyHostToDevice));
         s->n_streamed_blocks = (int32_t)streamed.size();
         OC_CREATE_TRY(upload(s, &s->d_streamed_blocks, streamed));
         if (!s->buckets.empty()) {
@@ -649,7 +666,7 @@ oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
         if (st != OC_OK) return st;
     }
     for (int32_t i = 0; i < n_steps; ++i) OC_TRY(cudaGraphLaunch(s->exec, s->stream));
-    s->host_launches += ((s->n_streamed_blocks > 0 ? 2 : 0) + (int64_t)s->buckets.size()) * (int64_t)n_steps;
+    s->host_launches += (1 + (s->n_streamed_blocks > 0 ? 1 : 0) + (int64_t)s->buckets.size()) * (int64_t)n_steps;
     return OC_OK;
 }
 

@@ -22,6 +22,8 @@ struct InstParams {
     int64_t v_off;  // first vertex (global index)
     int32_t nv;
     int32_t has_ext;
+    int32_t resident;  // 1: this cloth's CG runs in the resident kernel, not the streamed loop
+    int32_t pad_;
 };
 
 // Per-instance CG scalars, device resident, written by the last block of each

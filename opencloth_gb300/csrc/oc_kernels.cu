@@ -156,7 +156,8 @@ __device__ void finish(const StepArgs& a, int blk, int inst, bool participates, 
                         run = false;
                     }
                     st.active = run ? 1 : 0;
-                    if (run) atomicAdd(a.unconverged, 1);
+                    // Resident cloths run their CG loop in their own kernel.
+                    if (run && !ip.resident) atomicAdd(a.unconverged, 1);
                 } else if (KIND == K_CG_DIR) {
                     st.dq = total;
                     if (!(total > 0.0) || !isfinite(total)) {

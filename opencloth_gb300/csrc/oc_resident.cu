@@ -1,8 +1,8 @@
-// Resident executor: one cluster of CTAs per cloth runs the whole implicit step in one
-// launch — force gather, Jacobians and assembly (IMP:698-786), the complete
-// preconditioned CG to the cloth's own tolerance (IMP:308-330), and the update
-// (IMP:790-797).  The CG state (A, x, r, d: 60 B per vertex) lives in shared memory,
-// so the CG loop touches no HBM.  Dot products reduce per CTA (Acc pairs within warps,
+// Resident CG: after k_assemble has built every cloth's system and CG set-up, one
+// cluster of CTAs per cloth loads that cloth's CG state (A, x, r, d: 60 B per vertex)
+// into shared memory once, runs the complete preconditioned CG to the cloth's own
+// tolerance (IMP:308-330) on chip, and applies the update (IMP:790-797).  The CG loop
+// touches no HBM and needs no per-iteration launch.  Dot products reduce per CTA (Acc pairs within warps,
 // FP64 above), then in FP64 across the cluster through distributed shared memory
 // after a hardware cluster barrier; every
 // CTA sums the CTAs' partials in rank order, so all of them take identical
@@ -68,36 +68,28 @@ __global__ void __launch_bounds__(T) k_resident(const StepArgs a, const Resident
         sd[k] = smem + (12 + k) * cap;
     }
 
-    // Assembly and CG set-up.
-    Acc part = acc_zero();
+    // The CG state k_assemble left in the planes: A, x, r, d -> shared memory.
     for (int j = threadIdx.x; j < n_local; j += T) {
         const int64_t g = base + j;
-        const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
-        const OwnSpring os = load_own(a, g);
-        const float3 F = thread_gather<1>(a, ip, g, Xg, Vg);
-        const VertexSystem sys = vertex_system(a.dt, Xg, Vg, F, os);
-        const CgInit c = cg_init(sys, a.x[0][g], a.x[1][g], a.x[2][g], Vg.w != 0.0f);
 #pragma unroll
-        for (int k = 0; k < 6; ++k) sA[k][j] = sys.A[k];
+        for (int k = 0; k < 6; ++k) sA[k][j] = a.A[k][g];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            sx[k][j] = c.x[k];
-            sr[k][j] = c.r[k];
-            sd[k][j] = c.d[k];
+            sx[k][j] = a.x[k][g];
+            sr[k][j] = a.r[k][g];
+            sd[k][j] = a.d[k][g];
         }
-        acc_add(part, c.term);
     }
+    __syncthreads();
     int phase = 0;
-    const double delta0 = cluster_sum(part, C, slots, &bcast, phase);
+    Acc part;
+    const InstState& st0 = a.state[inst];
+    const double delta0 = st0.delta0;
     double delta = delta0;
     const double thresh = (double)ip.eps2 * delta0;
-    uint32_t flags = 0u;
+    uint32_t flags = st0.flags;
     int it = 0;
-    bool run = (0 < ip.imax) && (delta0 > thresh);
-    if (!isfinite(delta0)) {
-        flags |= OC_FLAG_NON_FINITE;
-        run = false;
-    }
+    bool run = st0.active != 0;
     float beta = 0.0f;
     while (run) {
         // d = r + beta d (after the first iteration), d.(A d), IMP:320-321, 327.

@@ -157,6 +157,8 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
         ip.v_off = vo;
         ip.nv = d.n_vertices;
         ip.has_ext = d.ext_force ? 1 : 0;
+        ip.resident = 0;
+        ip.pad_ = 0;
         ip.blk0 = (int32_t)P.blocks.size();
         ip.nblk = (d.n_vertices + vpb - 1) / vpb;
         for (int32_t b = 0; b < ip.nblk; ++b) {
