@@ -343,17 +343,27 @@ oc_status build_graph(oc_solver* s, float dt) {
 // to max_vertices and kResidentMaxCluster CTAs.
 constexpr int kResidentDefaultVcta = 1024;
 
+// The per-CTA vertex capacity and thread count are tuning knobs: OC_RESIDENT_SHAPE =
+// "vcta:threads" overrides the default 1024:256.
 bool resident_shape(int nv, int max_vertices, int* threads, int* cluster, int* vcta) {
     if (nv < 1 || nv > max_vertices) return false;
-    if (nv <= kResidentDefaultVcta) {
+    int base = kResidentDefaultVcta, thr = 256;
+    if (const char* e = std::getenv("OC_RESIDENT_SHAPE")) {
+        int v = 0, t = 0;
+        if (std::sscanf(e, "%d:%d", &v, &t) == 2 && v >= 128 && v <= kResidentMaxVcta && (t == 128 || t == 256 || t == 512)) {
+            base = v;
+            thr = t;
+        }
+    }
+    if (nv <= base) {
         int v = 128;
         while (v < nv) v <<= 1;
         *cluster = 1;
         *vcta = v;
-        *threads = v < 256 ? v : 256;
+        *threads = v < thr ? v : thr;
         return true;
     }
-    const int c = (nv + kResidentDefaultVcta - 1) / kResidentDefaultVcta;
+    const int c = (nv + base - 1) / base;
     if (c > kResidentMaxCluster) {
         const int c2 = (nv + kResidentMaxVcta - 1) / kResidentMaxVcta;
         if (c2 > kResidentMaxCluster) return false;
@@ -363,8 +373,8 @@ bool resident_shape(int nv, int max_vertices, int* threads, int* cluster, int* v
         return true;
     }
     *cluster = c;
-    *vcta = kResidentDefaultVcta;
-    *threads = 256;
+    *vcta = base;
+    *threads = thr;
     return true;
 }
 
