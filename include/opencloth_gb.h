@@ -161,6 +161,26 @@ oc_status oc_assemble(oc_solver* s, float dt, float* A9, float* b);
 oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_kernels, char* names,
                            double* ms_total, int64_t* launches, double* algorithmic_bytes, int32_t* n_kernels);
 
+/* ---- differentiation (no counterpart in the reference) ------------------------------ */
+/* Per-spring Ks / Kd of the handle (host arrays over all springs, instance by instance
+ * in creation order; either may be NULL to keep it). */
+oc_status oc_set_spring_params(oc_solver* s, const float* ks, const float* kd);
+/* A constant per-vertex external force added to every unpinned vertex (host, 3 floats
+ * per vertex), for cloths created without one too. */
+oc_status oc_set_ext_force(oc_solver* s, const float* ext);
+/* Run n_steps steps from the current state keeping a checkpoint of (X, V, dV) every
+ * checkpoint_every steps (0: about sqrt(n_steps)); fails with OC_ERR_OUT_OF_MEMORY when
+ * the checkpoints would exceed budget_bytes (0: no limit). */
+oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t checkpoint_every, int64_t budget_bytes);
+/* Reverse pass of the last oc_tape_forward: given dL/dX and dL/dV (NULL = 0) of its final
+ * state, returns dL/dX0, dL/dV0 (initial state), dL/dKs, dL/dKd (per spring) and dL/dext
+ * (the constant external force); any output may be NULL.  Segments between checkpoints
+ * are recomputed; each step's linear solve is back-propagated by one CG on the same
+ * symmetric system (exact-solve adjoint).  The handle's state is left at the final state. */
+oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV, float* dL_dX0, float* dL_dV0,
+                           float* dL_dKs, float* dL_dKd, float* dL_dext);
+oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* tape_bytes);
+
 /* ---- allocation-free solve -------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory
  * around a solve — an engine that manages a fixed device-memory budget itself, or a

@@ -91,6 +91,11 @@ SIGNATURES = {
     "oc_compute_forces": (C.c_int32, [_P, _P]),
     "oc_assemble": (C.c_int32, [_P, C.c_float, _P, _P]),
     "oc_profile_steps": (C.c_int32, [_P, C.c_float, C.c_int32, C.c_int32, _P, _P, _P, _P, _P]),
+    "oc_set_spring_params": (C.c_int32, [_P, _P, _P]),
+    "oc_set_ext_force": (C.c_int32, [_P, _P]),
+    "oc_tape_forward": (C.c_int32, [_P, C.c_float, C.c_int32, C.c_int32, C.c_int64]),
+    "oc_tape_backward": (C.c_int32, [_P, _P, _P, _P, _P, _P, _P, _P]),
+    "oc_tape_info": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
     "oc_pcg_solve_noalloc": (C.c_int32, [_P, _P, _P, _P, C.c_int32, C.c_int32, C.c_float, C.POINTER(C.c_int32),
                                          C.POINTER(C.c_uint32), _P]),
     "oc_grid_spring_count": (C.c_int32, [C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),

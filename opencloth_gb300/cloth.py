@@ -198,6 +198,42 @@ class ClothSolver:
         self._call(self._lib.oc_get_stats(self._h, ptr(it), ptr(rr), ptr(fl)))
         return it, rr, fl
 
+    # ---- differentiation ---------------------------------------------------------
+    def set_spring_params(self, ks=None, kd=None) -> None:
+        """Per-spring Ks / Kd over all springs of the handle (instance by instance)."""
+        ks = None if ks is None else np.ascontiguousarray(ks, np.float32).reshape(-1)
+        kd = None if kd is None else np.ascontiguousarray(kd, np.float32).reshape(-1)
+        for a in (ks, kd):
+            if a is not None and a.size != self.n_springs:
+                raise ValueError(f"expected {self.n_springs} values")
+        self._call(self._lib.oc_set_spring_params(self._h, ptr(ks), ptr(kd)))
+
+    def set_ext_force(self, ext) -> None:
+        """Constant per-vertex external force (3 floats per vertex)."""
+        self._call(self._lib.oc_set_ext_force(self._h, ptr(self._vec(ext))))
+
+    def tape_forward(self, dt: float, n_steps: int, checkpoint_every: int = 0, budget_bytes: int = 0) -> None:
+        """Run n_steps keeping checkpoints for tape_backward."""
+        self._call(self._lib.oc_tape_forward(self._h, float(dt), int(n_steps), int(checkpoint_every),
+                                             int(budget_bytes)))
+
+    def tape_backward(self, dL_dX, dL_dV=None) -> dict:
+        """Gradients of a loss of the final state with respect to the initial state, the
+        per-spring Ks / Kd and the constant external force."""
+        gX = self._vec(dL_dX)
+        gV = self._vec(dL_dV)
+        out = {k: np.zeros((self.n_vertices, 3), np.float32) for k in ("dX0", "dV0", "dext")}
+        out["dKs"] = np.zeros(self.n_springs, np.float32)
+        out["dKd"] = np.zeros(self.n_springs, np.float32)
+        self._call(self._lib.oc_tape_backward(self._h, ptr(gX), ptr(gV), ptr(out["dX0"]), ptr(out["dV0"]),
+                                              ptr(out["dKs"]), ptr(out["dKd"]), ptr(out["dext"])))
+        return out
+
+    def tape_info(self):
+        every, nbytes = C.c_int32(), C.c_int64()
+        self._call(self._lib.oc_tape_info(self._h, C.byref(every), C.byref(nbytes)))
+        return int(every.value), int(nbytes.value)
+
     def launch_count(self) -> int:
         n = C.c_int64()
         self._call(self._lib.oc_get_launch_count(self._h, C.byref(n)))

@@ -1,0 +1,311 @@
+// Adjoint of the implicit step (no counterpart in the reference): reverse-mode
+// gradients of a trajectory with respect to per-spring Ks and Kd, the initial state and
+// a per-vertex constant external force.
+//
+// Per step (REFERENCE Jacobian mode; vertex i takes spring i's Jacobians, IMP:737-798):
+//   X' = X + dt V' (y clamped at 0), V' = V + dt dV, A dV = b,
+//   A_i = m_i I - h Jv_i - h^2 J_i, b_i = h F_i + h^2 J_i V_i,
+//   J = Ks n n^T - (Ks C + Kd Cdot) D, D = C diag(1 - dP*dP), Jv = -Kd n n^T,
+//   f_s = (-Ks C + Kd (dV.dP)/L) n, F_i = m g + damping V_i + ext_i + sum_s +-f_s.
+// The solve is differentiated as an exact solve: one extra CG on the same symmetric A
+// gives lambda = A^-1 g_dV, then g_b = lambda and g_A = -lambda dV^T.  All sums are
+// gathers in a fixed order (spring-ordered incidences, and per vertex the list of the
+// vertices whose own spring touches it), so gradients are deterministic.
+#include <cuda_runtime.h>
+
+#include "oc_device.cuh"
+#include "oc_internal.h"
+
+namespace oc {
+namespace {
+
+constexpr int kAdjThreads = 256;
+
+__device__ __forceinline__ float dot3f(float ax, float ay, float az, float bx, float by, float bz) {
+    return ax * bx + ay * by + az * bz;
+}
+
+// Adjoint of one spring force f = (-Ks C + Kd u) n for dL/df = g.
+__device__ __forceinline__ void spring_force_adj(const float4 p1, const float4 p2, const float4 v1, const float4 v2,
+                                                 float rest, float ks, float kd, const float g[3], float gdP[3],
+                                                 float gdV[3], float& gks, float& gkd) {
+    const float dP[3] = {p1.x - p2.x, p1.y - p2.y, p1.z - p2.z};
+    const float dV[3] = {v1.x - v2.x, v1.y - v2.y, v1.z - v2.z};
+    const float L = sqrtf(dot3f(dP[0], dP[1], dP[2], dP[0], dP[1], dP[2]));
+    const float iL = 1.0f / L;
+    const float n[3] = {dP[0] * iL, dP[1] * iL, dP[2] * iL};
+    const float C = L - rest;
+    const float u = dot3f(dV[0], dV[1], dV[2], dP[0], dP[1], dP[2]) * iL;
+    const float m = -ks * C + kd * u;
+    const float gm = dot3f(g[0], g[1], g[2], n[0], n[1], n[2]);
+    const float gn[3] = {m * g[0], m * g[1], m * g[2]};
+    const float ng = dot3f(n[0], n[1], n[2], gn[0], gn[1], gn[2]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        gdP[k] = gm * (-ks * n[k] + kd * (dV[k] - u * n[k]) * iL) + (gn[k] - n[k] * ng) * iL;
+        gdV[k] = gm * kd * n[k];
+    }
+    gks = -C * gm;
+    gkd = u * gm;
+}
+
+// Adjoint of spring i's (J, Jv) for G = dL/dJ, H = dL/dJv (full 3x3, row-major).
+__device__ __forceinline__ void spring_jac_adj(const float4 p1, const float4 p2, const float4 v1, const float4 v2,
+                                               float rest, float ks, float kd, const float G[3][3],
+                                               const float H[3][3], float gdP[3], float gdV[3], float& gks,
+                                               float& gkd) {
+    const float dP[3] = {p1.x - p2.x, p1.y - p2.y, p1.z - p2.z};
+    const float dV[3] = {v1.x - v2.x, v1.y - v2.y, v1.z - v2.z};
+    const float L = sqrtf(dot3f(dP[0], dP[1], dP[2], dP[0], dP[1], dP[2]));
+    const float iL = 1.0f / L;
+    const float n[3] = {dP[0] * iL, dP[1] * iL, dP[2] * iL};
+    const float C = L - rest;
+    const float Cd = -dot3f(n[0], n[1], n[2], dV[0], dV[1], dV[2]);
+    const float w = ks * C + kd * Cd;
+    float gS[3][3];
+    gks = 0.0f;
+    gkd = 0.0f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float S = n[r] * n[c];
+            gS[r][c] = ks * G[r][c] - kd * H[r][c];
+            gks += G[r][c] * S;
+            gkd += -H[r][c] * S;
+        }
+    float gw = 0.0f, gC = 0.0f, gq[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float D = C * (1.0f - dP[k] * dP[k]);
+        gw += -G[k][k] * D;
+        const float gD = -w * G[k][k];
+        gC += gD * (1.0f - dP[k] * dP[k]);
+        gq[k] = -C * gD;
+    }
+    gC += ks * gw;
+    const float gCd = kd * gw;
+    gks += C * gw;
+    gkd += Cd * gw;
+    float gn[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+        gn[r] = (gS[r][0] + gS[0][r]) * n[0] + (gS[r][1] + gS[1][r]) * n[1] + (gS[r][2] + gS[2][r]) * n[2] -
+                gCd * dV[r];
+    const float ng = dot3f(n[0], n[1], n[2], gn[0], gn[1], gn[2]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        gdV[k] = -gCd * n[k];
+        gdP[k] = 2.0f * dP[k] * gq[k] + gC * n[k] + (gn[k] - n[k] * ng) * iL;
+    }
+}
+
+// Clamp, X' = X + dt V', V' = V + dt dV: the step's outputs' adjoints (gX, gV in the
+// planes) become gX, gV of X, V plus g_dV = dt gV'; then the adjoint CG is set up on
+// the system just assembled: x = 0, r = g_dV (pinned rows filtered), d = P^-1 r.
+__global__ void __launch_bounds__(kAdjThreads) k_adj_seed(const StepArgs a, const AdjArgs j) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const float dt = a.dt;
+    Acc part = acc_zero();
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Xg = a.X[g], Vg = a.V[g];
+        const float dvy = j.dV[1][g];
+        const float vy = Vg.y + dvy * dt;
+        const float ypre = Xg.y + dt * vy;
+        float gx0 = j.gX[0][g], gx1 = j.gX[1][g], gx2 = j.gX[2][g];
+        if (ypre < 0.0f) gx1 = 0.0f;  // clamped: X'.y does not depend on X, V
+        const float gv0 = j.gV[0][g] + dt * gx0, gv1 = j.gV[1][g] + dt * gx1, gv2 = j.gV[2][g] + dt * gx2;
+        j.gX[0][g] = gx0;
+        j.gX[1][g] = gx1;
+        j.gX[2][g] = gx2;
+        j.gV[0][g] = gv0;
+        j.gV[1][g] = gv1;
+        j.gV[2][g] = gv2;
+        const bool pinned = Vg.w != 0.0f;
+        const float r0 = pinned ? 0.0f : dt * gv0, r1 = pinned ? 0.0f : dt * gv1, r2 = pinned ? 0.0f : dt * gv2;
+        const float A0 = a.A[0][g], A3 = a.A[3][g], A5 = a.A[5][g];
+        a.x[0][g] = 0.0f;
+        a.x[1][g] = 0.0f;
+        a.x[2][g] = 0.0f;
+        a.r[0][g] = r0;
+        a.r[1][g] = r1;
+        a.r[2][g] = r2;
+        a.d[0][g] = (1.0f / A0) * r0;
+        a.d[1][g] = (1.0f / A3) * r1;
+        a.d[2][g] = (1.0f / A5) * r2;
+        acc_add(part, r0 * (A0 * r0) + r1 * (A3 * r1) + r2 * (A5 * r2));
+    }
+    finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
+}
+
+// Per vertex i: lambda -> g_F = h lambda, the terms of A_i and b_i: g_J = h^2 lambda (V +
+// dV)^T, g_Jv = h lambda dV^T, g_V += h^2 J lambda + damping g_F, g_ext += g_F; spring
+// i's Jacobian adjoint goes to the vertex's own-spring slots and to Ks_i, Kd_i.
+__global__ void __launch_bounds__(kAdjThreads) k_adj_vertex(const StepArgs a, const AdjArgs j) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const InstParams& ip = a.inst[bi.inst];
+    const float h = a.dt;
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Vg = a.V[g];
+        const bool pinned = Vg.w != 0.0f;
+        const float lam[3] = {a.x[0][g], a.x[1][g], a.x[2][g]};
+        const float dv[3] = {j.dV[0][g], j.dV[1][g], j.dV[2][g]};
+        const float v[3] = {Vg.x, Vg.y, Vg.z};
+        float gF[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) gF[k] = pinned ? 0.0f : h * lam[k];
+        float gv[3] = {j.gV[0][g], j.gV[1][g], j.gV[2][g]};
+        float gdP[3] = {0.f, 0.f, 0.f}, gdVs[3] = {0.f, 0.f, 0.f};
+        const OwnSpring os = load_own(a, g);
+        if (os.ends.x >= 0 && !pinned) {
+            SpringEval e;
+            spring_state(os.E1, os.E2, os.W1, os.W2, os.par.x, e);
+            float J[6], Jv[6];
+            jac_element(e, os.par.y, os.par.z, 0, 0, J[0], Jv[0]);
+            jac_element(e, os.par.y, os.par.z, 0, 1, J[1], Jv[1]);
+            jac_element(e, os.par.y, os.par.z, 0, 2, J[2], Jv[2]);
+            jac_element(e, os.par.y, os.par.z, 1, 1, J[3], Jv[3]);
+            jac_element(e, os.par.y, os.par.z, 1, 2, J[4], Jv[4]);
+            jac_element(e, os.par.y, os.par.z, 2, 2, J[5], Jv[5]);
+            float jl0, jl1, jl2;
+            matvec(J, lam[0], lam[1], lam[2], jl0, jl1, jl2);
+            gv[0] += h * h * jl0;
+            gv[1] += h * h * jl1;
+            gv[2] += h * h * jl2;
+            float G[3][3], H[3][3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    G[r][c] = h * h * lam[r] * (v[c] + dv[c]);
+                    H[r][c] = h * lam[r] * dv[c];
+                }
+            float gks, gkd;
+            spring_jac_adj(os.E1, os.E2, os.W1, os.W2, os.par.x, os.par.y, os.par.z, G, H, gdP, gdVs, gks, gkd);
+            const int32_t sid = j.own_sid[g];
+            j.gKs[sid] += gks;
+            j.gKd[sid] += gkd;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            gv[k] += ip.damping * gF[k];
+            j.gV[k][g] = gv[k];
+            j.gF[k][g] = gF[k];
+            j.gOwn[k][g] = gdP[k];
+            j.gOwn[3 + k][g] = gdVs[k];
+            if (!pinned) j.gExt[k][g] += gF[k];
+        }
+    }
+}
+
+// Per vertex v: every incident spring's force adjoint, in spring-id order (the spring's
+// p1 side also adds to Ks_s, Kd_s), then the own-spring Jacobian terms of the vertices
+// whose spring touches v.
+__global__ void __launch_bounds__(kAdjThreads) k_adj_springs(const StepArgs a, const AdjArgs j) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Xg = a.X[g], Vg = a.V[g];
+        const bool pin_g = Vg.w != 0.0f;
+        const float gFg[3] = {j.gF[0][g], j.gF[1][g], j.gF[2][g]};
+        float gx[3] = {j.gX[0][g], j.gX[1][g], j.gX[2][g]};
+        float gv[3] = {j.gV[0][g], j.gV[1][g], j.gV[2][g]};
+        const int32_t k0 = a.rowptr[g], k1 = a.rowptr[g + 1];
+        for (int32_t k = k0; k < k1; ++k) {
+            const int4 rec = a.inc[k];
+            const bool as_p2 = rec.x < 0;
+            const int32_t o = rec.x & 0x7fffffff;
+            const float4 Xo = a.X[o], Vo = a.V[o];
+            const bool pin_o = Vo.w != 0.0f;
+            const float gFo[3] = {j.gF[0][o], j.gF[1][o], j.gF[2][o]};
+            // g_f = [p1 free] gF[p1] - [p2 free] gF[p2]
+            float gf[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float g1 = as_p2 ? (pin_o ? 0.0f : gFo[c]) : (pin_g ? 0.0f : gFg[c]);
+                const float g2 = as_p2 ? (pin_g ? 0.0f : gFg[c]) : (pin_o ? 0.0f : gFo[c]);
+                gf[c] = g1 - g2;
+            }
+            const float rest = __int_as_float(rec.y), ks = __int_as_float(rec.z), kd = __int_as_float(rec.w);
+            float gdP[3], gdV[3], gks, gkd;
+            if (as_p2)
+                spring_force_adj(Xo, Xg, Vo, Vg, rest, ks, kd, gf, gdP, gdV, gks, gkd);
+            else
+                spring_force_adj(Xg, Xo, Vg, Vo, rest, ks, kd, gf, gdP, gdV, gks, gkd);
+            const float sgn = as_p2 ? -1.0f : 1.0f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                gx[c] += sgn * gdP[c];
+                gv[c] += sgn * gdV[c];
+            }
+            if (!as_p2) {
+                const int32_t sid = j.inc_sid[k];
+                j.gKs[sid] += gks;
+                j.gKd[sid] += gkd;
+            }
+        }
+        const int32_t o0 = j.own_rowptr[g], o1 = j.own_rowptr[g + 1];
+        for (int32_t k = o0; k < o1; ++k) {
+            const int32_t e = j.own_ent[k];
+            const int32_t i = e & 0x7fffffff;
+            const float sgn = e < 0 ? -1.0f : 1.0f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                gx[c] += sgn * j.gOwn[c][i];
+                gv[c] += sgn * j.gOwn[3 + c][i];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            j.gX[c][g] = gx[c];
+            j.gV[c][g] = gv[c];
+        }
+    }
+}
+
+// Per-spring Ks / Kd into the incidence records and spring i's parameters.
+__global__ void k_set_spring_params(const StepArgs a, const AdjArgs j, const float* ks, const float* kd, int64_t n_rec,
+                                    int64_t nv) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_rec; k += stride) {
+        const int32_t s = j.inc_sid[k];
+        int4 rec = a.inc[k];
+        rec.z = __float_as_int(ks[s]);
+        rec.w = __float_as_int(kd[s]);
+        const_cast<int4*>(a.inc)[k] = rec;
+    }
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nv; g += stride) {
+        const int32_t s = j.own_sid[g];
+        if (s >= 0) {
+            float4 p = a.own_par[g];
+            p.y = ks[s];
+            p.z = kd[s];
+            const_cast<float4*>(a.own_par)[g] = p;
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_adjoint(int which, const StepArgs& a, const AdjArgs& j, int nblocks, cudaStream_t stream) {
+    if (nblocks <= 0) return cudaSuccess;
+    switch (which) {
+        case 0: k_adj_seed<<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+        case 1: k_adj_vertex<<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+        case 2: k_adj_springs<<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+const void* adjoint_seed_fn() { return (const void*)k_adj_seed; }
+
+cudaError_t launch_set_spring_params(const StepArgs& a, const AdjArgs& j, const float* ks, const float* kd,
+                                     int64_t n_rec, int64_t nv, cudaStream_t stream) {
+    k_set_spring_params<<<152 * 8, 256, 0, stream>>>(a, j, ks, kd, n_rec, nv);
+    return cudaGetLastError();
+}
+
+}  // namespace oc

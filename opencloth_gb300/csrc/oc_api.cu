@@ -27,6 +27,7 @@ struct oc_solver {
     bool use_graph = true;
     int32_t n_inst = 0;
     int64_t nv = 0, ns = 0;
+    int64_t n_inc = 0;  // incidence records (2 per spring)
     int32_t n_blocks = 0;
     int32_t vertices_per_block = 0;
     std::vector<int64_t> v_off;
@@ -43,6 +44,23 @@ struct oc_solver {
     BlockInfo* d_streamed_blocks = nullptr;
     int32_t n_streamed_blocks = 0;
     // Resident buckets run concurrently: forked from the handle's stream onto these.
+    // Differentiation: spring ids, own-spring incidence, gradient planes and the tape.
+    AdjArgs adj{};
+    float* d_ks = nullptr;  // per spring, for oc_set_spring_params
+    float* d_kd = nullptr;
+    size_t stride = 0;      // plane stride (vertices)
+    struct Tape {
+        int32_t n_steps = 0, every = 0, n_ck = 0;
+        float dt = 0.0f;
+        float4 *ckX = nullptr, *ckV = nullptr, *segX = nullptr, *segV = nullptr, *finX = nullptr, *finV = nullptr;
+        float *ckx = nullptr, *segdV = nullptr, *finx = nullptr;
+        float* planes = nullptr;  // gX 3, gV 3, gF 3, gOwn 6, gExt 3, dV 3
+        float* gK = nullptr;      // gKs, gKd
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        float graph_dt = 0.0f;
+        bool valid = false;
+    } tape;
     std::vector<cudaStream_t> aux;
     std::vector<cudaEvent_t> aux_done;
     cudaEvent_t fork_ev = nullptr;
@@ -103,6 +121,8 @@ void release(oc_solver* s) {
     if (s->h_state) cudaFreeHost(s->h_state);
     if (s->h_scalar) cudaFreeHost(s->h_scalar);
     if (s->h_loop) cudaFreeHost(s->h_loop);
+    if (s->tape.exec) cudaGraphExecDestroy(s->tape.exec);
+    if (s->tape.graph) cudaGraphDestroy(s->tape.graph);
     for (cudaStream_t x : s->aux) cudaStreamDestroy(x);
     for (cudaEvent_t e : s->aux_done) cudaEventDestroy(e);
     if (s->fork_ev) cudaEventDestroy(s->fork_ev);
@@ -380,6 +400,79 @@ bool resident_shape(int nv, int max_vertices, int* threads, int* cluster, int* v
 
 bool valid_solver(const oc_solver* s) { return s != nullptr && s->nv > 0; }
 
+// Copies of the state triple (X, V float4; the warm-start planes) between the solver
+// and a tape slot.
+oc_status copy_state(oc_solver* s, float4* dX, float4* dV, float* dx, const float4* sX, const float4* sV,
+                     const float* sx) {
+    const size_t n4 = sizeof(float4) * (size_t)s->nv;
+    OC_TRY(cudaMemcpyAsync(dX, sX, n4, cudaMemcpyDeviceToDevice, s->stream));
+    OC_TRY(cudaMemcpyAsync(dV, sV, n4, cudaMemcpyDeviceToDevice, s->stream));
+    if (dx && sx) OC_TRY(cudaMemcpyAsync(dx, sx, 3 * s->stride * sizeof(float), cudaMemcpyDeviceToDevice, s->stream));
+    return OC_OK;
+}
+
+float* xplanes(oc_solver* s) { return s->args.x[0]; }  // the three x planes are contiguous
+
+// The adjoint solve of one step as a graph: reset the loop counter, set up the CG on
+// the adjoint right-hand side (k_adj_seed), iterate (WHILE node) over every cloth.
+oc_status build_adjoint_graph(oc_solver* s, float dt) {
+    auto& T = s->tape;
+    if (T.exec) {
+        cudaGraphExecDestroy(T.exec);
+        T.exec = nullptr;
+    }
+    if (T.graph) {
+        cudaGraphDestroy(T.graph);
+        T.graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    OC_TRY(cudaGraphCreate(&g, 0));
+    T.graph = g;
+    cudaGraphConditionalHandle handle;
+    OC_TRY(cudaGraphConditionalHandleCreate(&handle, g, 0, 0));
+    StepArgs a = s->args;
+    a.dt = dt;
+    a.blk_base = 0;
+    a.use_cond = 1;
+    a.cond = (unsigned long long)handle;
+    a.all_streamed = 1;
+    AdjArgs j = s->adj;
+    void* params_seed[] = {&a, &j};
+    void* params_cg[] = {&a};
+    cudaGraphNode_t n_reset, n_seed, n_loop, n_dir, n_upd;
+    cudaMemsetParams mp{};
+    mp.dst = a.unconverged;
+    mp.value = 0;
+    mp.elementSize = sizeof(int32_t);
+    mp.width = 1;
+    mp.height = 1;
+    mp.pitch = sizeof(int32_t);
+    OC_TRY(cudaGraphAddMemsetNode(&n_reset, g, nullptr, 0, &mp));
+    cudaKernelNodeParams kp{};
+    kp.func = const_cast<void*>(adjoint_seed_fn());
+    kp.gridDim = dim3((unsigned)s->n_blocks);
+    kp.blockDim = dim3(256);
+    kp.kernelParams = params_seed;
+    OC_TRY(cudaGraphAddKernelNode(&n_seed, g, &n_reset, 1, &kp));
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    OC_TRY(cudaGraphAddNode(&n_loop, g, &n_seed, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    kp.func = const_cast<void*>(kernel_fn(K_CG_DIR));
+    kp.gridDim = dim3((unsigned)s->n_blocks);
+    kp.blockDim = dim3((unsigned)kernel_block_threads());
+    kp.kernelParams = params_cg;
+    OC_TRY(cudaGraphAddKernelNode(&n_dir, body, nullptr, 0, &kp));
+    kp.func = const_cast<void*>(kernel_fn(K_CG_UPDATE));
+    OC_TRY(cudaGraphAddKernelNode(&n_upd, body, &n_dir, 1, &kp));
+    OC_TRY(cudaGraphInstantiate(&T.exec, g, 0));
+    T.graph_dt = dt;
+    return OC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -451,6 +544,7 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     s->n_inst = P.n_inst;
     s->nv = P.nv;
     s->ns = P.ns;
+    s->n_inc = (int64_t)P.inc.size();
     s->v_off = P.v_off;
     s->inst_host = P.inst;
     s->ns_inst.resize(P.n_inst);
@@ -489,6 +583,18 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     a.own_ends = own_ends;
     a.own_par = own_par;
     const size_t stride = (size_t)((P.nv + 63) / 64) * 64;
+    s->stride = stride;
+    {
+        int32_t *inc_sid = nullptr, *own_sid = nullptr, *own_rowptr = nullptr, *own_ent = nullptr;
+        OC_CREATE_TRY(upload(s, &inc_sid, P.inc_sid));
+        OC_CREATE_TRY(upload(s, &own_sid, P.own_sid));
+        OC_CREATE_TRY(upload(s, &own_rowptr, P.own_rowptr));
+        OC_CREATE_TRY(upload(s, &own_ent, P.own_ent));
+        s->adj.inc_sid = inc_sid;
+        s->adj.own_sid = own_sid;
+        s->adj.own_rowptr = own_rowptr;
+        s->adj.own_ent = own_ent;
+    }
     float* planes = nullptr;
     OC_CREATE_TRY(dalloc(s, &planes, 15 * stride));
     OC_CREATE_TRY(cudaMemset(planes, 0, 15 * stride * sizeof(float)));
@@ -774,6 +880,217 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
         ++n;
     }
     if (n_kernels) *n_kernels = n;
+    return OC_OK;
+}
+
+oc_status oc_set_spring_params(oc_solver* s, const float* ks, const float* kd) {
+    if (!valid_solver(s) || (!ks && !kd)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    const size_t ns = (size_t)s->ns;
+    for (size_t k = 0; k < ns; ++k)
+        if ((ks && !std::isfinite(ks[k])) || (kd && !std::isfinite(kd[k])))
+            return fail(s, OC_ERR_NON_FINITE, "oc_set_spring_params: non-finite parameter");
+    if (!s->d_ks) {
+        OC_TRY(dalloc(s, &s->d_ks, ns));
+        OC_TRY(dalloc(s, &s->d_kd, ns));
+        // Current values, read back from the records through the spring ids.
+        std::vector<int4> rec(s->n_inc);
+        std::vector<int32_t> sid(s->n_inc);
+        OC_TRY(cudaMemcpy(rec.data(), s->args.inc, sizeof(int4) * s->n_inc, cudaMemcpyDeviceToHost));
+        OC_TRY(cudaMemcpy(sid.data(), s->adj.inc_sid, sizeof(int32_t) * s->n_inc, cudaMemcpyDeviceToHost));
+        std::vector<float> hk(ns), hd(ns);
+        for (int64_t k = 0; k < s->n_inc; ++k) {
+            std::memcpy(&hk[sid[k]], &rec[k].z, 4);
+            std::memcpy(&hd[sid[k]], &rec[k].w, 4);
+        }
+        OC_TRY(cudaMemcpy(s->d_ks, hk.data(), sizeof(float) * ns, cudaMemcpyHostToDevice));
+        OC_TRY(cudaMemcpy(s->d_kd, hd.data(), sizeof(float) * ns, cudaMemcpyHostToDevice));
+    }
+    if (ks) OC_TRY(cudaMemcpyAsync(s->d_ks, ks, sizeof(float) * ns, cudaMemcpyHostToDevice, s->stream));
+    if (kd) OC_TRY(cudaMemcpyAsync(s->d_kd, kd, sizeof(float) * ns, cudaMemcpyHostToDevice, s->stream));
+    OC_TRY(launch_set_spring_params(s->args, s->adj, s->d_ks, s->d_kd, s->n_inc, s->nv, s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    s->tape.valid = false;
+    return OC_OK;
+}
+
+oc_status oc_set_ext_force(oc_solver* s, const float* ext) {
+    if (!valid_solver(s) || !ext) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    const size_t n3 = 3 * (size_t)s->nv;
+    for (size_t k = 0; k < n3; ++k)
+        if (!std::isfinite(ext[k])) return fail(s, OC_ERR_NON_FINITE, "oc_set_ext_force: non-finite value");
+    std::vector<float4> f(s->nv);
+    for (int64_t g = 0; g < s->nv; ++g) f[g] = make_float4(ext[3 * g], ext[3 * g + 1], ext[3 * g + 2], 0.f);
+    if (!s->args.fext) {
+        float4* p = nullptr;
+        OC_TRY(dalloc(s, &p, (size_t)s->nv));
+        s->args.fext = p;
+    }
+    OC_TRY(cudaMemcpy(const_cast<float4*>(s->args.fext), f.data(), sizeof(float4) * s->nv, cudaMemcpyHostToDevice));
+    bool changed = false;
+    for (auto& ip : s->inst_host) {
+        changed |= ip.has_ext == 0;
+        ip.has_ext = 1;
+    }
+    if (changed) {
+        OC_TRY(cudaMemcpy(const_cast<InstParams*>(s->args.inst), s->inst_host.data(),
+                          sizeof(InstParams) * s->n_inst, cudaMemcpyHostToDevice));
+    }
+    // The step graph holds the old StepArgs; rebuild it on the next step.
+    if (s->exec) {
+        cudaGraphExecDestroy(s->exec);
+        s->exec = nullptr;
+    }
+    s->tape.valid = false;
+    return OC_OK;
+}
+
+oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t checkpoint_every, int64_t budget_bytes) {
+    if (!valid_solver(s) || n_steps < 1 || checkpoint_every < 0 || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    auto& T = s->tape;
+    const size_t state_bytes = 2 * sizeof(float4) * (size_t)s->nv + 3 * s->stride * sizeof(float);
+    int32_t every = checkpoint_every;
+    if (every == 0) every = std::max(1, (int32_t)std::ceil(std::sqrt((double)n_steps)));
+    every = std::min(every, n_steps);
+    const int32_t n_ck = (n_steps + every - 1) / every;
+    const double need = (double)state_bytes * (double)(n_ck + every + 1);
+    if (budget_bytes > 0 && need > (double)budget_bytes)
+        return fail(s, OC_ERR_OUT_OF_MEMORY, "oc_tape_forward: checkpoints need " + std::to_string(need) +
+                                                 " bytes, above the budget");
+    // (Re)allocate when the shape changed; buffers live until the handle is destroyed.
+    if (T.n_ck < n_ck || T.every < every || !T.ckX) {
+        float4* p4 = nullptr;
+        float* pf = nullptr;
+        OC_TRY(dalloc(s, &p4, (size_t)s->nv * n_ck)); T.ckX = p4;
+        OC_TRY(dalloc(s, &p4, (size_t)s->nv * n_ck)); T.ckV = p4;
+        OC_TRY(dalloc(s, &pf, 3 * s->stride * n_ck)); T.ckx = pf;
+        OC_TRY(dalloc(s, &p4, (size_t)s->nv * every)); T.segX = p4;
+        OC_TRY(dalloc(s, &p4, (size_t)s->nv * every)); T.segV = p4;
+        OC_TRY(dalloc(s, &pf, 3 * s->stride * every)); T.segdV = pf;
+        if (!T.finX) {
+            OC_TRY(dalloc(s, &p4, (size_t)s->nv)); T.finX = p4;
+            OC_TRY(dalloc(s, &p4, (size_t)s->nv)); T.finV = p4;
+            OC_TRY(dalloc(s, &pf, 3 * s->stride)); T.finx = pf;
+            OC_TRY(dalloc(s, &pf, 21 * s->stride)); T.planes = pf;
+            OC_TRY(dalloc(s, &pf, 2 * (size_t)s->ns + 2)); T.gK = pf;
+        }
+    }
+    T.n_steps = n_steps;
+    T.every = every;
+    T.n_ck = n_ck;
+    T.dt = dt;
+    for (int32_t t = 0; t < n_steps; ++t) {
+        if (t % every == 0) {
+            const int32_t c = t / every;
+            oc_status st = copy_state(s, T.ckX + (size_t)c * s->nv, T.ckV + (size_t)c * s->nv,
+                                      T.ckx + 3 * s->stride * c, s->args.X, s->args.V, xplanes(s));
+            if (st != OC_OK) return st;
+        }
+        oc_status st = oc_step(s, dt, 1);
+        if (st != OC_OK) return st;
+    }
+    oc_status st = copy_state(s, T.finX, T.finV, T.finx, s->args.X, s->args.V, xplanes(s));
+    if (st != OC_OK) return st;
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    T.valid = true;
+    return OC_OK;
+}
+
+oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV, float* dL_dX0, float* dL_dV0,
+                           float* dL_dKs, float* dL_dKd, float* dL_dext) {
+    if (!valid_solver(s) || !dL_dX) return OC_ERR_INVALID_ARGUMENT;
+    auto& T = s->tape;
+    if (!T.valid) return fail(s, OC_ERR_INVALID_ARGUMENT, "oc_tape_backward: no tape (run oc_tape_forward first)");
+    OC_TRY(cudaSetDevice(s->device));
+    const size_t st = s->stride, n3 = 3 * (size_t)s->nv;
+    AdjArgs& j = s->adj;
+    for (int k = 0; k < 3; ++k) {
+        j.gX[k] = T.planes + (0 + k) * st;
+        j.gV[k] = T.planes + (3 + k) * st;
+        j.gF[k] = T.planes + (6 + k) * st;
+        j.gExt[k] = T.planes + (15 + k) * st;
+        j.dV[k] = T.planes + (18 + k) * st;
+    }
+    for (int k = 0; k < 6; ++k) j.gOwn[k] = T.planes + (9 + k) * st;
+    j.gKs = T.gK;
+    j.gKd = T.gK + s->ns;
+    OC_TRY(cudaMemsetAsync(T.planes, 0, 21 * st * sizeof(float), s->stream));
+    OC_TRY(cudaMemsetAsync(T.gK, 0, (2 * (size_t)s->ns + 2) * sizeof(float), s->stream));
+    // dL/dX_T, dL/dV_T -> gX, gV planes (through the state upload kernel).
+    StepArgs up = s->args;
+    for (int k = 0; k < 3; ++k) up.x[k] = j.gX[k];
+    OC_TRY(cudaMemcpyAsync(s->stage, dL_dX, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    OC_TRY(launch_state_in(up, nullptr, nullptr, s->stage, s->nv, s->d_err, s->stream));
+    if (dL_dV) {
+        for (int k = 0; k < 3; ++k) up.x[k] = j.gV[k];
+        OC_TRY(cudaMemcpyAsync(s->stage + n3, dL_dV, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        OC_TRY(launch_state_in(up, nullptr, nullptr, s->stage + n3, s->nv, s->d_err, s->stream));
+    }
+    if (!T.exec || T.graph_dt != T.dt) {
+        oc_status r = build_adjoint_graph(s, T.dt);
+        if (r != OC_OK) return r;
+    }
+    StepArgs a = s->args;
+    a.dt = T.dt;
+    a.blk_base = 0;
+    a.use_cond = 0;
+    a.all_streamed = 1;
+    for (int32_t c = T.n_ck - 1; c >= 0; --c) {
+        const int32_t t0 = c * T.every, t1 = std::min(T.n_steps, t0 + T.every);
+        oc_status r = copy_state(s, s->args.X, s->args.V, xplanes(s), T.ckX + (size_t)c * s->nv,
+                                 T.ckV + (size_t)c * s->nv, T.ckx + 3 * st * c);
+        if (r != OC_OK) return r;
+        for (int32_t t = t0; t < t1; ++t) {  // recompute the segment, keeping every state
+            const int32_t q = t - t0;
+            if ((r = copy_state(s, T.segX + (size_t)q * s->nv, T.segV + (size_t)q * s->nv, nullptr, s->args.X,
+                                s->args.V, nullptr)) != OC_OK)
+                return r;
+            if ((r = oc_step(s, T.dt, 1)) != OC_OK) return r;
+            OC_TRY(cudaMemcpyAsync(T.segdV + 3 * st * q, xplanes(s), 3 * st * sizeof(float), cudaMemcpyDeviceToDevice,
+                                   s->stream));
+        }
+        for (int32_t t = t1 - 1; t >= t0; --t) {  // and walk it backwards
+            const int32_t q = t - t0;
+            if ((r = copy_state(s, s->args.X, s->args.V, nullptr, T.segX + (size_t)q * s->nv,
+                                T.segV + (size_t)q * s->nv, nullptr)) != OC_OK)
+                return r;
+            OC_TRY(cudaMemcpyAsync(const_cast<float*>(j.dV[0]), T.segdV + 3 * st * q, 3 * st * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, s->stream));
+            OC_TRY(launch_kernel(K_ASSEMBLE, a, s->n_blocks, s->stream));  // A of this step
+            OC_TRY(cudaGraphLaunch(T.exec, s->stream));                    // lambda = A^-1 g_dV
+            OC_TRY(launch_adjoint(1, a, j, s->n_blocks, s->stream));
+            OC_TRY(launch_adjoint(2, a, j, s->n_blocks, s->stream));
+        }
+    }
+    oc_status r = copy_state(s, s->args.X, s->args.V, xplanes(s), T.finX, T.finV, T.finx);
+    if (r != OC_OK) return r;
+    // Gradients out (planes -> packed triples through the state download kernel).
+    StepArgs dn = s->args;
+    auto planes_out = [&](float* const* pl, float* host) -> oc_status {
+        if (!host) return OC_OK;
+        for (int k = 0; k < 3; ++k) dn.x[k] = pl[k];
+        OC_TRY(launch_state_out(dn, nullptr, nullptr, s->stage, s->nv, s->stream));
+        OC_TRY(cudaMemcpyAsync(host, s->stage, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+        OC_TRY(cudaStreamSynchronize(s->stream));
+        return OC_OK;
+    };
+    if ((r = planes_out(j.gX, dL_dX0)) != OC_OK) return r;
+    if ((r = planes_out(j.gV, dL_dV0)) != OC_OK) return r;
+    if ((r = planes_out(j.gExt, dL_dext)) != OC_OK) return r;
+    if (dL_dKs) OC_TRY(cudaMemcpyAsync(dL_dKs, j.gKs, sizeof(float) * s->ns, cudaMemcpyDeviceToHost, s->stream));
+    if (dL_dKd) OC_TRY(cudaMemcpyAsync(dL_dKd, j.gKd, sizeof(float) * s->ns, cudaMemcpyDeviceToHost, s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    return OC_OK;
+}
+
+oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* tape_bytes) {
+    if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
+    const auto& T = s->tape;
+    const size_t state_bytes = 2 * sizeof(float4) * (size_t)s->nv + 3 * s->stride * sizeof(float);
+    if (checkpoint_every) *checkpoint_every = T.every;
+    if (tape_bytes) *tape_bytes = (int64_t)(state_bytes * (size_t)(T.n_ck + T.every + 1));
     return OC_OK;
 }
 

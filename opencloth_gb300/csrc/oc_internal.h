@@ -72,10 +72,32 @@ struct StepArgs {
     int32_t vpt;             // vertices per thread
     int32_t use_cond;        // 1: set the graph WHILE condition
     unsigned long long cond; // cudaGraphConditionalHandle
+    int32_t all_streamed;    // 1: every cloth's CG runs in the streamed loop (adjoint solves)
     float* dbg_F;            // optional debug outputs (float triples) or nullptr
     float* dbg_A9;
     float* dbg_b;
 };
+
+// Adjoint buffers (oc_adjoint.cu); planes have the handle's vertex stride.
+struct AdjArgs {
+    float* gX[3];
+    float* gV[3];
+    float* gF[3];
+    float* gOwn[6];          // spring i's Jacobian adjoint (dP 3, dV 3) at vertex i
+    float* gExt[3];
+    const float* dV[3];      // the step's solution dV
+    float* gKs;              // per spring (handle-global spring id)
+    float* gKd;
+    const int32_t* inc_sid;  // spring id of every incidence record
+    const int32_t* own_sid;  // vertex i -> id of spring i, or -1
+    const int32_t* own_rowptr;  // vertex -> vertices whose spring touches it
+    const int32_t* own_ent;     // that vertex | (1 << 31 when the vertex is the spring's p2)
+};
+
+cudaError_t launch_adjoint(int which, const StepArgs& a, const AdjArgs& j, int nblocks, cudaStream_t stream);
+const void* adjoint_seed_fn();
+cudaError_t launch_set_spring_params(const StepArgs& a, const AdjArgs& j, const float* ks, const float* kd,
+                                     int64_t n_rec, int64_t nv, cudaStream_t stream);
 
 enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3, K_FORCES = 4, K_RESIDENT = 5,
                   K_COUNT = 6 };
@@ -122,6 +144,9 @@ struct PackedHost {
     std::vector<float4> own_par;
     std::vector<BlockInfo> blocks;
     int32_t vertices_per_block = 0;
+    std::vector<int32_t> inc_sid;                     // spring id of every incidence record
+    std::vector<int32_t> own_sid;                     // vertex i -> id of spring i, or -1
+    std::vector<int32_t> own_rowptr, own_ent;         // vertex -> vertices whose spring touches it
 };
 
 oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vertices_per_block, PackedHost* out,

@@ -141,6 +141,9 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
     P.rowptr.assign(nv + 1, 0);
     for (int64_t g = 0; g < nv; ++g) P.rowptr[g + 1] = P.rowptr[g] + deg[g];
     P.inc.assign((size_t)P.rowptr[nv], make_int4(0, 0, 0, 0));
+    P.inc_sid.assign((size_t)P.rowptr[nv], 0);
+    P.own_sid.assign(nv, -1);
+    std::vector<int32_t> own_deg(nv, 0);
     std::vector<int32_t> cursor(P.rowptr.begin(), P.rowptr.end() - 1);
 
     for (int32_t k = 0; k < n; ++k) {
@@ -180,13 +183,30 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
             const oc_spring& sp = d.springs[s];
             const int32_t g1 = (int32_t)(vo + sp.p1), g2 = (int32_t)(vo + sp.p2);
             const int32_t rb = float_bits(sp.rest_length), kb = float_bits(sp.ks), db = float_bits(sp.kd);
+            const int32_t sid = (int32_t)(P.s_off[k] + s);
+            P.inc_sid[cursor[g1]] = sid;
             P.inc[cursor[g1]++] = make_int4(g2, rb, kb, db);
+            P.inc_sid[cursor[g2]] = sid;
             P.inc[cursor[g2]++] = make_int4((int32_t)((uint32_t)g1 | 0x80000000u), rb, kb, db);
             if (s < d.n_vertices) {
                 P.own_ends[vo + s] = make_int2(g1, g2);
                 P.own_par[vo + s] = make_float4(sp.rest_length, sp.ks, sp.kd, 0.f);
+                P.own_sid[vo + s] = sid;
+                ++own_deg[g1];
+                ++own_deg[g2];
             }
         }
+    }
+    // Vertex -> vertices whose own spring (spring i for vertex i) touches it, ordered by i.
+    P.own_rowptr.assign(nv + 1, 0);
+    for (int64_t g = 0; g < nv; ++g) P.own_rowptr[g + 1] = P.own_rowptr[g] + own_deg[g];
+    P.own_ent.assign((size_t)P.own_rowptr[nv], 0);
+    std::vector<int32_t> oc(P.own_rowptr.begin(), P.own_rowptr.end() - 1);
+    for (int64_t i = 0; i < nv; ++i) {
+        const int2 e = P.own_ends[i];
+        if (e.x < 0) continue;
+        P.own_ent[oc[e.x]++] = (int32_t)i;
+        P.own_ent[oc[e.y]++] = (int32_t)((uint32_t)i | 0x80000000u);
     }
     return OC_OK;
 }

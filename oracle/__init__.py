@@ -38,11 +38,11 @@ SPRING_DTYPE = np.dtype(
 def build(reference: bool = True) -> None:
     """Compile the port (always) and the reference harness (when the tree is present)."""
     BUILD.mkdir(exist_ok=True)
-    srcs = [HERE / "oc_oracle.c", HERE / "oc_oracle_impl.h", HERE / "oc_oracle.h"]
+    srcs = [HERE / "oc_oracle.c", HERE / "oc_oracle_impl.h", HERE / "oc_oracle.h", HERE / "oc_adjoint.c"]
     if not PORT_LIB.exists() or any(s.stat().st_mtime > PORT_LIB.stat().st_mtime for s in srcs):
         tmp = PORT_LIB.with_suffix(".so.tmp")
         subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
-                        str(HERE / "oc_oracle.c"), "-o", str(tmp), "-lm"], check=True)
+                        str(HERE / "oc_oracle.c"), str(HERE / "oc_adjoint.c"), "-o", str(tmp), "-lm"], check=True)
         os.replace(tmp, PORT_LIB)
     if reference:
         subprocess.run(["bash", str(HERE / "build_ref.sh")], check=True, capture_output=True)
@@ -74,6 +74,8 @@ def port() -> C.CDLL:
             f = getattr(lib, f"ocr_step_{sfx}")
             f.argtypes = [P, real, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
             f.restype = C.c_int
+        lib.ocr_adjoint_f64.argtypes = [P, C.c_double, C.c_int32] + [C.c_void_p] * 10
+        lib.ocr_adjoint_f64.restype = C.c_int
         _port = lib
     return _port
 
@@ -254,3 +256,27 @@ def ref_run(cloth: Cloth, num_x: int, num_y: int, X, V, dV=None, dt=1.0 / 60.0, 
         import json
         return res, json.loads(r.stdout.strip().splitlines()[-1])["seconds"]
     return res
+
+
+def port_adjoint(cloth: Cloth, X0, V0, gX_T, gV_T=None, dt=1.0 / 60.0, n_steps=1):
+    """FP64 adjoint (pin filter on).  Returns dict with X_T, V_T, gX0, gV0, gKs, gKd, gExt."""
+    lib = port()
+    n3 = 3 * cloth.n_vertices
+    X0 = np.ascontiguousarray(X0, np.float64).reshape(-1)
+    V0 = np.ascontiguousarray(V0, np.float64).reshape(-1)
+    gX_T = np.ascontiguousarray(gX_T, np.float64).reshape(-1)
+    gV = None if gV_T is None else np.ascontiguousarray(gV_T, np.float64).reshape(-1)
+    out = {k: np.zeros(n3) for k in ("X_T", "V_T", "gX0", "gV0", "gExt")}
+    out["gKs"] = np.zeros(len(cloth.springs))
+    out["gKd"] = np.zeros(len(cloth.springs))
+    p, keep = cloth.params(True, True)
+    rc = lib.ocr_adjoint_f64(C.byref(p), float(np.float32(dt)), int(n_steps), X0.ctypes.data, V0.ctypes.data,
+                             gX_T.ctypes.data, None if gV is None else gV.ctypes.data, out["X_T"].ctypes.data,
+                             out["V_T"].ctypes.data, out["gX0"].ctypes.data, out["gV0"].ctypes.data,
+                             out["gKs"].ctypes.data, out["gKd"].ctypes.data, out["gExt"].ctypes.data)
+    del keep
+    if rc != 0:
+        raise RuntimeError("oracle adjoint failed")
+    for k in ("X_T", "V_T", "gX0", "gV0", "gExt"):
+        out[k] = out[k].reshape(-1, 3)
+    return out

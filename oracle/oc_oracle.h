@@ -65,6 +65,14 @@ void ocr_assemble_f64(const ocr_params* p, double dt, const double* X, const dou
 int ocr_step_f64(const ocr_params* p, double dt, int32_t n_steps, double* X, double* V, double* dV,
                  int32_t* iters, double* rel_residual);
 
+/* FP64 adjoint of n_steps steps from (X0, V0) with a zero warm start (oc_adjoint.c):
+ * given dL/dX_T, dL/dV_T (NULL = 0), returns the final state and dL/dX0, dL/dV0,
+ * dL/dKs, dL/dKd (per spring) and dL/d(external force) (per vertex, constant in time).
+ * The linear solve is differentiated as an exact solve. */
+int ocr_adjoint_f64(const ocr_params* p, double dt, int32_t n_steps, const double* X0, const double* V0,
+                    const double* gX_T, const double* gV_T, double* X_T, double* V_T, double* gX0, double* gV0,
+                    double* gKs, double* gKd, double* gExt);
+
 #ifdef __cplusplus
 }
 #endif
