@@ -14,7 +14,7 @@ from opencloth_gb300 import ClothDesc, ClothSolver
 pytestmark = pytest.mark.gpu
 
 
-def gpu_grads(case, every=4, executor="auto", cg_tol=1e-6):
+def gpu_grads(case, every=10, executor="auto", cg_tol=1e-6):
     desc = ClothDesc(n_vertices=len(case["X"]), springs=case["springs"], pinned=case["pins"], cg_max_iter=500,
                      cg_tol=cg_tol)
     with ClothSolver(desc, executor=executor) as s:
@@ -31,7 +31,9 @@ def gpu_grads(case, every=4, executor="auto", cg_tol=1e-6):
 
 @pytest.fixture(scope="module")
 def case():
-    return make_case(cols=10, rows=8, steps=12, seed=5)
+    # 120 steps: enough motion that X_T - target (~1e-3) sits far above the FP32
+    # resolution of positions near y = 5 (~5e-7), which bounds the FP32 gradient's accuracy.
+    return make_case(cols=10, rows=8, steps=120, seed=5)
 
 
 @pytest.fixture(scope="module")
@@ -72,7 +74,7 @@ def test_gpu_adjoint_matches_central_differences(case, name, key):
 
 def test_checkpoint_interval_does_not_change_gradients(case):
     ga, _ = gpu_grads(case, every=1)
-    gb, _ = gpu_grads(case, every=5)
+    gb, _ = gpu_grads(case, every=7)
     gc, _ = gpu_grads(case, every=case["steps"])
     for k in ga:
         assert np.array_equal(ga[k], gb[k]) and np.array_equal(ga[k], gc[k]), k
@@ -94,7 +96,7 @@ def test_batched_adjoint_equals_solo(case):
     with ClothSolver(descs) as s:
         s.set_ext_force(np.concatenate([c["ext"] for c in cases]))
         s.set_state(np.concatenate([c["X"] for c in cases]), np.concatenate([c["V0"] for c in cases]))
-        s.tape_forward(DT, case["steps"], 4)
+        s.tape_forward(DT, case["steps"], 10)
         X, _, _ = s.get_state()
         off = s.offsets
         gX = np.concatenate([2.0 * (X[off[k]:off[k + 1]] - c["target"]) / len(c["X"]) for k, c in enumerate(cases)])
@@ -118,7 +120,7 @@ def test_torch_autograd_function(case):
         v0 = torch.tensor(case["V0"], requires_grad=True)
         ext = torch.tensor(case["ext"], requires_grad=True)
         target = torch.tensor(case["target"], dtype=torch.float32)
-        X = trajectory(s, case["X"], ks, kd, v0, ext, DT, case["steps"], 4)
+        X = trajectory(s, case["X"], ks, kd, v0, ext, DT, case["steps"], 10)
         loss = ((X - target) ** 2).sum(dim=1).mean()
         loss.backward()
         g, _ = gpu_grads(case)
@@ -126,6 +128,6 @@ def test_torch_autograd_function(case):
         # One gradient step on Ks lowers the loss.
         with torch.no_grad():
             ks2 = ks - 1e3 * ks.grad / max(float(ks.grad.abs().max()), 1e-30) * 1e-3 * ks
-        X2 = trajectory(s, case["X"], ks2, kd.detach(), v0.detach(), ext.detach(), DT, case["steps"], 4)
+        X2 = trajectory(s, case["X"], ks2, kd.detach(), v0.detach(), ext.detach(), DT, case["steps"], 10)
         loss2 = ((X2 - target) ** 2).sum(dim=1).mean()
         assert float(loss2) < float(loss)
