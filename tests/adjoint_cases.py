@@ -11,12 +11,12 @@ from opencloth_gb300 import grid_cloth
 DT = 1.0 / 60.0
 
 
-def make_case(cols=10, rows=8, steps=12, seed=0, ks_range=(10.0, 100.0)):
+def make_case(cols=10, rows=8, steps=12, seed=0, ks_range=(10.0, 100.0), v_sigma=0.02):
     rng = np.random.default_rng(seed)
     X, sp = grid_cloth(cols, rows, jitter=0.02, seed=seed + 1)
     sp["ks"] = np.exp(rng.uniform(np.log(ks_range[0]), np.log(ks_range[1]), len(sp))).astype(np.float32)
     sp["kd"] = rng.uniform(-0.5, -0.05, len(sp)).astype(np.float32)
-    V0 = rng.normal(0, 0.02, X.shape).astype(np.float32)
+    V0 = rng.normal(0, v_sigma, X.shape).astype(np.float32)
     V0[[0, cols - 1]] = 0.0
     ext = rng.normal(0, 0.005, X.shape).astype(np.float32)
     pins = np.array([0, cols - 1], np.int32)
@@ -60,3 +60,26 @@ def fd_direction(case, name, u, rel_eps=1e-4):
     lp = loss_fp64(case, **kw)
     kw = {name: m}
     return lp - loss_fp64(case, **kw), d
+
+
+def fd_joint(case, u, rel_eps=1e-4):
+    """FP64 central difference along a joint direction u = (ks, kd, V0, ext); returns
+    (difference, the exact float32 perturbations applied, keyed like u)."""
+    sp_p, sp_m = case["springs"].copy(), case["springs"].copy()
+    d = {}
+    for name in ("ks", "kd"):
+        base = case["springs"][name].astype(np.float64)
+        sp_p[name] = (base * (1 + rel_eps * u[name])).astype(np.float32)
+        sp_m[name] = (base * (1 - rel_eps * u[name])).astype(np.float32)
+        d[name] = sp_p[name].astype(np.float64) - sp_m[name].astype(np.float64)
+    vals = {}
+    for name in ("V0", "ext"):
+        base = case[name].astype(np.float64)
+        scale = rel_eps * max(np.abs(base).max(), 1e-3)
+        p = (base + scale * u[name]).astype(np.float32)
+        m = (base - scale * u[name]).astype(np.float32)
+        d[name] = p.astype(np.float64) - m.astype(np.float64)
+        vals[name] = (p, m)
+    lp = loss_fp64(case, springs=sp_p, V0=vals["V0"][0], ext=vals["ext"][0])
+    lm = loss_fp64(case, springs=sp_m, V0=vals["V0"][1], ext=vals["ext"][1])
+    return lp - lm, d
