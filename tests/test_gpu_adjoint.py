@@ -148,7 +148,7 @@ def test_torch_autograd_function(case):
         assert np.allclose(ks.grad.numpy(), g["dKs"], rtol=1e-5, atol=1e-12)
         # One gradient step on Ks lowers the loss.
         with torch.no_grad():
-            ks2 = ks - 1e3 * ks.grad / max(float(ks.grad.abs().max()), 1e-30) * 1e-3 * ks
+            ks2 = ks * (1.0 - 1e-3 * ks.grad / max(float(ks.grad.abs().max()), 1e-30))
         X2 = trajectory(s, case["X"], ks2, kd.detach(), v0.detach(), ext.detach(), DT, case["steps"], 10)
         loss2 = ((X2.double() - target) ** 2).sum(dim=1).mean()
         assert float(loss2) < float(loss)
