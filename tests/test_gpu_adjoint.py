@@ -1,12 +1,13 @@
 """GPU adjoint of the implicit step (oc_tape_forward / oc_tape_backward).
 
-Tolerances: the GPU runs the forward in FP32 with the CG to 1e-6.  Against FP64 central
-differences (eps 1e-4 relative) of the same method, directional derivatives agree within
-1e-3 relative for Ks, the initial velocity, the external force and a joint direction over
-those three.  Kd is held to 1e-2: it acts through u = (dV.dP)/L, whose relative spring
-velocity dV = V1 - V2 is a difference of nearly equal FP32 velocities, so the FP32 model
-resolves the loss's Kd-sensitivity only to about that.  Gradient vectors agree with the
-FP64 CPU adjoint within 1e-2 in norm.
+Tolerance: the GPU runs the forward in FP32 with the CG to 1e-6; against FP64 central
+differences (eps 1e-4 relative) of the same method, directional derivatives for Ks, Kd,
+the initial velocity, the external force and joint directions agree within 1e-3
+relative (the spec bar).  What limits the agreement is the FP32 final state: an
+exact FP64 adjoint seeded with the GPU's final positions shows the same error, so the
+case is a 200-step trajectory whose loss residual X_T - target (~7e-3) sits far above
+FP32 position resolution near y = 5 (~5e-7).  Gradient vectors agree with the FP64 CPU
+adjoint within 1e-2 in norm.
 """
 import numpy as np
 import pytest
@@ -35,9 +36,7 @@ def gpu_grads(case, every=10, executor="auto", cg_tol=1e-6):
 
 @pytest.fixture(scope="module")
 def case():
-    # 120 steps: enough motion that X_T - target (~1e-3) sits far above the FP32
-    # resolution of positions near y = 5 (~5e-7), which bounds the FP32 gradient's accuracy.
-    return make_case(cols=10, rows=8, steps=120, seed=5, v_sigma=0.1)
+    return make_case(cols=10, rows=8, steps=200, seed=5, v_sigma=0.1)
 
 
 @pytest.fixture(scope="module")
@@ -73,8 +72,7 @@ def test_gpu_adjoint_matches_central_differences(case, name, key):
         u = rng.normal(size=shape)
         fd, d = fd_direction(case, name, u)
         ad = float(np.sum(g[key].astype(np.float64).reshape(d.shape) * d))
-        tol = 1e-2 if name == "kd" else 1e-3
-        assert abs(fd - ad) <= tol * abs(fd), (name, fd, ad)
+        assert abs(fd - ad) <= 1e-3 * abs(fd), (name, fd, ad)
 
 
 def test_gpu_adjoint_joint_direction_central_differences(case):
@@ -82,10 +80,9 @@ def test_gpu_adjoint_joint_direction_central_differences(case):
 
     g, _ = gpu_grads(case)
     rng = np.random.default_rng(12)
-    # Kd is left out of the joint direction: its own tolerance is 1e-2 (see the module docstring).
     keys = {"ks": "dKs", "kd": "dKd", "V0": "dV0", "ext": "dext"}
     for _ in range(4):
-        u = {"ks": rng.normal(size=case["springs"].shape), "kd": np.zeros(case["springs"].shape),
+        u = {"ks": rng.normal(size=case["springs"].shape), "kd": rng.normal(size=case["springs"].shape),
              "V0": rng.normal(size=case["X"].shape), "ext": rng.normal(size=case["X"].shape)}
         fd, d = fd_joint(case, u)
         ad = sum(float(np.sum(g[keys[k]].astype(np.float64).reshape(d[k].shape) * d[k])) for k in keys)
@@ -94,7 +91,7 @@ def test_gpu_adjoint_joint_direction_central_differences(case):
 
 def test_checkpoint_interval_does_not_change_gradients(case):
     ga, _ = gpu_grads(case, every=1)
-    gb, _ = gpu_grads(case, every=7)
+    gb, _ = gpu_grads(case, every=13)
     gc, _ = gpu_grads(case, every=case["steps"])
     for k in ga:
         assert np.array_equal(ga[k], gb[k]) and np.array_equal(ga[k], gc[k]), k
