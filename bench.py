@@ -361,6 +361,81 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
     }
 
 
+def adjoint_workload(name: str, seed: int):
+    """The differentiable configurations: one 257 x 257 cloth (200 steps, checkpoint every
+    20) and 512 cloths with sides uniform in [16,256] (100 steps, checkpoints chosen
+    under a 40 GB budget).  Targets are final positions of a run whose per-spring Ks carry
+    log-normal(0, 0.1^2) factors; the loss is the mean squared distance to them."""
+    from opencloth_gb300 import ClothDesc, grid_cloth
+
+    rng = np.random.default_rng(seed)
+    if name == "grid257":
+        sides, steps, every = [257], 200, 20
+    else:
+        sides, steps, every = list(rng.integers(16, 257, 512)), 100, 0
+    descs, Xs, ks_t = [], [], []
+    for k, n in enumerate(sides):
+        n = int(n)
+        if name == "grid257":
+            ks, kd = (50.75, 50.75, 50.95), (-0.25, -0.25, -0.25)
+        else:
+            ks, kd = tuple(np.exp(rng.uniform(np.log(10.0), np.log(500.0), 3))), tuple(rng.uniform(-0.5, -0.05, 3))
+        X, sp = grid_cloth(n, n, ks=ks, kd=kd, jitter=1e-3, seed=seed * 7 + k)
+        descs.append(ClothDesc(n_vertices=n * n, springs=sp, pinned=np.array([0, n - 1], np.int32),
+                               cg_max_iter=200, cg_tol=1e-5))
+        Xs.append(X)
+        ks_t.append((sp["ks"] * np.exp(rng.normal(0.0, 0.1, len(sp)))).astype(np.float32))
+    return descs, np.concatenate(Xs), np.concatenate(ks_t), steps, every
+
+
+def measure_adjoint(name: str, seed: int, local: int) -> dict:
+    """Forward, taped forward and reverse pass times of one gradient evaluation."""
+    import torch
+
+    from opencloth_gb300 import ClothSolver
+
+    descs, X0, ks_target, steps, every = adjoint_workload(name, seed)
+    nv = len(X0)
+    budget = 40 << 30
+    with ClothSolver(descs, device=local) as s:
+        ks0 = np.concatenate([d.springs["ks"] for d in descs])
+        s.set_spring_params(ks=ks_target)
+        s.set_state(X0, np.zeros_like(X0), np.zeros_like(X0))
+        s.step(DT, steps)
+        target, _, _ = s.get_state()
+        s.set_spring_params(ks=ks0)
+
+        def reset():
+            s.set_state(X0, np.zeros_like(X0), np.zeros_like(X0))
+            s.synchronize()
+
+        reset()
+        t0 = time.perf_counter()
+        s.step(DT, steps)
+        s.synchronize()
+        fwd = time.perf_counter() - t0
+        reset()
+        t0 = time.perf_counter()
+        s.tape_forward(DT, steps, every, budget)
+        tape = time.perf_counter() - t0
+        X, _, _ = s.get_state()
+        offs = s.offsets
+        gX = np.empty_like(X)
+        for k in range(len(descs)):
+            sl = slice(offs[k], offs[k + 1])
+            gX[sl] = 2.0 * (X[sl] - target[sl]) / (offs[k + 1] - offs[k])
+        t0 = time.perf_counter()
+        g = s.tape_backward(gX)
+        bwd = time.perf_counter() - t0
+        every_used, tape_bytes = s.tape_info()
+    torch.cuda.synchronize()
+    return {"vertices": nv, "instances": len(descs), "steps": steps, "checkpoint_every": every_used,
+            "tape_bytes": tape_bytes, "forward_ms": 1e3 * fwd, "taped_forward_ms": 1e3 * tape,
+            "backward_ms": 1e3 * bwd, "backward_to_forward": bwd / fwd, "gradient_to_forward": (tape + bwd) / fwd,
+            "gradients_per_s": len(descs) / (tape + bwd),
+            "grad_norm_ks": float(np.linalg.norm(g["dKs"])), "finite": bool(np.isfinite(g["dKs"]).all())}
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -396,6 +471,8 @@ def run_ours(args) -> None:
             "plain_gpu": r["plain_gpu"],
             "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cores, "kind": kind, "sample": sample},
         }
+        if args.workload == "all":
+            line["adjoint"] = {n: measure_adjoint(n, args.seed, local) for n in ("grid257", "batch512")}
         for b in results[1:]:
             line[b["name"]] = {
                 "value": b["value"], "unit": METRIC, "ms_per_step": b["ms_per_step"], "steps": b["steps"],
