@@ -88,7 +88,22 @@ typedef struct oc_cloth_desc {
     int32_t cg_max_iter;       /* i_max, IMP:128; at most OC_MAX_CG_ITER */
     float cg_tol;              /* EPS, IMP:126; the CG stops when r.r <= EPS^2 * delta0 */
     int32_t jacobian_mode;     /* OC_JAC_* */
+    /* Passes after the update, in StepPhysics' order (IMP:873-880); 0 = none, i.e.
+     * ComputeForces + IntegrateImplicit only.  Stepping only: oc_tape_forward refuses them. */
+    int32_t passes;            /* OC_PASS_* bits */
+    float ellipsoid[16];       /* OC_PASS_ELLIPSOID: object -> world, column-major (IMP:583-585) */
+    float ellipsoid_inv[16];   /* its inverse as the caller computed it (IMP:586) */
+    float provot_ratio;        /* OC_PASS_PROVOT: stretch limit over rest length; 0 -> 1.01 (IMP:808) */
 } oc_cloth_desc;
+
+/* ---- passes after the update ------------------------------------------------------- */
+/* EllipsoidCollision (IMP:824-848): a vertex inside the unit sphere of the ellipsoid's
+ * object space is moved to its surface and its velocity zeroed (pinned vertices too). */
+#define OC_PASS_ELLIPSOID 1
+/* ApplyProvotDynamicInverse (IMP:800-823): a spring longer than provot_ratio x rest moves
+ * its endpoints' velocities together by half the excess; a pinned p1 leaves the whole
+ * correction to p2, else a pinned p2 leaves it to p1. */
+#define OC_PASS_PROVOT 2
 
 /* ---- executors ---------------------------------------------------------------------- */
 #define OC_EXEC_AUTO 0     /* resident kernels for instances that fit on chip, streamed otherwise */
@@ -131,10 +146,18 @@ oc_status oc_get_state(oc_solver* s, float* X, float* V, float* dV);
 oc_status oc_set_state_device(oc_solver* s, const float* X, const float* V, const float* dV);
 oc_status oc_get_state_device(oc_solver* s, float* X, float* V, float* dV);
 
-/* n_steps x { ComputeForces(); IntegrateImplicit(dt); } for every instance.
+/* n_steps x { ComputeForces(); IntegrateImplicit(dt); [passes] } for every instance.
  * Asynchronous: enqueued on the handle's stream. */
 oc_status oc_step(oc_solver* s, float dt, int32_t n_steps);
 oc_status oc_synchronize(oc_solver* s);
+/* Set the passes after the update (OC_PASS_* bits) of one cloth (instance >= 0) or of
+ * every cloth (-1); the matrices and ratio stay those given at oc_create.  Waits for the
+ * handle's stream; the next oc_step rebuilds its graph. */
+oc_status oc_set_passes(oc_solver* s, int32_t instance, int32_t passes);
+/* Run the given passes once on the current state of every cloth, ellipsoid first, with
+ * no step: the reference's EllipsoidCollision (IMP:824) and ApplyProvotDynamicInverse
+ * (IMP:800) called on their own.  Asynchronous on the handle's stream. */
+oc_status oc_apply_passes(oc_solver* s, int32_t passes);
 
 /* Per-instance results of the last step: CG iterations, relative residual
  * sqrt(delta_new / delta0), OC_FLAG_* bits.  Any pointer may be NULL. */
@@ -170,7 +193,8 @@ oc_status oc_set_spring_params(oc_solver* s, const float* ks, const float* kd);
 oc_status oc_set_ext_force(oc_solver* s, const float* ext);
 /* Run n_steps steps from the current state keeping a checkpoint of (X, V, dV) every
  * checkpoint_every steps (0: about sqrt(n_steps)); fails with OC_ERR_OUT_OF_MEMORY when
- * the checkpoints would exceed budget_bytes (0: no limit). */
+ * the checkpoints would exceed budget_bytes (0: no limit), with OC_ERR_UNSUPPORTED when a
+ * cloth has passes after the update (the adjoint covers the implicit step only). */
 oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t checkpoint_every, int64_t budget_bytes);
 /* Reverse pass of the last oc_tape_forward: given dL/dX and dL/dV (NULL = 0) of its final
  * state, returns dL/dX0, dL/dV0 (initial state), dL/dKs, dL/dKd (per spring) and dL/dext

@@ -34,6 +34,7 @@ FLAG_NON_FINITE = 4
 
 EXEC_AUTO, EXEC_STREAMED, EXEC_RESIDENT, EXEC_PLAIN = 0, 1, 2, 3
 JAC_REFERENCE, JAC_COUPLED = 0, 1
+PASS_ELLIPSOID, PASS_PROVOT = 1, 2
 
 
 class Spring(C.Structure):
@@ -55,6 +56,10 @@ class ClothDescC(C.Structure):
         ("cg_max_iter", C.c_int32),
         ("cg_tol", C.c_float),
         ("jacobian_mode", C.c_int32),
+        ("passes", C.c_int32),
+        ("ellipsoid", C.c_float * 16),
+        ("ellipsoid_inv", C.c_float * 16),
+        ("provot_ratio", C.c_float),
     ]
 
 
@@ -86,6 +91,8 @@ SIGNATURES = {
     "oc_get_state_device": (C.c_int32, [_P, _P, _P, _P]),
     "oc_step": (C.c_int32, [_P, C.c_float, C.c_int32]),
     "oc_synchronize": (C.c_int32, [_P]),
+    "oc_set_passes": (C.c_int32, [_P, C.c_int32, C.c_int32]),
+    "oc_apply_passes": (C.c_int32, [_P, C.c_int32]),
     "oc_get_stats": (C.c_int32, [_P, _P, _P, _P]),
     "oc_get_launch_count": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
     "oc_compute_forces": (C.c_int32, [_P, _P]),

@@ -49,6 +49,13 @@ class ClothDesc:
     cg_max_iter: int = 10  # IMP:128
     cg_tol: float = 1e-3  # IMP:126
     jacobian_mode: int = N.JAC_REFERENCE
+    # Passes after the update (PASS_ELLIPSOID | PASS_PROVOT), StepPhysics' order
+    # (IMP:873-880).  The ellipsoid: object -> world 4x4 and its inverse, 16 floats
+    # column-major (m[c][r] at 4c + r, glm's layout); ``reference_ellipsoid()`` builds them.
+    passes: int = 0
+    ellipsoid: np.ndarray | None = None
+    ellipsoid_inv: np.ndarray | None = None
+    provot_ratio: float = 1.01  # IMP:808
     _keep: list = field(default_factory=list, repr=False)
 
     def to_c(self) -> N.ClothDescC:
@@ -70,7 +77,34 @@ class ClothDesc:
         d.cg_max_iter = int(self.cg_max_iter)
         d.cg_tol = float(self.cg_tol)
         d.jacobian_mode = int(self.jacobian_mode)
+        d.passes = int(self.passes)
+        if self.ellipsoid is not None:
+            d.ellipsoid[:] = [float(v) for v in np.asarray(self.ellipsoid, np.float32).ravel()]
+            inv = self.ellipsoid_inv
+            if inv is None:
+                inv = np.linalg.inv(column_major(self.ellipsoid).astype(np.float64)).astype(np.float32).T
+            d.ellipsoid_inv[:] = [float(v) for v in np.asarray(inv, np.float32).ravel()]
+        d.provot_ratio = float(self.provot_ratio)
         return d
+
+
+def column_major(m) -> np.ndarray:
+    """16 column-major floats -> the 4x4 matrix they hold (row index first)."""
+    return np.asarray(m, np.float32).reshape(4, 4).T
+
+
+def reference_ellipsoid():
+    """The reference's ellipsoid (InitGL, IMP:583-586): translate (0, 2, 0), rotate 45
+    degrees about x, scale (1, 1, 0.5), and its inverse; 16 floats each, column-major.
+    Computed in float64 and rounded, so an element may differ from glm's FP32 product by
+    an ulp."""
+    c, s_ = np.cos(np.radians(45.0)), np.sin(np.radians(45.0))
+    T = np.eye(4)
+    T[1, 3] = 2.0
+    R = np.array([[1, 0, 0, 0], [0, c, -s_, 0], [0, s_, c, 0], [0, 0, 0, 1]], np.float64)
+    S = np.diag([1.0, 1.0, 0.5, 1.0])
+    M = T @ R @ S
+    return (M.T.ravel().astype(np.float32), np.linalg.inv(M).T.ravel().astype(np.float32))
 
 
 def grid_spring_count(cols: int, rows: int) -> int:
@@ -191,6 +225,15 @@ class ClothSolver:
     def synchronize(self) -> None:
         self._call(self._lib.oc_synchronize(self._h))
 
+    def set_passes(self, passes: int, instance: int = -1) -> None:
+        """Passes after the update (PASS_* bits) of one cloth, or of all (-1)."""
+        self._call(self._lib.oc_set_passes(self._h, int(instance), int(passes)))
+
+    def apply_passes(self, passes: int) -> None:
+        """Run the passes once on the current state, no step (EllipsoidCollision,
+        ApplyProvotDynamicInverse called on their own)."""
+        self._call(self._lib.oc_apply_passes(self._h, int(passes)))
+
     def stats(self):
         it = np.zeros(self.n_instances, np.int32)
         rr = np.zeros(self.n_instances, np.float64)
@@ -278,7 +321,8 @@ class ImplicitCloth:
 
     def __init__(self, X: np.ndarray, V: np.ndarray | None = None, pinned: Sequence[int] | None = None,
                  gravity=DEFAULT_GRAVITY, velocity_damping: float = DEFAULT_DAMPING, mass=None,
-                 cg_max_iter: int = 10, cg_tol: float = 1e-3, executor: str = "auto"):
+                 cg_max_iter: int = 10, cg_tol: float = 1e-3, executor: str = "auto", ellipsoid=None,
+                 ellipsoid_inv=None):
         self.X = np.ascontiguousarray(X, np.float32).reshape(-1, 3).copy()
         self.V = np.zeros_like(self.X) if V is None else np.ascontiguousarray(V, np.float32).reshape(-1, 3).copy()
         self.dV = np.zeros_like(self.X)
@@ -291,8 +335,13 @@ class ImplicitCloth:
         self.cg_max_iter = int(cg_max_iter)
         self.cg_tol = float(cg_tol)
         self.executor = executor
+        if ellipsoid is None:
+            ellipsoid, ellipsoid_inv = reference_ellipsoid()
+        self.ellipsoid = np.asarray(ellipsoid, np.float32).ravel()
+        self.ellipsoid_inv = None if ellipsoid_inv is None else np.asarray(ellipsoid_inv, np.float32).ravel()
         self._solver: ClothSolver | None = None
         self._springs_seen = None
+        self._passes = 0
 
     def AddSpring(self, a: int, b: int, ks: float, kd: float, type: int) -> None:  # noqa: N802 (reference name)
         d = self.X[a] - self.X[b]
@@ -307,10 +356,27 @@ class ImplicitCloth:
                 self._solver.close()
             desc = ClothDesc(n_vertices=self.X.shape[0], springs=self.springs, pinned=self.pinned,
                              mass=self.mass, gravity=self.gravity, velocity_damping=self.velocity_damping,
-                             cg_max_iter=self.cg_max_iter, cg_tol=self.cg_tol)
+                             cg_max_iter=self.cg_max_iter, cg_tol=self.cg_tol, ellipsoid=self.ellipsoid,
+                             ellipsoid_inv=self.ellipsoid_inv)
             self._solver = ClothSolver(desc, executor=self.executor)
             self._springs_seen = key
+            self._passes = 0
         return self._solver
+
+    def _step(self, dt: float, passes: int) -> None:
+        s = self._handle()
+        if self._passes != passes:
+            s.set_passes(passes)
+            self._passes = passes
+        s.set_state(self.X, self.V, self.dV)
+        s.step(dt, 1)
+        self.X, self.V, self.dV = s.get_state()
+
+    def _apply(self, passes: int) -> None:
+        s = self._handle()
+        s.set_state(self.X, self.V, self.dV)
+        s.apply_passes(passes)
+        self.X, self.V, self.dV = s.get_state()
 
     def ComputeForces(self) -> np.ndarray:  # noqa: N802
         s = self._handle()
@@ -319,11 +385,15 @@ class ImplicitCloth:
         return self.F
 
     def IntegrateImplicit(self, dt: float) -> None:  # noqa: N802
-        s = self._handle()
-        s.set_state(self.X, self.V, self.dV)
-        s.step(dt, 1)
-        self.X, self.V, self.dV = s.get_state()
+        self._step(dt, 0)
+
+    def EllipsoidCollision(self) -> None:  # noqa: N802 (IMP:824)
+        self._apply(N.PASS_ELLIPSOID)
+
+    def ApplyProvotDynamicInverse(self) -> None:  # noqa: N802 (IMP:800)
+        self._apply(N.PASS_PROVOT)
 
     def StepPhysics(self, dt: float) -> None:  # noqa: N802
-        """ComputeForces(); IntegrateImplicit(dt); (IMP:873-876)."""
-        self.IntegrateImplicit(dt)
+        """ComputeForces(); IntegrateImplicit(dt); EllipsoidCollision();
+        ApplyProvotDynamicInverse(); (IMP:873-880), as one step on the device."""
+        self._step(dt, N.PASS_ELLIPSOID | N.PASS_PROVOT)

@@ -43,6 +43,8 @@ struct oc_solver {
     std::vector<uint8_t> resident;  // per instance
     BlockInfo* d_streamed_blocks = nullptr;
     int32_t n_streamed_blocks = 0;
+    bool any_provot = false;  // some cloth has OC_PASS_PROVOT: k_provot follows the update
+    bool any_passes = false;  // some cloth has a pass after the update
     // Resident buckets run concurrently: forked from the handle's stream onto these.
     // Differentiation: spring ids, own-spring incidence, gradient planes and the tape.
     AdjArgs adj{};
@@ -73,7 +75,7 @@ struct oc_solver {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     float graph_dt = 0.0f;
-    int64_t host_launches = 0;  // k_assemble + k_integrate launches enqueued
+    int64_t host_launches = 0;  // k_assemble, k_integrate, k_resident, k_provot launches enqueued
     unsigned long long* h_loop = nullptr;
     std::string err;
 };
@@ -142,12 +144,15 @@ struct KernelTimer {
 // Algorithmic bytes of one step, from each instance's CG iteration count: every array
 // element a kernel must read or write counted once, in the device layout (X/V float4,
 // 16-byte incidence records, FP32 planes).  Per vertex: k_assemble 120 B plus 32 B per
-// spring, first k_cg_dir pass 36 B, later passes 60 B, k_cg_update 84 B, k_integrate 76 B.
+// spring, first k_cg_dir pass 36 B, later passes 60 B, k_cg_update 84 B, k_integrate 76 B
+// (the ellipsoid pass adds no traffic), k_provot 53 B plus 32 B per spring.
 void account_step_bytes(const oc_solver* s, KernelTimer* t) {
     for (int32_t k = 0; k < s->n_inst; ++k) {
         const double nv = (double)s->inst_host[k].nv, ns = (double)s->ns_inst[k];
         const InstState& st = s->h_state[k];
         t->bytes[K_ASSEMBLE] += 120.0 * nv + 32.0 * ns;
+        // k_provot: X 16, V 32 in and out, pin flag 1, row pointer 4; 16-byte records.
+        if (s->inst_host[k].passes & OC_PASS_PROVOT) t->bytes[K_PROVOT] += 53.0 * nv + 32.0 * ns;
         if (s->resident[k]) {
             // CG state in (A 24 + x, r, d 36), X, V 32 in and out, dV 12 out; the CG
             // iterations run in shared memory.
@@ -224,7 +229,7 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
             a.blk_base = s->inst_host[grp].blk0;
             const int nb = s->inst_host[grp].nblk;
             if ((st = launch_timed(s, K_ASSEMBLE, a, nb, t)) != OC_OK) return st;
-            s->host_launches += 2;
+            s->host_launches += s->any_provot ? 3 : 2;
             for (;;) {
                 OC_TRY(cudaMemcpyAsync(s->h_scalar, &s->args.state[grp].active, sizeof(int32_t),
                                        cudaMemcpyDeviceToHost, s->stream));
@@ -234,6 +239,7 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
                 if ((st = launch_timed(s, K_CG_UPDATE, a, nb, t)) != OC_OK) return st;
             }
             if ((st = launch_timed(s, K_INTEGRATE, a, nb, t)) != OC_OK) return st;
+            if (s->any_provot && (st = launch_timed(s, K_PROVOT, a, nb, t)) != OC_OK) return st;
         }
     } else {
         // Assembly over every cloth, then the resident CG launches and the streamed loop.
@@ -254,6 +260,10 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
                 if ((st = launch_timed(s, K_CG_UPDATE, sa, nb, t)) != OC_OK) return st;
             }
             if ((st = launch_timed(s, K_INTEGRATE, sa, nb, t)) != OC_OK) return st;
+            s->host_launches += 1;
+        }
+        if (s->any_provot) {  // after every cloth's update, resident and streamed
+            if ((st = launch_timed(s, K_PROVOT, a, s->n_blocks, t)) != OC_OK) return st;
             s->host_launches += 1;
         }
     }
@@ -315,6 +325,7 @@ oc_status build_graph(oc_solver* s, float dt) {
     OC_TRY(cudaGraphAddMemsetNode(&n_reset, g, nullptr, 0, &mp));
     cudaKernelNodeParams kp = kparams(K_ASSEMBLE, true);
     OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &n_reset, 1, &kp));
+    std::vector<cudaGraphNode_t> updates;  // the nodes that write X and V
 
     if (streamed) {
         cudaGraphNode_t n_loop, n_dir, n_upd, n_int;
@@ -331,6 +342,7 @@ oc_status build_graph(oc_solver* s, float dt) {
         OC_TRY(cudaGraphAddKernelNode(&n_upd, body, &n_dir, 1, &kp));
         kp = kparams(K_INTEGRATE, false);
         OC_TRY(cudaGraphAddKernelNode(&n_int, g, &n_loop, 1, &kp));
+        updates.push_back(n_int);
     }
     if (!s->buckets.empty()) {
         // The resident CG launches (concurrent, fork/join) captured into a child graph that
@@ -352,6 +364,12 @@ oc_status build_graph(oc_solver* s, float dt) {
         cudaError_t e = cudaGraphAddChildGraphNode(&n_res, g, &n_asm, 1, rg);
         cudaGraphDestroy(rg);
         if (e != cudaSuccess) return fail_cuda(s, e, "cudaGraphAddChildGraphNode");
+        updates.push_back(n_res);
+    }
+    if (s->any_provot) {
+        cudaGraphNode_t n_prov;
+        kp = kparams(K_PROVOT, true);
+        OC_TRY(cudaGraphAddKernelNode(&n_prov, g, updates.data(), updates.size(), &kp));
     }
     OC_TRY(cudaGraphInstantiate(&s->exec, g, 0));
     s->graph_dt = dt;
@@ -613,6 +631,15 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     BlockInfo* blocks = nullptr;
     OC_CREATE_TRY(upload(s, &blocks, P.blocks));
     a.blocks = blocks;
+    for (const InstParams& ip : P.inst) s->any_passes = s->any_passes || ip.passes != 0;
+    s->any_provot = P.any_provot;
+    {
+        std::vector<uint8_t> pins((size_t)P.nv);
+        for (int64_t g = 0; g < P.nv; ++g) pins[g] = P.V0[g].w != 0.0f ? 1 : 0;
+        uint8_t* d_pins = nullptr;
+        OC_CREATE_TRY(upload(s, &d_pins, pins));
+        a.pinflag = d_pins;
+    }
 
     // Which cloths run resident (one cluster per cloth, the whole step on chip) and
     // which run streamed; resident cloths are grouped by launch shape.
@@ -782,7 +809,55 @@ oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
         if (st != OC_OK) return st;
     }
     for (int32_t i = 0; i < n_steps; ++i) OC_TRY(cudaGraphLaunch(s->exec, s->stream));
-    s->host_launches += (1 + (s->n_streamed_blocks > 0 ? 1 : 0) + (int64_t)s->buckets.size()) * (int64_t)n_steps;
+    s->host_launches += (1 + (s->n_streamed_blocks > 0 ? 1 : 0) + (int64_t)s->buckets.size() + (s->any_provot ? 1 : 0)) *
+                        (int64_t)n_steps;
+    return OC_OK;
+}
+
+oc_status oc_set_passes(oc_solver* s, int32_t instance, int32_t passes) {
+    if (!valid_solver(s) || instance < -1 || instance >= s->n_inst ||
+        (passes & ~(OC_PASS_ELLIPSOID | OC_PASS_PROVOT)))
+        return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    const int32_t k0 = instance < 0 ? 0 : instance, k1 = instance < 0 ? s->n_inst : instance + 1;
+    for (int32_t k = k0; k < k1; ++k) {
+        const InstParams& ip = s->inst_host[k];
+        if (passes & OC_PASS_ELLIPSOID)
+            for (int i = 0; i < 16; ++i)
+                if (!std::isfinite(ip.ellipsoid[i]) || !std::isfinite(ip.ellipsoid_inv[i]))
+                    return fail(s, OC_ERR_NON_FINITE, "oc_set_passes: ellipsoid matrix not finite");
+    }
+    for (int32_t k = k0; k < k1; ++k) s->inst_host[k].passes = passes;
+    OC_TRY(cudaStreamSynchronize(s->stream));  // no step in flight reads the parameters
+    OC_TRY(cudaMemcpy(const_cast<InstParams*>(s->args.inst), s->inst_host.data(), sizeof(InstParams) * s->n_inst,
+                      cudaMemcpyHostToDevice));
+    s->any_passes = s->any_provot = false;
+    for (const InstParams& ip : s->inst_host) {
+        s->any_passes = s->any_passes || ip.passes != 0;
+        s->any_provot = s->any_provot || (ip.passes & OC_PASS_PROVOT);
+    }
+    if (s->exec) {  // the graph's node set depends on the passes
+        cudaGraphExecDestroy(s->exec);
+        s->exec = nullptr;
+    }
+    return OC_OK;
+}
+
+oc_status oc_apply_passes(oc_solver* s, int32_t passes) {
+    if (!valid_solver(s) || (passes & ~(OC_PASS_ELLIPSOID | OC_PASS_PROVOT))) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    StepArgs a = s->args;
+    a.blk_base = 0;
+    if (passes & OC_PASS_ELLIPSOID) {
+        a.only_passes = OC_PASS_ELLIPSOID;
+        OC_TRY(launch_kernel(K_ELLIPSOID, a, s->n_blocks, s->stream));
+        s->host_launches += 1;
+    }
+    if (passes & OC_PASS_PROVOT) {
+        a.only_passes = OC_PASS_PROVOT;
+        OC_TRY(launch_kernel(K_PROVOT, a, s->n_blocks, s->stream));
+        s->host_launches += 1;
+    }
     return OC_OK;
 }
 
@@ -866,10 +941,11 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
     cudaEventDestroy(t.ev[0]);
     cudaEventDestroy(t.ev[1]);
     if (st != OC_OK) return st;
-    const KernelKind kinds[] = {K_ASSEMBLE, K_CG_DIR, K_CG_UPDATE, K_INTEGRATE, K_RESIDENT};
+    const KernelKind kinds[] = {K_ASSEMBLE, K_CG_DIR, K_CG_UPDATE, K_INTEGRATE, K_RESIDENT, K_PROVOT};
     int32_t n = 0;
     for (KernelKind k : kinds) {
         if (n >= max_kernels) break;
+        if (k == K_PROVOT && !s->any_provot) continue;
         if (names) {
             std::memset(names + 32 * n, 0, 32);
             std::strncpy(names + 32 * n, kernel_name(k), 31);
@@ -948,6 +1024,9 @@ oc_status oc_set_ext_force(oc_solver* s, const float* ext) {
 
 oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t checkpoint_every, int64_t budget_bytes) {
     if (!valid_solver(s) || n_steps < 1 || checkpoint_every < 0 || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
+    if (s->any_passes)
+        return fail(s, OC_ERR_UNSUPPORTED, "oc_tape_forward: the adjoint covers the implicit step only, not the "
+                                           "passes after it");
     OC_TRY(cudaSetDevice(s->device));
     auto& T = s->tape;
     const size_t state_bytes = 2 * sizeof(float4) * (size_t)s->nv + 3 * s->stride * sizeof(float);

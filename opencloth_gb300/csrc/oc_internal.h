@@ -23,7 +23,10 @@ struct InstParams {
     int32_t nv;
     int32_t has_ext;
     int32_t resident;  // 1: this cloth's CG runs in the resident kernel, not the streamed loop
-    int32_t pad_;
+    int32_t passes;    // OC_PASS_* bits applied after the update
+    float provot_ratio;     // IMP:808
+    float ellipsoid[16];    // object -> world, column-major (IMP:583-585)
+    float ellipsoid_inv[16];
 };
 
 // Per-instance CG scalars, device resident, written by the last block of each
@@ -76,6 +79,9 @@ struct StepArgs {
     float* dbg_F;            // optional debug outputs (float triples) or nullptr
     float* dbg_A9;
     float* dbg_b;
+    const uint8_t* pinflag;  // 1 for pinned vertices (read by k_provot)
+    int32_t only_passes;     // k_ellipsoid / k_provot: nonzero = apply these OC_PASS_* bits to
+                             // every cloth (a pass run on its own), 0 = each cloth's own bits
 };
 
 // Adjoint buffers (oc_adjoint.cu); planes have the handle's vertex stride.
@@ -100,7 +106,7 @@ cudaError_t launch_set_spring_params(const StepArgs& a, const AdjArgs& j, const 
                                      int64_t n_rec, int64_t nv, cudaStream_t stream);
 
 enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3, K_FORCES = 4, K_RESIDENT = 5,
-                  K_COUNT = 6 };
+                  K_PROVOT = 6, K_ELLIPSOID = 7, K_COUNT = 8 };
 
 const char* kernel_name(KernelKind k);
 const void* kernel_fn(KernelKind k);
@@ -147,6 +153,7 @@ struct PackedHost {
     std::vector<int32_t> inc_sid;                     // spring id of every incidence record
     std::vector<int32_t> own_sid;                     // vertex i -> id of spring i, or -1
     std::vector<int32_t> own_rowptr, own_ent;         // vertex -> vertices whose spring touches it
+    bool any_provot = false;                          // some cloth has OC_PASS_PROVOT
 };
 
 oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vertices_per_block, PackedHost* out,

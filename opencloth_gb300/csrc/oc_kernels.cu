@@ -1,4 +1,5 @@
-// Streamed executor: the implicit step as four kernels over a ragged batch.
+// Streamed executor: the implicit step as four kernels over a ragged batch, and the
+// passes after it.
 //
 //   k_assemble   ComputeForces (IMP:698-735) as a per-vertex gather over the
 //                incidence CSR, CalcForceDerivatives for spring i (IMP:737-772),
@@ -7,6 +8,9 @@
 //   k_cg_dir     [d = r + beta d]; alpha = delta_new / d.(A d)    (IMP:320-321, 327)
 //   k_cg_update  x += alpha d; r -= alpha A d; delta_new = r.r     (IMP:322-326)
 //   k_integrate  V += dV dt; X += dt V; ground clamp               (IMP:790-797)
+//                [+ EllipsoidCollision, IMP:824-848]
+//   k_provot     ApplyProvotDynamicInverse as a per-vertex gather   (IMP:800-823)
+//   k_ellipsoid  EllipsoidCollision on its own                      (IMP:824-848)
 //
 // Compiled with --fmad=false and IEEE division / square root so every FP32 operation
 // rounds exactly as the reference's scalar code does.  The CG dot products are summed
@@ -317,15 +321,73 @@ __global__ void __launch_bounds__(kThreads) k_integrate(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const float dt = a.dt;
+    const InstParams& ip = a.inst[bi.inst];
     for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
         float4 Xg = a.X[g], Vg = a.V[g];
-        Vg.x = Vg.x + a.x[0][g] * dt;  // V += dV dt, IMP:791
-        Vg.y = Vg.y + a.x[1][g] * dt;
-        Vg.z = Vg.z + a.x[2][g] * dt;
-        Xg.x = Xg.x + dt * Vg.x;  // X += dt V, IMP:792
-        Xg.y = Xg.y + dt * Vg.y;
-        Xg.z = Xg.z + dt * Vg.z;
-        if (Xg.y < 0.0f) Xg.y = 0.0f;  // IMP:794-796
+        update_vertex(ip, dt, a.x[0][g], a.x[1][g], a.x[2][g], Xg, Vg);
+        a.X[g] = Xg;
+        a.V[g] = Vg;
+    }
+}
+
+// ApplyProvotDynamicInverse (IMP:800-823) as a per-vertex gather.  The reference walks
+// the springs in order and moves the velocities of both ends; its corrections depend on
+// positions only, so vertex g's final velocity is its own plus the corrections of its
+// incident springs added in spring order — the order of g's incidence records.  Each
+// spring's correction is recomputed at both ends from p1 - p2, so both ends see the
+// same rounded value.  Pin flags come from a separate byte array: V is written here.
+__global__ void __launch_bounds__(kThreads) k_provot(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const InstParams& ip = a.inst[bi.inst];
+    if (!((a.only_passes ? a.only_passes : ip.passes) & OC_PASS_PROVOT)) return;
+    const float ratio = ip.provot_ratio;
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Xg = __ldg(a.X + g);
+        float4 Vg = a.V[g];
+        const bool pin_self = a.pinflag[g] != 0;
+        const int32_t k1 = __ldg(a.rowptr + g + 1);
+        for (int32_t k = __ldg(a.rowptr + g); k < k1; ++k) {
+            const int4 rec = __ldg(a.inc + k);
+            const bool is_p2 = rec.x < 0;
+            const int32_t o = rec.x & 0x7fffffff;
+            const float4 Xo = __ldg(a.X + o);
+            const float4 p1 = is_p2 ? Xo : Xg, p2 = is_p2 ? Xg : Xo;
+            const float dx = p1.x - p2.x, dy = p1.y - p2.y, dz = p1.z - p2.z;
+            const float sqr = dx * dx + dy * dy + dz * dz;
+            float dist = sqrtf(sqr);
+            const float lim = __int_as_float(rec.y) * ratio;
+            if (!(dist > lim)) continue;
+            dist = dist - lim;
+            dist = dist / 2.0f;
+            const float inv = 1.0f / sqrtf(sqr);
+            const float cx = (dx * inv) * dist, cy = (dy * inv) * dist, cz = (dz * inv) * dist;
+            const bool pin_o = __ldg(a.pinflag + o) != 0;
+            if (!is_p2) {
+                if (!pin_self) {  // p1 moves unless pinned
+                    Vg.x = Vg.x - cx;
+                    Vg.y = Vg.y - cy;
+                    Vg.z = Vg.z - cz;
+                }
+            } else if (pin_o || !pin_self) {  // p2 moves when p1 is pinned or p2 is free
+                Vg.x = Vg.x + cx;
+                Vg.y = Vg.y + cy;
+                Vg.z = Vg.z + cz;
+            }
+        }
+        a.V[g] = Vg;
+    }
+}
+
+// EllipsoidCollision on its own (the step fuses it into the update).
+__global__ void __launch_bounds__(kThreads) k_ellipsoid(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const InstParams& ip = a.inst[bi.inst];
+    if (!((a.only_passes ? a.only_passes : ip.passes) & OC_PASS_ELLIPSOID)) return;
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        float4 Xg = a.X[g], Vg = a.V[g];
+        ellipsoid_vertex(ip, Xg, Vg);
         a.X[g] = Xg;
         a.V[g] = Vg;
     }
@@ -423,6 +485,8 @@ const char* kernel_name(KernelKind k) {
         case K_INTEGRATE: return "k_integrate";
         case K_FORCES: return "k_forces";
         case K_RESIDENT: return "k_resident";
+        case K_PROVOT: return "k_provot";
+        case K_ELLIPSOID: return "k_ellipsoid";
         default: return "?";
     }
 }
@@ -434,6 +498,8 @@ const void* kernel_fn(KernelKind k) {
         case K_CG_UPDATE: return (const void*)k_cg_update;
         case K_INTEGRATE: return (const void*)k_integrate;
         case K_FORCES: return (const void*)k_forces;
+        case K_PROVOT: return (const void*)k_provot;
+        case K_ELLIPSOID: return (const void*)k_ellipsoid;
         default: return nullptr;
     }
 }
@@ -481,6 +547,8 @@ cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStre
         case K_CG_UPDATE: k_cg_update<<<nblocks, kThreads, 0, stream>>>(a); break;
         case K_INTEGRATE: k_integrate<<<nblocks, kThreads, 0, stream>>>(a); break;
         case K_FORCES: k_forces<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_PROVOT: k_provot<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_ELLIPSOID: k_ellipsoid<<<nblocks, kThreads, 0, stream>>>(a); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -146,20 +146,15 @@ __global__ void __launch_bounds__(T) k_resident(const StepArgs a, const Resident
             break;
         }
     }
-    // V += dV dt; X += dt V; ground clamp (IMP:790-797); dV stays as the warm start.
+    // V += dV dt; X += dt V; ground clamp (IMP:790-797), then the ellipsoid pass when
+    // enabled; dV stays as the warm start.
     const float dt = a.dt;
     __syncthreads();
     for (int j = threadIdx.x; j < n_local; j += T) {
         const int64_t g = base + j;
         float4 Xg = a.X[g], Vg = a.V[g];
         const float x0 = sx[0][j], x1 = sx[1][j], x2 = sx[2][j];
-        Vg.x = Vg.x + x0 * dt;
-        Vg.y = Vg.y + x1 * dt;
-        Vg.z = Vg.z + x2 * dt;
-        Xg.x = Xg.x + dt * Vg.x;
-        Xg.y = Xg.y + dt * Vg.y;
-        Xg.z = Xg.z + dt * Vg.z;
-        if (Xg.y < 0.0f) Xg.y = 0.0f;
+        update_vertex(ip, dt, x0, x1, x2, Xg, Vg);
         a.X[g] = Xg;
         a.V[g] = Vg;
         a.x[0][g] = x0;

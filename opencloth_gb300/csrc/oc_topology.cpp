@@ -93,6 +93,22 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
                 }
             }
         }
+        if (d.passes & ~(OC_PASS_ELLIPSOID | OC_PASS_PROVOT)) {
+            *err = who + "unknown pass bits";
+            return OC_ERR_INVALID_ARGUMENT;
+        }
+        if (d.passes & OC_PASS_ELLIPSOID) {
+            for (int i = 0; i < 16; ++i) {
+                if (!std::isfinite(d.ellipsoid[i]) || !std::isfinite(d.ellipsoid_inv[i])) {
+                    *err = who + "ellipsoid matrix not finite";
+                    return OC_ERR_NON_FINITE;
+                }
+            }
+        }
+        if ((d.passes & OC_PASS_PROVOT) && !(std::isfinite(d.provot_ratio) && d.provot_ratio >= 0.0f)) {
+            *err = who + "provot_ratio must be finite and >= 0";
+            return OC_ERR_INVALID_ARGUMENT;
+        }
         if (d.ext_force) {
             any_ext = true;
             for (int32_t i = 0; i < d.n_vertices; ++i) {
@@ -126,6 +142,7 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
     P.own_ends.assign(nv, make_int2(-1, -1));
     P.own_par.assign(nv, make_float4(0.f, 0.f, 0.f, 0.f));
     P.blocks.clear();
+    P.any_provot = false;
 
     std::vector<int32_t> deg(nv, 0);
     for (int32_t k = 0; k < n; ++k) {
@@ -161,7 +178,13 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
         ip.nv = d.n_vertices;
         ip.has_ext = d.ext_force ? 1 : 0;
         ip.resident = 0;
-        ip.pad_ = 0;
+        ip.passes = d.passes;
+        ip.provot_ratio = d.provot_ratio == 0.0f ? 1.01f : d.provot_ratio;
+        for (int i = 0; i < 16; ++i) {
+            ip.ellipsoid[i] = d.ellipsoid[i];
+            ip.ellipsoid_inv[i] = d.ellipsoid_inv[i];
+        }
+        if (d.passes & OC_PASS_PROVOT) P.any_provot = true;
         ip.blk0 = (int32_t)P.blocks.size();
         ip.nblk = (d.n_vertices + vpb - 1) / vpb;
         for (int32_t b = 0; b < ip.nblk; ++b) {

@@ -53,8 +53,12 @@ class Params(C.Structure):
         ("n_vertices", C.c_int32), ("n_springs", C.c_int32), ("springs", C.c_void_p), ("pinned", C.c_void_p),
         ("num_x", C.c_int32), ("mass", C.c_void_p), ("ext_force", C.c_void_p), ("gravity", C.c_float * 3),
         ("damping", C.c_float), ("i_max", C.c_int32), ("eps", C.c_float), ("dot_fp64", C.c_int32),
-        ("filter_pinned", C.c_int32),
+        ("filter_pinned", C.c_int32), ("passes", C.c_int32), ("ellipsoid", C.c_double * 16),
+        ("ellipsoid_inv", C.c_double * 16), ("provot_ratio", C.c_double),
     ]
+
+PASS_ELLIPSOID = 1
+PASS_PROVOT = 2
 
 
 _port = None
@@ -74,6 +78,7 @@ def port() -> C.CDLL:
             f = getattr(lib, f"ocr_step_{sfx}")
             f.argtypes = [P, real, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
             f.restype = C.c_int
+            getattr(lib, f"ocr_passes_{sfx}").argtypes = [P, C.c_void_p, C.c_void_p]
         lib.ocr_adjoint_f64.argtypes = [P, C.c_double, C.c_int32] + [C.c_void_p] * 10
         lib.ocr_adjoint_f64.restype = C.c_int
         _port = lib
@@ -84,7 +89,20 @@ class Cloth:
     """Inputs of one cloth for the oracle (mirrors oc_cloth_desc)."""
 
     def __init__(self, n_vertices, springs, pinned=None, num_x=None, mass=None, ext_force=None,
-                 gravity=(0.0, -0.00981, 0.0), damping=-0.125, i_max=10, eps=1e-3):
+                 gravity=(0.0, -0.00981, 0.0), damping=-0.125, i_max=10, eps=1e-3, passes=0, ellipsoid=None,
+                 ellipsoid_inv=None, provot_ratio=1.01, ellipsoid64=None, ellipsoid_inv64=None):
+        # The ellipsoid (column-major 4x4 and its inverse) as the FP32 reference holds it;
+        # the FP64 flavour uses the *64 copies when given (the FP64 reference computes the
+        # matrices in double), else the FP32 values widened.
+        self.passes = int(passes)
+        z = np.zeros(16)
+        self.ellipsoid = z if ellipsoid is None else np.asarray(ellipsoid, np.float32).astype(np.float64).ravel()
+        self.ellipsoid_inv = (z if ellipsoid_inv is None
+                              else np.asarray(ellipsoid_inv, np.float32).astype(np.float64).ravel())
+        self.ellipsoid64 = self.ellipsoid if ellipsoid64 is None else np.asarray(ellipsoid64, np.float64).ravel()
+        self.ellipsoid_inv64 = (self.ellipsoid_inv if ellipsoid_inv64 is None
+                                else np.asarray(ellipsoid_inv64, np.float64).ravel())
+        self.provot_ratio = float(provot_ratio)
         self.n_vertices = int(n_vertices)
         self.springs = np.ascontiguousarray(springs, SPRING_DTYPE)
         self.pinned = pinned  # index array or None (then the reference pins {0, num_x})
@@ -96,7 +114,7 @@ class Cloth:
         self.i_max = int(i_max)
         self.eps = float(eps)
 
-    def params(self, dot_fp64: bool, filter_pinned: bool):
+    def params(self, dot_fp64: bool, filter_pinned: bool, fp64: bool = False):
         keep = []
         p = Params()
         p.n_vertices = self.n_vertices
@@ -125,6 +143,10 @@ class Cloth:
         p.eps = self.eps
         p.dot_fp64 = 1 if dot_fp64 else 0
         p.filter_pinned = 1 if filter_pinned else 0
+        p.passes = self.passes
+        p.ellipsoid[:] = [float(v) for v in (self.ellipsoid64 if fp64 else self.ellipsoid)]
+        p.ellipsoid_inv[:] = [float(v) for v in (self.ellipsoid_inv64 if fp64 else self.ellipsoid_inv)]
+        p.provot_ratio = self.provot_ratio
         return p, keep
 
 
@@ -138,7 +160,7 @@ def port_step(cloth: Cloth, X, V, dV=None, dt=1.0 / 60.0, n_steps=1, fp64=False,
     dV = np.zeros_like(X) if dV is None else np.array(dV, real).reshape(-1)
     iters = np.zeros(max(n_steps, 1), np.int32)
     rr = np.zeros(max(n_steps, 1), np.float64)
-    p, keep = cloth.params(dot_fp64, filter_pinned)
+    p, keep = cloth.params(dot_fp64, filter_pinned, fp64)
     fn = lib.ocr_step_f64 if fp64 else lib.ocr_step_f32
     dtv = float(np.float32(dt))
     rc = fn(C.byref(p), dtv, int(n_steps), X.ctypes.data, V.ctypes.data, dV.ctypes.data, iters.ctypes.data,
@@ -147,6 +169,20 @@ def port_step(cloth: Cloth, X, V, dV=None, dt=1.0 / 60.0, n_steps=1, fp64=False,
         raise RuntimeError("oracle port step failed")
     del keep
     return X.reshape(-1, 3), V.reshape(-1, 3), dV.reshape(-1, 3), iters[:n_steps], rr[:n_steps]
+
+
+def port_passes(cloth: Cloth, X, V, passes, fp64=False):
+    """The passes (bit 1 EllipsoidCollision, bit 2 ApplyProvotDynamicInverse) alone on
+    copies of (X, V), with the cloth's matrices, ratio and pins."""
+    lib = port()
+    real = np.float64 if fp64 else np.float32
+    X = np.ascontiguousarray(X, real).reshape(-1).copy()
+    V = np.ascontiguousarray(V, real).reshape(-1).copy()
+    p, keep = cloth.params(False, False, fp64)
+    p.passes = int(passes)
+    (lib.ocr_passes_f64 if fp64 else lib.ocr_passes_f32)(C.byref(p), X.ctypes.data, V.ctypes.data)
+    del keep
+    return X.reshape(-1, 3), V.reshape(-1, 3)
 
 
 def port_forces(cloth: Cloth, X, V, fp64=False):
@@ -199,9 +235,20 @@ def ref_available() -> bool:
         return False
 
 
-def _ref_env(num_x, num_y, i_max, eps):
+def _ref_env(num_x, num_y, i_max, eps, passes=0):
     return dict(os.environ, OC_NUMX=str(num_x), OC_NUMY=str(num_y), OC_IMAX=str(int(i_max)),
-                OC_EPS="%.17g" % float(np.float32(eps)))
+                OC_EPS="%.17g" % float(np.float32(eps)), OC_PASSES=str(int(passes)))
+
+
+def ref_ellipsoid(fp64: bool = False):
+    """The reference's ellipsoid matrix and its inverse (16 reals each, column-major),
+    from the FP32 build (float32) or the FP64 build (float64)."""
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "ell.bin")
+        subprocess.run([str(ref_binary(fp64)), "--ellipsoid", out], env=_ref_env(20, 20, 10, 1e-3), check=True,
+                       capture_output=True)
+        b = np.fromfile(out, np.float64 if fp64 else np.float32)
+    return b[:16].copy(), b[16:32].copy()
 
 
 def ref_topology(num_x: int, num_y: int):
@@ -235,7 +282,8 @@ def ref_run(cloth: Cloth, num_x: int, num_y: int, X, V, dV=None, dt=1.0 / 60.0, 
         inp, out = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         open(inp, "wb").write(blob)
         cmd = [str(ref_binary(fp64)), inp, out] + (["--time"] if timed else [])
-        r = subprocess.run(cmd, env=_ref_env(num_x, num_y, cloth.i_max, cloth.eps), capture_output=True, text=True)
+        r = subprocess.run(cmd, env=_ref_env(num_x, num_y, cloth.i_max, cloth.eps, cloth.passes), capture_output=True,
+                           text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference run failed: {r.stderr}")
         b = open(out, "rb").read()

@@ -21,6 +21,8 @@
  *                    dot terms summed in FP64 (what the GPU solver does)
  *   filter_pinned    0 -> no filter (the reference); 1 -> pinned rows of the warm start
  *                    and of the residual are zeroed before the CG (the GPU solver)
+ *   passes           0 -> ComputeForces + IntegrateImplicit only; bits add the ellipsoid
+ *                    collision and the Provot correction of StepPhysics
  */
 #ifndef OC_ORACLE_H
 #define OC_ORACLE_H
@@ -49,6 +51,14 @@ typedef struct ocr_params {
     float eps;
     int32_t dot_fp64;
     int32_t filter_pinned;
+    /* Passes after the update, in StepPhysics' order (IMP:873-880): bit 1
+     * EllipsoidCollision (IMP:824-848), bit 2 ApplyProvotDynamicInverse (IMP:800-823). */
+    int32_t passes;
+    /* Held in double so the FP64 flavour gets the FP64 reference's dmat4 values; the
+     * FP32 flavour rounds them to float (exact for matrices that came from floats). */
+    double ellipsoid[16];     /* object -> world, glm column-major (IMP:583-585) */
+    double ellipsoid_inv[16]; /* its inverse (IMP:586) */
+    double provot_ratio;      /* 1.01 in the reference (IMP:808) */
 } ocr_params;
 
 /* FP32 flavour: state arrays are 3 * n_vertices floats, AoS (x, y, z). */
@@ -57,6 +67,9 @@ void ocr_assemble_f32(const ocr_params* p, float dt, const float* X, const float
                       float* b);
 int ocr_step_f32(const ocr_params* p, float dt, int32_t n_steps, float* X, float* V, float* dV, int32_t* iters,
                  double* rel_residual);
+/* The passes of p->passes alone, on (X, V) in place: EllipsoidCollision then
+ * ApplyProvotDynamicInverse (IMP:877-880). */
+void ocr_passes_f32(const ocr_params* p, float* X, float* V);
 
 /* FP64 flavour of the same method (the reference built with double everywhere). */
 void ocr_compute_forces_f64(const ocr_params* p, const double* X, const double* V, double* F);
@@ -64,6 +77,7 @@ void ocr_assemble_f64(const ocr_params* p, double dt, const double* X, const dou
                       double* A9, double* b);
 int ocr_step_f64(const ocr_params* p, double dt, int32_t n_steps, double* X, double* V, double* dV,
                  int32_t* iters, double* rel_residual);
+void ocr_passes_f64(const ocr_params* p, double* X, double* V);
 
 /* FP64 adjoint of n_steps steps from (X0, V0) with a zero warm start (oc_adjoint.c):
  * given dL/dX_T, dL/dV_T (NULL = 0), returns the final state and dL/dX0, dL/dV0,

@@ -184,8 +184,83 @@ static double SFX(dot)(const ocr_params* p, const REAL* a, const REAL* b, int32_
     return (double)sum;
 }
 
-/* ComputeForces(); IntegrateImplicit(dt); repeated n_steps times (IMP:873-876 without
- * the collision and Provot passes).  dV is the persistent warm start (IMP:361). */
+/* EllipsoidCollision, IMP:824-848: a vertex inside the unit sphere of the ellipsoid's
+ * object space (center 0, radius 1, IMP:136-137) is pushed to its surface and stopped.
+ * Matrices are glm column-major (m[c][r] at 4c + r); mat4 * vec4 sums left to right
+ * (GLM/core/type_mat4x4.inl:567-571). */
+static void SFX(ellipsoid_pass)(const ocr_params* p, REAL* X, REAL* V) {
+    const double* E = p->ellipsoid;
+    const double* I = p->ellipsoid_inv;
+    for (int32_t i = 0; i < p->n_vertices; ++i) {
+        REAL* x = X + 3 * (size_t)i;
+        const REAL one = 1;
+        REAL d0x = (REAL)I[0] * x[0] + (REAL)I[4] * x[1] + (REAL)I[8] * x[2] + (REAL)I[12] * one;
+        REAL d0y = (REAL)I[1] * x[0] + (REAL)I[5] * x[1] + (REAL)I[9] * x[2] + (REAL)I[13] * one;
+        REAL d0z = (REAL)I[2] * x[0] + (REAL)I[6] * x[1] + (REAL)I[10] * x[2] + (REAL)I[14] * one;
+        const REAL zero = 0;
+        d0x = d0x - zero;
+        d0y = d0y - zero;
+        d0z = d0z - zero;
+        const REAL dist = SQRT(d0x * d0x + d0y * d0y + d0z * d0z);
+        if (dist < one) {
+            const REAL k = one - dist;
+            d0x = (k * d0x) / dist;
+            d0y = (k * d0y) / dist;
+            d0z = (k * d0z) / dist;
+            REAL delta[3];
+            for (int r = 0; r < 3; ++r) {
+                REAL tx = (REAL)E[r], ty = (REAL)E[4 + r], tz = (REAL)E[8 + r];
+                const REAL dd = tx * tx + ty * ty + tz * tz;
+                tx = tx / dd;
+                ty = ty / dd;
+                tz = tz / dd;
+                delta[r] = d0x * tx + d0y * ty + d0z * tz;
+            }
+            x[0] += delta[0];
+            x[1] += delta[1];
+            x[2] += delta[2];
+            V[3 * (size_t)i] = V[3 * (size_t)i + 1] = V[3 * (size_t)i + 2] = 0;
+        }
+    }
+}
+
+/* ApplyProvotDynamicInverse, IMP:800-823: a spring stretched beyond ratio * rest moves
+ * its endpoints' velocities by half the excess along the spring, pinned ends excepted. */
+static void SFX(provot_pass)(const ocr_params* p, const REAL* X, REAL* V) {
+    for (int32_t s = 0; s < p->n_springs; ++s) {
+        const ocr_spring* sp = p->springs + s;
+        const REAL* a = X + 3 * (size_t)sp->p1;
+        const REAL* b = X + 3 * (size_t)sp->p2;
+        REAL dP[3] = {a[0] - b[0], a[1] - b[1], a[2] - b[2]};
+        const REAL sqr = dP[0] * dP[0] + dP[1] * dP[1] + dP[2] * dP[2];
+        REAL dist = SQRT(sqr);
+        const REAL lim = (REAL)sp->rest * (REAL)p->provot_ratio;
+        if (dist > lim) {
+            dist -= lim;
+            dist /= (REAL)2;
+            const REAL inv = (REAL)1 / SQRT(sqr);
+            for (int k = 0; k < 3; ++k) dP[k] = (dP[k] * inv) * dist;
+            REAL* v1 = V + 3 * (size_t)sp->p1;
+            REAL* v2 = V + 3 * (size_t)sp->p2;
+            if (SFX(is_pinned)(p, sp->p1)) {
+                for (int k = 0; k < 3; ++k) v2[k] += dP[k];
+            } else if (SFX(is_pinned)(p, sp->p2)) {
+                for (int k = 0; k < 3; ++k) v1[k] -= dP[k];
+            } else {
+                for (int k = 0; k < 3; ++k) v1[k] -= dP[k];
+                for (int k = 0; k < 3; ++k) v2[k] += dP[k];
+            }
+        }
+    }
+}
+
+void SFX(ocr_passes)(const ocr_params* p, REAL* X, REAL* V) {
+    if (p->passes & 1) SFX(ellipsoid_pass)(p, X, V);
+    if (p->passes & 2) SFX(provot_pass)(p, X, V);
+}
+
+/* ComputeForces(); IntegrateImplicit(dt); [EllipsoidCollision(); ApplyProvotDynamicInverse();]
+ * repeated n_steps times (IMP:873-880).  dV is the persistent warm start (IMP:361). */
 int SFX(ocr_step)(const ocr_params* p, REAL dt, int32_t n_steps, REAL* X, REAL* V, REAL* dV, int32_t* iters,
                   double* rel_residual) {
     const int32_t N = p->n_vertices;
@@ -257,6 +332,8 @@ int SFX(ocr_step)(const ocr_params* p, REAL dt, int32_t n_steps, REAL* X, REAL* 
             for (int k = 0; k < 3; ++k) X[3 * (size_t)i + k] += dt * V[3 * (size_t)i + k];
             if (X[3 * (size_t)i + 1] < 0) X[3 * (size_t)i + 1] = 0;
         }
+        if (p->passes & 1) SFX(ellipsoid_pass)(p, X, V);
+        if (p->passes & 2) SFX(provot_pass)(p, X, V);
     }
     free(F); free(A9); free(b); free(P); free(Pinv); free(r); free(d); free(q); free(Pr);
     return 0;

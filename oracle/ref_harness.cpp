@@ -19,6 +19,7 @@
 // Usage:
 //   ref_step <instance.bin> <out.bin> [--time]   step and write snapshots
 //   ref_step --topology <out.bin>                dump InitGL()'s springs and X
+//   ref_step --ellipsoid <out.bin>               dump InitGL()'s ellipsoid matrices
 #include <chrono>
 #include <cstdint>
 #include <cstdio>
@@ -97,8 +98,29 @@ int dump_topology(const char* out_path) {
 
 }  // namespace
 
+// The reference's ellipsoid (InitGL, IMP:583-586): the object-to-world matrix and its
+// inverse, 16 reals each (float or double with the build), glm column-major.
+int dump_ellipsoid(const char* out_path) {
+    InitGL();
+    FILE* f = std::fopen(out_path, "wb");
+    if (!f) return 2;
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            const real_t v = ellipsoid[c][r];
+            std::fwrite(&v, sizeof(v), 1, f);
+        }
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            const real_t v = inverse_ellipsoid[c][r];
+            std::fwrite(&v, sizeof(v), 1, f);
+        }
+    std::fclose(f);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc >= 3 && std::string(argv[1]) == "--topology") return dump_topology(argv[2]);
+    if (argc >= 3 && std::string(argv[1]) == "--ellipsoid") return dump_ellipsoid(argv[2]);
     if (argc < 3) {
         std::fprintf(stderr, "usage: %s <instance.bin> <out.bin> [--time] | --topology <out.bin>\n", argv[0]);
         return 2;
@@ -174,9 +196,14 @@ int main(int argc, char** argv) {
     while (next < snaps.size() && snaps[next] == 0) write_state(out, 0), ++next;
     const real_t dt = h.dt;
     auto t0 = std::chrono::steady_clock::now();
+    // OC_PASSES bit 1: EllipsoidCollision (IMP:824), bit 2: ApplyProvotDynamicInverse
+    // (IMP:800), in StepPhysics' order (IMP:873-880).
+    const int passes = oc_env_int("OC_PASSES", 0);
     for (int32_t step = 1; step <= last; ++step) {
         ComputeForces();
         IntegrateImplicit(dt);
+        if (passes & 1) EllipsoidCollision();
+        if (passes & 2) ApplyProvotDynamicInverse();
         while (next < snaps.size() && snaps[next] == step) write_state(out, step), ++next;
     }
     auto t1 = std::chrono::steady_clock::now();

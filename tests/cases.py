@@ -9,7 +9,7 @@ import oracle
 from opencloth_gb300 import SPRING_DTYPE, ClothDesc, grid_cloth
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-GOLDEN_CASES = ("grid21_ref", "random7x5_ref", "clamp9_ref")
+GOLDEN_CASES = ("grid21_ref", "random7x5_ref", "clamp9_ref", "stepphysics21_ref")
 
 
 def golden(name: str) -> dict:
@@ -19,6 +19,7 @@ def golden(name: str) -> dict:
         d[k] = int(d[k])
     d["dt"] = float(d["dt"])
     d["eps"] = float(d["eps"])
+    d["passes"] = int(d.get("passes", 0))
     return d
 
 
@@ -33,13 +34,16 @@ def desc_for(g: dict, **kw) -> ClothDesc:
     """Library description of a golden case; pins = the reference's {0, numX}."""
     return ClothDesc(n_vertices=g["cols"] * g["rows"], springs=g["springs"],
                      pinned=np.array([0, g["cols"] - 1], np.int32), gravity=tuple(g["gravity"]),
-                     cg_max_iter=g["i_max"], cg_tol=g["eps"], **kw)
+                     cg_max_iter=g["i_max"], cg_tol=g["eps"], passes=g["passes"], ellipsoid=g["ellipsoid"],
+                     ellipsoid_inv=g["ellipsoid_inv"], **kw)
 
 
 def oracle_for(g: dict, explicit_pins: bool = False) -> oracle.Cloth:
     return oracle.Cloth(g["cols"] * g["rows"], g["springs"], num_x=g["cols"] - 1,
                         pinned=[0, g["cols"] - 1] if explicit_pins else None, gravity=tuple(g["gravity"]),
-                        i_max=g["i_max"], eps=g["eps"])
+                        i_max=g["i_max"], eps=g["eps"], passes=g["passes"], ellipsoid=g["ellipsoid"],
+                        ellipsoid_inv=g["ellipsoid_inv"], ellipsoid64=g["ellipsoid64"],
+                        ellipsoid_inv64=g["ellipsoid_inv64"])
 
 
 def seeded_cloth(cols: int, rows: int, seed: int, i_max: int = 200, eps: float = 1e-5, jitter: float = 1e-3,

@@ -23,13 +23,17 @@ from opencloth_gb300 import grid_cloth  # noqa: E402
 OUT = Path(__file__).resolve().parent
 
 
-def save_case(name, cols, rows, X, V, dV, springs, dt, i_max, eps, gravity, snaps32, snaps64):
-    cl = oracle.Cloth(cols * rows, springs, num_x=cols - 1, gravity=gravity, i_max=i_max, eps=eps)
+def save_case(name, cols, rows, X, V, dV, springs, dt, i_max, eps, gravity, snaps32, snaps64, passes=0):
+    E, Einv = oracle.ref_ellipsoid()
+    E64, Einv64 = oracle.ref_ellipsoid(fp64=True)
+    cl = oracle.Cloth(cols * rows, springs, num_x=cols - 1, gravity=gravity, i_max=i_max, eps=eps, passes=passes,
+                      ellipsoid=E, ellipsoid_inv=Einv, ellipsoid64=E64, ellipsoid_inv64=Einv64)
     r32 = oracle.ref_run(cl, cols - 1, rows - 1, X, V, dV, dt=dt, snaps=snaps32)
     r64 = oracle.ref_run(cl, cols - 1, rows - 1, X, V, dV, dt=dt, snaps=snaps64, fp64=True)
     out = dict(cols=cols, rows=rows, X0=X, V0=V, dV0=dV, springs=springs.view(np.uint8).reshape(len(springs), -1),
                dt=np.float32(dt), i_max=i_max, eps=np.float32(eps), gravity=np.asarray(gravity, np.float32),
-               snaps32=np.asarray(snaps32, np.int32), snaps64=np.asarray(snaps64, np.int32))
+               snaps32=np.asarray(snaps32, np.int32), snaps64=np.asarray(snaps64, np.int32), passes=passes,
+               ellipsoid=E, ellipsoid_inv=Einv, ellipsoid64=E64, ellipsoid_inv64=Einv64)
     for s in snaps32:
         out[f"X32_{s}"], out[f"V32_{s}"], out[f"dV32_{s}"] = r32[s]
     for s in snaps64:
@@ -68,6 +72,13 @@ def main():
     X[:, 1] -= 1.95
     save_case("clamp9_ref", cols, rows, X, np.zeros_like(X), np.zeros_like(X), sp, 1.0 / 60.0, 30, 1e-4,
               (0.0, -9.81, 0.0), (1, 40), (1, 40))
+
+    # The whole StepPhysics (IMP:873-880): the ellipsoid of InitGL sits at y = 2 and cuts
+    # the lower rows of the cloth, and soft springs let Provot's correction act.
+    cols, rows = 21, 21
+    X, sp = grid_cloth(cols, rows, ks=(0.75, 0.75, 0.95), kd=(-0.25, -0.25, -0.25))
+    save_case("stepphysics21_ref", cols, rows, X, np.zeros_like(X), np.zeros_like(X), sp, 5.0 / 60.0, 10, 1e-3, g,
+              (1, 10, 100), (1,), passes=3)
 
     # InitGL's own topology for a few grid sizes.
     topo = {}

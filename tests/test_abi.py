@@ -125,6 +125,43 @@ def test_null_handle_calls_fail_cleanly():
     lib.oc_destroy(None)
 
 
+def _c_layout(struct: str, fields) -> list:
+    """sizeof and offsetof of a header struct, from a probe compiled with the host C compiler."""
+    import shutil
+    import subprocess
+    import tempfile
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    body = "".join(f'printf("%zu\\n", offsetof({struct}, {f}));' for f in fields)
+    src = ('#include <stddef.h>\n#include <stdio.h>\n#include "opencloth_gb.h"\n'
+           f'int main(void) {{ printf("%zu\\n", sizeof({struct})); {body} return 0; }}\n')
+    with tempfile.TemporaryDirectory() as td:
+        c = Path(td) / "probe.c"
+        c.write_text(src)
+        exe = Path(td) / "probe"
+        subprocess.run([cc, f"-I{INCLUDE}", str(c), "-o", str(exe)], check=True, capture_output=True)
+        out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    return [int(v) for v in out.split()]
+
+
+@pytest.mark.parametrize("cls,struct", [(N.ClothDescC, "oc_cloth_desc"), (N.OptionsC, "oc_options"),
+                                        (N.Spring, "oc_spring")])
+def test_ctypes_structs_match_the_header(cls, struct):
+    fields = [f[0] for f in cls._fields_]
+    got = _c_layout(struct, fields)
+    assert got[0] == C.sizeof(cls), struct
+    assert got[1:] == [getattr(cls, f).offset for f in fields], struct
+
+
 def test_spring_record_layout_matches_c():
     assert SPRING_DTYPE.itemsize == C.sizeof(N.Spring) == 24
-    assert C.sizeof(N.ClothDescC) == 80
+
+
+def test_create_rejects_bad_passes():
+    assert _status(_desc(passes=4)) == 1  # unknown pass bit: OC_ERR_INVALID_ARGUMENT
+    bad = np.eye(4, dtype=np.float32).ravel()
+    bad[5] = np.nan
+    assert _status(_desc(passes=1, ellipsoid=bad, ellipsoid_inv=np.eye(4).ravel())) == 3  # OC_ERR_NON_FINITE
+    assert _status(_desc(passes=2, provot_ratio=-1.0)) == 1
