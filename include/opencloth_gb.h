@@ -66,8 +66,12 @@ typedef struct oc_spring {
 /* REFERENCE: vertex i takes spring i's df/dx, df/dv (IMP:782-783 index the per-spring
  * arrays by vertex), giving a block-diagonal system solved by the reference's PCG. */
 #define OC_JAC_REFERENCE 0
-/* COUPLED: the same per-spring blocks assembled at (p1,p1),(p1,p2),(p2,p1),(p2,p2)
- * into a 3x3 block-CSR matrix (Baraff-Witkin coupling; no counterpart in the reference). */
+/* COUPLED: Baraff-Witkin coupling on the reference's force model (no counterpart in the
+ * reference).  Every spring adds B = h kdn nn^T + h^2 Kt at (p1,p1), (p2,p2) and -B at
+ * (p1,p2), (p2,p1), with Kt = ksn [nn^T + max(1 - L/l, 0)(I - nn^T)], ksn = max(ks, 0),
+ * kdn = max(-kd, 0): positive semi-definite by construction, so the system
+ * (m + h max(-c, 0)) I + sum B is SPD.  b = h (F - h sum Kt (v_i - v_j)); block-Jacobi
+ * PCG to cg_tol; V += dV.  Streamed executor only; no adjoint, no oc_assemble. */
 #define OC_JAC_COUPLED 1
 
 /* Upper bound on cg_max_iter: the device-driven CG loop of a step runs at most this

@@ -26,7 +26,8 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
     "-Xcompiler", "-fno-strict-aliasing", "-I", str(INCLUDE), "-I", str(CSRC),
 ]
-SOURCES = ["oc_kernels.cu", "oc_resident.cu", "oc_adjoint.cu", "oc_api.cu", "oc_topology.cpp", "oc_noalloc.cu"]
+SOURCES = ["oc_kernels.cu", "oc_resident.cu", "oc_adjoint.cu", "oc_api.cu", "oc_topology.cpp", "oc_noalloc.cu",
+           "oc_coupled.cu"]
 
 
 def _nvcc() -> str:

@@ -43,6 +43,17 @@ struct oc_solver {
     std::vector<uint8_t> resident;  // per instance
     BlockInfo* d_streamed_blocks = nullptr;
     int32_t n_streamed_blocks = 0;
+    // Block tables of a step: k_assemble over the REFERENCE cloths (resident and
+    // streamed), the coupled kernels over the COUPLED cloths, k_integrate over the
+    // streamed REFERENCE and the COUPLED cloths.  Without COUPLED cloths the first is the
+    // full table and the last is the streamed one.
+    BlockInfo* d_asm_blocks = nullptr;
+    int32_t n_asm_blocks = 0;
+    BlockInfo* d_cpl_blocks = nullptr;
+    int32_t n_cpl_blocks = 0;
+    BlockInfo* d_upd_blocks = nullptr;
+    int32_t n_upd_blocks = 0;
+    bool any_coupled = false;
     bool any_provot = false;  // some cloth has OC_PASS_PROVOT: k_provot follows the update
     bool any_passes = false;  // some cloth has a pass after the update
     // Resident buckets run concurrently: forked from the handle's stream onto these.
@@ -153,6 +164,20 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
         t->bytes[K_ASSEMBLE] += 120.0 * nv + 32.0 * ns;
         // k_provot: X 16, V 32 in and out, pin flag 1, row pointer 4; 16-byte records.
         if (s->inst_host[k].passes & OC_PASS_PROVOT) t->bytes[K_PROVOT] += 53.0 * nv + 32.0 * ns;
+        if (s->inst_host[k].coupled) {
+            // k_cpl_assemble 112 B + 72 B per spring (record in, block out at both ends);
+            // k_cpl_dir 33 B (first pass) or 45 B plus 48 B per spring (other vertex and
+            // block at both ends); k_cpl_update 120 B (first) or 132 B; k_integrate 76 B.
+            t->bytes[K_ASSEMBLE] -= 120.0 * nv + 32.0 * ns;
+            t->bytes[K_CPL_ASSEMBLE] += 112.0 * nv + 72.0 * ns;
+            const double it = (double)st.iter;
+            double dirs = it > 0 ? 33.0 * nv + 45.0 * nv * (it - 1.0) + 48.0 * ns * it : 0.0;
+            if (st.flags & OC_FLAG_BREAKDOWN) dirs += (it > 0 ? 45.0 : 33.0) * nv + 48.0 * ns;
+            t->bytes[K_CPL_DIR] += dirs;
+            t->bytes[K_CPL_UPDATE] += it > 0 ? 120.0 * nv + 132.0 * nv * (it - 1.0) : 0.0;
+            t->bytes[K_INTEGRATE] += 76.0 * nv;
+            continue;
+        }
         if (s->resident[k]) {
             // CG state in (A 24 + x, r, d 36), X, V 32 in and out, dV 12 out; the CG
             // iterations run in shared memory.
@@ -228,15 +253,16 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
         for (int grp = 0; grp < s->n_inst; ++grp) {
             a.blk_base = s->inst_host[grp].blk0;
             const int nb = s->inst_host[grp].nblk;
-            if ((st = launch_timed(s, K_ASSEMBLE, a, nb, t)) != OC_OK) return st;
+            const bool cpl = s->inst_host[grp].coupled != 0;
+            if ((st = launch_timed(s, cpl ? K_CPL_ASSEMBLE : K_ASSEMBLE, a, nb, t)) != OC_OK) return st;
             s->host_launches += s->any_provot ? 3 : 2;
             for (;;) {
                 OC_TRY(cudaMemcpyAsync(s->h_scalar, &s->args.state[grp].active, sizeof(int32_t),
                                        cudaMemcpyDeviceToHost, s->stream));
                 OC_TRY(cudaStreamSynchronize(s->stream));
                 if (*s->h_scalar <= 0) break;
-                if ((st = launch_timed(s, K_CG_DIR, a, nb, t)) != OC_OK) return st;
-                if ((st = launch_timed(s, K_CG_UPDATE, a, nb, t)) != OC_OK) return st;
+                if ((st = launch_timed(s, cpl ? K_CPL_DIR : K_CG_DIR, a, nb, t)) != OC_OK) return st;
+                if ((st = launch_timed(s, cpl ? K_CPL_UPDATE : K_CG_UPDATE, a, nb, t)) != OC_OK) return st;
             }
             if ((st = launch_timed(s, K_INTEGRATE, a, nb, t)) != OC_OK) return st;
             if (s->any_provot && (st = launch_timed(s, K_PROVOT, a, nb, t)) != OC_OK) return st;
@@ -244,22 +270,37 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
     } else {
         // Assembly over every cloth, then the resident CG launches and the streamed loop.
         a.blk_base = 0;
-        if ((st = launch_timed(s, K_ASSEMBLE, a, s->n_blocks, t)) != OC_OK) return st;
-        s->host_launches += 1;
-        if ((st = launch_resident_all(s, a, t)) != OC_OK) return st;
-        StepArgs sa = a;
+        StepArgs aa = a, ca = a, sa = a, ua = a;
+        aa.blocks = s->d_asm_blocks;
+        ca.blocks = s->d_cpl_blocks;
         sa.blocks = s->d_streamed_blocks;
-        const int nb = s->n_streamed_blocks;
-        if (nb > 0) {
+        ua.blocks = s->d_upd_blocks;
+        if (s->n_asm_blocks > 0) {
+            if ((st = launch_timed(s, K_ASSEMBLE, aa, s->n_asm_blocks, t)) != OC_OK) return st;
+            s->host_launches += 1;
+        }
+        if (s->n_cpl_blocks > 0) {
+            if ((st = launch_timed(s, K_CPL_ASSEMBLE, ca, s->n_cpl_blocks, t)) != OC_OK) return st;
+            s->host_launches += 1;
+        }
+        if ((st = launch_resident_all(s, a, t)) != OC_OK) return st;
+        const int nb = s->n_streamed_blocks, nc = s->n_cpl_blocks;
+        if (nb > 0 || nc > 0) {
             for (;;) {
                 OC_TRY(cudaMemcpyAsync(s->h_scalar, a.unconverged, sizeof(int32_t), cudaMemcpyDeviceToHost,
                                        s->stream));
                 OC_TRY(cudaStreamSynchronize(s->stream));
                 if (*s->h_scalar <= 0) break;
-                if ((st = launch_timed(s, K_CG_DIR, sa, nb, t)) != OC_OK) return st;
-                if ((st = launch_timed(s, K_CG_UPDATE, sa, nb, t)) != OC_OK) return st;
+                if (nb > 0) {
+                    if ((st = launch_timed(s, K_CG_DIR, sa, nb, t)) != OC_OK) return st;
+                    if ((st = launch_timed(s, K_CG_UPDATE, sa, nb, t)) != OC_OK) return st;
+                }
+                if (nc > 0) {
+                    if ((st = launch_timed(s, K_CPL_DIR, ca, nc, t)) != OC_OK) return st;
+                    if ((st = launch_timed(s, K_CPL_UPDATE, ca, nc, t)) != OC_OK) return st;
+                }
             }
-            if ((st = launch_timed(s, K_INTEGRATE, sa, nb, t)) != OC_OK) return st;
+            if ((st = launch_timed(s, K_INTEGRATE, ua, s->n_upd_blocks, t)) != OC_OK) return st;
             s->host_launches += 1;
         }
         if (s->any_provot) {  // after every cloth's update, resident and streamed
@@ -288,28 +329,38 @@ oc_status build_graph(oc_solver* s, float dt) {
     cudaGraph_t g = nullptr;
     OC_TRY(cudaGraphCreate(&g, 0));
     s->graph = g;
-    const bool streamed = s->n_streamed_blocks > 0;
+    const bool streamed = s->n_streamed_blocks > 0, coupled = s->n_cpl_blocks > 0;
+    const bool loop = streamed || coupled;
     // The WHILE loop's handle exists only when there are streamed cloths (a handle that
     // no conditional node uses makes the graph fail to instantiate).
     cudaGraphConditionalHandle handle = 0;
-    if (streamed) OC_TRY(cudaGraphConditionalHandleCreate(&handle, g, 0, 0));
+    if (loop) OC_TRY(cudaGraphConditionalHandleCreate(&handle, g, 0, 0));
 
-    StepArgs a = s->args;  // full block table: the assembly covers every cloth
+    StepArgs a = s->args;  // full block table (the passes)
     a.dt = dt;
     a.blk_base = 0;
-    a.use_cond = streamed ? 1 : 0;
+    a.use_cond = loop ? 1 : 0;
     a.cond = (unsigned long long)handle;
-    StepArgs sa = a;  // streamed cloths only
-    sa.blocks = s->d_streamed_blocks;
+    StepArgs aa = a, sa = a, ca = a, ua = a;
+    aa.blocks = s->d_asm_blocks;       // REFERENCE cloths: k_assemble
+    sa.blocks = s->d_streamed_blocks;  // streamed REFERENCE cloths: CG loop
+    ca.blocks = s->d_cpl_blocks;       // COUPLED cloths
+    ua.blocks = s->d_upd_blocks;       // k_integrate
     void* params_all[] = {&a};
+    void* params_asm[] = {&aa};
     void* params_str[] = {&sa};
-    auto kparams = [&](KernelKind k, bool all) {
+    void* params_cpl[] = {&ca};
+    void* params_upd[] = {&ua};
+    enum Table { T_ALL, T_ASM, T_STR, T_CPL, T_UPD };
+    auto kparams = [&](KernelKind k, Table tab) {
         cudaKernelNodeParams kp{};
         kp.func = const_cast<void*>(kernel_fn(k));
-        kp.gridDim = dim3((unsigned)(all ? s->n_blocks : s->n_streamed_blocks));
+        const int n[] = {s->n_blocks, s->n_asm_blocks, s->n_streamed_blocks, s->n_cpl_blocks, s->n_upd_blocks};
+        void** pp[] = {params_all, params_asm, params_str, params_cpl, params_upd};
+        kp.gridDim = dim3((unsigned)n[tab]);
         kp.blockDim = dim3((unsigned)kernel_block_threads());
         kp.sharedMemBytes = (unsigned)kernel_smem_bytes(k);
-        kp.kernelParams = all ? params_all : params_str;
+        kp.kernelParams = pp[tab];
         kp.extra = nullptr;
         return kp;
     };
@@ -323,24 +374,47 @@ oc_status build_graph(oc_solver* s, float dt) {
     mp.height = 1;
     mp.pitch = sizeof(int32_t);
     OC_TRY(cudaGraphAddMemsetNode(&n_reset, g, nullptr, 0, &mp));
-    cudaKernelNodeParams kp = kparams(K_ASSEMBLE, true);
-    OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &n_reset, 1, &kp));
+    cudaKernelNodeParams kp{};
+    n_asm = n_reset;
+    if (s->n_asm_blocks > 0) {
+        kp = kparams(K_ASSEMBLE, T_ASM);
+        OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &n_reset, 1, &kp));
+    }
+    cudaGraphNode_t n_last = n_asm;  // the loop waits for every assembly
+    if (coupled) {
+        kp = kparams(K_CPL_ASSEMBLE, T_CPL);
+        OC_TRY(cudaGraphAddKernelNode(&n_last, g, &n_asm, 1, &kp));
+    }
     std::vector<cudaGraphNode_t> updates;  // the nodes that write X and V
 
-    if (streamed) {
-        cudaGraphNode_t n_loop, n_dir, n_upd, n_int;
+    if (loop) {
+        cudaGraphNode_t n_loop, n_int;
         cudaGraphNodeParams cp{};
         cp.type = cudaGraphNodeTypeConditional;
         cp.conditional.handle = handle;
         cp.conditional.type = cudaGraphCondTypeWhile;
         cp.conditional.size = 1;
-        OC_TRY(cudaGraphAddNode(&n_loop, g, &n_asm, nullptr, 1, &cp));
+        OC_TRY(cudaGraphAddNode(&n_loop, g, &n_last, nullptr, 1, &cp));
         cudaGraph_t body = cp.conditional.phGraph_out[0];
-        kp = kparams(K_CG_DIR, false);
-        OC_TRY(cudaGraphAddKernelNode(&n_dir, body, nullptr, 0, &kp));
-        kp = kparams(K_CG_UPDATE, false);
-        OC_TRY(cudaGraphAddKernelNode(&n_upd, body, &n_dir, 1, &kp));
-        kp = kparams(K_INTEGRATE, false);
+        // Body: the REFERENCE pair, then the COUPLED pair; the last update kernel's last
+        // block sets the condition from the counter both loops decrement.
+        cudaGraphNode_t prev = nullptr;
+        auto add_body = [&](KernelKind k, Table tab) -> cudaError_t {
+            cudaKernelNodeParams bp = kparams(k, tab);
+            cudaGraphNode_t n;
+            cudaError_t e = cudaGraphAddKernelNode(&n, body, prev ? &prev : nullptr, prev ? 1 : 0, &bp);
+            prev = n;
+            return e;
+        };
+        if (streamed) {
+            OC_TRY(add_body(K_CG_DIR, T_STR));
+            OC_TRY(add_body(K_CG_UPDATE, T_STR));
+        }
+        if (coupled) {
+            OC_TRY(add_body(K_CPL_DIR, T_CPL));
+            OC_TRY(add_body(K_CPL_UPDATE, T_CPL));
+        }
+        kp = kparams(K_INTEGRATE, T_UPD);
         OC_TRY(cudaGraphAddKernelNode(&n_int, g, &n_loop, 1, &kp));
         updates.push_back(n_int);
     }
@@ -368,7 +442,7 @@ oc_status build_graph(oc_solver* s, float dt) {
     }
     if (s->any_provot) {
         cudaGraphNode_t n_prov;
-        kp = kparams(K_PROVOT, true);
+        kp = kparams(K_PROVOT, T_ALL);
         OC_TRY(cudaGraphAddKernelNode(&n_prov, g, updates.data(), updates.size(), &kp));
     }
     OC_TRY(cudaGraphInstantiate(&s->exec, g, 0));
@@ -633,6 +707,25 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     a.blocks = blocks;
     for (const InstParams& ip : P.inst) s->any_passes = s->any_passes || ip.passes != 0;
     s->any_provot = P.any_provot;
+    s->any_coupled = P.any_coupled;
+    if (P.any_coupled) {
+        std::vector<int32_t> other(P.inc.size());
+        for (size_t k = 0; k < P.inc.size(); ++k) other[k] = P.inc[k].x & 0x7fffffff;
+        int32_t* d_other = nullptr;
+        OC_CREATE_TRY(upload(s, &d_other, other));
+        a.cpl_o = d_other;
+        float* cplanes = nullptr;
+        OC_CREATE_TRY(dalloc(s, &cplanes, 5 * std::max<size_t>(P.inc.size(), 1)));
+        for (int k = 0; k < 5; ++k) a.cpl_c[k] = cplanes + (size_t)k * std::max<size_t>(P.inc.size(), 1);
+        float* vplanes = nullptr;
+        OC_CREATE_TRY(dalloc(s, &vplanes, 7 * stride));
+        OC_CREATE_TRY(cudaMemset(vplanes, 0, 7 * stride * sizeof(float)));
+        a.cpl_m = vplanes;
+        for (int k = 0; k < 3; ++k) {
+            a.z[k] = vplanes + (1 + k) * stride;
+            a.q[k] = vplanes + (4 + k) * stride;
+        }
+    }
     {
         std::vector<uint8_t> pins((size_t)P.nv);
         for (int64_t g = 0; g < P.nv; ++g) pins[g] = P.V0[g].w != 0.0f ? 1 : 0;
@@ -647,24 +740,43 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
         const int max_res = o.resident_max_vertices > 0 ? o.resident_max_vertices
                                                         : kResidentMaxCluster * kResidentDefaultVcta;
         s->resident.assign(P.n_inst, 0);
-        std::vector<BlockInfo> streamed;
+        std::vector<BlockInfo> streamed, asm_ref, cpl, upd;
         std::map<std::tuple<int, int, int>, std::vector<int32_t>> groups;
         for (int32_t k = 0; k < P.n_inst; ++k) {
+            const bool cpl_k = P.inst[k].coupled != 0;
+            if (s->executor == OC_EXEC_RESIDENT && cpl_k) {
+                s->err = "instance " + std::to_string(k) + " is COUPLED: the resident executor runs REFERENCE cloths";
+                return bail(OC_ERR_UNSUPPORTED);
+            }
             int threads = 0, cluster = 0, vcta = 0;
-            const bool want = (s->executor == OC_EXEC_RESIDENT || s->executor == OC_EXEC_AUTO) &&
+            const bool want = !cpl_k && (s->executor == OC_EXEC_RESIDENT || s->executor == OC_EXEC_AUTO) &&
                               resident_shape(P.inst[k].nv, max_res, &threads, &cluster, &vcta);
             if (s->executor == OC_EXEC_RESIDENT && !want) {
                 s->err = "instance " + std::to_string(k) + " (" + std::to_string(P.inst[k].nv) +
                          " vertices) is too large for the resident executor";
                 return bail(OC_ERR_UNSUPPORTED);
             }
+            const BlockInfo* kb = P.blocks.data() + P.inst[k].blk0;
+            if (cpl_k) {
+                cpl.insert(cpl.end(), kb, kb + P.inst[k].nblk);
+                upd.insert(upd.end(), kb, kb + P.inst[k].nblk);
+                continue;
+            }
+            asm_ref.insert(asm_ref.end(), kb, kb + P.inst[k].nblk);
             if (want) {
                 s->resident[k] = 1;
                 groups[std::make_tuple(threads, cluster, vcta)].push_back(k);
             } else {
-                for (int32_t b = 0; b < P.inst[k].nblk; ++b) streamed.push_back(P.blocks[P.inst[k].blk0 + b]);
+                streamed.insert(streamed.end(), kb, kb + P.inst[k].nblk);
+                upd.insert(upd.end(), kb, kb + P.inst[k].nblk);
             }
         }
+        s->n_asm_blocks = (int32_t)asm_ref.size();
+        OC_CREATE_TRY(upload(s, &s->d_asm_blocks, asm_ref));
+        s->n_cpl_blocks = (int32_t)cpl.size();
+        OC_CREATE_TRY(upload(s, &s->d_cpl_blocks, cpl));
+        s->n_upd_blocks = (int32_t)upd.size();
+        OC_CREATE_TRY(upload(s, &s->d_upd_blocks, upd));
         std::vector<std::pair<std::tuple<int, int, int>, std::vector<int32_t>>> ordered(groups.begin(), groups.end());
         // Largest buckets first, so their clusters start before the small ones fill in.
         std::stable_sort(ordered.begin(), ordered.end(), [](const auto& x, const auto& y) {
@@ -809,8 +921,9 @@ oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
         if (st != OC_OK) return st;
     }
     for (int32_t i = 0; i < n_steps; ++i) OC_TRY(cudaGraphLaunch(s->exec, s->stream));
-    s->host_launches += (1 + (s->n_streamed_blocks > 0 ? 1 : 0) + (int64_t)s->buckets.size() + (s->any_provot ? 1 : 0)) *
-                        (int64_t)n_steps;
+    const int64_t per_step = (s->n_asm_blocks > 0 ? 1 : 0) + (s->n_cpl_blocks > 0 ? 1 : 0) +
+                             (s->n_upd_blocks > 0 ? 1 : 0) + (int64_t)s->buckets.size() + (s->any_provot ? 1 : 0);
+    s->host_launches += per_step * (int64_t)n_steps;
     return OC_OK;
 }
 
@@ -906,6 +1019,8 @@ oc_status oc_compute_forces(oc_solver* s, float* F) {
 
 oc_status oc_assemble(oc_solver* s, float dt, float* A9, float* b) {
     if (!valid_solver(s) || !A9 || !b || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
+    if (s->any_coupled)
+        return fail(s, OC_ERR_UNSUPPORTED, "oc_assemble: a COUPLED cloth's system is not block-diagonal");
     OC_TRY(cudaSetDevice(s->device));
     float* dA9 = nullptr;
     OC_TRY(cudaMallocAsync(&dA9, 9 * (size_t)s->nv * sizeof(float), s->stream));
@@ -941,11 +1056,13 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
     cudaEventDestroy(t.ev[0]);
     cudaEventDestroy(t.ev[1]);
     if (st != OC_OK) return st;
-    const KernelKind kinds[] = {K_ASSEMBLE, K_CG_DIR, K_CG_UPDATE, K_INTEGRATE, K_RESIDENT, K_PROVOT};
+    const KernelKind kinds[] = {K_ASSEMBLE,    K_CG_DIR,  K_CG_UPDATE, K_INTEGRATE, K_RESIDENT,
+                                K_PROVOT,      K_CPL_ASSEMBLE, K_CPL_DIR, K_CPL_UPDATE};
     int32_t n = 0;
     for (KernelKind k : kinds) {
         if (n >= max_kernels) break;
         if (k == K_PROVOT && !s->any_provot) continue;
+        if ((k == K_CPL_ASSEMBLE || k == K_CPL_DIR || k == K_CPL_UPDATE) && !s->any_coupled) continue;
         if (names) {
             std::memset(names + 32 * n, 0, 32);
             std::strncpy(names + 32 * n, kernel_name(k), 31);
@@ -1027,6 +1144,8 @@ oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t check
     if (s->any_passes)
         return fail(s, OC_ERR_UNSUPPORTED, "oc_tape_forward: the adjoint covers the implicit step only, not the "
                                            "passes after it");
+    if (s->any_coupled)
+        return fail(s, OC_ERR_UNSUPPORTED, "oc_tape_forward: the adjoint covers the REFERENCE Jacobian mode");
     OC_TRY(cudaSetDevice(s->device));
     auto& T = s->tape;
     const size_t state_bytes = 2 * sizeof(float4) * (size_t)s->nv + 3 * s->stride * sizeof(float);

@@ -24,6 +24,7 @@ struct InstParams {
     int32_t has_ext;
     int32_t resident;  // 1: this cloth's CG runs in the resident kernel, not the streamed loop
     int32_t passes;    // OC_PASS_* bits applied after the update
+    int32_t coupled;   // 1: OC_JAC_COUPLED (block-sparse system, oc_coupled.cu)
     float provot_ratio;     // IMP:808
     float ellipsoid[16];    // object -> world, column-major (IMP:583-585)
     float ellipsoid_inv[16];
@@ -82,6 +83,15 @@ struct StepArgs {
     const uint8_t* pinflag;  // 1 for pinned vertices (read by k_provot)
     int32_t only_passes;     // k_ellipsoid / k_provot: nonzero = apply these OC_PASS_* bits to
                              // every cloth (a pass run on its own), 0 = each cloth's own bits
+    // COUPLED cloths (allocated only when the handle has one).  Per incidence record:
+    // the other vertex and the spring block B = beta I + gamma n n^T of this step; per
+    // vertex: m' and the CG vectors z = P^-1 r and q = A d.  P^-1 (the inverse of the
+    // vertex's diagonal block) lives in the A planes.
+    const int32_t* cpl_o;
+    float* cpl_c[5];         // n0, n1, n2, beta, gamma
+    float* cpl_m;
+    float* z[3];
+    float* q[3];
 };
 
 // Adjoint buffers (oc_adjoint.cu); planes have the handle's vertex stride.
@@ -106,7 +116,12 @@ cudaError_t launch_set_spring_params(const StepArgs& a, const AdjArgs& j, const 
                                      int64_t n_rec, int64_t nv, cudaStream_t stream);
 
 enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3, K_FORCES = 4, K_RESIDENT = 5,
-                  K_PROVOT = 6, K_ELLIPSOID = 7, K_COUNT = 8 };
+                  K_PROVOT = 6, K_ELLIPSOID = 7, K_CPL_ASSEMBLE = 8, K_CPL_DIR = 9, K_CPL_UPDATE = 10,
+                  K_COUNT = 11 };
+
+// COUPLED kernels (oc_coupled.cu).
+const void* coupled_fn(KernelKind k);
+cudaError_t launch_coupled(KernelKind k, const StepArgs& a, int nblocks, cudaStream_t stream);
 
 const char* kernel_name(KernelKind k);
 const void* kernel_fn(KernelKind k);
@@ -154,6 +169,7 @@ struct PackedHost {
     std::vector<int32_t> own_sid;                     // vertex i -> id of spring i, or -1
     std::vector<int32_t> own_rowptr, own_ent;         // vertex -> vertices whose spring touches it
     bool any_provot = false;                          // some cloth has OC_PASS_PROVOT
+    bool any_coupled = false;                         // some cloth is OC_JAC_COUPLED
 };
 
 oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vertices_per_block, PackedHost* out,

@@ -487,6 +487,9 @@ const char* kernel_name(KernelKind k) {
         case K_RESIDENT: return "k_resident";
         case K_PROVOT: return "k_provot";
         case K_ELLIPSOID: return "k_ellipsoid";
+        case K_CPL_ASSEMBLE: return "k_cpl_assemble";
+        case K_CPL_DIR: return "k_cpl_dir";
+        case K_CPL_UPDATE: return "k_cpl_update";
         default: return "?";
     }
 }
@@ -500,6 +503,9 @@ const void* kernel_fn(KernelKind k) {
         case K_FORCES: return (const void*)k_forces;
         case K_PROVOT: return (const void*)k_provot;
         case K_ELLIPSOID: return (const void*)k_ellipsoid;
+        case K_CPL_ASSEMBLE:
+        case K_CPL_DIR:
+        case K_CPL_UPDATE: return coupled_fn(k);
         default: return nullptr;
     }
 }
@@ -549,6 +555,9 @@ cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStre
         case K_FORCES: k_forces<<<nblocks, kThreads, 0, stream>>>(a); break;
         case K_PROVOT: k_provot<<<nblocks, kThreads, 0, stream>>>(a); break;
         case K_ELLIPSOID: k_ellipsoid<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_CPL_ASSEMBLE:
+        case K_CPL_DIR:
+        case K_CPL_UPDATE: return launch_coupled(k, a, nblocks, stream);
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -44,7 +44,7 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
             *err = who + "bad sizes or NULL arrays";
             return OC_ERR_INVALID_ARGUMENT;
         }
-        if (d.jacobian_mode != OC_JAC_REFERENCE) {
+        if (d.jacobian_mode != OC_JAC_REFERENCE && d.jacobian_mode != OC_JAC_COUPLED) {
             *err = who + "jacobian_mode " + std::to_string(d.jacobian_mode) + " is not available";
             return OC_ERR_UNSUPPORTED;
         }
@@ -143,6 +143,7 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
     P.own_par.assign(nv, make_float4(0.f, 0.f, 0.f, 0.f));
     P.blocks.clear();
     P.any_provot = false;
+    P.any_coupled = false;
 
     std::vector<int32_t> deg(nv, 0);
     for (int32_t k = 0; k < n; ++k) {
@@ -179,6 +180,8 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
         ip.has_ext = d.ext_force ? 1 : 0;
         ip.resident = 0;
         ip.passes = d.passes;
+        ip.coupled = d.jacobian_mode == OC_JAC_COUPLED ? 1 : 0;
+        if (ip.coupled) P.any_coupled = true;
         ip.provot_ratio = d.provot_ratio == 0.0f ? 1.01f : d.provot_ratio;
         for (int i = 0; i < 16; ++i) {
             ip.ellipsoid[i] = d.ellipsoid[i];

@@ -38,7 +38,8 @@ SPRING_DTYPE = np.dtype(
 def build(reference: bool = True) -> None:
     """Compile the port (always) and the reference harness (when the tree is present)."""
     BUILD.mkdir(exist_ok=True)
-    srcs = [HERE / "oc_oracle.c", HERE / "oc_oracle_impl.h", HERE / "oc_oracle.h", HERE / "oc_adjoint.c"]
+    srcs = [HERE / "oc_oracle.c", HERE / "oc_oracle_impl.h", HERE / "oc_coupled_impl.h", HERE / "oc_oracle.h",
+            HERE / "oc_adjoint.c"]
     if not PORT_LIB.exists() or any(s.stat().st_mtime > PORT_LIB.stat().st_mtime for s in srcs):
         tmp = PORT_LIB.with_suffix(".so.tmp")
         subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
@@ -79,6 +80,11 @@ def port() -> C.CDLL:
             f.argtypes = [P, real, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
             f.restype = C.c_int
             getattr(lib, f"ocr_passes_{sfx}").argtypes = [P, C.c_void_p, C.c_void_p]
+            getattr(lib, f"ocr_coupled_matvec_{sfx}").argtypes = [P, real] + [C.c_void_p] * 3
+            getattr(lib, f"ocr_coupled_system_{sfx}").argtypes = [P, real] + [C.c_void_p] * 6
+            f = getattr(lib, f"ocr_coupled_step_{sfx}")
+            f.argtypes = [P, real, C.c_int32] + [C.c_void_p] * 6
+            f.restype = C.c_int
         lib.ocr_adjoint_f64.argtypes = [P, C.c_double, C.c_int32] + [C.c_void_p] * 10
         lib.ocr_adjoint_f64.restype = C.c_int
         _port = lib
@@ -183,6 +189,58 @@ def port_passes(cloth: Cloth, X, V, passes, fp64=False):
     (lib.ocr_passes_f64 if fp64 else lib.ocr_passes_f32)(C.byref(p), X.ctypes.data, V.ctypes.data)
     del keep
     return X.reshape(-1, 3), V.reshape(-1, 3)
+
+
+def coupled_step(cloth: Cloth, X, V, dV=None, dt=1.0 / 60.0, n_steps=1, fp64=False):
+    """The COUPLED Jacobian mode: (X, V, dV, iters, rel_residual, flags) after n_steps."""
+    lib = port()
+    real = np.float64 if fp64 else np.float32
+    X = np.ascontiguousarray(X, real).reshape(-1).copy()
+    V = np.ascontiguousarray(V, real).reshape(-1).copy()
+    dV = np.zeros_like(X) if dV is None else np.ascontiguousarray(dV, real).reshape(-1).copy()
+    iters = np.zeros(max(n_steps, 1), np.int32)
+    rr = np.zeros(max(n_steps, 1), np.float64)
+    fl = np.zeros(max(n_steps, 1), np.uint32)
+    p, keep = cloth.params(True, True, fp64)
+    fn = lib.ocr_coupled_step_f64 if fp64 else lib.ocr_coupled_step_f32
+    rc = fn(C.byref(p), float(real(dt)), int(n_steps), X.ctypes.data, V.ctypes.data, dV.ctypes.data,
+            iters.ctypes.data, rr.ctypes.data, fl.ctypes.data)
+    del keep
+    if rc != 0:
+        raise MemoryError("oracle coupled step failed")
+    return X.reshape(-1, 3), V.reshape(-1, 3), dV.reshape(-1, 3), iters[:n_steps], rr[:n_steps], fl[:n_steps]
+
+
+def coupled_matvec(cloth: Cloth, X, w, dt, fp64=True):
+    """y = A w of the COUPLED system at positions X (no pin filter)."""
+    lib = port()
+    real = np.float64 if fp64 else np.float32
+    X = np.ascontiguousarray(X, real).reshape(-1)
+    w = np.ascontiguousarray(w, real).reshape(-1)
+    y = np.zeros_like(w)
+    p, keep = cloth.params(True, True, fp64)
+    (lib.ocr_coupled_matvec_f64 if fp64 else lib.ocr_coupled_matvec_f32)(C.byref(p), float(real(dt)), X.ctypes.data,
+                                                                         w.ctypes.data, y.ctypes.data)
+    del keep
+    return y.reshape(-1, 3)
+
+
+def coupled_system(cloth: Cloth, X, V, dt, fp64=True):
+    """(D6, P6, b) of the COUPLED system: diagonal blocks, their inverses, right-hand side."""
+    lib = port()
+    real = np.float64 if fp64 else np.float32
+    X = np.ascontiguousarray(X, real).reshape(-1)
+    V = np.ascontiguousarray(V, real).reshape(-1)
+    F = port_forces(cloth, X, V, fp64).reshape(-1).astype(real)
+    D6 = np.zeros(6 * cloth.n_vertices, real)
+    P6 = np.zeros_like(D6)
+    b = np.zeros(3 * cloth.n_vertices, real)
+    p, keep = cloth.params(True, True, fp64)
+    (lib.ocr_coupled_system_f64 if fp64 else lib.ocr_coupled_system_f32)(
+        C.byref(p), float(real(dt)), X.ctypes.data, V.ctypes.data, F.ctypes.data, D6.ctypes.data, P6.ctypes.data,
+        b.ctypes.data)
+    del keep
+    return D6.reshape(-1, 6), P6.reshape(-1, 6), b.reshape(-1, 3)
 
 
 def port_forces(cloth: Cloth, X, V, fp64=False):

@@ -1,5 +1,5 @@
-/* Test infrastructure: instantiates the CPU restatement of the reference implicit step
- * in FP32 and FP64 (see oc_oracle.h).  Build with -O2 -ffp-contract=off and without
+/* Test infrastructure: instantiates the CPU restatement of the reference implicit step,
+ * and of the COUPLED Jacobian mode, in FP32 and FP64 (see oc_oracle.h).  Build with -O2 -ffp-contract=off and without
  * -ffast-math so every operation rounds as written. */
 #include "oc_oracle.h"
 
@@ -11,6 +11,7 @@
 #define SQRT sqrtf
 #define SFX(name) name##_f32
 #include "oc_oracle_impl.h"
+#include "oc_coupled_impl.h"
 #undef REAL
 #undef SQRT
 #undef SFX
@@ -19,6 +20,7 @@
 #define SQRT sqrt
 #define SFX(name) name##_f64
 #include "oc_oracle_impl.h"
+#include "oc_coupled_impl.h"
 #undef REAL
 #undef SQRT
 #undef SFX

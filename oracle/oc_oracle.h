@@ -79,6 +79,23 @@ int ocr_step_f64(const ocr_params* p, double dt, int32_t n_steps, double* X, dou
                  int32_t* iters, double* rel_residual);
 void ocr_passes_f64(const ocr_params* p, double* X, double* V);
 
+/* COUPLED Jacobian mode (oc_coupled_impl.h; no counterpart in the reference):
+ * Baraff-Witkin coupling of the per-spring blocks into one SPD block-sparse system,
+ * block-Jacobi PCG, V += dV.  Pins are p->pinned or {0, num_x}, always filtered; dot
+ * products sum REAL per-vertex terms in double; p->dot_fp64 / filter_pinned unused.
+ * matvec: y = A w (no pin filter).  system: diagonal blocks D6, their inverses P6 (6
+ * per vertex: a00 a01 a02 a11 a12 a22; either may be NULL) and b, from F. */
+void ocr_coupled_matvec_f32(const ocr_params* p, float h, const float* X, const float* w, float* y);
+void ocr_coupled_system_f32(const ocr_params* p, float h, const float* X, const float* V, const float* F, float* D6,
+                            float* P6, float* b);
+int ocr_coupled_step_f32(const ocr_params* p, float dt, int32_t n_steps, float* X, float* V, float* dV,
+                         int32_t* iters, double* rel_residual, uint32_t* flags);
+void ocr_coupled_matvec_f64(const ocr_params* p, double h, const double* X, const double* w, double* y);
+void ocr_coupled_system_f64(const ocr_params* p, double h, const double* X, const double* V, const double* F,
+                            double* D6, double* P6, double* b);
+int ocr_coupled_step_f64(const ocr_params* p, double dt, int32_t n_steps, double* X, double* V, double* dV,
+                         int32_t* iters, double* rel_residual, uint32_t* flags);
+
 /* FP64 adjoint of n_steps steps from (X0, V0) with a zero warm start (oc_adjoint.c):
  * given dL/dX_T, dL/dV_T (NULL = 0), returns the final state and dL/dX0, dL/dV0,
  * dL/dKs, dL/dKd (per spring) and dL/d(external force) (per vertex, constant in time).
