@@ -14,6 +14,10 @@ Workloads (synthetic, seeded):
              N(0,(1e-3 spacing)^2) position jitter, CG <= 200 iterations to 1e-5.
   batch4096  4096 cloths, side uniform in [8,128], per-type Ks log-uniform [10,500],
              Kd uniform [-0.5,-0.05], same jitter, CG <= 200 iterations to 1e-5.
+  coupled1025      grid1025 in the COUPLED Jacobian mode (Baraff-Witkin block-sparse
+                   system, block-Jacobi PCG to 1e-5, at most 200 iterations).
+  stepphysics1025  grid1025 plus EllipsoidCollision and ApplyProvotDynamicInverse after
+                   every step (the reference's whole StepPhysics).
 
 The timed region replays the step's CUDA graph K times on the solver's stream with
 inputs resident in HBM; the per-step working set (grid1025: ~0.75 GB) exceeds the 129 MB
@@ -72,7 +76,27 @@ def batch4096(seed: int, count: int = 4096):
     return descs, shapes, X, np.zeros_like(X)
 
 
-WORKLOADS = {"grid1025": grid1025, "batch4096": batch4096}
+def coupled1025(seed: int):
+    """grid1025 in the COUPLED Jacobian mode (Baraff-Witkin block-sparse system)."""
+    from opencloth_gb300 import JAC_COUPLED
+
+    descs, shapes, X, V = grid1025(seed)
+    descs[0].jacobian_mode = JAC_COUPLED
+    return descs, shapes, X, V
+
+
+def stepphysics1025(seed: int):
+    """grid1025 with the rest of StepPhysics: the reference's ellipsoid and Provot pass."""
+    from opencloth_gb300 import PASS_ELLIPSOID, PASS_PROVOT, reference_ellipsoid
+
+    descs, shapes, X, V = grid1025(seed)
+    descs[0].passes = PASS_ELLIPSOID | PASS_PROVOT
+    descs[0].ellipsoid, descs[0].ellipsoid_inv = reference_ellipsoid()
+    return descs, shapes, X, V
+
+
+WORKLOADS = {"grid1025": grid1025, "batch4096": batch4096, "coupled1025": coupled1025,
+             "stepphysics1025": stepphysics1025}
 
 
 def algorithmic_bytes(kernel: str, n_vertices: int, n_springs: int, first_dir: bool = False) -> int:
@@ -91,6 +115,18 @@ def algorithmic_bytes(kernel: str, n_vertices: int, n_springs: int, first_dir: b
         return 84 * N  # A 24 + d 12 + x 12 + r 12, write x 12 + r 12
     if kernel == "k_integrate":
         return 76 * N  # X, V 32 + dV 12 in, X, V 32 out
+    if kernel == "k_provot":
+        return 53 * N + 32 * S  # X 16, V 32, pin flag 1, rowptr 4; two records per spring
+    if kernel == "k_cpl_assemble":
+        # X, V 32, rowptr 4, warm start 12, P^-1 24, m' 4, r, z, d 36 per vertex; per
+        # spring two records in and two 20-byte blocks out.
+        return 112 * N + 72 * S
+    if kernel == "k_cpl_dir":
+        # pin flag 1, z 12 (+ d 12), m' 4, rowptr 4, q 12 per vertex; per spring the other
+        # vertex and the block at both ends.
+        return (33 if first_dir else 45) * N + 48 * S
+    if kernel == "k_cpl_update":
+        return (120 if first_dir else 132) * N  # z, (d), x, r, q, P^-1 in; x, r, d, z out
     raise KeyError(kernel)
 
 
@@ -259,12 +295,13 @@ def _dominant_roofline(prof: dict, peak: float, workload: str) -> dict:
 
 
 def _cg_roofline(prof: dict, peak: float) -> dict:
-    """The two SpMV-bound CG passes together."""
-    byts = prof["k_cg_dir"]["bytes"] + prof["k_cg_update"]["bytes"]
-    secs = (prof["k_cg_dir"]["ms_total"] + prof["k_cg_update"]["ms_total"]) / 1e3
+    """The two SpMV-bound CG passes together (the COUPLED pair when present)."""
+    pair = ["k_cpl_dir", "k_cpl_update"] if "k_cpl_dir" in prof else ["k_cg_dir", "k_cg_update"]
+    byts = sum(prof[k]["bytes"] for k in pair)
+    secs = sum(prof[k]["ms_total"] for k in pair) / 1e3
     achieved = byts / secs / 1e9 if secs > 0 else 0.0
-    return {"bound": "hbm", "kernels": ["k_cg_dir", "k_cg_update"], "achieved": achieved, "peak": peak,
-            "unit": "GB/s", "frac": achieved / peak}
+    return {"bound": "hbm", "kernels": pair, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak}
 
 
 def measure(name: str, args, steps: int, rank: int, world: int, local: int, plain_steps: int) -> dict:
@@ -335,18 +372,22 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
 
     # The plain GPU step on the same inputs: the same kernels, one launch sequence per
     # cloth, the CG loop driven from the host.
-    plain = ClothSolver(descs, device=local, stream=stream.cuda_stream, executor="plain")
-    plain.set_state(X0, V0)
-    plain.step(DT, 1)
-    plain.synchronize()
-    barrier()
-    ev0.record(stream)
-    plain.step(DT, plain_steps)
-    ev1.record(stream)
-    ev1.synchronize()
-    pms = max_over_ranks(ev0.elapsed_time(ev1))
-    plain_value = nv * plain_steps * world / (pms / 1e3)
-    plain.close()
+    plain_gpu = None
+    if plain_steps > 0:
+        plain = ClothSolver(descs, device=local, stream=stream.cuda_stream, executor="plain")
+        plain.set_state(X0, V0)
+        plain.step(DT, 1)
+        plain.synchronize()
+        barrier()
+        ev0.record(stream)
+        plain.step(DT, plain_steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        pms = max_over_ranks(ev0.elapsed_time(ev1))
+        plain_value = nv * plain_steps * world / (pms / 1e3)
+        plain.close()
+        plain_gpu = {"value": plain_value, "unit": METRIC, "ms_per_step": pms / plain_steps, "steps": plain_steps,
+                     "speedup": value / plain_value}
 
     return {
         "name": name, "descs": descs, "shapes": shapes, "X0": X0, "nv": nv, "ns": ns, "value": value,
@@ -356,8 +397,7 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
         "roofline": roof, "cg_roofline": cg_roof, "e2e": e2e,
         "kernels": {k: {"avg_us": 1e3 * v["ms_total"] / max(v["launches"], 1), "launches": v["launches"]}
                     for k, v in prof.items()},
-        "plain_gpu": {"value": plain_value, "unit": METRIC, "ms_per_step": pms / plain_steps,
-                      "steps": plain_steps, "speedup": value / plain_value},
+        "plain_gpu": plain_gpu,
     }
 
 
@@ -448,12 +488,13 @@ def run_ours(args) -> None:
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    names = ["grid1025", "batch4096"] if args.workload == "all" else [args.workload]
+    names = (["grid1025", "batch4096", "coupled1025", "stepphysics1025"] if args.workload == "all"
+             else [args.workload])
+    plain_steps = {"grid1025": 20, "batch4096": 2, "coupled1025": 3, "stepphysics1025": 0}
     results = []
     for name in names:
         steps = args.steps if name == names[0] else max(10, args.steps // 20)
-        plain_steps = 20 if name == "grid1025" else 2
-        results.append(measure(name, args, steps, rank, world, local, plain_steps))
+        results.append(measure(name, args, steps, rank, world, local, plain_steps[name]))
     if rank == 0:
         r = results[0]
         cpu_v, cores, kind, sample = cpu_throughput(r["name"], r["descs"], r["shapes"], r["X0"], 12.0,
@@ -493,7 +534,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["all"], default="all",
-                    help="all: the 1M-vertex cloth (headline value) and the 4096-cloth batch")
+                    help="all: the 1M-vertex cloth (headline value), the 4096-cloth batch, the 1M-vertex "
+                         "cloth in the COUPLED mode and with the StepPhysics passes")
     ap.add_argument("--seed", type=int, default=20261203)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -1,6 +1,6 @@
 """Run a few implicit steps of a synthetic workload, for profilers and launch-shape sweeps.
 
-    python -m opencloth_gb300.profile_step --cols 1025 --steps 3 [--vpt 4] [--instances 1]
+    python -m opencloth_gb300.profile_step --cols 1025 --steps 3 [--vpt 4] [--instances 1] [--coupled] [--passes]
 
 Prints one JSON line: graph-replayed ms/step (CUDA events on the solver's stream) and
 the per-kernel average durations of an un-graphed pass.
@@ -13,10 +13,11 @@ import time
 
 import numpy as np
 
-from . import ClothDesc, ClothSolver, grid_cloth
+from . import JAC_COUPLED, JAC_REFERENCE, PASS_ELLIPSOID, PASS_PROVOT, ClothDesc, ClothSolver, grid_cloth
+from .cloth import reference_ellipsoid
 
 
-def workload(cols: int, instances: int, seed: int, random_sides: bool):
+def workload(cols: int, instances: int, seed: int, random_sides: bool, coupled: bool = False, passes: bool = False):
     rng = np.random.default_rng(seed)
     descs, Xs = [], []
     for k in range(instances):
@@ -24,8 +25,11 @@ def workload(cols: int, instances: int, seed: int, random_sides: bool):
         ks = np.exp(rng.uniform(np.log(10.0), np.log(500.0), 3)) if random_sides else (50.75, 50.75, 50.95)
         kd = rng.uniform(-0.5, -0.05, 3) if random_sides else (-0.25, -0.25, -0.25)
         X, sp = grid_cloth(n, n, ks=tuple(ks), kd=tuple(kd), jitter=1e-3, seed=seed + k)
+        E, Einv = reference_ellipsoid() if passes else (None, None)
         descs.append(ClothDesc(n_vertices=n * n, springs=sp, pinned=np.array([0, n - 1], np.int32),
-                               cg_max_iter=200, cg_tol=1e-5))
+                               cg_max_iter=200, cg_tol=1e-5, jacobian_mode=JAC_COUPLED if coupled else JAC_REFERENCE,
+                               passes=(PASS_ELLIPSOID | PASS_PROVOT) if passes else 0, ellipsoid=E,
+                               ellipsoid_inv=Einv))
         Xs.append(X)
     return descs, np.concatenate(Xs)
 
@@ -45,9 +49,11 @@ def main() -> None:
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--no-graph", action="store_true", help="launch kernels directly (CG loop driven from the host)")
     ap.add_argument("--own-stream", action="store_true", help="let the library create its stream")
+    ap.add_argument("--coupled", action="store_true", help="COUPLED Jacobian mode")
+    ap.add_argument("--passes", action="store_true", help="ellipsoid collision and Provot pass after each step")
     a = ap.parse_args()
     t0 = time.perf_counter()
-    descs, X = workload(a.cols, a.instances, a.seed, a.random_sides)
+    descs, X = workload(a.cols, a.instances, a.seed, a.random_sides, a.coupled, a.passes)
     stream = torch.cuda.Stream()
     s = ClothSolver(descs, stream=None if a.own_stream else stream.cuda_stream, vertices_per_thread=a.vpt,
                     executor=a.executor, use_graph=not a.no_graph)
