@@ -163,6 +163,24 @@ oc_status oc_set_passes(oc_solver* s, int32_t instance, int32_t passes);
  * (IMP:800) called on their own.  Asynchronous on the handle's stream. */
 oc_status oc_apply_passes(oc_solver* s, int32_t passes);
 
+/* ---- interaction and constraints (device state, on the handle's stream) --------------- */
+/* The reference's picking loop (IMP:399-405): the lowest vertex index of cloth `instance`
+ * (instance-local) whose distance to `point` is below `radius` (the reference uses 0.1),
+ * or -1.  Waits for the handle's stream. */
+oc_status oc_pick_vertex(oc_solver* s, int32_t instance, const float point[3], double radius, int32_t* index);
+/* The reference's drag of a picked vertex (IMP:433-438): V = 0; X.x += delta[0];
+ * X.y += delta[1] only if the result stays > 0; X.z += delta[2].  `index` is
+ * instance-local.  (The reference's delta is Right[0] valX, Up[1] valY and
+ * Right[2] valX + Up[2] valY from the view, IMP:424-438.) */
+oc_status oc_drag_vertex(oc_solver* s, int32_t instance, int32_t index, const float delta[3]);
+/* Overwrite the positions and/or velocities (either may be NULL) of n distinct vertices,
+ * given by handle-global index, from host float triples: per-step position/velocity
+ * constraints.  Masses and pin flags are kept. */
+oc_status oc_set_vertices(oc_solver* s, int32_t n, const int64_t* indices, const float* X, const float* V);
+/* Replace the pin set of one cloth (instance-local indices; n_pins may be 0).  Takes effect
+ * from the next step; invalidates the tape of oc_tape_forward. */
+oc_status oc_set_pins(oc_solver* s, int32_t instance, const int32_t* pins, int32_t n_pins);
+
 /* Per-instance results of the last step: CG iterations, relative residual
  * sqrt(delta_new / delta0), OC_FLAG_* bits.  Any pointer may be NULL. */
 oc_status oc_get_stats(oc_solver* s, int32_t* cg_iters, double* rel_residual, uint32_t* flags);

@@ -93,6 +93,10 @@ SIGNATURES = {
     "oc_synchronize": (C.c_int32, [_P]),
     "oc_set_passes": (C.c_int32, [_P, C.c_int32, C.c_int32]),
     "oc_apply_passes": (C.c_int32, [_P, C.c_int32]),
+    "oc_pick_vertex": (C.c_int32, [_P, C.c_int32, _P, C.c_double, C.POINTER(C.c_int32)]),
+    "oc_drag_vertex": (C.c_int32, [_P, C.c_int32, C.c_int32, _P]),
+    "oc_set_vertices": (C.c_int32, [_P, C.c_int32, _P, _P, _P]),
+    "oc_set_pins": (C.c_int32, [_P, C.c_int32, _P, C.c_int32]),
     "oc_get_stats": (C.c_int32, [_P, _P, _P, _P]),
     "oc_get_launch_count": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
     "oc_compute_forces": (C.c_int32, [_P, _P]),

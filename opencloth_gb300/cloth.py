@@ -229,6 +229,34 @@ class ClothSolver:
         """Passes after the update (PASS_* bits) of one cloth, or of all (-1)."""
         self._call(self._lib.oc_set_passes(self._h, int(instance), int(passes)))
 
+    def pick_vertex(self, point, radius: float = 0.1, instance: int = 0) -> int:
+        """The reference's picking (IMP:399-405): lowest index of cloth ``instance`` within
+        ``radius`` of ``point``, or -1."""
+        p = np.ascontiguousarray(point, np.float32).reshape(3)
+        out = C.c_int32()
+        self._call(self._lib.oc_pick_vertex(self._h, int(instance), ptr(p), float(radius), C.byref(out)))
+        return int(out.value)
+
+    def drag_vertex(self, index: int, delta, instance: int = 0) -> None:
+        """The reference's drag (IMP:433-438): V = 0, X += delta, y kept above 0."""
+        d = np.ascontiguousarray(delta, np.float32).reshape(3)
+        self._call(self._lib.oc_drag_vertex(self._h, int(instance), int(index), ptr(d)))
+
+    def set_vertices(self, indices, X=None, V=None) -> None:
+        """Overwrite positions and/or velocities of the given (handle-global) vertices."""
+        idx = np.ascontiguousarray(indices, np.int64).reshape(-1)
+        Xa = None if X is None else np.ascontiguousarray(X, np.float32).reshape(-1, 3)
+        Va = None if V is None else np.ascontiguousarray(V, np.float32).reshape(-1, 3)
+        for a in (Xa, Va):
+            if a is not None and len(a) != len(idx):
+                raise ValueError("one position / velocity triple per index")
+        self._call(self._lib.oc_set_vertices(self._h, len(idx), ptr(idx), ptr(Xa), ptr(Va)))
+
+    def set_pins(self, pins, instance: int = 0) -> None:
+        """Replace the pin set of cloth ``instance`` (instance-local indices)."""
+        p = np.ascontiguousarray(pins, np.int32).reshape(-1)
+        self._call(self._lib.oc_set_pins(self._h, int(instance), ptr(p) if p.size else None, int(p.size)))
+
     def apply_passes(self, passes: int) -> None:
         """Run the passes once on the current state, no step (EllipsoidCollision,
         ApplyProvotDynamicInverse called on their own)."""

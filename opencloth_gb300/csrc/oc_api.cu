@@ -974,6 +974,77 @@ oc_status oc_apply_passes(oc_solver* s, int32_t passes) {
     return OC_OK;
 }
 
+oc_status oc_pick_vertex(oc_solver* s, int32_t instance, const float point[3], double radius, int32_t* index) {
+    if (!valid_solver(s) || !point || !index || instance < 0 || instance >= s->n_inst || !std::isfinite(radius))
+        return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    OC_TRY(cudaMemsetAsync(s->d_err, 0x7f, sizeof(int32_t), s->stream));  // 0x7f7f7f7f: "none"
+    OC_TRY(launch_pick(s->args.X, s->v_off[instance], s->v_off[instance + 1] - s->v_off[instance], point, radius,
+                       s->d_err, s->stream));
+    OC_TRY(cudaMemcpyAsync(s->h_scalar, s->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    *index = *s->h_scalar == 0x7f7f7f7f ? -1 : *s->h_scalar;
+    return OC_OK;
+}
+
+oc_status oc_drag_vertex(oc_solver* s, int32_t instance, int32_t index, const float delta[3]) {
+    if (!valid_solver(s) || !delta || instance < 0 || instance >= s->n_inst) return OC_ERR_INVALID_ARGUMENT;
+    if (index < 0 || index >= s->v_off[instance + 1] - s->v_off[instance])
+        return fail(s, OC_ERR_BAD_INDEX, "oc_drag_vertex: index outside the cloth");
+    if (!std::isfinite(delta[0]) || !std::isfinite(delta[1]) || !std::isfinite(delta[2]))
+        return fail(s, OC_ERR_NON_FINITE, "oc_drag_vertex: delta not finite");
+    OC_TRY(cudaSetDevice(s->device));
+    OC_TRY(launch_drag(s->args.X, s->args.V, s->v_off[instance] + index, delta, s->stream));
+    return OC_OK;
+}
+
+oc_status oc_set_vertices(oc_solver* s, int32_t n, const int64_t* indices, const float* X, const float* V) {
+    if (!valid_solver(s) || n < 0 || (n > 0 && !indices)) return OC_ERR_INVALID_ARGUMENT;
+    if ((int64_t)n > s->nv) return fail(s, OC_ERR_INVALID_ARGUMENT, "oc_set_vertices: more entries than vertices");
+    for (int32_t k = 0; k < n; ++k)
+        if (indices[k] < 0 || indices[k] >= s->nv) return fail(s, OC_ERR_BAD_INDEX, "oc_set_vertices: bad index");
+    {
+        std::vector<int64_t> sorted(indices, indices + n);
+        std::sort(sorted.begin(), sorted.end());
+        if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+            return fail(s, OC_ERR_INVALID_ARGUMENT, "oc_set_vertices: an index appears twice");
+    }
+    for (const float* p : {X, V})
+        if (p)
+            for (size_t k = 0; k < 3 * (size_t)n; ++k)
+                if (!std::isfinite(p[k])) return fail(s, OC_ERR_NON_FINITE, "oc_set_vertices: value not finite");
+    if (n == 0 || (!X && !V)) return OC_OK;
+    OC_TRY(cudaSetDevice(s->device));
+    // Staging: indices (2 floats each), then X, then V, within the 9 x n_vertices buffer.
+    int64_t* d_idx = reinterpret_cast<int64_t*>(s->stage);
+    float* d_X = s->stage + 2 * (size_t)n;
+    float* d_V = d_X + 3 * (size_t)n;
+    OC_TRY(cudaMemcpyAsync(d_idx, indices, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s->stream));
+    if (X) OC_TRY(cudaMemcpyAsync(d_X, X, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->stream));
+    if (V) OC_TRY(cudaMemcpyAsync(d_V, V, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s->stream));
+    OC_TRY(launch_set_vertices(s->args.X, s->args.V, d_idx, X ? d_X : nullptr, V ? d_V : nullptr, n, s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));  // the host arrays may be reused on return
+    return OC_OK;
+}
+
+oc_status oc_set_pins(oc_solver* s, int32_t instance, const int32_t* pins, int32_t n_pins) {
+    if (!valid_solver(s) || instance < 0 || instance >= s->n_inst || n_pins < 0 || (n_pins > 0 && !pins))
+        return OC_ERR_INVALID_ARGUMENT;
+    const int64_t nv = s->v_off[instance + 1] - s->v_off[instance];
+    if (n_pins > nv) return fail(s, OC_ERR_INVALID_ARGUMENT, "oc_set_pins: more pins than vertices");
+    for (int32_t k = 0; k < n_pins; ++k)
+        if (pins[k] < 0 || pins[k] >= nv) return fail(s, OC_ERR_BAD_INDEX, "oc_set_pins: pin outside the cloth");
+    OC_TRY(cudaSetDevice(s->device));
+    int32_t* d_pins = reinterpret_cast<int32_t*>(s->stage);
+    if (n_pins > 0)
+        OC_TRY(cudaMemcpyAsync(d_pins, pins, sizeof(int32_t) * n_pins, cudaMemcpyHostToDevice, s->stream));
+    OC_TRY(launch_set_pins(s->args.V, const_cast<uint8_t*>(s->args.pinflag), s->v_off[instance], nv, d_pins, n_pins,
+                           s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    s->tape.valid = false;
+    return OC_OK;
+}
+
 oc_status oc_synchronize(oc_solver* s) {
     if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
     OC_TRY(cudaStreamSynchronize(s->stream));

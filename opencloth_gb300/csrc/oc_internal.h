@@ -119,6 +119,15 @@ enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3
                   K_PROVOT = 6, K_ELLIPSOID = 7, K_CPL_ASSEMBLE = 8, K_CPL_DIR = 9, K_CPL_UPDATE = 10,
                   K_COUNT = 11 };
 
+// Interaction kernels (oc_interact.cu).
+cudaError_t launch_pick(const float4* X, int64_t v0, int64_t nv, const float pt[3], double radius, int32_t* out,
+                        cudaStream_t stream);
+cudaError_t launch_drag(float4* X, float4* V, int64_t g, const float delta[3], cudaStream_t stream);
+cudaError_t launch_set_vertices(float4* X, float4* V, const int64_t* idx, const float* X3, const float* V3,
+                                int32_t n, cudaStream_t stream);
+cudaError_t launch_set_pins(float4* V, uint8_t* pinflag, int64_t v0, int64_t nv, const int32_t* pins, int32_t n,
+                            cudaStream_t stream);
+
 // COUPLED kernels (oc_coupled.cu).
 const void* coupled_fn(KernelKind k);
 cudaError_t launch_coupled(KernelKind k, const StepArgs& a, int nblocks, cudaStream_t stream);

@@ -243,6 +243,34 @@ def coupled_system(cloth: Cloth, X, V, dt, fp64=True):
     return D6.reshape(-1, 6), P6.reshape(-1, 6), b.reshape(-1, 3)
 
 
+def ref_pick(X, point, radius=0.1) -> int:
+    """OnMouseDown's picking loop, IMP:399-405: the first i with
+    glm::distance(X[i], pt) < 0.1 (FP32 length of pt - X[i], squares summed left to
+    right; compared in double, as the literal 0.1 is), else -1."""
+    X = np.asarray(X, np.float32).reshape(-1, 3)
+    p = np.asarray(point, np.float32).reshape(3)
+    d = p[None, :] - X
+    sq = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+    dist = np.sqrt(sq, dtype=np.float32)
+    hit = np.nonzero(dist.astype(np.float64) < float(radius))[0]
+    return int(hit[0]) if hit.size else -1
+
+
+def ref_drag(X, V, index, delta):
+    """OnMouseMove's drag of the selected vertex, IMP:433-438, on copies of (X, V):
+    V = 0; X.x += dx; X.y += dy only if the result stays > 0; X.z += dz (FP32)."""
+    X = np.array(X, np.float32).reshape(-1, 3)
+    V = np.array(V, np.float32).reshape(-1, 3)
+    d = np.asarray(delta, np.float32)
+    V[index] = 0.0
+    X[index, 0] = np.float32(X[index, 0] + d[0])
+    ny = np.float32(X[index, 1] + d[1])
+    if ny > 0:
+        X[index, 1] = ny
+    X[index, 2] = np.float32(X[index, 2] + d[2])
+    return X, V
+
+
 def port_forces(cloth: Cloth, X, V, fp64=False):
     lib = port()
     real = np.float64 if fp64 else np.float32
