@@ -247,6 +247,45 @@ oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* t
 oc_status oc_pcg_solve_noalloc(const float* A9, const float* b, float* x, const uint8_t* pinned, int32_t n_vertices,
                                int32_t cg_max_iter, float cg_tol, int32_t* cg_iters, uint32_t* flags, void* stream);
 
+/* ---- block-sparse CG of the FEM demo (FEM:837-922) --------------------------------- */
+/* ConjugateGradientSolver of OpenCloth_CoRotated_Linear_FEM (FEM), batched: each system
+ * is a block-row matrix (the reference's vector<map<int, mat3>> A_row, FEM:123) in CSR
+ * with strictly ascending columns per row (std::map order), 3x3 float blocks stored as
+ * glm keeps them (m[c][r] at 3c + r; the product's component c is
+ * m[c][0] x + m[c][1] y + m[c][2] z, FEM:873-875), a right-hand side b and the unknown V
+ * (warm start in, solution out).  Fixed rows (IsFixed, FEM:117) are skipped; their
+ * blocks and b may be non-finite, as the reference's FLT_MAX masses make them.  Exactly
+ * cg_max_iter iterations run (the reference's exit test, FEM:905, cannot fire). */
+typedef struct oc_bsr_desc {
+    int32_t n_rows;
+    int32_t nnzb;
+    const int32_t* row_ptr; /* n_rows + 1, row_ptr[0] = 0, row_ptr[n_rows] = nnzb */
+    const int32_t* col;     /* nnzb, strictly ascending within each row */
+    const uint8_t* fixed;   /* n_rows flags, or NULL for none */
+    int32_t cg_max_iter;    /* i_max, FEM:134 */
+    float tolerance;        /* tolerence, FEM:133 (kept for the record; see above) */
+    float tiny;             /* tiny, FEM:132: the d and d2 clamps, FEM:885-886, 908-909 */
+} oc_bsr_desc;
+
+typedef struct oc_bsr_solver oc_bsr_solver;
+
+/* Validate and upload the sparsity of n_systems systems (options: device, stream,
+ * use_graph).  Fails with OC_ERR_BAD_INDEX / OC_ERR_INVALID_ARGUMENT on bad patterns. */
+oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_options* opts, oc_bsr_solver** out);
+void oc_bsr_destroy(oc_bsr_solver* s);
+const char* oc_bsr_last_error(const oc_bsr_solver* s);
+oc_status oc_bsr_get_counts(const oc_bsr_solver* s, int64_t* rows, int64_t* nnzb, int32_t* n_systems);
+/* Host arrays concatenated over the systems in creation order: blocks 9 x nnzb, b and x
+ * 3 x rows; NULL keeps the current value.  Non-finite values in free rows fail with
+ * OC_ERR_NON_FINITE. */
+oc_status oc_bsr_set_system(oc_bsr_solver* s, const float* blocks, const float* b, const float* x);
+/* The CG on every system (asynchronous on the handle's stream). */
+oc_status oc_bsr_solve(oc_bsr_solver* s);
+/* The solution V and the final residual (3 x rows each; either may be NULL). */
+oc_status oc_bsr_get_solution(oc_bsr_solver* s, float* x, float* residual);
+oc_status oc_bsr_get_launch_count(oc_bsr_solver* s, int64_t* kernels_launched);
+oc_status oc_bsr_synchronize(oc_bsr_solver* s);
+
 /* ---- reference topology builder (IMP:497-565) ------------------------------------ */
 /* Number of springs InitGL() creates for a cols x rows vertex grid (cols, rows >= 3):
  * rows*(cols-1) + cols*(rows-1) + 2*(rows-1)*(cols-1) + rows*(cols-1) + cols*(rows-1),

@@ -63,6 +63,19 @@ class ClothDescC(C.Structure):
     ]
 
 
+class BsrDescC(C.Structure):
+    _fields_ = [
+        ("n_rows", C.c_int32),
+        ("nnzb", C.c_int32),
+        ("row_ptr", C.c_void_p),
+        ("col", C.c_void_p),
+        ("fixed", C.c_void_p),
+        ("cg_max_iter", C.c_int32),
+        ("tolerance", C.c_float),
+        ("tiny", C.c_float),
+    ]
+
+
 class OptionsC(C.Structure):
     _fields_ = [
         ("executor", C.c_int32),
@@ -109,6 +122,15 @@ SIGNATURES = {
     "oc_tape_info": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
     "oc_pcg_solve_noalloc": (C.c_int32, [_P, _P, _P, _P, C.c_int32, C.c_int32, C.c_float, C.POINTER(C.c_int32),
                                          C.POINTER(C.c_uint32), _P]),
+    "oc_bsr_create": (C.c_int32, [C.POINTER(BsrDescC), C.c_int32, C.POINTER(OptionsC), C.POINTER(_P)]),
+    "oc_bsr_destroy": (None, [_P]),
+    "oc_bsr_last_error": (C.c_char_p, [_P]),
+    "oc_bsr_get_counts": (C.c_int32, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
+    "oc_bsr_set_system": (C.c_int32, [_P, _P, _P, _P]),
+    "oc_bsr_solve": (C.c_int32, [_P]),
+    "oc_bsr_get_solution": (C.c_int32, [_P, _P, _P]),
+    "oc_bsr_get_launch_count": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
+    "oc_bsr_synchronize": (C.c_int32, [_P]),
     "oc_grid_spring_count": (C.c_int32, [C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
     "oc_grid_build": (C.c_int32, [C.c_int32, C.c_int32, C.c_float, _P, _P, C.c_float, C.c_uint64, _P, _P]),
 }

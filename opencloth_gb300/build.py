@@ -27,7 +27,7 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fno-strict-aliasing", "-I", str(INCLUDE), "-I", str(CSRC),
 ]
 SOURCES = ["oc_kernels.cu", "oc_resident.cu", "oc_adjoint.cu", "oc_api.cu", "oc_topology.cpp", "oc_noalloc.cu",
-           "oc_coupled.cu", "oc_interact.cu"]
+           "oc_coupled.cu", "oc_interact.cu", "oc_bsr.cu"]
 
 
 def _nvcc() -> str:

@@ -17,6 +17,7 @@ Two oracles:
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 import struct
 import subprocess
@@ -38,8 +39,8 @@ SPRING_DTYPE = np.dtype(
 def build(reference: bool = True) -> None:
     """Compile the port (always) and the reference harness (when the tree is present)."""
     BUILD.mkdir(exist_ok=True)
-    srcs = [HERE / "oc_oracle.c", HERE / "oc_oracle_impl.h", HERE / "oc_coupled_impl.h", HERE / "oc_oracle.h",
-            HERE / "oc_adjoint.c"]
+    srcs = [HERE / "oc_oracle.c", HERE / "oc_oracle_impl.h", HERE / "oc_coupled_impl.h", HERE / "oc_bsr_impl.h",
+            HERE / "oc_oracle.h", HERE / "oc_adjoint.c"]
     if not PORT_LIB.exists() or any(s.stat().st_mtime > PORT_LIB.stat().st_mtime for s in srcs):
         tmp = PORT_LIB.with_suffix(".so.tmp")
         subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
@@ -84,6 +85,9 @@ def port() -> C.CDLL:
             getattr(lib, f"ocr_coupled_system_{sfx}").argtypes = [P, real] + [C.c_void_p] * 6
             f = getattr(lib, f"ocr_coupled_step_{sfx}")
             f.argtypes = [P, real, C.c_int32] + [C.c_void_p] * 6
+            f.restype = C.c_int
+            f = getattr(lib, f"ocr_bsr_cg_{sfx}")
+            f.argtypes = [C.c_int32] + [C.c_void_p] * 6 + [C.c_int32, C.c_float, C.c_int32, C.c_void_p]
             f.restype = C.c_int
         lib.ocr_adjoint_f64.argtypes = [P, C.c_double, C.c_int32] + [C.c_void_p] * 10
         lib.ocr_adjoint_f64.restype = C.c_int
@@ -241,6 +245,101 @@ def coupled_system(cloth: Cloth, X, V, dt, fp64=True):
         b.ctypes.data)
     del keep
     return D6.reshape(-1, 6), P6.reshape(-1, 6), b.reshape(-1, 3)
+
+
+class BsrSystem:
+    """One block-sparse system of the FEM demo's CG (FEM:837-922): block rows in CSR
+    (ascending columns), blocks (nnzb, 9) float32 with m[c][r] at 3c + r, b and the warm
+    start V (n, 3), fixed flags, i_max, tolerance and tiny."""
+
+    def __init__(self, row_ptr, col, blocks, b, V, fixed, i_max=20, tolerance=1e-3, tiny=1e-10):
+        self.row_ptr = np.ascontiguousarray(row_ptr, np.int32)
+        self.col = np.ascontiguousarray(col, np.int32)
+        self.blocks = np.ascontiguousarray(blocks, np.float32).reshape(-1, 9)
+        self.b = np.ascontiguousarray(b, np.float32).reshape(-1, 3)
+        self.V = np.ascontiguousarray(V, np.float32).reshape(-1, 3)
+        self.fixed = np.ascontiguousarray(fixed, np.uint8)
+        self.i_max = int(i_max)
+        self.tolerance = float(np.float32(tolerance))
+        self.tiny = float(np.float32(tiny))
+
+    @property
+    def n(self) -> int:
+        return len(self.row_ptr) - 1
+
+    def to_bytes(self) -> bytes:
+        head = b"OCB1" + np.array([self.n, len(self.col), self.i_max], np.int32).tobytes() + \
+            np.array([self.tolerance, self.tiny], np.float32).tobytes()
+        return b"".join([head, self.row_ptr.tobytes(), self.col.tobytes(), self.blocks.tobytes(), self.b.tobytes(),
+                         self.V.tobytes(), self.fixed.tobytes()])
+
+    @classmethod
+    def from_bytes(cls, data: bytes) -> "BsrSystem":
+        n, nnzb, i_max = np.frombuffer(data, np.int32, 3, 4)
+        tol, tiny = np.frombuffer(data, np.float32, 2, 16)
+        o = 24
+        rp = np.frombuffer(data, np.int32, n + 1, o); o += 4 * (n + 1)
+        col = np.frombuffer(data, np.int32, nnzb, o); o += 4 * nnzb
+        blk = np.frombuffer(data, np.float32, 9 * nnzb, o); o += 36 * nnzb
+        b = np.frombuffer(data, np.float32, 3 * n, o); o += 12 * n
+        V = np.frombuffer(data, np.float32, 3 * n, o); o += 12 * n
+        fixed = np.frombuffer(data, np.uint8, n, o)
+        return cls(rp, col, blk, b, V, fixed, int(i_max), float(tol), float(tiny))
+
+
+def bsr_cg(sys_: BsrSystem, fp64=False, dot_fp64=False):
+    """The restatement of ConjugateGradientSolver (FEM:837-922): (V, residual)."""
+    lib = port()
+    real = np.float64 if fp64 else np.float32
+    x = sys_.V.astype(real).reshape(-1).copy()
+    b = sys_.b.astype(real).reshape(-1)
+    res = np.zeros_like(x)
+    fn = lib.ocr_bsr_cg_f64 if fp64 else lib.ocr_bsr_cg_f32
+    rc = fn(sys_.n, sys_.row_ptr.ctypes.data, sys_.col.ctypes.data, sys_.blocks.ctypes.data, b.ctypes.data,
+            x.ctypes.data, sys_.fixed.ctypes.data, sys_.i_max, sys_.tiny, 1 if dot_fp64 else 0, res.ctypes.data)
+    if rc != 0:
+        raise MemoryError("oracle bsr cg failed")
+    return x.reshape(-1, 3), res.reshape(-1, 3)
+
+
+def fem_binary(fp64: bool = False) -> Path:
+    return REF / ("fem_step_f64" if fp64 else "fem_step_f32")
+
+
+def fem_available() -> bool:
+    return fem_binary().exists() and fem_binary(True).exists()
+
+
+def _fem_env(dims):
+    return dict(os.environ, OC_FEM_X=str(int(dims[0])), OC_FEM_Y=str(int(dims[1])), OC_FEM_Z=str(int(dims[2])))
+
+
+def fem_ref_system(steps: int, dims=(10, 3, 3)):
+    """The reference FEM demo (mesh of dims cubes, InitGL FEM:424-426) after `steps`
+    steps: the system its CG receives in the next step, and the CG's own (V, residual)."""
+    with tempfile.TemporaryDirectory() as td:
+        sp, op = os.path.join(td, "sys.bin"), os.path.join(td, "sol.bin")
+        subprocess.run([str(fem_binary()), "--system", str(int(steps)), sp, op], env=_fem_env(dims), check=True,
+                       capture_output=True)
+        sys_ = BsrSystem.from_bytes(open(sp, "rb").read())
+        sol = np.fromfile(op, np.float32)
+    n3 = 3 * sys_.n
+    return sys_, sol[:n3].reshape(-1, 3), sol[n3:].reshape(-1, 3)
+
+
+def fem_ref_solve(sys_: BsrSystem, fp64: bool = False, timed: bool = False):
+    """The reference's ConjugateGradientSolver run on `sys_`: (V, residual[, seconds])."""
+    with tempfile.TemporaryDirectory() as td:
+        sp, op = os.path.join(td, "sys.bin"), os.path.join(td, "sol.bin")
+        open(sp, "wb").write(sys_.to_bytes())
+        r = subprocess.run([str(fem_binary(fp64)), "--solve", sp, op] + (["--time"] if timed else []), check=True,
+                           capture_output=True, text=True)
+        sol = np.fromfile(op, np.float64 if fp64 else np.float32)
+    n3 = 3 * sys_.n
+    out = (sol[:n3].reshape(-1, 3), sol[n3:].reshape(-1, 3))
+    if timed:
+        out = out + (json.loads(r.stdout.strip().splitlines()[-1])["seconds"],)
+    return out
 
 
 def ref_pick(X, point, radius=0.1) -> int:

@@ -1,10 +1,16 @@
 #!/usr/bin/env bash
-# Test infrastructure: builds the reference's own implicit step headless, from the
-# reference sources where they lie, into oracle/_ref/ (git-ignored; never committed).
+# Test infrastructure: builds the reference's own implicit step, and the block-sparse
+# CG of its FEM demo, headless, from the reference sources where they lie, into
+# oracle/_ref/ (git-ignored; never committed).
 #
 #   OpenCloth_Implicit/OpenCloth_Implicit/main.cpp  -> _ref/imp_f32.cpp (generated copy)
 #                                                  -> _ref/imp_f64.cpp (FP64 copy)
 #   ref_harness.cpp + shim/GL/*.h + dep/glm          -> _ref/ref_step_f32, _ref/ref_step_f64
+#   OpenCloth_CoRotated_Linear_FEM/.../main.cpp      -> _ref/fem_f32.cpp, _ref/fem_f64.cpp
+#   fem_harness.cpp + shim/GL/*.h + dep/glm          -> _ref/fem_step_f32, _ref/fem_step_f64
+#
+# The FEM copy differs from the reference only in InitGL's mesh size (main.cpp:426,
+# read from OC_FEM_X/OC_FEM_Y/OC_FEM_Z at start-up).
 #
 # The generated copies differ from the reference only where a compile-time constant
 # has to become a run-time value (grid size main.cpp:60, CG EPS main.cpp:126 and i_max
@@ -39,8 +45,21 @@ sed -E \
     -e 's/\b([0-9]+\.[0-9]*|[0-9]*\.[0-9]+)f\b/\1/g' \
     "$OUT/imp_f32.cpp" > "$OUT/imp_f64.cpp"
 
+FEM_SRC="$REF/OpenCloth_CoRotated_Linear_FEM/OpenCloth_CoRotated_Linear_FEM/main.cpp"
+sed -E \
+    -e 's/^\tGenerateBlocks\(10,3,3,0\.1f,0\.1f,0\.1f\);/\tGenerateBlocks(oc_env_int("OC_FEM_X", 10), oc_env_int("OC_FEM_Y", 3), oc_env_int("OC_FEM_Z", 3), 0.1f, 0.1f, 0.1f);/' \
+    "$FEM_SRC" > "$OUT/fem_f32.cpp"
+grep -qF 'oc_env_int("OC_FEM_X"' "$OUT/fem_f32.cpp" || { echo "build_ref: FEM substitution failed" >&2; exit 1; }
+sed -E \
+    -e 's/glm::(vec|mat)([234])/glm::d\1\2/g' \
+    -e 's/\bfloat\b/double/g' \
+    -e 's/\b([0-9]+\.[0-9]*|[0-9]*\.[0-9]+)f\b/\1/g' \
+    "$OUT/fem_f32.cpp" > "$OUT/fem_f64.cpp"
+
 CXXFLAGS="-std=c++14 -O2 -ffp-contract=off -w -I$HERE/shim -I$REF/dep/glm -I$OUT -Dglm_core_func_integer"
 g++ $CXXFLAGS -DOC_REAL=float '-DOC_REF_SOURCE="imp_f32.cpp"' "$HERE/ref_harness.cpp" -o "$OUT/ref_step_f32" &
 g++ $CXXFLAGS -DOC_REAL=double '-DOC_REF_SOURCE="imp_f64.cpp"' "$HERE/ref_harness.cpp" -o "$OUT/ref_step_f64" &
-wait %1 && wait %2
-echo "build_ref: built $OUT/ref_step_f32 $OUT/ref_step_f64"
+g++ $CXXFLAGS -DOC_REAL=float '-DOC_FEM_SOURCE="fem_f32.cpp"' "$HERE/fem_harness.cpp" -o "$OUT/fem_step_f32" &
+g++ $CXXFLAGS -DOC_REAL=double '-DOC_FEM_SOURCE="fem_f64.cpp"' "$HERE/fem_harness.cpp" -o "$OUT/fem_step_f64" &
+wait %1 && wait %2 && wait %3 && wait %4
+echo "build_ref: built $OUT/ref_step_f32 $OUT/ref_step_f64 $OUT/fem_step_f32 $OUT/fem_step_f64"

@@ -1,5 +1,6 @@
 /* Test infrastructure: instantiates the CPU restatement of the reference implicit step,
- * and of the COUPLED Jacobian mode, in FP32 and FP64 (see oc_oracle.h).  Build with -O2 -ffp-contract=off and without
+ * of the COUPLED Jacobian mode, and of the FEM demo's block-sparse CG, in FP32 and FP64
+ * (see oc_oracle.h).  Build with -O2 -ffp-contract=off and without
  * -ffast-math so every operation rounds as written. */
 #include "oc_oracle.h"
 
@@ -12,6 +13,7 @@
 #define SFX(name) name##_f32
 #include "oc_oracle_impl.h"
 #include "oc_coupled_impl.h"
+#include "oc_bsr_impl.h"
 #undef REAL
 #undef SQRT
 #undef SFX
@@ -21,6 +23,7 @@
 #define SFX(name) name##_f64
 #include "oc_oracle_impl.h"
 #include "oc_coupled_impl.h"
+#include "oc_bsr_impl.h"
 #undef REAL
 #undef SQRT
 #undef SFX

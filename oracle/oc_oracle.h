@@ -96,6 +96,16 @@ void ocr_coupled_system_f64(const ocr_params* p, double h, const double* X, cons
 int ocr_coupled_step_f64(const ocr_params* p, double dt, int32_t n_steps, double* X, double* V, double* dV,
                          int32_t* iters, double* rel_residual, uint32_t* flags);
 
+/* The FEM demo's block-sparse CG, FEM:837-922 (oc_bsr_impl.h): block rows in CSR with
+ * ascending columns, blocks of 9 floats (m[c][r] at 3c + r), fixed rows skipped; x (the
+ * unknown V) is the warm start in and the solution out; residual_out (3n, may be NULL)
+ * receives the final residual.  Exactly i_max iterations. */
+int ocr_bsr_cg_f32(int32_t n, const int32_t* row_ptr, const int32_t* col, const float* blocks, const float* b,
+                   float* x, const uint8_t* fixed, int32_t i_max, float tiny, int32_t dot_fp64, float* residual_out);
+int ocr_bsr_cg_f64(int32_t n, const int32_t* row_ptr, const int32_t* col, const float* blocks, const double* b,
+                   double* x, const uint8_t* fixed, int32_t i_max, float tiny, int32_t dot_fp64,
+                   double* residual_out);
+
 /* FP64 adjoint of n_steps steps from (X0, V0) with a zero warm start (oc_adjoint.c):
  * given dL/dX_T, dL/dV_T (NULL = 0), returns the final state and dL/dX0, dL/dV0,
  * dL/dKs, dL/dKd (per spring) and dL/d(external force) (per vertex, constant in time).

@@ -1,6 +1,7 @@
 /* Test infrastructure (oracle only): headless stand-in for freeglut.  The three
  * constants compared outside a call (main.cpp:383, :409, :414) get values; every
- * glut* call is a no-op expression. */
+ * glut* call is a no-op expression.  Used for OpenCloth_Implicit and
+ * OpenCloth_CoRotated_Linear_FEM. */
 #ifndef OC_SHIM_FREEGLUT_H
 #define OC_SHIM_FREEGLUT_H
 #include "glew.h"
@@ -24,4 +25,5 @@
 #define glutSetWindowTitle(...) (0)
 #define glutSwapBuffers(...) (0)
 #define glutWireSphere(...) (0)
+#define glutKeyboardFunc(...) (0)
 #endif

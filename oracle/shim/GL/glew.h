@@ -1,5 +1,6 @@
 /* Test infrastructure (oracle only): link-time stand-ins that let the reference's
- * OpenCloth_Implicit/OpenCloth_Implicit/main.cpp compile headless.  Every GL, GLU,
+ * OpenCloth_Implicit/OpenCloth_Implicit/main.cpp and
+ * OpenCloth_CoRotated_Linear_FEM/OpenCloth_CoRotated_Linear_FEM/main.cpp compile headless.  Every GL, GLU,
  * GLUT and WGL call expands to a no-op expression; no graphics stack is involved.
  * Only ref_harness.cpp includes this directory. */
 #ifndef OC_SHIM_GLEW_H

@@ -66,3 +66,14 @@ def seeded_cloth(cols: int, rows: int, seed: int, i_max: int = 200, eps: float =
     desc = ClothDesc(n_vertices=cols * rows, springs=sp, pinned=pins, cg_max_iter=i_max, cg_tol=eps)
     ocl = oracle.Cloth(cols * rows, sp, pinned=pins, i_max=i_max, eps=eps)
     return desc, ocl, X, V
+
+
+FEM_CASES = ("m0", "m30", "m120", "big10")
+
+
+def fem_golden(tag: str):
+    """A system the FEM demo's CG received (tests/golden/fem_cg_ref.npz), with the
+    reference CG's FP32 and FP64 results: (system, V32, r32, V64, r64)."""
+    d = np.load(GOLDEN / "fem_cg_ref.npz")
+    sys_ = oracle.BsrSystem.from_bytes(d[f"{tag}_system"].tobytes())
+    return sys_, d[f"{tag}_V32"], d[f"{tag}_r32"], d[f"{tag}_V64"], d[f"{tag}_r64"]

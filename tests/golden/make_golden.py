@@ -1,9 +1,9 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
-Runs the reference's own implicit step compiled headless (oracle/build_ref.sh ->
-oracle/_ref/ref_step_f32 and ref_step_f64) on seeded inputs and stores inputs and
-outputs as .npz, so hosts without the reference tree (the GPU host) can check against
-them.  Needs the reference tree; run from the repository root:
+Runs the reference's own implicit step and the FEM demo's CG compiled headless
+(oracle/build_ref.sh -> oracle/_ref/ref_step_f32/_f64 and fem_step_f32/_f64) on seeded
+inputs and stores inputs and outputs as .npz, so hosts without the reference tree (the
+GPU host) can check against them.  Needs the reference tree; run from the repository root:
 
     python tests/golden/make_golden.py
 """
@@ -79,6 +79,22 @@ def main():
     X, sp = grid_cloth(cols, rows, ks=(0.75, 0.75, 0.95), kd=(-0.25, -0.25, -0.25))
     save_case("stepphysics21_ref", cols, rows, X, np.zeros_like(X), np.zeros_like(X), sp, 5.0 / 60.0, 10, 1e-3, g,
               (1, 10, 100), (1,), passes=3)
+
+    # The FEM demo's block-sparse CG (FEM:837-922) on the systems the demo itself builds:
+    # its default mesh after 0, 30 and 120 steps and a larger mesh after 10 steps, with
+    # the reference CG's FP32 result and the FP64 build's result on the same system.
+    fem = {}
+    for tag, steps, dims in (("m0", 0, (10, 3, 3)), ("m30", 30, (10, 3, 3)), ("m120", 120, (10, 3, 3)),
+                             ("big10", 10, (14, 4, 4))):
+        sys_, V32, r32 = oracle.fem_ref_system(steps, dims)
+        V64, r64 = oracle.fem_ref_solve(sys_, fp64=True)
+        fem[f"{tag}_dims"] = np.array(dims, np.int32)
+        fem[f"{tag}_steps"] = np.int32(steps)
+        fem[f"{tag}_system"] = np.frombuffer(sys_.to_bytes(), np.uint8)
+        fem[f"{tag}_V32"], fem[f"{tag}_r32"] = V32, r32
+        fem[f"{tag}_V64"], fem[f"{tag}_r64"] = V64, r64
+    np.savez_compressed(OUT / "fem_cg_ref.npz", **fem)
+    print("wrote fem_cg_ref")
 
     # InitGL's own topology for a few grid sizes.
     topo = {}

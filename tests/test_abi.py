@@ -147,7 +147,7 @@ def _c_layout(struct: str, fields) -> list:
 
 
 @pytest.mark.parametrize("cls,struct", [(N.ClothDescC, "oc_cloth_desc"), (N.OptionsC, "oc_options"),
-                                        (N.Spring, "oc_spring")])
+                                        (N.Spring, "oc_spring"), (N.BsrDescC, "oc_bsr_desc")])
 def test_ctypes_structs_match_the_header(cls, struct):
     fields = [f[0] for f in cls._fields_]
     got = _c_layout(struct, fields)

@@ -1,0 +1,111 @@
+"""GPU parity of the batched block-sparse CG with the FEM demo's semantics (FEM:837-922).
+
+Tolerances (stated here, used below):
+* Against the oracle run with the GPU's arithmetic (FP64 sums of the FP32 per-row dot
+  terms): V within 1e-6 relative (max-norm over free rows).  The GPU's FP64 sums add
+  the same terms in another order (float pairs within a warp, FP64 above), which can
+  move d3 or d4 by an FP32 ulp.
+* Against the reference CG's own FP32 result (golden): within twice the reference's
+  FP32-to-FP64 distance on that system, or 1e-6.
+* A system gives the same bits alone or in a batch, with or without the CUDA graph.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from cases import FEM_CASES, fem_golden
+from opencloth_gb300 import OcError
+from opencloth_gb300.fem import BsrSolver, fem_system
+
+pytestmark = pytest.mark.gpu
+
+
+def desc(sys_):
+    return {"row_ptr": sys_.row_ptr, "col": sys_.col, "fixed": sys_.fixed, "i_max": sys_.i_max,
+            "tolerance": sys_.tolerance, "tiny": sys_.tiny}
+
+
+def solve(systems, use_graph=True):
+    with BsrSolver([desc(s) for s in systems], use_graph=use_graph) as s:
+        s.set_system(np.concatenate([x.blocks for x in systems]), np.concatenate([x.b for x in systems]),
+                     np.concatenate([x.V for x in systems]))
+        s.solve()
+        return s.solution()
+
+
+def rel_free(a, b, sys_):
+    free = sys_.fixed == 0
+    return float(np.abs(a[free].astype(np.float64) - b[free]).max() / np.abs(b[free]).max())
+
+
+@pytest.mark.parametrize("tag", FEM_CASES)
+def test_matches_oracle_and_reference(tag):
+    sys_, V32, _, V64, _ = fem_golden(tag)
+    V, r = solve([sys_])
+    Vo, ro = oracle.bsr_cg(sys_, dot_fp64=True)
+    assert rel_free(V, Vo, sys_) <= 1e-6
+    gap = rel_free(V32, V64, sys_)
+    assert rel_free(V, V64, sys_) <= max(2.0 * gap, 1e-6)
+    fixed = sys_.fixed == 1
+    assert np.array_equal(V[fixed], sys_.V[fixed])  # fixed rows are never touched
+    assert np.all(r[fixed] == 0.0)
+
+
+def test_batch_and_graph_give_the_same_bits():
+    systems = [fem_golden(t)[0] for t in FEM_CASES]
+    Vb, rb = solve(systems)
+    Vn, rn = solve(systems, use_graph=False)
+    assert np.array_equal(Vb, Vn) and np.array_equal(rb, rn)
+    off = np.cumsum([0] + [s.n for s in systems])
+    for k, s in enumerate(systems):
+        V1, r1 = solve([s])
+        assert np.array_equal(Vb[off[k]:off[k + 1]], V1) and np.array_equal(rb[off[k]:off[k + 1]], r1), k
+
+
+def test_iteration_counts_per_system():
+    """i_max 0 (no iteration: V kept, residual = b - A V), 1 and 7, in one batch."""
+    base = fem_golden("m30")[0]
+    systems = []
+    for imax in (0, 1, 7):
+        s = oracle.BsrSystem(base.row_ptr, base.col, base.blocks, base.b, base.V, base.fixed, imax, base.tolerance,
+                             base.tiny)
+        systems.append(s)
+    V, r = solve(systems)
+    n = base.n
+    for k, s in enumerate(systems):
+        Vo, ro = oracle.bsr_cg(s, dot_fp64=True)
+        assert rel_free(V[k * n:(k + 1) * n], Vo, s) <= 1e-6, k
+        if s.i_max == 0:
+            assert np.array_equal(V[:n], s.V)
+            assert np.abs(r[:n] - ro).max() <= 1e-6 * np.abs(ro).max()
+
+
+def test_generated_system_solves_like_the_oracle():
+    g = fem_system(12, 5, 4, V=np.random.default_rng(3).normal(0.0, 0.2, (13 * 6 * 5, 3)))
+    s = oracle.BsrSystem(g["row_ptr"], g["col"], g["blocks"], g["b"], g["V"], g["fixed"], 20)
+    V, _ = solve([s])
+    Vo, _ = oracle.bsr_cg(s, dot_fp64=True)
+    assert rel_free(V, Vo, s) <= 1e-6
+
+
+def test_validation():
+    sys_ = fem_golden("m0")[0]
+    with BsrSolver([desc(sys_)]) as s:
+        blocks = sys_.blocks.copy()
+        free_row = int(np.nonzero(sys_.fixed == 0)[0][0])
+        blocks[sys_.row_ptr[free_row]] = np.nan
+        with pytest.raises(OcError) as e:
+            s.set_system(blocks, sys_.b, sys_.V)
+        assert e.value.status == 3
+        s.set_system(sys_.blocks, sys_.b, sys_.V)  # infinities in fixed rows are the reference's own
+    bad = desc(sys_)
+    bad["col"] = sys_.col.copy()
+    bad["col"][[0, 1]] = bad["col"][[1, 0]]  # not ascending within the row
+    with pytest.raises(OcError) as e:
+        BsrSolver([bad])
+    assert e.value.status == 1
+    bad["col"] = sys_.col.copy()
+    bad["col"][3] = sys_.n
+    with pytest.raises(OcError) as e:
+        BsrSolver([bad])
+    assert e.value.status == 2
