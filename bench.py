@@ -476,6 +476,106 @@ def measure_adjoint(name: str, seed: int, local: int) -> dict:
             "grad_norm_ks": float(np.linalg.norm(g["dKs"])), "finite": bool(np.isfinite(g["dKs"]).all())}
 
 
+def fem_workload(name: str, seed: int):
+    """The FEM demo's CG on systems the demo's assembly builds at rest (opencloth_gb300.fem,
+    restating FEM:240-405, 659-831) with random velocities N(0, 0.1^2), i_max 20:
+      fem160x48x48   one mesh of 160 x 48 x 48 cubes (386,561 block rows, 4.9M blocks)
+      fem_batch4096  4096 bodies of the demo's own 10 x 3 x 3 mesh (176 rows each)."""
+    from opencloth_gb300.fem import fem_system
+
+    rng = np.random.default_rng(seed)
+    if name == "fem160x48x48":
+        n = 161 * 49 * 49
+        g = fem_system(160, 48, 48, V=rng.normal(0.0, 0.1, (n, 3)))
+        return [g]
+    base = fem_system(10, 3, 3)
+    out = []
+    mass_b = None
+    for _ in range(4096):
+        V = rng.normal(0.0, 0.1, base["V"].shape)
+        V[base["fixed"] == 1] = 0.0
+        if mass_b is None:  # b = b0 + V m: recover m from one assembly with unit velocity
+            ones = fem_system(10, 3, 3, V=np.ones_like(base["V"]))
+            mass_b = (ones["b"].astype(np.float64) - base["b"])[:, :1]
+        d = dict(base)
+        with np.errstate(invalid="ignore"):
+            d["b"] = (base["b"] + V * mass_b).astype(np.float32)
+        d["V"] = V.astype(np.float32)
+        out.append(d)
+    return out
+
+
+def measure_fem(name: str, seed: int, local: int, solves: int) -> dict:
+    """The batched block-sparse CG: solves/s and block-row iterations/s on the device,
+    end to end through the C ABI with host buffers, the SpMV roofline and the oracle's
+    restatement (bit-exact to the reference's CG) on the host cores."""
+    import torch
+
+    import oracle
+    from opencloth_gb300.fem import BsrSolver
+
+    systems = fem_workload(name, seed)
+    rows = sum(len(g["row_ptr"]) - 1 for g in systems)
+    iters = systems[0]["i_max"]
+    blocks = np.concatenate([g["blocks"] for g in systems])
+    b = np.concatenate([g["b"] for g in systems])
+    V0 = np.concatenate([g["V"] for g in systems])
+    stream = torch.cuda.Stream()
+    s = BsrSolver(systems, device=local, stream=stream.cuda_stream)
+    s.set_system(blocks, b, V0)
+    for _ in range(3):
+        s.solve()
+    s.synchronize()
+    l0 = s.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(solves):
+            s.solve()
+        ev1.record(stream)
+        ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / solves
+    launches = s.launch_count() - l0
+    prof = s.profile(2)
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    peak = float(json.loads(peaks_path.read_text())["hbm_gbs"]) if peaks_path.exists() else 6800.0
+    spmv = prof["k_bsr_spmv"]
+    achieved = spmv["bytes"] / (spmv["ms_total"] / 1e3) / 1e9
+    # End to end: host blocks, b and V in, solve, V out, every solve.
+    e2e_n = max(3, min(solves, 10))
+    Vh = np.empty_like(V0)
+    t0 = time.perf_counter()
+    for _ in range(e2e_n):
+        s.set_system(blocks, b, V0)
+        s.solve()
+        Vh[:], _ = s.solution()
+    e2e_s = (time.perf_counter() - t0) / e2e_n
+    s.close()
+    # CPU: the restatement of ConjugateGradientSolver on a bounded sample, one core.
+    sample = systems if name == "fem160x48x48" else systems[:256]
+    t0 = time.perf_counter()
+    for g in sample:
+        oracle.bsr_cg(oracle.BsrSystem(g["row_ptr"], g["col"], g["blocks"], g["b"], g["V"], g["fixed"], g["i_max"]))
+    cpu_s = time.perf_counter() - t0
+    cpu_rows = sum(len(g["row_ptr"]) - 1 for g in sample)
+    nnzb = len(blocks)
+    return {
+        "workload": name, "systems": len(systems), "block_rows": rows, "blocks": nnzb, "iterations": iters,
+        "metric": "block-row-iterations/s", "value": rows * iters / (ms / 1e3), "ms_per_solve": ms,
+        "solves_per_s": 1e3 / ms, "solves": solves, "gpu_launches": int(launches), "clocks": clocks.summary(),
+        "e2e": {"value": rows * iters / e2e_s, "unit": "block-row-iterations/s",
+                "h2d_bytes_per_solve": int(blocks.nbytes + b.nbytes + V0.nbytes), "d2h_bytes_per_solve": int(V0.nbytes)},
+        "roofline": {"bound": "hbm", "kernel": "k_bsr_spmv", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "algorithmic_bytes_per_launch": spmv["bytes"] / max(spmv["launches"], 1),
+                     "avg_launch_us": 1e3 * spmv["ms_total"] / max(spmv["launches"], 1),
+                     "peak_source": "measured" if peaks_path.exists() else "fallback"},
+        "kernels": {k: {"avg_us": 1e3 * v["ms_total"] / max(v["launches"], 1), "launches": v["launches"]}
+                    for k, v in prof.items()},
+        "cpu_baseline": {"value": cpu_rows * iters / cpu_s, "unit": "block-row-iterations/s", "cores": 1,
+                         "kind": "port", "sample": f"{len(sample)} of {len(systems)} systems, one solve each"},
+    }
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -514,6 +614,7 @@ def run_ours(args) -> None:
         }
         if args.workload == "all":
             line["adjoint"] = {n: measure_adjoint(n, args.seed, local) for n in ("grid257", "batch512")}
+            line["fem_cg"] = {n: measure_fem(n, args.seed, local, 20) for n in ("fem160x48x48", "fem_batch4096")}
         for b in results[1:]:
             line[b["name"]] = {
                 "value": b["value"], "unit": METRIC, "ms_per_step": b["ms_per_step"], "steps": b["steps"],

@@ -284,6 +284,11 @@ oc_status oc_bsr_solve(oc_bsr_solver* s);
 /* The solution V and the final residual (3 x rows each; either may be NULL). */
 oc_status oc_bsr_get_solution(oc_bsr_solver* s, float* x, float* residual);
 oc_status oc_bsr_get_launch_count(oc_bsr_solver* s, int64_t* kernels_launched);
+/* n_solves solves without the graph, each launch timed with CUDA events: per kernel
+ * (names, 32 chars each) the total ms, launches and algorithmic bytes, as
+ * oc_profile_steps does for the cloth step. */
+oc_status oc_bsr_profile(oc_bsr_solver* s, int32_t n_solves, int32_t max_kernels, char* names, double* ms_total,
+                         int64_t* launches, double* algorithmic_bytes, int32_t* n_kernels);
 oc_status oc_bsr_synchronize(oc_bsr_solver* s);
 
 /* ---- reference topology builder (IMP:497-565) ------------------------------------ */

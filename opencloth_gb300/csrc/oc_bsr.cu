@@ -4,12 +4,12 @@
 // CUDA-graph WHILE loop, batches of independent systems).
 //
 // The reference keeps each block row as a std::map<int, mat3> and walks it in ascending
-// column order.  Here the rows of a system are cut into slices of 32 consecutive rows
-// (one warp) stored slot-major (sliced ELL): slot j of lane l of slice s holds the j-th
-// block of that row, each of the 9 components in its own plane, so every load of a
-// warp is one coalesced 128-byte line; the columns are a static table built at create
-// time, and each solve first packs the caller's CSR blocks into the planes.  Each lane
-// sums its own row's products in slot order (the reference's order).
+// column order.  Here the rows of a system are reordered by block count (within windows)
+// and cut into slices of 32 rows (one warp) stored slot-major (sliced ELL with sorting):
+// slot j of lane l of slice s holds the j-th block of that row as two float4 and a
+// {component 8, column} pair, so every load of a warp is coalesced; the columns are a
+// static table built at create time, and each solve first packs the caller's CSR blocks.
+// Each lane sums its own row's products in slot order (the reference's order).
 //
 //   k_bsr_pack    CSR blocks -> sliced planes
 //   k_bsr_init    r = b - A V, p = r               (FEM:841-859)
@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -37,7 +38,8 @@ namespace oc {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kRowsPerBlock = 2048;  // 8 rows per thread
+constexpr int kRowsPerBlock = 256;  // one row per thread: enough warps to cover the gathers
+constexpr int kSortWindow = 2048;   // rows reordered by block count within windows of this size
 
 struct BsrState {
     double d, d2, d1;
@@ -61,16 +63,20 @@ struct BsrArgs {
     const BsrParams* sys;
     BsrState* state;
     const int64_t* slice_ptr;  // slot offset of each slice (units of 32 entries)
+    const int32_t* sb2_col;    // the static column of each slot (-1 for padding), merged into sb2 by pack
     const int32_t* width;      // slots of each slice
-    const int32_t* scol;       // sliced column (global row), -1 for padding
-    float* sblk[9];            // sliced block components
-    const int32_t* row_ptr;    // caller's CSR (global, over all systems)
+    float4* sb0;               // sliced blocks: components 0-3 and 4-7 of each slot, and
+    float4* sb1;               // {component 8, column (global row; -1 for padding)}
+    float2* sb2;
+    const int32_t* row_ptr;    // caller's CSR (global, over all systems, the caller's row order)
+    const int32_t* iperm;      // internal row -> caller's row
+    const int32_t* deg;        // blocks of each internal row
     const float* cblk;         // caller's CSR blocks (9 per block)
     const uint8_t* fixed;
     const float* b;            // 3 per row
     float* x[3];               // V (unknown) planes
-    float* r[3];
-    float* p[3];
+    float4* r4;                // residual and direction, gathered by the neighbours: one
+    float4* p4;                // 16-byte load each (w unused)
     float* q[3];
     double* partials;          // 2 per block
     int32_t* unfinished;
@@ -95,24 +101,70 @@ __device__ __forceinline__ int64_t slot_pos(const BsrArgs& a, const BsrParams& s
     return (a.slice_ptr[s] + j) * 32 + (local & 31);
 }
 
+// One slot: the block and its column.
+__device__ __forceinline__ int32_t load_block(const BsrArgs& a, int64_t pos, float m[9]) {
+    const float4 u = __ldg(a.sb0 + pos), v = __ldg(a.sb1 + pos);
+    const float2 w = __ldg(a.sb2 + pos);
+    m[0] = u.x; m[1] = u.y; m[2] = u.z; m[3] = u.w;
+    m[4] = v.x; m[5] = v.y; m[6] = v.z; m[7] = v.w;
+    m[8] = w.x;
+    return __float_as_int(w.y);
+}
+
 __global__ void __launch_bounds__(kThreads) k_bsr_pack(const BsrArgs a) {
     const BlockInfo bi = a.blocks[blockIdx.x];
     const BsrParams& sp = a.sys[bi.inst];
     for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
-        const int32_t e0 = a.row_ptr[g], e1 = a.row_ptr[g + 1];
+        const int64_t u = a.iperm[g];
+        const int32_t e0 = a.row_ptr[u], e1 = a.row_ptr[u + 1];
         for (int32_t e = e0; e < e1; ++e) {
             const int64_t pos = slot_pos(a, sp, g, e - e0);
-#pragma unroll
-            for (int c = 0; c < 9; ++c) a.sblk[c][pos] = a.cblk[9 * (size_t)e + c];
+            const float* m = a.cblk + 9 * (size_t)e;
+            a.sb0[pos] = make_float4(m[0], m[1], m[2], m[3]);
+            a.sb1[pos] = make_float4(m[4], m[5], m[6], m[7]);
+            a.sb2[pos] = make_float2(m[8], __int_as_float(__ldg(a.sb2_col + pos)));
         }
     }
 }
 
 // Two-value last-block epilogue (per system), and the grid-wide WHILE condition.
+// The per-system scalars from the system's totals (thread 0 of the system's last block).
+template <int KIND>
+__device__ void bsr_scalars(const BsrArgs& a, int inst, double tot0, double tot1) {
+    const BsrParams& sp = a.sys[inst];
+    BsrState& st = a.state[inst];
+    st.ticket = 0;
+    const double tiny = (double)sp.tiny;
+    if (KIND == 0) {  // after the matrix-vector pass: d, d2, d3
+        st.d = tot0;
+        double d2 = tot1;
+        st.d2 = d2;
+        if (fabs(d2) < tiny) d2 = tiny;  // FEM:885-886
+        st.d3 = (float)(tot0 / d2);
+    } else {  // after the update: d1, d4, next iteration
+        st.d1 = tot0;
+        double d = st.d;
+        if (fabs(d) < tiny) d = tiny;  // FEM:908-909
+        st.d4 = (float)(tot0 / d);
+        st.iter += 1;
+        if (st.iter >= sp.imax) {
+            st.active = 0;
+            atomicSub(a.unfinished, 1);
+        }
+    }
+    __threadfence();
+}
+
 template <int KIND>
 __device__ void bsr_finish(const BsrArgs& a, int blk, int inst, bool participates, Acc p0, Acc p1) {
     __shared__ int s_last;
-    if (participates) {
+    if (participates && a.sys[inst].nblk == 1) {
+        // A one-block system: its block sums are the totals (the multi-block path would
+        // add this one partial to zeros, which is exact).
+        const double s0 = block_sum_acc(p0);
+        const double s1 = KIND == 0 ? block_sum_acc(p1) : 0.0;
+        if (threadIdx.x == 0) bsr_scalars<KIND>(a, inst, s0, s1);
+    } else if (participates) {
         const double s0 = block_sum_acc(p0);
         const double s1 = KIND == 0 ? block_sum_acc(p1) : 0.0;
         if (threadIdx.x == 0) {
@@ -132,30 +184,8 @@ __device__ void bsr_finish(const BsrArgs& a, int blk, int inst, bool participate
                 t1 += __ldcg(a.partials + 2 * (sp.blk0 + j) + 1);
             }
             const double tot0 = block_sum(t0);
-            const double tot1 = block_sum(t1);
-            if (threadIdx.x == 0) {
-                BsrState& st = a.state[inst];
-                st.ticket = 0;
-                const double tiny = (double)sp.tiny;
-                if (KIND == 0) {  // after the matrix-vector pass: d, d2, d3
-                    st.d = tot0;
-                    double d2 = tot1;
-                    st.d2 = d2;
-                    if (fabs(d2) < tiny) d2 = tiny;  // FEM:885-886
-                    st.d3 = (float)(tot0 / d2);
-                } else {  // after the update: d1, d4, next iteration
-                    st.d1 = tot0;
-                    double d = st.d;
-                    if (fabs(d) < tiny) d = tiny;  // FEM:908-909
-                    st.d4 = (float)(tot0 / d);
-                    st.iter += 1;
-                    if (st.iter >= sp.imax) {
-                        st.active = 0;
-                        atomicSub(a.unfinished, 1);
-                    }
-                }
-                __threadfence();
-            }
+            const double tot1 = KIND == 0 ? block_sum(t1) : 0.0;
+            if (threadIdx.x == 0) bsr_scalars<KIND>(a, inst, tot0, tot1);
         }
     }
     if (KIND == 1 && threadIdx.x == 0) {
@@ -182,13 +212,12 @@ __global__ void __launch_bounds__(kThreads) k_bsr_init(const BsrArgs a) {
             r0 = a.b[3 * g];
             r1 = a.b[3 * g + 1];
             r2 = a.b[3 * g + 2];
-            const int n = a.row_ptr[g + 1] - a.row_ptr[g];
+            const int n = a.deg[g];
+            const int64_t base = slot_pos(a, sp, g, 0);
             for (int j = 0; j < n; ++j) {
-                const int64_t pos = slot_pos(a, sp, g, j);
-                const int32_t c = a.scol[pos];
+                const int64_t pos = base + 32 * (int64_t)j;
                 float m[9];
-#pragma unroll
-                for (int k = 0; k < 9; ++k) m[k] = a.sblk[k][pos];
+                const int32_t c = load_block(a, pos, m);
                 float o0, o1, o2;
                 block_mv(m, a.x[0][c], a.x[1][c], a.x[2][c], o0, o1, o2);
                 r0 = r0 - o0;
@@ -196,12 +225,8 @@ __global__ void __launch_bounds__(kThreads) k_bsr_init(const BsrArgs a) {
                 r2 = r2 - o2;
             }
         }
-        a.r[0][g] = r0;
-        a.r[1][g] = r1;
-        a.r[2][g] = r2;
-        a.p[0][g] = r0;
-        a.p[1][g] = r1;
-        a.p[2][g] = r2;
+        a.r4[g] = make_float4(r0, r1, r2, 0.0f);
+        a.p4[g] = make_float4(r0, r1, r2, 0.0f);
     }
     if (threadIdx.x == 0 && bi.gblk == a.sys[bi.inst].blk0) {
         BsrState& st = a.state[bi.inst];
@@ -215,7 +240,8 @@ __global__ void __launch_bounds__(kThreads) k_bsr_init(const BsrArgs a) {
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_bsr_spmv(const BsrArgs a) {
+template <int UNROLL, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_bsr_spmv(const BsrArgs a) {
     const BlockInfo bi = a.blocks[blockIdx.x];
     const BsrParams& sp = a.sys[bi.inst];
     const BsrState& st = a.state[bi.inst];
@@ -226,26 +252,30 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv(const BsrArgs a) {
         const float d4 = st.d4;
         for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
             if (a.fixed[g]) continue;
-            const float r0 = a.r[0][g], r1 = a.r[1][g], r2 = a.r[2][g];
-            float n0 = a.p[0][g], n1 = a.p[1][g], n2 = a.p[2][g];
+            const float4 rg = a.r4[g];
+            const float r0 = rg.x, r1 = rg.y, r2 = rg.z;
+            const float4 pg = a.p4[g];
+            float n0 = pg.x, n1 = pg.y, n2 = pg.z;
             if (!first) {
                 n0 = r0 + n0 * d4;
                 n1 = r1 + n1 * d4;
                 n2 = r2 + n2 * d4;
             }
             float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f;
-            const int n = a.row_ptr[g + 1] - a.row_ptr[g];
+            const int n = a.deg[g];
+            const int64_t base = slot_pos(a, sp, g, 0);
+#pragma unroll UNROLL
             for (int j = 0; j < n; ++j) {
-                const int64_t pos = slot_pos(a, sp, g, j);
-                const int32_t c = a.scol[pos];
+                const int64_t pos = base + 32 * (int64_t)j;
                 float m[9];
-#pragma unroll
-                for (int k = 0; k < 9; ++k) m[k] = a.sblk[k][pos];
-                float v0 = a.p[0][c], v1 = a.p[1][c], v2 = a.p[2][c];
+                const int32_t c = load_block(a, pos, m);
+                const float4 pc = a.p4[c];
+                float v0 = pc.x, v1 = pc.y, v2 = pc.z;
                 if (!first) {
-                    v0 = a.r[0][c] + v0 * d4;
-                    v1 = a.r[1][c] + v1 * d4;
-                    v2 = a.r[2][c] + v2 * d4;
+                    const float4 rc = a.r4[c];
+                    v0 = rc.x + v0 * d4;
+                    v1 = rc.y + v1 * d4;
+                    v2 = rc.z + v2 * d4;
                 }
                 float o0, o1, o2;
                 block_mv(m, v0, v1, v2, o0, o1, o2);
@@ -273,21 +303,41 @@ __global__ void __launch_bounds__(kThreads) k_bsr_update(const BsrArgs a) {
         const float d3 = st.d3, d4 = st.d4;
         for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
             if (a.fixed[g]) continue;
-            float r[3];
+            const float4 rg = a.r4[g], pg = a.p4[g];
+            const float ro[3] = {rg.x, rg.y, rg.z}, po[3] = {pg.x, pg.y, pg.z};
+            float r[3], pn[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const float rk = a.r[k][g];
-                float pk = a.p[k][g];
-                if (!first) pk = rk + pk * d4;
+                float pk = po[k];
+                if (!first) pk = ro[k] + pk * d4;
+                pn[k] = pk;
                 a.x[k][g] = a.x[k][g] + pk * d3;  // V += p d3, FEM:895
-                r[k] = rk - a.q[k][g] * d3;       // r -= q d3, FEM:896
-                a.r[k][g] = r[k];
-                a.p[k][g] = pk;
+                r[k] = ro[k] - a.q[k][g] * d3;    // r -= q d3, FEM:896
             }
+            a.r4[g] = make_float4(r[0], r[1], r[2], 0.0f);
+            a.p4[g] = make_float4(pn[0], pn[1], pn[2], 0.0f);
             acc_add(pd1, r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
         }
     }
     bsr_finish<1>(a, bi.gblk, bi.inst, active, pd1, acc_zero());
+}
+
+// Launch shapes of the matrix-vector pass (unroll of the slot loop, minimum resident
+// blocks per SM, which caps the registers).  OC_BSR_VARIANT picks one; the default was
+// chosen by measurement on GB300.
+typedef void (*SpmvFn)(BsrArgs);
+SpmvFn spmv_variant() {
+    int v = 0;
+    if (const char* e = std::getenv("OC_BSR_VARIANT")) v = std::atoi(e);
+    switch (v) {
+        case 1: return k_bsr_spmv<4, 5>;
+        case 2: return k_bsr_spmv<2, 6>;
+        case 3: return k_bsr_spmv<4, 6>;
+        case 5: return k_bsr_spmv<2, 4>;
+        case 6: return k_bsr_spmv<4, 4>;
+        case 7: return k_bsr_spmv<2, 1>;
+        default: return k_bsr_spmv<1, 8>;  // fastest on both the 386k-row mesh and the 4096-body batch
+    }
 }
 
 }  // namespace
@@ -307,6 +357,7 @@ struct oc_bsr_solver {
     std::vector<uint8_t> fixed_host;
     bool any_iter = false;  // some system has cg_max_iter > 0
     std::vector<int32_t> row_ptr_host;  // global CSR row pointer
+    std::vector<int32_t> perm;          // caller's row -> internal row
     BsrArgs args{};
     std::vector<void*> allocs;
     uint8_t* d_fixed = nullptr;
@@ -317,6 +368,7 @@ struct oc_bsr_solver {
     cudaGraphExec_t exec = nullptr;
     int64_t launches = 0;
     unsigned long long* h_loop = nullptr;
+    SpmvFn spmv = nullptr;
     std::string err;
 };
 
@@ -410,7 +462,7 @@ oc_status bsr_build_graph(oc_bsr_solver* s) {
     cp.conditional.size = 1;
     BSR_TRY(cudaGraphAddNode(&n_loop, g, &n_init, nullptr, 1, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    p = kp(k_bsr_spmv);
+    p = kp(s->spmv);
     BSR_TRY(cudaGraphAddKernelNode(&n_spmv, body, nullptr, 0, &p));
     p = kp(k_bsr_update);
     BSR_TRY(cudaGraphAddKernelNode(&n_upd, body, &n_spmv, 1, &p));
@@ -466,6 +518,7 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
     } while (0)
     s->device = o.device;
     s->use_graph = o.use_graph != 0;
+    s->spmv = spmv_variant();
     s->n_sys = n_systems;
     s->n_rows = rows;
     s->nnzb = nnzb;
@@ -477,13 +530,17 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
         s->own_stream = true;
     }
 
-    // Global CSR, fixed flags, systems, blocks of rows, slices.
-    std::vector<int32_t> row_ptr(1, 0);
-    std::vector<uint8_t> fixed;
+    // Global CSR (the caller's order), systems, blocks of rows and slices (internal order).
+    // Within each system the rows are reordered, window by window (kSortWindow rows), by
+    // decreasing number of blocks, so that the 32 rows of a slice have nearly the same
+    // count and the sliced layout carries little padding (sliced ELL with sorting,
+    // "SELL-C-sigma").  Each row still sums its own blocks in column order.
+    std::vector<int32_t> row_ptr(1, 0), perm(rows), iperm(rows), deg_int(rows);
+    std::vector<uint8_t> fixed(rows), fixed_int(rows);
     std::vector<BsrParams> sys(n_systems);
     std::vector<BlockInfo> blocks;
     std::vector<int64_t> slice_ptr;
-    std::vector<int32_t> width, scol_dummy;
+    std::vector<int32_t> width;
     s->row_off.assign(n_systems + 1, 0);
     s->nnz_off.assign(n_systems + 1, 0);
     int64_t slots = 0;
@@ -508,13 +565,28 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
             bi.v_end = std::min<int64_t>(r0 + d.n_rows, bi.v_begin + kRowsPerBlock);
             blocks.push_back(bi);
         }
+        std::vector<int32_t> order(d.n_rows);
         for (int32_t r = 0; r < d.n_rows; ++r) {
             row_ptr.push_back((int32_t)(e0 + d.row_ptr[r + 1]));
-            fixed.push_back(d.fixed ? (d.fixed[r] ? 1 : 0) : 0);
+            fixed[r0 + r] = d.fixed ? (d.fixed[r] ? 1 : 0) : 0;
+            order[r] = r;
         }
-        for (int32_t r = 0; r < d.n_rows; r += 32) {
+        auto degree = [&](int32_t r) { return d.row_ptr[r + 1] - d.row_ptr[r]; };
+        for (int32_t w0 = 0; w0 < d.n_rows; w0 += kSortWindow) {
+            const int32_t w1 = std::min(d.n_rows, w0 + kSortWindow);
+            std::stable_sort(order.begin() + w0, order.begin() + w1,
+                             [&](int32_t x, int32_t y) { return degree(x) > degree(y); });
+        }
+        for (int32_t i = 0; i < d.n_rows; ++i) {
+            const int32_t u = order[i];
+            perm[r0 + u] = (int32_t)(r0 + i);
+            iperm[r0 + i] = (int32_t)(r0 + u);
+            deg_int[r0 + i] = degree(u);
+            fixed_int[r0 + i] = fixed[r0 + u];
+        }
+        for (int32_t i = 0; i < d.n_rows; i += 32) {
             int32_t w = 0;
-            for (int32_t l = r; l < std::min(d.n_rows, r + 32); ++l) w = std::max(w, d.row_ptr[l + 1] - d.row_ptr[l]);
+            for (int32_t l = i; l < std::min(d.n_rows, i + 32); ++l) w = std::max(w, deg_int[r0 + l]);
             slice_ptr.push_back(slots);
             width.push_back(w);
             slots += w;
@@ -524,14 +596,17 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
     std::vector<int32_t> scol((size_t)slots * 32, -1);
     for (int32_t k = 0; k < n_systems; ++k) {
         const oc_bsr_desc& d = descs[k];
+        const int64_t r0 = s->row_off[k];
         for (int32_t r = 0; r < d.n_rows; ++r) {
-            const int64_t sl = sys[k].slice0 + r / 32;
+            const int64_t i = perm[r0 + r] - r0;
+            const int64_t sl = sys[k].slice0 + i / 32;
             for (int32_t e = d.row_ptr[r]; e < d.row_ptr[r + 1]; ++e)
-                scol[(size_t)((slice_ptr[sl] + (e - d.row_ptr[r])) * 32 + (r & 31))] = (int32_t)(s->row_off[k] + d.col[e]);
+                scol[(size_t)((slice_ptr[sl] + (e - d.row_ptr[r])) * 32 + (i & 31))] = perm[r0 + d.col[e]];
         }
     }
     s->fixed_host = fixed;
     s->row_ptr_host = row_ptr;
+    s->perm = perm;
     s->n_blocks = (int32_t)blocks.size();
 
     BsrArgs& a = s->args;
@@ -551,16 +626,24 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
     a.width = d_width;
     int32_t* d_scol = nullptr;
     BSR_CREATE_TRY(bsr_upload(s, &d_scol, scol));
-    a.scol = d_scol;
-    float* sblk = nullptr;
+    a.sb2_col = d_scol;
     const size_t plane = std::max<size_t>((size_t)slots * 32, 1);
-    BSR_CREATE_TRY(bsr_alloc(s, &sblk, 9 * plane));
-    BSR_CREATE_TRY(cudaMemset(sblk, 0, 9 * plane * sizeof(float)));
-    for (int c = 0; c < 9; ++c) a.sblk[c] = sblk + c * plane;
+    BSR_CREATE_TRY(bsr_alloc(s, &a.sb0, plane));
+    BSR_CREATE_TRY(bsr_alloc(s, &a.sb1, plane));
+    BSR_CREATE_TRY(bsr_alloc(s, &a.sb2, plane));
+    BSR_CREATE_TRY(cudaMemset(a.sb0, 0, plane * sizeof(float4)));
+    BSR_CREATE_TRY(cudaMemset(a.sb1, 0, plane * sizeof(float4)));
+    BSR_CREATE_TRY(cudaMemset(a.sb2, 0, plane * sizeof(float2)));
     BSR_CREATE_TRY(bsr_upload(s, &s->d_row_ptr, row_ptr));
     a.row_ptr = s->d_row_ptr;
-    BSR_CREATE_TRY(bsr_upload(s, &s->d_fixed, fixed));
+    BSR_CREATE_TRY(bsr_upload(s, &s->d_fixed, fixed_int));
     a.fixed = s->d_fixed;
+    int32_t* d_iperm = nullptr;
+    BSR_CREATE_TRY(bsr_upload(s, &d_iperm, iperm));
+    a.iperm = d_iperm;
+    int32_t* d_deg = nullptr;
+    BSR_CREATE_TRY(bsr_upload(s, &d_deg, deg_int));
+    a.deg = d_deg;
     BSR_CREATE_TRY(bsr_alloc(s, &s->d_cblk, 9 * std::max<size_t>((size_t)nnzb, 1)));
     BSR_CREATE_TRY(cudaMemset(s->d_cblk, 0, 9 * std::max<size_t>((size_t)nnzb, 1) * sizeof(float)));
     a.cblk = s->d_cblk;
@@ -569,14 +652,16 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
     a.b = s->d_b;
     const size_t stride = (size_t)((rows + 63) / 64) * 64;
     float* vec = nullptr;
-    BSR_CREATE_TRY(bsr_alloc(s, &vec, 12 * stride));
-    BSR_CREATE_TRY(cudaMemset(vec, 0, 12 * stride * sizeof(float)));
+    BSR_CREATE_TRY(bsr_alloc(s, &vec, 6 * stride));
+    BSR_CREATE_TRY(cudaMemset(vec, 0, 6 * stride * sizeof(float)));
     for (int k = 0; k < 3; ++k) {
         a.x[k] = vec + k * stride;
-        a.r[k] = vec + (3 + k) * stride;
-        a.p[k] = vec + (6 + k) * stride;
-        a.q[k] = vec + (9 + k) * stride;
+        a.q[k] = vec + (3 + k) * stride;
     }
+    BSR_CREATE_TRY(bsr_alloc(s, &a.r4, (size_t)rows));
+    BSR_CREATE_TRY(bsr_alloc(s, &a.p4, (size_t)rows));
+    BSR_CREATE_TRY(cudaMemset(a.r4, 0, (size_t)rows * sizeof(float4)));
+    BSR_CREATE_TRY(cudaMemset(a.p4, 0, (size_t)rows * sizeof(float4)));
     BSR_CREATE_TRY(bsr_alloc(s, &a.partials, 2 * (size_t)s->n_blocks));
     BSR_CREATE_TRY(bsr_alloc(s, &a.unfinished, 1));
     BSR_CREATE_TRY(bsr_alloc(s, &a.grid_ticket, 1));
@@ -630,18 +715,24 @@ oc_status oc_bsr_set_system(oc_bsr_solver* s, const float* blocks, const float* 
     BSR_TRY(cudaSetDevice(s->device));
     if (blocks)
         BSR_TRY(cudaMemcpyAsync(s->d_cblk, blocks, sizeof(float) * 9 * s->nnzb, cudaMemcpyHostToDevice, s->stream));
-    if (b) BSR_TRY(cudaMemcpyAsync(s->d_b, b, sizeof(float) * 3 * s->n_rows, cudaMemcpyHostToDevice, s->stream));
-    if (x) {
-        // interleaved triples -> planes, through the r planes as staging
-        std::vector<float> planes(3 * (size_t)s->n_rows);
+    // b and x in the internal row order (x as planes).
+    std::vector<float> bint, planes;
+    if (b) {
+        bint.resize(3 * (size_t)s->n_rows);
         for (int64_t r = 0; r < s->n_rows; ++r)
-            for (int c = 0; c < 3; ++c) planes[(size_t)c * s->n_rows + r] = x[3 * r + c];
+            for (int c = 0; c < 3; ++c) bint[3 * (size_t)s->perm[r] + c] = b[3 * r + c];
+        BSR_TRY(cudaMemcpyAsync(s->d_b, bint.data(), sizeof(float) * 3 * s->n_rows, cudaMemcpyHostToDevice,
+                                s->stream));
+    }
+    if (x) {
+        planes.resize(3 * (size_t)s->n_rows);
+        for (int64_t r = 0; r < s->n_rows; ++r)
+            for (int c = 0; c < 3; ++c) planes[(size_t)c * s->n_rows + s->perm[r]] = x[3 * r + c];
         for (int c = 0; c < 3; ++c)
             BSR_TRY(cudaMemcpyAsync(s->args.x[c], planes.data() + (size_t)c * s->n_rows, sizeof(float) * s->n_rows,
                                     cudaMemcpyHostToDevice, s->stream));
-        BSR_TRY(cudaStreamSynchronize(s->stream));  // `planes` goes out of scope
     }
-    BSR_TRY(cudaStreamSynchronize(s->stream));
+    BSR_TRY(cudaStreamSynchronize(s->stream));  // the staging vectors go out of scope
     return OC_OK;
 }
 
@@ -674,7 +765,7 @@ oc_status oc_bsr_solve(oc_bsr_solver* s) {
             return bsr_fail_cuda(s, e, "oc_bsr_solve");
         }
         if (*h <= 0) break;
-        launch(k_bsr_spmv, a, s->n_blocks, s->stream);
+        launch(s->spmv, a, s->n_blocks, s->stream);
         launch(k_bsr_update, a, s->n_blocks, s->stream);
         e = cudaGetLastError();
         if (e != cudaSuccess) {
@@ -686,20 +777,93 @@ oc_status oc_bsr_solve(oc_bsr_solver* s) {
     return OC_OK;
 }
 
+oc_status oc_bsr_profile(oc_bsr_solver* s, int32_t n_solves, int32_t max_kernels, char* names, double* ms_total,
+                         int64_t* launches, double* algorithmic_bytes, int32_t* n_kernels) {
+    if (!bsr_valid(s) || n_solves < 0 || max_kernels < 0) return OC_ERR_INVALID_ARGUMENT;
+    BSR_TRY(cudaSetDevice(s->device));
+    // Algorithmic bytes of one launch, each array element once in the device layout (r and
+    // p are 16-byte records): pack 72 B per block (read and write 36) + 8 B per row; init
+    // 40 B per block (block + column) + 61 B per row (b, V, r and p out, fixed, row_ptr);
+    // spmv 40 B per block + 53 B per row (fixed, row_ptr, r, p in, q out); update 109 B
+    // per row (fixed, r, p, x, q in; x, r, p out).
+    const double nb = (double)s->nnzb, nr = (double)s->n_rows;
+    const char* kname[4] = {"k_bsr_pack", "k_bsr_init", "k_bsr_spmv", "k_bsr_update"};
+    const double kbytes[4] = {72.0 * nb + 8.0 * nr, 40.0 * nb + 61.0 * nr, 40.0 * nb + 53.0 * nr, 109.0 * nr};
+    double ms[4] = {0, 0, 0, 0};
+    int64_t cnt[4] = {0, 0, 0, 0};
+    cudaEvent_t e0, e1;
+    BSR_TRY(cudaEventCreate(&e0));
+    BSR_TRY(cudaEventCreate(&e1));
+    BsrArgs a = s->args;
+    a.use_cond = 0;
+    void (*kfn[4])(BsrArgs) = {k_bsr_pack, k_bsr_init, s->spmv, k_bsr_update};
+    int32_t* h = nullptr;
+    cudaError_t e = cudaMallocHost(&h, sizeof(int32_t));
+    auto timed = [&](int k) -> cudaError_t {
+        cudaError_t x = cudaEventRecord(e0, s->stream);
+        launch(kfn[k], a, s->n_blocks, s->stream);
+        if (x == cudaSuccess) x = cudaGetLastError();
+        if (x == cudaSuccess) x = cudaEventRecord(e1, s->stream);
+        if (x == cudaSuccess) x = cudaEventSynchronize(e1);
+        float t = 0.0f;
+        if (x == cudaSuccess) x = cudaEventElapsedTime(&t, e0, e1);
+        ms[k] += t;
+        cnt[k] += 1;
+        return x;
+    };
+    for (int32_t i = 0; i < n_solves && e == cudaSuccess; ++i) {
+        e = cudaMemsetAsync(a.unfinished, 0, sizeof(int32_t), s->stream);
+        if (e == cudaSuccess) e = timed(0);
+        if (e == cudaSuccess) e = timed(1);
+        for (;;) {
+            if (e == cudaSuccess) e = cudaMemcpyAsync(h, a.unfinished, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+            if (e != cudaSuccess || *h <= 0) break;
+            e = timed(2);
+            if (e == cudaSuccess) e = timed(3);
+        }
+    }
+    if (h) cudaFreeHost(h);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return bsr_fail_cuda(s, e, "oc_bsr_profile");
+    int32_t n = 0;
+    for (int k = 0; k < 4 && n < max_kernels; ++k, ++n) {
+        if (names) {
+            std::memset(names + 32 * n, 0, 32);
+            std::strncpy(names + 32 * n, kname[k], 31);
+        }
+        if (ms_total) ms_total[n] = ms[k];
+        if (launches) launches[n] = cnt[k];
+        if (algorithmic_bytes) algorithmic_bytes[n] = kbytes[k] * (double)cnt[k];
+    }
+    if (n_kernels) *n_kernels = n;
+    return OC_OK;
+}
+
 oc_status oc_bsr_get_solution(oc_bsr_solver* s, float* x, float* residual) {
     if (!bsr_valid(s)) return OC_ERR_INVALID_ARGUMENT;
     BSR_TRY(cudaSetDevice(s->device));
-    std::vector<float> planes(3 * (size_t)s->n_rows);
-    for (int which = 0; which < 2; ++which) {
-        float* out = which == 0 ? x : residual;
-        if (!out) continue;
-        float* const* src = which == 0 ? s->args.x : s->args.r;
+    if (x) {
+        std::vector<float> planes(3 * (size_t)s->n_rows);
         for (int c = 0; c < 3; ++c)
-            BSR_TRY(cudaMemcpyAsync(planes.data() + (size_t)c * s->n_rows, src[c], sizeof(float) * s->n_rows,
+            BSR_TRY(cudaMemcpyAsync(planes.data() + (size_t)c * s->n_rows, s->args.x[c], sizeof(float) * s->n_rows,
                                     cudaMemcpyDeviceToHost, s->stream));
         BSR_TRY(cudaStreamSynchronize(s->stream));
         for (int64_t r = 0; r < s->n_rows; ++r)
-            for (int c = 0; c < 3; ++c) out[3 * r + c] = planes[(size_t)c * s->n_rows + r];
+            for (int c = 0; c < 3; ++c) x[3 * r + c] = planes[(size_t)c * s->n_rows + s->perm[r]];
+    }
+    if (residual) {
+        std::vector<float4> r4((size_t)s->n_rows);
+        BSR_TRY(cudaMemcpyAsync(r4.data(), s->args.r4, sizeof(float4) * s->n_rows, cudaMemcpyDeviceToHost,
+                                s->stream));
+        BSR_TRY(cudaStreamSynchronize(s->stream));
+        for (int64_t r = 0; r < s->n_rows; ++r) {
+            const float4 v = r4[s->perm[r]];
+            residual[3 * r] = v.x;
+            residual[3 * r + 1] = v.y;
+            residual[3 * r + 2] = v.z;
+        }
     }
     return OC_OK;
 }

@@ -57,6 +57,17 @@ def tet_block_mesh(xdim: int, ydim: int, zdim: int, width=0.1, height=0.1, depth
     return Xi, X, tets.astype(np.int64), fixed
 
 
+def _tet_shapes(xdim: int, ydim: int, zdim: int, tets: np.ndarray):
+    """Every cube of the mesh has the same size, so a tetrahedron's rest shape depends
+    only on its cube's parity and its place among the cube's five: the shape index of
+    each tetrahedron and one representative tetrahedron of each shape."""
+    ncube = xdim * ydim * zdim
+    i, j, k = np.unravel_index(np.arange(ncube), (xdim, ydim, zdim))
+    shape = (((i + j + k) % 2)[:, None] * 5 + np.arange(5)[None, :]).ravel()
+    rep = np.array([np.argmax(shape == t) if (shape == t).any() else 0 for t in range(10)])
+    return shape, rep
+
+
 def element_stiffness(Xi: np.ndarray, tets: np.ndarray):
     """CalculateK (FEM:240-327): per tetrahedron the volume and the 4 x 4 blocks Ke[i][j]
     (3 x 3, first index the row as the demo uses them, FEM:666-669)."""
@@ -109,38 +120,37 @@ def fem_system(xdim: int, ydim: int, zdim: int, dt: float = 1.0 / 60.0, V=None, 
     added; from the second step on ClearStiffnessAssembly (FEM:414-422) zeroes them."""
     Xi, X, tets, fixed = tet_block_mesh(xdim, ydim, zdim)
     n = len(Xi)
-    vol, Ke = element_stiffness(Xi, tets)
+    shape, rep = _tet_shapes(xdim, ydim, zdim, tets)
+    vol_s, Ke_s = element_stiffness(Xi, tets[rep])
+    vol = vol_s[shape]
     # StiffnessAssembly with Re = I (FEM:659-698): K[ti][tj] += Ke[i][j] for j >= i and
-    # K[tj][ti] += Ke[i][j]^T for j > i.
+    # K[tj][ti] += Ke[i][j]^T for j > i.  Every contribution is one of 10 shapes x 16
+    # local blocks (or a transpose), so the assembly is a sparse count matrix (entry x
+    # block code) times the table of the 320 distinct blocks.
+    import scipy.sparse as sps
+
     ii, jj = np.triu_indices(4)
-    rows = [tets[:, ii].ravel()]
-    cols = [tets[:, jj].ravel()]
-    vals = [Ke[:, ii, jj].reshape(-1, 3, 3)]
     strict = ii < jj
-    rows.append(tets[:, jj[strict]].ravel())
-    cols.append(tets[:, ii[strict]].ravel())
-    vals.append(np.swapaxes(Ke[:, ii[strict], jj[strict]], -1, -2).reshape(-1, 3, 3))
-    r = np.concatenate(rows)
-    c = np.concatenate(cols)
-    v = np.concatenate(vals)
-    key = r * n + c
-    order = np.argsort(key, kind="stable")
-    key = key[order]
-    uniq, start = np.unique(key, return_index=True)
-    K = np.add.reduceat(v[order], start, axis=0)
+    table = np.concatenate([Ke_s.reshape(-1, 9), np.swapaxes(Ke_s, -1, -2).reshape(-1, 9)])  # codes 0..159, 160..319
+    code_up = shape[:, None] * 16 + (ii * 4 + jj)[None, :]
+    code_lo = 160 + shape[:, None] * 16 + (ii * 4 + jj)[strict][None, :]
+    r = np.concatenate([tets[:, ii].ravel(), tets[:, jj[strict]].ravel()])
+    c = np.concatenate([tets[:, jj].ravel(), tets[:, ii[strict]].ravel()])
+    code = np.concatenate([code_up.ravel(), code_lo.ravel()])
+    uniq, inv = np.unique(r * n + c, return_inverse=True)
+    counts = sps.csr_matrix((np.ones(len(inv)), (inv, code)), shape=(len(uniq), 320))
+    K = np.asarray(counts @ table).reshape(-1, 3, 3)
     urow, ucol = uniq // n, uniq % n
     if first_step:
         K = K + np.eye(3)[None]
-    row_ptr = np.zeros(n + 1, np.int64)
-    np.add.at(row_ptr, urow + 1, 1)
-    row_ptr = np.cumsum(row_ptr)
+    row_ptr = np.concatenate([[0], np.cumsum(np.bincount(urow, minlength=n))])
+    row_start = row_ptr[:-1][np.bincount(urow, minlength=n) > 0]  # every row has its diagonal block
     # F0 = -K Xi (FEM:691-694), F = m g (FEM:572-580), masses (FEM:388-405).
     mass = np.where(fixed == 1, FLT_MAX, 1.0 / n)
-    np.add.at(mass, tets.ravel(), np.repeat(DENSITY * vol * 0.25, 4))
-    KXi = np.zeros((n, 3))  # the element sums, which never see the identity start
-    np.add.at(KXi, urow, np.einsum("kab,kb->ka", K - np.eye(3)[None] if first_step else K, Xi[ucol]))
-    KX = np.zeros((n, 3))
-    np.add.at(KX, urow, np.einsum("kab,kb->ka", K, X[ucol]))
+    mass = mass + np.bincount(tets.ravel(), weights=np.repeat(DENSITY * vol * 0.25, 4), minlength=n)
+    # the element sums (F0) never see the identity start of the first assembly
+    KXi = np.add.reduceat(np.einsum("kab,kb->ka", K - np.eye(3)[None] if first_step else K, Xi[ucol]), row_start)
+    KX = np.add.reduceat(np.einsum("kab,kb->ka", K, X[ucol]), row_start)
     F = np.asarray(gravity)[None, :] * mass[:, None]
     Vel = np.zeros((n, 3)) if V is None else np.asarray(V, np.float64).reshape(n, 3)
     # DynamicsAssembly (FEM:790-831): A = K dt^2 + (m + dt c m) I on the diagonal,
@@ -219,6 +229,20 @@ class BsrSolver:
         r = np.empty((self.n_rows, 3), np.float32)
         self._call(self._lib.oc_bsr_get_solution(self._h, ptr(x), ptr(r)))
         return x, r
+
+    def profile(self, n_solves: int = 1) -> dict:
+        """Per kernel: total ms, launches and algorithmic bytes over n_solves un-graphed
+        solves timed with CUDA events."""
+        names = C.create_string_buffer(32 * 8)
+        ms = np.zeros(8)
+        launches = np.zeros(8, np.int64)
+        byts = np.zeros(8)
+        n = C.c_int32()
+        self._call(self._lib.oc_bsr_profile(self._h, int(n_solves), 8, names, ptr(ms), ptr(launches), ptr(byts),
+                                            C.byref(n)))
+        raw = names.raw
+        return {raw[32 * k: 32 * (k + 1)].split(b"\0", 1)[0].decode(): {
+            "ms_total": float(ms[k]), "launches": int(launches[k]), "bytes": float(byts[k])} for k in range(n.value)}
 
     def launch_count(self) -> int:
         n = C.c_int64()
