@@ -647,7 +647,7 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     {
         // Force-gather variant (a tuning knob; OC_GATHER_VARIANT overrides the default).
         const char* gv = std::getenv("OC_GATHER_VARIANT");
-        OC_CREATE_TRY(prepare_kernels(gv ? std::atoi(gv) : 1));
+        OC_CREATE_TRY(prepare_kernels(gv ? std::atoi(gv) : 6));
     }
     if (o.stream) {
         s->stream = static_cast<cudaStream_t>(o.stream);

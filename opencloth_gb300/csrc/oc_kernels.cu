@@ -158,9 +158,10 @@ __device__ __forceinline__ float assemble_vertex(const StepArgs& a, int64_t g, c
     return c.term;
 }
 
-// Assembly with one thread per vertex.
-template <int B>
-__global__ void __launch_bounds__(kThreads) k_assemble_thread(const StepArgs a) {
+// Assembly with one thread per vertex (MINB: minimum resident blocks per SM, which caps
+// the registers).
+template <int B, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_assemble_thread(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstParams& ip = a.inst[bi.inst];
@@ -462,16 +463,22 @@ __global__ void k_state_out(const StepArgs a, float* X3, float* V3, float* dV3, 
 }
 
 // Force-gather variant of k_assemble: 0 block-cooperative, 1/2/3 one thread per
-// vertex fetching 1/2/4 incidences ahead.  Measured on GB300 (1025 x 1025 cloth and the
-// 4096-cloth batch): variant 1 is fastest; wider prefetch costs occupancy.
-int kGatherVariant = 1;
+// vertex fetching 1/2/4 incidences ahead, 4/5/6 one incidence ahead with registers
+// capped for 5/6/4 resident blocks per SM.  Measured on GB300 (1025 x 1025 cloth and
+// the 4096-cloth batch, 4/6/8 vertices per thread): variant 6 at 8 vertices per thread
+// is fastest (64 registers; the uncapped kernel takes 75 and runs 1.5x slower, tighter
+// caps spill; wider prefetch costs occupancy).
+int kGatherVariant = 6;
 
 const void* assemble_fn(int v) {
     switch (v) {
         case 0: return (const void*)k_assemble_coop;
-        case 1: return (const void*)k_assemble_thread<1>;
-        case 2: return (const void*)k_assemble_thread<2>;
-        default: return (const void*)k_assemble_thread<4>;
+        case 1: return (const void*)k_assemble_thread<1, 1>;
+        case 2: return (const void*)k_assemble_thread<2, 1>;
+        case 3: return (const void*)k_assemble_thread<4, 1>;
+        case 4: return (const void*)k_assemble_thread<1, 5>;
+        case 5: return (const void*)k_assemble_thread<1, 6>;
+        default: return (const void*)k_assemble_thread<1, 4>;
     }
 }
 
@@ -515,7 +522,7 @@ int kernel_block_threads() { return kThreads; }
 size_t kernel_smem_bytes(KernelKind k) { return (k == K_ASSEMBLE && kGatherVariant == 0) ? kGatherSmem : 0; }
 
 cudaError_t prepare_kernels(int gather_variant) {
-    if (gather_variant < 0 || gather_variant > 3) return cudaErrorInvalidValue;
+    if (gather_variant < 0 || gather_variant > 6) return cudaErrorInvalidValue;
     kGatherVariant = gather_variant;
     return cudaFuncSetAttribute(k_assemble_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGatherSmem);
 }
@@ -542,12 +549,9 @@ cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStre
         case K_ASSEMBLE:
             if (kGatherVariant == 0)
                 k_assemble_coop<<<nblocks, kThreads, kGatherSmem, stream>>>(a);
-            else if (kGatherVariant == 1)
-                k_assemble_thread<1><<<nblocks, kThreads, 0, stream>>>(a);
-            else if (kGatherVariant == 2)
-                k_assemble_thread<2><<<nblocks, kThreads, 0, stream>>>(a);
             else
-                k_assemble_thread<4><<<nblocks, kThreads, 0, stream>>>(a);
+                reinterpret_cast<void (*)(StepArgs)>(const_cast<void*>(assemble_fn(kGatherVariant)))
+                    <<<nblocks, kThreads, 0, stream>>>(a);
             break;
         case K_CG_DIR: k_cg_dir<<<nblocks, kThreads, 0, stream>>>(a); break;
         case K_CG_UPDATE: k_cg_update<<<nblocks, kThreads, 0, stream>>>(a); break;
