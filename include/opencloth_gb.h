@@ -292,6 +292,12 @@ oc_status oc_bsr_profile(oc_bsr_solver* s, int32_t n_solves, int32_t max_kernels
 oc_status oc_bsr_synchronize(oc_bsr_solver* s);
 
 /* ---- reference topology builder (IMP:497-565) ------------------------------------ */
+/* Host only (no device work): validate the descriptors as oc_create does and report, per
+ * cloth, the grid (cols x rows) on which its incidences follow a stencil, or 0 x 0.  A
+ * grid cloth (the reference's lattice and spring order, at most 16 distinct
+ * rest/ks/kd) is assembled without reading incidence records. */
+oc_status oc_describe_instances(const oc_cloth_desc* descs, int32_t n_instances, int32_t* grid_cols,
+                                int32_t* grid_rows);
 /* Number of springs InitGL() creates for a cols x rows vertex grid (cols, rows >= 3):
  * rows*(cols-1) + cols*(rows-1) + 2*(rows-1)*(cols-1) + rows*(cols-1) + cols*(rows-1),
  * which includes the reference's one duplicate bend spring per row and column. */

@@ -132,6 +132,7 @@ SIGNATURES = {
     "oc_bsr_get_launch_count": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
     "oc_bsr_synchronize": (C.c_int32, [_P]),
     "oc_bsr_profile": (C.c_int32, [_P, C.c_int32, C.c_int32, _P, _P, _P, _P, _P]),
+    "oc_describe_instances": (C.c_int32, [C.POINTER(ClothDescC), C.c_int32, _P, _P]),
     "oc_grid_spring_count": (C.c_int32, [C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
     "oc_grid_build": (C.c_int32, [C.c_int32, C.c_int32, C.c_float, _P, _P, C.c_float, C.c_uint64, _P, _P]),
 }

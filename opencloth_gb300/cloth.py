@@ -107,6 +107,18 @@ def reference_ellipsoid():
     return (M.T.ravel().astype(np.float32), np.linalg.inv(M).T.ravel().astype(np.float32))
 
 
+def describe(descs) -> list:
+    """Per cloth, (cols, rows) of the grid whose stencil the step uses for it, or (0, 0)
+    for the general incidence gather (host only: no device needed)."""
+    descs = [descs] if isinstance(descs, ClothDesc) else list(descs)
+    lib = N.load()
+    arr = (N.ClothDescC * len(descs))(*[d.to_c() for d in descs])
+    cols = np.zeros(len(descs), np.int32)
+    rows = np.zeros(len(descs), np.int32)
+    _check(lib, lib.oc_describe_instances(arr, len(descs), ptr(cols), ptr(rows)), what="oc_describe_instances")
+    return list(zip(cols.tolist(), rows.tolist()))
+
+
 def grid_spring_count(cols: int, rows: int) -> int:
     lib = N.load()
     n = C.c_int32()

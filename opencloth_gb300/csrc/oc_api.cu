@@ -47,8 +47,10 @@ struct oc_solver {
     // streamed), the coupled kernels over the COUPLED cloths, k_integrate over the
     // streamed REFERENCE and the COUPLED cloths.  Without COUPLED cloths the first is the
     // full table and the last is the streamed one.
-    BlockInfo* d_asm_blocks = nullptr;
+    BlockInfo* d_asm_blocks = nullptr;  // REFERENCE cloths on the CSR gather
     int32_t n_asm_blocks = 0;
+    BlockInfo* d_grid_blocks = nullptr;  // REFERENCE grid cloths on the stencil gather
+    int32_t n_grid_blocks = 0;
     BlockInfo* d_cpl_blocks = nullptr;
     int32_t n_cpl_blocks = 0;
     BlockInfo* d_upd_blocks = nullptr;
@@ -161,7 +163,10 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
     for (int32_t k = 0; k < s->n_inst; ++k) {
         const double nv = (double)s->inst_host[k].nv, ns = (double)s->ns_inst[k];
         const InstState& st = s->h_state[k];
-        t->bytes[K_ASSEMBLE] += 120.0 * nv + 32.0 * ns;
+        if (s->inst_host[k].grid_cols > 0)
+            t->bytes[K_ASSEMBLE_GRID] += 120.0 * nv;  // no incidence records
+        else
+            t->bytes[K_ASSEMBLE] += 120.0 * nv + 32.0 * ns;
         // k_provot: X 16, V 32 in and out, pin flag 1, row pointer 4; 16-byte records.
         if (s->inst_host[k].passes & OC_PASS_PROVOT) t->bytes[K_PROVOT] += 53.0 * nv + 32.0 * ns;
         if (s->inst_host[k].coupled) {
@@ -254,7 +259,8 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
             a.blk_base = s->inst_host[grp].blk0;
             const int nb = s->inst_host[grp].nblk;
             const bool cpl = s->inst_host[grp].coupled != 0;
-            if ((st = launch_timed(s, cpl ? K_CPL_ASSEMBLE : K_ASSEMBLE, a, nb, t)) != OC_OK) return st;
+            const KernelKind ka = cpl ? K_CPL_ASSEMBLE : (s->inst_host[grp].grid_cols > 0 ? K_ASSEMBLE_GRID : K_ASSEMBLE);
+            if ((st = launch_timed(s, ka, a, nb, t)) != OC_OK) return st;
             s->host_launches += s->any_provot ? 3 : 2;
             for (;;) {
                 OC_TRY(cudaMemcpyAsync(s->h_scalar, &s->args.state[grp].active, sizeof(int32_t),
@@ -270,13 +276,18 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
     } else {
         // Assembly over every cloth, then the resident CG launches and the streamed loop.
         a.blk_base = 0;
-        StepArgs aa = a, ca = a, sa = a, ua = a;
+        StepArgs aa = a, ga = a, ca = a, sa = a, ua = a;
         aa.blocks = s->d_asm_blocks;
+        ga.blocks = s->d_grid_blocks;
         ca.blocks = s->d_cpl_blocks;
         sa.blocks = s->d_streamed_blocks;
         ua.blocks = s->d_upd_blocks;
         if (s->n_asm_blocks > 0) {
             if ((st = launch_timed(s, K_ASSEMBLE, aa, s->n_asm_blocks, t)) != OC_OK) return st;
+            s->host_launches += 1;
+        }
+        if (s->n_grid_blocks > 0) {
+            if ((st = launch_timed(s, K_ASSEMBLE_GRID, ga, s->n_grid_blocks, t)) != OC_OK) return st;
             s->host_launches += 1;
         }
         if (s->n_cpl_blocks > 0) {
@@ -341,22 +352,25 @@ oc_status build_graph(oc_solver* s, float dt) {
     a.blk_base = 0;
     a.use_cond = loop ? 1 : 0;
     a.cond = (unsigned long long)handle;
-    StepArgs aa = a, sa = a, ca = a, ua = a;
+    StepArgs aa = a, ga = a, sa = a, ca = a, ua = a;
     aa.blocks = s->d_asm_blocks;       // REFERENCE cloths: k_assemble
+    ga.blocks = s->d_grid_blocks;      // REFERENCE grid cloths: k_assemble_grid
     sa.blocks = s->d_streamed_blocks;  // streamed REFERENCE cloths: CG loop
     ca.blocks = s->d_cpl_blocks;       // COUPLED cloths
     ua.blocks = s->d_upd_blocks;       // k_integrate
     void* params_all[] = {&a};
     void* params_asm[] = {&aa};
+    void* params_grid[] = {&ga};
     void* params_str[] = {&sa};
     void* params_cpl[] = {&ca};
     void* params_upd[] = {&ua};
-    enum Table { T_ALL, T_ASM, T_STR, T_CPL, T_UPD };
+    enum Table { T_ALL, T_ASM, T_STR, T_CPL, T_UPD, T_GRID };
     auto kparams = [&](KernelKind k, Table tab) {
         cudaKernelNodeParams kp{};
         kp.func = const_cast<void*>(kernel_fn(k));
-        const int n[] = {s->n_blocks, s->n_asm_blocks, s->n_streamed_blocks, s->n_cpl_blocks, s->n_upd_blocks};
-        void** pp[] = {params_all, params_asm, params_str, params_cpl, params_upd};
+        const int n[] = {s->n_blocks, s->n_asm_blocks, s->n_streamed_blocks, s->n_cpl_blocks, s->n_upd_blocks,
+                         s->n_grid_blocks};
+        void** pp[] = {params_all, params_asm, params_str, params_cpl, params_upd, params_grid};
         kp.gridDim = dim3((unsigned)n[tab]);
         kp.blockDim = dim3((unsigned)kernel_block_threads());
         kp.sharedMemBytes = (unsigned)kernel_smem_bytes(k);
@@ -379,6 +393,11 @@ oc_status build_graph(oc_solver* s, float dt) {
     if (s->n_asm_blocks > 0) {
         kp = kparams(K_ASSEMBLE, T_ASM);
         OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &n_reset, 1, &kp));
+    }
+    if (s->n_grid_blocks > 0) {  // serialised after k_assemble: both end in the same counters
+        cudaGraphNode_t prev = n_asm;
+        kp = kparams(K_ASSEMBLE_GRID, T_GRID);
+        OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &prev, 1, &kp));
     }
     cudaGraphNode_t n_last = n_asm;  // the loop waits for every assembly
     if (coupled) {
@@ -618,6 +637,11 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
         delete s;
         return st;
     }
+    // OC_STENCIL=0 keeps grid cloths on the CSR gather (a diagnostic switch: both paths
+    // give the same bits).
+    if (const char* e = std::getenv("OC_STENCIL"))
+        if (std::atoi(e) == 0)
+            for (InstParams& ip : P.inst) ip.grid_cols = ip.grid_rows = 0;
     auto bail = [&](oc_status code) {
         std::fprintf(stderr, "oc_create: %s\n", s->err.c_str());
         release(s);
@@ -672,6 +696,21 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     OC_CREATE_TRY(upload(s, &own_par, P.own_par));
     a.rowptr = rowptr;
     a.inc = inc;
+    {
+        int32_t* d_st = nullptr;
+        OC_CREATE_TRY(upload(s, &d_st, P.st_data));
+        a.st_data = d_st;
+        float4* d_sp = nullptr;
+        OC_CREATE_TRY(upload(s, &d_sp, P.st_param));
+        a.st_param = d_sp;
+        if (P.any_st_rest) {
+            std::vector<float> rest(P.inc.size());
+            for (size_t k = 0; k < P.inc.size(); ++k) std::memcpy(&rest[k], &P.inc[k].y, 4);
+            float* d_rest = nullptr;
+            OC_CREATE_TRY(upload(s, &d_rest, rest));
+            a.rest_inc = d_rest;
+        }
+    }
     a.own_ends = own_ends;
     a.own_par = own_par;
     const size_t stride = (size_t)((P.nv + 63) / 64) * 64;
@@ -740,7 +779,7 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
         const int max_res = o.resident_max_vertices > 0 ? o.resident_max_vertices
                                                         : kResidentMaxCluster * kResidentDefaultVcta;
         s->resident.assign(P.n_inst, 0);
-        std::vector<BlockInfo> streamed, asm_ref, cpl, upd;
+        std::vector<BlockInfo> streamed, asm_ref, cpl, upd, grid;
         std::map<std::tuple<int, int, int>, std::vector<int32_t>> groups;
         for (int32_t k = 0; k < P.n_inst; ++k) {
             const bool cpl_k = P.inst[k].coupled != 0;
@@ -762,7 +801,10 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
                 upd.insert(upd.end(), kb, kb + P.inst[k].nblk);
                 continue;
             }
-            asm_ref.insert(asm_ref.end(), kb, kb + P.inst[k].nblk);
+            if (P.inst[k].grid_cols > 0)
+                grid.insert(grid.end(), kb, kb + P.inst[k].nblk);
+            else
+                asm_ref.insert(asm_ref.end(), kb, kb + P.inst[k].nblk);
             if (want) {
                 s->resident[k] = 1;
                 groups[std::make_tuple(threads, cluster, vcta)].push_back(k);
@@ -773,6 +815,8 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
         }
         s->n_asm_blocks = (int32_t)asm_ref.size();
         OC_CREATE_TRY(upload(s, &s->d_asm_blocks, asm_ref));
+        s->n_grid_blocks = (int32_t)grid.size();
+        OC_CREATE_TRY(upload(s, &s->d_grid_blocks, grid));
         s->n_cpl_blocks = (int32_t)cpl.size();
         OC_CREATE_TRY(upload(s, &s->d_cpl_blocks, cpl));
         s->n_upd_blocks = (int32_t)upd.size();
@@ -921,7 +965,7 @@ oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
         if (st != OC_OK) return st;
     }
     for (int32_t i = 0; i < n_steps; ++i) OC_TRY(cudaGraphLaunch(s->exec, s->stream));
-    const int64_t per_step = (s->n_asm_blocks > 0 ? 1 : 0) + (s->n_cpl_blocks > 0 ? 1 : 0) +
+    const int64_t per_step = (s->n_asm_blocks > 0 ? 1 : 0) + (s->n_grid_blocks > 0 ? 1 : 0) + (s->n_cpl_blocks > 0 ? 1 : 0) +
                              (s->n_upd_blocks > 0 ? 1 : 0) + (int64_t)s->buckets.size() + (s->any_provot ? 1 : 0);
     s->host_launches += per_step * (int64_t)n_steps;
     return OC_OK;
@@ -1127,13 +1171,15 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
     cudaEventDestroy(t.ev[0]);
     cudaEventDestroy(t.ev[1]);
     if (st != OC_OK) return st;
-    const KernelKind kinds[] = {K_ASSEMBLE,    K_CG_DIR,  K_CG_UPDATE, K_INTEGRATE, K_RESIDENT,
-                                K_PROVOT,      K_CPL_ASSEMBLE, K_CPL_DIR, K_CPL_UPDATE};
+    const KernelKind kinds[] = {K_ASSEMBLE, K_ASSEMBLE_GRID, K_CG_DIR,       K_CG_UPDATE, K_INTEGRATE,
+                                K_RESIDENT, K_PROVOT,        K_CPL_ASSEMBLE, K_CPL_DIR,   K_CPL_UPDATE};
     int32_t n = 0;
     for (KernelKind k : kinds) {
         if (n >= max_kernels) break;
         if (k == K_PROVOT && !s->any_provot) continue;
         if ((k == K_CPL_ASSEMBLE || k == K_CPL_DIR || k == K_CPL_UPDATE) && !s->any_coupled) continue;
+        if (k == K_ASSEMBLE_GRID && s->n_grid_blocks == 0) continue;
+        if (k == K_ASSEMBLE && s->n_grid_blocks > 0 && s->n_asm_blocks == 0) continue;
         if (names) {
             std::memset(names + 32 * n, 0, 32);
             std::strncpy(names + 32 * n, kernel_name(k), 31);

@@ -25,6 +25,11 @@ struct InstParams {
     int32_t resident;  // 1: this cloth's CG runs in the resident kernel, not the streamed loop
     int32_t passes;    // OC_PASS_* bits applied after the update
     int32_t coupled;   // 1: OC_JAC_COUPLED (block-sparse system, oc_coupled.cu)
+    int32_t grid_cols;  // > 0: the cloth is a grid whose incidences follow a stencil (k_assemble_grid)
+    int32_t grid_rows;
+    int32_t st_off;     // its class table and entries in StepArgs::st_data
+    int32_t st_par;     // its first parameter slot in StepArgs::st_param
+    int32_t st_rest;    // 1: rest lengths vary; read them per incidence from StepArgs::rest_inc
     float provot_ratio;     // IMP:808
     float ellipsoid[16];    // object -> world, column-major (IMP:583-585)
     float ellipsoid_inv[16];
@@ -87,6 +92,12 @@ struct StepArgs {
     // the other vertex and the spring block B = beta I + gamma n n^T of this step; per
     // vertex: m' and the CG vectors z = P^-1 r and q = A d.  P^-1 (the inverse of the
     // vertex's diagonal block) lives in the A planes.
+    // Grid cloths (InstParams::grid_cols > 0): per cloth 37 class starts then the entries
+    // (di + 2 | dj + 2 << 3 | is_p2 << 6 | slot << 7), and kStencilSlots parameter slots
+    // {rest, ks, kd, 0}.
+    const int32_t* st_data;
+    const float4* st_param;
+    const float* rest_inc;   // rest length of every incidence record (CSR order), or nullptr
     const int32_t* cpl_o;
     float* cpl_c[5];         // n0, n1, n2, beta, gamma
     float* cpl_m;
@@ -115,9 +126,19 @@ const void* adjoint_seed_fn();
 cudaError_t launch_set_spring_params(const StepArgs& a, const AdjArgs& j, const float* ks, const float* kd,
                                      int64_t n_rec, int64_t nv, cudaStream_t stream);
 
+constexpr int kStencilClasses = 36;  // 6 row classes x 6 column classes
+constexpr int kStencilSlots = 16;    // distinct (rest, ks, kd) per grid cloth
+
+// The position class of vertex (r, c) of a rows x cols grid, per dimension: 0 and 1 for
+// the first two rows (columns), 5, 4 and 3 for the last three (the third-last carries
+// the reference's extra bend spring, IMP:557-558 and 563-564), 2 inside.
+__host__ __device__ inline int stencil_class_1d(int32_t i, int32_t n) {
+    return i == 0 ? 0 : (i == n - 1 ? 5 : (i == 1 ? 1 : (i == n - 2 ? 4 : (i == n - 3 ? 3 : 2))));
+}
+
 enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3, K_FORCES = 4, K_RESIDENT = 5,
                   K_PROVOT = 6, K_ELLIPSOID = 7, K_CPL_ASSEMBLE = 8, K_CPL_DIR = 9, K_CPL_UPDATE = 10,
-                  K_COUNT = 11 };
+                  K_ASSEMBLE_GRID = 11, K_COUNT = 12 };
 
 // Interaction kernels (oc_interact.cu).
 cudaError_t launch_pick(const float4* X, int64_t v0, int64_t nv, const float pt[3], double radius, int32_t* out,
@@ -177,6 +198,9 @@ struct PackedHost {
     std::vector<int32_t> inc_sid;                     // spring id of every incidence record
     std::vector<int32_t> own_sid;                     // vertex i -> id of spring i, or -1
     std::vector<int32_t> own_rowptr, own_ent;         // vertex -> vertices whose spring touches it
+    std::vector<int32_t> st_data;                     // stencils of the grid cloths (see StepArgs)
+    std::vector<float4> st_param;
+    bool any_st_rest = false;                         // a grid cloth reads rest lengths per incidence
     bool any_provot = false;                          // some cloth has OC_PASS_PROVOT
     bool any_coupled = false;                         // some cloth is OC_JAC_COUPLED
 };

@@ -5,6 +5,7 @@
 //                incidence CSR, CalcForceDerivatives for spring i (IMP:737-772),
 //                the assembly of A_i, b_i, P_i (IMP:781-786) and the CG set-up
 //                r = b - A x, d = P^-1 r, delta0 = r.(P r) (IMP:310-318).
+//   k_assemble_grid  the same for grid cloths, with the neighbours from a stencil
 //   k_cg_dir     [d = r + beta d]; alpha = delta_new / d.(A d)    (IMP:320-321, 327)
 //   k_cg_update  x += alpha d; r -= alpha A d; delta_new = r.r     (IMP:322-326)
 //   k_integrate  V += dV dt; X += dt V; ground clamp               (IMP:790-797)
@@ -170,6 +171,74 @@ __global__ void __launch_bounds__(kThreads, MINB) k_assemble_thread(const StepAr
         const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
         const OwnSpring os = load_own(a, g);
         const float3 F = thread_gather<B>(a, ip, g, Xg, Vg);
+        acc_add(part, assemble_vertex(a, g, Xg, Vg, F, os));
+    }
+    finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
+}
+
+// F_i of a grid cloth from its stencil: the incidences of vertex (r, c) in spring-id
+// order are its class's template entries, neighbour = g + di cols + dj, parameters from
+// the cloth's slot table; the arithmetic and the summation order are thread_gather's.
+__device__ __forceinline__ float3 stencil_gather(const StepArgs& a, const InstParams& ip, int64_t g,
+                                                 const float4 Xg, const float4 Vg) {
+    const bool pinned = Vg.w != 0.0f;
+    float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
+    if (!pinned) {
+        Fx += Xg.w * ip.gravity[0];
+        Fy += Xg.w * ip.gravity[1];
+        Fz += Xg.w * ip.gravity[2];
+    }
+    Fx += ip.damping * Vg.x;
+    Fy += ip.damping * Vg.y;
+    Fz += ip.damping * Vg.z;
+    if (pinned) return make_float3(Fx, Fy, Fz);
+    if (ip.has_ext) {
+        const float4 e = __ldg(a.fext + g);
+        Fx += e.x;
+        Fy += e.y;
+        Fz += e.z;
+    }
+    const int32_t cols = ip.grid_cols;
+    const int32_t l = (int32_t)(g - ip.v_off);
+    const int32_t r = l / cols, c = l - r * cols;
+    const int cl = stencil_class_1d(r, ip.grid_rows) * 6 + stencil_class_1d(c, cols);
+    const int32_t* st = a.st_data + ip.st_off;
+    const float4* par = a.st_param + ip.st_par;
+    const int32_t e0 = __ldg(st + cl), e1 = __ldg(st + cl + 1);
+    // Rest lengths that vary come from the incidence's own slot of rest_inc.
+    const float* rest_inc = ip.st_rest ? a.rest_inc + __ldg(a.rowptr + g) - e0 : nullptr;
+    for (int32_t e = e0; e < e1; ++e) {
+        const int32_t v = __ldg(st + e);
+        const int32_t di = (v & 7) - 2, dj = ((v >> 3) & 7) - 2;
+        const int64_t o = g + (int64_t)di * cols + dj;
+        float4 p = __ldg(par + (v >> 7));
+        if (rest_inc) p.x = __ldg(rest_inc + e);
+        const float4 Xo = __ldg(a.X + o), Vo = __ldg(a.V + o);
+        if (v & 64) {  // F[p2] -= f, IMP:733
+            const float3 f = spring_force(Xo, Xg, Vo, Vg, p.x, p.y, p.z);
+            Fx -= f.x;
+            Fy -= f.y;
+            Fz -= f.z;
+        } else {  // F[p1] += f, IMP:731
+            const float3 f = spring_force(Xg, Xo, Vg, Vo, p.x, p.y, p.z);
+            Fx += f.x;
+            Fy += f.y;
+            Fz += f.z;
+        }
+    }
+    return make_float3(Fx, Fy, Fz);
+}
+
+// Assembly of grid cloths (one thread per vertex, no incidence records).
+__global__ void __launch_bounds__(kThreads, 4) k_assemble_grid(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const InstParams& ip = a.inst[bi.inst];
+    Acc part = acc_zero();
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
+        const OwnSpring os = load_own(a, g);
+        const float3 F = stencil_gather(a, ip, g, Xg, Vg);
         acc_add(part, assemble_vertex(a, g, Xg, Vg, F, os));
     }
     finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
@@ -495,6 +564,7 @@ const char* kernel_name(KernelKind k) {
         case K_PROVOT: return "k_provot";
         case K_ELLIPSOID: return "k_ellipsoid";
         case K_CPL_ASSEMBLE: return "k_cpl_assemble";
+        case K_ASSEMBLE_GRID: return "k_assemble_grid";
         case K_CPL_DIR: return "k_cpl_dir";
         case K_CPL_UPDATE: return "k_cpl_update";
         default: return "?";
@@ -513,6 +583,7 @@ const void* kernel_fn(KernelKind k) {
         case K_CPL_ASSEMBLE:
         case K_CPL_DIR:
         case K_CPL_UPDATE: return coupled_fn(k);
+        case K_ASSEMBLE_GRID: return (const void*)k_assemble_grid;
         default: return nullptr;
     }
 }
@@ -562,6 +633,7 @@ cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStre
         case K_CPL_ASSEMBLE:
         case K_CPL_DIR:
         case K_CPL_UPDATE: return launch_coupled(k, a, nblocks, stream);
+        case K_ASSEMBLE_GRID: k_assemble_grid<<<nblocks, kThreads, 0, stream>>>(a); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -223,6 +223,108 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
             }
         }
     }
+    // Grid cloths: the incidences of a vertex of a grid cloth made by the reference's
+    // lattice (InitGL, IMP:497-565) depend only on its position class (first, second,
+    // inner, third-last, second-last, last row, and the same for columns): the same neighbour offsets
+    // in the same spring order, with parameters from a few distinct (rest, ks, kd).  Such
+    // a cloth is stepped by a stencil kernel that reads no incidence records.  Every
+    // vertex is checked against its class's template; any mismatch keeps the CSR path.
+    P.st_data.clear();
+    P.st_param.clear();
+    P.any_st_rest = false;
+    for (int32_t k = 0; k < n; ++k) {
+        InstParams& ip = P.inst[k];
+        ip.grid_cols = ip.grid_rows = 0;
+        ip.st_off = ip.st_par = -1;
+        ip.st_rest = 0;
+        const int64_t vo = P.v_off[k];
+        const int32_t nvk = ip.nv;
+        if (nvk < 9) continue;
+        int32_t cols = 0;
+        for (int32_t e = P.rowptr[vo]; e < P.rowptr[vo + 1]; ++e) {
+            const int32_t o = (int32_t)((P.inc[e].x & 0x7fffffff) - vo);
+            if (o > 2 && (cols == 0 || o < cols)) cols = o;
+        }
+        if (cols < 3 || nvk % cols != 0 || nvk / cols < 3) continue;
+        const int32_t rows = nvk / cols;
+        // Two tries: parameter slots of (rest, ks, kd) -- no per-incidence data at all --
+        // and, when the rest lengths vary (grid spacings that FP32 does not hold exactly),
+        // slots of (ks, kd) with the rest lengths read per incidence.
+        std::vector<int4> slots;  // rest, ks, kd bits
+        std::vector<std::vector<int32_t>> tmpl;
+        bool ok = false;
+        int32_t mode = 0;
+        for (int32_t try_mode = 1; try_mode <= 2 && !ok; ++try_mode) {
+            const bool with_rest = try_mode == 1;
+            slots.clear();
+            tmpl.assign(kStencilClasses, std::vector<int32_t>());
+            std::vector<int32_t> rep(kStencilClasses, -1);
+            ok = true;
+            auto entry_of = [&](int32_t l, int32_t e, int32_t* out) -> bool {
+                const int4 rec = P.inc[e];
+                const int32_t o = (int32_t)((rec.x & 0x7fffffff) - vo);
+                const int32_t r = l / cols, c = l % cols, ro = o / cols, co = o % cols;
+                const int32_t di = ro - r, dj = co - c;
+                if (o < 0 || o >= nvk || di < -2 || di > 2 || dj < -2 || dj > 2) return false;
+                const int32_t rest_key = with_rest ? rec.y : 0;
+                int32_t slot = -1;
+                for (size_t q = 0; q < slots.size(); ++q)
+                    if (slots[q].y == rest_key && slots[q].z == rec.z && slots[q].w == rec.w) slot = (int32_t)q;
+                if (slot < 0) {
+                    if ((int)slots.size() >= kStencilSlots) return false;
+                    slot = (int32_t)slots.size();
+                    slots.push_back(make_int4(0, rest_key, rec.z, rec.w));
+                }
+                *out = (di + 2) | ((dj + 2) << 3) | ((rec.x < 0 ? 1 : 0) << 6) | (slot << 7);
+                return true;
+            };
+            // Templates from the first vertex of each class.
+            for (int32_t l = 0; l < nvk && ok; ++l) {
+                const int cl = stencil_class_1d(l / cols, rows) * 6 + stencil_class_1d(l % cols, cols);
+                if (rep[cl] >= 0) continue;
+                rep[cl] = l;
+                for (int32_t e = P.rowptr[vo + l]; e < P.rowptr[vo + l + 1] && ok; ++e) {
+                    int32_t v = 0;
+                    ok = entry_of(l, e, &v);
+                    tmpl[cl].push_back(v);
+                }
+            }
+            // Every vertex against its template.
+            for (int32_t l = 0; l < nvk && ok; ++l) {
+                const int cl = stencil_class_1d(l / cols, rows) * 6 + stencil_class_1d(l % cols, cols);
+                const int32_t e0 = P.rowptr[vo + l], e1 = P.rowptr[vo + l + 1];
+                if ((size_t)(e1 - e0) != tmpl[cl].size()) ok = false;
+                for (int32_t e = e0; e < e1 && ok; ++e) {
+                    int32_t v = 0;
+                    ok = entry_of(l, e, &v) && v == tmpl[cl][e - e0];
+                }
+            }
+            if (ok) mode = try_mode;
+        }
+        if (!ok) continue;
+        ip.st_rest = mode == 2 ? 1 : 0;
+        if (mode == 2) P.any_st_rest = true;
+        ip.grid_cols = cols;
+        ip.grid_rows = rows;
+        ip.st_off = (int32_t)P.st_data.size();
+        int32_t pos = kStencilClasses + 1;
+        for (int cl = 0; cl < kStencilClasses; ++cl) {
+            P.st_data.push_back(pos);
+            pos += (int32_t)tmpl[cl].size();
+        }
+        P.st_data.push_back(pos);
+        for (int cl = 0; cl < kStencilClasses; ++cl) P.st_data.insert(P.st_data.end(), tmpl[cl].begin(), tmpl[cl].end());
+        ip.st_par = (int32_t)P.st_param.size();
+        for (int q = 0; q < kStencilSlots; ++q) {
+            float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (q < (int)slots.size()) {
+                std::memcpy(&f.x, &slots[q].y, 4);
+                std::memcpy(&f.y, &slots[q].z, 4);
+                std::memcpy(&f.z, &slots[q].w, 4);
+            }
+            P.st_param.push_back(f);
+        }
+    }
     // Vertex -> vertices whose own spring (spring i for vertex i) touches it, ordered by i.
     P.own_rowptr.assign(nv + 1, 0);
     for (int64_t g = 0; g < nv; ++g) P.own_rowptr[g + 1] = P.own_rowptr[g] + own_deg[g];
@@ -240,6 +342,20 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
 }  // namespace oc
 
 extern "C" {
+
+oc_status oc_describe_instances(const oc_cloth_desc* descs, int32_t n_instances, int32_t* grid_cols,
+                                int32_t* grid_rows) {
+    if (!descs || n_instances < 1) return OC_ERR_INVALID_ARGUMENT;
+    oc::PackedHost P;
+    std::string err;
+    const oc_status st = oc::pack_instances(descs, n_instances, 2048, &P, &err);
+    if (st != OC_OK) return st;
+    for (int32_t k = 0; k < n_instances; ++k) {
+        if (grid_cols) grid_cols[k] = P.inst[k].grid_cols;
+        if (grid_rows) grid_rows[k] = P.inst[k].grid_rows;
+    }
+    return OC_OK;
+}
 
 oc_status oc_grid_spring_count(int32_t cols, int32_t rows, int32_t* n_springs) {
     if (!n_springs || cols < 3 || rows < 3) return OC_ERR_INVALID_ARGUMENT;

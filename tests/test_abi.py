@@ -165,3 +165,18 @@ def test_create_rejects_bad_passes():
     bad[5] = np.nan
     assert _status(_desc(passes=1, ellipsoid=bad, ellipsoid_inv=np.eye(4).ravel())) == 3  # OC_ERR_NON_FINITE
     assert _status(_desc(passes=2, provot_ratio=-1.0)) == 1
+
+
+def test_describe_detects_reference_grids():
+    """Grid cloths of the reference's lattice use the stencil assembly; anything else
+    (random per-spring parameters, a missing spring) the incidence gather."""
+    from opencloth_gb300 import describe
+
+    for cols, rows in ((3, 3), (6, 6), (21, 21), (9, 7), (128, 128), (1025, 65)):
+        X, sp = grid_cloth(cols, rows, jitter=1e-3)
+        assert describe(ClothDesc(n_vertices=cols * rows, springs=sp)) == [(cols, rows)]
+    X, sp = grid_cloth(9, 7)
+    odd = sp.copy()
+    odd["ks"][10] = 1.0
+    assert describe(ClothDesc(n_vertices=63, springs=odd)) == [(0, 0)]
+    assert describe(ClothDesc(n_vertices=63, springs=np.delete(sp, 5))) == [(0, 0)]
