@@ -56,6 +56,14 @@ struct oc_solver {
     BlockInfo* d_upd_blocks = nullptr;
     int32_t n_upd_blocks = 0;
     bool any_coupled = false;
+    // The CG loop of the streamed REFERENCE cloths as one cooperative launch (k_cg_persist)
+    // when there are few of them and no COUPLED cloth; otherwise the WHILE loop.
+    bool persist = false;
+    int32_t* d_persist_ids = nullptr;
+    int32_t n_persist = 0;
+    int persist_grid = 0;
+    unsigned* d_bar = nullptr;  // grid barrier: count at [0], generation at [32]
+    int* d_perr = nullptr;      // bit 0: a grid barrier gave up
     bool any_provot = false;  // some cloth has OC_PASS_PROVOT: k_provot follows the update
     bool any_passes = false;  // some cloth has a pass after the update
     // Resident buckets run concurrently: forked from the handle's stream onto these.
@@ -110,6 +118,15 @@ oc_status fail_cuda(oc_solver* s, cudaError_t e, const char* what) {
         cudaError_t e_ = (call);                              \
         if (e_ != cudaSuccess) return fail_cuda(s, e_, #call); \
     } while (0)
+
+// A grid barrier of k_cg_persist that gave up (the stream is synchronised).
+oc_status check_device_error(oc_solver* s) {
+    if (!s->d_perr) return OC_OK;
+    int h = 0;
+    OC_TRY(cudaMemcpy(&h, s->d_perr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h != 0) return fail(s, OC_ERR_DEVICE_TIMEOUT, "k_cg_persist: a grid barrier gave up");
+    return OC_OK;
+}
 
 template <class T>
 cudaError_t dalloc(oc_solver* s, T** p, size_t count) {
@@ -190,10 +207,14 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
             continue;
         }
         const double it = (double)st.iter;
-        t->bytes[K_INTEGRATE] += 76.0 * nv;
-        t->bytes[K_CG_UPDATE] += 84.0 * nv * it;
         double dirs = it > 0 ? 36.0 * nv + 60.0 * nv * (it - 1.0) : 0.0;
         if (st.flags & OC_FLAG_BREAKDOWN) dirs += (it > 0 ? 60.0 : 36.0) * nv;
+        if (s->persist) {  // k_cg_persist: the same passes and the update in one launch
+            t->bytes[K_CG_PERSIST] += dirs + 84.0 * nv * it + 76.0 * nv;
+            continue;
+        }
+        t->bytes[K_INTEGRATE] += 76.0 * nv;
+        t->bytes[K_CG_UPDATE] += 84.0 * nv * it;
         t->bytes[K_CG_DIR] += dirs;
     }
 }
@@ -296,7 +317,21 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
         }
         if ((st = launch_resident_all(s, a, t)) != OC_OK) return st;
         const int nb = s->n_streamed_blocks, nc = s->n_cpl_blocks;
-        if (nb > 0 || nc > 0) {
+        if (s->persist) {
+            if (t) OC_TRY(cudaEventRecord(t->ev[0], s->stream));
+            OC_TRY(cudaMemsetAsync(s->d_bar, 0, sizeof(unsigned), s->stream));
+            OC_TRY(launch_cg_persist(sa, s->d_persist_ids, s->n_persist, nb, s->persist_grid, s->d_bar, s->d_perr,
+                                     s->stream));
+            s->host_launches += 1;
+            if (t) {
+                OC_TRY(cudaEventRecord(t->ev[1], s->stream));
+                OC_TRY(cudaEventSynchronize(t->ev[1]));
+                float ms = 0.0f;
+                OC_TRY(cudaEventElapsedTime(&ms, t->ev[0], t->ev[1]));
+                t->ms[K_CG_PERSIST] += ms;
+                t->launches[K_CG_PERSIST] += 1;
+            }
+        } else if (nb > 0 || nc > 0) {
             for (;;) {
                 OC_TRY(cudaMemcpyAsync(s->h_scalar, a.unconverged, sizeof(int32_t), cudaMemcpyDeviceToHost,
                                        s->stream));
@@ -340,7 +375,8 @@ oc_status build_graph(oc_solver* s, float dt) {
     cudaGraph_t g = nullptr;
     OC_TRY(cudaGraphCreate(&g, 0));
     s->graph = g;
-    const bool streamed = s->n_streamed_blocks > 0, coupled = s->n_cpl_blocks > 0;
+    const bool persist = s->persist;
+    const bool streamed = s->n_streamed_blocks > 0 && !persist, coupled = s->n_cpl_blocks > 0;
     const bool loop = streamed || coupled;
     // The WHILE loop's handle exists only when there are streamed cloths (a handle that
     // no conditional node uses makes the graph fail to instantiate).
@@ -436,6 +472,35 @@ oc_status build_graph(oc_solver* s, float dt) {
         kp = kparams(K_INTEGRATE, T_UPD);
         OC_TRY(cudaGraphAddKernelNode(&n_int, g, &n_loop, 1, &kp));
         updates.push_back(n_int);
+    }
+    if (persist) {
+        // The streamed cloths' whole CG loop and update: a cooperative launch captured
+        // into a child graph after a memset of the barrier counter.
+        cudaGraphNode_t n_bar, n_pc;
+        cudaMemsetParams bp{};
+        bp.dst = s->d_bar;
+        bp.value = 0;
+        bp.elementSize = sizeof(unsigned);
+        bp.width = 1;
+        bp.height = 1;
+        bp.pitch = sizeof(unsigned);
+        OC_TRY(cudaGraphAddMemsetNode(&n_bar, g, &n_last, 1, &bp));
+        cudaGraph_t pg = nullptr;
+        OC_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        StepArgs pa = sa;
+        pa.blocks = s->d_streamed_blocks;
+        pa.use_cond = 0;
+        cudaError_t le = launch_cg_persist(pa, s->d_persist_ids, s->n_persist, s->n_streamed_blocks, s->persist_grid,
+                                           s->d_bar, s->d_perr, s->stream);
+        cudaError_t ce = cudaStreamEndCapture(s->stream, &pg);
+        if (le != cudaSuccess || ce != cudaSuccess) {
+            if (pg) cudaGraphDestroy(pg);
+            return fail_cuda(s, le != cudaSuccess ? le : ce, "capture of k_cg_persist");
+        }
+        cudaError_t e = cudaGraphAddChildGraphNode(&n_pc, g, &n_bar, 1, pg);
+        cudaGraphDestroy(pg);
+        if (e != cudaSuccess) return fail_cuda(s, e, "cudaGraphAddChildGraphNode");
+        updates.push_back(n_pc);
     }
     if (!s->buckets.empty()) {
         // The resident CG launches (concurrent, fork/join) captured into a child graph that
@@ -626,11 +691,29 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
 
     oc_solver* s = new (std::nothrow) oc_solver();
     if (!s) return OC_ERR_OUT_OF_MEMORY;
-    // Eight vertices per thread: fewer, longer-lived blocks (one wave for a 1M-vertex
-    // cloth) amortise the per-block reduction epilogue.
-    const int vpt = o.vertices_per_thread > 0 ? o.vertices_per_thread : 8;
+    // Block size: up to eight vertices per thread (2048-vertex blocks): fewer, longer-lived
+    // blocks amortise the per-block reduction epilogue.  When the whole batch would fill
+    // less than a few waves, the size is chosen so the block count is a multiple of the
+    // resident capacity (4 blocks per SM), so every SM gets the same work: a 1M-vertex
+    // cloth gets 608 blocks of 1728 vertices instead of 514 of 2048.
+    int vpb = kernel_block_threads() * (o.vertices_per_thread > 0 ? o.vertices_per_thread : 8);
+    if (o.vertices_per_thread <= 0) {
+        int n_sm = 0;
+        if (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, o.device) != cudaSuccess || n_sm <= 0)
+            n_sm = 152;
+        int64_t total = 0;
+        for (int32_t k = 0; k < n_instances; ++k) total += std::max(0, descs[k].n_vertices);
+        const int64_t slots = 4LL * n_sm;
+        if (total > 0 && total <= 3 * slots * (int64_t)vpb) {
+            const int64_t waves = (total + slots * vpb - 1) / (slots * vpb);  // 1..3
+            int64_t want = (total + waves * slots - 1) / (waves * slots);
+            want = (want + 31) / 32 * 32;
+            vpb = (int)std::min<int64_t>(std::max<int64_t>(want, 256), vpb);
+        }
+    }
+    const int vpt = (vpb + kernel_block_threads() - 1) / kernel_block_threads();
     PackedHost P;
-    oc_status st = pack_instances(descs, n_instances, kernel_block_threads() * vpt, &P, &s->err);
+    oc_status st = pack_instances(descs, n_instances, vpb, &P, &s->err);
     if (st != OC_OK) {
         // The message is only reachable through a handle; print it for the caller.
         std::fprintf(stderr, "oc_create: %s\n", s->err.c_str());
@@ -856,6 +939,31 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
             }
         }
     }
+    {
+        // Persistent CG for the streamed REFERENCE cloths: few of them, no COUPLED cloth,
+        // a cooperative launch fits, and OC_PERSIST is not 0.
+        std::vector<int32_t> ids;
+        for (int32_t k = 0; k < P.n_inst; ++k)
+            if (!s->resident[k] && !P.inst[k].coupled) ids.push_back(k);
+        const char* pe = std::getenv("OC_PERSIST");
+        const bool allowed = !(pe && std::atoi(pe) == 0) && s->executor != OC_EXEC_PLAIN;
+        const int per_sm = allowed ? persist_blocks_per_sm() : 0;
+        int n_sm = 0;
+        OC_CREATE_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, s->device));
+        int coop = 0;
+        OC_CREATE_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->device));
+        if (allowed && coop && per_sm > 0 && !ids.empty() && (int)ids.size() <= persist_max_instances() &&
+            !P.any_coupled) {
+            s->persist = true;
+            s->n_persist = (int32_t)ids.size();
+            s->persist_grid = std::min(per_sm * n_sm, std::max(1, s->n_streamed_blocks));
+            OC_CREATE_TRY(upload(s, &s->d_persist_ids, ids));
+            OC_CREATE_TRY(dalloc(s, &s->d_bar, 64));  // count at [0], generation at [32]
+            OC_CREATE_TRY(cudaMemset(s->d_bar, 0, 64 * sizeof(unsigned)));
+            OC_CREATE_TRY(dalloc(s, &s->d_perr, 1));
+            OC_CREATE_TRY(cudaMemset(s->d_perr, 0, sizeof(int)));
+        }
+    }
     OC_CREATE_TRY(dalloc(s, &a.unconverged, 1));
     OC_CREATE_TRY(dalloc(s, &a.grid_ticket, 1));
     OC_CREATE_TRY(dalloc(s, &a.loop_count, 1));
@@ -940,7 +1048,7 @@ oc_status oc_get_state(oc_solver* s, float* X, float* V, float* dV) {
     if (V) OC_TRY(cudaMemcpyAsync(V, sv, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     if (dV) OC_TRY(cudaMemcpyAsync(dV, sd, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     OC_TRY(cudaStreamSynchronize(s->stream));
-    return OC_OK;
+    return check_device_error(s);
 }
 
 oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
@@ -965,8 +1073,12 @@ oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
         if (st != OC_OK) return st;
     }
     for (int32_t i = 0; i < n_steps; ++i) OC_TRY(cudaGraphLaunch(s->exec, s->stream));
+    // assemblies, the persistent CG (which includes the update) or the update kernel,
+    // the resident launches and the Provot pass; the WHILE loop's launches are counted on
+    // the device (loop_count).
     const int64_t per_step = (s->n_asm_blocks > 0 ? 1 : 0) + (s->n_grid_blocks > 0 ? 1 : 0) + (s->n_cpl_blocks > 0 ? 1 : 0) +
-                             (s->n_upd_blocks > 0 ? 1 : 0) + (int64_t)s->buckets.size() + (s->any_provot ? 1 : 0);
+                             (s->persist ? 1 : (s->n_upd_blocks > 0 ? 1 : 0)) + (int64_t)s->buckets.size() +
+                             (s->any_provot ? 1 : 0);
     s->host_launches += per_step * (int64_t)n_steps;
     return OC_OK;
 }
@@ -1092,7 +1204,7 @@ oc_status oc_set_pins(oc_solver* s, int32_t instance, const int32_t* pins, int32
 oc_status oc_synchronize(oc_solver* s) {
     if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
     OC_TRY(cudaStreamSynchronize(s->stream));
-    return OC_OK;
+    return check_device_error(s);
 }
 
 oc_status oc_get_stats(oc_solver* s, int32_t* cg_iters, double* rel_residual, uint32_t* flags) {
@@ -1101,6 +1213,7 @@ oc_status oc_get_stats(oc_solver* s, int32_t* cg_iters, double* rel_residual, ui
     OC_TRY(cudaMemcpyAsync(s->h_state, s->args.state, sizeof(InstState) * s->n_inst, cudaMemcpyDeviceToHost,
                            s->stream));
     OC_TRY(cudaStreamSynchronize(s->stream));
+    if (oc_status e = check_device_error(s)) return e;
     for (int32_t k = 0; k < s->n_inst; ++k) {
         const InstState& st = s->h_state[k];
         if (cg_iters) cg_iters[k] = st.iter;
@@ -1171,14 +1284,16 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
     cudaEventDestroy(t.ev[0]);
     cudaEventDestroy(t.ev[1]);
     if (st != OC_OK) return st;
-    const KernelKind kinds[] = {K_ASSEMBLE, K_ASSEMBLE_GRID, K_CG_DIR,       K_CG_UPDATE, K_INTEGRATE,
-                                K_RESIDENT, K_PROVOT,        K_CPL_ASSEMBLE, K_CPL_DIR,   K_CPL_UPDATE};
+    const KernelKind kinds[] = {K_ASSEMBLE, K_ASSEMBLE_GRID, K_CG_DIR,  K_CG_UPDATE, K_INTEGRATE,  K_CG_PERSIST,
+                                K_RESIDENT, K_PROVOT,        K_CPL_ASSEMBLE, K_CPL_DIR, K_CPL_UPDATE};
     int32_t n = 0;
     for (KernelKind k : kinds) {
         if (n >= max_kernels) break;
         if (k == K_PROVOT && !s->any_provot) continue;
         if ((k == K_CPL_ASSEMBLE || k == K_CPL_DIR || k == K_CPL_UPDATE) && !s->any_coupled) continue;
         if (k == K_ASSEMBLE_GRID && s->n_grid_blocks == 0) continue;
+        if (k == K_CG_PERSIST && !s->persist) continue;
+        if ((k == K_CG_DIR || k == K_CG_UPDATE || k == K_INTEGRATE) && s->persist) continue;
         if (k == K_ASSEMBLE && s->n_grid_blocks > 0 && s->n_asm_blocks == 0) continue;
         if (names) {
             std::memset(names + 32 * n, 0, 32);

@@ -138,7 +138,16 @@ __host__ __device__ inline int stencil_class_1d(int32_t i, int32_t n) {
 
 enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3, K_FORCES = 4, K_RESIDENT = 5,
                   K_PROVOT = 6, K_ELLIPSOID = 7, K_CPL_ASSEMBLE = 8, K_CPL_DIR = 9, K_CPL_UPDATE = 10,
-                  K_ASSEMBLE_GRID = 11, K_COUNT = 12 };
+                  K_ASSEMBLE_GRID = 11, K_CG_PERSIST = 12, K_COUNT = 13 };
+
+// The whole CG loop of a few large streamed cloths in one cooperative launch
+// (oc_kernels.cu): block table a.blocks[0, n_entries), cloths inst_ids[0, n_inst);
+// bar: the arrival counter (zeroed before each launch) and, 128 bytes on, the generation;
+// err: bit 0 set if a grid barrier gave up.
+int persist_max_instances();
+int persist_blocks_per_sm();
+cudaError_t launch_cg_persist(const StepArgs& a, const int32_t* inst_ids, int32_t n_inst, int32_t n_entries,
+                              int grid, unsigned* bar, int* err, cudaStream_t stream);
 
 // Interaction kernels (oc_interact.cu).
 cudaError_t launch_pick(const float4* X, int64_t v0, int64_t nv, const float pt[3], double radius, int32_t* out,

@@ -267,63 +267,120 @@ __global__ void __launch_bounds__(kThreads) k_assemble_coop(const StepArgs a) {
 // flight (g and g + blockDim) before computing; __restrict__ lets the loads of the
 // next pair be issued ahead of this pair's stores.  The per-thread FP64 partial still
 // adds vertices in the order g, g + blockDim, g + 2 blockDim, ...
+//
+// The direction pass of one block: [d = r + beta d]; q = A d; its d.(A d) terms.
+__device__ __forceinline__ Acc cg_dir_block(const StepArgs& a, const BlockInfo& bi, bool first, float beta) {
+    Acc part = acc_zero();
+    const float* __restrict__ A0 = a.A[0];
+    const float* __restrict__ A1 = a.A[1];
+    const float* __restrict__ A2 = a.A[2];
+    const float* __restrict__ A3 = a.A[3];
+    const float* __restrict__ A4 = a.A[4];
+    const float* __restrict__ A5 = a.A[5];
+    const float* __restrict__ R0 = a.r[0];
+    const float* __restrict__ R1 = a.r[1];
+    const float* __restrict__ R2 = a.r[2];
+    float* __restrict__ D0 = a.d[0];
+    float* __restrict__ D1 = a.d[1];
+    float* __restrict__ D2 = a.d[2];
+    const int64_t T = blockDim.x;
+    for (int64_t base = bi.v_begin + threadIdx.x; base < bi.v_end; base += 2 * T) {
+        float A[2][6], d[2][3], r[2][3];
+        bool ok[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int64_t g = base + u * T;
+            ok[u] = g < bi.v_end;
+            const int64_t q = ok[u] ? g : base;
+            A[u][0] = A0[q]; A[u][1] = A1[q]; A[u][2] = A2[q];
+            A[u][3] = A3[q]; A[u][4] = A4[q]; A[u][5] = A5[q];
+            d[u][0] = D0[q]; d[u][1] = D1[q]; d[u][2] = D2[q];
+            r[u][0] = 0.f; r[u][1] = 0.f; r[u][2] = 0.f;
+            if (!first) {
+                r[u][0] = R0[q]; r[u][1] = R1[q]; r[u][2] = R2[q];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (!ok[u]) continue;
+            const int64_t g = base + u * T;
+            float d0 = d[u][0], d1 = d[u][1], d2 = d[u][2];
+            if (!first) {  // d = r + beta d, IMP:327
+                d0 = r[u][0] + d0 * beta;
+                d1 = r[u][1] + d1 * beta;
+                d2 = r[u][2] + d2 * beta;
+                D0[g] = d0;
+                D1[g] = d1;
+                D2[g] = d2;
+            }
+            float q0, q1, q2;
+            matvec(A[u], d0, d1, d2, q0, q1, q2);
+            acc_add(part, d0 * q0 + d1 * q1 + d2 * q2);
+        }
+    }
+    return part;
+}
+
+// The update pass of one block: x += alpha d; r -= alpha A d; its r.r terms.
+__device__ __forceinline__ Acc cg_update_block(const StepArgs& a, const BlockInfo& bi, float alpha) {
+    Acc part = acc_zero();
+    const float* __restrict__ A0 = a.A[0];
+    const float* __restrict__ A1 = a.A[1];
+    const float* __restrict__ A2 = a.A[2];
+    const float* __restrict__ A3 = a.A[3];
+    const float* __restrict__ A4 = a.A[4];
+    const float* __restrict__ A5 = a.A[5];
+    const float* __restrict__ D0 = a.d[0];
+    const float* __restrict__ D1 = a.d[1];
+    const float* __restrict__ D2 = a.d[2];
+    float* __restrict__ X0 = a.x[0];
+    float* __restrict__ X1 = a.x[1];
+    float* __restrict__ X2 = a.x[2];
+    float* __restrict__ R0 = a.r[0];
+    float* __restrict__ R1 = a.r[1];
+    float* __restrict__ R2 = a.r[2];
+    const int64_t T = blockDim.x;
+    for (int64_t base = bi.v_begin + threadIdx.x; base < bi.v_end; base += 2 * T) {
+        float A[2][6], d[2][3], x[2][3], r[2][3];
+        bool ok[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int64_t g = base + u * T;
+            ok[u] = g < bi.v_end;
+            const int64_t q = ok[u] ? g : base;
+            A[u][0] = A0[q]; A[u][1] = A1[q]; A[u][2] = A2[q];
+            A[u][3] = A3[q]; A[u][4] = A4[q]; A[u][5] = A5[q];
+            d[u][0] = D0[q]; d[u][1] = D1[q]; d[u][2] = D2[q];
+            x[u][0] = X0[q]; x[u][1] = X1[q]; x[u][2] = X2[q];
+            r[u][0] = R0[q]; r[u][1] = R1[q]; r[u][2] = R2[q];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (!ok[u]) continue;
+            const int64_t g = base + u * T;
+            float q0, q1, q2;
+            matvec(A[u], d[u][0], d[u][1], d[u][2], q0, q1, q2);
+            X0[g] = x[u][0] + d[u][0] * alpha;  // x = x + alpha d, IMP:322
+            X1[g] = x[u][1] + d[u][1] * alpha;
+            X2[g] = x[u][2] + d[u][2] * alpha;
+            const float r0 = r[u][0] - q0 * alpha;  // r = r - alpha q, IMP:323
+            const float r1 = r[u][1] - q1 * alpha;
+            const float r2 = r[u][2] - q2 * alpha;
+            R0[g] = r0;
+            R1[g] = r1;
+            R2[g] = r2;
+            acc_add(part, r0 * r0 + r1 * r1 + r2 * r2);
+        }
+    }
+    return part;
+}
+
 __global__ void __launch_bounds__(kThreads) k_cg_dir(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstState& st = a.state[bi.inst];
     const bool active = st.active != 0;
-    Acc part = acc_zero();
-    if (active) {
-        const bool first = st.iter == 0;
-        const float beta = st.beta;
-        const float* __restrict__ A0 = a.A[0];
-        const float* __restrict__ A1 = a.A[1];
-        const float* __restrict__ A2 = a.A[2];
-        const float* __restrict__ A3 = a.A[3];
-        const float* __restrict__ A4 = a.A[4];
-        const float* __restrict__ A5 = a.A[5];
-        const float* __restrict__ R0 = a.r[0];
-        const float* __restrict__ R1 = a.r[1];
-        const float* __restrict__ R2 = a.r[2];
-        float* __restrict__ D0 = a.d[0];
-        float* __restrict__ D1 = a.d[1];
-        float* __restrict__ D2 = a.d[2];
-        const int64_t T = blockDim.x;
-        for (int64_t base = bi.v_begin + threadIdx.x; base < bi.v_end; base += 2 * T) {
-            float A[2][6], d[2][3], r[2][3];
-            bool ok[2];
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                const int64_t g = base + u * T;
-                ok[u] = g < bi.v_end;
-                const int64_t q = ok[u] ? g : base;
-                A[u][0] = A0[q]; A[u][1] = A1[q]; A[u][2] = A2[q];
-                A[u][3] = A3[q]; A[u][4] = A4[q]; A[u][5] = A5[q];
-                d[u][0] = D0[q]; d[u][1] = D1[q]; d[u][2] = D2[q];
-                r[u][0] = 0.f; r[u][1] = 0.f; r[u][2] = 0.f;
-                if (!first) {
-                    r[u][0] = R0[q]; r[u][1] = R1[q]; r[u][2] = R2[q];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                if (!ok[u]) continue;
-                const int64_t g = base + u * T;
-                float d0 = d[u][0], d1 = d[u][1], d2 = d[u][2];
-                if (!first) {  // d = r + beta d, IMP:327
-                    d0 = r[u][0] + d0 * beta;
-                    d1 = r[u][1] + d1 * beta;
-                    d2 = r[u][2] + d2 * beta;
-                    D0[g] = d0;
-                    D1[g] = d1;
-                    D2[g] = d2;
-                }
-                float q0, q1, q2;
-                matvec(A[u], d0, d1, d2, q0, q1, q2);
-                acc_add(part, d0 * q0 + d1 * q1 + d2 * q2);
-            }
-        }
-    }
+    const Acc part = active ? cg_dir_block(a, bi, st.iter == 0, st.beta) : acc_zero();
     finish<K_CG_DIR>(a, bi.gblk, bi.inst, active, part);
 }
 
@@ -332,59 +389,198 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
     const BlockInfo bi = a.blocks[blk];
     const InstState& st = a.state[bi.inst];
     const bool active = st.active != 0;
-    Acc part = acc_zero();
-    if (active) {
-        const float alpha = st.alpha;
-        const float* __restrict__ A0 = a.A[0];
-        const float* __restrict__ A1 = a.A[1];
-        const float* __restrict__ A2 = a.A[2];
-        const float* __restrict__ A3 = a.A[3];
-        const float* __restrict__ A4 = a.A[4];
-        const float* __restrict__ A5 = a.A[5];
-        const float* __restrict__ D0 = a.d[0];
-        const float* __restrict__ D1 = a.d[1];
-        const float* __restrict__ D2 = a.d[2];
-        float* __restrict__ X0 = a.x[0];
-        float* __restrict__ X1 = a.x[1];
-        float* __restrict__ X2 = a.x[2];
-        float* __restrict__ R0 = a.r[0];
-        float* __restrict__ R1 = a.r[1];
-        float* __restrict__ R2 = a.r[2];
-        const int64_t T = blockDim.x;
-        for (int64_t base = bi.v_begin + threadIdx.x; base < bi.v_end; base += 2 * T) {
-            float A[2][6], d[2][3], x[2][3], r[2][3];
-            bool ok[2];
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                const int64_t g = base + u * T;
-                ok[u] = g < bi.v_end;
-                const int64_t q = ok[u] ? g : base;
-                A[u][0] = A0[q]; A[u][1] = A1[q]; A[u][2] = A2[q];
-                A[u][3] = A3[q]; A[u][4] = A4[q]; A[u][5] = A5[q];
-                d[u][0] = D0[q]; d[u][1] = D1[q]; d[u][2] = D2[q];
-                x[u][0] = X0[q]; x[u][1] = X1[q]; x[u][2] = X2[q];
-                r[u][0] = R0[q]; r[u][1] = R1[q]; r[u][2] = R2[q];
+    const Acc part = active ? cg_update_block(a, bi, st.alpha) : acc_zero();
+    finish<K_CG_UPDATE>(a, bi.gblk, bi.inst, active, part);
+}
+
+// ---- the whole CG loop in one cooperative launch ----------------------------------------
+// For a few large streamed cloths the loop's cost is the kernel boundaries, not the
+// bytes: each (k_cg_dir, k_cg_update) launch pays a launch, a tail and a serial
+// epilogue of about 12 us even on a small cloth.  k_cg_persist runs every iteration of
+// every streamed cloth in one launch, all its blocks co-resident (cooperative launch),
+// with two grid barriers per iteration.  Each block walks the streamed block table with
+// a stride of the grid and runs the same per-block passes as k_cg_dir / k_cg_update,
+// writing the same per-block partials.  After each barrier every block recomputes each
+// cloth's totals from those partials with the same fixed-order sum the last-block
+// epilogue uses, and applies the same scalar rules, so all blocks hold identical copies
+// of the scalars without further communication and the results are those of the
+// two-kernel loop bit for bit.  The update is fused at the end (it is per vertex).
+
+constexpr int kPersistMaxInst = 16;       // streamed cloths one launch handles
+constexpr unsigned kBarrierSpins = 1u << 22;  // a barrier gives up after ~0.5 s
+
+// Grid-wide barrier on a generation counter, bounded: a wait that runs out sets bit 0 of
+// *err and returns false (the kernel then unwinds; the host reports the error).  The
+// arrival counter and the generation live on separate 128-byte lines, and waiters poll
+// the generation with plain acquire loads, so the polling does not queue behind the
+// arrivals' atomics.
+__device__ __forceinline__ unsigned load_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ bool grid_barrier(unsigned* count, unsigned* gen, unsigned nblocks, int* err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s_ok = 1;
+        const unsigned g0 = load_acquire(gen);
+        __threadfence();
+        const unsigned t = atomicAdd(count, 1u);
+        if (t == nblocks - 1) {
+            atomicExch(count, 0u);
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            unsigned spins = 0;
+            while (load_acquire(gen) == g0) {
+                if (++spins > kBarrierSpins) {
+                    atomicOr(err, 1);
+                    s_ok = 0;
+                    break;
+                }
+                __nanosleep(32);
             }
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                if (!ok[u]) continue;
-                const int64_t g = base + u * T;
-                float q0, q1, q2;
-                matvec(A[u], d[u][0], d[u][1], d[u][2], q0, q1, q2);
-                X0[g] = x[u][0] + d[u][0] * alpha;  // x = x + alpha d, IMP:322
-                X1[g] = x[u][1] + d[u][1] * alpha;
-                X2[g] = x[u][2] + d[u][2] * alpha;
-                const float r0 = r[u][0] - q0 * alpha;  // r = r - alpha q, IMP:323
-                const float r1 = r[u][1] - q1 * alpha;
-                const float r2 = r[u][2] - q2 * alpha;
-                R0[g] = r0;
-                R1[g] = r1;
-                R2[g] = r2;
-                acc_add(part, r0 * r0 + r1 * r1 + r2 * r2);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// A cloth's total over its blocks' partials: the last-block epilogue's order (finish).
+__device__ double instance_total(const StepArgs& a, const InstParams& ip) {
+    __shared__ double s_tot;
+    double acc = 0.0;
+#pragma unroll 8
+    for (int j = threadIdx.x; j < ip.nblk; j += blockDim.x) acc += __ldcg(a.partials + ip.blk0 + j);
+    const double total = block_sum(acc);
+    if (threadIdx.x == 0) s_tot = total;
+    __syncthreads();
+    const double t = s_tot;
+    __syncthreads();
+    return t;
+}
+
+struct PersistScalars {
+    double delta_new, delta0, dq;
+    float alpha, beta;
+    int32_t iter, active;
+    uint32_t flags;
+};
+
+__global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, const int32_t* inst_ids, int32_t n_inst,
+                                                            int32_t n_entries, unsigned* bar, int* err) {
+    __shared__ PersistScalars sc[kPersistMaxInst];
+    __shared__ int s_any;
+    for (int k = threadIdx.x; k < n_inst; k += blockDim.x) {
+        const InstState& st = a.state[inst_ids[k]];
+        sc[k].delta_new = st.delta_new;
+        sc[k].delta0 = st.delta0;
+        sc[k].dq = st.dq;
+        sc[k].alpha = st.alpha;
+        sc[k].beta = st.beta;
+        sc[k].iter = st.iter;
+        sc[k].active = st.active;
+        sc[k].flags = st.flags;
+    }
+    __syncthreads();
+    auto local = [&](int32_t inst) {
+        int li = 0;
+        while (li < n_inst - 1 && inst_ids[li] != inst) ++li;
+        return li;
+    };
+    bool ok = true;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int any = 0;
+            for (int k = 0; k < n_inst; ++k) any |= sc[k].active;
+            s_any = any;
+        }
+        __syncthreads();
+        if (!s_any || !ok) break;
+        // Direction pass (k_cg_dir).
+        for (int32_t e = blockIdx.x; e < n_entries; e += gridDim.x) {
+            const BlockInfo bi = a.blocks[e];
+            const PersistScalars& c = sc[local(bi.inst)];
+            if (!c.active) continue;
+            const double bsum = block_sum_acc(cg_dir_block(a, bi, c.iter == 0, c.beta));
+            if (threadIdx.x == 0) a.partials[bi.gblk] = bsum;
+        }
+        ok = grid_barrier(bar, bar + 32, gridDim.x, err);
+        if (!ok) break;
+        for (int k = 0; k < n_inst; ++k) {
+            if (!sc[k].active) continue;
+            const double total = instance_total(a, a.inst[inst_ids[k]]);
+            if (threadIdx.x == 0) {  // finish<K_CG_DIR>
+                PersistScalars& c = sc[k];
+                c.dq = total;
+                if (!(total > 0.0) || !isfinite(total)) {
+                    c.flags |= isfinite(total) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
+                    c.active = 0;
+                } else {
+                    c.alpha = (float)(c.delta_new / total);
+                }
+            }
+            __syncthreads();
+        }
+        // Update pass (k_cg_update).
+        for (int32_t e = blockIdx.x; e < n_entries; e += gridDim.x) {
+            const BlockInfo bi = a.blocks[e];
+            const PersistScalars& c = sc[local(bi.inst)];
+            if (!c.active) continue;
+            const double bsum = block_sum_acc(cg_update_block(a, bi, c.alpha));
+            if (threadIdx.x == 0) a.partials[bi.gblk] = bsum;
+        }
+        ok = grid_barrier(bar, bar + 32, gridDim.x, err);
+        if (!ok) break;
+        for (int k = 0; k < n_inst; ++k) {
+            if (!sc[k].active) continue;
+            const InstParams& ip = a.inst[inst_ids[k]];
+            const double total = instance_total(a, ip);
+            if (threadIdx.x == 0) {  // finish<K_CG_UPDATE>
+                PersistScalars& c = sc[k];
+                const double old = c.delta_new;
+                c.delta_new = total;
+                c.beta = (float)(total / old);
+                c.iter += 1;
+                const bool more = c.iter < ip.imax && total > (double)ip.eps2 * c.delta0;
+                if (!isfinite(total)) c.flags |= OC_FLAG_NON_FINITE;
+                if (!more || !isfinite(total)) {
+                    if (isfinite(total) && total > (double)ip.eps2 * c.delta0) c.flags |= OC_FLAG_NOT_CONVERGED;
+                    c.active = 0;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // The update of these cloths (k_integrate): per vertex, no barrier needed.
+    if (ok) {
+        for (int32_t e = blockIdx.x; e < n_entries; e += gridDim.x) {
+            const BlockInfo bi = a.blocks[e];
+            const InstParams& ip = a.inst[bi.inst];
+            for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+                float4 Xg = a.X[g], Vg = a.V[g];
+                update_vertex(ip, a.dt, a.x[0][g], a.x[1][g], a.x[2][g], Xg, Vg);
+                a.X[g] = Xg;
+                a.V[g] = Vg;
             }
         }
     }
-    finish<K_CG_UPDATE>(a, bi.gblk, bi.inst, active, part);
+    if (blockIdx.x == 0) {
+        for (int k = threadIdx.x; k < n_inst; k += blockDim.x) {
+            InstState& st = a.state[inst_ids[k]];
+            const PersistScalars& c = sc[k];
+            st.delta_new = c.delta_new;
+            st.dq = c.dq;
+            st.alpha = c.alpha;
+            st.beta = c.beta;
+            st.iter = c.iter;
+            st.active = 0;
+            st.flags = c.flags;
+        }
+    }
 }
 
 __global__ void __launch_bounds__(kThreads) k_integrate(const StepArgs a) {
@@ -565,6 +761,7 @@ const char* kernel_name(KernelKind k) {
         case K_ELLIPSOID: return "k_ellipsoid";
         case K_CPL_ASSEMBLE: return "k_cpl_assemble";
         case K_ASSEMBLE_GRID: return "k_assemble_grid";
+        case K_CG_PERSIST: return "k_cg_persist";
         case K_CPL_DIR: return "k_cpl_dir";
         case K_CPL_UPDATE: return "k_cpl_update";
         default: return "?";
@@ -637,6 +834,29 @@ cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStre
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+int persist_max_instances() { return kPersistMaxInst; }
+
+int persist_blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cg_persist, kThreads, 0) != cudaSuccess) return 0;
+    return n;
+}
+
+cudaError_t launch_cg_persist(const StepArgs& a, const int32_t* inst_ids, int32_t n_inst, int32_t n_entries,
+                              int grid, unsigned* bar, int* err, cudaStream_t stream) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)kThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_cg_persist, a, inst_ids, n_inst, n_entries, bar, err);
 }
 
 }  // namespace oc

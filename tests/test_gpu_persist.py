@@ -1,0 +1,90 @@
+"""The persistent CG (k_cg_persist: every iteration of the streamed cloths in one
+cooperative launch) against the two-kernel WHILE loop (OC_PERSIST=0): the same per-block
+passes, the same fixed-order totals and scalar rules, so the same bits and the same
+iteration counts."""
+import os
+
+import numpy as np
+import pytest
+
+from opencloth_gb300 import PASS_ELLIPSOID, PASS_PROVOT, ClothDesc, ClothSolver, grid_cloth, reference_ellipsoid
+
+pytestmark = pytest.mark.gpu
+
+DT = 1.0 / 60.0
+
+
+def same_bits(a, b) -> bool:
+    return np.array_equal(np.asarray(a).view(np.uint32), np.asarray(b).view(np.uint32))
+
+
+def run(descs, X, V, steps, persist: bool, **kw):
+    old = os.environ.get("OC_PERSIST")
+    os.environ["OC_PERSIST"] = "1" if persist else "0"
+    try:
+        s = ClothSolver(descs, **kw)
+    finally:
+        if old is None:
+            del os.environ["OC_PERSIST"]
+        else:
+            os.environ["OC_PERSIST"] = old
+    with s:
+        s.set_state(X, V)
+        s.step(DT, steps)
+        return s.get_state(), s.stats()
+
+
+def cloth(cols, rows, seed, ks=(50.75, 50.75, 50.95), passes=0):
+    rng = np.random.default_rng(seed)
+    X, sp = grid_cloth(cols, rows, ks=ks, kd=(-0.25, -0.25, -0.25), jitter=1e-2, seed=seed)
+    V = rng.normal(0.0, 0.01, X.shape).astype(np.float32)
+    V[[0, cols - 1]] = 0.0
+    E = Einv = None
+    if passes:
+        E, Einv = reference_ellipsoid()
+    d = ClothDesc(n_vertices=cols * rows, springs=sp, pinned=np.array([0, cols - 1], np.int32), cg_max_iter=200,
+                  cg_tol=1e-5, passes=passes, ellipsoid=E, ellipsoid_inv=Einv)
+    return d, X, V
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_single_large_cloth(graph):
+    d, X, V = cloth(193, 161, 1)  # 31k vertices: streamed
+    a, sa = run(d, X, V, 12, True, use_graph=graph)
+    b, sb = run(d, X, V, 12, False, use_graph=graph)
+    for x, y in zip(a, b):
+        assert same_bits(x, y)
+    assert np.array_equal(sa[0], sb[0]) and np.array_equal(sa[2], sb[2]) and sa[0][0] > 1
+
+
+def test_several_streamed_cloths_beside_resident_ones():
+    parts = [cloth(150, 140, 2), cloth(40, 40, 3), cloth(260, 90, 4, ks=(500.0, 400.0, 300.0)), cloth(17, 23, 5)]
+    descs = [p[0] for p in parts]
+    X = np.concatenate([p[1] for p in parts])
+    V = np.concatenate([p[2] for p in parts])
+    a, sa = run(descs, X, V, 10, True)
+    b, sb = run(descs, X, V, 10, False)
+    for x, y in zip(a, b):
+        assert same_bits(x, y)
+    assert np.array_equal(sa[0], sb[0]) and np.array_equal(sa[2], sb[2])
+
+
+def test_with_passes():
+    d, X, V = cloth(150, 130, 6, ks=(5.0, 5.0, 5.0), passes=PASS_ELLIPSOID | PASS_PROVOT)
+    X = X.copy()
+    X[:, 1] -= 2.0
+    a, _ = run(d, X, V, 8, True)
+    b, _ = run(d, X, V, 8, False)
+    for x, y in zip(a, b):
+        assert same_bits(x, y)
+
+
+def test_launch_count_is_per_step():
+    d, X, V = cloth(193, 161, 7)
+    with ClothSolver(d) as s:
+        s.set_state(X, V)
+        s.step(DT, 1)
+        l0 = s.launch_count()
+        s.step(DT, 5)
+        # assembly + the persistent CG (with the update) per step
+        assert s.launch_count() - l0 == 10
