@@ -109,10 +109,20 @@ def algorithmic_bytes(kernel: str, n_vertices: int, n_springs: int, first_dir: b
         # X, V 32 + rowptr 4 + own spring ends/params 24 + warm start 12 + A 24 + r 12 + d 12
         # per vertex, plus two 16-byte incidence records per spring.
         return 120 * N + 32 * S
+    if kernel == "k_assemble_grid":
+        # k_assemble without the incidence records and the row pointer (the neighbours come
+        # from the lattice's stencil); rest lengths that vary add the row pointer and 4 B
+        # per incidence.
+        return 116 * N
     if kernel == "k_cg_dir":
         return (36 if first_dir else 60) * N  # A 24 + d 12 (+ r 12, d write 12)
     if kernel == "k_cg_update":
         return 84 * N  # A 24 + d 12 + x 12 + r 12, write x 12 + r 12
+    if kernel == "k_cg_persist":
+        # one step's CG passes and the update in one launch: 36 + 60 (it - 1) B for the
+        # directions, 84 it B for the updates, 76 B for the closing update; use
+        # first_dir=True for one iteration.
+        return (36 + 84 + 76) * N if first_dir else (60 + 84) * N
     if kernel == "k_integrate":
         return 76 * N  # X, V 32 + dV 12 in, X, V 32 out
     if kernel == "k_provot":
@@ -295,8 +305,13 @@ def _dominant_roofline(prof: dict, peak: float, workload: str) -> dict:
 
 
 def _cg_roofline(prof: dict, peak: float) -> dict:
-    """The two SpMV-bound CG passes together (the COUPLED pair when present)."""
-    pair = ["k_cpl_dir", "k_cpl_update"] if "k_cpl_dir" in prof else ["k_cg_dir", "k_cg_update"]
+    """The SpMV-bound CG kernels the step actually launched (persistent, block-resident,
+    direction/update or the COUPLED pair), their algorithmic bytes over their summed
+    CUDA-event durations."""
+    cg = ["k_cg_persist", "k_resident", "k_cg_dir", "k_cg_update", "k_cpl_dir", "k_cpl_update"]
+    pair = [k for k in cg if k in prof and prof[k]["launches"] > 0]
+    if not pair:
+        return None
     byts = sum(prof[k]["bytes"] for k in pair)
     secs = sum(prof[k]["ms_total"] for k in pair) / 1e3
     achieved = byts / secs / 1e9 if secs > 0 else 0.0

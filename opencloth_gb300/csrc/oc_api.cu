@@ -41,6 +41,12 @@ struct oc_solver {
     };
     std::vector<Bucket> buckets;
     std::vector<uint8_t> resident;  // per instance
+    // OC_RESIDENT_FUSED=1: resident cloths assemble inside the resident kernel (no
+    // k_assemble pass over them).  Off by default: on 4096 cloths of 64 to 16,384 vertices
+    // the fused step measured 4.97 ms against 4.37 ms for the separate passes (the
+    // resident CTAs, 3 per SM by shared memory, assemble and then wait in the CG in
+    // step with each other, so the assembly runs at lower occupancy and overlaps nothing).
+    bool resident_fused = false;
     BlockInfo* d_streamed_blocks = nullptr;
     int32_t n_streamed_blocks = 0;
     // Block tables of a step: k_assemble over the REFERENCE cloths (resident and
@@ -174,15 +180,18 @@ struct KernelTimer {
 // Algorithmic bytes of one step, from each instance's CG iteration count: every array
 // element a kernel must read or write counted once, in the device layout (X/V float4,
 // 16-byte incidence records, FP32 planes).  Per vertex: k_assemble 120 B plus 32 B per
-// spring, first k_cg_dir pass 36 B, later passes 60 B, k_cg_update 84 B, k_integrate 76 B
+// spring, k_assemble_grid 116 B (plus the row pointer 4 B and 4 B per incidence when rest
+// lengths are read per incidence), first k_cg_dir pass 36 B, later passes 60 B, k_cg_update 84 B, k_integrate 76 B
 // (the ellipsoid pass adds no traffic), k_provot 53 B plus 32 B per spring.
 void account_step_bytes(const oc_solver* s, KernelTimer* t) {
     for (int32_t k = 0; k < s->n_inst; ++k) {
         const double nv = (double)s->inst_host[k].nv, ns = (double)s->ns_inst[k];
         const InstState& st = s->h_state[k];
-        if (s->inst_host[k].grid_cols > 0)
-            t->bytes[K_ASSEMBLE_GRID] += 120.0 * nv;  // no incidence records
-        else
+        const bool fused = s->resident[k] && s->resident_fused;  // assembled by k_resident
+        if (!fused && s->inst_host[k].grid_cols > 0)  // no incidence records, no row pointer
+            t->bytes[K_ASSEMBLE_GRID] +=              // unless rest lengths are per incidence
+                116.0 * nv + (s->inst_host[k].st_rest ? 4.0 * nv + 8.0 * ns : 0.0);
+        else if (!fused)
             t->bytes[K_ASSEMBLE] += 120.0 * nv + 32.0 * ns;
         // k_provot: X 16, V 32 in and out, pin flag 1, row pointer 4; 16-byte records.
         if (s->inst_host[k].passes & OC_PASS_PROVOT) t->bytes[K_PROVOT] += 53.0 * nv + 32.0 * ns;
@@ -201,9 +210,19 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
             continue;
         }
         if (s->resident[k]) {
-            // CG state in (A 24 + x, r, d 36), X, V 32 in and out, dV 12 out; the CG
-            // iterations run in shared memory.
-            t->bytes[K_RESIDENT] += 136.0 * nv;
+            if (s->resident_fused) {
+                // X, V 32 in and out, spring i 24, warm start 12 in and out, plus the
+                // gather's row pointer and records (or stencil rest lengths); the CG
+                // iterations run in shared memory.
+                const InstParams& ip = s->inst_host[k];
+                double gather = 4.0 * nv + 32.0 * ns;
+                if (ip.grid_cols > 0) gather = ip.st_rest ? 4.0 * nv + 8.0 * ns : 0.0;
+                t->bytes[K_RESIDENT] += 112.0 * nv + gather;
+            } else {
+                // CG state in (A 24 + x, r, d 36), X, V 32 in and out, dV 12 out; the CG
+                // iterations run in shared memory.
+                t->bytes[K_RESIDENT] += 136.0 * nv;
+            }
             continue;
         }
         const double it = (double)st.iter;
@@ -240,7 +259,7 @@ oc_status launch_resident_all(oc_solver* s, const StepArgs& a, KernelTimer* t) {
         for (size_t i = 0; i < s->aux.size(); ++i) OC_TRY(cudaStreamWaitEvent(s->aux[i], s->fork_ev, 0));
         for (size_t i = 0; i < s->buckets.size(); ++i) {
             const auto& b = s->buckets[i];
-            ResidentLaunch L{b.d_ids, b.cluster, b.vcta};
+            ResidentLaunch L{b.d_ids, b.cluster, b.vcta, s->resident_fused ? 1 : 0};
             OC_TRY(launch_resident(a, L, b.threads, b.n, s->aux[i % s->aux.size()]));
             s->host_launches += 1;
         }
@@ -252,7 +271,7 @@ oc_status launch_resident_all(oc_solver* s, const StepArgs& a, KernelTimer* t) {
     }
     for (const auto& b : s->buckets) {
         if (t) OC_TRY(cudaEventRecord(t->ev[0], s->stream));
-        ResidentLaunch L{b.d_ids, b.cluster, b.vcta};
+        ResidentLaunch L{b.d_ids, b.cluster, b.vcta, s->resident_fused ? 1 : 0};
         OC_TRY(launch_resident(a, L, b.threads, b.n, s->stream));
         s->host_launches += 1;
         if (t) {
@@ -503,8 +522,9 @@ oc_status build_graph(oc_solver* s, float dt) {
         updates.push_back(n_pc);
     }
     if (!s->buckets.empty()) {
-        // The resident CG launches (concurrent, fork/join) captured into a child graph that
-        // runs after the assembly, beside the streamed loop (they touch disjoint cloths).
+        // The resident launches (concurrent, fork/join) captured into a child graph that
+        // runs beside the streamed cloths' kernels (they touch disjoint cloths): after the
+        // assembly when that pass builds the resident cloths' systems, else from the start.
         cudaGraph_t rg = nullptr;
         OC_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
         StepArgs ra = a;
@@ -519,7 +539,7 @@ oc_status build_graph(oc_solver* s, float dt) {
         }
         if (ce != cudaSuccess) return fail_cuda(s, ce, "cudaStreamEndCapture");
         cudaGraphNode_t n_res;
-        cudaError_t e = cudaGraphAddChildGraphNode(&n_res, g, &n_asm, 1, rg);
+        cudaError_t e = cudaGraphAddChildGraphNode(&n_res, g, s->resident_fused ? &n_reset : &n_asm, 1, rg);
         cudaGraphDestroy(rg);
         if (e != cudaSuccess) return fail_cuda(s, e, "cudaGraphAddChildGraphNode");
         updates.push_back(n_res);
@@ -739,6 +759,7 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
 
     s->device = o.device;
     s->executor = o.executor;
+    if (const char* rf = std::getenv("OC_RESIDENT_FUSED")) s->resident_fused = std::atoi(rf) != 0;
     s->use_graph = o.use_graph != 0;
     s->n_inst = P.n_inst;
     s->nv = P.nv;
@@ -884,10 +905,12 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
                 upd.insert(upd.end(), kb, kb + P.inst[k].nblk);
                 continue;
             }
-            if (P.inst[k].grid_cols > 0)
-                grid.insert(grid.end(), kb, kb + P.inst[k].nblk);
-            else
-                asm_ref.insert(asm_ref.end(), kb, kb + P.inst[k].nblk);
+            if (!(want && s->resident_fused)) {
+                if (P.inst[k].grid_cols > 0)
+                    grid.insert(grid.end(), kb, kb + P.inst[k].nblk);
+                else
+                    asm_ref.insert(asm_ref.end(), kb, kb + P.inst[k].nblk);
+            }
             if (want) {
                 s->resident[k] = 1;
                 groups[std::make_tuple(threads, cluster, vcta)].push_back(k);

@@ -179,6 +179,7 @@ struct ResidentLaunch {
     const int32_t* inst_ids;  // the cloth of each cluster
     int32_t cluster;
     int32_t vcta;
+    int32_t fused;  // 1: the kernel assembles its cloth's system itself (no k_assemble pass)
 };
 constexpr int kResidentMaxVcta = 2048;
 constexpr int kResidentMaxCluster = 16;

@@ -176,59 +176,6 @@ __global__ void __launch_bounds__(kThreads, MINB) k_assemble_thread(const StepAr
     finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
 }
 
-// F_i of a grid cloth from its stencil: the incidences of vertex (r, c) in spring-id
-// order are its class's template entries, neighbour = g + di cols + dj, parameters from
-// the cloth's slot table; the arithmetic and the summation order are thread_gather's.
-__device__ __forceinline__ float3 stencil_gather(const StepArgs& a, const InstParams& ip, int64_t g,
-                                                 const float4 Xg, const float4 Vg) {
-    const bool pinned = Vg.w != 0.0f;
-    float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
-    if (!pinned) {
-        Fx += Xg.w * ip.gravity[0];
-        Fy += Xg.w * ip.gravity[1];
-        Fz += Xg.w * ip.gravity[2];
-    }
-    Fx += ip.damping * Vg.x;
-    Fy += ip.damping * Vg.y;
-    Fz += ip.damping * Vg.z;
-    if (pinned) return make_float3(Fx, Fy, Fz);
-    if (ip.has_ext) {
-        const float4 e = __ldg(a.fext + g);
-        Fx += e.x;
-        Fy += e.y;
-        Fz += e.z;
-    }
-    const int32_t cols = ip.grid_cols;
-    const int32_t l = (int32_t)(g - ip.v_off);
-    const int32_t r = l / cols, c = l - r * cols;
-    const int cl = stencil_class_1d(r, ip.grid_rows) * 6 + stencil_class_1d(c, cols);
-    const int32_t* st = a.st_data + ip.st_off;
-    const float4* par = a.st_param + ip.st_par;
-    const int32_t e0 = __ldg(st + cl), e1 = __ldg(st + cl + 1);
-    // Rest lengths that vary come from the incidence's own slot of rest_inc.
-    const float* rest_inc = ip.st_rest ? a.rest_inc + __ldg(a.rowptr + g) - e0 : nullptr;
-    for (int32_t e = e0; e < e1; ++e) {
-        const int32_t v = __ldg(st + e);
-        const int32_t di = (v & 7) - 2, dj = ((v >> 3) & 7) - 2;
-        const int64_t o = g + (int64_t)di * cols + dj;
-        float4 p = __ldg(par + (v >> 7));
-        if (rest_inc) p.x = __ldg(rest_inc + e);
-        const float4 Xo = __ldg(a.X + o), Vo = __ldg(a.V + o);
-        if (v & 64) {  // F[p2] -= f, IMP:733
-            const float3 f = spring_force(Xo, Xg, Vo, Vg, p.x, p.y, p.z);
-            Fx -= f.x;
-            Fy -= f.y;
-            Fz -= f.z;
-        } else {  // F[p1] += f, IMP:731
-            const float3 f = spring_force(Xg, Xo, Vg, Vo, p.x, p.y, p.z);
-            Fx += f.x;
-            Fy += f.y;
-            Fz += f.z;
-        }
-    }
-    return make_float3(Fx, Fy, Fz);
-}
-
 // Assembly of grid cloths (one thread per vertex, no incidence records).
 __global__ void __launch_bounds__(kThreads, 4) k_assemble_grid(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;

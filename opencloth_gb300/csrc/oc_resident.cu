@@ -1,12 +1,16 @@
-// Resident CG: after k_assemble has built every cloth's system and CG set-up, one
-// cluster of CTAs per cloth loads that cloth's CG state (A, x, r, d: 60 B per vertex)
-// into shared memory once, runs the complete preconditioned CG to the cloth's own
-// tolerance (IMP:308-330) on chip, and applies the update (IMP:790-797).  The CG loop
-// touches no HBM and needs no per-iteration launch.  Dot products reduce per CTA (Acc pairs within warps,
-// FP64 above), then in FP64 across the cluster through distributed shared memory
-// after a hardware cluster barrier; every
-// CTA sums the CTAs' partials in rank order, so all of them take identical
-// decisions.  There are no spin-waits.
+// Resident step: one cluster of CTAs per cloth holds that cloth's CG state (A, x, r, d:
+// 60 B per vertex) in shared memory, runs the complete preconditioned CG to the cloth's
+// own tolerance (IMP:308-330) on chip, and applies the update (IMP:790-797).  Fused (an
+// option of the solver), the CTAs first assemble their vertices' systems themselves (ComputeForces
+// and the Jacobians, IMP:701-783, with the same per-vertex functions as k_assemble /
+// k_assemble_grid) straight into shared memory, so a small cloth's whole step is one
+// kernel whose HBM traffic is the state in and out; unfused, they load the state
+// k_assemble left in the planes.  The CG loop touches no HBM and needs no per-iteration
+// launch.
+// Dot products reduce per CTA (Acc pairs within warps, FP64 above), then in FP64 across
+// the cluster through distributed shared memory after a hardware cluster barrier, in
+// the same fixed order in every CTA, so all of them take identical decisions.  There
+// are no spin-waits.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -19,7 +23,10 @@ namespace oc {
 namespace {
 
 // FP64 sum over the CTA, then over the cluster (C CTAs), identical in every CTA.
-// slots[2] (double-buffered per call) and bcast live in shared memory.
+// slots[2] (double-buffered per call) and bcast live in shared memory.  Lane r of warp 0
+// reads CTA r's partial over distributed shared memory, so the C remote loads are in
+// flight together, and the lanes combine them with a fixed shuffle tree (absent ranks
+// are zero): every CTA runs the same tree on the same values.
 __device__ double cluster_sum(Acc part, int C, double* slots, double* bcast, int& phase) {
     const double bs = block_sum_acc(part);
     if (C == 1) {
@@ -32,17 +39,26 @@ __device__ double cluster_sum(Acc part, int C, double* slots, double* bcast, int
     ++phase;
     if (threadIdx.x == 0) *slot = bs;
     cl.sync();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int r = 0; r < C; ++r) t += *cl.map_shared_rank(slot, r);
-        *bcast = t;
+    if (threadIdx.x < 32) {
+        const int r = threadIdx.x;
+        double t = r < C ? *cl.map_shared_rank(slot, r) : 0.0;
+        t = warp_sum(t);
+        if (r == 0) *bcast = t;
     }
     __syncthreads();
     return *bcast;
 }
 
+// Resident CTAs per SM the register budget is set for: 128-thread CTAs hold up to 512
+// vertices, 256-thread CTAs 256 to 1024 (3 to 15 CTAs by shared memory), 512-thread CTAs
+// 2048 (one).
 template <int T>
-__global__ void __launch_bounds__(T) k_resident(const StepArgs a, const ResidentLaunch L) {
+constexpr int resident_min_blocks() {
+    return T == 128 ? 8 : (T == 256 ? 4 : 1);
+}
+
+template <int T>
+__global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const StepArgs a, const ResidentLaunch L) {
     extern __shared__ __align__(16) float smem[];
     __shared__ double slots[2];
     __shared__ double bcast;
@@ -68,28 +84,66 @@ __global__ void __launch_bounds__(T) k_resident(const StepArgs a, const Resident
         sd[k] = smem + (12 + k) * cap;
     }
 
-    // The CG state k_assemble left in the planes: A, x, r, d -> shared memory.
-    for (int j = threadIdx.x; j < n_local; j += T) {
-        const int64_t g = base + j;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) sA[k][j] = a.A[k][g];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            sx[k][j] = a.x[k][g];
-            sr[k][j] = a.r[k][g];
-            sd[k][j] = a.d[k][g];
-        }
-    }
-    __syncthreads();
     int phase = 0;
     Acc part;
-    const InstState& st0 = a.state[inst];
-    const double delta0 = st0.delta0;
+    double delta0;
+    uint32_t flags;
+    bool run;
+    if (L.fused) {
+        // The assembly of these vertices (k_assemble / k_assemble_grid), into shared
+        // memory; X and V are written at the end of this kernel, so they are read with
+        // plain loads.
+        part = acc_zero();
+        for (int j = threadIdx.x; j < n_local; j += T) {
+            const int64_t g = base + j;
+            const float4 Xg = a.X[g], Vg = a.V[g];
+            const OwnSpring os = load_own<false>(a, g);
+            const float3 F =
+                ip.grid_cols > 0 ? stencil_gather<false>(a, ip, g, Xg, Vg) : thread_gather<1, false>(a, ip, g, Xg, Vg);
+            const VertexSystem sys = vertex_system(a.dt, Xg, Vg, F, os);
+            const CgInit c = cg_init(sys, a.x[0][g], a.x[1][g], a.x[2][g], Vg.w != 0.0f);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) sA[k][j] = sys.A[k];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                sx[k][j] = c.x[k];
+                sr[k][j] = c.r[k];
+                sd[k][j] = c.d[k];
+            }
+            acc_add(part, c.term);
+        }
+        // delta0 and the decision to iterate, as the assembly's last-block epilogue takes
+        // them (finish<K_ASSEMBLE>).  The cluster reduction also orders every CTA's reads
+        // of X and V before any CTA's writes below.
+        delta0 = cluster_sum(part, C, slots, &bcast, phase);
+        flags = 0u;
+        run = (0 < ip.imax) && (delta0 > (double)ip.eps2 * delta0);
+        if (!isfinite(delta0)) {
+            flags |= OC_FLAG_NON_FINITE;
+            run = false;
+        }
+    } else {
+        // The CG state k_assemble left in the planes: A, x, r, d -> shared memory.
+        for (int j = threadIdx.x; j < n_local; j += T) {
+            const int64_t g = base + j;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) sA[k][j] = a.A[k][g];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                sx[k][j] = a.x[k][g];
+                sr[k][j] = a.r[k][g];
+                sd[k][j] = a.d[k][g];
+            }
+        }
+        __syncthreads();
+        const InstState& st0 = a.state[inst];
+        delta0 = st0.delta0;
+        flags = st0.flags;
+        run = st0.active != 0;
+    }
     double delta = delta0;
     const double thresh = (double)ip.eps2 * delta0;
-    uint32_t flags = st0.flags;
     int it = 0;
-    bool run = st0.active != 0;
     float beta = 0.0f;
     while (run) {
         // d = r + beta d (after the first iteration), d.(A d), IMP:320-321, 327.
@@ -165,6 +219,7 @@ __global__ void __launch_bounds__(T) k_resident(const StepArgs a, const Resident
         InstState& st = a.state[inst];
         st.delta0 = delta0;
         st.delta_new = delta;
+        st.dq = 0.0;
         st.iter = it;
         st.flags = flags;
         st.active = 0;
