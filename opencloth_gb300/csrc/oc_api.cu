@@ -68,7 +68,7 @@ struct oc_solver {
     int32_t* d_persist_ids = nullptr;
     int32_t n_persist = 0;
     int persist_grid = 0;
-    unsigned* d_bar = nullptr;  // grid barrier: count at [0], generation at [32]
+    unsigned* d_bar = nullptr;  // grid barrier: arrivals [0], generation [32], totals [64]
     int* d_perr = nullptr;      // bit 0: a grid barrier gave up
     bool any_provot = false;  // some cloth has OC_PASS_PROVOT: k_provot follows the update
     bool any_passes = false;  // some cloth has a pass after the update
@@ -981,8 +981,9 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
             s->n_persist = (int32_t)ids.size();
             s->persist_grid = std::min(per_sm * n_sm, std::max(1, s->n_streamed_blocks));
             OC_CREATE_TRY(upload(s, &s->d_persist_ids, ids));
-            OC_CREATE_TRY(dalloc(s, &s->d_bar, 64));  // count at [0], generation at [32]
-            OC_CREATE_TRY(cudaMemset(s->d_bar, 0, 64 * sizeof(unsigned)));
+            // arrival word at [0], generation at [32], the cloths' totals (16 doubles) at [64]
+            OC_CREATE_TRY(dalloc(s, &s->d_bar, 128));
+            OC_CREATE_TRY(cudaMemset(s->d_bar, 0, 128 * sizeof(unsigned)));
             OC_CREATE_TRY(dalloc(s, &s->d_perr, 1));
             OC_CREATE_TRY(cudaMemset(s->d_perr, 0, sizeof(int)));
         }

@@ -347,53 +347,30 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
 // every streamed cloth in one launch, all its blocks co-resident (cooperative launch),
 // with two grid barriers per iteration.  Each block walks the streamed block table with
 // a stride of the grid and runs the same per-block passes as k_cg_dir / k_cg_update,
-// writing the same per-block partials.  After each barrier every block recomputes each
-// cloth's totals from those partials with the same fixed-order sum the last-block
-// epilogue uses, and applies the same scalar rules, so all blocks hold identical copies
-// of the scalars without further communication and the results are those of the
-// two-kernel loop bit for bit.  The update is fused at the end (it is per vertex).
+// writing the same per-block partials.  The last block to reach a barrier sums each
+// cloth's partials with the same fixed-order sum the last-block epilogue uses and
+// publishes the totals before it releases the others; every block then applies the
+// same scalar rules to the same totals, so all blocks hold identical copies of the
+// scalars and the results are those of the two-kernel loop bit for bit.  The update is
+// fused at the end (it is per vertex).
 
 constexpr int kPersistMaxInst = 16;       // streamed cloths one launch handles
 constexpr unsigned kBarrierSpins = 1u << 22;  // a barrier gives up after ~0.5 s
 
-// Grid-wide barrier on a generation counter, bounded: a wait that runs out sets bit 0 of
-// *err and returns false (the kernel then unwinds; the host reports the error).  The
-// arrival counter and the generation live on separate 128-byte lines, and waiters poll
-// the generation with plain acquire loads, so the polling does not queue behind the
-// arrivals' atomics.
 __device__ __forceinline__ unsigned load_acquire(const unsigned* p) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
 
-__device__ bool grid_barrier(unsigned* count, unsigned* gen, unsigned nblocks, int* err) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        s_ok = 1;
-        const unsigned g0 = load_acquire(gen);
-        __threadfence();
-        const unsigned t = atomicAdd(count, 1u);
-        if (t == nblocks - 1) {
-            atomicExch(count, 0u);
-            __threadfence();
-            atomicAdd(gen, 1u);
-        } else {
-            unsigned spins = 0;
-            while (load_acquire(gen) == g0) {
-                if (++spins > kBarrierSpins) {
-                    atomicOr(err, 1);
-                    s_ok = 0;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return s_ok != 0;
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned x) {
+    unsigned v;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "r"(x) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void red_add_release(unsigned* p, unsigned x) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(x) : "memory");
 }
 
 // A cloth's total over its blocks' partials: the last-block epilogue's order (finish).
@@ -417,10 +394,63 @@ struct PersistScalars {
     uint32_t flags;
 };
 
+// Grid barrier that also forms the cloths' totals, bounded.  bar[0] is the arrival word:
+// block 0 adds 2^31 - (n - 1), every other block 1, so the n-th arrival, whichever it
+// is, flips bit 31 and the low bits are back where they started (no reset).  That last
+// block sums the partials of every active cloth into totals[] and then bumps the
+// generation bar[32] with a release; the others poll the generation with acquire loads
+// and read the totals into tot[] (shared).  A wait that runs out sets bit 0 of *err and
+// returns false (the kernel then unwinds; the host reports the error).
+__device__ bool barrier_totals(const StepArgs& a, const int32_t* inst_ids, int n_inst, const PersistScalars* sc,
+                               unsigned* bar, double* totals, int* err, double* tot) {
+    __shared__ int s_last, s_ok;
+    unsigned* gen = bar + 32;
+    __syncthreads();  // this block's partial (thread 0's store) precedes its arrival
+    if (threadIdx.x == 0) {
+        s_ok = 1;
+        const unsigned nb = gridDim.x;
+        const unsigned add = blockIdx.x == 0 ? 0x80000000u - (nb - 1) : 1u;
+        const unsigned g0 = load_acquire(gen);
+        const unsigned old = atom_add_acq_rel(bar, add);
+        s_last = ((old ^ (old + add)) & 0x80000000u) != 0;
+        if (!s_last) {
+            unsigned spins = 0;
+            while (load_acquire(gen) == g0) {
+                if (++spins > kBarrierSpins) {
+                    atomicOr(err, 1);
+                    s_ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+    }
+    __syncthreads();
+    if (!s_ok) return false;
+    if (s_last) {
+        for (int k = 0; k < n_inst; ++k) {
+            if (!sc[k].active) continue;
+            const double t = instance_total(a, a.inst[inst_ids[k]]);
+            if (threadIdx.x == 0) {
+                tot[k] = t;
+                totals[k] = t;
+            }
+        }
+        if (threadIdx.x == 0) red_add_release(gen, 1u);
+    } else if (threadIdx.x == 0) {
+        for (int k = 0; k < n_inst; ++k)
+            if (sc[k].active) tot[k] = __ldcg(totals + k);
+    }
+    __syncthreads();
+    return true;
+}
+
 __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, const int32_t* inst_ids, int32_t n_inst,
                                                             int32_t n_entries, unsigned* bar, int* err) {
     __shared__ PersistScalars sc[kPersistMaxInst];
+    __shared__ double tot[kPersistMaxInst];
     __shared__ int s_any;
+    double* totals = reinterpret_cast<double*>(bar + 64);
     for (int k = threadIdx.x; k < n_inst; k += blockDim.x) {
         const InstState& st = a.state[inst_ids[k]];
         sc[k].delta_new = st.delta_new;
@@ -455,13 +485,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, co
             const double bsum = block_sum_acc(cg_dir_block(a, bi, c.iter == 0, c.beta));
             if (threadIdx.x == 0) a.partials[bi.gblk] = bsum;
         }
-        ok = grid_barrier(bar, bar + 32, gridDim.x, err);
+        ok = barrier_totals(a, inst_ids, n_inst, sc, bar, totals, err, tot);
         if (!ok) break;
-        for (int k = 0; k < n_inst; ++k) {
-            if (!sc[k].active) continue;
-            const double total = instance_total(a, a.inst[inst_ids[k]]);
-            if (threadIdx.x == 0) {  // finish<K_CG_DIR>
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < n_inst; ++k) {  // finish<K_CG_DIR>
                 PersistScalars& c = sc[k];
+                if (!c.active) continue;
+                const double total = tot[k];
                 c.dq = total;
                 if (!(total > 0.0) || !isfinite(total)) {
                     c.flags |= isfinite(total) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
@@ -470,8 +500,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, co
                     c.alpha = (float)(c.delta_new / total);
                 }
             }
-            __syncthreads();
         }
+        __syncthreads();
         // Update pass (k_cg_update).
         for (int32_t e = blockIdx.x; e < n_entries; e += gridDim.x) {
             const BlockInfo bi = a.blocks[e];
@@ -480,14 +510,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, co
             const double bsum = block_sum_acc(cg_update_block(a, bi, c.alpha));
             if (threadIdx.x == 0) a.partials[bi.gblk] = bsum;
         }
-        ok = grid_barrier(bar, bar + 32, gridDim.x, err);
+        ok = barrier_totals(a, inst_ids, n_inst, sc, bar, totals, err, tot);
         if (!ok) break;
-        for (int k = 0; k < n_inst; ++k) {
-            if (!sc[k].active) continue;
-            const InstParams& ip = a.inst[inst_ids[k]];
-            const double total = instance_total(a, ip);
-            if (threadIdx.x == 0) {  // finish<K_CG_UPDATE>
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < n_inst; ++k) {  // finish<K_CG_UPDATE>
                 PersistScalars& c = sc[k];
+                if (!c.active) continue;
+                const InstParams& ip = a.inst[inst_ids[k]];
+                const double total = tot[k];
                 const double old = c.delta_new;
                 c.delta_new = total;
                 c.beta = (float)(total / old);
@@ -499,8 +529,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, co
                     c.active = 0;
                 }
             }
-            __syncthreads();
         }
+        __syncthreads();
     }
     // The update of these cloths (k_integrate): per vertex, no barrier needed.
     if (ok) {

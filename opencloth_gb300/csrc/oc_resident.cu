@@ -22,31 +22,54 @@ namespace cgx = cooperative_groups;
 namespace oc {
 namespace {
 
-// FP64 sum over the CTA, then over the cluster (C CTAs), identical in every CTA.
-// slots[2] (double-buffered per call) and bcast live in shared memory.  Lane r of warp 0
-// reads CTA r's partial over distributed shared memory, so the C remote loads are in
-// flight together, and the lanes combine them with a fixed shuffle tree (absent ranks
-// are zero): every CTA runs the same tree on the same values.
-__device__ double cluster_sum(Acc part, int C, double* slots, double* bcast, int& phase) {
-    const double bs = block_sum_acc(part);
-    if (C == 1) {
-        if (threadIdx.x == 0) *bcast = bs;
-        __syncthreads();
-        return *bcast;
-    }
-    cgx::cluster_group cl = cgx::this_cluster();
-    double* slot = slots + (phase & 1);
-    ++phase;
-    if (threadIdx.x == 0) *slot = bs;
-    cl.sync();
-    if (threadIdx.x < 32) {
-        const int r = threadIdx.x;
-        double t = r < C ? *cl.map_shared_rank(slot, r) : 0.0;
-        t = warp_sum(t);
-        if (r == 0) *bcast = t;
-    }
+// Sum over the CTA, then over the cluster (C CTAs), carried as error-free float pairs
+// (Acc: the running sum and its exact rounding errors, about 48 significant bits) up to
+// the cluster total, which thread 0 turns into one FP64 value.  FP64 is slow on this GPU
+// and these reductions are the serial part of every CG iteration, so no level uses it.
+// The CTA's warps merge in a fixed tree in warp 0.  Each CTA then pushes its pair into
+// slot [rank] of every CTA of the cluster (lane r of warp 0 stores into CTA r's shared
+// memory), one cluster barrier makes the pushes visible, and every CTA merges its C local
+// slots in the same fixed tree (absent ranks are zero pairs), so all CTAs get identical
+// totals.  slots[2][16] is double-buffered per call: a buffer is written again only two
+// barriers after its last reads.  The result is valid in thread 0.
+__device__ __forceinline__ Acc shfl_acc(Acc v, int o) {
+    Acc u;
+    u.s = __shfl_down_sync(0xffffffffu, v.s, o);
+    u.c = __shfl_down_sync(0xffffffffu, v.c, o);
+    return u;
+}
+
+__device__ double cluster_sum(Acc part, int C, Acc (*slots)[kResidentMaxCluster], int& phase) {
+    __shared__ Acc warp_part[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part = acc_merge(part, shfl_acc(part, o));
+    __syncthreads();  // warp_part's previous readers are done
+    if (lane == 0) warp_part[w] = part;
     __syncthreads();
-    return *bcast;
+    Acc v = acc_zero();
+    if (w == 0) {
+        v = lane < nw ? warp_part[lane] : acc_zero();
+        for (int o = nw >> 1; o > 0; o >>= 1) v = acc_merge(v, shfl_acc(v, o));
+    }
+    if (C > 1) {
+        // Every thread of every CTA takes part in the cluster barrier.
+        cgx::cluster_group cl = cgx::this_cluster();
+        Acc* slot = slots[phase & 1];
+        if (w == 0) {
+            const unsigned me = cl.block_rank();
+            const Acc mine = make_acc(__shfl_sync(0xffffffffu, v.s, 0), __shfl_sync(0xffffffffu, v.c, 0));
+            if (lane < C) cl.map_shared_rank(slot, lane)[me] = mine;
+        }
+        cl.sync();
+        if (w == 0) {
+            v = lane < C ? slot[lane] : acc_zero();
+#pragma unroll
+            for (int o = kResidentMaxCluster >> 1; o > 0; o >>= 1) v = acc_merge(v, shfl_acc(v, o));
+        }
+    }
+    ++phase;
+    return (double)v.s + (double)v.c;
 }
 
 // Resident CTAs per SM the register budget is set for: 128-thread CTAs hold up to 512
@@ -60,8 +83,11 @@ constexpr int resident_min_blocks() {
 template <int T>
 __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const StepArgs a, const ResidentLaunch L) {
     extern __shared__ __align__(16) float smem[];
-    __shared__ double slots[2];
-    __shared__ double bcast;
+    __shared__ Acc slots[2][kResidentMaxCluster];
+    // The CG scalars live in thread 0 (FP64 is slow on this GPU: one thread does the
+    // divisions and tests); the other threads get alpha, beta and the go / stop decision.
+    __shared__ float s_alpha, s_beta;
+    __shared__ int s_go;
     const int C = L.cluster;
     const int rank = (C > 1) ? (int)cgx::this_cluster().block_rank() : 0;
     const int inst = L.inst_ids[blockIdx.x / C];
@@ -86,9 +112,8 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
 
     int phase = 0;
     Acc part;
-    double delta0;
-    uint32_t flags;
-    bool run;
+    double delta0 = 0.0, delta = 0.0, thresh = 0.0;  // thread 0's
+    uint32_t flags = 0u;                             // thread 0's
     if (L.fused) {
         // The assembly of these vertices (k_assemble / k_assemble_grid), into shared
         // memory; X and V are written at the end of this kernel, so they are read with
@@ -115,12 +140,15 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
         // delta0 and the decision to iterate, as the assembly's last-block epilogue takes
         // them (finish<K_ASSEMBLE>).  The cluster reduction also orders every CTA's reads
         // of X and V before any CTA's writes below.
-        delta0 = cluster_sum(part, C, slots, &bcast, phase);
-        flags = 0u;
-        run = (0 < ip.imax) && (delta0 > (double)ip.eps2 * delta0);
-        if (!isfinite(delta0)) {
-            flags |= OC_FLAG_NON_FINITE;
-            run = false;
+        const double total = cluster_sum(part, C, slots, phase);
+        if (threadIdx.x == 0) {
+            delta0 = total;
+            bool run = (0 < ip.imax) && (total > (double)ip.eps2 * total);
+            if (!isfinite(total)) {
+                flags |= OC_FLAG_NON_FINITE;
+                run = false;
+            }
+            s_go = run ? 1 : 0;
         }
     } else {
         // The CG state k_assemble left in the planes: A, x, r, d -> shared memory.
@@ -135,14 +163,19 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
                 sd[k][j] = a.d[k][g];
             }
         }
-        __syncthreads();
-        const InstState& st0 = a.state[inst];
-        delta0 = st0.delta0;
-        flags = st0.flags;
-        run = st0.active != 0;
+        if (threadIdx.x == 0) {
+            const InstState& st0 = a.state[inst];
+            delta0 = st0.delta0;
+            flags = st0.flags;
+            s_go = st0.active != 0 ? 1 : 0;
+        }
     }
-    double delta = delta0;
-    const double thresh = (double)ip.eps2 * delta0;
+    __syncthreads();
+    bool run = s_go != 0;
+    if (threadIdx.x == 0) {
+        delta = delta0;
+        thresh = (double)ip.eps2 * delta0;
+    }
     int it = 0;
     float beta = 0.0f;
     while (run) {
@@ -163,12 +196,19 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
             matvec(A, d0, d1, d2, q0, q1, q2);
             acc_add(part, d0 * q0 + d1 * q1 + d2 * q2);
         }
-        const double dq = cluster_sum(part, C, slots, &bcast, phase);
-        if (!(dq > 0.0) || !isfinite(dq)) {
-            flags |= isfinite(dq) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
-            break;
+        const double dq = cluster_sum(part, C, slots, phase);
+        if (threadIdx.x == 0) {
+            if (!(dq > 0.0) || !isfinite(dq)) {
+                flags |= isfinite(dq) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
+                s_go = 0;
+            } else {
+                s_alpha = (float)(delta / dq);
+                s_go = 1;
+            }
         }
-        const float alpha = (float)(delta / dq);
+        __syncthreads();
+        if (!s_go) break;
+        const float alpha = s_alpha;
         // x += alpha d; r -= alpha A d; r.r, IMP:322-325.
         part = acc_zero();
         for (int j = threadIdx.x; j < n_local; j += T) {
@@ -187,18 +227,25 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
             sr[2][j] = r2;
             acc_add(part, r0 * r0 + r1 * r1 + r2 * r2);
         }
-        const double old = delta;
-        delta = cluster_sum(part, C, slots, &bcast, phase);
-        beta = (float)(delta / old);
+        const double rr = cluster_sum(part, C, slots, phase);
         ++it;
-        if (!isfinite(delta)) {
-            flags |= OC_FLAG_NON_FINITE;
-            break;
+        if (threadIdx.x == 0) {
+            const double old = delta;
+            delta = rr;
+            s_beta = (float)(delta / old);
+            int go = 1;
+            if (!isfinite(delta)) {
+                flags |= OC_FLAG_NON_FINITE;
+                go = 0;
+            } else if (!(it < ip.imax && delta > thresh)) {
+                if (delta > thresh) flags |= OC_FLAG_NOT_CONVERGED;
+                go = 0;
+            }
+            s_go = go;
         }
-        if (!(it < ip.imax && delta > thresh)) {
-            if (delta > thresh) flags |= OC_FLAG_NOT_CONVERGED;
-            break;
-        }
+        __syncthreads();
+        beta = s_beta;
+        if (!s_go) break;
     }
     // V += dV dt; X += dt V; ground clamp (IMP:790-797), then the ellipsoid pass when
     // enabled; dV stays as the warm start.
