@@ -10,7 +10,10 @@
 // The solve is differentiated as an exact solve: one extra CG on the same symmetric A
 // gives lambda = A^-1 g_dV, then g_b = lambda and g_A = -lambda dV^T.  All sums are
 // gathers in a fixed order (spring-ordered incidences, and per vertex the list of the
-// vertices whose own spring touches it), so gradients are deterministic.
+// vertices whose own spring touches it), so gradients are deterministic.  This unit is
+// compiled with multiply-add contraction and approximate division and square root: the
+// gradients are checked against finite differences and an FP64 adjoint, not against the
+// reference's rounding sequence.
 #include <cuda_runtime.h>
 
 #include "oc_device.cuh"

@@ -57,6 +57,12 @@ struct oc_solver {
     int32_t n_asm_blocks = 0;
     BlockInfo* d_grid_blocks = nullptr;  // REFERENCE grid cloths on the stencil gather
     int32_t n_grid_blocks = 0;
+    // Grid cloths' stencil data on the host, to refit the parameter slots when
+    // oc_set_spring_params changes Ks or Kd, and each cloth's grid shape as detected
+    // ({0, 0}: not a grid).
+    std::vector<int32_t> h_st_data;
+    std::vector<float4> h_st_param;
+    std::vector<int2> grid_shape;
     BlockInfo* d_cpl_blocks = nullptr;
     int32_t n_cpl_blocks = 0;
     BlockInfo* d_upd_blocks = nullptr;
@@ -70,6 +76,11 @@ struct oc_solver {
     int persist_grid = 0;
     unsigned* d_bar = nullptr;  // grid barrier: arrivals [0], generation [32], totals [64]
     int* d_perr = nullptr;      // bit 0: a grid barrier gave up
+    // The adjoint solve (every cloth iterates) as one cooperative launch of k_cg_persist
+    // without the update, when the handle has few enough cloths.
+    bool adj_persist = false;
+    int32_t* d_adj_ids = nullptr;
+    int adj_persist_grid = 0;
     bool any_provot = false;  // some cloth has OC_PASS_PROVOT: k_provot follows the update
     bool any_passes = false;  // some cloth has a pass after the update
     // Resident buckets run concurrently: forked from the handle's stream onto these.
@@ -82,11 +93,15 @@ struct oc_solver {
         int32_t n_steps = 0, every = 0, n_ck = 0;
         float dt = 0.0f;
         float4 *ckX = nullptr, *ckV = nullptr, *segX = nullptr, *segV = nullptr, *finX = nullptr, *finV = nullptr;
-        float *ckx = nullptr, *segdV = nullptr, *finx = nullptr;
+        // segAx: per step of a segment, the system A (6 planes) and the solution dV (3
+        // planes) as the step left them (the A and x planes are contiguous).
+        float *ckx = nullptr, *segAx = nullptr, *finx = nullptr;
         float* planes = nullptr;  // gX 3, gV 3, gF 3, gOwn 6, gExt 3, dV 3
         float* gK = nullptr;      // gKs, gKd
-        cudaGraph_t graph = nullptr;
+        cudaGraph_t graph = nullptr;  // the adjoint solve as a WHILE loop (many cloths)
         cudaGraphExec_t exec = nullptr;
+        cudaGraphNode_t n_seed = nullptr;  // k_adj_seed: its arguments change every step
+        cudaGraphConditionalHandle handle = 0;
         float graph_dt = 0.0f;
         bool valid = false;
     } tape;
@@ -650,6 +665,8 @@ oc_status build_adjoint_graph(oc_solver* s, float dt) {
     kp.blockDim = dim3(256);
     kp.kernelParams = params_seed;
     OC_TRY(cudaGraphAddKernelNode(&n_seed, g, &n_reset, 1, &kp));
+    T.n_seed = n_seed;
+    T.handle = handle;
     cudaGraphNodeParams cp{};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = handle;
@@ -666,6 +683,105 @@ oc_status build_adjoint_graph(oc_solver* s, float dt) {
     OC_TRY(cudaGraphAddKernelNode(&n_upd, body, &n_dir, 1, &kp));
     OC_TRY(cudaGraphInstantiate(&T.exec, g, 0));
     T.graph_dt = dt;
+    return OC_OK;
+}
+
+// The CSR and stencil assembly tables from the full block table, after a cloth moved
+// between the two gathers: REFERENCE cloths that the step assembles (not a resident cloth
+// that the fused resident kernel assembles), by their current grid_cols.
+oc_status rebuild_assembly_tables(oc_solver* s) {
+    std::vector<BlockInfo> all((size_t)s->n_blocks), asm_ref, grid;
+    OC_TRY(cudaMemcpy(all.data(), s->args.blocks, sizeof(BlockInfo) * all.size(), cudaMemcpyDeviceToHost));
+    for (const BlockInfo& b : all) {
+        const InstParams& ip = s->inst_host[(size_t)b.inst];
+        if (ip.coupled || (s->resident[(size_t)b.inst] && s->resident_fused)) continue;
+        (ip.grid_cols > 0 ? grid : asm_ref).push_back(b);
+    }
+    s->n_asm_blocks = (int32_t)asm_ref.size();
+    OC_TRY(upload(s, &s->d_asm_blocks, asm_ref));
+    s->n_grid_blocks = (int32_t)grid.size();
+    OC_TRY(upload(s, &s->d_grid_blocks, grid));
+    return OC_OK;
+}
+
+// After new per-spring Ks / Kd: a grid cloth reads them from its stencil's parameter
+// slots, so either every spring of each slot still shares one (Ks, Kd) and the slots take
+// the new values, or the cloth moves to the CSR gather (which reads the records).  A cloth
+// whose values fit again moves back.  Either move rebuilds the tables and the graph.
+oc_status refit_stencils(oc_solver* s) {
+    bool any = false;
+    for (const int2& g : s->grid_shape) any |= g.x > 0;
+    if (!any) return OC_OK;
+    std::vector<int32_t> rowptr((size_t)s->nv + 1), sid((size_t)s->n_inc);
+    std::vector<float> ks((size_t)s->ns), kd((size_t)s->ns);
+    OC_TRY(cudaMemcpy(rowptr.data(), s->args.rowptr, sizeof(int32_t) * rowptr.size(), cudaMemcpyDeviceToHost));
+    OC_TRY(cudaMemcpy(sid.data(), s->adj.inc_sid, sizeof(int32_t) * sid.size(), cudaMemcpyDeviceToHost));
+    OC_TRY(cudaMemcpy(ks.data(), s->d_ks, sizeof(float) * ks.size(), cudaMemcpyDeviceToHost));
+    OC_TRY(cudaMemcpy(kd.data(), s->d_kd, sizeof(float) * kd.size(), cudaMemcpyDeviceToHost));
+    bool moved = false, slots_changed = false;
+    for (int32_t k = 0; k < s->n_inst; ++k) {
+        const int2 shape = s->grid_shape[(size_t)k];
+        if (shape.x <= 0) continue;
+        InstParams& ip = s->inst_host[(size_t)k];
+        const int32_t* st = s->h_st_data.data() + ip.st_off;
+        int32_t slot_ks[kStencilSlots], slot_kd[kStencilSlots];
+        bool seen[kStencilSlots] = {false};
+        bool fits = true;
+        const int64_t vo = s->v_off[(size_t)k];
+        for (int32_t l = 0; l < ip.nv && fits; ++l) {
+            const int cl = stencil_class_1d(l / shape.x, shape.y) * 6 + stencil_class_1d(l % shape.x, shape.x);
+            const int32_t e0 = st[cl], e1 = st[cl + 1], k0 = rowptr[(size_t)(vo + l)];
+            for (int32_t e = e0; e < e1 && fits; ++e) {
+                const int q = st[e] >> 7;
+                const int32_t sp = sid[(size_t)(k0 + (e - e0))];
+                int32_t bk, bd;
+                std::memcpy(&bk, &ks[(size_t)sp], 4);
+                std::memcpy(&bd, &kd[(size_t)sp], 4);
+                if (!seen[q]) {
+                    seen[q] = true;
+                    slot_ks[q] = bk;
+                    slot_kd[q] = bd;
+                } else if (slot_ks[q] != bk || slot_kd[q] != bd) {
+                    fits = false;
+                }
+            }
+        }
+        if (fits)
+            for (int q = 0; q < kStencilSlots; ++q) {
+                if (!seen[q]) continue;
+                float4& f = s->h_st_param[(size_t)(ip.st_par + q)];
+                int32_t ok_, od_;
+                std::memcpy(&ok_, &f.y, 4);
+                std::memcpy(&od_, &f.z, 4);
+                if (ok_ != slot_ks[q] || od_ != slot_kd[q]) {
+                    std::memcpy(&f.y, &slot_ks[q], 4);
+                    std::memcpy(&f.z, &slot_kd[q], 4);
+                    slots_changed = true;
+                }
+            }
+        const int32_t cols = fits ? shape.x : 0;
+        if (cols != ip.grid_cols) {
+            ip.grid_cols = cols;
+            ip.grid_rows = fits ? shape.y : 0;
+            moved = true;
+        }
+    }
+    if (slots_changed)
+        OC_TRY(cudaMemcpy(const_cast<float4*>(s->args.st_param), s->h_st_param.data(),
+                          sizeof(float4) * s->h_st_param.size(), cudaMemcpyHostToDevice));
+    if (moved) {
+        OC_TRY(cudaMemcpy(const_cast<InstParams*>(s->args.inst), s->inst_host.data(),
+                          sizeof(InstParams) * s->inst_host.size(), cudaMemcpyHostToDevice));
+        if (oc_status r = rebuild_assembly_tables(s)) return r;
+        if (s->exec) {
+            cudaGraphExecDestroy(s->exec);
+            s->exec = nullptr;
+        }
+        if (s->graph) {
+            cudaGraphDestroy(s->graph);
+            s->graph = nullptr;
+        }
+    }
     return OC_OK;
 }
 
@@ -801,6 +917,10 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     a.rowptr = rowptr;
     a.inc = inc;
     {
+        s->h_st_data = P.st_data;
+        s->h_st_param = P.st_param;
+        s->grid_shape.resize((size_t)P.n_inst);
+        for (int32_t k = 0; k < P.n_inst; ++k) s->grid_shape[(size_t)k] = make_int2(P.inst[k].grid_cols, P.inst[k].grid_rows);
         int32_t* d_st = nullptr;
         OC_CREATE_TRY(upload(s, &d_st, P.st_data));
         a.st_data = d_st;
@@ -986,6 +1106,21 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
             OC_CREATE_TRY(cudaMemset(s->d_bar, 0, 128 * sizeof(unsigned)));
             OC_CREATE_TRY(dalloc(s, &s->d_perr, 1));
             OC_CREATE_TRY(cudaMemset(s->d_perr, 0, sizeof(int)));
+        }
+        // The adjoint solve runs every cloth's CG: one cooperative launch without the
+        // update when the handle holds at most persist_max_instances() cloths.
+        if (allowed && coop && per_sm > 0 && P.n_inst <= persist_max_instances() && !P.any_coupled) {
+            s->adj_persist = true;
+            std::vector<int32_t> all((size_t)P.n_inst);
+            for (int32_t k = 0; k < P.n_inst; ++k) all[(size_t)k] = k;
+            OC_CREATE_TRY(upload(s, &s->d_adj_ids, all));
+            s->adj_persist_grid = std::min(per_sm * n_sm, std::max(1, s->n_blocks));
+            if (!s->d_bar) {
+                OC_CREATE_TRY(dalloc(s, &s->d_bar, 128));
+                OC_CREATE_TRY(cudaMemset(s->d_bar, 0, 128 * sizeof(unsigned)));
+                OC_CREATE_TRY(dalloc(s, &s->d_perr, 1));
+                OC_CREATE_TRY(cudaMemset(s->d_perr, 0, sizeof(int)));
+            }
         }
     }
     OC_CREATE_TRY(dalloc(s, &a.unconverged, 1));
@@ -1360,7 +1495,7 @@ oc_status oc_set_spring_params(oc_solver* s, const float* ks, const float* kd) {
     OC_TRY(launch_set_spring_params(s->args, s->adj, s->d_ks, s->d_kd, s->n_inc, s->nv, s->stream));
     OC_TRY(cudaStreamSynchronize(s->stream));
     s->tape.valid = false;
-    return OC_OK;
+    return refit_stencils(s);
 }
 
 oc_status oc_set_ext_force(oc_solver* s, const float* ext) {
@@ -1405,11 +1540,12 @@ oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t check
     OC_TRY(cudaSetDevice(s->device));
     auto& T = s->tape;
     const size_t state_bytes = 2 * sizeof(float4) * (size_t)s->nv + 3 * s->stride * sizeof(float);
+    const size_t seg_bytes = 2 * sizeof(float4) * (size_t)s->nv + 9 * s->stride * sizeof(float);
     int32_t every = checkpoint_every;
     if (every == 0) every = std::max(1, (int32_t)std::ceil(std::sqrt((double)n_steps)));
     every = std::min(every, n_steps);
     const int32_t n_ck = (n_steps + every - 1) / every;
-    const double need = (double)state_bytes * (double)(n_ck + every + 1);
+    const double need = (double)state_bytes * (double)(n_ck + 1) + (double)seg_bytes * (double)every;
     if (budget_bytes > 0 && need > (double)budget_bytes)
         return fail(s, OC_ERR_OUT_OF_MEMORY, "oc_tape_forward: checkpoints need " + std::to_string(need) +
                                                  " bytes, above the budget");
@@ -1422,7 +1558,7 @@ oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t check
         OC_TRY(dalloc(s, &pf, 3 * s->stride * n_ck)); T.ckx = pf;
         OC_TRY(dalloc(s, &p4, (size_t)s->nv * every)); T.segX = p4;
         OC_TRY(dalloc(s, &p4, (size_t)s->nv * every)); T.segV = p4;
-        OC_TRY(dalloc(s, &pf, 3 * s->stride * every)); T.segdV = pf;
+        OC_TRY(dalloc(s, &pf, 9 * s->stride * every)); T.segAx = pf;
         if (!T.finX) {
             OC_TRY(dalloc(s, &p4, (size_t)s->nv)); T.finX = p4;
             OC_TRY(dalloc(s, &p4, (size_t)s->nv)); T.finV = p4;
@@ -1482,7 +1618,7 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
         OC_TRY(cudaMemcpyAsync(s->stage + n3, dL_dV, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
         OC_TRY(launch_state_in(up, nullptr, nullptr, s->stage + n3, s->nv, s->d_err, s->stream));
     }
-    if (!T.exec || T.graph_dt != T.dt) {
+    if (!s->adj_persist && (!T.exec || T.graph_dt != T.dt)) {
         oc_status r = build_adjoint_graph(s, T.dt);
         if (r != OC_OK) return r;
     }
@@ -1491,35 +1627,78 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
     a.blk_base = 0;
     a.use_cond = 0;
     a.all_streamed = 1;
+    // A step's system A comes from the tape, where the recompute left it, unless a
+    // resident cloth assembles in shared memory only (the fused resident kernel): then the
+    // CSR assembly rebuilds every cloth's A.
+    const bool split_asm = !(s->resident_fused && !s->buckets.empty());
+    const bool taped_A = split_asm;
+    auto assemble = [&](const StepArgs& b) -> cudaError_t {
+        cudaError_t e = cudaSuccess;
+        if (!split_asm) return launch_kernel(K_ASSEMBLE, b, s->n_blocks, s->stream);
+        StepArgs ba = b, bg = b;
+        ba.blocks = s->d_asm_blocks;
+        bg.blocks = s->d_grid_blocks;
+        if (s->n_asm_blocks > 0) e = launch_kernel(K_ASSEMBLE, ba, s->n_asm_blocks, s->stream);
+        if (e == cudaSuccess && s->n_grid_blocks > 0) e = launch_kernel(K_ASSEMBLE_GRID, bg, s->n_grid_blocks, s->stream);
+        return e;
+    };
+    const size_t nAx = 9 * st;
+    float* live_Ax = s->args.A[0];  // A (6 planes) then x (3 planes)
     for (int32_t c = T.n_ck - 1; c >= 0; --c) {
-        const int32_t t0 = c * T.every, t1 = std::min(T.n_steps, t0 + T.every);
+        const int32_t t0 = c * T.every, t1 = std::min(T.n_steps, t0 + T.every), len = t1 - t0;
         oc_status r = copy_state(s, s->args.X, s->args.V, xplanes(s), T.ckX + (size_t)c * s->nv,
                                  T.ckV + (size_t)c * s->nv, T.ckx + 3 * st * c);
         if (r != OC_OK) return r;
-        for (int32_t t = t0; t < t1; ++t) {  // recompute the segment, keeping every state
-            const int32_t q = t - t0;
-            if ((r = copy_state(s, T.segX + (size_t)q * s->nv, T.segV + (size_t)q * s->nv, nullptr, s->args.X,
-                                s->args.V, nullptr)) != OC_OK)
-                return r;
+        // Recompute the segment, keeping every step's input state and solution.
+        OC_TRY(launch_snapshot(s->args.X, s->args.V, T.segX, T.segV, nullptr, nullptr, s->nv, 0, s->stream));
+        for (int32_t q = 0; q < len; ++q) {
             if ((r = oc_step(s, T.dt, 1)) != OC_OK) return r;
-            OC_TRY(cudaMemcpyAsync(T.segdV + 3 * st * q, xplanes(s), 3 * st * sizeof(float), cudaMemcpyDeviceToDevice,
-                                   s->stream));
+            const bool more = q + 1 < len;
+            OC_TRY(launch_snapshot(s->args.X, s->args.V, more ? T.segX + (size_t)(q + 1) * s->nv : nullptr,
+                                   more ? T.segV + (size_t)(q + 1) * s->nv : nullptr, live_Ax, T.segAx + nAx * q,
+                                   s->nv, (int64_t)nAx, s->stream));
         }
-        for (int32_t t = t1 - 1; t >= t0; --t) {  // and walk it backwards
-            const int32_t q = t - t0;
-            if ((r = copy_state(s, s->args.X, s->args.V, nullptr, T.segX + (size_t)q * s->nv,
-                                T.segV + (size_t)q * s->nv, nullptr)) != OC_OK)
-                return r;
-            OC_TRY(cudaMemcpyAsync(const_cast<float*>(j.dV[0]), T.segdV + 3 * st * q, 3 * st * sizeof(float),
-                                   cudaMemcpyDeviceToDevice, s->stream));
-            OC_TRY(launch_kernel(K_ASSEMBLE, a, s->n_blocks, s->stream));  // A of this step
-            OC_TRY(cudaGraphLaunch(T.exec, s->stream));                    // lambda = A^-1 g_dV
-            OC_TRY(launch_adjoint(1, a, j, s->n_blocks, s->stream));
-            OC_TRY(launch_adjoint(2, a, j, s->n_blocks, s->stream));
+        // And walk it backwards: the kernels read the step's state in place in the tape.
+        for (int32_t q = len - 1; q >= 0; --q) {
+            StepArgs b = a;
+            b.X = T.segX + (size_t)q * s->nv;
+            b.V = T.segV + (size_t)q * s->nv;
+            AdjArgs jj = j;
+            float* slot = T.segAx + nAx * q;
+            for (int k = 0; k < 3; ++k) jj.dV[k] = slot + (6 + k) * st;
+            if (!taped_A)
+                OC_TRY(assemble(b));  // A of this step, rebuilt
+            else if (s->adj_persist)
+                for (int k = 0; k < 6; ++k) b.A[k] = slot + k * st;  // read in place
+            else  // the WHILE graph's nodes read the handle's A planes
+                OC_TRY(cudaMemcpyAsync(live_Ax, slot, 6 * st * sizeof(float), cudaMemcpyDeviceToDevice, s->stream));
+            if (s->adj_persist) {  // lambda = A^-1 g_dV: seed, then one cooperative launch
+                OC_TRY(launch_adjoint(0, b, jj, s->n_blocks, s->stream));
+                OC_TRY(cudaMemsetAsync(s->d_bar, 0, sizeof(unsigned), s->stream));
+                StepArgs pa = b;
+                pa.cg_only = 1;
+                OC_TRY(launch_cg_persist(pa, s->d_adj_ids, s->n_inst, s->n_blocks, s->adj_persist_grid, s->d_bar,
+                                         s->d_perr, s->stream));
+            } else {  // the WHILE-loop graph, its seed node pointed at this step
+                StepArgs bs = b;
+                bs.use_cond = 1;
+                bs.cond = (unsigned long long)T.handle;
+                void* params_seed[] = {&bs, &jj};
+                cudaKernelNodeParams kp{};
+                kp.func = const_cast<void*>(adjoint_seed_fn());
+                kp.gridDim = dim3((unsigned)s->n_blocks);
+                kp.blockDim = dim3(256);
+                kp.kernelParams = params_seed;
+                OC_TRY(cudaGraphExecKernelNodeSetParams(T.exec, T.n_seed, &kp));
+                OC_TRY(cudaGraphLaunch(T.exec, s->stream));
+            }
+            OC_TRY(launch_adjoint(1, b, jj, s->n_blocks, s->stream));
+            OC_TRY(launch_adjoint(2, b, jj, s->n_blocks, s->stream));
         }
     }
     oc_status r = copy_state(s, s->args.X, s->args.V, xplanes(s), T.finX, T.finV, T.finx);
     if (r != OC_OK) return r;
+    if ((r = check_device_error(s)) != OC_OK) return r;
     // Gradients out (planes -> packed triples through the state download kernel).
     StepArgs dn = s->args;
     auto planes_out = [&](float* const* pl, float* host) -> oc_status {
@@ -1544,7 +1723,8 @@ oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* t
     const auto& T = s->tape;
     const size_t state_bytes = 2 * sizeof(float4) * (size_t)s->nv + 3 * s->stride * sizeof(float);
     if (checkpoint_every) *checkpoint_every = T.every;
-    if (tape_bytes) *tape_bytes = (int64_t)(state_bytes * (size_t)(T.n_ck + T.every + 1));
+    const size_t seg_bytes = 2 * sizeof(float4) * (size_t)s->nv + 9 * s->stride * sizeof(float);
+    if (tape_bytes) *tape_bytes = (int64_t)(state_bytes * (size_t)(T.n_ck + 1) + seg_bytes * (size_t)T.every);
     return OC_OK;
 }
 

@@ -82,6 +82,7 @@ struct StepArgs {
     int32_t use_cond;        // 1: set the graph WHILE condition
     unsigned long long cond; // cudaGraphConditionalHandle
     int32_t all_streamed;    // 1: every cloth's CG runs in the streamed loop (adjoint solves)
+    int32_t cg_only;         // k_cg_persist: 1 = the CG alone, no update (adjoint solves)
     float* dbg_F;            // optional debug outputs (float triples) or nullptr
     float* dbg_A9;
     float* dbg_b;
@@ -122,6 +123,10 @@ struct AdjArgs {
 };
 
 cudaError_t launch_adjoint(int which, const StepArgs& a, const AdjArgs& j, int nblocks, cudaStream_t stream);
+// Tape snapshots: X, V into dX, dV (nv float4 each, skipped when dX is null) and nx floats
+// of x into dx (skipped when dx is null).
+cudaError_t launch_snapshot(const float4* X, const float4* V, float4* dX, float4* dV, const float* x, float* dx,
+                            int64_t nv, int64_t nx, cudaStream_t stream);
 const void* adjoint_seed_fn();
 cudaError_t launch_set_spring_params(const StepArgs& a, const AdjArgs& j, const float* ks, const float* kd,
                                      int64_t n_rec, int64_t nv, cudaStream_t stream);

@@ -22,6 +22,8 @@
 // an instance to finish (atomic ticket) sums that instance's partials in a fixed order
 // and updates the instance's CG scalars.  The last block of the whole grid sets the
 // CUDA-graph WHILE condition to "some instance still iterating".
+#include <algorithm>
+
 #include <cuda_runtime.h>
 
 #include "oc_device.cuh"
@@ -532,8 +534,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, co
         }
         __syncthreads();
     }
-    // The update of these cloths (k_integrate): per vertex, no barrier needed.
-    if (ok) {
+    // The update of these cloths (k_integrate): per vertex, no barrier needed.  An
+    // adjoint solve (cg_only) stops at the solution.
+    if (ok && !a.cg_only) {
         for (int32_t e = blockIdx.x; e < n_entries; e += gridDim.x) {
             const BlockInfo bi = a.blocks[e];
             const InstParams& ip = a.inst[bi.inst];
@@ -558,6 +561,19 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, co
             st.flags = c.flags;
         }
     }
+}
+
+__global__ void k_snapshot(const float4* X, const float4* V, float4* dX, float4* dV, const float* x, float* dx,
+                           int64_t nv, int64_t nx) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (dX)
+        for (int64_t g = t0; g < nv; g += stride) {
+            dX[g] = X[g];
+            dV[g] = V[g];
+        }
+    if (dx)
+        for (int64_t k = t0; k < nx; k += stride) dx[k] = x[k];
 }
 
 __global__ void __launch_bounds__(kThreads) k_integrate(const StepArgs a) {
@@ -819,6 +835,15 @@ int persist_blocks_per_sm() {
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cg_persist, kThreads, 0) != cudaSuccess) return 0;
     return n;
+}
+
+cudaError_t launch_snapshot(const float4* X, const float4* V, float4* dX, float4* dV, const float* x, float* dx,
+                            int64_t nv, int64_t nx, cudaStream_t stream) {
+    const int64_t n = std::max(dX ? nv : 0, dx ? nx : 0);
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<int64_t>((n + kThreads - 1) / kThreads, 152 * 8);
+    k_snapshot<<<blocks, kThreads, 0, stream>>>(X, V, dX, dV, x, dx, nv, nx);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_cg_persist(const StepArgs& a, const int32_t* inst_ids, int32_t n_inst, int32_t n_entries,

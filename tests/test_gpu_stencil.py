@@ -87,3 +87,52 @@ def test_coupled_grid_unaffected():
     b, _ = run(d, X, np.zeros_like(X), 5, False)
     for x, y in zip(a, b):
         assert same_bits(x, y)
+
+
+@pytest.mark.parametrize("executor", ["streamed", "resident"])
+def test_spring_params_refit_the_stencil(executor):
+    """oc_set_spring_params on grid cloths: Ks / Kd scaled per spring type still fit the
+    stencil's parameter slots (the slots take the new values); per-spring values move the
+    cloth to the incidence gather; the original values move it back.  Each state steps
+    exactly (bit for bit) like a handle created with those parameters."""
+    rng = np.random.default_rng(8)
+    descs, Xs, Vs = [], [], []
+    for cols, rows in ((19, 19), (26, 11)):
+        X, sp = grid_cloth(cols, rows, ks=(50.75, 40.0, 30.0), kd=(-0.25, -0.2, -0.1), jitter=1e-3,
+                           seed=cols + rows)
+        V = rng.normal(0.0, 0.02, X.shape).astype(np.float32)
+        V[[0, cols - 1]] = 0.0
+        descs.append(ClothDesc(n_vertices=cols * rows, springs=sp, pinned=np.array([0, cols - 1], np.int32),
+                               cg_max_iter=40, cg_tol=1e-5))
+        Xs.append(X)
+        Vs.append(V)
+    X, V = np.concatenate(Xs), np.concatenate(Vs)
+    ks0 = np.concatenate([d.springs["ks"] for d in descs])
+    kd0 = np.concatenate([d.springs["kd"] for d in descs])
+    scaled = (ks0 * np.float32(1.5)).astype(np.float32)
+    per_spring = (ks0 * np.exp(rng.normal(0.0, 0.1, ks0.size))).astype(np.float32)
+
+    def fresh(ks, kd):
+        out, o = [], 0
+        for d in descs:
+            sp = d.springs.copy()
+            n = len(sp)
+            sp["ks"], sp["kd"] = ks[o:o + n], kd[o:o + n]
+            o += n
+            out.append(ClothDesc(n_vertices=d.n_vertices, springs=sp, pinned=d.pinned, cg_max_iter=40, cg_tol=1e-5))
+        with ClothSolver(out, executor=executor) as s:
+            s.set_state(X, V)
+            s.step(DT, 6)
+            return s.get_state(), [k != (0, 0) for k in describe(out)]
+
+    with ClothSolver(descs, executor=executor) as s:
+        for ks, kd, stencil in ((scaled, kd0 * np.float32(0.5), True), (per_spring, kd0, False), (ks0, kd0, True)):
+            kd = kd.astype(np.float32)
+            s.set_spring_params(ks=ks, kd=kd)
+            s.set_state(X, V, np.zeros_like(X))
+            s.step(DT, 6)
+            got = s.get_state()
+            want, kinds = fresh(ks, kd)
+            assert all(k == stencil for k in kinds)
+            for x, y in zip(got, want):
+                assert same_bits(x, y)
