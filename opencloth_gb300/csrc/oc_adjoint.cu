@@ -205,53 +205,87 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_vertex(const StepArgs a, co
 
 // Per vertex v: every incident spring's force adjoint, in spring-id order (the spring's
 // p1 side also adds to Ks_s, Kd_s), then the own-spring Jacobian terms of the vertices
-// whose spring touches v.
-__global__ void __launch_bounds__(kAdjThreads) k_adj_springs(const StepArgs a, const AdjArgs j) {
+// whose spring touches v.  The incidences are taken kAdjAhead at a time: their records,
+// then the neighbours' states and gradient entries, are all in flight before the first
+// is used (a serial walk waits on two dependent loads per incidence).  A spring's Ks / Kd
+// gradient is written only by its p1 vertex, so its old value can be fetched early.
+constexpr int kAdjAhead = 4;
+
+__global__ void __launch_bounds__(kAdjThreads, 2) k_adj_springs(const StepArgs a, const AdjArgs j) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
+    const float4* __restrict__ X = a.X;
+    const float4* __restrict__ V = a.V;
+    const int4* __restrict__ inc = a.inc;
+    const int32_t* __restrict__ isid = j.inc_sid;
+    const float* __restrict__ gF0 = j.gF[0];
+    const float* __restrict__ gF1 = j.gF[1];
+    const float* __restrict__ gF2 = j.gF[2];
     for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
-        const float4 Xg = a.X[g], Vg = a.V[g];
+        const float4 Xg = __ldg(X + g), Vg = __ldg(V + g);
         const bool pin_g = Vg.w != 0.0f;
-        const float gFg[3] = {j.gF[0][g], j.gF[1][g], j.gF[2][g]};
+        const float gFg[3] = {__ldg(gF0 + g), __ldg(gF1 + g), __ldg(gF2 + g)};
         float gx[3] = {j.gX[0][g], j.gX[1][g], j.gX[2][g]};
         float gv[3] = {j.gV[0][g], j.gV[1][g], j.gV[2][g]};
-        const int32_t k0 = a.rowptr[g], k1 = a.rowptr[g + 1];
-        for (int32_t k = k0; k < k1; ++k) {
-            const int4 rec = a.inc[k];
-            const bool as_p2 = rec.x < 0;
-            const int32_t o = rec.x & 0x7fffffff;
-            const float4 Xo = a.X[o], Vo = a.V[o];
-            const bool pin_o = Vo.w != 0.0f;
-            const float gFo[3] = {j.gF[0][o], j.gF[1][o], j.gF[2][o]};
-            // g_f = [p1 free] gF[p1] - [p2 free] gF[p2]
-            float gf[3];
+        const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
+        for (int32_t kb = k0; kb < k1; kb += kAdjAhead) {
+            int4 rec[kAdjAhead];
+            int32_t sid[kAdjAhead];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float g1 = as_p2 ? (pin_o ? 0.0f : gFo[c]) : (pin_g ? 0.0f : gFg[c]);
-                const float g2 = as_p2 ? (pin_g ? 0.0f : gFg[c]) : (pin_o ? 0.0f : gFo[c]);
-                gf[c] = g1 - g2;
+            for (int u = 0; u < kAdjAhead; ++u) {
+                const bool in = kb + u < k1;
+                rec[u] = in ? __ldg(inc + kb + u) : make_int4((int)g, 0, 0, 0);
+                sid[u] = in ? __ldg(isid + kb + u) : 0;
             }
-            const float rest = __int_as_float(rec.y), ks = __int_as_float(rec.z), kd = __int_as_float(rec.w);
-            float gdP[3], gdV[3], gks, gkd;
-            if (as_p2)
-                spring_force_adj(Xo, Xg, Vo, Vg, rest, ks, kd, gf, gdP, gdV, gks, gkd);
-            else
-                spring_force_adj(Xg, Xo, Vg, Vo, rest, ks, kd, gf, gdP, gdV, gks, gkd);
-            const float sgn = as_p2 ? -1.0f : 1.0f;
+            float4 Xo[kAdjAhead], Vo[kAdjAhead];
+            float gFo[kAdjAhead][3], gk_old[kAdjAhead], gd_old[kAdjAhead];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                gx[c] += sgn * gdP[c];
-                gv[c] += sgn * gdV[c];
+            for (int u = 0; u < kAdjAhead; ++u) {
+                const int32_t o = rec[u].x & 0x7fffffff;
+                Xo[u] = __ldg(X + o);
+                Vo[u] = __ldg(V + o);
+                gFo[u][0] = __ldg(gF0 + o);
+                gFo[u][1] = __ldg(gF1 + o);
+                gFo[u][2] = __ldg(gF2 + o);
+                const bool p1 = kb + u < k1 && rec[u].x >= 0;
+                gk_old[u] = p1 ? j.gKs[sid[u]] : 0.0f;
+                gd_old[u] = p1 ? j.gKd[sid[u]] : 0.0f;
             }
-            if (!as_p2) {
-                const int32_t sid = j.inc_sid[k];
-                j.gKs[sid] += gks;
-                j.gKd[sid] += gkd;
+#pragma unroll
+            for (int u = 0; u < kAdjAhead; ++u) {
+                if (kb + u >= k1) break;
+                const bool as_p2 = rec[u].x < 0;
+                const bool pin_o = Vo[u].w != 0.0f;
+                // g_f = [p1 free] gF[p1] - [p2 free] gF[p2]
+                float gf[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float g1 = as_p2 ? (pin_o ? 0.0f : gFo[u][c]) : (pin_g ? 0.0f : gFg[c]);
+                    const float g2 = as_p2 ? (pin_g ? 0.0f : gFg[c]) : (pin_o ? 0.0f : gFo[u][c]);
+                    gf[c] = g1 - g2;
+                }
+                const float rest = __int_as_float(rec[u].y), ks = __int_as_float(rec[u].z),
+                            kd = __int_as_float(rec[u].w);
+                float gdP[3], gdV[3], gks, gkd;
+                if (as_p2)
+                    spring_force_adj(Xo[u], Xg, Vo[u], Vg, rest, ks, kd, gf, gdP, gdV, gks, gkd);
+                else
+                    spring_force_adj(Xg, Xo[u], Vg, Vo[u], rest, ks, kd, gf, gdP, gdV, gks, gkd);
+                const float sgn = as_p2 ? -1.0f : 1.0f;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    gx[c] += sgn * gdP[c];
+                    gv[c] += sgn * gdV[c];
+                }
+                if (!as_p2) {
+                    j.gKs[sid[u]] = gk_old[u] + gks;
+                    j.gKd[sid[u]] = gd_old[u] + gkd;
+                }
             }
         }
-        const int32_t o0 = j.own_rowptr[g], o1 = j.own_rowptr[g + 1];
+        const int32_t o0 = __ldg(j.own_rowptr + g), o1 = __ldg(j.own_rowptr + g + 1);
         for (int32_t k = o0; k < o1; ++k) {
-            const int32_t e = j.own_ent[k];
+            const int32_t e = __ldg(j.own_ent + k);
             const int32_t i = e & 0x7fffffff;
             const float sgn = e < 0 ? -1.0f : 1.0f;
 #pragma unroll
