@@ -202,7 +202,8 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
     for (int32_t k = 0; k < s->n_inst; ++k) {
         const double nv = (double)s->inst_host[k].nv, ns = (double)s->ns_inst[k];
         const InstState& st = s->h_state[k];
-        const bool fused = s->resident[k] && s->resident_fused;  // assembled by k_resident
+        // Assembled by k_resident (fused) or by the COUPLED kernels: no assembly bytes here.
+        const bool fused = (s->resident[k] && s->resident_fused) || s->inst_host[k].coupled;
         if (!fused && s->inst_host[k].grid_cols > 0)  // no incidence records, no row pointer
             t->bytes[K_ASSEMBLE_GRID] +=              // unless rest lengths are per incidence
                 116.0 * nv + (s->inst_host[k].st_rest ? 4.0 * nv + 8.0 * ns : 0.0);
@@ -214,7 +215,6 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
             // k_cpl_assemble 112 B + 72 B per spring (record in, block out at both ends);
             // k_cpl_dir 33 B (first pass) or 45 B plus 48 B per spring (other vertex and
             // block at both ends); k_cpl_update 120 B (first) or 132 B; k_integrate 76 B.
-            t->bytes[K_ASSEMBLE] -= 120.0 * nv + 32.0 * ns;
             t->bytes[K_CPL_ASSEMBLE] += 112.0 * nv + 72.0 * ns;
             const double it = (double)st.iter;
             double dirs = it > 0 ? 33.0 * nv + 45.0 * nv * (it - 1.0) + 48.0 * ns * it : 0.0;
