@@ -581,7 +581,8 @@ bool resident_shape(int nv, int max_vertices, int* threads, int* cluster, int* v
     int base = kResidentDefaultVcta, thr = 256;
     if (const char* e = std::getenv("OC_RESIDENT_SHAPE")) {
         int v = 0, t = 0;
-        if (std::sscanf(e, "%d:%d", &v, &t) == 2 && v >= 128 && v <= kResidentMaxVcta && (t == 128 || t == 256 || t == 512)) {
+        if (std::sscanf(e, "%d:%d", &v, &t) == 2 && v >= 128 && v <= kResidentMaxVcta && v <= kResidentVpt * t &&
+            (t == 128 || t == 256 || t == 512)) {
             base = v;
             thr = t;
         }

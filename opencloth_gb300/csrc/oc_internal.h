@@ -187,6 +187,7 @@ struct ResidentLaunch {
     int32_t fused;  // 1: the kernel assembles its cloth's system itself (no k_assemble pass)
 };
 constexpr int kResidentMaxVcta = 2048;
+constexpr int kResidentVpt = 4;  // vertices per thread of the resident kernel: vcta <= 4 x threads
 constexpr int kResidentMaxCluster = 16;
 size_t resident_smem_bytes(int vcta);
 cudaError_t prepare_resident();  // function attributes (once per device)

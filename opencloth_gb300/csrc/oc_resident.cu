@@ -73,14 +73,14 @@ __device__ double cluster_sum(Acc part, int C, Acc (*slots)[kResidentMaxCluster]
 }
 
 // Resident CTAs per SM the register budget is set for: 128-thread CTAs hold up to 512
-// vertices, 256-thread CTAs 256 to 1024 (3 to 15 CTAs by shared memory), 512-thread CTAs
-// 2048 (one).
+// vertices, 256-thread CTAs 256 to 1024, 512-thread CTAs 2048 (shared memory holds only
+// A, 24 bytes per vertex; x, r and d are in registers).
 template <int T>
 constexpr int resident_min_blocks() {
     return T == 128 ? 8 : (T == 256 ? 4 : 1);
 }
 
-template <int T>
+template <int T, bool FUSED>
 __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const StepArgs a, const ResidentLaunch L) {
     extern __shared__ __align__(16) float smem[];
     __shared__ Acc slots[2][kResidentMaxCluster];
@@ -98,28 +98,28 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
     const int64_t base = ip.v_off + lb;
     const int cap = L.vcta;
     float* sA[6];
-    float* sx[3];
-    float* sr[3];
-    float* sd[3];
 #pragma unroll
     for (int k = 0; k < 6; ++k) sA[k] = smem + k * cap;
+    // Thread t owns vertices t, t + T, t + 2T, t + 3T of the CTA's range (every launch
+    // shape has vcta <= 4T): their x, r, d live in its registers for the whole solve, and
+    // A in shared memory.
+    float x[kResidentVpt][3], r[kResidentVpt][3], d[kResidentVpt][3];
+    bool own[kResidentVpt];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        sx[k] = smem + (6 + k) * cap;
-        sr[k] = smem + (9 + k) * cap;
-        sd[k] = smem + (12 + k) * cap;
-    }
+    for (int u = 0; u < kResidentVpt; ++u) own[u] = (int)threadIdx.x + u * T < n_local;
 
     int phase = 0;
     Acc part;
     double delta0 = 0.0, delta = 0.0, thresh = 0.0;  // thread 0's
     uint32_t flags = 0u;                             // thread 0's
-    if (L.fused) {
-        // The assembly of these vertices (k_assemble / k_assemble_grid), into shared
-        // memory; X and V are written at the end of this kernel, so they are read with
-        // plain loads.
+    if constexpr (FUSED) {
+        // The assembly of these vertices (k_assemble / k_assemble_grid); X and V are
+        // written at the end of this kernel, so they are read with plain loads.
         part = acc_zero();
-        for (int j = threadIdx.x; j < n_local; j += T) {
+#pragma unroll
+        for (int u = 0; u < kResidentVpt; ++u) {
+            if (!own[u]) continue;
+            const int j = threadIdx.x + u * T;
             const int64_t g = base + j;
             const float4 Xg = a.X[g], Vg = a.V[g];
             const OwnSpring os = load_own<false>(a, g);
@@ -131,9 +131,9 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
             for (int k = 0; k < 6; ++k) sA[k][j] = sys.A[k];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                sx[k][j] = c.x[k];
-                sr[k][j] = c.r[k];
-                sd[k][j] = c.d[k];
+                x[u][k] = c.x[k];
+                r[u][k] = c.r[k];
+                d[u][k] = c.d[k];
             }
             acc_add(part, c.term);
         }
@@ -151,16 +151,20 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
             s_go = run ? 1 : 0;
         }
     } else {
-        // The CG state k_assemble left in the planes: A, x, r, d -> shared memory.
-        for (int j = threadIdx.x; j < n_local; j += T) {
+        // The CG state k_assemble left in the planes: A -> shared memory, x, r, d ->
+        // registers.
+#pragma unroll
+        for (int u = 0; u < kResidentVpt; ++u) {
+            if (!own[u]) continue;
+            const int j = threadIdx.x + u * T;
             const int64_t g = base + j;
 #pragma unroll
             for (int k = 0; k < 6; ++k) sA[k][j] = a.A[k][g];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                sx[k][j] = a.x[k][g];
-                sr[k][j] = a.r[k][g];
-                sd[k][j] = a.d[k][g];
+                x[u][k] = a.x[k][g];
+                r[u][k] = a.r[k][g];
+                d[u][k] = a.d[k][g];
             }
         }
         if (threadIdx.x == 0) {
@@ -181,20 +185,19 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
     while (run) {
         // d = r + beta d (after the first iteration), d.(A d), IMP:320-321, 327.
         part = acc_zero();
-        for (int j = threadIdx.x; j < n_local; j += T) {
-            float d0 = sd[0][j], d1 = sd[1][j], d2 = sd[2][j];
+#pragma unroll
+        for (int u = 0; u < kResidentVpt; ++u) {
+            if (!own[u]) continue;
+            const int j = threadIdx.x + u * T;
             if (it > 0) {
-                d0 = sr[0][j] + d0 * beta;
-                d1 = sr[1][j] + d1 * beta;
-                d2 = sr[2][j] + d2 * beta;
-                sd[0][j] = d0;
-                sd[1][j] = d1;
-                sd[2][j] = d2;
+                d[u][0] = r[u][0] + d[u][0] * beta;
+                d[u][1] = r[u][1] + d[u][1] * beta;
+                d[u][2] = r[u][2] + d[u][2] * beta;
             }
             const float A[6] = {sA[0][j], sA[1][j], sA[2][j], sA[3][j], sA[4][j], sA[5][j]};
             float q0, q1, q2;
-            matvec(A, d0, d1, d2, q0, q1, q2);
-            acc_add(part, d0 * q0 + d1 * q1 + d2 * q2);
+            matvec(A, d[u][0], d[u][1], d[u][2], q0, q1, q2);
+            acc_add(part, d[u][0] * q0 + d[u][1] * q1 + d[u][2] * q2);
         }
         const double dq = cluster_sum(part, C, slots, phase);
         if (threadIdx.x == 0) {
@@ -211,21 +214,19 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
         const float alpha = s_alpha;
         // x += alpha d; r -= alpha A d; r.r, IMP:322-325.
         part = acc_zero();
-        for (int j = threadIdx.x; j < n_local; j += T) {
-            const float d0 = sd[0][j], d1 = sd[1][j], d2 = sd[2][j];
+#pragma unroll
+        for (int u = 0; u < kResidentVpt; ++u) {
+            if (!own[u]) continue;
+            const int j = threadIdx.x + u * T;
             const float A[6] = {sA[0][j], sA[1][j], sA[2][j], sA[3][j], sA[4][j], sA[5][j]};
-            float q0, q1, q2;
-            matvec(A, d0, d1, d2, q0, q1, q2);
-            sx[0][j] = sx[0][j] + d0 * alpha;
-            sx[1][j] = sx[1][j] + d1 * alpha;
-            sx[2][j] = sx[2][j] + d2 * alpha;
-            const float r0 = sr[0][j] - q0 * alpha;
-            const float r1 = sr[1][j] - q1 * alpha;
-            const float r2 = sr[2][j] - q2 * alpha;
-            sr[0][j] = r0;
-            sr[1][j] = r1;
-            sr[2][j] = r2;
-            acc_add(part, r0 * r0 + r1 * r1 + r2 * r2);
+            float q[3];
+            matvec(A, d[u][0], d[u][1], d[u][2], q[0], q[1], q[2]);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                x[u][k] = x[u][k] + d[u][k] * alpha;
+                r[u][k] = r[u][k] - q[k] * alpha;
+            }
+            acc_add(part, r[u][0] * r[u][0] + r[u][1] * r[u][1] + r[u][2] * r[u][2]);
         }
         const double rr = cluster_sum(part, C, slots, phase);
         ++it;
@@ -250,17 +251,17 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
     // V += dV dt; X += dt V; ground clamp (IMP:790-797), then the ellipsoid pass when
     // enabled; dV stays as the warm start.
     const float dt = a.dt;
-    __syncthreads();
-    for (int j = threadIdx.x; j < n_local; j += T) {
-        const int64_t g = base + j;
+#pragma unroll
+    for (int u = 0; u < kResidentVpt; ++u) {
+        if (!own[u]) continue;
+        const int64_t g = base + threadIdx.x + u * T;
         float4 Xg = a.X[g], Vg = a.V[g];
-        const float x0 = sx[0][j], x1 = sx[1][j], x2 = sx[2][j];
-        update_vertex(ip, dt, x0, x1, x2, Xg, Vg);
+        update_vertex(ip, dt, x[u][0], x[u][1], x[u][2], Xg, Vg);
         a.X[g] = Xg;
         a.V[g] = Vg;
-        a.x[0][g] = x0;
-        a.x[1][g] = x1;
-        a.x[2][g] = x2;
+        a.x[0][g] = x[u][0];
+        a.x[1][g] = x[u][1];
+        a.x[2][g] = x[u][2];
     }
     if (rank == 0 && threadIdx.x == 0) {
         InstState& st = a.state[inst];
@@ -277,12 +278,19 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
     if (C > 1) cgx::this_cluster().sync();
 }
 
+template <int T, bool FUSED>
+cudaError_t prepare_k() {
+    cudaError_t e = cudaFuncSetAttribute(k_resident<T, FUSED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)resident_smem_bytes(kResidentMaxVcta));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_resident<T, FUSED>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+}
+
 template <int T>
 cudaError_t prepare_t() {
-    cudaError_t e = cudaFuncSetAttribute(k_resident<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(15 * kResidentMaxVcta * sizeof(float)));
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_resident<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    return e;
+    cudaError_t e = prepare_k<T, false>();
+    return e == cudaSuccess ? prepare_k<T, true>() : e;
 }
 
 template <int T>
@@ -300,12 +308,12 @@ cudaError_t launch_t(const StepArgs& a, const ResidentLaunch& L, int n_clusters,
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = L.cluster > 1 ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k_resident<T>, a, L);
+    return L.fused ? cudaLaunchKernelEx(&cfg, k_resident<T, true>, a, L) : cudaLaunchKernelEx(&cfg, k_resident<T, false>, a, L);
 }
 
 }  // namespace
 
-size_t resident_smem_bytes(int vcta) { return (size_t)15 * vcta * sizeof(float); }
+size_t resident_smem_bytes(int vcta) { return (size_t)6 * vcta * sizeof(float); }  // A
 
 cudaError_t prepare_resident() {
     cudaError_t e = prepare_t<128>();
@@ -317,6 +325,7 @@ cudaError_t prepare_resident() {
 cudaError_t launch_resident(const StepArgs& a, const ResidentLaunch& L, int threads, int n_clusters,
                             cudaStream_t stream) {
     if (n_clusters <= 0) return cudaSuccess;
+    if (L.vcta > kResidentVpt * threads) return cudaErrorInvalidValue;  // a thread holds at most kResidentVpt
     switch (threads) {
         case 128: return launch_t<128>(a, L, n_clusters, stream);
         case 256: return launch_t<256>(a, L, n_clusters, stream);
