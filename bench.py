@@ -369,7 +369,8 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
     cg_roof = _cg_roofline(prof, peak)
 
     # End to end through the public API with host buffers: each step copies pinned
-    # host X, V in, runs the step and reads X, V back.
+    # host X, V in, runs the step and reads X, V back (oc_step_host: StepPhysics on host
+    # arrays, one wait per step).
     e2e_steps = max(5, min(steps, 50 if nv < 4_000_000 else 10))
     Xh = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True).numpy()
     Vh = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True).numpy()
@@ -377,9 +378,7 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        solver.set_state(Xh, Vh)
-        solver.step(DT, 1)
-        solver.get_state_into(Xh, Vh, None)
+        solver.step_host(Xh, Vh, DT, 1)
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = {"value": nv * e2e_steps * world / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 24 * nv,
            "d2h_bytes_per_step": 24 * nv, "steps": e2e_steps}

@@ -154,6 +154,12 @@ oc_status oc_get_state_device(oc_solver* s, float* X, float* V, float* dV);
  * Asynchronous: enqueued on the handle's stream. */
 oc_status oc_step(oc_solver* s, float dt, int32_t n_steps);
 oc_status oc_synchronize(oc_solver* s);
+/* The reference's StepPhysics on host arrays (IMP:873-880 over the globals X, V of
+ * IMP:80-81): X and V (packed float triples, either may be NULL) are copied in, n_steps
+ * steps run, and X and V are copied back out, with one wait on the handle's stream.
+ * OC_ERR_NON_FINITE when the input held a NaN or Inf (the state then holds it too; set
+ * a finite state before stepping again). */
+oc_status oc_step_host(oc_solver* s, float dt, int32_t n_steps, float* X, float* V);
 /* Set the passes after the update (OC_PASS_* bits) of one cloth (instance >= 0) or of
  * every cloth (-1); the matrices and ratio stay those given at oc_create.  Waits for the
  * handle's stream; the next oc_step rebuilds its graph. */

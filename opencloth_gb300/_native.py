@@ -103,6 +103,7 @@ SIGNATURES = {
     "oc_set_state_device": (C.c_int32, [_P, _P, _P, _P]),
     "oc_get_state_device": (C.c_int32, [_P, _P, _P, _P]),
     "oc_step": (C.c_int32, [_P, C.c_float, C.c_int32]),
+    "oc_step_host": (C.c_int32, [_P, C.c_float, C.c_int32, _P, _P]),
     "oc_synchronize": (C.c_int32, [_P]),
     "oc_set_passes": (C.c_int32, [_P, C.c_int32, C.c_int32]),
     "oc_apply_passes": (C.c_int32, [_P, C.c_int32]),

@@ -234,6 +234,14 @@ class ClothSolver:
     def step(self, dt: float, n_steps: int = 1) -> None:
         self._call(self._lib.oc_step(self._h, float(dt), int(n_steps)))
 
+    def step_host(self, X, V, dt: float, n_steps: int = 1) -> None:
+        """StepPhysics on host arrays: X and V (contiguous float32, 3 per vertex; either may
+        be None) are copied in, stepped n_steps times and written back in place."""
+        for a in (X, V):
+            if a is not None and (a.dtype != np.float32 or not a.flags.c_contiguous or a.size != 3 * self.n_vertices):
+                raise ValueError("step_host needs contiguous float32 arrays of 3 * n_vertices")
+        self._call(self._lib.oc_step_host(self._h, float(dt), int(n_steps), ptr(X), ptr(V)))
+
     def synchronize(self) -> None:
         self._call(self._lib.oc_synchronize(self._h))
 

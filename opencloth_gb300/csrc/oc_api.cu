@@ -1211,6 +1211,28 @@ oc_status oc_get_state(oc_solver* s, float* X, float* V, float* dV) {
     return check_device_error(s);
 }
 
+oc_status oc_step_host(oc_solver* s, float dt, int32_t n_steps, float* X, float* V) {
+    if (!valid_solver(s) || n_steps < 0 || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    const size_t n3 = 3 * (size_t)s->nv;
+    float* sx = X ? s->stage : nullptr;
+    float* sv = V ? s->stage + n3 : nullptr;
+    if (X) OC_TRY(cudaMemcpyAsync(sx, X, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    if (V) OC_TRY(cudaMemcpyAsync(sv, V, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    OC_TRY(cudaMemsetAsync(s->d_err, 0, sizeof(int32_t), s->stream));
+    OC_TRY(launch_state_in(s->args, sx, sv, nullptr, s->nv, s->d_err, s->stream));
+    if (oc_status st = oc_step(s, dt, n_steps)) return st;
+    OC_TRY(launch_state_out(s->args, sx, sv, nullptr, s->nv, s->stream));
+    if (X) OC_TRY(cudaMemcpyAsync(X, sx, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    if (V) OC_TRY(cudaMemcpyAsync(V, sv, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    // The input check's flag, read after the step (a host-driven step uses the same
+    // pinned scalar for its loop control; the step's kernels do not touch the flag).
+    OC_TRY(cudaMemcpyAsync(s->h_scalar, s->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    if (*s->h_scalar != 0) return fail(s, OC_ERR_NON_FINITE, "oc_step_host: non-finite value in the input state");
+    return check_device_error(s);
+}
+
 oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
     if (!valid_solver(s) || n_steps < 0 || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
     OC_TRY(cudaSetDevice(s->device));

@@ -53,3 +53,34 @@ def test_pinned_non_finite_input_rejected():
         with pytest.raises(OcError) as e:
             s.set_state(Xi, V)
         assert e.value.status == 3
+
+
+@pytest.mark.parametrize("executor", ["auto", "plain"])
+def test_step_host_equals_set_step_get(executor):
+    """oc_step_host (StepPhysics on host arrays, one wait) moves the same bits as
+    oc_set_state + oc_step + oc_get_state, for every executor's step."""
+    desc, _, X, V = seeded_cloth(40, 23, seed=21, velocity=0.01)
+    with ClothSolver(desc, executor=executor) as a, ClothSolver(desc, executor=executor) as b:
+        a.set_state(X, V, np.zeros_like(X))
+        b.set_state(X, V, np.zeros_like(X))
+        Xa, Va = X.copy(), V.copy()
+        Xb, Vb = X.copy(), V.copy()
+        for _ in range(3):
+            a.step_host(Xa, Va, DT, 2)
+            b.set_state(Xb, Vb)
+            b.step(DT, 2)
+            Xb, Vb, _ = b.get_state()
+        assert np.array_equal(Xa.view(np.uint32), Xb.view(np.uint32))
+        assert np.array_equal(Va.view(np.uint32), Vb.view(np.uint32))
+
+
+def test_step_host_rejects_non_finite_input():
+    from opencloth_gb300 import OcError
+
+    desc, _, X, V = seeded_cloth(9, 9, seed=2)
+    Xi = X.copy()
+    Xi[7, 2] = np.inf
+    with ClothSolver(desc) as s:
+        with pytest.raises(OcError) as e:
+            s.step_host(Xi, V.copy(), DT, 1)
+        assert e.value.status == 3
