@@ -209,8 +209,13 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
                 116.0 * nv + (s->inst_host[k].st_rest ? 4.0 * nv + 8.0 * ns : 0.0);
         else if (!fused)
             t->bytes[K_ASSEMBLE] += 120.0 * nv + 32.0 * ns;
-        // k_provot: X 16, V 32 in and out, pin flag 1, row pointer 4; 16-byte records.
-        if (s->inst_host[k].passes & OC_PASS_PROVOT) t->bytes[K_PROVOT] += 53.0 * nv + 32.0 * ns;
+        // k_provot: X 16, V 32 in and out, pin flag 1, row pointer 4; 16-byte records (a
+        // grid cloth reads its stencil instead, and rest lengths per incidence if they vary).
+        if (s->inst_host[k].passes & OC_PASS_PROVOT) {
+            const InstParams& ip = s->inst_host[k];
+            t->bytes[K_PROVOT] += ip.grid_cols > 0 ? 49.0 * nv + (ip.st_rest ? 4.0 * nv + 8.0 * ns : 0.0)
+                                                   : 53.0 * nv + 32.0 * ns;
+        }
         if (s->inst_host[k].coupled) {
             // k_cpl_assemble 112 B + 72 B per spring (record in, block out at both ends);
             // k_cpl_dir 33 B (first pass) or 45 B plus 48 B per spring (other vertex and

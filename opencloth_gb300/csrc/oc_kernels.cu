@@ -592,46 +592,66 @@ __global__ void __launch_bounds__(kThreads) k_integrate(const StepArgs a) {
 // ApplyProvotDynamicInverse (IMP:800-823) as a per-vertex gather.  The reference walks
 // the springs in order and moves the velocities of both ends; its corrections depend on
 // positions only, so vertex g's final velocity is its own plus the corrections of its
-// incident springs added in spring order — the order of g's incidence records.  Each
-// spring's correction is recomputed at both ends from p1 - p2, so both ends see the
-// same rounded value.  Pin flags come from a separate byte array: V is written here.
+// incident springs added in spring order — the order of g's incidence records (or of
+// its class's stencil template, for a grid cloth: no records read).  Each spring's
+// correction is recomputed at both ends from p1 - p2, so both ends see the same rounded
+// value.  Pin flags come from a separate byte array: V is written here.
+__device__ __forceinline__ void provot_incidence(const StepArgs& a, float ratio, const float4 Xg, bool pin_self,
+                                                 int32_t o, bool is_p2, float rest, float4& Vg) {
+    const float4 Xo = __ldg(a.X + o);
+    const float4 p1 = is_p2 ? Xo : Xg, p2 = is_p2 ? Xg : Xo;
+    const float dx = p1.x - p2.x, dy = p1.y - p2.y, dz = p1.z - p2.z;
+    const float sqr = dx * dx + dy * dy + dz * dz;
+    float dist = sqrtf(sqr);
+    const float lim = rest * ratio;
+    if (!(dist > lim)) return;
+    dist = dist - lim;
+    dist = dist / 2.0f;
+    const float inv = 1.0f / sqrtf(sqr);
+    const float cx = (dx * inv) * dist, cy = (dy * inv) * dist, cz = (dz * inv) * dist;
+    const bool pin_o = __ldg(a.pinflag + o) != 0;
+    if (!is_p2) {
+        if (!pin_self) {  // p1 moves unless pinned
+            Vg.x = Vg.x - cx;
+            Vg.y = Vg.y - cy;
+            Vg.z = Vg.z - cz;
+        }
+    } else if (pin_o || !pin_self) {  // p2 moves when p1 is pinned or p2 is free
+        Vg.x = Vg.x + cx;
+        Vg.y = Vg.y + cy;
+        Vg.z = Vg.z + cz;
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) k_provot(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstParams& ip = a.inst[bi.inst];
     if (!((a.only_passes ? a.only_passes : ip.passes) & OC_PASS_PROVOT)) return;
     const float ratio = ip.provot_ratio;
+    const int32_t cols = ip.grid_cols;
     for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
         const float4 Xg = __ldg(a.X + g);
         float4 Vg = a.V[g];
         const bool pin_self = a.pinflag[g] != 0;
-        const int32_t k1 = __ldg(a.rowptr + g + 1);
-        for (int32_t k = __ldg(a.rowptr + g); k < k1; ++k) {
-            const int4 rec = __ldg(a.inc + k);
-            const bool is_p2 = rec.x < 0;
-            const int32_t o = rec.x & 0x7fffffff;
-            const float4 Xo = __ldg(a.X + o);
-            const float4 p1 = is_p2 ? Xo : Xg, p2 = is_p2 ? Xg : Xo;
-            const float dx = p1.x - p2.x, dy = p1.y - p2.y, dz = p1.z - p2.z;
-            const float sqr = dx * dx + dy * dy + dz * dz;
-            float dist = sqrtf(sqr);
-            const float lim = __int_as_float(rec.y) * ratio;
-            if (!(dist > lim)) continue;
-            dist = dist - lim;
-            dist = dist / 2.0f;
-            const float inv = 1.0f / sqrtf(sqr);
-            const float cx = (dx * inv) * dist, cy = (dy * inv) * dist, cz = (dz * inv) * dist;
-            const bool pin_o = __ldg(a.pinflag + o) != 0;
-            if (!is_p2) {
-                if (!pin_self) {  // p1 moves unless pinned
-                    Vg.x = Vg.x - cx;
-                    Vg.y = Vg.y - cy;
-                    Vg.z = Vg.z - cz;
-                }
-            } else if (pin_o || !pin_self) {  // p2 moves when p1 is pinned or p2 is free
-                Vg.x = Vg.x + cx;
-                Vg.y = Vg.y + cy;
-                Vg.z = Vg.z + cz;
+        if (cols > 0) {  // grid cloth: the incidences from its class's stencil template
+            const int32_t l = (int32_t)(g - ip.v_off), r = l / cols, c = l - r * cols;
+            const int cl = stencil_class_1d(r, ip.grid_rows) * 6 + stencil_class_1d(c, cols);
+            const int32_t* st = a.st_data + ip.st_off;
+            const float4* par = a.st_param + ip.st_par;
+            const int32_t e0 = __ldg(st + cl), e1 = __ldg(st + cl + 1);
+            const float* rest_inc = ip.st_rest ? a.rest_inc + __ldg(a.rowptr + g) - e0 : nullptr;
+            for (int32_t e = e0; e < e1; ++e) {
+                const int32_t v = __ldg(st + e);
+                const int32_t o = (int32_t)(g + (int64_t)((v & 7) - 2) * cols + (((v >> 3) & 7) - 2));
+                const float rest = rest_inc ? __ldg(rest_inc + e) : __ldg(par + (v >> 7)).x;
+                provot_incidence(a, ratio, Xg, pin_self, o, (v & 64) != 0, rest, Vg);
+            }
+        } else {
+            const int32_t k1 = __ldg(a.rowptr + g + 1);
+            for (int32_t k = __ldg(a.rowptr + g); k < k1; ++k) {
+                const int4 rec = __ldg(a.inc + k);
+                provot_incidence(a, ratio, Xg, pin_self, rec.x & 0x7fffffff, rec.x < 0, __int_as_float(rec.y), Vg);
             }
         }
         a.V[g] = Vg;
