@@ -367,6 +367,21 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
     roof = _dominant_roofline(prof, peak, name)
     roof["peak_source"] = "measured" if peaks_path.exists() else "fallback"
     cg_roof = _cg_roofline(prof, peak)
+    if cg_roof is not None and cg_roof["kernels"] == ["k_resident"]:
+        # The resident kernel keeps the CG on chip, so its HBM figure counts only the state
+        # it loads and stores.  Beside it: the CG's algorithmic bytes in the streamed
+        # layout (first direction 36 B, 60 B per later direction pass, 84 B per update
+        # pass, 76 B for the update, per vertex) over the resident kernel's time.
+        it_p, _, _ = solver.stats()
+        nv_k = np.array([d.n_vertices for d in descs], np.float64)
+        itk = it_p.astype(np.float64)
+        per_step = float(np.sum(nv_k * np.where(itk > 0, 36 + 60 * (itk - 1) + 84 * itk + 76, 76)))
+        secs = prof["k_resident"]["ms_total"] / 1e3
+        eq = 3 * per_step / secs / 1e9 if secs > 0 else 0.0
+        cg_roof["equivalent"] = {"achieved": eq, "frac": eq / peak, "unit": "GB/s",
+                                 "bytes_per_step": per_step,
+                                 "note": "the CG's algorithmic bytes in the streamed layout over k_resident's time "
+                                         "(the iterations run in shared memory and registers)"}
 
     # End to end through the public API with host buffers: each step copies pinned
     # host X, V in, runs the step and reads X, V back (oc_step_host: StepPhysics on host
