@@ -978,14 +978,32 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     s->any_provot = P.any_provot;
     s->any_coupled = P.any_coupled;
     if (P.any_coupled) {
-        std::vector<int32_t> other(P.inc.size());
-        for (size_t k = 0; k < P.inc.size(); ++k) other[k] = P.inc[k].x & 0x7fffffff;
+        // Slot-major per-incidence layout: slices of 32 vertices, each as wide as its
+        // largest degree (padding slots hold the vertex itself and are never read).
+        const int64_t n_slices = (P.nv + 31) / 32;
+        std::vector<int64_t> slice((size_t)n_slices + 1, 0);
+        for (int64_t sl = 0; sl < n_slices; ++sl) {
+            int32_t width = 0;
+            for (int64_t g = 32 * sl; g < std::min<int64_t>(P.nv, 32 * sl + 32); ++g)
+                width = std::max(width, P.rowptr[g + 1] - P.rowptr[g]);
+            slice[(size_t)sl + 1] = slice[(size_t)sl] + 32 * (int64_t)width;
+        }
+        const size_t slots = std::max<size_t>((size_t)slice[(size_t)n_slices], 1);
+        std::vector<int32_t> other(slots, 0);
+        for (int64_t g = 0; g < P.nv; ++g) {
+            const int64_t base = slice[(size_t)(g >> 5)] + (g & 31);
+            const int32_t deg = P.rowptr[g + 1] - P.rowptr[g];
+            for (int32_t e = 0; e < deg; ++e) other[(size_t)(base + 32 * e)] = P.inc[P.rowptr[g] + e].x & 0x7fffffff;
+        }
+        int64_t* d_slice = nullptr;
+        OC_CREATE_TRY(upload(s, &d_slice, slice));
+        a.cpl_slice = d_slice;
         int32_t* d_other = nullptr;
         OC_CREATE_TRY(upload(s, &d_other, other));
         a.cpl_o = d_other;
         float* cplanes = nullptr;
-        OC_CREATE_TRY(dalloc(s, &cplanes, 5 * std::max<size_t>(P.inc.size(), 1)));
-        for (int k = 0; k < 5; ++k) a.cpl_c[k] = cplanes + (size_t)k * std::max<size_t>(P.inc.size(), 1);
+        OC_CREATE_TRY(dalloc(s, &cplanes, 5 * slots));
+        for (int k = 0; k < 5; ++k) a.cpl_c[k] = cplanes + (size_t)k * slots;
         float* vplanes = nullptr;
         OC_CREATE_TRY(dalloc(s, &vplanes, 7 * stride));
         OC_CREATE_TRY(cudaMemset(vplanes, 0, 7 * stride * sizeof(float)));

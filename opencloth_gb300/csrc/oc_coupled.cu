@@ -15,7 +15,7 @@
 // Dirichlet rows filtered out of the CG.
 //
 //   k_cpl_assemble  F (the reference's forces, bit for bit), each incidence's B_s into
-//                   per-record planes, the diagonal block and its inverse P^-1, b, and
+//                   slot-major per-incidence planes (StepArgs::cpl_slice), the diagonal block and its inverse P^-1, b, and
 //                   the CG set-up r = b - A x, z = P^-1 r, delta0 = r.z
 //   k_cpl_dir       dn = z + beta d (first pass: z); q = A dn with the neighbours' dn
 //                   rebuilt from their z and d; d.q
@@ -106,7 +106,9 @@ __global__ void __launch_bounds__(kThreads) k_cpl_assemble(const StepArgs a) {
         float w0 = 0.0f, w1 = 0.0f, w2 = 0.0f;
         float ax0 = mp * xi0, ax1 = mp * xi1, ax2 = mp * xi2;
         const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
+        const int64_t slot0 = __ldg(a.cpl_slice + (g >> 5)) + (g & 31);
         for (int32_t k = k0; k < k1; ++k) {
+            const int64_t sk = slot0 + 32 * (int64_t)(k - k0);
             const int4 rec = __ldg(a.inc + k);
             const bool as_p2 = rec.x < 0;
             const int32_t o = rec.x & 0x7fffffff;
@@ -127,11 +129,11 @@ __global__ void __launch_bounds__(kThreads) k_cpl_assemble(const StepArgs a) {
             }
             const SpringBlock c = as_p2 ? spring_block(Xo, Xg, rest, ks, kd, h, hh)
                                         : spring_block(Xg, Xo, rest, ks, kd, h, hh);
-            a.cpl_c[0][k] = c.n0;
-            a.cpl_c[1][k] = c.n1;
-            a.cpl_c[2][k] = c.n2;
-            a.cpl_c[3][k] = c.beta;
-            a.cpl_c[4][k] = c.gamma;
+            a.cpl_c[0][sk] = c.n0;
+            a.cpl_c[1][sk] = c.n1;
+            a.cpl_c[2][sk] = c.n2;
+            a.cpl_c[3][sk] = c.beta;
+            a.cpl_c[4][sk] = c.gamma;
             const float g0 = c.gamma * c.n0, g1 = c.gamma * c.n1, g2 = c.gamma * c.n2;
             D[0] = D[0] + (c.beta + g0 * c.n0);
             D[1] = D[1] + g0 * c.n1;
@@ -222,8 +224,10 @@ __global__ void __launch_bounds__(kThreads) k_cpl_dir(const StepArgs a) {
                 q0 = mp * n0;
                 q1 = mp * n1;
                 q2 = mp * n2;
-                const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
-                for (int32_t k = k0; k < k1; ++k) {
+                const int32_t deg = __ldg(a.rowptr + g + 1) - __ldg(a.rowptr + g);
+                const int64_t slot0 = __ldg(a.cpl_slice + (g >> 5)) + (g & 31);
+                for (int32_t e = 0; e < deg; ++e) {
+                    const int64_t k = slot0 + 32 * (int64_t)e;
                     const int32_t o = __ldg(a.cpl_o + k);
                     float m0 = Z0[o], m1 = Z1[o], m2 = Z2[o];
                     if (!first) {

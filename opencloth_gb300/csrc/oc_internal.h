@@ -99,6 +99,10 @@ struct StepArgs {
     const int32_t* st_data;
     const float4* st_param;
     const float* rest_inc;   // rest length of every incidence record (CSR order), or nullptr
+    // COUPLED per-incidence data is slot-major over slices of 32 consecutive vertices:
+    // incidence e of vertex g sits at cpl_slice[g >> 5] + 32 e + (g & 31), so a warp's
+    // accesses to one slot are contiguous.
+    const int64_t* cpl_slice;
     const int32_t* cpl_o;
     float* cpl_c[5];         // n0, n1, n2, beta, gamma
     float* cpl_m;
