@@ -132,11 +132,11 @@ def algorithmic_bytes(kernel: str, n_vertices: int, n_springs: int, first_dir: b
         # spring two records in and two 20-byte blocks out.
         return 112 * N + 72 * S
     if kernel == "k_cpl_dir":
-        # pin flag 1, z 12 (+ d 12), m' 4, rowptr 4, q 12 per vertex; per spring the other
-        # vertex and the block at both ends.
-        return (33 if first_dir else 45) * N + 48 * S
+        # pin flag 1, z 16 (+ d 16; 16-byte records), m' 4, rowptr 4, q 12 per vertex; per
+        # spring the other vertex and the block at both ends.
+        return (37 if first_dir else 53) * N + 48 * S
     if kernel == "k_cpl_update":
-        return (120 if first_dir else 132) * N  # z, (d), x, r, q, P^-1 in; x, r, d, z out
+        return (132 if first_dir else 148) * N  # z, (d), x, r, q, P^-1 in; x, r, d, z out
     raise KeyError(kernel)
 
 

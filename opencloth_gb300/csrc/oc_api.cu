@@ -218,14 +218,15 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
         }
         if (s->inst_host[k].coupled) {
             // k_cpl_assemble 112 B + 72 B per spring (record in, block out at both ends);
-            // k_cpl_dir 33 B (first pass) or 45 B plus 48 B per spring (other vertex and
-            // block at both ends); k_cpl_update 120 B (first) or 132 B; k_integrate 76 B.
+            // k_cpl_dir 37 B (first pass) or 53 B plus 48 B per spring (other vertex and
+            // block at both ends; z and d are 16-byte records); k_cpl_update 132 B (first)
+            // or 148 B; k_integrate 76 B.
             t->bytes[K_CPL_ASSEMBLE] += 112.0 * nv + 72.0 * ns;
             const double it = (double)st.iter;
-            double dirs = it > 0 ? 33.0 * nv + 45.0 * nv * (it - 1.0) + 48.0 * ns * it : 0.0;
-            if (st.flags & OC_FLAG_BREAKDOWN) dirs += (it > 0 ? 45.0 : 33.0) * nv + 48.0 * ns;
+            double dirs = it > 0 ? 37.0 * nv + 53.0 * nv * (it - 1.0) + 48.0 * ns * it : 0.0;
+            if (st.flags & OC_FLAG_BREAKDOWN) dirs += (it > 0 ? 53.0 : 37.0) * nv + 48.0 * ns;
             t->bytes[K_CPL_DIR] += dirs;
-            t->bytes[K_CPL_UPDATE] += it > 0 ? 120.0 * nv + 132.0 * nv * (it - 1.0) : 0.0;
+            t->bytes[K_CPL_UPDATE] += it > 0 ? 132.0 * nv + 148.0 * nv * (it - 1.0) : 0.0;
             t->bytes[K_INTEGRATE] += 76.0 * nv;
             continue;
         }
@@ -1005,13 +1006,14 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
         OC_CREATE_TRY(dalloc(s, &cplanes, 5 * slots));
         for (int k = 0; k < 5; ++k) a.cpl_c[k] = cplanes + (size_t)k * slots;
         float* vplanes = nullptr;
-        OC_CREATE_TRY(dalloc(s, &vplanes, 7 * stride));
-        OC_CREATE_TRY(cudaMemset(vplanes, 0, 7 * stride * sizeof(float)));
+        OC_CREATE_TRY(dalloc(s, &vplanes, 4 * stride));
+        OC_CREATE_TRY(cudaMemset(vplanes, 0, 4 * stride * sizeof(float)));
         a.cpl_m = vplanes;
-        for (int k = 0; k < 3; ++k) {
-            a.z[k] = vplanes + (1 + k) * stride;
-            a.q[k] = vplanes + (4 + k) * stride;
-        }
+        for (int k = 0; k < 3; ++k) a.q[k] = vplanes + (1 + k) * stride;
+        OC_CREATE_TRY(dalloc(s, &a.cpl_z, (size_t)P.nv));
+        OC_CREATE_TRY(dalloc(s, &a.cpl_d, (size_t)P.nv));
+        OC_CREATE_TRY(cudaMemset(a.cpl_z, 0, sizeof(float4) * (size_t)P.nv));
+        OC_CREATE_TRY(cudaMemset(a.cpl_d, 0, sizeof(float4) * (size_t)P.nv));
     }
     {
         std::vector<uint8_t> pins((size_t)P.nv);

@@ -175,12 +175,8 @@ __global__ void __launch_bounds__(kThreads) k_cpl_assemble(const StepArgs a) {
         a.r[0][g] = r0;
         a.r[1][g] = r1;
         a.r[2][g] = r2;
-        a.z[0][g] = z0;
-        a.z[1][g] = z1;
-        a.z[2][g] = z2;
-        a.d[0][g] = 0.0f;
-        a.d[1][g] = 0.0f;
-        a.d[2][g] = 0.0f;
+        a.cpl_z[g] = make_float4(z0, z1, z2, 0.0f);
+        a.cpl_d[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (pinned) {
             a.x[0][g] = 0.0f;
             a.x[1][g] = 0.0f;
@@ -200,12 +196,8 @@ __global__ void __launch_bounds__(kThreads) k_cpl_dir(const StepArgs a) {
     if (active) {
         const bool first = st.iter == 0;
         const float beta = st.beta;
-        const float* __restrict__ Z0 = a.z[0];
-        const float* __restrict__ Z1 = a.z[1];
-        const float* __restrict__ Z2 = a.z[2];
-        const float* __restrict__ D0 = a.d[0];
-        const float* __restrict__ D1 = a.d[1];
-        const float* __restrict__ D2 = a.d[2];
+        const float4* __restrict__ Z = a.cpl_z;
+        const float4* __restrict__ D = a.cpl_d;
         const float* __restrict__ C0 = a.cpl_c[0];
         const float* __restrict__ C1 = a.cpl_c[1];
         const float* __restrict__ C2 = a.cpl_c[2];
@@ -214,11 +206,13 @@ __global__ void __launch_bounds__(kThreads) k_cpl_dir(const StepArgs a) {
         for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
             float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f;
             if (!__ldg(a.pinflag + g)) {
-                float n0 = Z0[g], n1 = Z1[g], n2 = Z2[g];
+                const float4 zg = Z[g];
+                float n0 = zg.x, n1 = zg.y, n2 = zg.z;
                 if (!first) {
-                    n0 = n0 + D0[g] * beta;
-                    n1 = n1 + D1[g] * beta;
-                    n2 = n2 + D2[g] * beta;
+                    const float4 dg = D[g];
+                    n0 = n0 + dg.x * beta;
+                    n1 = n1 + dg.y * beta;
+                    n2 = n2 + dg.z * beta;
                 }
                 const float mp = __ldg(a.cpl_m + g);
                 q0 = mp * n0;
@@ -229,11 +223,13 @@ __global__ void __launch_bounds__(kThreads) k_cpl_dir(const StepArgs a) {
                 for (int32_t e = 0; e < deg; ++e) {
                     const int64_t k = slot0 + 32 * (int64_t)e;
                     const int32_t o = __ldg(a.cpl_o + k);
-                    float m0 = Z0[o], m1 = Z1[o], m2 = Z2[o];
+                    const float4 zo = Z[o];
+                    float m0 = zo.x, m1 = zo.y, m2 = zo.z;
                     if (!first) {
-                        m0 = m0 + D0[o] * beta;
-                        m1 = m1 + D1[o] * beta;
-                        m2 = m2 + D2[o] * beta;
+                        const float4 dd = D[o];
+                        m0 = m0 + dd.x * beta;
+                        m1 = m1 + dd.y * beta;
+                        m2 = m2 + dd.z * beta;
                     }
                     block_apply(C0[k], C1[k], C2[k], C3[k], C4[k], n0 - m0, n1 - m1, n2 - m2, q0, q1, q2);
                 }
@@ -258,22 +254,22 @@ __global__ void __launch_bounds__(kThreads) k_cpl_update(const StepArgs a) {
         const float alpha = st.alpha, beta = st.beta;
         for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
             float dn[3], r[3];
+            const float4 zg = a.cpl_z[g], dg = a.cpl_d[g];
+            const float zv[3] = {zg.x, zg.y, zg.z}, dv[3] = {dg.x, dg.y, dg.z};
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                float v = a.z[k][g];
-                if (!first) v = v + a.d[k][g] * beta;
+                float v = zv[k];
+                if (!first) v = v + dv[k] * beta;
                 dn[k] = v;
                 a.x[k][g] = a.x[k][g] + dn[k] * alpha;
                 r[k] = a.r[k][g] - a.q[k][g] * alpha;
                 a.r[k][g] = r[k];
-                a.d[k][g] = dn[k];
             }
+            a.cpl_d[g] = make_float4(dn[0], dn[1], dn[2], 0.0f);
             const float P[6] = {a.A[0][g], a.A[1][g], a.A[2][g], a.A[3][g], a.A[4][g], a.A[5][g]};
             float z0, z1, z2;
             matvec(P, r[0], r[1], r[2], z0, z1, z2);
-            a.z[0][g] = z0;
-            a.z[1][g] = z1;
-            a.z[2][g] = z2;
+            a.cpl_z[g] = make_float4(z0, z1, z2, 0.0f);
             acc_add(part, r[0] * z0 + r[1] * z1 + r[2] * z2);
         }
     }

@@ -91,8 +91,8 @@ struct StepArgs {
                              // every cloth (a pass run on its own), 0 = each cloth's own bits
     // COUPLED cloths (allocated only when the handle has one).  Per incidence record:
     // the other vertex and the spring block B = beta I + gamma n n^T of this step; per
-    // vertex: m' and the CG vectors z = P^-1 r and q = A d.  P^-1 (the inverse of the
-    // vertex's diagonal block) lives in the A planes.
+    // vertex: m' and the CG vectors z = P^-1 r, the direction d and q = A d.  P^-1 (the
+    // inverse of the vertex's diagonal block) lives in the A planes.
     // Grid cloths (InstParams::grid_cols > 0): per cloth 37 class starts then the entries
     // (di + 2 | dj + 2 << 3 | is_p2 << 6 | slot << 7), and kStencilSlots parameter slots
     // {rest, ks, kd, 0}.
@@ -106,7 +106,8 @@ struct StepArgs {
     const int32_t* cpl_o;
     float* cpl_c[5];         // n0, n1, n2, beta, gamma
     float* cpl_m;
-    float* z[3];
+    float4* cpl_z;           // z = P^-1 r, 16-byte records (w unused): a neighbour's z and d are
+    float4* cpl_d;           // two vector loads in k_cpl_dir
     float* q[3];
 };
 
