@@ -221,7 +221,9 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
             // k_cpl_dir 37 B (first pass) or 53 B plus 48 B per spring (other vertex and
             // block at both ends; z and d are 16-byte records); k_cpl_update 132 B (first)
             // or 148 B; k_integrate 76 B.
-            t->bytes[K_CPL_ASSEMBLE] += 112.0 * nv + 72.0 * ns;
+            const InstParams& cp = s->inst_host[k];  // a grid cloth reads its stencil, not records
+            t->bytes[K_CPL_ASSEMBLE] += cp.grid_cols > 0 ? 112.0 * nv + 40.0 * ns + (cp.st_rest ? 4.0 * nv + 8.0 * ns : 0.0)
+                                                         : 112.0 * nv + 72.0 * ns;
             const double it = (double)st.iter;
             double dirs = it > 0 ? 37.0 * nv + 53.0 * nv * (it - 1.0) + 48.0 * ns * it : 0.0;
             if (st.flags & OC_FLAG_BREAKDOWN) dirs += (it > 0 ? 53.0 : 37.0) * nv + 48.0 * ns;

@@ -105,15 +105,12 @@ __global__ void __launch_bounds__(kThreads) k_cpl_assemble(const StepArgs a) {
         float D[6] = {mp, 0.0f, 0.0f, mp, 0.0f, mp};
         float w0 = 0.0f, w1 = 0.0f, w2 = 0.0f;
         float ax0 = mp * xi0, ax1 = mp * xi1, ax2 = mp * xi2;
-        const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
         const int64_t slot0 = __ldg(a.cpl_slice + (g >> 5)) + (g & 31);
-        for (int32_t k = k0; k < k1; ++k) {
-            const int64_t sk = slot0 + 32 * (int64_t)(k - k0);
-            const int4 rec = __ldg(a.inc + k);
-            const bool as_p2 = rec.x < 0;
-            const int32_t o = rec.x & 0x7fffffff;
+        // Incidence e of the vertex (spring-id order): neighbour o, the vertex's side, and
+        // the spring's parameters.
+        auto incidence = [&](int32_t e, int32_t o, bool as_p2, float rest, float ks, float kd) {
+            const int64_t sk = slot0 + 32 * (int64_t)e;
             const float4 Xo = __ldg(a.X + o), Vo = __ldg(a.V + o);
-            const float rest = __int_as_float(rec.y), ks = __int_as_float(rec.z), kd = __int_as_float(rec.w);
             if (!pinned) {  // pinned vertices take no spring force (IMP:730-733)
                 if (as_p2) {
                     const float3 f = spring_force(Xo, Xg, Vo, Vg, rest, ks, kd);
@@ -155,6 +152,28 @@ __global__ void __launch_bounds__(kThreads) k_cpl_assemble(const StepArgs a) {
                 xo2 = a.x[2][o];
             }
             block_apply(c.n0, c.n1, c.n2, c.beta, c.gamma, xi0 - xo0, xi1 - xo1, xi2 - xo2, ax0, ax1, ax2);
+        };
+        if (ip.grid_cols > 0) {  // grid cloth: its class's stencil template, no records
+            const int32_t cols = ip.grid_cols;
+            const int32_t l = (int32_t)(g - ip.v_off), row = l / cols, col = l - row * cols;
+            const int cl = stencil_class_1d(row, ip.grid_rows) * 6 + stencil_class_1d(col, cols);
+            const int32_t* st = a.st_data + ip.st_off;
+            const float4* par = a.st_param + ip.st_par;
+            const int32_t e0 = __ldg(st + cl), e1 = __ldg(st + cl + 1);
+            const float* rest_inc = ip.st_rest ? a.rest_inc + __ldg(a.rowptr + g) - e0 : nullptr;
+            for (int32_t e = e0; e < e1; ++e) {
+                const int32_t v = __ldg(st + e);
+                const float4 p = __ldg(par + (v >> 7));
+                const int32_t o = (int32_t)(g + (int64_t)((v & 7) - 2) * cols + (((v >> 3) & 7) - 2));
+                incidence(e - e0, o, (v & 64) != 0, rest_inc ? __ldg(rest_inc + e) : p.x, p.y, p.z);
+            }
+        } else {
+            const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
+            for (int32_t k = k0; k < k1; ++k) {
+                const int4 rec = __ldg(a.inc + k);
+                incidence(k - k0, rec.x & 0x7fffffff, rec.x < 0, __int_as_float(rec.y), __int_as_float(rec.z),
+                          __int_as_float(rec.w));
+            }
         }
         const float c00 = D[3] * D[5] - D[4] * D[4], c01 = D[2] * D[4] - D[1] * D[5], c02 = D[1] * D[4] - D[2] * D[3];
         const float c11 = D[0] * D[5] - D[2] * D[2], c12 = D[1] * D[2] - D[0] * D[4], c22 = D[0] * D[3] - D[1] * D[1];
