@@ -91,6 +91,10 @@ struct oc_solver {
     size_t stride = 0;      // plane stride (vertices)
     struct Tape {
         int32_t n_steps = 0, every = 0, n_ck = 0;
+        // Segment buffers (every step's X, V, A, dV of one segment): n_buf of them.  The
+        // last n_keep segments are kept from the taped forward and walked without a
+        // recompute; the others are recomputed into buffer 0 (absent when n_keep = n_ck).
+        int32_t n_buf = 0, n_keep = 0, cap_buf = 0, cap_every = 0;
         float dt = 0.0f;
         float4 *ckX = nullptr, *ckV = nullptr, *segX = nullptr, *segV = nullptr, *finX = nullptr, *finV = nullptr;
         // segAx: per step of a segment, the system A (6 planes) and the solution dV (3
@@ -632,6 +636,14 @@ oc_status copy_state(oc_solver* s, float4* dX, float4* dV, float* dx, const floa
 }
 
 float* xplanes(oc_solver* s) { return s->args.x[0]; }  // the three x planes are contiguous
+
+// The segment buffer of segment c: a kept segment's own buffer, or -1 for a segment the
+// reverse pass recomputes (into buffer 0).
+int32_t tape_buffer(const oc_solver::Tape& T, int32_t c) {
+    const int32_t first_kept = T.n_ck - T.n_keep;
+    if (c < first_kept) return -1;
+    return (c - first_kept) + (T.n_keep < T.n_ck ? 1 : 0);
+}
 
 // The adjoint solve of one step as a graph: reset the loop counter, set up the CG on
 // the adjoint right-hand side (k_adj_seed), iterate (WHILE node) over every cloth.
@@ -1595,20 +1607,30 @@ oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t check
     if (every == 0) every = std::max(1, (int32_t)std::ceil(std::sqrt((double)n_steps)));
     every = std::min(every, n_steps);
     const int32_t n_ck = (n_steps + every - 1) / every;
-    const double need = (double)state_bytes * (double)(n_ck + 1) + (double)seg_bytes * (double)every;
+    const double buf_bytes = (double)seg_bytes * (double)every;
+    const double need = (double)state_bytes * (double)(n_ck + 1) + buf_bytes;
     if (budget_bytes > 0 && need > (double)budget_bytes)
         return fail(s, OC_ERR_OUT_OF_MEMORY, "oc_tape_forward: checkpoints need " + std::to_string(need) +
                                                  " bytes, above the budget");
-    // (Re)allocate when the shape changed; buffers live until the handle is destroyed.
-    if (T.n_ck < n_ck || T.every < every || !T.ckX) {
+    // With a budget, the room left after the checkpoints keeps whole segments from this
+    // forward, the last ones first, so that the reverse pass need not recompute them.
+    int32_t n_buf = 1;
+    if (budget_bytes > 0)
+        n_buf = (int32_t)std::min<double>(n_ck, 1.0 + std::floor(((double)budget_bytes - need) / buf_bytes));
+    const int32_t n_keep = n_buf >= n_ck ? n_ck : n_buf - 1;
+    // (Re)allocate when the shape grew; buffers live until the handle is destroyed.
+    if (T.n_ck < n_ck || T.cap_every < every || T.cap_buf < n_buf || !T.ckX) {
         float4* p4 = nullptr;
         float* pf = nullptr;
         OC_TRY(dalloc(s, &p4, (size_t)s->nv * n_ck)); T.ckX = p4;
         OC_TRY(dalloc(s, &p4, (size_t)s->nv * n_ck)); T.ckV = p4;
         OC_TRY(dalloc(s, &pf, 3 * s->stride * n_ck)); T.ckx = pf;
-        OC_TRY(dalloc(s, &p4, (size_t)s->nv * every)); T.segX = p4;
-        OC_TRY(dalloc(s, &p4, (size_t)s->nv * every)); T.segV = p4;
-        OC_TRY(dalloc(s, &pf, 9 * s->stride * every)); T.segAx = pf;
+        const size_t slots = (size_t)every * n_buf;
+        OC_TRY(dalloc(s, &p4, (size_t)s->nv * slots)); T.segX = p4;
+        OC_TRY(dalloc(s, &p4, (size_t)s->nv * slots)); T.segV = p4;
+        OC_TRY(dalloc(s, &pf, 9 * s->stride * slots)); T.segAx = pf;
+        T.cap_buf = n_buf;
+        T.cap_every = every;
         if (!T.finX) {
             OC_TRY(dalloc(s, &p4, (size_t)s->nv)); T.finX = p4;
             OC_TRY(dalloc(s, &p4, (size_t)s->nv)); T.finV = p4;
@@ -1620,16 +1642,32 @@ oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t check
     T.n_steps = n_steps;
     T.every = every;
     T.n_ck = n_ck;
+    T.n_buf = n_buf;
+    T.n_keep = n_keep;
     T.dt = dt;
+    const size_t nAx = 9 * s->stride;
     for (int32_t t = 0; t < n_steps; ++t) {
-        if (t % every == 0) {
-            const int32_t c = t / every;
+        const int32_t c = t / every, q = t - c * every;
+        const int32_t len = std::min(n_steps, (c + 1) * every) - c * every;
+        if (q == 0) {
             oc_status st = copy_state(s, T.ckX + (size_t)c * s->nv, T.ckV + (size_t)c * s->nv,
                                       T.ckx + 3 * s->stride * c, s->args.X, s->args.V, xplanes(s));
             if (st != OC_OK) return st;
         }
+        const int32_t b = tape_buffer(T, c);  // a kept segment: snapshot as the recompute would
+        float4* sX = T.segX + (size_t)b * every * s->nv;
+        float4* sV = T.segV + (size_t)b * every * s->nv;
+        float* sAx = T.segAx + (size_t)b * every * nAx;
+        if (b >= 0 && q == 0)
+            OC_TRY(launch_snapshot(s->args.X, s->args.V, sX, sV, nullptr, nullptr, s->nv, 0, s->stream));
         oc_status st = oc_step(s, dt, 1);
         if (st != OC_OK) return st;
+        if (b >= 0) {
+            const bool more = q + 1 < len;
+            OC_TRY(launch_snapshot(s->args.X, s->args.V, more ? sX + (size_t)(q + 1) * s->nv : nullptr,
+                                   more ? sV + (size_t)(q + 1) * s->nv : nullptr, s->args.A[0], sAx + nAx * q,
+                                   s->nv, (int64_t)nAx, s->stream));
+        }
     }
     oc_status st = copy_state(s, T.finX, T.finV, T.finx, s->args.X, s->args.V, xplanes(s));
     if (st != OC_OK) return st;
@@ -1696,25 +1734,34 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
     float* live_Ax = s->args.A[0];  // A (6 planes) then x (3 planes)
     for (int32_t c = T.n_ck - 1; c >= 0; --c) {
         const int32_t t0 = c * T.every, t1 = std::min(T.n_steps, t0 + T.every), len = t1 - t0;
-        oc_status r = copy_state(s, s->args.X, s->args.V, xplanes(s), T.ckX + (size_t)c * s->nv,
-                                 T.ckV + (size_t)c * s->nv, T.ckx + 3 * st * c);
-        if (r != OC_OK) return r;
-        // Recompute the segment, keeping every step's input state and solution.
-        OC_TRY(launch_snapshot(s->args.X, s->args.V, T.segX, T.segV, nullptr, nullptr, s->nv, 0, s->stream));
-        for (int32_t q = 0; q < len; ++q) {
-            if ((r = oc_step(s, T.dt, 1)) != OC_OK) return r;
-            const bool more = q + 1 < len;
-            OC_TRY(launch_snapshot(s->args.X, s->args.V, more ? T.segX + (size_t)(q + 1) * s->nv : nullptr,
-                                   more ? T.segV + (size_t)(q + 1) * s->nv : nullptr, live_Ax, T.segAx + nAx * q,
-                                   s->nv, (int64_t)nAx, s->stream));
+        const int32_t kept = tape_buffer(T, c);
+        const int32_t buf = kept >= 0 ? kept : 0;
+        float4* const segX = T.segX + (size_t)buf * T.every * s->nv;
+        float4* const segV = T.segV + (size_t)buf * T.every * s->nv;
+        float* const segAx = T.segAx + (size_t)buf * T.every * nAx;
+        oc_status r = OC_OK;
+        if (kept < 0) {
+            // Recompute the segment from its checkpoint, keeping every step's input state,
+            // system and solution.
+            r = copy_state(s, s->args.X, s->args.V, xplanes(s), T.ckX + (size_t)c * s->nv, T.ckV + (size_t)c * s->nv,
+                           T.ckx + 3 * st * c);
+            if (r != OC_OK) return r;
+            OC_TRY(launch_snapshot(s->args.X, s->args.V, segX, segV, nullptr, nullptr, s->nv, 0, s->stream));
+            for (int32_t q = 0; q < len; ++q) {
+                if ((r = oc_step(s, T.dt, 1)) != OC_OK) return r;
+                const bool more = q + 1 < len;
+                OC_TRY(launch_snapshot(s->args.X, s->args.V, more ? segX + (size_t)(q + 1) * s->nv : nullptr,
+                                       more ? segV + (size_t)(q + 1) * s->nv : nullptr, live_Ax, segAx + nAx * q,
+                                       s->nv, (int64_t)nAx, s->stream));
+            }
         }
         // And walk it backwards: the kernels read the step's state in place in the tape.
         for (int32_t q = len - 1; q >= 0; --q) {
             StepArgs b = a;
-            b.X = T.segX + (size_t)q * s->nv;
-            b.V = T.segV + (size_t)q * s->nv;
+            b.X = segX + (size_t)q * s->nv;
+            b.V = segV + (size_t)q * s->nv;
             AdjArgs jj = j;
-            float* slot = T.segAx + nAx * q;
+            float* slot = segAx + nAx * q;
             for (int k = 0; k < 3; ++k) jj.dV[k] = slot + (6 + k) * st;
             if (!taped_A)
                 OC_TRY(assemble(b));  // A of this step, rebuilt
@@ -1774,7 +1821,8 @@ oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* t
     const size_t state_bytes = 2 * sizeof(float4) * (size_t)s->nv + 3 * s->stride * sizeof(float);
     if (checkpoint_every) *checkpoint_every = T.every;
     const size_t seg_bytes = 2 * sizeof(float4) * (size_t)s->nv + 9 * s->stride * sizeof(float);
-    if (tape_bytes) *tape_bytes = (int64_t)(state_bytes * (size_t)(T.n_ck + 1) + seg_bytes * (size_t)T.every);
+    if (tape_bytes)
+        *tape_bytes = (int64_t)(state_bytes * (size_t)(T.n_ck + 1) + seg_bytes * (size_t)T.every * (size_t)T.n_buf);
     return OC_OK;
 }
 

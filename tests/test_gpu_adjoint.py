@@ -20,13 +20,15 @@ from opencloth_gb300 import ClothDesc, ClothSolver
 pytestmark = pytest.mark.gpu
 
 
-def gpu_grads(case, every=10, executor="auto", cg_tol=1e-6):
+def gpu_grads(case, every=10, executor="auto", cg_tol=1e-6, budget=0, info=None):
     desc = ClothDesc(n_vertices=len(case["X"]), springs=case["springs"], pinned=case["pins"], cg_max_iter=500,
                      cg_tol=cg_tol)
     with ClothSolver(desc, executor=executor) as s:
         s.set_ext_force(case["ext"])
         s.set_state(case["X"], case["V0"], np.zeros_like(case["X"]))
-        s.tape_forward(DT, case["steps"], every)
+        s.tape_forward(DT, case["steps"], every, budget)
+        if info is not None:
+            info.append(s.tape_info())
         X, _, _ = s.get_state()
         gX = 2.0 * (X - case["target"]) / len(X)
         g = s.tape_backward(gX)
@@ -106,6 +108,20 @@ def test_checkpoint_interval_does_not_change_gradients(case):
     ga, _ = gpu_grads(case, every=1)
     gb, _ = gpu_grads(case, every=13)
     gc, _ = gpu_grads(case, every=case["steps"])
+    for k in ga:
+        assert np.array_equal(ga[k], gb[k]) and np.array_equal(ga[k], gc[k]), k
+
+
+def test_kept_segments_do_not_change_gradients(case):
+    """With a byte budget the taped forward keeps its last segments' step states and the
+    reverse pass walks them without a recompute: the same gradients bit for bit, whether
+    no segment, some or all of them are kept."""
+    info = []
+    ga, _ = gpu_grads(case, every=10, info=info)
+    base = info[-1][1]
+    gb, _ = gpu_grads(case, every=10, budget=3 * base, info=info)
+    gc, _ = gpu_grads(case, every=10, budget=1 << 30, info=info)
+    assert base < info[1][1] < info[2][1]  # some segments kept, then all
     for k in ga:
         assert np.array_equal(ga[k], gb[k]) and np.array_equal(ga[k], gc[k]), k
 
