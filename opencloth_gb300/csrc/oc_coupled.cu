@@ -71,7 +71,7 @@ __device__ __forceinline__ void block_apply(float n0, float n1, float n2, float 
     a2 = a2 + (beta * e2 + g * n2);
 }
 
-__global__ void __launch_bounds__(kThreads) k_cpl_assemble(const StepArgs a) {
+__global__ void __launch_bounds__(kThreads, 4) k_cpl_assemble(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstParams& ip = a.inst[bi.inst];
