@@ -287,6 +287,13 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def _traffic(kernel: str, workload: str):
+    """ncu's DRAM bytes per launch of the kernel on the workload, from its summary in
+    profiles/ (None when no capture exists)."""
+    tpath = ROOT / "profiles" / f"{kernel}_{workload}.traffic.json"
+    return json.loads(tpath.read_text()).get("dram_bytes_per_launch") if tpath.exists() else None
+
+
 def _dominant_roofline(prof: dict, peak: float, workload: str) -> dict:
     """Roofline of the kernel with the largest share of the step: its algorithmic bytes
     (reported by the library for the instances still iterating) over its CUDA-event
@@ -295,10 +302,7 @@ def _dominant_roofline(prof: dict, peak: float, workload: str) -> dict:
     n = max(prof[dom]["launches"], 1)
     secs = prof[dom]["ms_total"] / 1e3
     achieved = prof[dom]["bytes"] / secs / 1e9
-    traffic = None
-    tpath = ROOT / "profiles" / f"{dom}_{workload}.traffic.json"
-    if tpath.exists():
-        traffic = json.loads(tpath.read_text()).get("dram_bytes_per_launch")
+    traffic = _traffic(dom, workload)
     return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_launch": prof[dom]["bytes"] / n,
             "avg_launch_us": 1e6 * secs / n}
@@ -607,6 +611,7 @@ def measure_fem(name: str, seed: int, local: int, solves: int) -> dict:
         "roofline": {"bound": "hbm", "kernel": "k_bsr_spmv", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "algorithmic_bytes_per_launch": spmv["bytes"] / max(spmv["launches"], 1),
                      "avg_launch_us": 1e3 * spmv["ms_total"] / max(spmv["launches"], 1),
+                     "traffic": _traffic("k_bsr_spmv", name),
                      "peak_source": "measured" if peaks_path.exists() else "fallback"},
         "kernels": {k: {"avg_us": 1e3 * v["ms_total"] / max(v["launches"], 1), "launches": v["launches"]}
                     for k, v in prof.items()},
