@@ -1,7 +1,9 @@
 // C ABI (include/opencloth_gb.h): handle lifetime, state transfer, and the three ways
-// of running a step — a CUDA graph whose CG loop is a device-driven WHILE node, the
-// same kernels launched directly with the loop driven from the host, and the plain
-// one-cloth-per-launch sequence.
+// of running a step — a CUDA graph (the assemblies; the CG of up to 16 streamed cloths
+// as one cooperative launch, of more as a device-driven WHILE node; the resident
+// buckets beside them), the same kernels launched directly with the loop driven from
+// the host, and the plain one-cloth-per-launch sequence.  Also the adjoint tape, the
+// stencil refit after new spring parameters, and the interaction entry points.
 #include <cuda_runtime.h>
 
 #include <algorithm>

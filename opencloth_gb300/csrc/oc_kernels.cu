@@ -1,5 +1,5 @@
-// Streamed executor: the implicit step as four kernels over a ragged batch, and the
-// passes after it.
+// Streamed executor: the implicit step's kernels over a ragged batch, and the passes
+// after it.
 //
 //   k_assemble   ComputeForces (IMP:698-735) as a per-vertex gather over the
 //                incidence CSR, CalcForceDerivatives for spring i (IMP:737-772),
@@ -8,6 +8,8 @@
 //   k_assemble_grid  the same for grid cloths, with the neighbours from a stencil
 //   k_cg_dir     [d = r + beta d]; alpha = delta_new / d.(A d)    (IMP:320-321, 327)
 //   k_cg_update  x += alpha d; r -= alpha A d; delta_new = r.r     (IMP:322-326)
+//   k_cg_persist the CG loop of up to 16 cloths and their update in one cooperative
+//                launch (the two passes above, grid barriers between them)
 //   k_integrate  V += dV dt; X += dt V; ground clamp               (IMP:790-797)
 //                [+ EllipsoidCollision, IMP:824-848]
 //   k_provot     ApplyProvotDynamicInverse as a per-vertex gather   (IMP:800-823)
@@ -21,7 +23,8 @@
 // Reductions are deterministic: each block writes one FP64 partial; the last block of
 // an instance to finish (atomic ticket) sums that instance's partials in a fixed order
 // and updates the instance's CG scalars.  The last block of the whole grid sets the
-// CUDA-graph WHILE condition to "some instance still iterating".
+// CUDA-graph WHILE condition to "some instance still iterating".  k_cg_persist forms
+// the same sums in the same order at its grid barriers.
 #include <algorithm>
 
 #include <cuda_runtime.h>
