@@ -266,6 +266,24 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(v: float, world: int, device: str = "cuda") -> float:
+    """The maximum of v over the ranks (the timed region's length is the slowest rank's);
+    device "cpu" for a gloo group."""
+    if world == 1:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_value(vertices_per_rank: int, steps: int, world: int, ms: float) -> float:
+    """Whole-job vertex-steps/s: every rank's vertices times the steps, over the slowest
+    rank's time (weak scaling: each rank steps its own replica)."""
+    return vertices_per_rank * steps * world / (ms / 1e3)
+
+
 def run_reference(args) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
@@ -344,12 +362,8 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(v: float) -> float:
-        if world == 1:
-            return v
-        t = torch.tensor([v], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+    def slowest(v: float) -> float:
+        return max_over_ranks(v, world)
 
     barrier()
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -360,10 +374,10 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
         ev1.record(stream)
         ev1.synchronize()
     barrier()
-    ms = max_over_ranks(ev0.elapsed_time(ev1))
+    ms = slowest(ev0.elapsed_time(ev1))
     launches = solver.launch_count() - l0
     iters, rr, flags = solver.stats()
-    value = nv * steps * world / (ms / 1e3)
+    value = aggregate_value(nv, steps, world, ms)
 
     prof = solver.profile(DT, 3)
     peaks_path = ROOT / "MEASURED_PEAKS.json"
@@ -398,8 +412,8 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         solver.step_host(Xh, Vh, DT, 1)
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e = {"value": nv * e2e_steps * world / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 24 * nv,
+    e2e_s = slowest(time.perf_counter() - t0)
+    e2e = {"value": aggregate_value(nv, e2e_steps, world, 1e3 * e2e_s), "unit": METRIC, "h2d_bytes_per_step": 24 * nv,
            "d2h_bytes_per_step": 24 * nv, "steps": e2e_steps}
     solver.close()
 
@@ -416,8 +430,8 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
         plain.step(DT, plain_steps)
         ev1.record(stream)
         ev1.synchronize()
-        pms = max_over_ranks(ev0.elapsed_time(ev1))
-        plain_value = nv * plain_steps * world / (pms / 1e3)
+        pms = slowest(ev0.elapsed_time(ev1))
+        plain_value = aggregate_value(nv, plain_steps, world, pms)
         plain.close()
         plain_gpu = {"value": plain_value, "unit": METRIC, "ms_per_step": pms / plain_steps, "steps": plain_steps,
                      "speedup": value / plain_value}
