@@ -596,8 +596,28 @@ def measure_fem(name: str, seed: int, local: int, solves: int) -> dict:
     prof = s.profile(2)
     peaks_path = ROOT / "MEASURED_PEAKS.json"
     peak = float(json.loads(peaks_path.read_text())["hbm_gbs"]) if peaks_path.exists() else 6800.0
-    spmv = prof["k_bsr_spmv"]
-    achieved = spmv["bytes"] / (spmv["ms_total"] / 1e3) / 1e9
+    # The dominant kernel: the streamed matrix-vector pass, or the resident CG when every
+    # system runs on chip (the demo's 176-row bodies).
+    kname = max(("k_bsr_spmv", "k_bsr_resident"), key=lambda k: prof.get(k, {"ms_total": 0.0})["ms_total"])
+    dom = prof[kname]
+    achieved = dom["bytes"] / (dom["ms_total"] / 1e3) / 1e9 if dom["ms_total"] > 0 else 0.0
+    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "algorithmic_bytes_per_launch": dom["bytes"] / max(dom["launches"], 1),
+            "avg_launch_us": 1e3 * dom["ms_total"] / max(dom["launches"], 1),
+            "traffic": _traffic(kname, name),
+            "peak_source": "measured" if peaks_path.exists() else "fallback"}
+    if kname == "k_bsr_resident":
+        # The iterations run in shared memory, so the HBM figure counts the blocks and rows
+        # read once and the solution written.  Beside it: the solve's algorithmic bytes in
+        # the streamed layout (pack 72 B/block + 8 B/row, init 40 B/block + 61 B/row, per
+        # iteration 40 B/block + 162 B/row) over the resident kernel's time.
+        nnzb_r = float(len(blocks))
+        per_solve = 72 * nnzb_r + 8 * rows + 40 * nnzb_r + 61 * rows + iters * (40 * nnzb_r + 162 * rows)
+        secs = dom["ms_total"] / 1e3 / max(dom["launches"], 1)
+        eq = per_solve / secs / 1e9 if secs > 0 else 0.0
+        roof["equivalent"] = {"achieved": eq, "frac": eq / peak, "unit": "GB/s", "bytes_per_solve": per_solve,
+                              "note": "the solve's algorithmic bytes in the streamed layout over k_bsr_resident's "
+                                      "time (the iterations run in shared memory)"}
     # End to end: host blocks, b and V in, solve, V out, every solve.
     e2e_n = max(3, min(solves, 10))
     Vh = np.empty_like(V0)
@@ -622,11 +642,7 @@ def measure_fem(name: str, seed: int, local: int, solves: int) -> dict:
         "solves_per_s": 1e3 / ms, "solves": solves, "gpu_launches": int(launches), "clocks": clocks.summary(),
         "e2e": {"value": rows * iters / e2e_s, "unit": "block-row-iterations/s",
                 "h2d_bytes_per_solve": int(blocks.nbytes + b.nbytes + V0.nbytes), "d2h_bytes_per_solve": int(V0.nbytes)},
-        "roofline": {"bound": "hbm", "kernel": "k_bsr_spmv", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "algorithmic_bytes_per_launch": spmv["bytes"] / max(spmv["launches"], 1),
-                     "avg_launch_us": 1e3 * spmv["ms_total"] / max(spmv["launches"], 1),
-                     "traffic": _traffic("k_bsr_spmv", name),
-                     "peak_source": "measured" if peaks_path.exists() else "fallback"},
+        "roofline": roof,
         "kernels": {k: {"avg_us": 1e3 * v["ms_total"] / max(v["launches"], 1), "launches": v["launches"]}
                     for k, v in prof.items()},
         "cpu_baseline": {"value": cpu_rows * iters / cpu_s, "unit": "block-row-iterations/s", "cores": 1,

@@ -276,7 +276,11 @@ typedef struct oc_bsr_desc {
 typedef struct oc_bsr_solver oc_bsr_solver;
 
 /* Validate and upload the sparsity of n_systems systems (options: device, stream,
- * use_graph).  Fails with OC_ERR_BAD_INDEX / OC_ERR_INVALID_ARGUMENT on bad patterns. */
+ * use_graph, executor).  Executors: OC_EXEC_AUTO solves each system of up to 256 rows
+ * whose blocks fit in one CTA's shared memory in one CTA (the whole CG on chip, the
+ * streamed path's bits) and streams the others; OC_EXEC_STREAMED (and OC_EXEC_PLAIN)
+ * stream every system; OC_EXEC_RESIDENT fails with OC_ERR_UNSUPPORTED unless every
+ * system fits.  Fails with OC_ERR_BAD_INDEX / OC_ERR_INVALID_ARGUMENT on bad patterns. */
 oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_options* opts, oc_bsr_solver** out);
 void oc_bsr_destroy(oc_bsr_solver* s);
 const char* oc_bsr_last_error(const oc_bsr_solver* s);

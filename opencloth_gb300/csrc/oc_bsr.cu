@@ -16,6 +16,9 @@
 //   k_bsr_spmv    p = r + d4 p (not in the first pass, FEM:913-917, rebuilt for the
 //                 neighbours from their r and p); q = A p; d = r.r, d2 = p.q  (FEM:865-883)
 //   k_bsr_update  d3 = d / d2; V += d3 p; r -= d3 q; d1 = r.r  (FEM:885-901), d4 = d1 / d
+//   k_bsr_resident  all of the above for a system of up to 256 rows whose blocks fit in
+//                 shared memory, in one CTA: the blocks are read once, the iterations run
+//                 on chip, with the streamed kernels' bits (the default executor's choice)
 //
 // FP32 vector arithmetic in the reference's order (--fmad=false); the dot products sum
 // FP32 per-row terms in error-free float pairs within a warp and FP64 above, and
@@ -40,6 +43,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kRowsPerBlock = 256;  // one row per thread: enough warps to cover the gathers
 constexpr int kSortWindow = 2048;   // rows reordered by block count within windows of this size
+static_assert(kSortWindow >= kThreads, "a resident system's rows are sorted as one window");
 
 struct BsrState {
     double d, d2, d1;
@@ -53,9 +57,11 @@ struct BsrState {
 struct BsrParams {
     int32_t imax;
     float tiny;
-    int32_t blk0, nblk;  // the system's blocks in the block table
+    int32_t blk0, nblk;  // the system's blocks in the streamed block table (none if resident)
     int64_t row0;         // first (global) row
     int64_t slice0;       // first slice
+    int32_t n_rows;
+    int32_t pad_;
 };
 
 struct BsrArgs {
@@ -322,6 +328,264 @@ __global__ void __launch_bounds__(kThreads) k_bsr_update(const BsrArgs a) {
     bsr_finish<1>(a, bi.gblk, bi.inst, active, pd1, acc_zero());
 }
 
+// Dynamic shared memory of the resident CG: each row's new direction r + d4 p (a 16-byte
+// record the neighbours gather; x passes through it during init), then the system's
+// blocks without padding: two float4 planes, component 8 and an 8-bit local column (a
+// resident system has at most 256 rows).
+__host__ __device__ constexpr size_t resident_vec_bytes(int threads) { return 16 * (size_t)threads; }
+constexpr int kResSlots = 4;  // slots of a row multiplied together in the resident loop
+constexpr int kResMaxDeg = 64;  // blocks of a resident system's longest row (bounds its offset table)
+// ... and each warp's offset of each slot (ints, stride = the largest row's block count).
+__host__ __device__ constexpr size_t resident_smem_bytes(int threads, int64_t nnzb, int stride) {
+    return resident_vec_bytes(threads) + ((size_t)nnzb * 37 + 15) / 16 * 16 + 4 * (size_t)(threads / 32) * stride;
+}
+
+// The first half of block_sum_acc: each warp's pair, reduced by the same shuffle tree,
+// becomes one FP64 value in wacc[warp] (read after a barrier).
+__device__ __forceinline__ void warp_partial(Acc v, double* wacc) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        Acc u;
+        u.s = __shfl_down_sync(0xffffffffu, v.s, o);
+        u.c = __shfl_down_sync(0xffffffffu, v.c, o);
+        v = acc_merge(v, u);
+    }
+    if ((threadIdx.x & 31) == 0) wacc[threadIdx.x >> 5] = (double)v.s + (double)v.c;
+}
+
+// The second half, by one thread: block_sum_acc's shuffle tree over at most 8 warp
+// values.  The tree's first two levels add zeros (lanes 8-31), which leaves each value
+// unchanged (a warp value is never -0: its pair starts at +0), so lane 0's result is
+// ((w0 + w4) + (w2 + w6)) + ((w1 + w5) + (w3 + w7)): the same bits.
+__device__ __forceinline__ double sum_warp_partials(const double* wacc, int nw) {
+    double w[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) w[i] = i < nw ? wacc[i] : 0.0;
+    return ((w[0] + w[4]) + (w[2] + w[6])) + ((w[1] + w[5]) + (w[3] + w[7]));
+}
+
+// The whole solve of one small system in one CTA: the system's blocks are read once
+// from the caller's CSR into shared memory (the pack), then init and every iteration
+// run on chip with the streamed kernels' arithmetic.  Thread t owns internal row
+// row0 + t, as in the system's only block of the streamed path, and the dot products
+// go through the same block sums, so the results are the streamed path's bits.
+//
+// Shared-memory layout of the blocks (jagged diagonals): a system's rows are sorted by
+// decreasing block count, so in each warp the lanes whose row has more than j blocks
+// are lanes 0 .. cnt_j - 1.  Slot j of the warp's rows is stored as those cnt_j entries,
+// after the warp's slots 0 .. j-1; cnt_j is a ballot over the warp.
+// map[e] places the caller's block e: its internal local row (bits 0-7), its slot in the
+// row (bits 8-15) and its internal local column (bits 16-23), so the pack reads the
+// caller's blocks in order, coalesced.
+__global__ void __launch_bounds__(kThreads) k_bsr_resident(const BsrArgs a, const int32_t* ids, int64_t nnzb_max,
+                                                           const uint32_t* map, int stride) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ float s_d3, s_d4;
+    __shared__ int s_wcount[kThreads / 32];
+    __shared__ double s_w0[kThreads / 32], s_w1[kThreads / 32], s_w2[kThreads / 32];
+    static_assert(kThreads / 32 <= 8, "sum_warp_partials takes at most 8 warps");
+    float4* s_n4 = reinterpret_cast<float4*>(smem);
+    float4* s_b0 = s_n4 + blockDim.x;
+    float4* s_b1 = s_b0 + nnzb_max;
+    float* s_b8 = reinterpret_cast<float*>(s_b1 + nnzb_max);
+    uint8_t* s_col = reinterpret_cast<uint8_t*>(s_b8 + nnzb_max);
+    int* s_pre = reinterpret_cast<int*>(smem + resident_smem_bytes(blockDim.x, nnzb_max, 0));
+    constexpr unsigned kFull = 0xffffffffu;
+
+    const int k = ids[blockIdx.x];
+    const BsrParams& sp = a.sys[k];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const bool valid = t < sp.n_rows;
+    const int64_t g = sp.row0 + t;
+    bool fx = true;
+    int n = 0;
+    float x0 = 0.0f, x1 = 0.0f, x2 = 0.0f;
+    if (valid) {
+        fx = a.fixed[g] != 0;
+        n = a.deg[g];
+    }
+    const int width = __reduce_max_sync(kFull, n);
+    const int wsum = __reduce_add_sync(kFull, n);
+    if (lane == 0) s_wcount[w] = wsum;
+    __syncthreads();
+    int base = 0;
+    for (int u = 0; u < w; ++u) base += s_wcount[u];
+    {  // each warp's slot offsets, then k_bsr_pack into shared memory
+        int pre = base;
+        for (int j = 0; j < width; ++j) {
+            const int cnt = __popc(__ballot_sync(kFull, n > j));
+            if (lane == 0) s_pre[w * stride + j] = pre;
+            pre += cnt;
+        }
+        __syncthreads();
+        const int64_t e1 = a.row_ptr[sp.row0 + sp.n_rows];
+#pragma unroll 4
+        for (int64_t e = a.row_ptr[sp.row0] + t; e < e1; e += blockDim.x) {
+            const uint32_t mp = __ldg(map + e);
+            const int i = mp & 255, j = (mp >> 8) & 255;
+            const float* m = a.cblk + 9 * (size_t)e;
+            const int pos = s_pre[(i >> 5) * stride + j] + (i & 31);
+            s_b0[pos] = make_float4(m[0], m[1], m[2], m[3]);
+            s_b1[pos] = make_float4(m[4], m[5], m[6], m[7]);
+            s_b8[pos] = m[8];
+            s_col[pos] = (uint8_t)(mp >> 16);
+        }
+    }
+    if (valid) {
+        x0 = a.x[0][g];
+        x1 = a.x[1][g];
+        x2 = a.x[2][g];
+        s_n4[t] = make_float4(x0, x1, x2, 0.0f);  // x, for init's gathers
+    }
+    __syncthreads();
+    // k_bsr_init: r = b - A V, p = r.
+    const bool act = valid && !fx;
+    float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+    if (act) {
+        r0 = a.b[3 * g];
+        r1 = a.b[3 * g + 1];
+        r2 = a.b[3 * g + 2];
+    }
+    {
+        int pre = base;
+        for (int j = 0; j < width; ++j) {
+            const int cnt = __popc(__ballot_sync(kFull, n > j));
+            if (act && j < n) {
+                const int pos = pre + lane;
+                const float4 u = s_b0[pos], v = s_b1[pos];
+                const float m[9] = {u.x, u.y, u.z, u.w, v.x, v.y, v.z, v.w, s_b8[pos]};
+                const float4 xc = s_n4[s_col[pos]];
+                float o0, o1, o2;
+                block_mv(m, xc.x, xc.y, xc.z, o0, o1, o2);
+                r0 = r0 - o0;
+                r1 = r1 - o1;
+                r2 = r2 - o2;
+            }
+            pre += cnt;
+        }
+    }
+    float p0 = r0, p1 = r1, p2 = r2;
+    double d = 0.0, d1 = 0.0, d2 = 0.0;
+    float d3 = 0.0f, d4 = 0.0f;
+    const double tiny = (double)sp.tiny;
+    const int nw = (int)(blockDim.x >> 5);
+    // Five barriers an iteration: after the directions, the products (d2), d3, the
+    // update (d1) and d4; the last also orders this iteration's reads of the directions
+    // before the next iteration writes them.
+    for (int it = 0; it < sp.imax; ++it) {
+        const bool first = it == 0;
+        // The new direction of every row, fixed rows included (r = p = 0 there), by the
+        // expression the streamed pass evaluates for each neighbour and for its own row.
+        float n0 = p0, n1 = p1, n2 = p2;
+        if (!first) {
+            n0 = r0 + n0 * d4;
+            n1 = r1 + n1 * d4;
+            n2 = r2 + n2 * d4;
+        }
+        if (first) __syncthreads();  // init's reads of x are done (later: the barrier after d4)
+        if (valid) s_n4[t] = make_float4(n0, n1, n2, 0.0f);
+        __syncthreads();
+        // k_bsr_spmv
+        Acc pd = acc_zero(), pd2 = acc_zero();
+        float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f;
+        // Four slots at a time: their loads and products are independent, so they are
+        // issued together (a slot past the row's end reads entry 0, which every system
+        // with blocks has, and is not added); the sums still run in slot order.
+        int pre = base;
+        for (int j = 0; j < width; j += kResSlots) {
+            int pos[kResSlots];
+            bool ok[kResSlots];
+#pragma unroll
+            for (int u = 0; u < kResSlots; ++u) {
+                const int cnt = __popc(__ballot_sync(kFull, n > j + u));
+                ok[u] = act && j + u < n;
+                pos[u] = ok[u] ? pre + lane : 0;
+                pre += cnt;
+            }
+            float o[kResSlots][3];
+#pragma unroll
+            for (int u = 0; u < kResSlots; ++u) {
+                const float4 b0 = s_b0[pos[u]], b1 = s_b1[pos[u]];
+                const float m[9] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w, s_b8[pos[u]]};
+                const float4 nc = s_n4[s_col[pos[u]]];
+                block_mv(m, nc.x, nc.y, nc.z, o[u][0], o[u][1], o[u][2]);
+            }
+#pragma unroll
+            for (int u = 0; u < kResSlots; ++u) {
+                if (ok[u]) {
+                    q0 = q0 + o[u][0];
+                    q1 = q1 + o[u][1];
+                    q2 = q2 + o[u][2];
+                }
+            }
+        }
+        if (act) {
+            acc_add(pd, r0 * r0 + r1 * r1 + r2 * r2);
+            acc_add(pd2, n0 * q0 + n1 * q1 + n2 * q2);
+        }
+        // d = r.r is the previous update's d1: the same terms in the same order.
+        if (first) warp_partial(pd, s_w0);
+        warp_partial(pd2, s_w1);
+        __syncthreads();
+        if (t == 0) {  // bsr_scalars<0>
+            const double t0 = first ? sum_warp_partials(s_w0, nw) : d1;
+            const double t1 = sum_warp_partials(s_w1, nw);
+            d = t0;
+            d2 = t1;
+            double dd2 = d2;
+            if (fabs(dd2) < tiny) dd2 = tiny;  // FEM:885-886
+            s_d3 = (float)(t0 / dd2);
+        }
+        __syncthreads();  // d3, and every row's reads of r and p are done
+        d3 = s_d3;
+        // k_bsr_update
+        Acc pd1 = acc_zero();
+        if (act) {
+            x0 = x0 + n0 * d3;  // V += p d3, FEM:895
+            x1 = x1 + n1 * d3;
+            x2 = x2 + n2 * d3;
+            r0 = r0 - q0 * d3;  // r -= q d3, FEM:896
+            r1 = r1 - q1 * d3;
+            r2 = r2 - q2 * d3;
+            p0 = n0;
+            p1 = n1;
+            p2 = n2;
+            acc_add(pd1, r0 * r0 + r1 * r1 + r2 * r2);
+        }
+        warp_partial(pd1, s_w2);
+        __syncthreads();
+        if (t == 0) {  // bsr_scalars<1>
+            const double t2 = sum_warp_partials(s_w2, nw);
+            d1 = t2;
+            double dd = d;
+            if (fabs(dd) < tiny) dd = tiny;  // FEM:908-909
+            s_d4 = (float)(t2 / dd);
+        }
+        __syncthreads();
+        d4 = s_d4;
+    }
+    if (valid) {
+        if (!fx) {
+            a.x[0][g] = x0;
+            a.x[1][g] = x1;
+            a.x[2][g] = x2;
+        }
+        a.r4[g] = make_float4(r0, r1, r2, 0.0f);
+        a.p4[g] = make_float4(p0, p1, p2, 0.0f);
+    }
+    if (t == 0) {
+        BsrState& st = a.state[k];
+        st.d = d;
+        st.d1 = d1;
+        st.d2 = d2;
+        st.d3 = d3;
+        st.d4 = d4;
+        st.iter = sp.imax;
+        st.active = 0;
+        st.ticket = 0;
+    }
+}
+
 // Launch shapes of the matrix-vector pass (unroll of the slot loop, minimum resident
 // blocks per SM, which caps the registers).  OC_BSR_VARIANT picks one; the default was
 // chosen by measurement on GB300.
@@ -336,7 +600,7 @@ SpmvFn spmv_variant() {
         case 5: return k_bsr_spmv<2, 4>;
         case 6: return k_bsr_spmv<4, 4>;
         case 7: return k_bsr_spmv<2, 1>;
-        default: return k_bsr_spmv<1, 8>;  // fastest on both the 386k-row mesh and the 4096-body batch
+        default: return k_bsr_spmv<1, 8>;  // fastest on the 386k-row mesh and on the streamed 4096-body batch
     }
 }
 
@@ -369,6 +633,15 @@ struct oc_bsr_solver {
     int64_t launches = 0;
     unsigned long long* h_loop = nullptr;
     SpmvFn spmv = nullptr;
+    // Systems solved by k_bsr_resident (one CTA each) and its launch shape.
+    int32_t n_res = 0;
+    int32_t* d_res_ids = nullptr;
+    int32_t res_threads = 0;
+    int64_t res_nnzb_max = 0;  // blocks of the largest resident system
+    int32_t res_stride = 0;    // blocks of the longest row of a resident system
+    uint32_t* d_res_map = nullptr;
+    size_t res_smem = 0;
+    int64_t st_rows = 0, st_nnzb = 0, res_rows = 0, res_nnzb = 0;  // streamed / resident sizes
     std::string err;
 };
 
@@ -421,17 +694,17 @@ void launch(void (*k)(BsrArgs), const BsrArgs& a, int n, cudaStream_t stream) {
     if (n > 0) k<<<n, kThreads, 0, stream>>>(a);
 }
 
+void launch_resident(const oc_bsr_solver* s, const BsrArgs& a) {
+    k_bsr_resident<<<s->n_res, s->res_threads, s->res_smem, s->stream>>>(a, s->d_res_ids, s->res_nnzb_max,
+                                                                        s->d_res_map, s->res_stride);
+}
+
 oc_status bsr_build_graph(oc_bsr_solver* s) {
     cudaGraph_t g = nullptr;
     BSR_TRY(cudaGraphCreate(&g, 0));
     s->graph = g;
-    // The loop condition starts every launch at "some system iterates" (nothing before
-    // the loop sets it); the last block of each update pass sets it from then on.
-    cudaGraphConditionalHandle handle = 0;
-    BSR_TRY(cudaGraphConditionalHandleCreate(&handle, g, s->any_iter ? 1u : 0u, cudaGraphCondAssignDefault));
     BsrArgs a = s->args;
-    a.use_cond = 1;
-    a.cond = (unsigned long long)handle;
+    a.use_cond = 0;
     void* params[] = {&a};
     auto kp = [&](void (*k)(BsrArgs)) {
         cudaKernelNodeParams p{};
@@ -442,7 +715,31 @@ oc_status bsr_build_graph(oc_bsr_solver* s) {
         p.kernelParams = params;
         return p;
     };
-    cudaGraphNode_t n_reset, n_pack, n_init, n_loop, n_spmv, n_upd;
+    cudaGraphNode_t n_reset, n_pack, n_init, n_loop, n_spmv, n_upd, n_res;
+    if (s->n_res > 0) {  // independent of the streamed systems' nodes
+        const int32_t* ids = s->d_res_ids;
+        int64_t nnzb_max = s->res_nnzb_max;
+        const uint32_t* map = s->d_res_map;
+        int stride = s->res_stride;
+        void* rparams[] = {&a, &ids, &nnzb_max, &map, &stride};
+        cudaKernelNodeParams p{};
+        p.func = (void*)k_bsr_resident;
+        p.gridDim = dim3((unsigned)s->n_res);
+        p.blockDim = dim3((unsigned)s->res_threads);
+        p.sharedMemBytes = (unsigned)s->res_smem;
+        p.kernelParams = rparams;
+        BSR_TRY(cudaGraphAddKernelNode(&n_res, g, nullptr, 0, &p));
+    }
+    if (s->n_blocks == 0) {  // every system resident: no loop (a conditional handle needs its node)
+        BSR_TRY(cudaGraphInstantiate(&s->exec, g, 0));
+        return OC_OK;
+    }
+    // The loop condition starts every launch at "some system iterates" (nothing before
+    // the loop sets it); the last block of each update pass sets it from then on.
+    cudaGraphConditionalHandle handle = 0;
+    BSR_TRY(cudaGraphConditionalHandleCreate(&handle, g, s->any_iter ? 1u : 0u, cudaGraphCondAssignDefault));
+    a.use_cond = 1;
+    a.cond = (unsigned long long)handle;
     cudaMemsetParams mp{};
     mp.dst = a.unfinished;
     mp.value = 0;
@@ -541,6 +838,13 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
     std::vector<BlockInfo> blocks;
     std::vector<int64_t> slice_ptr;
     std::vector<int32_t> width;
+    std::vector<int32_t> res_ids;
+    int smem_optin = 0;
+    BSR_CREATE_TRY(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device));
+    // Room for the kernel's static shared memory (block sums and the two broadcast scalars).
+    const size_t smem_cap = smem_optin > 1024 ? (size_t)smem_optin - 1024 : 0;
+    auto who_of = [](int32_t k) { return "system " + std::to_string(k) + ": "; };
+    if (o.executor < OC_EXEC_AUTO || o.executor > OC_EXEC_PLAIN) return bail(OC_ERR_INVALID_ARGUMENT);
     s->row_off.assign(n_systems + 1, 0);
     s->nnz_off.assign(n_systems + 1, 0);
     int64_t slots = 0;
@@ -551,20 +855,10 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
         s->nnz_off[k + 1] = e0 + d.nnzb;
         BsrParams& sp = sys[k];
         sp.imax = d.cg_max_iter;
-        s->any_iter = s->any_iter || d.cg_max_iter > 0;
         sp.tiny = d.tiny;
         sp.row0 = r0;
+        sp.n_rows = d.n_rows;
         sp.slice0 = (int64_t)slice_ptr.size();
-        sp.blk0 = (int32_t)blocks.size();
-        sp.nblk = (d.n_rows + kRowsPerBlock - 1) / kRowsPerBlock;
-        for (int32_t b = 0; b < sp.nblk; ++b) {
-            BlockInfo bi;
-            bi.inst = k;
-            bi.gblk = (int32_t)blocks.size();
-            bi.v_begin = r0 + (int64_t)b * kRowsPerBlock;
-            bi.v_end = std::min<int64_t>(r0 + d.n_rows, bi.v_begin + kRowsPerBlock);
-            blocks.push_back(bi);
-        }
         std::vector<int32_t> order(d.n_rows);
         for (int32_t r = 0; r < d.n_rows; ++r) {
             row_ptr.push_back((int32_t)(e0 + d.row_ptr[r + 1]));
@@ -590,6 +884,39 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
             slice_ptr.push_back(slots);
             width.push_back(w);
             slots += w;
+        }
+        // A system of one block of rows whose blocks fit in shared memory runs resident.
+        int32_t maxdeg = 0;
+        for (int32_t r = 0; r < d.n_rows; ++r) maxdeg = std::max(maxdeg, degree(r));
+        const bool fits = d.n_rows <= kThreads && maxdeg <= kResMaxDeg &&
+                          resident_smem_bytes(kThreads, d.nnzb, kResMaxDeg) <= smem_cap;
+        if (o.executor == OC_EXEC_RESIDENT && !fits) {
+            bsr_fail(s, OC_ERR_UNSUPPORTED, who_of(k) + "too large for the resident executor");
+            return bail(OC_ERR_UNSUPPORTED);
+        }
+        if (fits && o.executor != OC_EXEC_STREAMED && o.executor != OC_EXEC_PLAIN) {
+            sp.blk0 = 0;
+            sp.nblk = 0;
+            res_ids.push_back(k);
+            s->res_nnzb_max = std::max<int64_t>(s->res_nnzb_max, d.nnzb);
+            s->res_stride = std::max(s->res_stride, std::max(maxdeg, 1));
+            s->res_threads = std::max(s->res_threads, (d.n_rows + 31) / 32 * 32);
+            s->res_rows += d.n_rows;
+            s->res_nnzb += d.nnzb;
+            continue;
+        }
+        s->any_iter = s->any_iter || d.cg_max_iter > 0;
+        s->st_rows += d.n_rows;
+        s->st_nnzb += d.nnzb;
+        sp.blk0 = (int32_t)blocks.size();
+        sp.nblk = (d.n_rows + kRowsPerBlock - 1) / kRowsPerBlock;
+        for (int32_t b = 0; b < sp.nblk; ++b) {
+            BlockInfo bi;
+            bi.inst = k;
+            bi.gblk = (int32_t)blocks.size();
+            bi.v_begin = r0 + (int64_t)b * kRowsPerBlock;
+            bi.v_end = std::min<int64_t>(r0 + d.n_rows, bi.v_begin + kRowsPerBlock);
+            blocks.push_back(bi);
         }
     }
     s->n_slots = slots;
@@ -670,6 +997,24 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
     BSR_CREATE_TRY(cudaMemset(a.grid_ticket, 0, sizeof(uint32_t)));
     BSR_CREATE_TRY(cudaMemset(a.loop_count, 0, sizeof(unsigned long long)));
     BSR_CREATE_TRY(cudaMallocHost(&s->h_loop, sizeof(unsigned long long)));
+    s->n_res = (int32_t)res_ids.size();
+    if (s->n_res > 0) {
+        BSR_CREATE_TRY(bsr_upload(s, &s->d_res_ids, res_ids));
+        s->res_smem = resident_smem_bytes(s->res_threads, s->res_nnzb_max, s->res_stride);
+        // Where each caller block goes: internal local row, slot, internal local column.
+        std::vector<uint32_t> map((size_t)std::max<int64_t>(nnzb, 1), 0u);
+        for (int32_t k : res_ids) {
+            const oc_bsr_desc& d = descs[k];
+            const int64_t r0 = s->row_off[k], e0 = s->nnz_off[k];
+            for (int32_t r = 0; r < d.n_rows; ++r)
+                for (int32_t e = d.row_ptr[r]; e < d.row_ptr[r + 1]; ++e)
+                    map[(size_t)(e0 + e)] = (uint32_t)(perm[r0 + r] - r0) | (uint32_t)(e - d.row_ptr[r]) << 8 |
+                                            (uint32_t)(perm[r0 + d.col[e]] - r0) << 16;
+        }
+        BSR_CREATE_TRY(bsr_upload(s, &s->d_res_map, map));
+        BSR_CREATE_TRY(cudaFuncSetAttribute(k_bsr_resident, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)s->res_smem));
+    }
     BSR_CREATE_TRY(cudaDeviceSynchronize());
 #undef BSR_CREATE_TRY
     *out = s;
@@ -745,11 +1090,17 @@ oc_status oc_bsr_solve(oc_bsr_solver* s) {
             if (st != OC_OK) return st;
         }
         BSR_TRY(cudaGraphLaunch(s->exec, s->stream));
-        s->launches += 2;
+        s->launches += (s->n_blocks > 0 ? 2 : 0) + (s->n_res > 0 ? 1 : 0);
         return OC_OK;
     }
     BsrArgs a = s->args;
     a.use_cond = 0;
+    if (s->n_res > 0) {
+        launch_resident(s, a);
+        BSR_TRY(cudaGetLastError());
+        s->launches += 1;
+    }
+    if (s->n_blocks == 0) return OC_OK;
     BSR_TRY(cudaMemsetAsync(a.unfinished, 0, sizeof(int32_t), s->stream));
     launch(k_bsr_pack, a, s->n_blocks, s->stream);
     launch(k_bsr_init, a, s->n_blocks, s->stream);
@@ -782,15 +1133,20 @@ oc_status oc_bsr_profile(oc_bsr_solver* s, int32_t n_solves, int32_t max_kernels
     if (!bsr_valid(s) || n_solves < 0 || max_kernels < 0) return OC_ERR_INVALID_ARGUMENT;
     BSR_TRY(cudaSetDevice(s->device));
     // Algorithmic bytes of one launch, each array element once in the device layout (r and
-    // p are 16-byte records): pack 72 B per block (read and write 36) + 8 B per row; init
-    // 40 B per block (block + column) + 61 B per row (b, V, r and p out, fixed, row_ptr);
-    // spmv 40 B per block + 53 B per row (fixed, row_ptr, r, p in, q out); update 109 B
-    // per row (fixed, r, p, x, q in; x, r, p out).
-    const double nb = (double)s->nnzb, nr = (double)s->n_rows;
-    const char* kname[4] = {"k_bsr_pack", "k_bsr_init", "k_bsr_spmv", "k_bsr_update"};
-    const double kbytes[4] = {72.0 * nb + 8.0 * nr, 40.0 * nb + 61.0 * nr, 40.0 * nb + 53.0 * nr, 109.0 * nr};
-    double ms[4] = {0, 0, 0, 0};
-    int64_t cnt[4] = {0, 0, 0, 0};
+    // p are 16-byte records), over the systems the kernel runs: pack 72 B per block (read
+    // and write 36) + 8 B per row; init 40 B per block (block + column) + 61 B per row (b,
+    // V, r and p out, fixed, row_ptr); spmv 40 B per block + 53 B per row (fixed, row_ptr,
+    // r, p in, q out); update 109 B per row (fixed, r, p, x, q in; x, r, p out); resident
+    // 40 B per block (block + column, read once) + 85 B per row (row tables, fixed, b, V in
+    // and out, r and p out): its iterations stay on chip.
+    const double nb = (double)s->st_nnzb, nr = (double)s->st_rows;
+    const double rb = (double)s->res_nnzb, rr = (double)s->res_rows;
+    constexpr int K = 5;
+    const char* kname[K] = {"k_bsr_pack", "k_bsr_init", "k_bsr_spmv", "k_bsr_update", "k_bsr_resident"};
+    const double kbytes[K] = {72.0 * nb + 8.0 * nr, 40.0 * nb + 61.0 * nr, 40.0 * nb + 53.0 * nr, 109.0 * nr,
+                              40.0 * rb + 85.0 * rr};
+    double ms[K] = {0, 0, 0, 0, 0};
+    int64_t cnt[K] = {0, 0, 0, 0, 0};
     cudaEvent_t e0, e1;
     BSR_TRY(cudaEventCreate(&e0));
     BSR_TRY(cudaEventCreate(&e1));
@@ -801,7 +1157,10 @@ oc_status oc_bsr_profile(oc_bsr_solver* s, int32_t n_solves, int32_t max_kernels
     cudaError_t e = cudaMallocHost(&h, sizeof(int32_t));
     auto timed = [&](int k) -> cudaError_t {
         cudaError_t x = cudaEventRecord(e0, s->stream);
-        launch(kfn[k], a, s->n_blocks, s->stream);
+        if (k < 4)
+            launch(kfn[k], a, s->n_blocks, s->stream);
+        else
+            launch_resident(s, a);
         if (x == cudaSuccess) x = cudaGetLastError();
         if (x == cudaSuccess) x = cudaEventRecord(e1, s->stream);
         if (x == cudaSuccess) x = cudaEventSynchronize(e1);
@@ -812,7 +1171,9 @@ oc_status oc_bsr_profile(oc_bsr_solver* s, int32_t n_solves, int32_t max_kernels
         return x;
     };
     for (int32_t i = 0; i < n_solves && e == cudaSuccess; ++i) {
-        e = cudaMemsetAsync(a.unfinished, 0, sizeof(int32_t), s->stream);
+        if (s->n_res > 0) e = timed(4);
+        if (s->n_blocks == 0) continue;
+        if (e == cudaSuccess) e = cudaMemsetAsync(a.unfinished, 0, sizeof(int32_t), s->stream);
         if (e == cudaSuccess) e = timed(0);
         if (e == cudaSuccess) e = timed(1);
         for (;;) {
@@ -828,7 +1189,7 @@ oc_status oc_bsr_profile(oc_bsr_solver* s, int32_t n_solves, int32_t max_kernels
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return bsr_fail_cuda(s, e, "oc_bsr_profile");
     int32_t n = 0;
-    for (int k = 0; k < 4 && n < max_kernels; ++k, ++n) {
+    for (int k = 0; k < K && n < max_kernels; ++k, ++n) {
         if (names) {
             std::memset(names + 32 * n, 0, 32);
             std::strncpy(names + 32 * n, kname[k], 31);

@@ -174,9 +174,12 @@ class BsrSolver:
 
     ``systems``: dicts (or objects) with row_ptr, col, fixed, i_max, tolerance, tiny.
     ``set_system`` takes blocks (nnzb, 9), b and V (rows, 3), concatenated over the
-    systems; ``solve`` runs the CG; ``solution`` returns (V, residual)."""
+    systems; ``solve`` runs the CG; ``solution`` returns (V, residual).  ``executor``:
+    0 (auto: systems of up to 256 rows whose blocks fit in shared memory are solved by
+    one CTA each), 1 (every system streamed) or 2 (every system resident)."""
 
-    def __init__(self, systems: Sequence, device: int = 0, use_graph: bool = True, stream: int | None = None):
+    def __init__(self, systems: Sequence, device: int = 0, use_graph: bool = True, stream: int | None = None,
+                 executor: int = 0):
         self._lib = N.load()
         self._keep = []
         descs = (N.BsrDescC * len(systems))()
@@ -199,6 +202,7 @@ class BsrSolver:
         opts.device = device
         opts.use_graph = 1 if use_graph else 0
         opts.stream = stream
+        opts.executor = int(executor)
         h = C.c_void_p()
         st = self._lib.oc_bsr_create(descs, len(systems), C.byref(opts), C.byref(h))
         if st != N.OC_OK:

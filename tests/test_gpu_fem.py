@@ -7,7 +7,9 @@ Tolerances (stated here, used below):
   move d3 or d4 by an FP32 ulp.
 * Against the reference CG's own FP32 result (golden): within twice the reference's
   FP32-to-FP64 distance on that system, or 1e-6.
-* A system gives the same bits alone or in a batch, with or without the CUDA graph.
+* A system gives the same bits alone or in a batch, with or without the CUDA graph, and
+  solved by one CTA on chip (the resident kernel, systems of up to 256 rows) or by the
+  streamed kernels.
 """
 import numpy as np
 import pytest
@@ -25,8 +27,8 @@ def desc(sys_):
             "tolerance": sys_.tolerance, "tiny": sys_.tiny}
 
 
-def solve(systems, use_graph=True):
-    with BsrSolver([desc(s) for s in systems], use_graph=use_graph) as s:
+def solve(systems, use_graph=True, executor=0):
+    with BsrSolver([desc(s) for s in systems], use_graph=use_graph, executor=executor) as s:
         s.set_system(np.concatenate([x.blocks for x in systems]), np.concatenate([x.b for x in systems]),
                      np.concatenate([x.V for x in systems]))
         s.solve()
@@ -109,3 +111,44 @@ def test_validation():
     with pytest.raises(OcError) as e:
         BsrSolver([bad])
     assert e.value.status == 2
+
+
+def test_resident_gives_the_streamed_bits():
+    """The demo's 176-row systems run resident under the default executor; the 375-row
+    system is streamed beside them.  Every system gets the streamed executor's bits."""
+    systems = [fem_golden(t)[0] for t in FEM_CASES]
+    Vs, rs = solve(systems, executor=1)
+    Va, ra = solve(systems)
+    assert np.array_equal(Vs, Va) and np.array_equal(rs, ra)
+    Vn, rn = solve(systems, use_graph=False)
+    assert np.array_equal(Vs, Vn) and np.array_equal(rs, rn)
+    small = systems[:3]
+    Vr, rr = solve(small, executor=2)
+    n = sum(x.n for x in small)
+    assert np.array_equal(Vr, Vs[:n]) and np.array_equal(rr, rs[:n])
+    with pytest.raises(OcError) as e:
+        BsrSolver([desc(systems[3])], executor=2)  # 375 rows: more than one CTA's rows
+    assert e.value.status == 7
+
+
+def test_resident_iteration_counts_and_demo_mesh():
+    """i_max 0, 1 and 7 in one resident batch, and a generated 10 x 3 x 3 demo mesh, against
+    the oracle; the launch count is one kernel per solve."""
+    base = fem_golden("m30")[0]
+    systems = [oracle.BsrSystem(base.row_ptr, base.col, base.blocks, base.b, base.V, base.fixed, imax,
+                                base.tolerance, base.tiny) for imax in (0, 1, 7)]
+    g = fem_system(10, 3, 3, V=np.random.default_rng(5).normal(0.0, 0.2, (11 * 4 * 4, 3)))
+    systems.append(oracle.BsrSystem(g["row_ptr"], g["col"], g["blocks"], g["b"], g["V"], g["fixed"], 20))
+    with BsrSolver([desc(x) for x in systems], executor=2) as s:
+        s.set_system(np.concatenate([x.blocks for x in systems]), np.concatenate([x.b for x in systems]),
+                     np.concatenate([x.V for x in systems]))
+        s.solve()
+        V, r = s.solution()
+        assert s.launch_count() == 1
+    off = np.cumsum([0] + [x.n for x in systems])
+    for k, x in enumerate(systems):
+        Vo, ro = oracle.bsr_cg(x, dot_fp64=True)
+        assert rel_free(V[off[k]:off[k + 1]], Vo, x) <= 1e-6, k
+        if x.i_max == 0:
+            assert np.array_equal(V[off[k]:off[k + 1]], x.V)
+            assert np.abs(r[off[k]:off[k + 1]] - ro).max() <= 1e-6 * np.abs(ro).max()
