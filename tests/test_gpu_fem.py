@@ -152,3 +152,33 @@ def test_resident_iteration_counts_and_demo_mesh():
         if x.i_max == 0:
             assert np.array_equal(V[off[k]:off[k + 1]], x.V)
             assert np.abs(r[off[k]:off[k + 1]] - ro).max() <= 1e-6 * np.abs(ro).max()
+
+
+def test_resident_edge_systems_give_the_streamed_bits():
+    """Resident systems of different sizes in one launch (the shared-memory layout is
+    sized for the largest), a system whose rows are all fixed, one with no blocks and
+    one with i_max 0, beside a streamed system: the same bits as every system streamed."""
+    rng = np.random.default_rng(11)
+
+    def gen(dims, seed):
+        n = (dims[0] + 1) * (dims[1] + 1) * (dims[2] + 1)
+        g = fem_system(*dims, V=np.random.default_rng(seed).normal(0.0, 0.2, (n, 3)))
+        return oracle.BsrSystem(g["row_ptr"], g["col"], g["blocks"], g["b"], g["V"], g["fixed"], 20)
+
+    small, demo, big = gen((4, 2, 2), 1), gen((10, 3, 3), 2), gen((12, 5, 4), 3)
+    all_fixed = oracle.BsrSystem(small.row_ptr, small.col, small.blocks, small.b, small.V,
+                                 np.ones_like(small.fixed), 20)
+    n0 = 40
+    empty = oracle.BsrSystem(np.zeros(n0 + 1, np.int32), np.zeros(0, np.int32), np.zeros((0, 9), np.float32),
+                             rng.normal(0.0, 1.0, (n0, 3)), rng.normal(0.0, 1.0, (n0, 3)), np.zeros(n0, np.uint8), 2)
+    no_iter = oracle.BsrSystem(demo.row_ptr, demo.col, demo.blocks, demo.b, demo.V, demo.fixed, 0)
+    systems = [small, demo, all_fixed, big, empty, no_iter]
+    Vs, rs = solve(systems, executor=1)
+    Va, ra = solve(systems)
+    assert np.array_equal(Vs, Va, equal_nan=True) and np.array_equal(rs, ra, equal_nan=True)
+    off = np.cumsum([0] + [x.n for x in systems])
+    k = systems.index(all_fixed)
+    assert np.array_equal(Va[off[k]:off[k + 1]], all_fixed.V) and np.all(ra[off[k]:off[k + 1]] == 0.0)
+    for k in (0, 1, 3):
+        Vo, _ = oracle.bsr_cg(systems[k], dot_fp64=True)
+        assert rel_free(Va[off[k]:off[k + 1]], Vo, systems[k]) <= 1e-6, k
