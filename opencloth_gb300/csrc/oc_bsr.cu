@@ -329,16 +329,16 @@ __global__ void __launch_bounds__(kThreads) k_bsr_update(const BsrArgs a) {
 }
 
 // Dynamic shared memory of the resident CG: each row's new direction r + d4 p (a 16-byte
-// record the neighbours gather; x passes through it during init), then the system's
-// blocks without padding: two float4 planes, component 8 and an 8-bit local column (a
-// resident system has at most 256 rows).
+// record the neighbours gather; x passes through it during init); the system's blocks
+// without padding: two float4 planes, component 8 and an 8-bit local column (a resident
+// system has at most 256 rows); each warp's offset of each slot (ints, `stride` of them
+// per warp: the longest row's block count).
 __host__ __device__ constexpr size_t resident_vec_bytes(int threads) { return 16 * (size_t)threads; }
-constexpr int kResSlots = 4;  // slots of a row multiplied together in the resident loop
-constexpr int kResMaxDeg = 64;  // blocks of a resident system's longest row (bounds its offset table)
-// ... and each warp's offset of each slot (ints, stride = the largest row's block count).
 __host__ __device__ constexpr size_t resident_smem_bytes(int threads, int64_t nnzb, int stride) {
     return resident_vec_bytes(threads) + ((size_t)nnzb * 37 + 15) / 16 * 16 + 4 * (size_t)(threads / 32) * stride;
 }
+constexpr int kResSlots = 4;    // slots of a row multiplied together in the resident loop
+constexpr int kResMaxDeg = 64;  // blocks of a resident system's longest row (bounds the offset table)
 
 // The first half of block_sum_acc: each warp's pair, reduced by the same shuffle tree,
 // becomes one FP64 value in wacc[warp] (read after a barrier).
