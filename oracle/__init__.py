@@ -1,8 +1,8 @@
 """Test infrastructure: the oracle for the implicit cloth step.
 
 Only ``tests/``, ``bench.py`` (its CPU-baseline leg and reference arm) and
-``__graft_entry__.smoke()`` may use this package, and only as the checker or the timed
-CPU baseline.  The product (``opencloth_gb300``) never imports it.
+``__graft_entry__.smoke()`` may use this package, and only as the reference that results
+are compared against or as the timed CPU baseline.  The product (``opencloth_gb300``) never imports it.
 
 Two oracles:
 

@@ -9,7 +9,7 @@
 //   InitGL()                   FEM:424   mesh, element stiffness, lumped masses
 //   StepPhysics(dt)            FEM:981   whole steps, to reach a deformed state
 //   ComputeForces ... DynamicsAssembly   FEM:983-995, the first half of one more step
-//   ConjugateGradientSolver    FEM:837-922, the block-sparse CG this build restates
+//   ConjugateGradientSolver    FEM:837-922, the block-sparse CG the library restates
 //
 // Usage:
 //   fem_step --system <steps> <system.bin> <solution.bin>

@@ -1,5 +1,5 @@
-/* Test infrastructure: a straightforward FP64 CPU adjoint of the implicit step, the
- * checker of the GPU adjoint.  Only tests/ and bench-side gradient checks use it.
+/* Test infrastructure: a straightforward FP64 CPU adjoint of the implicit step, which
+ * the GPU adjoint is compared against.  Only tests/ and bench-side gradient checks use it.
  *
  * Forward: ocr_step_f64 one step at a time (the reference step in FP64, with the pin
  * filter); every state is kept.  Backward, per step (REFERENCE Jacobian mode, vertex i

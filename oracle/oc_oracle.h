@@ -1,7 +1,8 @@
 /* Test infrastructure: CPU restatement of the reference's implicit mass-spring step.
  *
  * Only tests/, bench.py's cpu_baseline / reference arm and __graft_entry__.smoke()
- * use this, and only as the checker.  The library (opencloth_gb300/) never links it.
+ * use this, and only as the reference results are compared against.  The library
+ * (opencloth_gb300/) never links it.
  *
  * It restates, operation for operation and in the same rounding order (compile with
  * -ffp-contract=off), the reference's

@@ -1,5 +1,5 @@
-"""The FP64 CPU adjoint (oracle/oc_adjoint.c), the checker of the GPU adjoint, against
-FP64 central differences of the same method."""
+"""The FP64 CPU adjoint (oracle/oc_adjoint.c), which the GPU adjoint is compared against,
+against FP64 central differences of the same method."""
 import numpy as np
 import pytest
 

@@ -3,8 +3,8 @@
 Tolerance: the GPU runs the forward in FP32 with the CG to 1e-6; against FP64 central
 differences (eps 1e-4 relative) of the same method, the directional derivatives along
 six random directions per parameter group (Ks, Kd, initial velocity, external force, and
-joint directions) agree within 1e-3 relative as a vector, ||ad - fd|| / ||fd|| (the
-spec bar).  What limits the agreement is the FP32 final state: an
+joint directions) agree within 1e-3 relative as a vector, ||ad - fd|| / ||fd||.  What
+limits the agreement is the FP32 final state: an
 exact FP64 adjoint seeded with the GPU's final positions shows the same error, so the
 case is a 200-step trajectory whose loss residual X_T - target (~7e-3) sits far above
 FP32 position resolution near y = 5 (~5e-7).  Gradient vectors agree with the FP64 CPU

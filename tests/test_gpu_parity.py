@@ -203,7 +203,7 @@ def test_config2_settings_600_steps_against_fp64():
     """The 1M-vertex configuration's settings on a 257 x 257 cloth (Ks 50.75/50.75/50.95,
     Kd -0.25, dt 1/60, N(0, (1e-3 spacing)^2) jitter, CG up to 200 iterations to 1e-5),
     600 steps: X within TOL_FP64_X of the FP64 method (the restatement in FP64 with FP64
-    dots and the pin filter), the benchmark spec's accuracy bar.  The full 1025 x 1025 cloth
+    dots and the pin filter): positions within 1e-4 relative after 600 steps.  The full 1025 x 1025 cloth
     takes hours in FP64 on the host; the per-vertex arithmetic is the same."""
     from opencloth_gb300 import grid_cloth
 
