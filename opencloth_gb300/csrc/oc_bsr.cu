@@ -586,6 +586,54 @@ __global__ void __launch_bounds__(kThreads) k_bsr_resident(const BsrArgs a, cons
     }
 }
 
+// Host arrays arrive in the caller's order in staging buffers.  k_bsr_check flags a
+// non-finite block or b in a free row, or a non-finite x (FEM:392-393 puts FLT_MAX in
+// fixed rows); nothing is committed unless the flag stays clear.
+__global__ void __launch_bounds__(kThreads) k_bsr_check(const float* blk, const float* b, const float* x,
+                                                       const int32_t* row_ptr, const uint8_t* fixed_caller,
+                                                       int64_t rows, int* flag) {
+    int bad = 0;  // bit 0: a block, bit 1: b, bit 2: x
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+        if (x)
+            for (int c = 0; c < 3; ++c) bad |= isfinite(x[3 * r + c]) ? 0 : 4;
+        if (fixed_caller[r]) continue;
+        if (b)
+            for (int c = 0; c < 3; ++c) bad |= isfinite(b[3 * r + c]) ? 0 : 2;
+        if (blk)
+            for (int64_t i = 9 * (int64_t)row_ptr[r]; i < 9 * (int64_t)row_ptr[r + 1]; ++i)
+                bad |= isfinite(blk[i]) ? 0 : 1;
+    }
+    if (bad) atomicOr(flag, bad);
+}
+
+// b into the internal row order, x into planes in the internal order.
+__global__ void __launch_bounds__(kThreads) k_bsr_commit(const BsrArgs a, float* bint, const float* b, const float* x,
+                                                        const int32_t* perm, int64_t rows) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = perm[r];
+        if (b)
+            for (int c = 0; c < 3; ++c) bint[3 * i + c] = b[3 * r + c];
+        if (x)
+            for (int c = 0; c < 3; ++c) a.x[c][i] = x[3 * r + c];
+    }
+}
+
+// The solution and the residual back in the caller's order (3 floats per row).
+__global__ void __launch_bounds__(kThreads) k_bsr_gather_out(const BsrArgs a, const int32_t* perm, int64_t rows,
+                                                            float* x, float* res) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = perm[r];
+        if (x)
+            for (int c = 0; c < 3; ++c) x[3 * r + c] = a.x[c][i];
+        if (res) {
+            const float4 v = a.r4[i];
+            res[3 * r] = v.x;
+            res[3 * r + 1] = v.y;
+            res[3 * r + 2] = v.z;
+        }
+    }
+}
+
 // Launch shapes of the matrix-vector pass (unroll of the slot loop, minimum resident
 // blocks per SM, which caps the registers).  OC_BSR_VARIANT picks one; the default was
 // chosen by measurement on GB300.
@@ -618,16 +666,22 @@ struct oc_bsr_solver {
     int64_t n_rows = 0, nnzb = 0, n_slots = 0;
     int32_t n_blocks = 0;
     std::vector<int64_t> row_off, nnz_off;
-    std::vector<uint8_t> fixed_host;
     bool any_iter = false;  // some system has cg_max_iter > 0
-    std::vector<int32_t> row_ptr_host;  // global CSR row pointer
-    std::vector<int32_t> perm;          // caller's row -> internal row
     BsrArgs args{};
     std::vector<void*> allocs;
     uint8_t* d_fixed = nullptr;
     int32_t* d_row_ptr = nullptr;
-    float* d_cblk = nullptr;  // staging of the caller's CSR blocks
+    float* d_cblk = nullptr;  // the caller's CSR blocks (packed at each solve)
     float* d_b = nullptr;
+    // set_system's staging (caller order) and the tables its kernels use
+    float* d_stage_blk = nullptr;
+    float* d_stage_b = nullptr;
+    float* d_stage_x = nullptr;
+    float* d_out = nullptr;  // get_solution: x and residual in the caller's order
+    uint8_t* d_fixed_caller = nullptr;
+    int32_t* d_perm = nullptr;
+    int* d_flag = nullptr;
+    int* h_flag = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int64_t launches = 0;
@@ -685,10 +739,14 @@ void bsr_release(oc_bsr_solver* s) {
     for (void* p : s->allocs) cudaFree(p);
     s->allocs.clear();
     if (s->h_loop) cudaFreeHost(s->h_loop);
+    if (s->h_flag) cudaFreeHost(s->h_flag);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
 }
 
 bool bsr_valid(const oc_bsr_solver* s) { return s != nullptr && s->n_sys > 0; }
+
+// Grid of the row-parallel host-facing kernels (grid-stride over the rows).
+int row_grid(int64_t rows) { return (int)std::max<int64_t>(1, std::min<int64_t>((rows + kThreads - 1) / kThreads, 152 * 8)); }
 
 void launch(void (*k)(BsrArgs), const BsrArgs& a, int n, cudaStream_t stream) {
     if (n > 0) k<<<n, kThreads, 0, stream>>>(a);
@@ -931,9 +989,6 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
                 scol[(size_t)((slice_ptr[sl] + (e - d.row_ptr[r])) * 32 + (i & 31))] = perm[r0 + d.col[e]];
         }
     }
-    s->fixed_host = fixed;
-    s->row_ptr_host = row_ptr;
-    s->perm = perm;
     s->n_blocks = (int32_t)blocks.size();
 
     BsrArgs& a = s->args;
@@ -977,6 +1032,14 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
     BSR_CREATE_TRY(bsr_alloc(s, &s->d_b, 3 * (size_t)rows));
     BSR_CREATE_TRY(cudaMemset(s->d_b, 0, 3 * (size_t)rows * sizeof(float)));
     a.b = s->d_b;
+    BSR_CREATE_TRY(bsr_alloc(s, &s->d_stage_blk, 9 * std::max<size_t>((size_t)nnzb, 1)));
+    BSR_CREATE_TRY(bsr_alloc(s, &s->d_stage_b, 3 * (size_t)rows));
+    BSR_CREATE_TRY(bsr_alloc(s, &s->d_stage_x, 3 * (size_t)rows));
+    BSR_CREATE_TRY(bsr_alloc(s, &s->d_out, 6 * (size_t)rows));
+    BSR_CREATE_TRY(bsr_upload(s, &s->d_fixed_caller, fixed));
+    BSR_CREATE_TRY(bsr_upload(s, &s->d_perm, perm));
+    BSR_CREATE_TRY(bsr_alloc(s, &s->d_flag, 1));
+    BSR_CREATE_TRY(cudaMallocHost(&s->h_flag, sizeof(int)));
     const size_t stride = (size_t)((rows + 63) / 64) * 64;
     float* vec = nullptr;
     BSR_CREATE_TRY(bsr_alloc(s, &vec, 6 * stride));
@@ -1040,44 +1103,40 @@ oc_status oc_bsr_get_counts(const oc_bsr_solver* s, int64_t* rows, int64_t* nnzb
 
 oc_status oc_bsr_set_system(oc_bsr_solver* s, const float* blocks, const float* b, const float* x) {
     if (!bsr_valid(s)) return OC_ERR_INVALID_ARGUMENT;
-    // Non-finite values are allowed only where the reference has them: in the rows of
-    // fixed vertices (their lumped mass is FLT_MAX, FEM:392-393), which the CG skips.
-    for (int64_t r = 0; r < s->n_rows; ++r) {
-        if (s->fixed_host[r]) continue;
-        if (blocks)
-            for (int64_t e = s->row_ptr_host[r]; e < s->row_ptr_host[r + 1]; ++e)
-                for (int c = 0; c < 9; ++c)
-                    if (!std::isfinite(blocks[9 * e + c]))
-                        return bsr_fail(s, OC_ERR_NON_FINITE, "oc_bsr_set_system: non-finite block in a free row");
-        if (b)
-            for (int c = 0; c < 3; ++c)
-                if (!std::isfinite(b[3 * r + c]))
-                    return bsr_fail(s, OC_ERR_NON_FINITE, "oc_bsr_set_system: non-finite b in a free row");
-    }
-    if (x)
-        for (int64_t e = 0; e < 3 * s->n_rows; ++e)
-            if (!std::isfinite(x[e])) return bsr_fail(s, OC_ERR_NON_FINITE, "oc_bsr_set_system: non-finite x");
+    if (!blocks && !b && !x) return OC_OK;
     BSR_TRY(cudaSetDevice(s->device));
+    // The host arrays go to staging buffers in the caller's order, and a kernel checks
+    // them: non-finite values are allowed only where the reference has them, in the rows
+    // of fixed vertices (their lumped mass is FLT_MAX, FEM:392-393), which the CG skips.
+    // Nothing is committed when the check fails.
+    const int64_t rows = s->n_rows;
     if (blocks)
-        BSR_TRY(cudaMemcpyAsync(s->d_cblk, blocks, sizeof(float) * 9 * s->nnzb, cudaMemcpyHostToDevice, s->stream));
-    // b and x in the internal row order (x as planes).
-    std::vector<float> bint, planes;
-    if (b) {
-        bint.resize(3 * (size_t)s->n_rows);
-        for (int64_t r = 0; r < s->n_rows; ++r)
-            for (int c = 0; c < 3; ++c) bint[3 * (size_t)s->perm[r] + c] = b[3 * r + c];
-        BSR_TRY(cudaMemcpyAsync(s->d_b, bint.data(), sizeof(float) * 3 * s->n_rows, cudaMemcpyHostToDevice,
+        BSR_TRY(cudaMemcpyAsync(s->d_stage_blk, blocks, sizeof(float) * 9 * s->nnzb, cudaMemcpyHostToDevice,
                                 s->stream));
+    if (b) BSR_TRY(cudaMemcpyAsync(s->d_stage_b, b, sizeof(float) * 3 * rows, cudaMemcpyHostToDevice, s->stream));
+    if (x) BSR_TRY(cudaMemcpyAsync(s->d_stage_x, x, sizeof(float) * 3 * rows, cudaMemcpyHostToDevice, s->stream));
+    BSR_TRY(cudaMemsetAsync(s->d_flag, 0, sizeof(int), s->stream));
+    const int grid = row_grid(rows);
+    k_bsr_check<<<grid, kThreads, 0, s->stream>>>(blocks ? s->d_stage_blk : nullptr, b ? s->d_stage_b : nullptr,
+                                                  x ? s->d_stage_x : nullptr, s->d_row_ptr, s->d_fixed_caller, rows,
+                                                  s->d_flag);
+    BSR_TRY(cudaGetLastError());
+    BSR_TRY(cudaMemcpyAsync(s->h_flag, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    BSR_TRY(cudaStreamSynchronize(s->stream));
+    const int bad = *s->h_flag;
+    if (bad & 1) return bsr_fail(s, OC_ERR_NON_FINITE, "oc_bsr_set_system: non-finite block in a free row");
+    if (bad & 2) return bsr_fail(s, OC_ERR_NON_FINITE, "oc_bsr_set_system: non-finite b in a free row");
+    if (bad & 4) return bsr_fail(s, OC_ERR_NON_FINITE, "oc_bsr_set_system: non-finite x");
+    // Commit, stream-ordered before the next solve: the blocks as given, b and x into the
+    // internal row order (x as planes).
+    if (blocks)
+        BSR_TRY(cudaMemcpyAsync(s->d_cblk, s->d_stage_blk, sizeof(float) * 9 * s->nnzb, cudaMemcpyDeviceToDevice,
+                                s->stream));
+    if (b || x) {
+        k_bsr_commit<<<grid, kThreads, 0, s->stream>>>(s->args, s->d_b, b ? s->d_stage_b : nullptr,
+                                                       x ? s->d_stage_x : nullptr, s->d_perm, rows);
+        BSR_TRY(cudaGetLastError());
     }
-    if (x) {
-        planes.resize(3 * (size_t)s->n_rows);
-        for (int64_t r = 0; r < s->n_rows; ++r)
-            for (int c = 0; c < 3; ++c) planes[(size_t)c * s->n_rows + s->perm[r]] = x[3 * r + c];
-        for (int c = 0; c < 3; ++c)
-            BSR_TRY(cudaMemcpyAsync(s->args.x[c], planes.data() + (size_t)c * s->n_rows, sizeof(float) * s->n_rows,
-                                    cudaMemcpyHostToDevice, s->stream));
-    }
-    BSR_TRY(cudaStreamSynchronize(s->stream));  // the staging vectors go out of scope
     return OC_OK;
 }
 
@@ -1204,28 +1263,18 @@ oc_status oc_bsr_profile(oc_bsr_solver* s, int32_t n_solves, int32_t max_kernels
 
 oc_status oc_bsr_get_solution(oc_bsr_solver* s, float* x, float* residual) {
     if (!bsr_valid(s)) return OC_ERR_INVALID_ARGUMENT;
+    if (!x && !residual) return OC_OK;
     BSR_TRY(cudaSetDevice(s->device));
-    if (x) {
-        std::vector<float> planes(3 * (size_t)s->n_rows);
-        for (int c = 0; c < 3; ++c)
-            BSR_TRY(cudaMemcpyAsync(planes.data() + (size_t)c * s->n_rows, s->args.x[c], sizeof(float) * s->n_rows,
-                                    cudaMemcpyDeviceToHost, s->stream));
-        BSR_TRY(cudaStreamSynchronize(s->stream));
-        for (int64_t r = 0; r < s->n_rows; ++r)
-            for (int c = 0; c < 3; ++c) x[3 * r + c] = planes[(size_t)c * s->n_rows + s->perm[r]];
-    }
-    if (residual) {
-        std::vector<float4> r4((size_t)s->n_rows);
-        BSR_TRY(cudaMemcpyAsync(r4.data(), s->args.r4, sizeof(float4) * s->n_rows, cudaMemcpyDeviceToHost,
-                                s->stream));
-        BSR_TRY(cudaStreamSynchronize(s->stream));
-        for (int64_t r = 0; r < s->n_rows; ++r) {
-            const float4 v = r4[s->perm[r]];
-            residual[3 * r] = v.x;
-            residual[3 * r + 1] = v.y;
-            residual[3 * r + 2] = v.z;
-        }
-    }
+    const int64_t rows = s->n_rows;
+    float* dx = s->d_out;
+    float* dr = s->d_out + 3 * rows;
+    k_bsr_gather_out<<<row_grid(rows), kThreads, 0, s->stream>>>(s->args, s->d_perm, rows, x ? dx : nullptr,
+                                                                 residual ? dr : nullptr);
+    BSR_TRY(cudaGetLastError());
+    if (x) BSR_TRY(cudaMemcpyAsync(x, dx, sizeof(float) * 3 * rows, cudaMemcpyDeviceToHost, s->stream));
+    if (residual)
+        BSR_TRY(cudaMemcpyAsync(residual, dr, sizeof(float) * 3 * rows, cudaMemcpyDeviceToHost, s->stream));
+    BSR_TRY(cudaStreamSynchronize(s->stream));
     return OC_OK;
 }
 
