@@ -177,4 +177,4 @@ def test_torch_autograd_function(case):
             ks2 = ks * (1.0 - 1e-3 * ks.grad / max(float(ks.grad.abs().max()), 1e-30))
         X2 = trajectory(s, case["X"], ks2, kd.detach(), v0.detach(), ext.detach(), DT, case["steps"], 10)
         loss2 = ((X2.double() - target) ** 2).sum(dim=1).mean()
-        assert float(loss2) < float(loss)
+        assert float(loss2.detach()) < float(loss.detach())
