@@ -641,7 +641,7 @@ def measure_fem(name: str, seed: int, local: int, solves: int) -> dict:
         "metric": "block-row-iterations/s", "value": rows * iters / (ms / 1e3), "ms_per_solve": ms,
         "solves_per_s": 1e3 / ms, "solves": solves, "gpu_launches": int(launches), "clocks": clocks.summary(),
         "e2e": {"value": rows * iters / e2e_s, "unit": "block-row-iterations/s",
-                "h2d_bytes_per_solve": int(blocks.nbytes + b.nbytes + V0.nbytes), "d2h_bytes_per_solve": int(V0.nbytes)},
+                "h2d_bytes_per_solve": int(blocks.nbytes + b.nbytes + V0.nbytes), "d2h_bytes_per_solve": int(2 * V0.nbytes)},  # V and the residual
         "roofline": roof,
         "kernels": {k: {"avg_us": 1e3 * v["ms_total"] / max(v["launches"], 1), "launches": v["launches"]}
                     for k, v in prof.items()},
