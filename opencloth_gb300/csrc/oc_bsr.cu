@@ -835,6 +835,7 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
     oc_options o;
     oc_default_options(&o);
     if (opts) o = *opts;
+    if (o.executor < OC_EXEC_AUTO || o.executor > OC_EXEC_PLAIN) return OC_ERR_INVALID_ARGUMENT;
     std::string err;
     int64_t rows = 0, nnzb = 0;
     for (int32_t k = 0; k < n_systems; ++k) {
@@ -902,7 +903,6 @@ oc_status oc_bsr_create(const oc_bsr_desc* descs, int32_t n_systems, const oc_op
     // Room for the kernel's static shared memory (block sums and the two broadcast scalars).
     const size_t smem_cap = smem_optin > 1024 ? (size_t)smem_optin - 1024 : 0;
     auto who_of = [](int32_t k) { return "system " + std::to_string(k) + ": "; };
-    if (o.executor < OC_EXEC_AUTO || o.executor > OC_EXEC_PLAIN) return bail(OC_ERR_INVALID_ARGUMENT);
     s->row_off.assign(n_systems + 1, 0);
     s->nnz_off.assign(n_systems + 1, 0);
     int64_t slots = 0;

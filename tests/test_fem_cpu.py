@@ -98,3 +98,48 @@ def test_port_matches_reference_cg_on_modified_systems(seed):
     V32, r32 = oracle.fem_ref_solve(sys_)
     V, r = oracle.bsr_cg(sys_)
     assert np.array_equal(V, V32) and np.array_equal(r, r32)
+
+
+def _desc(sys_, **over):
+    d = {"row_ptr": sys_.row_ptr.copy(), "col": sys_.col.copy(), "fixed": sys_.fixed.copy(), "i_max": sys_.i_max,
+         "tolerance": sys_.tolerance, "tiny": sys_.tiny}
+    d.update(over)
+    return d
+
+
+def test_create_validates_patterns_before_any_device_work():
+    """oc_bsr_create checks every system's pattern and limits on the host first, so these
+    fail the same way with or without a GPU: OC_ERR_INVALID_ARGUMENT (1) for a bad size,
+    row pointer, column order (std::map order), limit or executor, OC_ERR_BAD_INDEX (2)
+    for a column outside the system."""
+    from opencloth_gb300 import OcError
+    from opencloth_gb300.fem import BsrSolver
+
+    sys_ = fem_golden("m0")[0]
+    swapped = sys_.col.copy()
+    swapped[[0, 1]] = swapped[[1, 0]]
+    outside = sys_.col.copy()
+    outside[3] = sys_.n
+    negative = sys_.col.copy()
+    negative[5] = -1
+    shifted = sys_.row_ptr.copy()
+    shifted[0] = 1
+    cases = [
+        ([_desc(sys_, col=swapped)], {}, 1),
+        ([_desc(sys_, col=outside)], {}, 2),
+        ([_desc(sys_, col=negative)], {}, 2),
+        ([_desc(sys_, row_ptr=shifted)], {}, 1),
+        ([_desc(sys_, i_max=-1)], {}, 1),
+        ([_desc(sys_, tiny=-1.0)], {}, 1),
+        ([_desc(sys_, tiny=float("nan"))], {}, 1),
+        ([_desc(sys_), _desc(sys_, col=outside)], {}, 2),
+        ([_desc(sys_)], {"executor": 9}, 1),
+        ([_desc(sys_)], {"executor": -1}, 1),
+    ]
+    for descs, kw, status in cases:
+        with pytest.raises(OcError) as e:
+            BsrSolver(descs, **kw)
+        assert e.value.status == status, (kw, status)
+    with pytest.raises(OcError) as e:
+        BsrSolver([])
+    assert e.value.status == 1
