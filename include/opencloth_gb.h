@@ -286,8 +286,10 @@ void oc_bsr_destroy(oc_bsr_solver* s);
 const char* oc_bsr_last_error(const oc_bsr_solver* s);
 oc_status oc_bsr_get_counts(const oc_bsr_solver* s, int64_t* rows, int64_t* nnzb, int32_t* n_systems);
 /* Host arrays concatenated over the systems in creation order: blocks 9 x nnzb, b and x
- * 3 x rows; NULL keeps the current value.  Non-finite values in free rows fail with
- * OC_ERR_NON_FINITE. */
+ * 3 x rows; NULL keeps the current value.  A non-finite block or b in a free row, or a
+ * non-finite x, fails with OC_ERR_NON_FINITE and changes nothing (the arrays are staged
+ * and checked on the device, then committed).  Returns when the host arrays may be
+ * reused; the commit is ordered before the next solve on the handle's stream. */
 oc_status oc_bsr_set_system(oc_bsr_solver* s, const float* blocks, const float* b, const float* x);
 /* The CG on every system (asynchronous on the handle's stream). */
 oc_status oc_bsr_solve(oc_bsr_solver* s);
