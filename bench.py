@@ -34,6 +34,7 @@ import subprocess
 import sys
 import tempfile
 import time
+from dataclasses import dataclass
 from pathlib import Path
 
 import numpy as np
@@ -46,57 +47,102 @@ METRIC = "vertex-steps/s"
 
 
 # ---- workloads ------------------------------------------------------------------------
+#
+# A workload is a list of cloth specifications plus the initial state.  The GPU arm turns
+# the specifications into the library's descriptors; the reference arm builds the same
+# lattices with the oracle's own builder (bit-identical to the library's, a CPU test checks
+# it), so its process never loads the GPU library.
 
-def grid1025(seed: int):
-    from opencloth_gb300 import ClothDesc, grid_cloth
+@dataclass
+class ClothSpec:
+    n_vertices: int
+    springs: np.ndarray
+    pinned: np.ndarray
+    cg_max_iter: int = 200
+    cg_tol: float = 1e-5
+    coupled: bool = False  # the COUPLED Jacobian mode (no counterpart in the reference)
+    passes: bool = False  # EllipsoidCollision and ApplyProvotDynamicInverse after each step
 
+
+def _grid_builder(impl: str):
+    if impl == "reference":
+        import oracle
+
+        return oracle.grid_cloth
+    from opencloth_gb300 import grid_cloth
+
+    return grid_cloth
+
+
+def grid1025(seed: int, impl: str = "ours"):
     cols = 1025
-    X, sp = grid_cloth(cols, cols, ks=(50.75, 50.75, 50.95), kd=(-0.25, -0.25, -0.25), jitter=1e-3, seed=seed)
-    desc = ClothDesc(n_vertices=cols * cols, springs=sp, pinned=np.array([0, cols - 1], np.int32),
-                     cg_max_iter=200, cg_tol=1e-5)
-    return [desc], [(cols, cols)], X, np.zeros_like(X)
+    X, sp = _grid_builder(impl)(cols, cols, ks=(50.75, 50.75, 50.95), kd=(-0.25, -0.25, -0.25), jitter=1e-3,
+                                seed=seed)
+    spec = ClothSpec(n_vertices=cols * cols, springs=sp, pinned=np.array([0, cols - 1], np.int32))
+    return [spec], [(cols, cols)], X, np.zeros_like(X)
 
 
-def batch4096(seed: int, count: int = 4096):
-    from opencloth_gb300 import ClothDesc, grid_cloth
-
+def batch4096(seed: int, impl: str = "ours", count: int = 4096):
     rng = np.random.default_rng(seed)
     sides = rng.integers(8, 129, count)
-    descs, shapes, Xs = [], [], []
+    build = _grid_builder(impl)
+    specs, shapes, Xs = [], [], []
     for k, n in enumerate(sides):
         n = int(n)
         ks = np.exp(rng.uniform(np.log(10.0), np.log(500.0), 3))
         kd = rng.uniform(-0.5, -0.05, 3)
-        X, sp = grid_cloth(n, n, ks=tuple(ks), kd=tuple(kd), jitter=1e-3, seed=seed * 100003 + k)
-        descs.append(ClothDesc(n_vertices=n * n, springs=sp, pinned=np.array([0, n - 1], np.int32),
-                               cg_max_iter=200, cg_tol=1e-5))
+        X, sp = build(n, n, ks=tuple(ks), kd=tuple(kd), jitter=1e-3, seed=seed * 100003 + k)
+        specs.append(ClothSpec(n_vertices=n * n, springs=sp, pinned=np.array([0, n - 1], np.int32)))
         shapes.append((n, n))
         Xs.append(X)
     X = np.concatenate(Xs)
-    return descs, shapes, X, np.zeros_like(X)
+    return specs, shapes, X, np.zeros_like(X)
 
 
-def coupled1025(seed: int):
+def coupled1025(seed: int, impl: str = "ours"):
     """grid1025 in the COUPLED Jacobian mode (Baraff-Witkin block-sparse system)."""
-    from opencloth_gb300 import JAC_COUPLED
-
-    descs, shapes, X, V = grid1025(seed)
-    descs[0].jacobian_mode = JAC_COUPLED
-    return descs, shapes, X, V
+    specs, shapes, X, V = grid1025(seed, impl)
+    specs[0].coupled = True
+    return specs, shapes, X, V
 
 
-def stepphysics1025(seed: int):
+def stepphysics1025(seed: int, impl: str = "ours"):
     """grid1025 with the rest of StepPhysics: the reference's ellipsoid and Provot pass."""
-    from opencloth_gb300 import PASS_ELLIPSOID, PASS_PROVOT, reference_ellipsoid
-
-    descs, shapes, X, V = grid1025(seed)
-    descs[0].passes = PASS_ELLIPSOID | PASS_PROVOT
-    descs[0].ellipsoid, descs[0].ellipsoid_inv = reference_ellipsoid()
-    return descs, shapes, X, V
+    specs, shapes, X, V = grid1025(seed, impl)
+    specs[0].passes = True
+    return specs, shapes, X, V
 
 
 WORKLOADS = {"grid1025": grid1025, "batch4096": batch4096, "coupled1025": coupled1025,
              "stepphysics1025": stepphysics1025}
+# The reference arm steps the reference's implicit step alone (ComputeForces +
+# IntegrateImplicit); the COUPLED mode has no counterpart there.
+REFERENCE_WORKLOADS = ("grid1025", "batch4096")
+
+
+def to_descs(specs):
+    """The library's descriptors for a workload's cloth specifications."""
+    from opencloth_gb300 import JAC_COUPLED, PASS_ELLIPSOID, PASS_PROVOT, ClothDesc, reference_ellipsoid
+
+    out = []
+    for c in specs:
+        d = ClothDesc(n_vertices=c.n_vertices, springs=c.springs, pinned=c.pinned, cg_max_iter=c.cg_max_iter,
+                      cg_tol=c.cg_tol)
+        if c.coupled:
+            d.jacobian_mode = JAC_COUPLED
+        if c.passes:
+            d.passes = PASS_ELLIPSOID | PASS_PROVOT
+            d.ellipsoid, d.ellipsoid_inv = reference_ellipsoid()
+        out.append(d)
+    return out
+
+
+def workload_config(name: str, specs, world: int) -> dict:
+    """The ``config`` object of a workload's JSON line (the same for both arms)."""
+    return {"workload": name, "vertices": int(sum(c.n_vertices for c in specs)),
+            "springs": int(sum(len(c.springs) for c in specs)), "instances": len(specs), "dt": DT,
+            "cg_max_iter": 200, "cg_tol": 1e-5, "parallelism": f"replicas x{world}",
+            "l2": "per-step working set larger than the 129 MB L2; no flush"}
 
 
 def algorithmic_bytes(kernel: str, n_vertices: int, n_springs: int, first_dir: bool = False) -> int:
@@ -220,8 +266,9 @@ def _cpu_worker(args):
 
 
 def cpu_throughput(workload: str, descs, shapes, X, budget_s: float, processes: int):
-    """The reference step (or its port) on a bounded sample of the same workload.
-    Returns (vertex-steps/s, cores, kind, sample description)."""
+    """The reference step (or its port) on a bounded sample of the same workload
+    (``descs``: the cloth specifications).  Returns (vertex-steps/s, cores, kind, sample
+    description)."""
     import oracle
 
     oracle.build(reference=True)
@@ -285,20 +332,27 @@ def aggregate_value(vertices_per_rank: int, steps: int, world: int, ms: float) -
 
 
 def run_reference(args) -> None:
+    """The reference's CPU step (the reference build where it exists, else the oracle's
+    restatement of it) on the GPU arm's workload and config; rank 0 only.  The process
+    builds its inputs with the oracle and never loads the GPU library."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     name = "grid1025" if args.workload == "all" else args.workload
-    descs, shapes, X, _ = WORKLOADS[name](args.seed)
-    nv = sum(d.n_vertices for d in descs)
+    if name not in REFERENCE_WORKLOADS:
+        print(json.dumps({"impl": "reference", "unavailable": f"{name} has no counterpart in the reference"}),
+              flush=True)
+        return
+    specs, shapes, X, _ = WORKLOADS[name](args.seed, impl="reference")
+    nv = sum(c.n_vertices for c in specs)
     procs = max(1, os.cpu_count() or 1)
     budget = min(120.0, 2.0 * max(args.steps, 1))
-    value, cores, kind, sample = cpu_throughput(name, descs, shapes, X, budget, procs)
+    value, cores, kind, sample = cpu_throughput(name, specs, shapes, X, budget, procs)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * nv / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": name, "vertices": nv, "instances": len(descs)},
+        "config": workload_config(name, specs, world),
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -347,7 +401,8 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
 
     from opencloth_gb300 import ClothSolver
 
-    descs, shapes, X0, V0 = WORKLOADS[name](args.seed + 7919 * rank)
+    specs, shapes, X0, V0 = WORKLOADS[name](args.seed + 7919 * rank)
+    descs = to_descs(specs)
     nv = sum(d.n_vertices for d in descs)
     ns = sum(len(d.springs) for d in descs)
     stream = torch.cuda.Stream()
@@ -437,7 +492,7 @@ def measure(name: str, args, steps: int, rank: int, world: int, local: int, plai
                      "speedup": value / plain_value}
 
     return {
-        "name": name, "descs": descs, "shapes": shapes, "X0": X0, "nv": nv, "ns": ns, "value": value,
+        "name": name, "specs": specs, "descs": descs, "shapes": shapes, "X0": X0, "nv": nv, "ns": ns, "value": value,
         "ms_per_step": ms / steps, "steps": steps, "launches": launches, "clocks": clocks.summary(),
         "cg": {"iters_last_step_max": int(iters.max()), "iters_last_step_mean": float(iters.mean()),
                "rel_residual_max": float(rr.max()), "flags_any": int(np.bitwise_or.reduce(flags))},
@@ -671,16 +726,13 @@ def run_ours(args) -> None:
         results.append(measure(name, args, steps, rank, world, local, plain_steps[name]))
     if rank == 0:
         r = results[0]
-        cpu_v, cores, kind, sample = cpu_throughput(r["name"], r["descs"], r["shapes"], r["X0"], 12.0,
+        cpu_v, cores, kind, sample = cpu_throughput(r["name"], r["specs"], r["shapes"], r["X0"], 12.0,
                                                     max(1, os.cpu_count() or 1))
         line = {
             "metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": world, "steps": r["steps"],
             "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": r["name"], "vertices": r["nv"], "springs": r["ns"],
-                       "instances": len(r["descs"]), "dt": DT, "cg_max_iter": 200, "cg_tol": 1e-5,
-                       "parallelism": f"replicas x{world}",
-                       "l2": "per-step working set larger than the 129 MB L2; no flush"},
+            "config": workload_config(r["name"], r["specs"], world),
             "cg": r["cg"], "gpu_launches": int(r["launches"]), "clocks": r["clocks"], "e2e": r["e2e"],
             "roofline": r["roofline"], "cg_roofline": r["cg_roofline"], "kernels": r["kernels"],
             "plain_gpu": r["plain_gpu"],

@@ -22,8 +22,10 @@ INCLUDE = ROOT / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false keeps every FP32 multiply and add separately rounded, as the
 # reference's scalar code rounds them; division and sqrt stay IEEE (no fast math).
+# -ffp-contract=off does the same for host code (the lattice builder), where gcc on
+# aarch64 would otherwise fuse multiply-adds.
 NVCC_FLAGS = ARCH + [
-    "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+    "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
     "-Xcompiler", "-fno-strict-aliasing", "-I", str(INCLUDE), "-I", str(CSRC),
 ]
 # The adjoint kernels differentiate the step; they are checked against finite differences

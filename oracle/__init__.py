@@ -40,11 +40,12 @@ def build(reference: bool = True) -> None:
     """Compile the port (always) and the reference harness (when the tree is present)."""
     BUILD.mkdir(exist_ok=True)
     srcs = [HERE / "oc_oracle.c", HERE / "oc_oracle_impl.h", HERE / "oc_coupled_impl.h", HERE / "oc_bsr_impl.h",
-            HERE / "oc_oracle.h", HERE / "oc_adjoint.c"]
+            HERE / "oc_oracle.h", HERE / "oc_adjoint.c", HERE / "oc_grid.c", Path(__file__)]
     if not PORT_LIB.exists() or any(s.stat().st_mtime > PORT_LIB.stat().st_mtime for s in srcs):
         tmp = PORT_LIB.with_suffix(".so.tmp")
         subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
-                        str(HERE / "oc_oracle.c"), str(HERE / "oc_adjoint.c"), "-o", str(tmp), "-lm"], check=True)
+                        str(HERE / "oc_oracle.c"), str(HERE / "oc_adjoint.c"), str(HERE / "oc_grid.c"), "-o", str(tmp),
+                        "-lm"], check=True)
         os.replace(tmp, PORT_LIB)
     if reference:
         subprocess.run(["bash", str(HERE / "build_ref.sh")], check=True, capture_output=True)
@@ -91,8 +92,35 @@ def port() -> C.CDLL:
             f.restype = C.c_int
         lib.ocr_adjoint_f64.argtypes = [P, C.c_double, C.c_int32] + [C.c_void_p] * 10
         lib.ocr_adjoint_f64.restype = C.c_int
+        lib.ocr_grid_spring_count.argtypes = [C.c_int32, C.c_int32]
+        lib.ocr_grid_spring_count.restype = C.c_int64
+        lib.ocr_grid_build.argtypes = [C.c_int32, C.c_int32, C.c_float, C.c_void_p, C.c_void_p, C.c_float,
+                                       C.c_uint64, C.c_void_p, C.c_void_p]
+        lib.ocr_grid_build.restype = C.c_int
         _port = lib
     return _port
+
+
+def grid_cloth(cols: int, rows: int, size: float = 4.0, ks=(0.75, 0.75, 0.95), kd=(-0.25, -0.25, -0.25),
+               jitter: float = 0.0, seed: int = 0):
+    """InitGL's cloth (IMP:497-565) on the x-y plane, row 0 on top, built by the oracle
+    (oc_grid.c): ``(X, springs)`` with positions (cols*rows, 3) float32 and spring records
+    in the reference's creation order; ``jitter`` is the position noise sigma as a
+    fraction of the grid spacing, applied after the rest lengths are taken.  The same
+    arguments give the same arrays as the library's ``grid_cloth``."""
+    lib = port()
+    ns = int(lib.ocr_grid_spring_count(cols, rows))
+    if ns < 0:
+        raise ValueError("grid_cloth needs at least 3 x 3 vertices")
+    X = np.zeros((cols * rows, 3), np.float32)
+    springs = np.zeros(ns, SPRING_DTYPE)
+    ks_a = np.ascontiguousarray(ks, np.float32)
+    kd_a = np.ascontiguousarray(kd, np.float32)
+    rc = lib.ocr_grid_build(cols, rows, float(size), ks_a.ctypes.data, kd_a.ctypes.data, float(jitter),
+                            seed & (2**64 - 1), X.ctypes.data, springs.ctypes.data)
+    if rc != 0:
+        raise ValueError("ocr_grid_build rejected its arguments")
+    return X, springs
 
 
 class Cloth:

@@ -18,10 +18,12 @@
 # additionally maps glm::vecN/matN -> glm::dvecN/dmatN, float -> double and strips the
 # f suffix from floating literals.
 #
-# Exits 0 without building when the reference tree is absent.
+# The reference tree is OC_REFERENCE_DIR when set, else a checkout named `reference`
+# beside this repository (../reference from the repository root).  Exits 0 without
+# building when the tree is absent.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${OC_REFERENCE_DIR:-/root/reference}"
+REF="${OC_REFERENCE_DIR:-$HERE/../../reference}"
 SRC="$REF/OpenCloth_Implicit/OpenCloth_Implicit/main.cpp"
 OUT="$HERE/_ref"
 if [ ! -f "$SRC" ]; then

@@ -115,6 +115,14 @@ int ocr_adjoint_f64(const ocr_params* p, double dt, int32_t n_steps, const doubl
                     const double* gX_T, const double* gV_T, double* X_T, double* V_T, double* gX0, double* gV0,
                     double* gKs, double* gKd, double* gExt);
 
+/* InitGL's lattice and spring list (oc_grid.c): cols x rows vertices in the x-y plane,
+ * springs in creation order with rest lengths from the exact lattice, then seeded
+ * position jitter of sigma = jitter * spacing.  ocr_grid_spring_count gives the spring
+ * count (-1 below 3 x 3); ocr_grid_build returns 0 on success. */
+int64_t ocr_grid_spring_count(int32_t cols, int32_t rows);
+int ocr_grid_build(int32_t cols, int32_t rows, float size, const float ks[3], const float kd[3], float jitter,
+                   uint64_t seed, float* X, ocr_spring* springs);
+
 #ifdef __cplusplus
 }
 #endif

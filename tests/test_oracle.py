@@ -99,3 +99,26 @@ def test_grid_builder_matches_reference_initgl_live():
         _, spr = oracle.ref_topology(nx, ny)
         _, sp = grid_cloth(nx + 1, ny + 1)
         assert np.array_equal(sp["p1"], spr["p1"]) and np.array_equal(sp["p2"], spr["p2"])
+
+
+def test_oracle_grid_builder_matches_topology_golden():
+    """The oracle's own lattice builder (used by the benchmark's CPU arms) reproduces
+    InitGL's spring order from the reference build."""
+    t = dict(np.load(GOLDEN / "topology_ref.npz"))
+    for nx, ny in ((20, 20), (2, 2), (5, 9), (9, 3)):
+        _, sp = oracle.grid_cloth(nx + 1, ny + 1)
+        assert np.array_equal(sp["p1"], t[f"p1_{nx}_{ny}"])
+        assert np.array_equal(sp["p2"], t[f"p2_{nx}_{ny}"])
+        assert np.array_equal(sp["type"], t[f"type_{nx}_{ny}"])
+
+
+@pytest.mark.parametrize("cols,rows,jitter,seed", [(21, 21, 0.0, 0), (33, 17, 1e-3, 7), (129, 64, 2e-2, 20261203),
+                                                   (8, 8, 1e-3, 123456789)])
+def test_oracle_grid_builder_matches_library_builder(cols, rows, jitter, seed):
+    """Same arguments, same bits: positions (jitter included), spring records and rest
+    lengths, so the benchmark's CPU arms step exactly the GPU arm's inputs."""
+    ks, kd = (50.75, 49.5, 50.95), (-0.25, -0.3, -0.2)
+    Xo, so = oracle.grid_cloth(cols, rows, ks=ks, kd=kd, jitter=jitter, seed=seed)
+    Xl, sl = grid_cloth(cols, rows, ks=ks, kd=kd, jitter=jitter, seed=seed)
+    assert np.array_equal(Xo.view(np.uint32), Xl.view(np.uint32))
+    assert so.tobytes() == sl.tobytes()
