@@ -143,10 +143,13 @@ oc_status oc_get_vertex_offsets(const oc_solver* s, int64_t* offsets /* n_instan
 
 /* State = X, V and the CG warm start dV (IMP:361, reused as the initial guess at
  * IMP:788).  Host pointers; any may be NULL to leave that array unchanged/unread.
- * Synchronous with respect to the handle's stream. */
+ * Synchronous with respect to the handle's stream.  oc_set_state stages the arrays and
+ * checks them on the device first: a NaN or Inf fails with OC_ERR_NON_FINITE and leaves
+ * the state unchanged. */
 oc_status oc_set_state(oc_solver* s, const float* X, const float* V, const float* dV);
 oc_status oc_get_state(oc_solver* s, float* X, float* V, float* dV);
-/* Same with device pointers (packed float triples); enqueued on the handle's stream. */
+/* Same with device pointers (packed float triples); enqueued on the handle's stream,
+ * with no wait and no check of the values. */
 oc_status oc_set_state_device(oc_solver* s, const float* X, const float* V, const float* dV);
 oc_status oc_get_state_device(oc_solver* s, float* X, float* V, float* dV);
 
@@ -156,9 +159,10 @@ oc_status oc_step(oc_solver* s, float dt, int32_t n_steps);
 oc_status oc_synchronize(oc_solver* s);
 /* The reference's StepPhysics on host arrays (IMP:873-880 over the globals X, V of
  * IMP:80-81): X and V (packed float triples, either may be NULL) are copied in, n_steps
- * steps run, and X and V are copied back out, with one wait on the handle's stream.
- * OC_ERR_NON_FINITE when the input held a NaN or Inf (the state then holds it too; set
- * a finite state before stepping again). */
+ * steps run, and X and V are copied back out.  The input is staged and checked on the
+ * device before it is committed (one wait), then the step and the copy back out end
+ * with a second wait.  A NaN or Inf in the input fails with OC_ERR_NON_FINITE and leaves
+ * both the device state and the caller's arrays unchanged. */
 oc_status oc_step_host(oc_solver* s, float dt, int32_t n_steps, float* X, float* V);
 /* Set the passes after the update (OC_PASS_* bits) of one cloth (instance >= 0) or of
  * every cloth (-1); the matrices and ratio stay those given at oc_create.  Waits for the
@@ -242,13 +246,16 @@ oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* t
  * system the caller assembled, such as the A and b that oc_assemble returns.
  *   A9      device, 9 floats per vertex (glm column-major, symmetric)
  *   b, x    device float triples; x holds the warm start on entry, the solution on return
- *   pinned  device, one byte per vertex (non-zero = pinned), or NULL
- *   stream  cudaStream_t, or NULL for the default stream; the call is synchronous
+ *   pinned  device, one byte per vertex (non-zero = pinned), or NULL; a pinned row's
+ *           solution is 0 and its A and b are not used
+ *   stream  cudaStream_t, or NULL for the default stream; the call is synchronous: it
+ *           waits on the stream between iterations and before it returns
  * Scratch is a fixed static device array sized for OC_NOALLOC_MAX_VERTICES vertices
  * (about 3.8 MB, held by every GPU that loads the library until exit); larger systems
- * return OC_ERR_UNSUPPORTED.  All calls on a device share that array: calls whose GPU
- * work overlaps race.  The first call on a device looks up the array's address; make
- * that call before any stream capture. */
+ * return OC_ERR_UNSUPPORTED.  All calls on a device share that array, which keeps the
+ * last call's contents (each call clears what must start at zero): calls whose GPU work
+ * overlaps race.  The first call on a device looks up the array's address; make that
+ * call before any stream capture. */
 #define OC_NOALLOC_MAX_VERTICES 65536
 oc_status oc_pcg_solve_noalloc(const float* A9, const float* b, float* x, const uint8_t* pinned, int32_t n_vertices,
                                int32_t cg_max_iter, float cg_tol, int32_t* cg_iters, uint32_t* flags, void* stream);

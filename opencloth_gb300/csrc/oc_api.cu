@@ -1219,21 +1219,39 @@ oc_status oc_get_state_device(oc_solver* s, float* X, float* V, float* dV) {
     return OC_OK;
 }
 
+namespace {
+
+// Copies the caller's host triples into the staging buffer and checks them on the device,
+// writing nothing into the state; returns OC_ERR_NON_FINITE when one holds a NaN or Inf.
+// The staged arrays are left in *sx, *sv, *sd (NULL where the caller passed NULL) for a
+// commit with launch_state_in.
+oc_status stage_checked(oc_solver* s, const float* X, const float* V, const float* dV, float** sx, float** sv,
+                        float** sd, const char* who) {
+    const size_t n3 = 3 * (size_t)s->nv;
+    *sx = X ? s->stage : nullptr;
+    *sv = V ? s->stage + n3 : nullptr;
+    *sd = dV ? s->stage + 2 * n3 : nullptr;
+    if (X) OC_TRY(cudaMemcpyAsync(*sx, X, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    if (V) OC_TRY(cudaMemcpyAsync(*sv, V, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    if (dV) OC_TRY(cudaMemcpyAsync(*sd, dV, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    OC_TRY(cudaMemsetAsync(s->d_err, 0, sizeof(int32_t), s->stream));
+    OC_TRY(launch_state_check(*sx, *sv, *sd, s->nv, s->d_err, s->stream));
+    OC_TRY(cudaMemcpyAsync(s->h_scalar, s->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    if (*s->h_scalar != 0)
+        return fail(s, OC_ERR_NON_FINITE, std::string(who) + ": non-finite value in the input state (nothing changed)");
+    return OC_OK;
+}
+
+}  // namespace
+
 oc_status oc_set_state(oc_solver* s, const float* X, const float* V, const float* dV) {
     if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
     OC_TRY(cudaSetDevice(s->device));
-    const size_t n3 = 3 * (size_t)s->nv;
-    float* sx = X ? s->stage : nullptr;
-    float* sv = V ? s->stage + n3 : nullptr;
-    float* sd = dV ? s->stage + 2 * n3 : nullptr;
-    if (X) OC_TRY(cudaMemcpyAsync(sx, X, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    if (V) OC_TRY(cudaMemcpyAsync(sv, V, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    if (dV) OC_TRY(cudaMemcpyAsync(sd, dV, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    OC_TRY(cudaMemsetAsync(s->d_err, 0, sizeof(int32_t), s->stream));
+    float *sx, *sv, *sd;
+    if (oc_status st = stage_checked(s, X, V, dV, &sx, &sv, &sd, "oc_set_state")) return st;
     OC_TRY(launch_state_in(s->args, sx, sv, sd, s->nv, s->d_err, s->stream));
-    OC_TRY(cudaMemcpyAsync(s->h_scalar, s->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
     OC_TRY(cudaStreamSynchronize(s->stream));
-    if (*s->h_scalar != 0) return fail(s, OC_ERR_NON_FINITE, "oc_set_state: non-finite value in the new state");
     return OC_OK;
 }
 
@@ -1256,21 +1274,16 @@ oc_status oc_step_host(oc_solver* s, float dt, int32_t n_steps, float* X, float*
     if (!valid_solver(s) || n_steps < 0 || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
     OC_TRY(cudaSetDevice(s->device));
     const size_t n3 = 3 * (size_t)s->nv;
-    float* sx = X ? s->stage : nullptr;
-    float* sv = V ? s->stage + n3 : nullptr;
-    if (X) OC_TRY(cudaMemcpyAsync(sx, X, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    if (V) OC_TRY(cudaMemcpyAsync(sv, V, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    OC_TRY(cudaMemsetAsync(s->d_err, 0, sizeof(int32_t), s->stream));
+    // The input is staged and checked before anything is committed: a NaN or Inf leaves
+    // the device state and the caller's arrays as they were.
+    float *sx, *sv, *sd;
+    if (oc_status st = stage_checked(s, X, V, nullptr, &sx, &sv, &sd, "oc_step_host")) return st;
     OC_TRY(launch_state_in(s->args, sx, sv, nullptr, s->nv, s->d_err, s->stream));
     if (oc_status st = oc_step(s, dt, n_steps)) return st;
     OC_TRY(launch_state_out(s->args, sx, sv, nullptr, s->nv, s->stream));
     if (X) OC_TRY(cudaMemcpyAsync(X, sx, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     if (V) OC_TRY(cudaMemcpyAsync(V, sv, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
-    // The input check's flag, read after the step (a host-driven step uses the same
-    // pinned scalar for its loop control; the step's kernels do not touch the flag).
-    OC_TRY(cudaMemcpyAsync(s->h_scalar, s->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
     OC_TRY(cudaStreamSynchronize(s->stream));
-    if (*s->h_scalar != 0) return fail(s, OC_ERR_NON_FINITE, "oc_step_host: non-finite value in the input state");
     return check_device_error(s);
 }
 

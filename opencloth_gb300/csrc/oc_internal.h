@@ -202,6 +202,9 @@ cudaError_t launch_resident(const StepArgs& a, const ResidentLaunch& L, int thre
 cudaError_t launch_state_in(const StepArgs& a, const float* X3, const float* V3, const float* dV3, int64_t nv,
                             int32_t* err, cudaStream_t stream);
 cudaError_t launch_state_out(const StepArgs& a, float* X3, float* V3, float* dV3, int64_t nv, cudaStream_t stream);
+// Sets *err when a staged triple array (any may be NULL) holds a NaN or Inf; writes nothing else.
+cudaError_t launch_state_check(const float* X3, const float* V3, const float* dV3, int64_t nv, int32_t* err,
+                               cudaStream_t stream);
 
 // Topology / validation helpers (oc_topology.cpp).
 struct PackedHost {

@@ -721,6 +721,18 @@ __global__ void k_state_in(const StepArgs a, const float* X3, const float* V3, c
     }
 }
 
+// Flags a non-finite value among staged float triples in *err, writing nothing else: the
+// host commits the staged state with k_state_in only when the flag stays clear.
+__global__ void k_state_check(const float* X3, const float* V3, const float* dV3, int64_t nv, int32_t* err) {
+    bool bad = false;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < 3 * nv; g += (int64_t)gridDim.x * blockDim.x) {
+        if (X3) bad |= !isfinite(X3[g]);
+        if (V3) bad |= !isfinite(V3[g]);
+        if (dV3) bad |= !isfinite(dV3[g]);
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, 1);
+}
+
 __global__ void k_state_out(const StepArgs a, float* X3, float* V3, float* dV3, int64_t nv) {
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nv; g += (int64_t)gridDim.x * blockDim.x) {
         if (X3) {
@@ -819,6 +831,12 @@ static int state_blocks(int64_t nv) {
 cudaError_t launch_state_in(const StepArgs& a, const float* X3, const float* V3, const float* dV3, int64_t nv,
                             int32_t* err, cudaStream_t stream) {
     k_state_in<<<state_blocks(nv), kThreads, 0, stream>>>(a, X3, V3, dV3, nv, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_state_check(const float* X3, const float* V3, const float* dV3, int64_t nv, int32_t* err,
+                               cudaStream_t stream) {
+    k_state_check<<<state_blocks(3 * nv), kThreads, 0, stream>>>(X3, V3, dV3, nv, err);
     return cudaGetLastError();
 }
 

@@ -1,6 +1,6 @@
-"""State transfer through the C ABI: page-locked host arrays are read and written by the
-packing kernels directly (over the GPU's link to host memory), pageable arrays through a
-staging buffer and the copy engine.  Both must move the same bits."""
+"""State transfer through the C ABI: page-locked and pageable host arrays both go through
+the handle's staging buffer and the copy engine and must move the same bits; input that
+holds a NaN or Inf is refused before anything is committed."""
 import numpy as np
 import pytest
 
@@ -75,12 +75,46 @@ def test_step_host_equals_set_step_get(executor):
 
 
 def test_step_host_rejects_non_finite_input():
+    """A NaN or Inf in oc_step_host's input fails with OC_ERR_NON_FINITE and changes
+    neither the device state nor the caller's arrays; the handle then steps on as if the
+    call had not happened."""
     from opencloth_gb300 import OcError
 
-    desc, _, X, V = seeded_cloth(9, 9, seed=2)
-    Xi = X.copy()
-    Xi[7, 2] = np.inf
+    desc, _, X, V = seeded_cloth(9, 9, seed=2, velocity=0.01)
+    with ClothSolver(desc) as s, ClothSolver(desc) as t:
+        for h in (s, t):
+            h.set_state(X, V)
+            h.step(DT, 2)
+        before = s.get_state()
+        for bad in ((7, 2, np.inf), (40, 0, np.nan)):
+            Xi, Vi = X.copy(), V.copy()
+            (Xi if bad[2] == np.inf else Vi)[bad[0], bad[1]] = bad[2]
+            Xc, Vc = Xi.copy(), Vi.copy()
+            with pytest.raises(OcError) as e:
+                s.step_host(Xi, Vi, DT, 1)
+            assert e.value.status == 3
+            assert np.array_equal(Xi, Xc, equal_nan=True) and np.array_equal(Vi, Vc, equal_nan=True)
+            after = s.get_state()
+            for a, b in zip(before, after):
+                assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+        s.step(DT, 3)
+        t.step(DT, 3)
+        for a, b in zip(s.get_state(), t.get_state()):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_set_state_rejects_non_finite_input_without_effect():
+    from opencloth_gb300 import OcError
+
+    desc, _, X, V = seeded_cloth(9, 9, seed=4, velocity=0.01)
     with ClothSolver(desc) as s:
+        s.set_state(X, V)
+        s.step(DT, 1)
+        before = s.get_state()
+        dV = np.zeros_like(X)
+        dV[5, 1] = np.nan
         with pytest.raises(OcError) as e:
-            s.step_host(Xi, V.copy(), DT, 1)
+            s.set_state(X, V, dV)
         assert e.value.status == 3
+        for a, b in zip(before, s.get_state()):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
