@@ -16,12 +16,18 @@
 //
 // The first call on a device looks the array up (cudaGetSymbolAddress with that
 // device current) and caches the address; make that first call before any stream
-// capture.
+// capture.  Two host threads making their first calls on one device at the same time
+// both look it up and store the same address; the cache entries are atomics.
+//
+// The call is synchronous: it waits on the stream between CG iterations (the host reads
+// whether the system is still iterating) and before it returns.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 
+#include "oc_device.cuh"
 #include "oc_internal.h"
 
 namespace oc {
@@ -47,38 +53,23 @@ struct NoAllocScratch {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
 constexpr int kMaxDevices = 64;
-NoAllocScratch* g_scratch_ptr[kMaxDevices] = {nullptr};
-
-__device__ __forceinline__ double na_warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
-__device__ double na_block_sum(double v) {
-    __shared__ double part[32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    v = na_warp_sum(v);
-    __syncthreads();
-    if (lane == 0) part[w] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (w == 0) {
-        t = (lane < (int)(blockDim.x >> 5)) ? part[lane] : 0.0;
-        t = na_warp_sum(t);
-    }
-    return t;
-}
+std::atomic<NoAllocScratch*> g_scratch_ptr[kMaxDevices] = {};
 
 // CG set-up of IMP:310-318 on a given system: A (glm column-major, 9 floats per
 // vertex, symmetric part used), b and the warm start x (float triples), pinned rows
-// filtered out — the same arithmetic as the set-up inside the step's assembly.
+// filtered out.  Per vertex this is the arithmetic of the set-up inside the step's
+// assembly, and delta0's terms are summed as the step sums them (error-free float pairs
+// per thread and warp, FP64 above).  The blocks here hold 2048 vertices each, which need
+// not be the step's partition of the same vertices, so delta0 can differ from the step's
+// by the FP64 rounding of a different grouping (about 2^-48 relative).  A pinned row
+// gets a zero direction without a reciprocal of its diagonal, so its A may be anything
+// finite, zero included.
 __global__ void __launch_bounds__(kNaThreads) k_noalloc_setup(const StepArgs a, const float* A9, const float* b,
                                                                const float* x3, const uint8_t* pinned, int32_t n) {
     const int blk = blockIdx.x;
     const int64_t v0 = (int64_t)blk * kNaVertsPerBlock;
     const int64_t v1 = min((int64_t)n, v0 + kNaVertsPerBlock);
-    double part = 0.0;
+    Acc part = acc_zero();
     for (int64_t g = v0 + threadIdx.x; g < v1; g += blockDim.x) {
         const float* m = A9 + 9 * g;
         const float A[6] = {m[0], m[1], m[2], m[4], m[5], m[8]};
@@ -90,9 +81,15 @@ __global__ void __launch_bounds__(kNaThreads) k_noalloc_setup(const StepArgs a, 
         const float az = A[2] * x0 + A[4] * x1 + A[5] * x2;
         float r0 = b[3 * g] - ax, r1 = b[3 * g + 1] - ay, r2 = b[3 * g + 2] - az;
         if (pin) r0 = r1 = r2 = 0.0f;
-        const float pi0 = 1.0f / A[0], pi1 = 1.0f / A[3], pi2 = 1.0f / A[5];
         const float pr0 = A[0] * r0, pr1 = A[3] * r1, pr2 = A[5] * r2;
-        part += (double)(r0 * pr0 + r1 * pr1 + r2 * pr2);
+        float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f;
+        if (!pin) {
+            const float pi0 = 1.0f / A[0], pi1 = 1.0f / A[3], pi2 = 1.0f / A[5];
+            d0 = pi0 * r0;
+            d1 = pi1 * r1;
+            d2 = pi2 * r2;
+        }
+        acc_add(part, pin ? 0.0f : r0 * pr0 + r1 * pr1 + r2 * pr2);
 #pragma unroll
         for (int k = 0; k < 6; ++k) a.A[k][g] = A[k];
         a.x[0][g] = x0;
@@ -101,13 +98,13 @@ __global__ void __launch_bounds__(kNaThreads) k_noalloc_setup(const StepArgs a, 
         a.r[0][g] = r0;
         a.r[1][g] = r1;
         a.r[2][g] = r2;
-        a.d[0][g] = pi0 * r0;
-        a.d[1][g] = pi1 * r1;
-        a.d[2][g] = pi2 * r2;
+        a.d[0][g] = d0;
+        a.d[1][g] = d1;
+        a.d[2][g] = d2;
     }
     // One instance: the last block sums the partials in order and primes the loop.
     __shared__ int s_last;
-    const double bsum = na_block_sum(part);
+    const double bsum = block_sum_acc(part);
     if (threadIdx.x == 0) {
         a.partials[blk] = bsum;
         __threadfence();
@@ -118,7 +115,7 @@ __global__ void __launch_bounds__(kNaThreads) k_noalloc_setup(const StepArgs a, 
         __threadfence();
         double acc = 0.0;
         for (int j = threadIdx.x; j < (int)gridDim.x; j += blockDim.x) acc += __ldcg(a.partials + j);
-        const double total = na_block_sum(acc);
+        const double total = block_sum(acc);
         if (threadIdx.x == 0) {
             InstState& st = *a.state;
             st.ticket = 0;
@@ -163,13 +160,14 @@ extern "C" oc_status oc_pcg_solve_noalloc(const float* A9, const float* b, float
     if (n_vertices > OC_NOALLOC_MAX_VERTICES) return OC_ERR_UNSUPPORTED;  // beyond the static scratch
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return OC_ERR_CUDA;
-    if (!g_scratch_ptr[dev]) {
+    NoAllocScratch* sc = g_scratch_ptr[dev].load(std::memory_order_acquire);
+    if (!sc) {
         // Set-up, once per device, with that device current.
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return OC_ERR_CUDA;
-        g_scratch_ptr[dev] = static_cast<NoAllocScratch*>(p);
+        sc = static_cast<NoAllocScratch*>(p);
+        g_scratch_ptr[dev].store(sc, std::memory_order_release);
     }
-    NoAllocScratch* sc = g_scratch_ptr[dev];
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int nblk = (n_vertices + kNaVertsPerBlock - 1) / kNaVertsPerBlock;
 

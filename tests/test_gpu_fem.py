@@ -93,13 +93,28 @@ def test_generated_system_solves_like_the_oracle():
 def test_validation():
     sys_ = fem_golden("m0")[0]
     with BsrSolver([desc(sys_)]) as s:
-        blocks = sys_.blocks.copy()
-        free_row = int(np.nonzero(sys_.fixed == 0)[0][0])
-        blocks[sys_.row_ptr[free_row]] = np.nan
-        with pytest.raises(OcError) as e:
-            s.set_system(blocks, sys_.b, sys_.V)
-        assert e.value.status == 3
+        # A refused system changes nothing: the next solve is the solve of the system
+        # committed before it, bit for bit.
         s.set_system(sys_.blocks, sys_.b, sys_.V)  # infinities in fixed rows are the reference's own
+        s.solve()
+        V_ok, r_ok = s.solution()
+        free_row = int(np.nonzero(sys_.fixed == 0)[0][0])
+        for what in ("blocks", "b", "V"):
+            s.set_system(sys_.blocks, sys_.b, sys_.V)  # the solve updates V in place: start over
+            blocks, b, V = sys_.blocks.copy(), sys_.b.copy(), sys_.V.copy()
+            if what == "blocks":
+                blocks[sys_.row_ptr[free_row]] = np.nan
+            elif what == "b":
+                b[free_row, 1] = np.inf
+            else:
+                V[free_row, 2] = np.nan
+            with pytest.raises(OcError) as e:
+                s.set_system(blocks, b, V)
+            assert e.value.status == 3, what
+            s.solve()
+            V2, r2 = s.solution()
+            assert np.array_equal(V2.view(np.uint32), V_ok.view(np.uint32)), what
+            assert np.array_equal(r2.view(np.uint32), r_ok.view(np.uint32)), what
     bad = desc(sys_)
     bad["col"] = sys_.col.copy()
     bad["col"][[0, 1]] = bad["col"][[1, 0]]  # not ascending within the row

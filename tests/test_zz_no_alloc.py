@@ -50,7 +50,10 @@ def test_noalloc_solve_matches_step_solve_on_two_calls():
             assert st == 0, (call, N.STATUS_NAMES.get(st, st))
             x = d_x.cpu().numpy().reshape(-1, 3)
             assert rel(x, dV) <= TOL, (call, rel(x, dV))
-            assert iters.value == step_iters and flags.value == 0, (call, iters.value, step_iters, flags.value)
+            # The two solves group delta0's FP64 partials by different block partitions
+            # (about 2^-48 apart), which could move the stop test by one iteration.
+            assert abs(iters.value - step_iters) <= 1 and flags.value == 0, (call, iters.value, step_iters,
+                                                                             flags.value)
             warm = dV
 
 
@@ -61,3 +64,37 @@ def test_noalloc_solve_rejects_oversize_and_bad_arguments():
     # Sizes beyond the static scratch are refused before any device work.
     big = 65536 + 1
     assert lib.oc_pcg_solve_noalloc(1, 1, 1, None, big, 10, 1e-3, C.byref(it), C.byref(fl), None) == 7
+
+
+def test_noalloc_solve_ignores_pinned_rows_system():
+    """A pinned row's block and right-hand side are not used: a zero diagonal there (what a
+    caller that filters pinned rows out of its own assembly may leave) still solves, and the
+    free rows match the solve of the system with the pinned rows' original values."""
+    import torch
+
+    lib = N.load()
+    desc, _, X, V = seeded_cloth(33, 17, seed=5, random_params=False, velocity=0.01)
+    n = desc.n_vertices
+    mask = np.zeros(n, np.uint8)
+    mask[desc.pinned] = 1
+    with ClothSolver(desc) as s:
+        s.set_state(X, V, np.zeros_like(X))
+        A9, b = s.assemble(DT)
+    out = []
+    for zero in (False, True):
+        A, bb = A9.copy(), b.copy()
+        if zero:
+            A[desc.pinned] = 0.0
+            bb[desc.pinned] = 123.0
+        d_A = torch.from_numpy(np.ascontiguousarray(A.reshape(-1))).cuda()
+        d_b = torch.from_numpy(np.ascontiguousarray(bb.reshape(-1))).cuda()
+        d_x = torch.zeros(3 * n, dtype=torch.float32, device="cuda")
+        d_pin = torch.from_numpy(mask).cuda()
+        torch.cuda.synchronize()
+        iters, flags = C.c_int32(-1), C.c_uint32(99)
+        st = lib.oc_pcg_solve_noalloc(d_A.data_ptr(), d_b.data_ptr(), d_x.data_ptr(), d_pin.data_ptr(), n,
+                                      desc.cg_max_iter, desc.cg_tol, C.byref(iters), C.byref(flags), None)
+        assert st == 0 and flags.value == 0, (zero, st, flags.value)
+        out.append(d_x.cpu().numpy().reshape(-1, 3))
+    assert np.array_equal(out[0], out[1])
+    assert not out[1][desc.pinned].any()
