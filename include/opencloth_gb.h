@@ -237,6 +237,18 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
                            float* dL_dKs, float* dL_dKd, float* dL_dext);
 oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* tape_bytes);
 
+/* ---- testing aid: the bounded grid-barrier wait ---------------------------------- */
+/* The persistent CG (one cooperative launch per step, used for up to 16 streamed cloths
+ * and for the adjoint solves of up to 16 cloths) waits at grid barriers; each wait gives
+ * up after a bounded number of polls and the step then fails with OC_ERR_DEVICE_TIMEOUT
+ * at the next oc_synchronize / oc_get_state / oc_get_stats, after which the handle steps
+ * on (the step whose wait gave up applied no update).  For tests of that path: from the
+ * next step on, block `withhold_block` of those launches returns at its first barrier
+ * without arriving (-1: none), and a wait gives up after `max_polls` polls (0: the
+ * default, about half a second).  Nothing waits longer than that bound.  Fails with
+ * OC_ERR_UNSUPPORTED when the handle runs no persistent CG. */
+oc_status oc_test_barrier_timeout(oc_solver* s, int32_t withhold_block, uint32_t max_polls);
+
 /* ---- allocation-free solve -------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory
  * around a solve — an engine that manages a fixed device-memory budget itself, or a

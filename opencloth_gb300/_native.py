@@ -121,6 +121,7 @@ SIGNATURES = {
     "oc_tape_forward": (C.c_int32, [_P, C.c_float, C.c_int32, C.c_int32, C.c_int64]),
     "oc_tape_backward": (C.c_int32, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "oc_tape_info": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
+    "oc_test_barrier_timeout": (C.c_int32, [_P, C.c_int32, C.c_uint32]),
     "oc_pcg_solve_noalloc": (C.c_int32, [_P, _P, _P, _P, C.c_int32, C.c_int32, C.c_float, C.POINTER(C.c_int32),
                                          C.POINTER(C.c_uint32), _P]),
     "oc_bsr_create": (C.c_int32, [C.POINTER(BsrDescC), C.c_int32, C.POINTER(OptionsC), C.POINTER(_P)]),

@@ -146,12 +146,22 @@ oc_status fail_cuda(oc_solver* s, cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return fail_cuda(s, e_, #call); \
     } while (0)
 
-// A grid barrier of k_cg_persist that gave up (the stream is synchronised).
+// Polls of a grid barrier's generation word before k_cg_persist gives up (about half a
+// second with its 32 ns back-off).
+constexpr uint32_t kDefaultBarrierPolls = 1u << 22;
+
+// A grid barrier of k_cg_persist that gave up (the stream is synchronised).  The error
+// word is cleared once reported; the next launch starts from a reset arrival word, so
+// the handle steps on.
 oc_status check_device_error(oc_solver* s) {
     if (!s->d_perr) return OC_OK;
     int h = 0;
     OC_TRY(cudaMemcpy(&h, s->d_perr, sizeof(int), cudaMemcpyDeviceToHost));
-    if (h != 0) return fail(s, OC_ERR_DEVICE_TIMEOUT, "k_cg_persist: a grid barrier gave up");
+    if (h != 0) {
+        OC_TRY(cudaMemset(s->d_perr, 0, sizeof(int)));
+        return fail(s, OC_ERR_DEVICE_TIMEOUT,
+                    "k_cg_persist: a grid barrier gave up (that step's update was not applied)");
+    }
     return OC_OK;
 }
 
@@ -1177,6 +1187,8 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     OC_CREATE_TRY(cudaMallocHost(&s->h_state, sizeof(InstState) * P.n_inst));
     OC_CREATE_TRY(cudaMallocHost(&s->h_scalar, sizeof(int32_t)));
     a.vpt = vpt;
+    a.barrier_polls = kDefaultBarrierPolls;
+    a.withhold_block = -1;
     OC_CREATE_TRY(cudaDeviceSynchronize());
 #undef OC_CREATE_TRY
     *out = s;
@@ -1827,6 +1839,25 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
     if (dL_dKs) OC_TRY(cudaMemcpyAsync(dL_dKs, j.gKs, sizeof(float) * s->ns, cudaMemcpyDeviceToHost, s->stream));
     if (dL_dKd) OC_TRY(cudaMemcpyAsync(dL_dKd, j.gKd, sizeof(float) * s->ns, cudaMemcpyDeviceToHost, s->stream));
     OC_TRY(cudaStreamSynchronize(s->stream));
+    return OC_OK;
+}
+
+oc_status oc_test_barrier_timeout(oc_solver* s, int32_t withhold_block, uint32_t max_polls) {
+    if (!valid_solver(s) || withhold_block < -1) return OC_ERR_INVALID_ARGUMENT;
+    if (!s->persist && !s->adj_persist) return fail(s, OC_ERR_UNSUPPORTED, "the handle runs no persistent CG");
+    OC_TRY(cudaSetDevice(s->device));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    s->args.withhold_block = withhold_block;
+    s->args.barrier_polls = max_polls > 0 ? max_polls : kDefaultBarrierPolls;
+    // The step graph holds the launch arguments: rebuild it at the next step.
+    if (s->exec) {
+        cudaGraphExecDestroy(s->exec);
+        s->exec = nullptr;
+    }
+    if (s->graph) {
+        cudaGraphDestroy(s->graph);
+        s->graph = nullptr;
+    }
     return OC_OK;
 }
 

@@ -83,6 +83,10 @@ struct StepArgs {
     unsigned long long cond; // cudaGraphConditionalHandle
     int32_t all_streamed;    // 1: every cloth's CG runs in the streamed loop (adjoint solves)
     int32_t cg_only;         // k_cg_persist: 1 = the CG alone, no update (adjoint solves)
+    // k_cg_persist's grid barrier: polls of the generation word before a wait gives up,
+    // and a block that never arrives (-1: none; set only by oc_test_barrier_timeout).
+    uint32_t barrier_polls;
+    int32_t withhold_block;
     float* dbg_F;            // optional debug outputs (float triples) or nullptr
     float* dbg_A9;
     float* dbg_b;

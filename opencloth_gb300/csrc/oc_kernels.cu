@@ -360,7 +360,6 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
 // fused at the end (it is per vertex).
 
 constexpr int kPersistMaxInst = 16;       // streamed cloths one launch handles
-constexpr unsigned kBarrierSpins = 1u << 22;  // a barrier gives up after ~0.5 s
 
 __device__ __forceinline__ unsigned load_acquire(const unsigned* p) {
     unsigned v;
@@ -404,14 +403,19 @@ struct PersistScalars {
 // is, flips bit 31 and the low bits are back where they started (no reset).  That last
 // block sums the partials of every active cloth into totals[] and then bumps the
 // generation bar[32] with a release; the others poll the generation with acquire loads
-// and read the totals into tot[] (shared).  A wait that runs out sets bit 0 of *err and
-// returns false (the kernel then unwinds; the host reports the error).
+// and read the totals into tot[] (shared).  A wait gives up after a.barrier_polls polls
+// (the default, 2^22 polls with a 32 ns back-off, is about half a second): it sets bit 0
+// of *err and returns false, the kernel unwinds and the host reports the error.  The
+// block a.withhold_block (a testing aid; normally -1) returns false at its first barrier
+// without arriving, so every other block's wait runs out.
 __device__ bool barrier_totals(const StepArgs& a, const int32_t* inst_ids, int n_inst, const PersistScalars* sc,
                                unsigned* bar, double* totals, int* err, double* tot) {
     __shared__ int s_last, s_ok;
     unsigned* gen = bar + 32;
     __syncthreads();  // this block's partial (thread 0's store) precedes its arrival
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && (int)blockIdx.x == a.withhold_block) {
+        s_ok = 0;
+    } else if (threadIdx.x == 0) {
         s_ok = 1;
         const unsigned nb = gridDim.x;
         const unsigned add = blockIdx.x == 0 ? 0x80000000u - (nb - 1) : 1u;
@@ -421,7 +425,7 @@ __device__ bool barrier_totals(const StepArgs& a, const int32_t* inst_ids, int n
         if (!s_last) {
             unsigned spins = 0;
             while (load_acquire(gen) == g0) {
-                if (++spins > kBarrierSpins) {
+                if (++spins > a.barrier_polls) {
                     atomicOr(err, 1);
                     s_ok = 0;
                     break;

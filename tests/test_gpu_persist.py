@@ -88,3 +88,35 @@ def test_launch_count_is_per_step():
         s.step(DT, 5)
         # assembly + the persistent CG (with the update) per step
         assert s.launch_count() - l0 == 10
+
+
+def test_barrier_wait_runs_out_and_the_handle_steps_on():
+    """One block of the persistent CG withholds its arrival at the first grid barrier
+    and the others' waits run out after a short poll limit: the step reports
+    OC_ERR_DEVICE_TIMEOUT (status 8), applies no update, and the handle then steps on
+    with the same bits as a handle that never saw the fault."""
+    from opencloth_gb300 import OcError
+    from opencloth_gb300 import _native as N
+
+    desc, X, V = cloth(65, 65, seed=31)
+    with ClothSolver(desc, executor="streamed") as s, ClothSolver(desc, executor="streamed") as t:
+        lib = N.load()
+        for h in (s, t):
+            h.set_state(X, V)
+            h.step(DT, 1)
+        before = s.get_state()
+        assert lib.oc_test_barrier_timeout(s._h, 1, 2000) == 0
+        s.step(DT, 1)
+        with pytest.raises(OcError) as e:
+            s.synchronize()
+        assert e.value.status == 8
+        after = s.get_state()
+        assert same_bits(before[0], after[0]) and same_bits(before[1], after[1])  # no update applied
+        assert lib.oc_test_barrier_timeout(s._h, -1, 0) == 0
+        state = t.get_state()
+        s.set_state(*state)
+        s.step(DT, 3)
+        t.step(DT, 3)
+        for a, b in zip(s.get_state(), t.get_state()):
+            assert same_bits(a, b)
+        assert np.array_equal(s.stats()[0], t.stats()[0])
