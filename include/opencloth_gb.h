@@ -237,6 +237,60 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
                            float* dL_dKs, float* dL_dKd, float* dL_dext);
 oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* tape_bytes);
 
+/* ---- launch configuration and its autotuner ------------------------------------------ */
+/* How a handle launches its step: which cloths run resident and in what CTA shape, whether
+ * the resident kernel also assembles, whether up to 16 streamed cloths run their CG as one
+ * cooperative launch, the force-gather variant, and the strip sweep of grid cloths.  None
+ * of these changes the method; the resident kernel's reductions follow its CTA shape, so
+ * results of different resident shapes can differ in the last bits (each shape is
+ * deterministic).  No counterpart in the reference (its step has one serial code path). */
+typedef struct oc_launch_config {
+    int32_t resident_max_vertices; /* OC_EXEC_AUTO: cloths up to this many vertices run resident; 0: none */
+    int32_t resident_vcta;         /* vertices per resident CTA: 256, 512, 1024 or 2048 */
+    int32_t resident_threads;      /* threads per resident CTA: 128, 256 or 512, with vcta <= 4 x threads */
+    int32_t resident_fused;        /* 1: resident cloths assemble inside the resident kernel */
+    int32_t persist;               /* 1: the CG of up to 16 streamed cloths as one cooperative launch */
+    int32_t gather_variant;        /* incidence-record force gather: 0 block-cooperative, 1..6 per vertex */
+    int32_t strip;                 /* 1: grid cloths in the reference's spring order take the strip sweep */
+    int32_t strip_rows;            /* rows per strip band (1 ... 64); 0: chosen from the work size */
+    int32_t strip_variant;         /* strip CTAs per SM the registers are capped for: 2 or 3 */
+} oc_launch_config;
+
+oc_status oc_get_launch_config(const oc_solver* s, oc_launch_config* cfg);
+/* Re-plan the handle's launches (tables, resident buckets, graphs are rebuilt; the state is
+ * kept; the adjoint tape is invalidated).  OC_ERR_INVALID_ARGUMENT for a value outside the
+ * ranges above, OC_ERR_UNSUPPORTED when the executor cannot honour it (OC_EXEC_RESIDENT
+ * with a cloth above resident_max_vertices); the earlier configuration then stays. */
+oc_status oc_set_launch_config(oc_solver* s, const oc_launch_config* cfg);
+
+/* Times candidate configurations on the handle's own cloths and current state and keeps
+ * the fastest: one knob at a time from the current configuration (strip sweep on/off, band
+ * rows and register cap; resident size cut-off, CTA shape and fused assembly; persistent
+ * or WHILE-loop CG; gather variant), each candidate replaying the step graph for about
+ * 20 ms after two warm-up steps (CUDA events on the handle's stream); a candidate must be
+ * 1% faster to replace the current one.  The state is saved first and restored after every
+ * candidate, so tuning does not advance the simulation.  With cache_path (may be NULL) the
+ * choice is looked up first by oc_tune_key's key and stored after tuning (flags:
+ * OC_TUNE_USE_CACHE, OC_TUNE_STORE).  *chosen and *ms_per_step (either may be NULL) receive
+ * the configuration in use and its measured time per step (0 when taken from the cache). */
+#define OC_TUNE_USE_CACHE 1
+#define OC_TUNE_STORE 2
+oc_status oc_autotune(oc_solver* s, float dt, const char* cache_path, int32_t flags, oc_launch_config* chosen,
+                      double* ms_per_step);
+
+/* Host only.  The tuning cache key of a set of cloths on a GPU: the GPU's name and SM
+ * count, and a 64-bit FNV-1a hash of the sorted per-cloth signatures (vertices, grid
+ * shape, Jacobian mode, passes), written as text into key (key_size >= 96). */
+oc_status oc_tune_key(const oc_cloth_desc* descs, int32_t n_instances, const char* gpu_name, int32_t sm_count,
+                      char* key, int32_t key_size);
+/* The handle's own key (its device's name and SM count). */
+oc_status oc_tune_key_of(const oc_solver* s, char* key, int32_t key_size);
+/* Host only.  The cache is a text file, one line per key: the key, the nine configuration
+ * fields and the measured ms per step; a later line for a key replaces an earlier one.
+ * *found is 1 when the key is present. */
+oc_status oc_tune_cache_lookup(const char* path, const char* key, oc_launch_config* cfg, int32_t* found);
+oc_status oc_tune_cache_store(const char* path, const char* key, const oc_launch_config* cfg, double ms_per_step);
+
 /* ---- testing aid: the bounded grid-barrier wait ---------------------------------- */
 /* The persistent CG (one cooperative launch per step, used for up to 16 streamed cloths
  * and for the adjoint solves of up to 16 cloths) waits at grid barriers; each wait gives

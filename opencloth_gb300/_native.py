@@ -88,6 +88,14 @@ class OptionsC(C.Structure):
     ]
 
 
+class LaunchConfigC(C.Structure):
+    _fields_ = [(name, C.c_int32) for name in (
+        "resident_max_vertices", "resident_vcta", "resident_threads", "resident_fused", "persist", "gather_variant",
+        "strip", "strip_rows", "strip_variant")]
+
+
+TUNE_USE_CACHE, TUNE_STORE = 1, 2
+
 # name -> (restype, argtypes); every symbol include/opencloth_gb.h declares.
 _P = C.c_void_p
 SIGNATURES = {
@@ -122,6 +130,14 @@ SIGNATURES = {
     "oc_tape_backward": (C.c_int32, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "oc_tape_info": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
     "oc_test_barrier_timeout": (C.c_int32, [_P, C.c_int32, C.c_uint32]),
+    "oc_get_launch_config": (C.c_int32, [_P, C.POINTER(LaunchConfigC)]),
+    "oc_set_launch_config": (C.c_int32, [_P, C.POINTER(LaunchConfigC)]),
+    "oc_autotune": (C.c_int32, [_P, C.c_float, C.c_char_p, C.c_int32, C.POINTER(LaunchConfigC),
+                                C.POINTER(C.c_double)]),
+    "oc_tune_key": (C.c_int32, [C.POINTER(ClothDescC), C.c_int32, C.c_char_p, C.c_int32, C.c_char_p, C.c_int32]),
+    "oc_tune_key_of": (C.c_int32, [_P, C.c_char_p, C.c_int32]),
+    "oc_tune_cache_lookup": (C.c_int32, [C.c_char_p, C.c_char_p, C.POINTER(LaunchConfigC), C.POINTER(C.c_int32)]),
+    "oc_tune_cache_store": (C.c_int32, [C.c_char_p, C.c_char_p, C.POINTER(LaunchConfigC), C.c_double]),
     "oc_pcg_solve_noalloc": (C.c_int32, [_P, _P, _P, _P, C.c_int32, C.c_int32, C.c_float, C.POINTER(C.c_int32),
                                          C.POINTER(C.c_uint32), _P]),
     "oc_bsr_create": (C.c_int32, [C.POINTER(BsrDescC), C.c_int32, C.POINTER(OptionsC), C.POINTER(_P)]),

@@ -325,6 +325,38 @@ class ClothSolver:
         self._call(self._lib.oc_tape_info(self._h, C.byref(every), C.byref(nbytes)))
         return int(every.value), int(nbytes.value)
 
+    def launch_config(self) -> dict:
+        """The handle's launch configuration (oc_launch_config) as a dict."""
+        c = N.LaunchConfigC()
+        self._call(self._lib.oc_get_launch_config(self._h, C.byref(c)))
+        return {name: int(getattr(c, name)) for name, _ in N.LaunchConfigC._fields_}
+
+    def set_launch_config(self, **fields) -> None:
+        """Change fields of the launch configuration (re-plans the handle's launches)."""
+        cfg = self.launch_config()
+        unknown = set(fields) - set(cfg)
+        if unknown:
+            raise KeyError(f"unknown launch configuration fields: {sorted(unknown)}")
+        cfg.update(fields)
+        c = N.LaunchConfigC(**cfg)
+        self._call(self._lib.oc_set_launch_config(self._h, C.byref(c)))
+
+    def autotune(self, dt: float, cache_path: str | None = None, use_cache: bool = True, store: bool = True):
+        """Time candidate launch configurations on the current state (which is kept) and
+        keep the fastest; returns (configuration dict, measured ms per step, 0 when it came
+        from the cache)."""
+        c = N.LaunchConfigC()
+        ms = C.c_double()
+        flags = (N.TUNE_USE_CACHE if use_cache else 0) | (N.TUNE_STORE if store else 0)
+        path = cache_path.encode() if cache_path else None
+        self._call(self._lib.oc_autotune(self._h, float(dt), path, flags, C.byref(c), C.byref(ms)))
+        return {name: int(getattr(c, name)) for name, _ in N.LaunchConfigC._fields_}, float(ms.value)
+
+    def tune_key(self) -> str:
+        buf = C.create_string_buffer(256)
+        self._call(self._lib.oc_tune_key_of(self._h, buf, 256))
+        return buf.value.decode()
+
     def launch_count(self) -> int:
         n = C.c_int64()
         self._call(self._lib.oc_get_launch_count(self._h, C.byref(n)))

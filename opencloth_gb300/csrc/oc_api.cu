@@ -7,13 +7,16 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <map>
 #include <tuple>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <new>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -59,6 +62,20 @@ struct oc_solver {
     int32_t n_asm_blocks = 0;
     BlockInfo* d_grid_blocks = nullptr;  // REFERENCE grid cloths on the stencil gather
     int32_t n_grid_blocks = 0;
+    // Grid cloths on the strip sweep (k_assemble_strip, then k_assemble_reduce over their
+    // standard blocks and k_assemble_finish per cloth): the work items (in
+    // args.strip_work), each cloth's range of them and its index in args.strip_ids.
+    BlockInfo* d_sred_blocks = nullptr;
+    int32_t n_sred_blocks = 0;
+    std::vector<std::pair<int32_t, int32_t>> strip_range;
+    std::vector<int32_t> strip_pos;
+    // The launch configuration (oc_launch_config) and what re-planning needs: the full
+    // block table on the host and the device's cooperative-launch capacity.
+    oc_launch_config cfg{};
+    std::vector<BlockInfo> h_blocks;
+    int sm_count = 0;
+    bool coop = false;
+    int persist_per_sm = 0;
     // Grid cloths' stencil data on the host, to refit the parameter slots when
     // oc_set_spring_params changes Ks or Kd, and each cloth's grid shape as detected
     // ({0, 0}: not a grid).
@@ -165,6 +182,18 @@ oc_status check_device_error(oc_solver* s) {
     return OC_OK;
 }
 
+// Whether a grid cloth that may take the strip sweep should: its warps own 28 columns
+// each, so narrow cloths leave lanes idle.  With cfg.strip = 0 every grid cloth stays on
+// k_assemble_grid (both give the same bits).
+bool strip_wanted(const oc_launch_config& cfg, const InstParams& ip) {
+    if (!cfg.strip || !ip.strip_ok || ip.grid_cols <= 0 || ip.coupled) return false;
+    const int32_t cols = ip.grid_cols;
+    const int32_t strips = (cols + kStripOwned - 1) / kStripOwned;
+    return cols >= 20 && 2 * cols >= 32 * strips;  // at least half the lanes own a vertex
+}
+
+int strip_blocks(int32_t n_work) { return (n_work + kStripThreads / 32 - 1) / (kStripThreads / 32); }
+
 template <class T>
 cudaError_t dalloc(oc_solver* s, T** p, size_t count) {
     void* q = nullptr;
@@ -179,6 +208,26 @@ cudaError_t upload(oc_solver* s, T** p, const std::vector<T>& v) {
     cudaError_t e = dalloc(s, p, v.size());
     if (e != cudaSuccess || v.empty()) return e;
     return cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+// Frees a table of the handle (re-planning replaces its tables).
+template <class T>
+void dfree(oc_solver* s, T** p) {
+    if (*p) {
+        auto it = std::find(s->allocs.begin(), s->allocs.end(), (void*)*p);
+        if (it != s->allocs.end()) {
+            cudaFree((void*)*p);
+            s->allocs.erase(it);
+        }
+        *p = nullptr;
+    }
+}
+
+// upload() into a pointer that may hold an earlier table of the handle, which is freed.
+template <class T>
+cudaError_t reupload(oc_solver* s, T** p, const std::vector<T>& v) {
+    dfree(s, p);
+    return upload(s, p, v);
 }
 
 void release(oc_solver* s) {
@@ -220,7 +269,12 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
         const InstState& st = s->h_state[k];
         // Assembled by k_resident (fused) or by the COUPLED kernels: no assembly bytes here.
         const bool fused = (s->resident[k] && s->resident_fused) || s->inst_host[k].coupled;
-        if (!fused && s->inst_host[k].grid_cols > 0)  // no incidence records, no row pointer
+        if (!fused && s->inst_host[k].strip) {
+            // The strip sweep: k_assemble_grid's bytes plus the delta0 term written, rest
+            // lengths (when they vary) as six planes by anchor; k_assemble_reduce reads the terms.
+            t->bytes[K_ASSEMBLE_STRIP] += 120.0 * nv + (s->inst_host[k].st_rest ? 24.0 * nv : 0.0);
+            t->bytes[K_ASSEMBLE_REDUCE] += 4.0 * nv;
+        } else if (!fused && s->inst_host[k].grid_cols > 0)  // no incidence records, no row pointer
             t->bytes[K_ASSEMBLE_GRID] +=              // unless rest lengths are per incidence
                 116.0 * nv + (s->inst_host[k].st_rest ? 4.0 * nv + 8.0 * ns : 0.0);
         else if (!fused)
@@ -338,8 +392,21 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
             a.blk_base = s->inst_host[grp].blk0;
             const int nb = s->inst_host[grp].nblk;
             const bool cpl = s->inst_host[grp].coupled != 0;
-            const KernelKind ka = cpl ? K_CPL_ASSEMBLE : (s->inst_host[grp].grid_cols > 0 ? K_ASSEMBLE_GRID : K_ASSEMBLE);
-            if ((st = launch_timed(s, ka, a, nb, t)) != OC_OK) return st;
+            if (s->inst_host[grp].strip && !cpl) {
+                StepArgs w = a;
+                w.strip_work = s->args.strip_work + s->strip_range[(size_t)grp].first;
+                w.n_strip_work = s->strip_range[(size_t)grp].second;
+                if ((st = launch_timed(s, K_ASSEMBLE_STRIP, w, strip_blocks(w.n_strip_work), t)) != OC_OK) return st;
+                if ((st = launch_timed(s, K_ASSEMBLE_REDUCE, a, nb, t)) != OC_OK) return st;
+                StepArgs fa = a;
+                fa.strip_ids = s->args.strip_ids + s->strip_pos[(size_t)grp];
+                if ((st = launch_timed(s, K_ASSEMBLE_FINISH, fa, 1, t)) != OC_OK) return st;
+                s->host_launches += 2;
+            } else {
+                const KernelKind ka =
+                    cpl ? K_CPL_ASSEMBLE : (s->inst_host[grp].grid_cols > 0 ? K_ASSEMBLE_GRID : K_ASSEMBLE);
+                if ((st = launch_timed(s, ka, a, nb, t)) != OC_OK) return st;
+            }
             s->host_launches += s->any_provot ? 3 : 2;
             for (;;) {
                 OC_TRY(cudaMemcpyAsync(s->h_scalar, &s->args.state[grp].active, sizeof(int32_t),
@@ -368,6 +435,14 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
         if (s->n_grid_blocks > 0) {
             if ((st = launch_timed(s, K_ASSEMBLE_GRID, ga, s->n_grid_blocks, t)) != OC_OK) return st;
             s->host_launches += 1;
+        }
+        if (s->args.n_strip_work > 0) {
+            StepArgs ra = a;
+            ra.blocks = s->d_sred_blocks;
+            if ((st = launch_timed(s, K_ASSEMBLE_STRIP, a, strip_blocks(a.n_strip_work), t)) != OC_OK) return st;
+            if ((st = launch_timed(s, K_ASSEMBLE_REDUCE, ra, s->n_sred_blocks, t)) != OC_OK) return st;
+            if ((st = launch_timed(s, K_ASSEMBLE_FINISH, a, a.n_strip_ids, t)) != OC_OK) return st;
+            s->host_launches += 3;
         }
         if (s->n_cpl_blocks > 0) {
             if ((st = launch_timed(s, K_CPL_ASSEMBLE, ca, s->n_cpl_blocks, t)) != OC_OK) return st;
@@ -446,9 +521,10 @@ oc_status build_graph(oc_solver* s, float dt) {
     a.blk_base = 0;
     a.use_cond = loop ? 1 : 0;
     a.cond = (unsigned long long)handle;
-    StepArgs aa = a, ga = a, sa = a, ca = a, ua = a;
+    StepArgs aa = a, ga = a, sa = a, ca = a, ua = a, ra = a;
     aa.blocks = s->d_asm_blocks;       // REFERENCE cloths: k_assemble
     ga.blocks = s->d_grid_blocks;      // REFERENCE grid cloths: k_assemble_grid
+    ra.blocks = s->d_sred_blocks;      // grid cloths on the strip sweep: k_assemble_reduce
     sa.blocks = s->d_streamed_blocks;  // streamed REFERENCE cloths: CG loop
     ca.blocks = s->d_cpl_blocks;       // COUPLED cloths
     ua.blocks = s->d_upd_blocks;       // k_integrate
@@ -458,16 +534,18 @@ oc_status build_graph(oc_solver* s, float dt) {
     void* params_str[] = {&sa};
     void* params_cpl[] = {&ca};
     void* params_upd[] = {&ua};
-    enum Table { T_ALL, T_ASM, T_STR, T_CPL, T_UPD, T_GRID };
+    void* params_sred[] = {&ra};
+    enum Table { T_ALL, T_ASM, T_STR, T_CPL, T_UPD, T_GRID, T_STRIP, T_SRED, T_SFIN };
     auto kparams = [&](KernelKind k, Table tab) {
         cudaKernelNodeParams kp{};
-        kp.func = const_cast<void*>(kernel_fn(k));
+        kp.func = const_cast<void*>(kernel_fn(k, a));
         const int n[] = {s->n_blocks, s->n_asm_blocks, s->n_streamed_blocks, s->n_cpl_blocks, s->n_upd_blocks,
-                         s->n_grid_blocks};
-        void** pp[] = {params_all, params_asm, params_str, params_cpl, params_upd, params_grid};
+                         s->n_grid_blocks, strip_blocks(s->args.n_strip_work), s->n_sred_blocks, s->args.n_strip_ids};
+        void** pp[] = {params_all, params_asm, params_str, params_cpl, params_upd, params_grid, params_all, params_sred,
+                       params_all};
         kp.gridDim = dim3((unsigned)n[tab]);
         kp.blockDim = dim3((unsigned)kernel_block_threads());
-        kp.sharedMemBytes = (unsigned)kernel_smem_bytes(k);
+        kp.sharedMemBytes = (unsigned)kernel_smem_bytes(k, a);
         kp.kernelParams = pp[tab];
         kp.extra = nullptr;
         return kp;
@@ -491,6 +569,17 @@ oc_status build_graph(oc_solver* s, float dt) {
     if (s->n_grid_blocks > 0) {  // serialised after k_assemble: both end in the same counters
         cudaGraphNode_t prev = n_asm;
         kp = kparams(K_ASSEMBLE_GRID, T_GRID);
+        OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &prev, 1, &kp));
+    }
+    if (s->args.n_strip_work > 0) {  // the strip sweep, then its delta0 partials and totals
+        cudaGraphNode_t prev = n_asm;
+        kp = kparams(K_ASSEMBLE_STRIP, T_STRIP);
+        OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &prev, 1, &kp));
+        prev = n_asm;
+        kp = kparams(K_ASSEMBLE_REDUCE, T_SRED);
+        OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &prev, 1, &kp));
+        prev = n_asm;
+        kp = kparams(K_ASSEMBLE_FINISH, T_SFIN);
         OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &prev, 1, &kp));
     }
     cudaGraphNode_t n_last = n_asm;  // the loop waits for every assembly
@@ -598,19 +687,10 @@ oc_status build_graph(oc_solver* s, float dt) {
 // to max_vertices and kResidentMaxCluster CTAs.
 constexpr int kResidentDefaultVcta = 1024;
 
-// The per-CTA vertex capacity and thread count are tuning knobs: OC_RESIDENT_SHAPE =
-// "vcta:threads" overrides the default 1024:256.
-bool resident_shape(int nv, int max_vertices, int* threads, int* cluster, int* vcta) {
+// The per-CTA vertex capacity and thread count come from the launch configuration
+// (resident_vcta, resident_threads).
+bool resident_shape(int nv, int max_vertices, int base, int thr, int* threads, int* cluster, int* vcta) {
     if (nv < 1 || nv > max_vertices) return false;
-    int base = kResidentDefaultVcta, thr = 256;
-    if (const char* e = std::getenv("OC_RESIDENT_SHAPE")) {
-        int v = 0, t = 0;
-        if (std::sscanf(e, "%d:%d", &v, &t) == 2 && v >= 128 && v <= kResidentMaxVcta && v <= kResidentVpt * t &&
-            (t == 128 || t == 256 || t == 512)) {
-            base = v;
-            thr = t;
-        }
-    }
     if (nv <= base) {
         int v = 128;
         while (v < nv) v <<= 1;
@@ -707,35 +787,209 @@ oc_status build_adjoint_graph(oc_solver* s, float dt) {
     cp.conditional.size = 1;
     OC_TRY(cudaGraphAddNode(&n_loop, g, &n_seed, nullptr, 1, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    kp.func = const_cast<void*>(kernel_fn(K_CG_DIR));
+    kp.func = const_cast<void*>(kernel_fn(K_CG_DIR, s->args));
     kp.gridDim = dim3((unsigned)s->n_blocks);
     kp.blockDim = dim3((unsigned)kernel_block_threads());
     kp.kernelParams = params_cg;
     OC_TRY(cudaGraphAddKernelNode(&n_dir, body, nullptr, 0, &kp));
-    kp.func = const_cast<void*>(kernel_fn(K_CG_UPDATE));
+    kp.func = const_cast<void*>(kernel_fn(K_CG_UPDATE, s->args));
     OC_TRY(cudaGraphAddKernelNode(&n_upd, body, &n_dir, 1, &kp));
     OC_TRY(cudaGraphInstantiate(&T.exec, g, 0));
     T.graph_dt = dt;
     return OC_OK;
 }
 
-// The CSR and stencil assembly tables from the full block table, after a cloth moved
-// between the two gathers: REFERENCE cloths that the step assembles (not a resident cloth
-// that the fused resident kernel assembles), by their current grid_cols.
-oc_status rebuild_assembly_tables(oc_solver* s) {
-    std::vector<BlockInfo> all((size_t)s->n_blocks), asm_ref, grid;
-    OC_TRY(cudaMemcpy(all.data(), s->args.blocks, sizeof(BlockInfo) * all.size(), cudaMemcpyDeviceToHost));
-    for (const BlockInfo& b : all) {
-        const InstParams& ip = s->inst_host[(size_t)b.inst];
-        if (ip.coupled || (s->resident[(size_t)b.inst] && s->resident_fused)) continue;
-        (ip.grid_cols > 0 ? grid : asm_ref).push_back(b);
+// The strip sweep's work items: per cloth on the sweep, bands of rows times strips of 28
+// columns, one warp each, a band's strips adjacent so a CTA's warps share rows.  Each warp
+// walks its band row by row, so short bands give more warps to hide the memory latency of
+// each row, and long bands recompute fewer springs (a band recomputes the springs of the
+// two rows above it): R rows per band, R chosen for about four waves of 16 warps per SM,
+// between 4 and 16, unless the launch configuration sets it (strip_rows).
+oc_status build_strip_work(oc_solver* s) {
+    std::vector<StripWork> work;
+    s->strip_range.assign((size_t)s->n_inst, std::make_pair(0, 0));
+    const int64_t target = 64LL * std::max(1, s->sm_count);
+    int64_t area = 0;
+    for (int32_t k = 0; k < s->n_inst; ++k) {
+        const InstParams& ip = s->inst_host[(size_t)k];
+        if (ip.strip) area += (int64_t)((ip.grid_cols + kStripOwned - 1) / kStripOwned) * ip.grid_rows;
     }
-    s->n_asm_blocks = (int32_t)asm_ref.size();
-    OC_TRY(upload(s, &s->d_asm_blocks, asm_ref));
-    s->n_grid_blocks = (int32_t)grid.size();
-    OC_TRY(upload(s, &s->d_grid_blocks, grid));
+    int32_t R = (int32_t)std::min<int64_t>(16, std::max<int64_t>(4, area / target));
+    if (s->cfg.strip_rows > 0) R = s->cfg.strip_rows;
+    for (int32_t k = 0; k < s->n_inst; ++k) {
+        const InstParams& ip = s->inst_host[(size_t)k];
+        if (!ip.strip) continue;
+        const int32_t first = (int32_t)work.size();
+        const int32_t rows = ip.grid_rows, band = std::min(R, rows);
+        for (int32_t r0 = 0; r0 < rows; r0 += band)
+            for (int32_t c0 = 0; c0 < ip.grid_cols; c0 += kStripOwned)
+                work.push_back(StripWork{k, c0, r0, std::min(rows, r0 + band)});
+        s->strip_range[(size_t)k] = std::make_pair(first, (int32_t)work.size() - first);
+    }
+    StripWork* d = const_cast<StripWork*>(s->args.strip_work);
+    OC_TRY(reupload(s, &d, work));
+    s->args.strip_work = d;
+    s->args.n_strip_work = (int32_t)work.size();
+    std::vector<int32_t> ids;
+    s->strip_pos.assign((size_t)s->n_inst, -1);
+    for (int32_t k = 0; k < s->n_inst; ++k)
+        if (s->inst_host[(size_t)k].strip) {
+            s->strip_pos[(size_t)k] = (int32_t)ids.size();
+            ids.push_back(k);
+        }
+    int32_t* di = const_cast<int32_t*>(s->args.strip_ids);
+    OC_TRY(reupload(s, &di, ids));
+    s->args.strip_ids = di;
+    s->args.n_strip_ids = (int32_t)ids.size();
     return OC_OK;
 }
+
+bool launch_config_valid(const oc_launch_config& c) {
+    const int v = c.resident_vcta, t = c.resident_threads;
+    const bool pow2 = v == 256 || v == 512 || v == 1024 || v == 2048;
+    return c.resident_max_vertices >= 0 && pow2 && v <= kResidentMaxVcta && (t == 128 || t == 256 || t == 512) &&
+           v <= kResidentVpt * t && (c.resident_fused == 0 || c.resident_fused == 1) &&
+           (c.persist == 0 || c.persist == 1) && c.gather_variant >= 0 && c.gather_variant <= 6 &&
+           (c.strip == 0 || c.strip == 1) && c.strip_rows >= 0 && c.strip_rows <= 64 &&
+           (c.strip_variant == 2 || c.strip_variant == 3);
+}
+
+void drop_graphs(oc_solver* s) {
+    if (s->exec) {
+        cudaGraphExecDestroy(s->exec);
+        s->exec = nullptr;
+    }
+    if (s->graph) {
+        cudaGraphDestroy(s->graph);
+        s->graph = nullptr;
+    }
+}
+
+// The launch plan from the handle's cloths and its launch configuration: which cloths run
+// resident (one cluster per cloth, the whole step on chip) and which streamed, resident
+// cloths grouped by launch shape into buckets, the assembly tables (record gather,
+// stencil, strip sweep), the update table, and the persistent CG of the streamed cloths.
+// Run at create and again by oc_set_launch_config (an earlier plan's tables are freed).
+oc_status plan_execution(oc_solver* s) {
+    const oc_launch_config& cfg = s->cfg;
+    StepArgs& a = s->args;
+    a.gather_variant = cfg.gather_variant;
+    a.strip_variant = cfg.strip_variant;
+    s->resident_fused = cfg.resident_fused != 0;
+    const int max_res = cfg.resident_max_vertices;
+    s->resident.assign((size_t)s->n_inst, 0);
+    for (oc_solver::Bucket& b : s->buckets) dfree(s, &b.d_ids);
+    s->buckets.clear();
+    std::vector<BlockInfo> streamed, asm_ref, cpl, upd, grid, sred;
+    std::map<std::tuple<int, int, int>, std::vector<int32_t>> groups;
+    for (int32_t k = 0; k < s->n_inst; ++k) {
+        InstParams& ip = s->inst_host[(size_t)k];
+        const bool cpl_k = ip.coupled != 0;
+        if (s->executor == OC_EXEC_RESIDENT && cpl_k)
+            return fail(s, OC_ERR_UNSUPPORTED,
+                        "instance " + std::to_string(k) + " is COUPLED: the resident executor runs REFERENCE cloths");
+        int threads = 0, cluster = 0, vcta = 0;
+        const bool want = !cpl_k && (s->executor == OC_EXEC_RESIDENT || s->executor == OC_EXEC_AUTO) &&
+                          resident_shape(ip.nv, max_res, cfg.resident_vcta, cfg.resident_threads, &threads, &cluster,
+                                         &vcta);
+        if (s->executor == OC_EXEC_RESIDENT && !want)
+            return fail(s, OC_ERR_UNSUPPORTED, "instance " + std::to_string(k) + " (" + std::to_string(ip.nv) +
+                                                   " vertices) is too large for the resident executor");
+        const BlockInfo* kb = s->h_blocks.data() + ip.blk0;
+        ip.strip = 0;
+        ip.resident = want ? 1 : 0;
+        if (cpl_k) {
+            cpl.insert(cpl.end(), kb, kb + ip.nblk);
+            upd.insert(upd.end(), kb, kb + ip.nblk);
+            continue;
+        }
+        if (!(want && s->resident_fused)) {
+            ip.strip = strip_wanted(cfg, ip) ? 1 : 0;
+            auto& tab = ip.grid_cols > 0 ? (ip.strip ? sred : grid) : asm_ref;
+            tab.insert(tab.end(), kb, kb + ip.nblk);
+        }
+        if (want) {
+            s->resident[(size_t)k] = 1;
+            groups[std::make_tuple(threads, cluster, vcta)].push_back(k);
+        } else {
+            streamed.insert(streamed.end(), kb, kb + ip.nblk);
+            upd.insert(upd.end(), kb, kb + ip.nblk);
+        }
+    }
+    s->n_asm_blocks = (int32_t)asm_ref.size();
+    OC_TRY(reupload(s, &s->d_asm_blocks, asm_ref));
+    s->n_grid_blocks = (int32_t)grid.size();
+    OC_TRY(reupload(s, &s->d_grid_blocks, grid));
+    s->n_sred_blocks = (int32_t)sred.size();
+    OC_TRY(reupload(s, &s->d_sred_blocks, sred));
+    s->n_cpl_blocks = (int32_t)cpl.size();
+    OC_TRY(reupload(s, &s->d_cpl_blocks, cpl));
+    s->n_upd_blocks = (int32_t)upd.size();
+    OC_TRY(reupload(s, &s->d_upd_blocks, upd));
+    s->n_streamed_blocks = (int32_t)streamed.size();
+    OC_TRY(reupload(s, &s->d_streamed_blocks, streamed));
+    if (oc_status r = build_strip_work(s)) return r;
+    std::vector<std::pair<std::tuple<int, int, int>, std::vector<int32_t>>> ordered(groups.begin(), groups.end());
+    // Largest buckets first, so their clusters start before the small ones fill in.
+    std::stable_sort(ordered.begin(), ordered.end(), [](const auto& x, const auto& y) {
+        const double wx = (double)x.second.size() * std::get<1>(x.first) * std::get<2>(x.first);
+        const double wy = (double)y.second.size() * std::get<1>(y.first) * std::get<2>(y.first);
+        return wx > wy;
+    });
+    for (auto& kv : ordered) {
+        oc_solver::Bucket b{};
+        b.threads = std::get<0>(kv.first);
+        b.cluster = std::get<1>(kv.first);
+        b.vcta = std::get<2>(kv.first);
+        b.n = (int)kv.second.size();
+        OC_TRY(upload(s, &b.d_ids, kv.second));
+        s->buckets.push_back(b);
+    }
+    OC_TRY(cudaMemcpy(const_cast<InstParams*>(a.inst), s->inst_host.data(), sizeof(InstParams) * s->inst_host.size(),
+                      cudaMemcpyHostToDevice));
+    if (!s->buckets.empty()) {
+        OC_TRY(prepare_resident());
+        const size_t naux = std::min<size_t>(s->buckets.size(), 8);
+        if (!s->fork_ev) OC_TRY(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming));
+        while (s->aux.size() < naux) {
+            cudaStream_t x = nullptr;
+            cudaEvent_t e = nullptr;
+            OC_TRY(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+            s->aux.push_back(x);
+            OC_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            s->aux_done.push_back(e);
+        }
+    }
+    // Persistent CG for the streamed REFERENCE cloths: few of them, no COUPLED cloth, a
+    // cooperative launch fits, and the configuration allows it.
+    std::vector<int32_t> ids;
+    bool any_coupled = false;
+    for (int32_t k = 0; k < s->n_inst; ++k) {
+        any_coupled |= s->inst_host[(size_t)k].coupled != 0;
+        if (!s->resident[(size_t)k] && !s->inst_host[(size_t)k].coupled) ids.push_back(k);
+    }
+    s->persist = false;
+    if (cfg.persist && s->coop && s->persist_per_sm > 0 && !ids.empty() &&
+        (int)ids.size() <= persist_max_instances() && !any_coupled) {
+        s->persist = true;
+        s->n_persist = (int32_t)ids.size();
+        s->persist_grid = std::min(s->persist_per_sm * s->sm_count, std::max(1, s->n_streamed_blocks));
+        OC_TRY(reupload(s, &s->d_persist_ids, ids));
+        if (!s->d_bar) {
+            // arrival word at [0], generation at [32], the cloths' totals (16 doubles) at [64]
+            OC_TRY(dalloc(s, &s->d_bar, 128));
+            OC_TRY(cudaMemset(s->d_bar, 0, 128 * sizeof(unsigned)));
+            OC_TRY(dalloc(s, &s->d_perr, 1));
+            OC_TRY(cudaMemset(s->d_perr, 0, sizeof(int)));
+        }
+    }
+    drop_graphs(s);
+    return OC_OK;
+}
+
+// After a cloth moved between the gathers (its grid_cols changed): the plan again, which
+// rebuilds the assembly tables and the strip work from the current grid_cols.
+oc_status rebuild_assembly_tables(oc_solver* s) { return plan_execution(s); }
 
 // After new per-spring Ks / Kd: a grid cloth reads them from its stencil's parameter
 // slots, so either every spring of each slot still shares one (Ks, Kd) and the slots take
@@ -894,6 +1148,7 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     if (const char* e = std::getenv("OC_STENCIL"))
         if (std::atoi(e) == 0)
             for (InstParams& ip : P.inst) ip.grid_cols = ip.grid_rows = 0;
+    build_strip_tables(&P);
     auto bail = [&](oc_status code) {
         std::fprintf(stderr, "oc_create: %s\n", s->err.c_str());
         release(s);
@@ -921,11 +1176,7 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     s->n_blocks = (int32_t)P.blocks.size();
     s->vertices_per_block = P.vertices_per_block;
     OC_CREATE_TRY(cudaSetDevice(o.device));
-    {
-        // Force-gather variant (a tuning knob; OC_GATHER_VARIANT overrides the default).
-        const char* gv = std::getenv("OC_GATHER_VARIANT");
-        OC_CREATE_TRY(prepare_kernels(gv ? std::atoi(gv) : 6));
-    }
+    OC_CREATE_TRY(prepare_kernels());
     if (o.stream) {
         s->stream = static_cast<cudaStream_t>(o.stream);
     } else {
@@ -966,6 +1217,19 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
             float* d_rest = nullptr;
             OC_CREATE_TRY(upload(s, &d_rest, rest));
             a.rest_inc = d_rest;
+        }
+        if (!P.strip_slot.empty()) {
+            uint32_t* d_ss = nullptr;
+            OC_CREATE_TRY(upload(s, &d_ss, P.strip_slot));
+            a.strip_slot = d_ss;
+            if (!P.strip_rest.empty()) {
+                float* d_sr = nullptr;
+                OC_CREATE_TRY(upload(s, &d_sr, P.strip_rest));
+                a.strip_rest = d_sr;
+            }
+            float* term = nullptr;  // delta0 terms of the swept vertices
+            OC_CREATE_TRY(dalloc(s, &term, (size_t)P.nv));
+            a.term = term;
         }
     }
     a.own_ends = own_ends;
@@ -1049,116 +1313,54 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
         a.pinflag = d_pins;
     }
 
-    // Which cloths run resident (one cluster per cloth, the whole step on chip) and
-    // which run streamed; resident cloths are grouped by launch shape.
+    // The launch configuration: the options and the environment's diagnostic switches
+    // over the measured defaults, then the plan (resident buckets, block tables, strip
+    // work, persistent CG).
     {
-        const int max_res = o.resident_max_vertices > 0 ? o.resident_max_vertices
-                                                        : kResidentMaxCluster * kResidentDefaultVcta;
-        s->resident.assign(P.n_inst, 0);
-        std::vector<BlockInfo> streamed, asm_ref, cpl, upd, grid;
-        std::map<std::tuple<int, int, int>, std::vector<int32_t>> groups;
-        for (int32_t k = 0; k < P.n_inst; ++k) {
-            const bool cpl_k = P.inst[k].coupled != 0;
-            if (s->executor == OC_EXEC_RESIDENT && cpl_k) {
-                s->err = "instance " + std::to_string(k) + " is COUPLED: the resident executor runs REFERENCE cloths";
-                return bail(OC_ERR_UNSUPPORTED);
-            }
-            int threads = 0, cluster = 0, vcta = 0;
-            const bool want = !cpl_k && (s->executor == OC_EXEC_RESIDENT || s->executor == OC_EXEC_AUTO) &&
-                              resident_shape(P.inst[k].nv, max_res, &threads, &cluster, &vcta);
-            if (s->executor == OC_EXEC_RESIDENT && !want) {
-                s->err = "instance " + std::to_string(k) + " (" + std::to_string(P.inst[k].nv) +
-                         " vertices) is too large for the resident executor";
-                return bail(OC_ERR_UNSUPPORTED);
-            }
-            const BlockInfo* kb = P.blocks.data() + P.inst[k].blk0;
-            if (cpl_k) {
-                cpl.insert(cpl.end(), kb, kb + P.inst[k].nblk);
-                upd.insert(upd.end(), kb, kb + P.inst[k].nblk);
-                continue;
-            }
-            if (!(want && s->resident_fused)) {
-                if (P.inst[k].grid_cols > 0)
-                    grid.insert(grid.end(), kb, kb + P.inst[k].nblk);
-                else
-                    asm_ref.insert(asm_ref.end(), kb, kb + P.inst[k].nblk);
-            }
-            if (want) {
-                s->resident[k] = 1;
-                groups[std::make_tuple(threads, cluster, vcta)].push_back(k);
-            } else {
-                streamed.insert(streamed.end(), kb, kb + P.inst[k].nblk);
-                upd.insert(upd.end(), kb, kb + P.inst[k].nblk);
+        oc_launch_config& c = s->cfg;
+        c.resident_max_vertices = o.resident_max_vertices > 0 ? o.resident_max_vertices
+                                                              : kResidentMaxCluster * kResidentDefaultVcta;
+        c.resident_vcta = kResidentDefaultVcta;
+        c.resident_threads = 256;
+        if (const char* e = std::getenv("OC_RESIDENT_SHAPE")) {
+            int v = 0, t = 0;
+            if (std::sscanf(e, "%d:%d", &v, &t) == 2) {
+                c.resident_vcta = v;
+                c.resident_threads = t;
             }
         }
-        s->n_asm_blocks = (int32_t)asm_ref.size();
-        OC_CREATE_TRY(upload(s, &s->d_asm_blocks, asm_ref));
-        s->n_grid_blocks = (int32_t)grid.size();
-        OC_CREATE_TRY(upload(s, &s->d_grid_blocks, grid));
-        s->n_cpl_blocks = (int32_t)cpl.size();
-        OC_CREATE_TRY(upload(s, &s->d_cpl_blocks, cpl));
-        s->n_upd_blocks = (int32_t)upd.size();
-        OC_CREATE_TRY(upload(s, &s->d_upd_blocks, upd));
-        std::vector<std::pair<std::tuple<int, int, int>, std::vector<int32_t>>> ordered(groups.begin(), groups.end());
-        // Largest buckets first, so their clusters start before the small ones fill in.
-        std::stable_sort(ordered.begin(), ordered.end(), [](const auto& x, const auto& y) {
-            const double wx = (double)x.second.size() * std::get<1>(x.first) * std::get<2>(x.first);
-            const double wy = (double)y.second.size() * std::get<1>(y.first) * std::get<2>(y.first);
-            return wx > wy;
-        });
-        for (auto& kv : ordered) {
-            oc_solver::Bucket b;
-            b.threads = std::get<0>(kv.first);
-            b.cluster = std::get<1>(kv.first);
-            b.vcta = std::get<2>(kv.first);
-            b.n = (int)kv.second.size();
-            OC_CREATE_TRY(upload(s, &b.d_ids, kv.second));
-            s->buckets.push_back(b);
-        }
-        for (int32_t k = 0; k < P.n_inst; ++k) P.inst[k].resident = s->resident[k];
-        s->inst_host = P.inst;
-        OC_CREATE_TRY(cudaMemcpy(inst, P.inst.data(), sizeof(InstParams) * P.n_inst, cudaMemcpyHostToDevice));
-        s->n_streamed_blocks = (int32_t)streamed.size();
-        OC_CREATE_TRY(upload(s, &s->d_streamed_blocks, streamed));
-        if (!s->buckets.empty()) {
-            OC_CREATE_TRY(prepare_resident());
-            const size_t naux = std::min<size_t>(s->buckets.size(), 8);
-            OC_CREATE_TRY(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming));
-            for (size_t i = 0; i < naux; ++i) {
-                cudaStream_t x = nullptr;
-                cudaEvent_t e = nullptr;
-                OC_CREATE_TRY(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
-                s->aux.push_back(x);
-                OC_CREATE_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-                s->aux_done.push_back(e);
-            }
-        }
-    }
-    {
-        // Persistent CG for the streamed REFERENCE cloths: few of them, no COUPLED cloth,
-        // a cooperative launch fits, and OC_PERSIST is not 0.
-        std::vector<int32_t> ids;
-        for (int32_t k = 0; k < P.n_inst; ++k)
-            if (!s->resident[k] && !P.inst[k].coupled) ids.push_back(k);
+        c.resident_fused = s->resident_fused ? 1 : 0;
         const char* pe = std::getenv("OC_PERSIST");
-        const bool allowed = !(pe && std::atoi(pe) == 0) && s->executor != OC_EXEC_PLAIN;
-        const int per_sm = allowed ? persist_blocks_per_sm() : 0;
-        int n_sm = 0;
-        OC_CREATE_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, s->device));
+        c.persist = (pe && std::atoi(pe) == 0) ? 0 : 1;
+        const char* gv = std::getenv("OC_GATHER_VARIANT");
+        c.gather_variant = gv ? std::atoi(gv) : 6;
+        // The strip sweep is off by default: on GB300 it measured level with the stencil
+        // gather on the 1M-vertex cloth (its delta0 reduction costs what its single spring
+        // evaluations save) and slower on the 4096-cloth batch; the autotuner tries it.
+        const char* se = std::getenv("OC_STRIP");
+        c.strip = (se && std::atoi(se) != 0) ? 1 : 0;
+        const char* sr = std::getenv("OC_STRIP_ROWS");
+        c.strip_rows = sr ? std::max(0, std::atoi(sr)) : 0;
+        const char* sv = std::getenv("OC_STRIP_VARIANT");
+        c.strip_variant = (sv && std::atoi(sv) == 3) ? 3 : 2;
+        if (!launch_config_valid(c)) {
+            s->err = "oc_create: invalid launch configuration from the environment";
+            return bail(OC_ERR_INVALID_ARGUMENT);
+        }
+        OC_CREATE_TRY(cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device));
         int coop = 0;
         OC_CREATE_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->device));
-        if (allowed && coop && per_sm > 0 && !ids.empty() && (int)ids.size() <= persist_max_instances() &&
-            !P.any_coupled) {
-            s->persist = true;
-            s->n_persist = (int32_t)ids.size();
-            s->persist_grid = std::min(per_sm * n_sm, std::max(1, s->n_streamed_blocks));
-            OC_CREATE_TRY(upload(s, &s->d_persist_ids, ids));
-            // arrival word at [0], generation at [32], the cloths' totals (16 doubles) at [64]
-            OC_CREATE_TRY(dalloc(s, &s->d_bar, 128));
-            OC_CREATE_TRY(cudaMemset(s->d_bar, 0, 128 * sizeof(unsigned)));
-            OC_CREATE_TRY(dalloc(s, &s->d_perr, 1));
-            OC_CREATE_TRY(cudaMemset(s->d_perr, 0, sizeof(int)));
-        }
+        s->coop = coop != 0;
+        s->persist_per_sm = s->executor != OC_EXEC_PLAIN ? persist_blocks_per_sm() : 0;
+        s->h_blocks = P.blocks;
+        if (oc_status r = plan_execution(s)) return bail(r);
+    }
+    {
+        const char* pe = std::getenv("OC_PERSIST");
+        const bool allowed = !(pe && std::atoi(pe) == 0) && s->executor != OC_EXEC_PLAIN;
+        const int per_sm = allowed ? s->persist_per_sm : 0;
+        const int n_sm = s->sm_count;
+        const int coop = s->coop ? 1 : 0;
         // The adjoint solve runs every cloth's CG: one cooperative launch without the
         // update when the handle holds at most persist_max_instances() cloths.
         if (allowed && coop && per_sm > 0 && P.n_inst <= persist_max_instances() && !P.any_coupled) {
@@ -1324,7 +1526,8 @@ oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
     // assemblies, the persistent CG (which includes the update) or the update kernel,
     // the resident launches and the Provot pass; the WHILE loop's launches are counted on
     // the device (loop_count).
-    const int64_t per_step = (s->n_asm_blocks > 0 ? 1 : 0) + (s->n_grid_blocks > 0 ? 1 : 0) + (s->n_cpl_blocks > 0 ? 1 : 0) +
+    const int64_t per_step = (s->n_asm_blocks > 0 ? 1 : 0) + (s->n_grid_blocks > 0 ? 1 : 0) +
+                             (s->args.n_strip_work > 0 ? 3 : 0) + (s->n_cpl_blocks > 0 ? 1 : 0) +
                              (s->persist ? 1 : (s->n_upd_blocks > 0 ? 1 : 0)) + (int64_t)s->buckets.size() +
                              (s->any_provot ? 1 : 0);
     s->host_launches += per_step * (int64_t)n_steps;
@@ -1532,8 +1735,9 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
     cudaEventDestroy(t.ev[0]);
     cudaEventDestroy(t.ev[1]);
     if (st != OC_OK) return st;
-    const KernelKind kinds[] = {K_ASSEMBLE, K_ASSEMBLE_GRID, K_CG_DIR,  K_CG_UPDATE, K_INTEGRATE,  K_CG_PERSIST,
-                                K_RESIDENT, K_PROVOT,        K_CPL_ASSEMBLE, K_CPL_DIR, K_CPL_UPDATE};
+    const KernelKind kinds[] = {K_ASSEMBLE, K_ASSEMBLE_GRID, K_ASSEMBLE_STRIP, K_ASSEMBLE_REDUCE, K_ASSEMBLE_FINISH,
+                                K_CG_DIR, K_CG_UPDATE, K_INTEGRATE, K_CG_PERSIST, K_RESIDENT, K_PROVOT,
+                                K_CPL_ASSEMBLE, K_CPL_DIR, K_CPL_UPDATE};
     int32_t n = 0;
     for (KernelKind k : kinds) {
         if (n >= max_kernels) break;
@@ -1542,7 +1746,9 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
         if (k == K_ASSEMBLE_GRID && s->n_grid_blocks == 0) continue;
         if (k == K_CG_PERSIST && !s->persist) continue;
         if ((k == K_CG_DIR || k == K_CG_UPDATE || k == K_INTEGRATE) && s->persist) continue;
-        if (k == K_ASSEMBLE && s->n_grid_blocks > 0 && s->n_asm_blocks == 0) continue;
+        if ((k == K_ASSEMBLE_STRIP || k == K_ASSEMBLE_REDUCE || k == K_ASSEMBLE_FINISH) && s->args.n_strip_work == 0)
+            continue;
+        if (k == K_ASSEMBLE && s->n_asm_blocks == 0 && (s->n_grid_blocks > 0 || s->args.n_strip_work > 0)) continue;
         if (names) {
             std::memset(names + 32 * n, 0, 32);
             std::strncpy(names + 32 * n, kernel_name(k), 31);
@@ -1755,6 +1961,13 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
         bg.blocks = s->d_grid_blocks;
         if (s->n_asm_blocks > 0) e = launch_kernel(K_ASSEMBLE, ba, s->n_asm_blocks, s->stream);
         if (e == cudaSuccess && s->n_grid_blocks > 0) e = launch_kernel(K_ASSEMBLE_GRID, bg, s->n_grid_blocks, s->stream);
+        if (e == cudaSuccess && b.n_strip_work > 0) {
+            StepArgs br = b;
+            br.blocks = s->d_sred_blocks;
+            e = launch_kernel(K_ASSEMBLE_STRIP, b, strip_blocks(b.n_strip_work), s->stream);
+            if (e == cudaSuccess) e = launch_kernel(K_ASSEMBLE_REDUCE, br, s->n_sred_blocks, s->stream);
+            if (e == cudaSuccess) e = launch_kernel(K_ASSEMBLE_FINISH, b, b.n_strip_ids, s->stream);
+        }
         return e;
     };
     const size_t nAx = 9 * st;
@@ -1840,6 +2053,277 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
     if (dL_dKd) OC_TRY(cudaMemcpyAsync(dL_dKd, j.gKd, sizeof(float) * s->ns, cudaMemcpyDeviceToHost, s->stream));
     OC_TRY(cudaStreamSynchronize(s->stream));
     return OC_OK;
+}
+
+oc_status oc_get_launch_config(const oc_solver* s, oc_launch_config* cfg) {
+    if (!valid_solver(s) || !cfg) return OC_ERR_INVALID_ARGUMENT;
+    *cfg = s->cfg;
+    return OC_OK;
+}
+
+oc_status oc_set_launch_config(oc_solver* s, const oc_launch_config* cfg) {
+    if (!valid_solver(s) || !cfg || !launch_config_valid(*cfg)) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    const oc_launch_config old = s->cfg;
+    s->cfg = *cfg;
+    oc_status r = plan_execution(s);
+    if (r != OC_OK) {
+        const std::string why = s->err;
+        s->cfg = old;
+        if (plan_execution(s) != OC_OK) return r;
+        return fail(s, r, why);
+    }
+    s->tape.valid = false;
+    if (s->tape.exec) {
+        cudaGraphExecDestroy(s->tape.exec);
+        s->tape.exec = nullptr;
+    }
+    if (s->tape.graph) {
+        cudaGraphDestroy(s->tape.graph);
+        s->tape.graph = nullptr;
+    }
+    return OC_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// 64-bit FNV-1a.
+uint64_t fnv1a(const void* data, size_t n, uint64_t h = 0xcbf29ce484222325ull) {
+    const unsigned char* p = static_cast<const unsigned char*>(data);
+    for (size_t i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 0x100000001b3ull;
+    }
+    return h;
+}
+
+// The tuning key: GPU name (spaces as '_'), SM count and the hash of the sorted per-cloth
+// signatures (vertices, grid shape, Jacobian mode, passes, strip eligibility).
+oc_status make_tune_key(const std::vector<InstParams>& inst, const char* gpu_name, int32_t sm_count, char* key,
+                        int32_t key_size) {
+    if (!gpu_name || !key || key_size < 96 || sm_count < 0) return OC_ERR_INVALID_ARGUMENT;
+    std::vector<std::array<int32_t, 6>> sig;
+    sig.reserve(inst.size());
+    for (const InstParams& ip : inst)
+        sig.push_back({ip.nv, ip.grid_cols, ip.grid_rows, ip.coupled, ip.passes, ip.strip_ok});
+    std::sort(sig.begin(), sig.end());
+    const uint64_t h = fnv1a(sig.data(), sig.size() * sizeof(sig[0]));
+    std::string name(gpu_name);
+    for (char& ch : name)
+        if (ch == ' ' || ch == '\t' || ch == '\n') ch = '_';
+    char buf[64];
+    std::snprintf(buf, sizeof buf, ";sm=%d;n=%zu;h=%016llx", sm_count, inst.size(), (unsigned long long)h);
+    const std::string k = "gpu=" + name.substr(0, (size_t)std::max(0, key_size - 64)) + buf;
+    if ((int32_t)k.size() >= key_size) return OC_ERR_INVALID_ARGUMENT;
+    std::memcpy(key, k.c_str(), k.size() + 1);
+    return OC_OK;
+}
+
+// Device copies of a handle's state (X, V, the warm-start planes), to time candidates
+// without advancing the simulation.
+struct StateBackup {
+    float4* X = nullptr;
+    float4* V = nullptr;
+    float* x = nullptr;
+};
+
+}  // namespace
+
+extern "C" {
+
+oc_status oc_tune_key(const oc_cloth_desc* descs, int32_t n_instances, const char* gpu_name, int32_t sm_count,
+                      char* key, int32_t key_size) {
+    if (!descs || n_instances < 1) return OC_ERR_INVALID_ARGUMENT;
+    PackedHost P;
+    std::string err;
+    if (oc_status st = pack_instances(descs, n_instances, 2048, &P, &err)) return st;
+    build_strip_tables(&P);
+    return make_tune_key(P.inst, gpu_name, sm_count, key, key_size);
+}
+
+oc_status oc_tune_key_of(const oc_solver* s, char* key, int32_t key_size) {
+    if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, s->device) != cudaSuccess) return OC_ERR_CUDA;
+    return make_tune_key(s->inst_host, prop.name, prop.multiProcessorCount, key, key_size);
+}
+
+oc_status oc_tune_cache_lookup(const char* path, const char* key, oc_launch_config* cfg, int32_t* found) {
+    if (!path || !key || !cfg || !found) return OC_ERR_INVALID_ARGUMENT;
+    *found = 0;
+    std::ifstream in(path);
+    if (!in) return OC_OK;  // no cache yet
+    std::string line;
+    while (std::getline(in, line)) {
+        std::istringstream ls(line);
+        std::string k;
+        oc_launch_config c{};
+        double ms = 0.0;
+        if (!(ls >> k >> c.resident_max_vertices >> c.resident_vcta >> c.resident_threads >> c.resident_fused >>
+              c.persist >> c.gather_variant >> c.strip >> c.strip_rows >> c.strip_variant >> ms))
+            continue;  // not a cache line
+        if (k == key && launch_config_valid(c)) {
+            *cfg = c;
+            *found = 1;
+        }
+    }
+    return OC_OK;
+}
+
+oc_status oc_tune_cache_store(const char* path, const char* key, const oc_launch_config* cfg, double ms_per_step) {
+    if (!path || !key || !cfg || !launch_config_valid(*cfg) || std::strchr(key, ' ') || std::strchr(key, '\n'))
+        return OC_ERR_INVALID_ARGUMENT;
+    std::ofstream out(path, std::ios::app);
+    if (!out) return OC_ERR_INVALID_ARGUMENT;
+    const oc_launch_config& c = *cfg;
+    out << key << ' ' << c.resident_max_vertices << ' ' << c.resident_vcta << ' ' << c.resident_threads << ' '
+        << c.resident_fused << ' ' << c.persist << ' ' << c.gather_variant << ' ' << c.strip << ' ' << c.strip_rows
+        << ' ' << c.strip_variant << ' ' << ms_per_step << '\n';
+    return out ? OC_OK : OC_ERR_INVALID_ARGUMENT;
+}
+
+oc_status oc_autotune(oc_solver* s, float dt, const char* cache_path, int32_t flags, oc_launch_config* chosen,
+                      double* ms_per_step) {
+    if (!valid_solver(s) || !std::isfinite(dt) || dt <= 0.0f) return OC_ERR_INVALID_ARGUMENT;
+    OC_TRY(cudaSetDevice(s->device));
+    char key[256];
+    if (oc_status st = oc_tune_key_of(s, key, (int32_t)sizeof key)) return st;
+    if (cache_path && (flags & OC_TUNE_USE_CACHE)) {
+        oc_launch_config c{};
+        int32_t found = 0;
+        if (oc_status st = oc_tune_cache_lookup(cache_path, key, &c, &found)) return st;
+        if (found && oc_set_launch_config(s, &c) == OC_OK) {
+            if (chosen) *chosen = s->cfg;
+            if (ms_per_step) *ms_per_step = 0.0;
+            return OC_OK;
+        }
+    }
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    // Save the state; every candidate starts from it, and it is put back at the end.
+    StateBackup B;
+    const size_t n4 = sizeof(float4) * (size_t)s->nv, nx = 3 * s->stride * sizeof(float);
+    OC_TRY(cudaMalloc(&B.X, n4));
+    OC_TRY(cudaMalloc(&B.V, n4));
+    OC_TRY(cudaMalloc(&B.x, nx));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&](oc_status st) {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        cudaFree(B.X);
+        cudaFree(B.V);
+        cudaFree(B.x);
+        return st;
+    };
+    if (copy_state(s, B.X, B.V, B.x, s->args.X, s->args.V, xplanes(s)) != OC_OK ||
+        cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        return cleanup(fail(s, OC_ERR_CUDA, "oc_autotune: set-up failed"));
+    auto restore = [&]() { return copy_state(s, s->args.X, s->args.V, xplanes(s), B.X, B.V, B.x); };
+    int32_t timed_steps = 0;  // fixed after the first candidate (about 20 ms of steps)
+    // Time one configuration: re-plan, two warm-up steps from the saved state, then the
+    // timed steps from the saved state again.  A configuration the handle cannot run is
+    // skipped (returns a negative time).
+    auto measure = [&](const oc_launch_config& c) -> double {
+        if (oc_set_launch_config(s, &c) != OC_OK) return -1.0;
+        if (restore() != OC_OK || oc_step(s, dt, 2) != OC_OK) return -1.0;
+        if (cudaEventRecord(e0, s->stream) != cudaSuccess || oc_step(s, dt, 1) != OC_OK ||
+            cudaEventRecord(e1, s->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+            return -1.0;
+        float one = 0.0f;
+        cudaEventElapsedTime(&one, e0, e1);
+        if (timed_steps == 0) timed_steps = (int32_t)std::min(200.0, std::max(3.0, 20.0 / std::max(one, 1e-3f)));
+        if (restore() != OC_OK || cudaEventRecord(e0, s->stream) != cudaSuccess ||
+            oc_step(s, dt, timed_steps) != OC_OK || cudaEventRecord(e1, s->stream) != cudaSuccess ||
+            cudaEventSynchronize(e1) != cudaSuccess || check_device_error(s) != OC_OK)
+            return -1.0;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return (double)ms / timed_steps;
+    };
+    // Which knobs matter for these cloths.
+    bool any_strip = false, any_small = false, any_records = false;
+    for (int32_t k = 0; k < s->n_inst; ++k) {
+        const InstParams& ip = s->inst_host[(size_t)k];
+        if (ip.coupled) continue;
+        any_strip |= ip.strip_ok != 0 && ip.grid_cols > 0;
+        any_small |= ip.nv <= kResidentMaxCluster * kResidentDefaultVcta;
+        any_records |= ip.grid_cols <= 0;
+    }
+    oc_launch_config best = s->cfg;
+    double t_best = measure(best);
+    if (t_best < 0.0) {
+        oc_set_launch_config(s, &best);
+        restore();
+        return cleanup(fail(s, OC_ERR_CUDA, "oc_autotune: the current configuration failed to run"));
+    }
+    auto consider = [&](oc_launch_config c) {
+        if (std::memcmp(&c, &best, sizeof c) == 0 || !launch_config_valid(c)) return;
+        const double t = measure(c);
+        if (t > 0.0 && t < 0.99 * t_best) {
+            best = c;
+            t_best = t;
+        }
+    };
+    if (any_strip) {
+        for (int32_t v : {1, 0}) {
+            oc_launch_config c = best;
+            c.strip = v;
+            consider(c);
+        }
+        if (best.strip) {
+            for (int32_t rows : {0, 4, 8, 16, 32}) {
+                oc_launch_config c = best;
+                c.strip_rows = rows;
+                consider(c);
+            }
+            for (int32_t v : {2, 3}) {
+                oc_launch_config c = best;
+                c.strip_variant = v;
+                consider(c);
+            }
+        }
+    }
+    if (any_small && s->executor == OC_EXEC_AUTO) {
+        for (int32_t m : {kResidentMaxCluster * kResidentDefaultVcta, 4096, 1024, 0}) {
+            oc_launch_config c = best;
+            c.resident_max_vertices = m;
+            consider(c);
+        }
+    }
+    if (any_small && s->executor != OC_EXEC_STREAMED && s->executor != OC_EXEC_PLAIN && !s->buckets.empty()) {
+        const int32_t shapes[3][2] = {{1024, 256}, {512, 128}, {2048, 512}};
+        for (const auto& sh : shapes) {
+            oc_launch_config c = best;
+            c.resident_vcta = sh[0];
+            c.resident_threads = sh[1];
+            consider(c);
+        }
+        for (int32_t v : {0, 1}) {
+            oc_launch_config c = best;
+            c.resident_fused = v;
+            consider(c);
+        }
+    }
+    for (int32_t v : {1, 0}) {
+        oc_launch_config c = best;
+        c.persist = v;
+        consider(c);
+    }
+    if (any_records)
+        for (int32_t v : {6, 4, 1}) {
+            oc_launch_config c = best;
+            c.gather_variant = v;
+            consider(c);
+        }
+    oc_status st = oc_set_launch_config(s, &best);
+    if (st == OC_OK) st = restore();
+    if (st == OC_OK) st = cudaStreamSynchronize(s->stream) == cudaSuccess ? OC_OK : OC_ERR_CUDA;
+    if (st == OC_OK && cache_path && (flags & OC_TUNE_STORE)) st = oc_tune_cache_store(cache_path, key, &best, t_best);
+    if (chosen) *chosen = best;
+    if (ms_per_step) *ms_per_step = t_best;
+    return cleanup(st);
 }
 
 oc_status oc_test_barrier_timeout(oc_solver* s, int32_t withhold_block, uint32_t max_polls) {

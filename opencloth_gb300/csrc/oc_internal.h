@@ -30,6 +30,16 @@ struct InstParams {
     int32_t st_off;     // its class table and entries in StepArgs::st_data
     int32_t st_par;     // its first parameter slot in StepArgs::st_param
     int32_t st_rest;    // 1: rest lengths vary; read them per incidence from StepArgs::rest_inc
+    // The strip sweep (k_assemble_strip), for grid cloths whose incidences follow the
+    // reference's spring order: strip_slot is the cloth's first word in StepArgs::strip_slot
+    // (36 words, one per anchor position class, six 4-bit parameter slots each: H, bR, V,
+    // shA, shB, bC), strip_rest its first rest length in StepArgs::strip_rest (six planes of
+    // nv floats, by kind and anchor vertex) or -1 when the slots hold the rest lengths;
+    // strip_ok 1 when the cloth may take the sweep (strip 1 when it does).
+    int32_t strip;
+    int32_t strip_ok;
+    int32_t strip_slot;
+    int64_t strip_rest;
     float provot_ratio;     // IMP:808
     float ellipsoid[16];    // object -> world, column-major (IMP:583-585)
     float ellipsoid_inv[16];
@@ -55,6 +65,17 @@ struct BlockInfo {
     int64_t v_begin;  // global vertex range [v_begin, v_end)
     int64_t v_end;
 };
+
+// One warp's share of the strip sweep: columns c0 - 2 ... c0 + 29 of rows [r0, r1) of a
+// grid cloth (lanes 2 ... 29 own their vertex; the two lanes each side only supply their
+// springs and positions to the owners).
+struct StripWork {
+    int32_t inst;
+    int32_t c0;
+    int32_t r0, r1;
+};
+constexpr int kStripOwned = 28;    // owned columns per warp
+constexpr int kStripThreads = 256;  // 8 warps per CTA
 
 // Everything a streamed kernel needs, passed by value.
 struct StepArgs {
@@ -87,6 +108,11 @@ struct StepArgs {
     // and a block that never arrives (-1: none; set only by oc_test_barrier_timeout).
     uint32_t barrier_polls;
     int32_t withhold_block;
+    // Kernel variants of this handle: the incidence-record gather of k_assemble (0 block
+    // cooperative, 1-6 one thread per vertex, see oc_kernels.cu) and the strip sweep's
+    // register cap (2 or 3 CTAs per SM).
+    int32_t gather_variant;
+    int32_t strip_variant;
     float* dbg_F;            // optional debug outputs (float triples) or nullptr
     float* dbg_A9;
     float* dbg_b;
@@ -103,6 +129,16 @@ struct StepArgs {
     const int32_t* st_data;
     const float4* st_param;
     const float* rest_inc;   // rest length of every incidence record (CSR order), or nullptr
+    // The strip sweep: its work items, parameter-slot words and rest planes (see
+    // InstParams), the per-vertex delta0 terms it leaves for k_assemble_reduce, and the
+    // cloths on the sweep (k_assemble_finish: one CTA each).
+    const StripWork* strip_work;
+    int32_t n_strip_work;
+    const uint32_t* strip_slot;
+    const float* strip_rest;
+    float* term;
+    const int32_t* strip_ids;
+    int32_t n_strip_ids;
     // COUPLED per-incidence data is slot-major over slices of 32 consecutive vertices:
     // incidence e of vertex g sits at cpl_slice[g >> 5] + 32 e + (g & 31), so a warp's
     // accesses to one slot are contiguous.
@@ -152,7 +188,8 @@ __host__ __device__ inline int stencil_class_1d(int32_t i, int32_t n) {
 
 enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3, K_FORCES = 4, K_RESIDENT = 5,
                   K_PROVOT = 6, K_ELLIPSOID = 7, K_CPL_ASSEMBLE = 8, K_CPL_DIR = 9, K_CPL_UPDATE = 10,
-                  K_ASSEMBLE_GRID = 11, K_CG_PERSIST = 12, K_COUNT = 13 };
+                  K_ASSEMBLE_GRID = 11, K_CG_PERSIST = 12, K_ASSEMBLE_STRIP = 13, K_ASSEMBLE_REDUCE = 14,
+                  K_ASSEMBLE_FINISH = 15, K_COUNT = 16 };
 
 // The whole CG loop of a few large streamed cloths in one cooperative launch
 // (oc_kernels.cu): block table a.blocks[0, n_entries), cloths inst_ids[0, n_inst);
@@ -177,12 +214,10 @@ const void* coupled_fn(KernelKind k);
 cudaError_t launch_coupled(KernelKind k, const StepArgs& a, int nblocks, cudaStream_t stream);
 
 const char* kernel_name(KernelKind k);
-const void* kernel_fn(KernelKind k);
+const void* kernel_fn(KernelKind k, const StepArgs& a);  // the variant a selects
 int kernel_block_threads();
-size_t kernel_smem_bytes(KernelKind k);  // dynamic shared memory of a launch
-// Function attributes and the force-gather variant of k_assemble (0 block-cooperative,
-// 1/2/3 one thread per vertex with 1/2/4 incidences in flight).
-cudaError_t prepare_kernels(int gather_variant);
+size_t kernel_smem_bytes(KernelKind k, const StepArgs& a);  // dynamic shared memory of a launch
+cudaError_t prepare_kernels();  // function attributes (once per device)
 
 // Host-side launch of one kernel kind over [blk_base, blk_base + nblocks).
 cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStream_t stream);
@@ -229,11 +264,17 @@ struct PackedHost {
     std::vector<int32_t> st_data;                     // stencils of the grid cloths (see StepArgs)
     std::vector<float4> st_param;
     bool any_st_rest = false;                         // a grid cloth reads rest lengths per incidence
+    std::vector<uint32_t> strip_slot;                 // strip sweep tables (see InstParams)
+    std::vector<float> strip_rest;
     bool any_provot = false;                          // some cloth has OC_PASS_PROVOT
     bool any_coupled = false;                         // some cloth is OC_JAC_COUPLED
 };
 
 oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vertices_per_block, PackedHost* out,
                          std::string* err);
+// Marks the grid cloths whose incidences follow the reference's spring order with one
+// parameter slot per spring kind and anchor class (InstParams::strip_ok) and builds their
+// slot words and, where the rest lengths vary, their rest planes.
+void build_strip_tables(PackedHost* P);
 
 }  // namespace oc

@@ -132,10 +132,8 @@ __device__ float3 chunk_gather(const StepArgs& a, const InstParams& ip, int64_t 
 // Per-vertex part of the assembly after the force gather: the vertex's system and CG
 // set-up (pinned rows filtered out), stored to the SoA planes.  Returns the vertex's
 // term of delta0.
-__device__ __forceinline__ float assemble_vertex(const StepArgs& a, int64_t g, const float4 Xg, const float4 Vg,
-                                                 const float3 F, const OwnSpring& os) {
+__device__ __forceinline__ float store_system(const StepArgs& a, int64_t g, const float4 Vg, const VertexSystem& sys) {
     const bool pinned = Vg.w != 0.0f;
-    const VertexSystem sys = vertex_system(a.dt, Xg, Vg, F, os);
     const CgInit c = cg_init(sys, a.x[0][g], a.x[1][g], a.x[2][g], pinned);
     if (pinned) {
         a.x[0][g] = 0.0f;
@@ -162,6 +160,11 @@ __device__ __forceinline__ float assemble_vertex(const StepArgs& a, int64_t g, c
         a.dbg_b[3 * g + 2] = sys.b[2];
     }
     return c.term;
+}
+
+__device__ __forceinline__ float assemble_vertex(const StepArgs& a, int64_t g, const float4 Xg, const float4 Vg,
+                                                 const float3 F, const OwnSpring& os) {
+    return store_system(a, g, Vg, vertex_system(a.dt, Xg, Vg, F, os));
 }
 
 // Assembly with one thread per vertex (MINB: minimum resident blocks per SM, which caps
@@ -194,6 +197,289 @@ __global__ void __launch_bounds__(kThreads, 4) k_assemble_grid(const StepArgs a)
         acc_add(part, assemble_vertex(a, g, Xg, Vg, F, os));
     }
     finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
+}
+
+// ---- the strip sweep: every spring force of a grid cloth evaluated once ----------------
+// k_assemble_grid evaluates each spring at both of its ends (12 forces per vertex).  Here a
+// warp owns 28 columns of a band of rows and walks down the band one row per iteration,
+// lane l on column c0 - 2 + l, holding rows r, r+1 and r+2 of its column in registers.  In
+// row r each lane evaluates the six springs anchored at its vertex (r, c):
+//   H  (r,c)-(r,c+1)    bR (r,c)-(r,c+2)    V  (r,c)-(r+1,c)
+//   shA (r,c)-(r+1,c+1) shB (r+1,c)-(r,c+1) bC (r,c)-(r+2,c)
+// with its neighbours' positions from the lanes to its right (__shfl_down_sync), each in
+// its p1 -> p2 orientation, as the stencil gather evaluates it.  The owned vertex (r, c)
+// then has all twelve of its springs: its own six, H, bR and shB of the lanes to its left
+// this row (__shfl_up_sync), shA of the lane to its left and V and shB of its own lane one
+// row up, bC two rows up (registers); the reference's repeated bend springs are the
+// originals' values again.  It adds them in spring-id order with the p1 / p2 signs, so F is
+// the stencil gather's bits, then forms its system and CG set-up as k_assemble_grid does.
+// The two lanes on each side own nothing, and a band starts two rows early to form the
+// springs that reach into it from above.  delta0's per-vertex terms go to a.term;
+// k_assemble_reduce and k_assemble_finish sum them over the standard block table in
+// k_assemble_grid's order (the same partials and totals, so the same CG).
+
+__device__ __forceinline__ float3 shfl_down3(const float4 v, int d) {
+    return make_float3(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d),
+                       __shfl_down_sync(0xffffffffu, v.z, d));
+}
+
+__device__ __forceinline__ float3 shfl_up3(const float3 v, int d) {
+    return make_float3(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d),
+                       __shfl_up_sync(0xffffffffu, v.z, d));
+}
+
+__device__ __forceinline__ float4 xyz0(const float3 v) { return make_float4(v.x, v.y, v.z, 0.0f); }
+
+__device__ __forceinline__ void add3(float& Fx, float& Fy, float& Fz, const float3 f) {
+    Fx += f.x;
+    Fy += f.y;
+    Fz += f.z;
+}
+
+__device__ __forceinline__ void sub3(float& Fx, float& Fy, float& Fz, const float3 f) {
+    Fx -= f.x;
+    Fy -= f.y;
+    Fz -= f.z;
+}
+
+// A warp's copy of its cloth's parameter slots and slot words, in shared memory.
+struct StripParams {
+    float4 par[kStencilSlots];
+    uint32_t slot[kStencilClasses];
+};
+
+// (rest, ks, kd) of the spring of `kind` (slot word w of the anchor's class); rest lengths
+// that vary come from the anchor's rest planes (rs, fetched a row ahead).
+__device__ __forceinline__ float4 strip_param(const StripParams& sp, bool has_rest, const float* rs, uint32_t w,
+                                              int kind) {
+    float4 p = sp.par[(w >> (4 * kind)) & 15u];
+    if (has_rest) p.x = rs[kind];
+    return p;
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(kStripThreads, MINB) k_assemble_strip(const StepArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int wid = blockIdx.x * (kStripThreads / 32) + (threadIdx.x >> 5);
+    if (wid >= a.n_strip_work) return;  // whole warps leave together; no block barrier follows
+    const StripWork w = a.strip_work[wid];
+    const InstParams& ip = a.inst[w.inst];
+    const int32_t cols = ip.grid_cols, rows = ip.grid_rows, nvk = ip.nv;
+    const int64_t vo = ip.v_off;
+    const int32_t c = w.c0 - 2 + lane;
+    const bool colok = c >= 0 && c < cols;
+    const bool owner = colok && lane >= 2 && lane < 2 + kStripOwned;
+    const bool right1 = colok && c + 1 < cols && lane < 31, right2 = colok && c + 2 < cols && lane < 30;
+    __shared__ StripParams smem_par[kStripThreads / 32];
+    StripParams& sp = smem_par[threadIdx.x >> 5];
+    if (lane < kStencilSlots) sp.par[lane] = __ldg(a.st_param + ip.st_par + lane);
+    for (int q = lane; q < kStencilClasses; q += 32) sp.slot[q] = __ldg(a.strip_slot + ip.strip_slot + q);
+    __syncwarp();
+    const bool has_rest = ip.strip_rest >= 0;
+    const float* rest = has_rest ? a.strip_rest + ip.strip_rest : nullptr;
+    const int ccls = colok ? stencil_class_1d(c, cols) : 0;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float3 zero3 = make_float3(0.f, 0.f, 0.f);
+    const float h = a.dt;
+
+    // Rows r, r+1, r+2 of this lane's column; row r+3 is fetched one iteration ahead, and
+    // so are the rest lengths of the springs anchored one row down.
+    int32_t r = max(w.r0 - 2, 0);
+    const float4* Xcol = a.X + vo + c;
+    const float4* Vcol = a.V + vo + c;
+    float4 Xa = zero4, Va = zero4, Xb = zero4, Vb = zero4, Xc = zero4, Vc = zero4;
+    if (colok) {
+        Xa = __ldg(Xcol + (int64_t)r * cols);
+        Va = __ldg(Vcol + (int64_t)r * cols);
+        if (r + 1 < rows) {
+            Xb = __ldg(Xcol + (int64_t)(r + 1) * cols);
+            Vb = __ldg(Vcol + (int64_t)(r + 1) * cols);
+        }
+        if (r + 2 < rows) {
+            Xc = __ldg(Xcol + (int64_t)(r + 2) * cols);
+            Vc = __ldg(Vcol + (int64_t)(r + 2) * cols);
+        }
+    }
+    float rs[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (has_rest && colok)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) rs[k] = __ldg(rest + (size_t)k * nvk + r * cols + c);
+    // Springs anchored one and two rows up (this lane's column).
+    float3 fV1 = zero3, fA1 = zero3, fB1 = zero3, fC1 = zero3, fC2 = zero3;
+    for (; r < w.r1; ++r) {
+        const bool band = r >= w.r0;
+        const bool own = owner && band;
+        const bool springs = own && Va.w == 0.0f;  // pinned vertices take no spring force
+        const int64_t g = vo + (int64_t)r * cols + c;
+        const uint32_t sw = colok ? sp.slot[stencil_class_1d(r, rows) * 6 + ccls] : 0u;
+        float rn[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (has_rest && colok && r + 1 < w.r1)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) rn[k] = __ldg(rest + (size_t)k * nvk + (r + 1) * cols + c);
+        float4 Xd = zero4, Vd = zero4;
+        if (colok && r + 3 < rows && r + 1 < w.r1) {
+            Xd = __ldg(Xcol + (int64_t)(r + 3) * cols);
+            Vd = __ldg(Vcol + (int64_t)(r + 3) * cols);
+        }
+        // Spring i's records are fetched now and used after the forces.
+        OwnSpring os;
+        if (own) os = load_own(a, g);
+        float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
+        if (own) {
+            if (Va.w == 0.0f) {
+                Fx += Xa.w * ip.gravity[0];
+                Fy += Xa.w * ip.gravity[1];
+                Fz += Xa.w * ip.gravity[2];
+            }
+            Fx += ip.damping * Va.x;
+            Fy += ip.damping * Va.y;
+            Fz += ip.damping * Va.z;
+            if (springs && ip.has_ext) {
+                const float4 e = __ldg(a.fext + g);
+                Fx += e.x;
+                Fy += e.y;
+                Fz += e.z;
+            }
+        }
+        // The springs in spring-id order (InitGL, IMP:531-565): each evaluated where it is
+        // anchored, added at both ends, p2 subtracting and p1 adding (IMP:731-733).
+        const float4 XR1 = xyz0(shfl_down3(Xa, 1)), VR1 = xyz0(shfl_down3(Va, 1));
+        float3 fH = zero3;
+        if (band && right1) {
+            const float4 p = strip_param(sp, has_rest, rs, sw, 0);
+            fH = spring_force(Xa, XR1, Va, VR1, p.x, p.y, p.z);
+        }
+        const float3 hL = shfl_up3(fH, 1);
+        if (springs && c >= 1) sub3(Fx, Fy, Fz, hL);
+        if (springs && c + 1 < cols) add3(Fx, Fy, Fz, fH);
+        float3 fV = zero3, fA = zero3, fB = zero3;
+        const bool down1 = colok && r + 1 < rows && r >= w.r0 - 1;
+        if (down1) {
+            const float4 p = strip_param(sp, has_rest, rs, sw, 2);
+            fV = spring_force(Xa, Xb, Va, Vb, p.x, p.y, p.z);
+        }
+        if (springs && r >= 1) sub3(Fx, Fy, Fz, fV1);
+        if (springs && r + 1 < rows) add3(Fx, Fy, Fz, fV);
+        const float3 aL = shfl_up3(fA1, 1);
+        if (springs && r >= 1 && c >= 1) sub3(Fx, Fy, Fz, aL);
+        if (springs && r >= 1 && c + 1 < cols) add3(Fx, Fy, Fz, fB1);
+        if (down1 && right1) {
+            const float4 p = strip_param(sp, has_rest, rs, sw, 4);
+            fB = spring_force(Xb, XR1, Vb, VR1, p.x, p.y, p.z);
+        }
+        const float3 bL = shfl_up3(fB, 1);
+        if (springs && r + 1 < rows && c >= 1) sub3(Fx, Fy, Fz, bL);
+        {
+            const float4 XS1 = xyz0(shfl_down3(Xb, 1)), VS1 = xyz0(shfl_down3(Vb, 1));
+            if (down1 && right1) {
+                const float4 p = strip_param(sp, has_rest, rs, sw, 3);
+                fA = spring_force(Xa, XS1, Va, VS1, p.x, p.y, p.z);
+            }
+        }
+        if (springs && r + 1 < rows && c + 1 < cols) add3(Fx, Fy, Fz, fA);
+        float3 fR = zero3;
+        {
+            const float4 XR2 = xyz0(shfl_down3(Xa, 2)), VR2 = xyz0(shfl_down3(Va, 2));
+            if (band && right2) {
+                const float4 p = strip_param(sp, has_rest, rs, sw, 1);
+                fR = spring_force(Xa, XR2, Va, VR2, p.x, p.y, p.z);
+            }
+        }
+        const float3 rL = shfl_up3(fR, 2);
+        if (springs && c >= 2) sub3(Fx, Fy, Fz, rL);
+        if (springs && c + 2 < cols) add3(Fx, Fy, Fz, fR);
+        if (springs && c == cols - 3) add3(Fx, Fy, Fz, fR);  // the repeated bend spring
+        if (springs && c == cols - 1) sub3(Fx, Fy, Fz, rL);
+        float3 fC = zero3;
+        if (colok && r + 2 < rows) {
+            const float4 p = strip_param(sp, has_rest, rs, sw, 5);
+            fC = spring_force(Xa, Xc, Va, Vc, p.x, p.y, p.z);
+        }
+        if (springs && r >= 2) sub3(Fx, Fy, Fz, fC2);
+        if (springs && r + 2 < rows) add3(Fx, Fy, Fz, fC);
+        if (springs && r == rows - 3) add3(Fx, Fy, Fz, fC);
+        if (springs && r == rows - 1) sub3(Fx, Fy, Fz, fC2);
+        if (own)
+            a.term[g] = store_system(a, g, Va, system_from(own_blocks(h, Xa.w, os), h, Va, make_float3(Fx, Fy, Fz)));
+        fC2 = fC1;
+        fC1 = fC;
+        fV1 = fV;
+        fA1 = fA;
+        fB1 = fB;
+        Xa = Xb;
+        Va = Vb;
+        Xb = Xc;
+        Vb = Vc;
+        Xc = Xd;
+        Vc = Vd;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) rs[k] = rn[k];
+    }
+}
+
+// delta0 of the strip-swept cloths over the standard block table, in two launches so
+// that no blocks pile up on one atomic counter (they all finish together here, unlike
+// the assembly kernels whose epilogue this splits):
+//   k_assemble_reduce  each block sums its vertices' terms in k_assemble_grid's order into
+//                      its partial (loads eight per thread at a time; a block holds at most
+//                      2048 vertices);
+//   k_assemble_finish  one CTA per cloth sums the cloth's partials with the last-block
+//                      epilogue's tree and sets the CG scalars as finish<K_ASSEMBLE> does.
+// The same partials and the same totals, so the same CG as after k_assemble_grid.
+__global__ void __launch_bounds__(kThreads) k_assemble_reduce(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    Acc part = acc_zero();
+    for (int64_t g0 = bi.v_begin + threadIdx.x; g0 < bi.v_end; g0 += 8 * (int64_t)blockDim.x) {
+        float t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int64_t g = g0 + (int64_t)u * blockDim.x;
+            t[u] = g < bi.v_end ? __ldcg(a.term + g) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (g0 + (int64_t)u * blockDim.x < bi.v_end) acc_add(part, t[u]);
+    }
+    const double bsum = block_sum_acc(part);
+    if (threadIdx.x == 0) a.partials[bi.gblk] = bsum;
+}
+
+__global__ void __launch_bounds__(kThreads) k_assemble_finish(const StepArgs a) {
+    const int32_t inst = a.strip_ids[blockIdx.x];
+    const InstParams& ip = a.inst[inst];
+    double acc = 0.0;
+#pragma unroll 8
+    for (int j = threadIdx.x; j < ip.nblk; j += blockDim.x) acc += __ldcg(a.partials + ip.blk0 + j);
+    const double total = block_sum(acc);
+    if (threadIdx.x == 0) {
+        InstState& st = a.state[inst];
+        st.ticket = 0;
+        st.delta0 = total;
+        st.delta_new = total;
+        st.dq = 0.0;
+        st.alpha = 0.0f;
+        st.beta = 0.0f;
+        st.iter = 0;
+        st.flags = 0u;
+        bool run = (0 < ip.imax) && (total > (double)ip.eps2 * total);
+        if (!isfinite(total)) {
+            st.flags |= OC_FLAG_NON_FINITE;
+            run = false;
+        }
+        st.active = run ? 1 : 0;
+        if (run && (a.all_streamed || !ip.resident)) atomicAdd(a.unconverged, 1);
+        __threadfence();
+        if (a.use_cond) {  // the last CTA sets the graph's WHILE condition
+            const unsigned t = atomicAdd(a.grid_ticket, 1u);
+            if (t == gridDim.x - 1) {
+                *a.grid_ticket = 0u;
+                __threadfence();
+                const int u = atomicAdd(a.unconverged, 0);
+                cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond, u > 0 ? 1u : 0u);
+            }
+        }
+    }
 }
 
 // Assembly with the block-cooperative gather (shared-memory staging).
@@ -759,13 +1045,18 @@ __global__ void k_state_out(const StepArgs a, float* X3, float* V3, float* dV3, 
     }
 }
 
-// Force-gather variant of k_assemble: 0 block-cooperative, 1/2/3 one thread per
-// vertex fetching 1/2/4 incidences ahead, 4/5/6 one incidence ahead with registers
-// capped for 5/6/4 resident blocks per SM.  Measured on GB300 (1025 x 1025 cloth and
-// the 4096-cloth batch, 4/6/8 vertices per thread): variant 6 at 8 vertices per thread
-// is fastest (64 registers; the uncapped kernel takes 75 and runs 1.5x slower, tighter
-// caps spill; wider prefetch costs occupancy).
-int kGatherVariant = 6;
+// Force-gather variant of k_assemble (StepArgs::gather_variant): 0 block-cooperative,
+// 1/2/3 one thread per vertex fetching 1/2/4 incidences ahead, 4/5/6 one incidence ahead
+// with registers capped for 5/6/4 resident blocks per SM.  Measured on GB300 (1025 x 1025
+// cloth and the 4096-cloth batch, 4/6/8 vertices per thread): variant 6 at 8 vertices per
+// thread is fastest (64 registers; the uncapped kernel takes 75 and runs 1.5x slower,
+// tighter caps spill; wider prefetch costs occupancy).
+//
+// The strip sweep's register cap (StepArgs::strip_variant): 2 resident CTAs per SM (128
+// registers, no spill) or 3 (80 registers, with spills).
+const void* strip_fn(int v) {
+    return v == 3 ? (const void*)k_assemble_strip<3> : (const void*)k_assemble_strip<2>;
+}
 
 const void* assemble_fn(int v) {
     switch (v) {
@@ -794,15 +1085,18 @@ const char* kernel_name(KernelKind k) {
         case K_CPL_ASSEMBLE: return "k_cpl_assemble";
         case K_ASSEMBLE_GRID: return "k_assemble_grid";
         case K_CG_PERSIST: return "k_cg_persist";
+        case K_ASSEMBLE_STRIP: return "k_assemble_strip";
+        case K_ASSEMBLE_REDUCE: return "k_assemble_reduce";
+        case K_ASSEMBLE_FINISH: return "k_assemble_finish";
         case K_CPL_DIR: return "k_cpl_dir";
         case K_CPL_UPDATE: return "k_cpl_update";
         default: return "?";
     }
 }
 
-const void* kernel_fn(KernelKind k) {
+const void* kernel_fn(KernelKind k, const StepArgs& a) {
     switch (k) {
-        case K_ASSEMBLE: return assemble_fn(kGatherVariant);
+        case K_ASSEMBLE: return assemble_fn(a.gather_variant);
         case K_CG_DIR: return (const void*)k_cg_dir;
         case K_CG_UPDATE: return (const void*)k_cg_update;
         case K_INTEGRATE: return (const void*)k_integrate;
@@ -813,17 +1107,20 @@ const void* kernel_fn(KernelKind k) {
         case K_CPL_DIR:
         case K_CPL_UPDATE: return coupled_fn(k);
         case K_ASSEMBLE_GRID: return (const void*)k_assemble_grid;
+        case K_ASSEMBLE_STRIP: return strip_fn(a.strip_variant);
+        case K_ASSEMBLE_REDUCE: return (const void*)k_assemble_reduce;
+        case K_ASSEMBLE_FINISH: return (const void*)k_assemble_finish;
         default: return nullptr;
     }
 }
 
 int kernel_block_threads() { return kThreads; }
 
-size_t kernel_smem_bytes(KernelKind k) { return (k == K_ASSEMBLE && kGatherVariant == 0) ? kGatherSmem : 0; }
+size_t kernel_smem_bytes(KernelKind k, const StepArgs& a) {
+    return (k == K_ASSEMBLE && a.gather_variant == 0) ? kGatherSmem : 0;
+}
 
-cudaError_t prepare_kernels(int gather_variant) {
-    if (gather_variant < 0 || gather_variant > 6) return cudaErrorInvalidValue;
-    kGatherVariant = gather_variant;
+cudaError_t prepare_kernels() {
     return cudaFuncSetAttribute(k_assemble_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGatherSmem);
 }
 
@@ -853,10 +1150,10 @@ cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStre
     if (nblocks <= 0) return cudaSuccess;
     switch (k) {
         case K_ASSEMBLE:
-            if (kGatherVariant == 0)
+            if (a.gather_variant == 0)
                 k_assemble_coop<<<nblocks, kThreads, kGatherSmem, stream>>>(a);
             else
-                reinterpret_cast<void (*)(StepArgs)>(const_cast<void*>(assemble_fn(kGatherVariant)))
+                reinterpret_cast<void (*)(StepArgs)>(const_cast<void*>(assemble_fn(a.gather_variant)))
                     <<<nblocks, kThreads, 0, stream>>>(a);
             break;
         case K_CG_DIR: k_cg_dir<<<nblocks, kThreads, 0, stream>>>(a); break;
@@ -869,6 +1166,12 @@ cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStre
         case K_CPL_DIR:
         case K_CPL_UPDATE: return launch_coupled(k, a, nblocks, stream);
         case K_ASSEMBLE_GRID: k_assemble_grid<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_ASSEMBLE_STRIP:
+            reinterpret_cast<void (*)(StepArgs)>(const_cast<void*>(strip_fn(a.strip_variant)))
+                <<<nblocks, kStripThreads, 0, stream>>>(a);
+            break;
+        case K_ASSEMBLE_REDUCE: k_assemble_reduce<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_ASSEMBLE_FINISH: k_assemble_finish<<<nblocks, kThreads, 0, stream>>>(a); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -1,6 +1,7 @@
 // Host-side topology: the reference grid builder, input validation, and packing of
 // many cloths into one ragged structure-of-arrays batch with a vertex->spring
 // incidence (CSR) ordered by spring id.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -337,6 +338,119 @@ oc_status pack_instances(const oc_cloth_desc* descs, int32_t n, int32_t vpb, Pac
         P.own_ent[oc[e.y]++] = (int32_t)((uint32_t)i | 0x80000000u);
     }
     return OC_OK;
+}
+
+// The strip sweep's tables.  A grid cloth qualifies when every vertex's incidences are,
+// in order, the springs the reference's InitGL loops give it (IMP:531-565), listed below
+// with the anchor that owns each spring in the sweep (the spring's upper-left end; for
+// the second shear spring of a quad, the quad's upper-left corner), and every spring of a
+// kind whose anchor lies in one position class shares one parameter slot.  The repeated
+// bend springs of the last three rows and columns must share their original's slot (and
+// rest length), so the sweep reuses the original's force for them.
+namespace {
+
+enum StripKind { SK_H = 0, SK_BR = 1, SK_V = 2, SK_SHA = 3, SK_SHB = 4, SK_BC = 5 };
+
+struct StripEntry {
+    int8_t dr, dc, p2, kind;
+    int32_t ar, ac;  // anchor
+};
+
+// Vertex (r, c)'s incidences in spring-id order (the kernel adds them in this order).
+int strip_entries(int32_t r, int32_t c, int32_t rows, int32_t cols, StripEntry* out) {
+    int n = 0;
+    auto add = [&](int dr, int dc, int p2, int kind, int32_t ar, int32_t ac) {
+        out[n++] = StripEntry{(int8_t)dr, (int8_t)dc, (int8_t)p2, (int8_t)kind, ar, ac};
+    };
+    if (c >= 1) add(0, -1, 1, SK_H, r, c - 1);                                    // horizontal structural
+    if (c + 1 < cols) add(0, 1, 0, SK_H, r, c);
+    if (r >= 1) add(-1, 0, 1, SK_V, r - 1, c);                                    // vertical structural
+    if (r + 1 < rows) add(1, 0, 0, SK_V, r, c);
+    if (r >= 1 && c >= 1) add(-1, -1, 1, SK_SHA, r - 1, c - 1);                   // shear, quad by quad
+    if (r >= 1 && c + 1 < cols) add(-1, 1, 0, SK_SHB, r - 1, c);
+    if (r + 1 < rows && c >= 1) add(1, -1, 1, SK_SHB, r, c - 1);
+    if (r + 1 < rows && c + 1 < cols) add(1, 1, 0, SK_SHA, r, c);
+    if (c >= 2) add(0, -2, 1, SK_BR, r, c - 2);                                   // bend along the row
+    if (c + 2 < cols) add(0, 2, 0, SK_BR, r, c);
+    if (c == cols - 3) add(0, 2, 0, SK_BR, r, c);                                 // its repeat
+    if (c == cols - 1) add(0, -2, 1, SK_BR, r, c - 2);
+    if (r >= 2) add(-2, 0, 1, SK_BC, r - 2, c);                                   // bend along the column
+    if (r + 2 < rows) add(2, 0, 0, SK_BC, r, c);
+    if (r == rows - 3) add(2, 0, 0, SK_BC, r, c);                                 // its repeat
+    if (r == rows - 1) add(-2, 0, 1, SK_BC, r - 2, c);
+    return n;
+}
+
+}  // namespace
+
+void build_strip_tables(PackedHost* Pp) {
+    PackedHost& P = *Pp;
+    P.strip_slot.clear();
+    P.strip_rest.clear();
+    for (int32_t k = 0; k < P.n_inst; ++k) {
+        InstParams& ip = P.inst[k];
+        ip.strip = ip.strip_ok = 0;
+        ip.strip_slot = -1;
+        ip.strip_rest = -1;
+        if (ip.grid_cols <= 0 || ip.coupled) continue;
+        const int32_t cols = ip.grid_cols, rows = ip.grid_rows, nvk = ip.nv;
+        const int64_t vo = P.v_off[k];
+        const int32_t* st = P.st_data.data() + ip.st_off;
+        int slot[6][kStencilClasses];
+        for (auto& row : slot)
+            for (int& x : row) x = -1;
+        std::vector<int32_t> rest_bits(ip.st_rest ? 6 * (size_t)nvk : 0, 0);
+        std::vector<uint8_t> rest_set(rest_bits.size(), 0);
+        bool ok = true;
+        StripEntry ex[16];
+        for (int32_t l = 0; l < nvk && ok; ++l) {
+            const int32_t r = l / cols, c = l % cols;
+            const int cl = stencil_class_1d(r, rows) * 6 + stencil_class_1d(c, cols);
+            const int32_t e0 = st[cl], e1 = st[cl + 1];
+            const int n = strip_entries(r, c, rows, cols, ex);
+            if (n != e1 - e0) {
+                ok = false;
+                break;
+            }
+            for (int i = 0; i < n && ok; ++i) {
+                const int32_t v = st[e0 + i];
+                if ((v & 7) - 2 != ex[i].dr || ((v >> 3) & 7) - 2 != ex[i].dc || ((v >> 6) & 1) != ex[i].p2) {
+                    ok = false;
+                    break;
+                }
+                const int acl = stencil_class_1d(ex[i].ar, rows) * 6 + stencil_class_1d(ex[i].ac, cols);
+                int& sl = slot[ex[i].kind][acl];
+                if (sl < 0)
+                    sl = v >> 7;
+                else if (sl != (v >> 7))
+                    ok = false;
+                if (ip.st_rest && ok) {
+                    const size_t at = (size_t)ex[i].kind * nvk + (size_t)ex[i].ar * cols + ex[i].ac;
+                    const int32_t rb = P.inc[(size_t)(P.rowptr[vo + l] + i)].y;
+                    if (!rest_set[at]) {
+                        rest_set[at] = 1;
+                        rest_bits[at] = rb;
+                    } else if (rest_bits[at] != rb) {
+                        ok = false;
+                    }
+                }
+            }
+        }
+        if (!ok) continue;
+        ip.strip_ok = 1;
+        ip.strip_slot = (int32_t)P.strip_slot.size();
+        for (int cl = 0; cl < kStencilClasses; ++cl) {
+            uint32_t w = 0;
+            for (int kind = 0; kind < 6; ++kind) w |= (uint32_t)(std::max(slot[kind][cl], 0) & 15) << (4 * kind);
+            P.strip_slot.push_back(w);
+        }
+        if (ip.st_rest) {
+            ip.strip_rest = (int64_t)P.strip_rest.size();
+            const size_t base = P.strip_rest.size();
+            P.strip_rest.resize(base + rest_bits.size());
+            std::memcpy(P.strip_rest.data() + base, rest_bits.data(), rest_bits.size() * sizeof(float));
+        }
+    }
 }
 
 }  // namespace oc

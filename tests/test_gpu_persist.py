@@ -86,8 +86,13 @@ def test_launch_count_is_per_step():
         s.step(DT, 1)
         l0 = s.launch_count()
         s.step(DT, 5)
-        # assembly + the persistent CG (with the update) per step
+        # the stencil assembly and the persistent CG (with the update) per step
         assert s.launch_count() - l0 == 10
+        s.set_launch_config(strip=1)
+        l0 = s.launch_count()
+        s.step(DT, 5)
+        # with the strip sweep: the sweep, its delta0 partials and totals, and the persistent CG
+        assert s.launch_count() - l0 == 20
 
 
 def test_barrier_wait_runs_out_and_the_handle_steps_on():

@@ -136,3 +136,86 @@ def test_spring_params_refit_the_stencil(executor):
             assert all(k == stencil for k in kinds)
             for x, y in zip(got, want):
                 assert same_bits(x, y)
+
+
+def run_env(descs, X, V, steps, env: dict, dt: float = DT, **kw):
+    """Create a handle with the given environment switches set (read at create time)."""
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update({k: str(v) for k, v in env.items()})
+    try:
+        s = ClothSolver(descs, **kw)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+    with s:
+        s.set_state(X, V)
+        s.step(dt, steps)
+        return s.get_state(), s.stats()
+
+
+def strip_batch(seed: int):
+    """Grid cloths for the strip sweep: exact spacing (rest lengths in the slots) and
+    inexact (rest planes), square and not, widths around the strip boundaries (28 owned
+    columns per warp), extra pins, per-vertex masses and an external force on one cloth."""
+    rng = np.random.default_rng(seed)
+    descs, Xs, Vs = [], [], []
+    for cols, rows in ((21, 21), (28, 9), (29, 30), (33, 17), (56, 57), (57, 20), (85, 40), (129, 65)):
+        X, sp = grid_cloth(cols, rows, ks=tuple(rng.uniform(20, 80, 3)), kd=tuple(rng.uniform(-0.5, -0.05, 3)),
+                           jitter=1e-2, seed=cols * 1000 + rows)
+        V = rng.normal(0.0, 0.02, X.shape).astype(np.float32)
+        pins = np.unique(np.array([0, cols - 1, int(rng.integers(0, cols * rows))], np.int32))
+        V[pins] = 0.0
+        mass = rng.uniform(0.5, 2.0, cols * rows).astype(np.float32) if cols == 33 else None
+        ext = rng.normal(0.0, 1e-3, X.shape).astype(np.float32) if cols == 57 else None
+        descs.append(ClothDesc(n_vertices=cols * rows, springs=sp, pinned=pins, mass=mass, ext_force=ext,
+                               cg_max_iter=60, cg_tol=1e-6))
+        Xs.append(X)
+        Vs.append(V)
+    return descs, np.concatenate(Xs), np.concatenate(Vs)
+
+
+@pytest.mark.parametrize("rows_per_band", [0, 1, 2, 5, 16])
+@pytest.mark.parametrize("executor", ["streamed", "resident"])
+def test_strip_sweep_same_bits_as_stencil(rows_per_band, executor):
+    """k_assemble_strip (each spring force once, bands of rows, delta0 reduced over the
+    standard blocks) against k_assemble_grid (each spring at both ends): the same F, A, b
+    and delta0, so the same steps bit for bit, for any band height."""
+    descs, X, V = strip_batch(11)
+    env = {"OC_STRIP": 1}
+    if rows_per_band:
+        env["OC_STRIP_ROWS"] = rows_per_band
+    a, sa = run_env(descs, X, V, 12, env, executor=executor)
+    b, sb = run_env(descs, X, V, 12, {"OC_STRIP": 0}, executor=executor)
+    for x, y in zip(a, b):
+        assert same_bits(x, y)
+    assert np.array_equal(sa[0], sb[0]) and np.array_equal(sa[2], sb[2])
+
+
+def test_strip_sweep_exact_spacing_and_passes():
+    """Exact grid spacing (rest lengths in the parameter slots) with the StepPhysics passes,
+    against the incidence-record gather."""
+    from opencloth_gb300 import PASS_ELLIPSOID, PASS_PROVOT, reference_ellipsoid
+
+    E, Einv = reference_ellipsoid()
+    X, sp = grid_cloth(65, 33, ks=(50.75, 50.75, 50.95), kd=(-0.25, -0.25, -0.25))
+    d = ClothDesc(n_vertices=65 * 33, springs=sp, pinned=np.array([0, 64], np.int32), cg_max_iter=200, cg_tol=1e-5,
+                  passes=PASS_ELLIPSOID | PASS_PROVOT, ellipsoid=E, ellipsoid_inv=Einv)
+    V = np.zeros_like(X)
+    a, sa = run_env(d, X, V, 20, {"OC_STRIP": 1, "OC_STRIP_ROWS": 4})
+    b, sb = run_env(d, X, V, 20, {"OC_STENCIL": 0})
+    for x, y in zip(a, b):
+        assert same_bits(x, y)
+    assert np.array_equal(sa[0], sb[0])
+
+
+def test_strip_sweep_profile_names_its_kernels():
+    descs, X, V = strip_batch(3)
+    with ClothSolver(descs, executor="streamed") as s:
+        s.set_launch_config(strip=1)
+        s.set_state(X, V)
+        prof = s.profile(DT, 2)
+    assert prof["k_assemble_strip"]["launches"] == 2 and prof["k_assemble_reduce"]["launches"] == 2
+    assert prof["k_assemble_finish"]["launches"] == 2
