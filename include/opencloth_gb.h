@@ -236,6 +236,22 @@ oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t check
 oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV, float* dL_dX0, float* dL_dV0,
                            float* dL_dKs, float* dL_dKd, float* dL_dext);
 oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* tape_bytes);
+/* How the taped forward holds positions.  OC_TAPE_POSITIONS: as the step does (FP32
+ * positions; the forward is the step itself).  OC_TAPE_DISPLACEMENT: as the start
+ * positions plus an FP32 displacement, with each spring's elongation formed from its
+ * start constants rounded from FP64, so that a cloth that moves little keeps the digits
+ * of its motion (an FP32 position near 5 resolves about 5e-7; a gradient of a loss whose
+ * residual is a few 1e-6 needs about 1e-9).  The displacement forward otherwise follows
+ * the step's arithmetic; it needs the handle to run its adjoint solves as one cooperative
+ * launch (at most 16 cloths, no COUPLED cloth; OC_ERR_UNSUPPORTED otherwise).  Setting the
+ * mode invalidates the tape. */
+#define OC_TAPE_POSITIONS 0
+#define OC_TAPE_DISPLACEMENT 1
+oc_status oc_set_tape_mode(oc_solver* s, int32_t mode);
+/* After a displacement-mode oc_tape_forward: the final displacement from the positions
+ * the forward started from (host float triples).  A caller forms its loss residual from
+ * it in FP64 (start positions + displacement - target). */
+oc_status oc_tape_displacement(oc_solver* s, float* u);
 
 /* ---- launch configuration and its autotuner ------------------------------------------ */
 /* How a handle launches its step: which cloths run resident and in what CTA shape, whether

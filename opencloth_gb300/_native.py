@@ -130,6 +130,8 @@ SIGNATURES = {
     "oc_tape_backward": (C.c_int32, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "oc_tape_info": (C.c_int32, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
     "oc_test_barrier_timeout": (C.c_int32, [_P, C.c_int32, C.c_uint32]),
+    "oc_set_tape_mode": (C.c_int32, [_P, C.c_int32]),
+    "oc_tape_displacement": (C.c_int32, [_P, _P]),
     "oc_get_launch_config": (C.c_int32, [_P, C.POINTER(LaunchConfigC)]),
     "oc_set_launch_config": (C.c_int32, [_P, C.POINTER(LaunchConfigC)]),
     "oc_autotune": (C.c_int32, [_P, C.c_float, C.c_char_p, C.c_int32, C.POINTER(LaunchConfigC),

@@ -320,6 +320,17 @@ class ClothSolver:
                                               ptr(out["dKs"]), ptr(out["dKd"]), ptr(out["dext"])))
         return out
 
+    def set_tape_mode(self, displacement: bool) -> None:
+        """Taped forward in the displacement mode (start positions + FP32 displacement,
+        precise elongations) or in positions (the step itself)."""
+        self._call(self._lib.oc_set_tape_mode(self._h, 1 if displacement else 0))
+
+    def tape_displacement(self) -> np.ndarray:
+        """The final displacement of the last displacement-mode taped forward."""
+        u = np.empty((self.n_vertices, 3), np.float32)
+        self._call(self._lib.oc_tape_displacement(self._h, ptr(u)))
+        return u
+
     def tape_info(self):
         every, nbytes = C.c_int32(), C.c_int64()
         self._call(self._lib.oc_tape_info(self._h, C.byref(every), C.byref(nbytes)))

@@ -16,6 +16,8 @@
 // reference's rounding sequence.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "oc_device.cuh"
 #include "oc_internal.h"
 
@@ -28,16 +30,72 @@ __device__ __forceinline__ float dot3f(float ax, float ay, float az, float bx, f
     return ax * bx + ay * by + az * bz;
 }
 
+// A spring's geometry: dP = x_p1 - x_p2, its length L, 1/L and the elongation C = L - rest.
+struct Geo {
+    float dP[3];
+    float L, iL, C;
+};
+
+// From positions.
+__device__ __forceinline__ Geo geo_plain(const float4 p1, const float4 p2, float rest) {
+    Geo g;
+    g.dP[0] = p1.x - p2.x;
+    g.dP[1] = p1.y - p2.y;
+    g.dP[2] = p1.z - p2.z;
+    g.L = sqrtf(dot3f(g.dP[0], g.dP[1], g.dP[2], g.dP[0], g.dP[1], g.dP[2]));
+    g.iL = 1.0f / g.L;
+    g.C = g.L - rest;
+    return g;
+}
+
+// Displacement mode: base positions b and displacements u of the two ends, and the
+// spring's constants k = {c0, L0} (c0 = |d0| - rest, L0 = |d0|, d0 = b1 - b2, rounded
+// from FP64).  dP = d0 + (u1 - u2); the elongation is c0 + (|dP|^2 - |d0|^2) / (|dP| + |d0|)
+// with |dP|^2 - |d0|^2 = 2 d0.du + du.du, so it keeps its relative precision when the
+// elongation is small against the length (an FP32 L - rest would not).
+__device__ __forceinline__ Geo geo_disp(const float4 b1, const float4 b2, const float4 u1, const float4 u2,
+                                        const float2 k) {
+    const float d0[3] = {b1.x - b2.x, b1.y - b2.y, b1.z - b2.z};
+    const float du[3] = {u1.x - u2.x, u1.y - u2.y, u1.z - u2.z};
+    Geo g;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) g.dP[c] = d0[c] + du[c];
+    g.L = sqrtf(dot3f(g.dP[0], g.dP[1], g.dP[2], g.dP[0], g.dP[1], g.dP[2]));
+    g.iL = 1.0f / g.L;
+    const float grow =
+        2.0f * dot3f(d0[0], d0[1], d0[2], du[0], du[1], du[2]) + dot3f(du[0], du[1], du[2], du[0], du[1], du[2]);
+    g.C = k.x + grow / (g.L + k.y);
+    return g;
+}
+
+// Spring (p1, p2) with ends at x1, x2 (positions, or displacements in the displacement
+// mode, where consts[at] holds its start constants).
+__device__ __forceinline__ Geo spring_geo(const StepArgs& a, int32_t p1, int32_t p2, const float4 x1, const float4 x2,
+                                          float rest, const float2* consts, int64_t at) {
+    if (!a.gm) return geo_plain(x1, x2, rest);
+    return geo_disp(__ldg(a.Xbase + p1), __ldg(a.Xbase + p2), x1, x2, __ldg(consts + at));
+}
+
+// The per-spring quantities of CalcForceDerivatives (IMP:719-724) from a geometry.
+__device__ __forceinline__ void spring_eval(const Geo& G, const float4 v1, const float4 v2, SpringEval& e) {
+    e.C = G.C;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        e.n[c] = G.dP[c] * G.iL;
+        e.q[c] = G.dP[c] * G.dP[c];
+    }
+    e.Cdot = (v1.x * (-e.n[0]) + v1.y * (-e.n[1]) + v1.z * (-e.n[2])) + (v2.x * e.n[0] + v2.y * e.n[1] + v2.z * e.n[2]);
+}
+
 // Adjoint of one spring force f = (-Ks C + Kd u) n for dL/df = g.
-__device__ __forceinline__ void spring_force_adj(const float4 p1, const float4 p2, const float4 v1, const float4 v2,
-                                                 float rest, float ks, float kd, const float g[3], float gdP[3],
-                                                 float gdV[3], float& gks, float& gkd) {
-    const float dP[3] = {p1.x - p2.x, p1.y - p2.y, p1.z - p2.z};
+__device__ __forceinline__ void spring_force_adj(const Geo& G, const float4 v1, const float4 v2, float ks, float kd,
+                                                 const float g[3], float gdP[3], float gdV[3], float& gks,
+                                                 float& gkd) {
+    const float* dP = G.dP;
     const float dV[3] = {v1.x - v2.x, v1.y - v2.y, v1.z - v2.z};
-    const float L = sqrtf(dot3f(dP[0], dP[1], dP[2], dP[0], dP[1], dP[2]));
-    const float iL = 1.0f / L;
+    const float iL = G.iL;
     const float n[3] = {dP[0] * iL, dP[1] * iL, dP[2] * iL};
-    const float C = L - rest;
+    const float C = G.C;
     const float u = dot3f(dV[0], dV[1], dV[2], dP[0], dP[1], dP[2]) * iL;
     const float m = -ks * C + kd * u;
     const float gm = dot3f(g[0], g[1], g[2], n[0], n[1], n[2]);
@@ -53,16 +111,14 @@ __device__ __forceinline__ void spring_force_adj(const float4 p1, const float4 p
 }
 
 // Adjoint of spring i's (J, Jv) for G = dL/dJ, H = dL/dJv (full 3x3, row-major).
-__device__ __forceinline__ void spring_jac_adj(const float4 p1, const float4 p2, const float4 v1, const float4 v2,
-                                               float rest, float ks, float kd, const float G[3][3],
-                                               const float H[3][3], float gdP[3], float gdV[3], float& gks,
-                                               float& gkd) {
-    const float dP[3] = {p1.x - p2.x, p1.y - p2.y, p1.z - p2.z};
+__device__ __forceinline__ void spring_jac_adj(const Geo& Gm, const float4 v1, const float4 v2, float ks, float kd,
+                                               const float G[3][3], const float H[3][3], float gdP[3], float gdV[3],
+                                               float& gks, float& gkd) {
+    const float* dP = Gm.dP;
     const float dV[3] = {v1.x - v2.x, v1.y - v2.y, v1.z - v2.z};
-    const float L = sqrtf(dot3f(dP[0], dP[1], dP[2], dP[0], dP[1], dP[2]));
-    const float iL = 1.0f / L;
+    const float iL = Gm.iL;
     const float n[3] = {dP[0] * iL, dP[1] * iL, dP[2] * iL};
-    const float C = L - rest;
+    const float C = Gm.C;
     const float Cd = -dot3f(n[0], n[1], n[2], dV[0], dV[1], dV[2]);
     const float w = ks * C + kd * Cd;
     float gS[3][3];
@@ -115,7 +171,8 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_seed(const StepArgs a, cons
         const float4 Xg = a.X[g], Vg = a.V[g];
         const float dvy = j.dV[1][g];
         const float vy = Vg.y + dvy * dt;
-        const float ypre = Xg.y + dt * vy;
+        const float y = a.gm ? __ldg(a.Xbase + g).y + Xg.y : Xg.y;  // displacement mode: X holds u
+        const float ypre = y + dt * vy;
         float gx0 = j.gX[0][g], gx1 = j.gX[1][g], gx2 = j.gX[2][g];
         if (ypre < 0.0f) gx1 = 0.0f;  // clamped: X'.y does not depend on X, V
         const float gv0 = j.gV[0][g] + dt * gx0, gv1 = j.gV[1][g] + dt * gx1, gv2 = j.gV[2][g] + dt * gx2;
@@ -163,8 +220,9 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_vertex(const StepArgs a, co
         float gdP[3] = {0.f, 0.f, 0.f}, gdVs[3] = {0.f, 0.f, 0.f};
         const OwnSpring os = load_own(a, g);
         if (os.ends.x >= 0 && !pinned) {
+            const Geo geo = spring_geo(a, os.ends.x, os.ends.y, os.E1, os.E2, os.par.x, a.gm_own, g);
             SpringEval e;
-            spring_state(os.E1, os.E2, os.W1, os.W2, os.par.x, e);
+            spring_eval(geo, os.W1, os.W2, e);
             float J[6], Jv[6];
             jac_element(e, os.par.y, os.par.z, 0, 0, J[0], Jv[0]);
             jac_element(e, os.par.y, os.par.z, 0, 1, J[1], Jv[1]);
@@ -186,7 +244,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_vertex(const StepArgs a, co
                     H[r][c] = h * lam[r] * dv[c];
                 }
             float gks, gkd;
-            spring_jac_adj(os.E1, os.E2, os.W1, os.W2, os.par.x, os.par.y, os.par.z, G, H, gdP, gdVs, gks, gkd);
+            spring_jac_adj(geo, os.W1, os.W2, os.par.y, os.par.z, G, H, gdP, gdVs, gks, gkd);
             const int32_t sid = j.own_sid[g];
             j.gKs[sid] += gks;
             j.gKd[sid] += gkd;
@@ -267,10 +325,13 @@ __global__ void __launch_bounds__(kAdjThreads, 2) k_adj_springs(const StepArgs a
                 const float rest = __int_as_float(rec[u].y), ks = __int_as_float(rec[u].z),
                             kd = __int_as_float(rec[u].w);
                 float gdP[3], gdV[3], gks, gkd;
+                const int32_t o = rec[u].x & 0x7fffffff;
                 if (as_p2)
-                    spring_force_adj(Xo[u], Xg, Vo[u], Vg, rest, ks, kd, gf, gdP, gdV, gks, gkd);
+                    spring_force_adj(spring_geo(a, o, (int32_t)g, Xo[u], Xg, rest, a.gm_inc, kb + u), Vo[u], Vg, ks, kd,
+                                     gf, gdP, gdV, gks, gkd);
                 else
-                    spring_force_adj(Xg, Xo[u], Vg, Vo[u], rest, ks, kd, gf, gdP, gdV, gks, gkd);
+                    spring_force_adj(spring_geo(a, (int32_t)g, o, Xg, Xo[u], rest, a.gm_inc, kb + u), Vg, Vo[u], ks, kd,
+                                     gf, gdP, gdV, gks, gkd);
                 const float sgn = as_p2 ? -1.0f : 1.0f;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
@@ -299,6 +360,170 @@ __global__ void __launch_bounds__(kAdjThreads, 2) k_adj_springs(const StepArgs a
             j.gX[c][g] = gx[c];
             j.gV[c][g] = gv[c];
         }
+    }
+}
+
+// ---- displacement mode: the taped forward in X = Xbase + u --------------------------------
+// An FP32 position near 5 resolves steps of about 5e-7, and an FP32 L - rest loses the
+// bits of an elongation 1e-3 of the length, so an FP32 trajectory of a slow cloth drifts
+// from the FP64 one by a good fraction of a small loss residual.  In this mode the state
+// holds the displacement u from the tape's start and each spring's elongation is formed
+// from its FP64-rounded start constants (geo_disp); the forward otherwise follows the
+// step's arithmetic, the CG included.
+
+// 0: Xbase = X.
+__global__ void k_gm_base(const StepArgs a, int64_t nv) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nv; g += (int64_t)gridDim.x * blockDim.x)
+        const_cast<float4*>(a.Xbase)[g] = a.X[g];
+}
+
+__device__ __forceinline__ float2 spring_consts(const float4 b1, const float4 b2, float rest) {
+    const double dx = (double)b1.x - (double)b2.x, dy = (double)b1.y - (double)b2.y, dz = (double)b1.z - (double)b2.z;
+    const double L0 = sqrt(dx * dx + dy * dy + dz * dz);
+    return make_float2((float)(L0 - (double)rest), (float)L0);
+}
+
+// 4: the spring constants from Xbase, and u = 0 (mass kept in w).
+__global__ void k_gm_consts(const StepArgs a, int64_t nv) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nv; g += (int64_t)gridDim.x * blockDim.x) {
+        const float4 bg = __ldg(a.Xbase + g);
+        const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
+        for (int32_t k = k0; k < k1; ++k) {
+            const int4 rec = __ldg(a.inc + k);
+            const float4 bo = __ldg(a.Xbase + (rec.x & 0x7fffffff));
+            const float rest = __int_as_float(rec.y);
+            const_cast<float2*>(a.gm_inc)[k] = rec.x < 0 ? spring_consts(bo, bg, rest) : spring_consts(bg, bo, rest);
+        }
+        const int2 e = __ldg(a.own_ends + g);
+        float2 own = make_float2(0.f, 0.f);
+        if (e.x >= 0) own = spring_consts(__ldg(a.Xbase + e.x), __ldg(a.Xbase + e.y), __ldg(a.own_par + g).x);
+        const_cast<float2*>(a.gm_own)[g] = own;
+        a.X[g] = make_float4(0.f, 0.f, 0.f, bg.w);
+    }
+}
+
+// 3: X = Xbase + u.
+__global__ void k_gm_leave(const StepArgs a, int64_t nv) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nv; g += (int64_t)gridDim.x * blockDim.x) {
+        const float4 b = __ldg(a.Xbase + g), u = a.X[g];
+        a.X[g] = make_float4(b.x + u.x, b.y + u.y, b.z + u.z, u.w);
+    }
+}
+
+// The spring force on p1 (IMP:717-728) from a geometry.
+__device__ __forceinline__ float3 spring_force_geo(const Geo& G, const float4 v1, const float4 v2, float ks, float kd) {
+    const float dVx = v1.x - v2.x, dVy = v1.y - v2.y, dVz = v1.z - v2.z;
+    const float left = (-ks) * G.C;
+    const float right = kd * (dot3f(dVx, dVy, dVz, G.dP[0], G.dP[1], G.dP[2]) * G.iL);
+    const float mag = left + right;
+    return make_float3(mag * (G.dP[0] * G.iL), mag * (G.dP[1] * G.iL), mag * (G.dP[2] * G.iL));
+}
+
+// 1: the step's assembly in displacement mode (incidence-record gather in spring order,
+// spring i's Jacobians, A and b, the CG set-up), one thread per vertex.
+__global__ void __launch_bounds__(kAdjThreads) k_gm_assemble(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const InstParams& ip = a.inst[bi.inst];
+    const float h = a.dt;
+    Acc part = acc_zero();
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Ug = a.X[g], Vg = a.V[g];
+        const bool pinned = Vg.w != 0.0f;
+        float Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
+        if (!pinned) {
+            Fx += Ug.w * ip.gravity[0];
+            Fy += Ug.w * ip.gravity[1];
+            Fz += Ug.w * ip.gravity[2];
+        }
+        Fx += ip.damping * Vg.x;
+        Fy += ip.damping * Vg.y;
+        Fz += ip.damping * Vg.z;
+        if (!pinned) {
+            if (ip.has_ext) {
+                const float4 e = __ldg(a.fext + g);
+                Fx += e.x;
+                Fy += e.y;
+                Fz += e.z;
+            }
+            const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
+            for (int32_t k = k0; k < k1; ++k) {
+                const int4 rec = __ldg(a.inc + k);
+                const int32_t o = rec.x & 0x7fffffff;
+                const float4 Uo = a.X[o], Vo = a.V[o];
+                const float ks = __int_as_float(rec.z), kd = __int_as_float(rec.w);
+                if (rec.x < 0) {  // F[p2] -= f
+                    const float3 f =
+                        spring_force_geo(spring_geo(a, o, (int32_t)g, Uo, Ug, 0.0f, a.gm_inc, k), Vo, Vg, ks, kd);
+                    Fx -= f.x;
+                    Fy -= f.y;
+                    Fz -= f.z;
+                } else {  // F[p1] += f
+                    const float3 f =
+                        spring_force_geo(spring_geo(a, (int32_t)g, o, Ug, Uo, 0.0f, a.gm_inc, k), Vg, Vo, ks, kd);
+                    Fx += f.x;
+                    Fy += f.y;
+                    Fz += f.z;
+                }
+            }
+        }
+        // Spring i's Jacobians (IMP:744-770) and the vertex's system.
+        const OwnSpring os = load_own(a, g);
+        float J[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, Jv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (os.ends.x >= 0) {
+            SpringEval e;
+            spring_eval(spring_geo(a, os.ends.x, os.ends.y, os.E1, os.E2, 0.0f, a.gm_own, g), os.W1, os.W2, e);
+            jac_element(e, os.par.y, os.par.z, 0, 0, J[0], Jv[0]);
+            jac_element(e, os.par.y, os.par.z, 0, 1, J[1], Jv[1]);
+            jac_element(e, os.par.y, os.par.z, 0, 2, J[2], Jv[2]);
+            jac_element(e, os.par.y, os.par.z, 1, 1, J[3], Jv[3]);
+            jac_element(e, os.par.y, os.par.z, 1, 2, J[4], Jv[4]);
+            jac_element(e, os.par.y, os.par.z, 2, 2, J[5], Jv[5]);
+        }
+        VertexSystem sys;
+        float hJ[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float Mk = (k == 0 || k == 3 || k == 5) ? Ug.w : 0.0f;
+            sys.A[k] = Mk - h * (Jv[k] + h * J[k]);
+            hJ[k] = h * J[k];
+        }
+        float wx, wy, wz;
+        matvec(hJ, Vg.x, Vg.y, Vg.z, wx, wy, wz);
+        sys.b[0] = h * (Fx + wx);
+        sys.b[1] = h * (Fy + wy);
+        sys.b[2] = h * (Fz + wz);
+        const CgInit c = cg_init(sys, a.x[0][g], a.x[1][g], a.x[2][g], pinned);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.A[k][g] = sys.A[k];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            a.x[k][g] = c.x[k];
+            a.r[k][g] = c.r[k];
+            a.d[k][g] = c.d[k];
+        }
+        acc_add(part, c.term);
+    }
+    finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
+}
+
+// 2: V += dV dt, u += dt V, ground clamp on the position (IMP:790-797).
+__global__ void __launch_bounds__(kAdjThreads) k_gm_update(const StepArgs a) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const float dt = a.dt;
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        float4 U = a.X[g], V = a.V[g];
+        V.x = V.x + a.x[0][g] * dt;
+        V.y = V.y + a.x[1][g] * dt;
+        V.z = V.z + a.x[2][g] * dt;
+        U.x = U.x + dt * V.x;
+        U.y = U.y + dt * V.y;
+        U.z = U.z + dt * V.z;
+        const float by = __ldg(a.Xbase + g).y;
+        if (by + U.y < 0.0f) U.y = -by;
+        a.X[g] = U;
+        a.V[g] = V;
     }
 }
 
@@ -338,6 +563,20 @@ cudaError_t launch_adjoint(int which, const StepArgs& a, const AdjArgs& j, int n
 }
 
 const void* adjoint_seed_fn() { return (const void*)k_adj_seed; }
+
+cudaError_t launch_gm(int which, const StepArgs& a, int n, cudaStream_t stream) {
+    const int64_t nv = (int64_t)n;  // the per-vertex kernels (0, 3, 4) take the vertex count
+    const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((nv + kAdjThreads - 1) / kAdjThreads, 152 * 8));
+    switch (which) {
+        case 0: k_gm_base<<<gs, kAdjThreads, 0, stream>>>(a, nv); break;
+        case 1: if (n > 0) k_gm_assemble<<<n, kAdjThreads, 0, stream>>>(a); break;
+        case 2: if (n > 0) k_gm_update<<<n, kAdjThreads, 0, stream>>>(a); break;
+        case 3: k_gm_leave<<<gs, kAdjThreads, 0, stream>>>(a, nv); break;
+        case 4: k_gm_consts<<<gs, kAdjThreads, 0, stream>>>(a, nv); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t launch_set_spring_params(const StepArgs& a, const AdjArgs& j, const float* ks, const float* kd,
                                      int64_t n_rec, int64_t nv, cudaStream_t stream) {

@@ -127,6 +127,14 @@ struct oc_solver {
         cudaGraphConditionalHandle handle = 0;
         float graph_dt = 0.0f;
         bool valid = false;
+        // Displacement mode (oc_set_tape_mode): the start positions, the springs' start
+        // constants and the final displacement of the last taped forward.
+        int32_t mode = OC_TAPE_POSITIONS;
+        bool gm_valid = false;
+        float4* Xbase = nullptr;
+        float2* gm_inc = nullptr;
+        float2* gm_own = nullptr;
+        float4* finU = nullptr;
     } tape;
     std::vector<cudaStream_t> aux;
     std::vector<cudaEvent_t> aux_done;
@@ -735,6 +743,36 @@ int32_t tape_buffer(const oc_solver::Tape& T, int32_t c) {
     const int32_t first_kept = T.n_ck - T.n_keep;
     if (c < first_kept) return -1;
     return (c - first_kept) + (T.n_keep < T.n_ck ? 1 : 0);
+}
+
+// The handle's arguments in the tape's displacement mode (X then holds u).
+StepArgs gm_args(const oc_solver* s, float dt) {
+    StepArgs a = s->args;
+    a.dt = dt;
+    a.blk_base = 0;
+    a.use_cond = 0;
+    a.all_streamed = 1;
+    a.gm = 1;
+    a.Xbase = s->tape.Xbase;
+    a.gm_inc = s->tape.gm_inc;
+    a.gm_own = s->tape.gm_own;
+    return a;
+}
+
+// One step in displacement mode: the assembly over every cloth, the CG of every cloth as
+// one cooperative launch without the update, then the displacement update.
+oc_status gm_step(oc_solver* s, float dt) {
+    const StepArgs a = gm_args(s, dt);
+    OC_TRY(cudaMemsetAsync(a.unconverged, 0, sizeof(int32_t), s->stream));
+    OC_TRY(launch_gm(1, a, s->n_blocks, s->stream));
+    OC_TRY(cudaMemsetAsync(s->d_bar, 0, sizeof(unsigned), s->stream));
+    StepArgs pa = a;
+    pa.cg_only = 1;
+    OC_TRY(launch_cg_persist(pa, s->d_adj_ids, s->n_inst, s->n_blocks, s->adj_persist_grid, s->d_bar, s->d_perr,
+                             s->stream));
+    OC_TRY(launch_gm(2, a, s->n_blocks, s->stream));
+    s->host_launches += 3;
+    return OC_OK;
 }
 
 // The adjoint solve of one step as a graph: reset the loop counter, set up the CG on
@@ -1878,6 +1916,13 @@ oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t check
     T.n_buf = n_buf;
     T.n_keep = n_keep;
     T.dt = dt;
+    const bool gm = T.mode == OC_TAPE_DISPLACEMENT;
+    T.gm_valid = false;
+    if (gm) {  // the start positions and spring constants; the state becomes u = 0
+        const StepArgs ga = gm_args(s, dt);
+        OC_TRY(launch_gm(0, ga, (int)s->nv, s->stream));
+        OC_TRY(launch_gm(4, ga, (int)s->nv, s->stream));
+    }
     const size_t nAx = 9 * s->stride;
     for (int32_t t = 0; t < n_steps; ++t) {
         const int32_t c = t / every, q = t - c * every;
@@ -1893,7 +1938,7 @@ oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t check
         float* sAx = T.segAx + (size_t)b * every * nAx;
         if (b >= 0 && q == 0)
             OC_TRY(launch_snapshot(s->args.X, s->args.V, sX, sV, nullptr, nullptr, s->nv, 0, s->stream));
-        oc_status st = oc_step(s, dt, 1);
+        oc_status st = gm ? gm_step(s, dt) : oc_step(s, dt, 1);
         if (st != OC_OK) return st;
         if (b >= 0) {
             const bool more = q + 1 < len;
@@ -1902,10 +1947,51 @@ oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t check
                                    s->nv, (int64_t)nAx, s->stream));
         }
     }
+    if (gm) {  // keep the final displacement, then the state goes back to positions
+        OC_TRY(cudaMemcpyAsync(T.finU, s->args.X, sizeof(float4) * (size_t)s->nv, cudaMemcpyDeviceToDevice, s->stream));
+        OC_TRY(launch_gm(3, gm_args(s, dt), (int)s->nv, s->stream));
+    }
     oc_status st = copy_state(s, T.finX, T.finV, T.finx, s->args.X, s->args.V, xplanes(s));
     if (st != OC_OK) return st;
     OC_TRY(cudaStreamSynchronize(s->stream));
+    if ((st = check_device_error(s)) != OC_OK) return st;
     T.valid = true;
+    T.gm_valid = gm;
+    return OC_OK;
+}
+
+oc_status oc_set_tape_mode(oc_solver* s, int32_t mode) {
+    if (!valid_solver(s) || (mode != OC_TAPE_POSITIONS && mode != OC_TAPE_DISPLACEMENT)) return OC_ERR_INVALID_ARGUMENT;
+    auto& T = s->tape;
+    if (mode == OC_TAPE_DISPLACEMENT) {
+        if (!s->adj_persist)
+            return fail(s, OC_ERR_UNSUPPORTED, "oc_set_tape_mode: the displacement mode runs every cloth's CG as one "
+                                               "cooperative launch (at most 16 cloths, no COUPLED cloth)");
+        OC_TRY(cudaSetDevice(s->device));
+        if (!T.Xbase) {
+            OC_TRY(dalloc(s, &T.Xbase, (size_t)s->nv));
+            OC_TRY(dalloc(s, &T.gm_inc, (size_t)s->n_inc));
+            OC_TRY(dalloc(s, &T.gm_own, (size_t)s->nv));
+            OC_TRY(dalloc(s, &T.finU, (size_t)s->nv));
+        }
+    }
+    T.mode = mode;
+    T.valid = false;
+    T.gm_valid = false;
+    return OC_OK;
+}
+
+oc_status oc_tape_displacement(oc_solver* s, float* u) {
+    if (!valid_solver(s) || !u) return OC_ERR_INVALID_ARGUMENT;
+    auto& T = s->tape;
+    if (!T.valid || !T.gm_valid)
+        return fail(s, OC_ERR_INVALID_ARGUMENT, "oc_tape_displacement: no displacement-mode tape");
+    OC_TRY(cudaSetDevice(s->device));
+    StepArgs dn = s->args;
+    dn.X = T.finU;
+    OC_TRY(launch_state_out(dn, s->stage, nullptr, nullptr, s->nv, s->stream));
+    OC_TRY(cudaMemcpyAsync(u, s->stage, 3 * (size_t)s->nv * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    OC_TRY(cudaStreamSynchronize(s->stream));
     return OC_OK;
 }
 
@@ -1943,16 +2029,17 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
         oc_status r = build_adjoint_graph(s, T.dt);
         if (r != OC_OK) return r;
     }
-    StepArgs a = s->args;
+    const bool gm = T.gm_valid;
+    StepArgs a = gm ? gm_args(s, T.dt) : s->args;
     a.dt = T.dt;
     a.blk_base = 0;
     a.use_cond = 0;
     a.all_streamed = 1;
     // A step's system A comes from the tape, where the recompute left it, unless a
     // resident cloth assembles in shared memory only (the fused resident kernel): then the
-    // CSR assembly rebuilds every cloth's A.
+    // CSR assembly rebuilds every cloth's A.  The displacement mode always tapes its A.
     const bool split_asm = !(s->resident_fused && !s->buckets.empty());
-    const bool taped_A = split_asm;
+    const bool taped_A = split_asm || gm;
     auto assemble = [&](const StepArgs& b) -> cudaError_t {
         cudaError_t e = cudaSuccess;
         if (!split_asm) return launch_kernel(K_ASSEMBLE, b, s->n_blocks, s->stream);
@@ -1988,7 +2075,7 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
             if (r != OC_OK) return r;
             OC_TRY(launch_snapshot(s->args.X, s->args.V, segX, segV, nullptr, nullptr, s->nv, 0, s->stream));
             for (int32_t q = 0; q < len; ++q) {
-                if ((r = oc_step(s, T.dt, 1)) != OC_OK) return r;
+                if ((r = gm ? gm_step(s, T.dt) : oc_step(s, T.dt, 1)) != OC_OK) return r;
                 const bool more = q + 1 < len;
                 OC_TRY(launch_snapshot(s->args.X, s->args.V, more ? segX + (size_t)(q + 1) * s->nv : nullptr,
                                        more ? segV + (size_t)(q + 1) * s->nv : nullptr, live_Ax, segAx + nAx * q,

@@ -139,6 +139,15 @@ struct StepArgs {
     float* term;
     const int32_t* strip_ids;
     int32_t n_strip_ids;
+    // Displacement mode of the adjoint tape (oc_set_tape_mode): X holds the displacement u
+    // from Xbase (the positions at the tape's start, mass in w); each spring's elongation is
+    // formed from its start constants {c0 = |d0| - rest, L0 = |d0|}, d0 the spring vector at
+    // the start, rounded from FP64: per incidence record (gm_inc) and for vertex i's own
+    // spring (gm_own).
+    int32_t gm;
+    const float4* Xbase;
+    const float2* gm_inc;
+    const float2* gm_own;
     // COUPLED per-incidence data is slot-major over slices of 32 consecutive vertices:
     // incidence e of vertex g sits at cpl_slice[g >> 5] + 32 e + (g & 31), so a warp's
     // accesses to one slot are contiguous.
@@ -168,6 +177,12 @@ struct AdjArgs {
 };
 
 cudaError_t launch_adjoint(int which, const StepArgs& a, const AdjArgs& j, int nblocks, cudaStream_t stream);
+// Displacement mode kernels (oc_adjoint.cu).  Per vertex (n = the vertex count):
+//   0 Xbase = X;  4 the spring constants gm_inc, gm_own from Xbase and X = (0, 0, 0, mass);
+//   3 X = Xbase + u.  Over the blocks a.blocks[blk_base, blk_base + n):
+//   1 assembly: forces, spring i's Jacobians, A, b and the CG set-up (incidence records);
+//   2 update: V += dt dV, u += dt V, ground clamp on Xbase.y + u.y.
+cudaError_t launch_gm(int which, const StepArgs& a, int n, cudaStream_t stream);
 // Tape snapshots: X, V into dX, dV (nv float4 each, skipped when dX is null) and nx floats
 // of x into dx (skipped when dx is null).
 cudaError_t launch_snapshot(const float4* X, const float4* V, float4* dX, float4* dV, const float* x, float* dx,

@@ -178,3 +178,55 @@ def test_torch_autograd_function(case):
         X2 = trajectory(s, case["X"], ks2, kd.detach(), v0.detach(), ext.detach(), DT, case["steps"], 10)
         loss2 = ((X2.double() - target) ** 2).sum(dim=1).mean()
         assert float(loss2.detach()) < float(loss.detach())
+
+
+def test_displacement_mode_tracks_the_positions_forward_and_its_gradients(case, cpu):
+    """The displacement-mode taped forward (start positions + FP32 displacement, precise
+    elongations): its final state agrees with the step's own forward (1e-5 of the motion)
+    and with the FP64 method at least as closely; its gradients agree with the FP64 CPU
+    adjoint within the positions mode's 1e-2, and the handle is left at the final
+    positions."""
+    desc = ClothDesc(n_vertices=len(case["X"]), springs=case["springs"], pinned=case["pins"], cg_max_iter=500,
+                     cg_tol=1e-6)
+    X0 = case["X"].astype(np.float64)
+    cl = oracle.Cloth(len(case["X"]), case["springs"], pinned=case["pins"], i_max=1000, eps=1e-10,
+                      ext_force=case["ext"])
+    X64, _, _, _, _ = oracle.port_step(cl, case["X"], case["V0"], n_steps=case["steps"], fp64=True, dot_fp64=True,
+                                       filter_pinned=True)
+    out = {}
+    for mode in (False, True):
+        with ClothSolver(desc) as s:
+            s.set_tape_mode(mode)
+            s.set_ext_force(case["ext"])
+            s.set_state(case["X"], case["V0"], np.zeros_like(case["X"]))
+            s.tape_forward(DT, case["steps"], 10)
+            Xp, _, _ = s.get_state()
+            XT = X0 + s.tape_displacement() if mode else Xp.astype(np.float64)
+            g = s.tape_backward(2.0 * (XT - case["target"]) / len(XT))
+            assert np.array_equal(s.get_state()[0], Xp)
+        out[mode] = (XT, g, Xp)
+    motion = np.abs(X64 - X0).max()
+    err_pos = np.abs(out[False][0] - X64).max() / motion
+    err_disp = np.abs(out[True][0] - X64).max() / motion
+    assert np.abs(out[True][0] - out[False][0]).max() / motion <= 1e-5
+    assert err_disp <= max(err_pos, 1e-7), (err_disp, err_pos)
+    assert np.abs(out[True][2] - out[True][0]).max() <= 1e-6  # the positions are start + u, rounded
+    for k_gpu, k_cpu in (("dKs", "gKs"), ("dKd", "gKd"), ("dV0", "gV0"), ("dext", "gExt")):
+        a = out[True][1][k_gpu].astype(np.float64).ravel()
+        b = cpu[k_cpu].ravel()
+        assert np.linalg.norm(a - b) <= 1e-2 * np.linalg.norm(b), k_gpu
+
+
+def test_displacement_mode_needs_a_cooperative_adjoint():
+    from opencloth_gb300 import OcError, grid_cloth
+
+    descs = []
+    for k in range(17):  # more cloths than one cooperative launch takes
+        X, sp = grid_cloth(5, 5, seed=k)
+        descs.append(ClothDesc(n_vertices=25, springs=sp, pinned=np.array([0, 4], np.int32)))
+    with ClothSolver(descs) as s:
+        with pytest.raises(OcError) as e:
+            s.set_tape_mode(True)
+        assert e.value.status == 7
+        with pytest.raises(OcError):
+            s.tape_displacement()
