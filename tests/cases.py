@@ -30,6 +30,14 @@ def rel(a, b) -> float:
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
 
 
+def rel_disp(a, b, x0) -> float:
+    """max |a - b| / max |b - x0|: the error relative to the motion from x0 (b the
+    reference), which a solver that did not move the cloth fails."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b - np.asarray(x0, np.float64)).max(), 1e-30))
+
+
 def desc_for(g: dict, **kw) -> ClothDesc:
     """Library description of a golden case; pins = the reference's {0, numX}."""
     return ClothDesc(n_vertices=g["cols"] * g["rows"], springs=g["springs"],

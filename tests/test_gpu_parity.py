@@ -1,28 +1,36 @@
 """GPU parity: the sm_103a step against the oracle and the reference's own outputs.
 
-Tolerances (stated here, used below):
+Tolerances (stated here, used below).  "Relative" is the max-norm error over the
+max-norm of the reference; "of the motion" is the max-norm error over the largest
+displacement of the reference from the initial state, which a solver that did not move
+the cloth fails.
 * ComputeForces, the Jacobians and the assembly of A and b are FP32 with the
   reference's operation order and no FMA contraction: bit-exact against the port.
 * The step differs from the FP32 reference only through the CG dot products, which
-  accumulate in FP64: X within 1e-6 and V within 1e-5 relative (max-norm) of the
-  reference after 1 step, and X within 1e-5 / V within 1e-4 after 600 steps.
+  accumulate in FP64: X within 1e-6 and V within 1e-5 relative after 1 step, X within
+  1e-5 / V within 1e-4 after the last snapshot (600 steps at most); X within 1e-5 of the
+  motion after 1 step and 1e-4 of the motion after the last snapshot.
 * Against the port run with the GPU's arithmetic (FP64 dots, pinned filter) only the
-  FP64 summation order differs: 1e-6 relative.
-* Against the FP64 build of the reference: X within 1e-4 relative after 600 steps.
+  FP64 summation order differs: 1e-6 relative, 1e-4 of the motion.
+* Against the FP64 build of the reference: X within 1e-4 relative after 600 steps.  Of
+  the motion, the FP32 method itself is 6.1e-4 from FP64 after 600 steps of the 21 x 21
+  cloth (the restatement in FP32 measures the same), so the bound there is 2e-3.
 """
 import numpy as np
 import pytest
 
 import oracle
-from cases import GOLDEN_CASES, desc_for, golden, oracle_for, rel, seeded_cloth
-from opencloth_gb300 import FLAG_BREAKDOWN, FLAG_NON_FINITE, ClothDesc, ClothSolver
+from cases import GOLDEN_CASES, desc_for, golden, oracle_for, rel, rel_disp, seeded_cloth
+from opencloth_gb300 import FLAG_BREAKDOWN, FLAG_NON_FINITE, ClothSolver
 
 pytestmark = pytest.mark.gpu
 
 TOL_X_1, TOL_V_1 = 1e-6, 1e-5
 TOL_X_600, TOL_V_600 = 1e-5, 1e-4
+TOL_MOTION_1, TOL_MOTION_600 = 1e-5, 1e-4
 TOL_PORT = 1e-6
 TOL_FP64_X = 1e-4
+TOL_FP64_MOTION = 2e-3
 DT = 1.0 / 60.0
 
 
@@ -60,9 +68,10 @@ def test_step_matches_reference_golden(name):
             s.step(g["dt"], int(n) - done)
             done = int(n)
             X, V, _ = s.get_state()
-            tx, tv = (TOL_X_1, TOL_V_1) if n == 1 else (TOL_X_600, TOL_V_600)
+            tx, tv, tm = (TOL_X_1, TOL_V_1, TOL_MOTION_1) if n == 1 else (TOL_X_600, TOL_V_600, TOL_MOTION_600)
             assert rel(X, g[f"X32_{n}"]) <= tx, (name, n, rel(X, g[f"X32_{n}"]))
             assert rel(V, g[f"V32_{n}"]) <= tv, (name, n, rel(V, g[f"V32_{n}"]))
+            assert rel_disp(X, g[f"X32_{n}"], g["X0"]) <= tm, (name, n, rel_disp(X, g[f"X32_{n}"], g["X0"]))
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
@@ -75,6 +84,7 @@ def test_step_matches_port_with_gpu_arithmetic(name):
     Xo, Vo, dVo, _, _ = oracle.port_step(oracle_for(g, explicit_pins=True), g["X0"], g["V0"], g["dV0"], dt=g["dt"],
                                          n_steps=n, dot_fp64=True, filter_pinned=True)
     assert rel(X, Xo) <= TOL_PORT and rel(V, Vo) <= TOL_PORT and rel(dV, dVo) <= 10 * TOL_PORT
+    assert rel_disp(X, Xo, g["X0"]) <= TOL_MOTION_600, rel_disp(X, Xo, g["X0"])
 
 
 def test_one_step_bit_exact_against_port():
@@ -93,6 +103,7 @@ def test_error_against_fp64_reference():
         s.step(g["dt"], 600)
         X, V, _ = s.get_state()
     assert rel(X, g["X64_600"]) <= TOL_FP64_X
+    assert rel_disp(X, g["X64_600"], g["X0"]) <= TOL_FP64_MOTION
 
 
 @pytest.mark.parametrize("executor,graph", [("streamed", True), ("streamed", False), ("plain", False),
@@ -197,27 +208,3 @@ def test_indefinite_system_is_flagged():
         s.step(1.0, 1)
         it, _, fl = s.stats()
     assert fl[0] & (FLAG_BREAKDOWN | FLAG_NON_FINITE) or it[0] < 50
-
-
-def test_config2_settings_600_steps_against_fp64():
-    """The 1M-vertex configuration's settings on a 257 x 257 cloth (Ks 50.75/50.75/50.95,
-    Kd -0.25, dt 1/60, N(0, (1e-3 spacing)^2) jitter, CG up to 200 iterations to 1e-5),
-    600 steps: X within TOL_FP64_X of the FP64 method (the restatement in FP64 with FP64
-    dots and the pin filter): positions within 1e-4 relative after 600 steps.  The full 1025 x 1025 cloth
-    takes hours in FP64 on the host; the per-vertex arithmetic is the same."""
-    from opencloth_gb300 import grid_cloth
-
-    n = 257
-    X, sp = grid_cloth(n, n, ks=(50.75, 50.75, 50.95), kd=(-0.25, -0.25, -0.25), jitter=1e-3, seed=20261203)
-    pins = np.array([0, n - 1], np.int32)
-    V = np.zeros_like(X)
-    desc = ClothDesc(n_vertices=n * n, springs=sp, pinned=pins, cg_max_iter=200, cg_tol=1e-5)
-    with ClothSolver(desc) as s:
-        s.set_state(X, V, np.zeros_like(X))
-        s.step(DT, 600)
-        Xg, _, _ = s.get_state()
-        it, _, fl = s.stats()
-    assert fl[0] == 0
-    cl = oracle.Cloth(n * n, sp, pinned=pins, i_max=200, eps=1e-5)
-    X64, _, _, _, _ = oracle.port_step(cl, X, V, dt=DT, n_steps=600, fp64=True, dot_fp64=True, filter_pinned=True)
-    assert rel(Xg, X64) <= TOL_FP64_X
