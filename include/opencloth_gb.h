@@ -242,9 +242,9 @@ oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* t
  * start constants rounded from FP64, so that a cloth that moves little keeps the digits
  * of its motion (an FP32 position near 5 resolves about 5e-7; a gradient of a loss whose
  * residual is a few 1e-6 needs about 1e-9).  The displacement forward otherwise follows
- * the step's arithmetic; it needs the handle to run its adjoint solves as one cooperative
- * launch (at most 16 cloths, no COUPLED cloth; OC_ERR_UNSUPPORTED otherwise).  Setting the
- * mode invalidates the tape. */
+ * the step's arithmetic; it needs the handle to run its adjoint solves through the
+ * cooperative CG (no COUPLED cloth, a device with cooperative launch, persistence not
+ * switched off; OC_ERR_UNSUPPORTED otherwise).  Setting the mode invalidates the tape. */
 #define OC_TAPE_POSITIONS 0
 #define OC_TAPE_DISPLACEMENT 1
 oc_status oc_set_tape_mode(oc_solver* s, int32_t mode);
@@ -307,16 +307,17 @@ oc_status oc_tune_key_of(const oc_solver* s, char* key, int32_t key_size);
 oc_status oc_tune_cache_lookup(const char* path, const char* key, oc_launch_config* cfg, int32_t* found);
 oc_status oc_tune_cache_store(const char* path, const char* key, const oc_launch_config* cfg, double ms_per_step);
 
-/* ---- testing aid: the bounded grid-barrier wait ---------------------------------- */
-/* The persistent CG (one cooperative launch per step, used for up to 16 streamed cloths
- * and for the adjoint solves of up to 16 cloths) waits at grid barriers; each wait gives
- * up after a bounded number of polls and the step then fails with OC_ERR_DEVICE_TIMEOUT
- * at the next oc_synchronize / oc_get_state / oc_get_stats, after which the handle steps
- * on (the step whose wait gave up applied no update).  For tests of that path: from the
- * next step on, block `withhold_block` of those launches returns at its first barrier
- * without arriving (-1: none), and a wait gives up after `max_polls` polls (0: the
- * default, about half a second).  Nothing waits longer than that bound.  Fails with
- * OC_ERR_UNSUPPORTED when the handle runs no persistent CG. */
+/* ---- testing aid: the bounded waits of the persistent CG -------------------------- */
+/* The persistent CG (one cooperative launch per step for the streamed cloths, and for
+ * the adjoint solves) waits, before each pass over a cloth's vertices, for that cloth's
+ * previous pass to complete on every block; each wait gives up after a bounded number of
+ * polls and the step then fails with OC_ERR_DEVICE_TIMEOUT at the next oc_synchronize /
+ * oc_get_state / oc_get_stats, after which the handle steps on (a cloth whose solve had
+ * not ended got no update).  For tests of that path: from the next step on, block
+ * `withhold_block` of those launches returns before its first arrival (-1: none), and a
+ * wait gives up after `max_polls` polls (0: the default, about half a second).  Nothing
+ * waits longer than that bound.  Fails with OC_ERR_UNSUPPORTED when the handle runs no
+ * persistent CG. */
 oc_status oc_test_barrier_timeout(oc_solver* s, int32_t withhold_block, uint32_t max_polls);
 
 /* ---- allocation-free solve -------------------------------------------------------- */

@@ -88,17 +88,14 @@ struct oc_solver {
     int32_t n_upd_blocks = 0;
     bool any_coupled = false;
     // The CG loop of the streamed REFERENCE cloths as one cooperative launch (k_cg_persist)
-    // when there are few of them and no COUPLED cloth; otherwise the WHILE loop.
+    // when there is no COUPLED cloth; otherwise the WHILE loop.
     bool persist = false;
-    int32_t* d_persist_ids = nullptr;
-    int32_t n_persist = 0;
     int persist_grid = 0;
-    unsigned* d_bar = nullptr;  // grid barrier: arrivals [0], generation [32], totals [64]
-    int* d_perr = nullptr;      // bit 0: a grid barrier gave up
+    unsigned* d_words = nullptr;  // k_cg_persist: one completion word per cloth
+    int* d_perr = nullptr;        // bit 0: a wait of k_cg_persist gave up
     // The adjoint solve (every cloth iterates) as one cooperative launch of k_cg_persist
-    // without the update, when the handle has few enough cloths.
+    // without the update, when the handle has no COUPLED cloth.
     bool adj_persist = false;
-    int32_t* d_adj_ids = nullptr;
     int adj_persist_grid = 0;
     bool any_provot = false;  // some cloth has OC_PASS_PROVOT: k_provot follows the update
     bool any_passes = false;  // some cloth has a pass after the update
@@ -171,24 +168,34 @@ oc_status fail_cuda(oc_solver* s, cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return fail_cuda(s, e_, #call); \
     } while (0)
 
-// Polls of a grid barrier's generation word before k_cg_persist gives up (about half a
-// second with its 32 ns back-off).
+// Polls of a cloth's completion word before a wait of k_cg_persist gives up (about half
+// a second with its 32 ns back-off).
 constexpr uint32_t kDefaultBarrierPolls = 1u << 22;
 
-// A grid barrier of k_cg_persist that gave up (the stream is synchronised).  The error
-// word is cleared once reported; the next launch starts from a reset arrival word, so
-// the handle steps on.
+// A wait of k_cg_persist that gave up (the stream is synchronised).  The error word is
+// cleared once reported and the cloths' CG state (whose tickets the abandoned launch
+// left part-counted) is zeroed: every step's assembly sets it up again, and the next
+// launch starts from zeroed completion words, so the handle steps on.
 oc_status check_device_error(oc_solver* s) {
     if (!s->d_perr) return OC_OK;
     int h = 0;
     OC_TRY(cudaMemcpy(&h, s->d_perr, sizeof(int), cudaMemcpyDeviceToHost));
     if (h != 0) {
         OC_TRY(cudaMemset(s->d_perr, 0, sizeof(int)));
+        OC_TRY(cudaMemset(s->args.state, 0, sizeof(InstState) * (size_t)s->n_inst));
         return fail(s, OC_ERR_DEVICE_TIMEOUT,
-                    "k_cg_persist: a grid barrier gave up (that step's update was not applied)");
+                    "k_cg_persist: a wait gave up (cloths whose solve had not ended were not updated)");
     }
     return OC_OK;
 }
+
+// k_cg_persist over block table a.blocks[0, n): its cloths' completion words zeroed, then
+// the cooperative launch.
+cudaError_t persist_cg(oc_solver* s, const StepArgs& a, int32_t n, int grid) {
+    cudaError_t e = cudaMemsetAsync(s->d_words, 0, sizeof(unsigned) * (size_t)s->n_inst, s->stream);
+    return e == cudaSuccess ? launch_cg_persist(a, n, grid, s->d_words, s->d_perr, s->stream) : e;
+}
+
 
 // Whether a grid cloth that may take the strip sweep should: its warps own 28 columns
 // each, so narrow cloths leave lanes idle.  With cfg.strip = 0 every grid cloth stays on
@@ -209,6 +216,16 @@ cudaError_t dalloc(oc_solver* s, T** p, size_t count) {
     if (e == cudaSuccess) s->allocs.push_back(q);
     *p = static_cast<T*>(q);
     return e;
+}
+
+// The persistent CG's words (once per handle).
+oc_status alloc_persist_words(oc_solver* s) {
+    if (s->d_words) return OC_OK;
+    OC_TRY(dalloc(s, &s->d_words, (size_t)s->n_inst));
+    OC_TRY(cudaMemset(s->d_words, 0, sizeof(unsigned) * (size_t)s->n_inst));
+    OC_TRY(dalloc(s, &s->d_perr, 1));
+    OC_TRY(cudaMemset(s->d_perr, 0, sizeof(int)));
+    return OC_OK;
 }
 
 template <class T>
@@ -353,6 +370,8 @@ oc_status launch_timed(oc_solver* s, KernelKind k, const StepArgs& a, int nblock
     return OC_OK;
 }
 
+// The resident cloths' launches (one per bucket).  With a.cg_only they run unfused: the
+// adjoint solve of each resident cloth on chip.
 oc_status launch_resident_all(oc_solver* s, const StepArgs& a, KernelTimer* t) {
     if (!t && !s->aux.empty()) {
         // Fork: every bucket on its own stream, joined back into the handle's stream.
@@ -360,7 +379,7 @@ oc_status launch_resident_all(oc_solver* s, const StepArgs& a, KernelTimer* t) {
         for (size_t i = 0; i < s->aux.size(); ++i) OC_TRY(cudaStreamWaitEvent(s->aux[i], s->fork_ev, 0));
         for (size_t i = 0; i < s->buckets.size(); ++i) {
             const auto& b = s->buckets[i];
-            ResidentLaunch L{b.d_ids, b.cluster, b.vcta, s->resident_fused ? 1 : 0};
+            ResidentLaunch L{b.d_ids, b.cluster, b.vcta, (s->resident_fused && !a.cg_only) ? 1 : 0};
             OC_TRY(launch_resident(a, L, b.threads, b.n, s->aux[i % s->aux.size()]));
             s->host_launches += 1;
         }
@@ -372,7 +391,7 @@ oc_status launch_resident_all(oc_solver* s, const StepArgs& a, KernelTimer* t) {
     }
     for (const auto& b : s->buckets) {
         if (t) OC_TRY(cudaEventRecord(t->ev[0], s->stream));
-        ResidentLaunch L{b.d_ids, b.cluster, b.vcta, s->resident_fused ? 1 : 0};
+        ResidentLaunch L{b.d_ids, b.cluster, b.vcta, (s->resident_fused && !a.cg_only) ? 1 : 0};
         OC_TRY(launch_resident(a, L, b.threads, b.n, s->stream));
         s->host_launches += 1;
         if (t) {
@@ -460,9 +479,7 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
         const int nb = s->n_streamed_blocks, nc = s->n_cpl_blocks;
         if (s->persist) {
             if (t) OC_TRY(cudaEventRecord(t->ev[0], s->stream));
-            OC_TRY(cudaMemsetAsync(s->d_bar, 0, sizeof(unsigned), s->stream));
-            OC_TRY(launch_cg_persist(sa, s->d_persist_ids, s->n_persist, nb, s->persist_grid, s->d_bar, s->d_perr,
-                                     s->stream));
+            OC_TRY(persist_cg(s, sa, nb, s->persist_grid));
             s->host_launches += 1;
             if (t) {
                 OC_TRY(cudaEventRecord(t->ev[1], s->stream));
@@ -629,30 +646,21 @@ oc_status build_graph(oc_solver* s, float dt) {
         updates.push_back(n_int);
     }
     if (persist) {
-        // The streamed cloths' whole CG loop and update: a cooperative launch captured
-        // into a child graph after a memset of the barrier counter.
-        cudaGraphNode_t n_bar, n_pc;
-        cudaMemsetParams bp{};
-        bp.dst = s->d_bar;
-        bp.value = 0;
-        bp.elementSize = sizeof(unsigned);
-        bp.width = 1;
-        bp.height = 1;
-        bp.pitch = sizeof(unsigned);
-        OC_TRY(cudaGraphAddMemsetNode(&n_bar, g, &n_last, 1, &bp));
+        // The streamed cloths' whole CG loop and update: the memset of their completion
+        // words and the cooperative launch, captured into a child graph.
+        cudaGraphNode_t n_pc;
         cudaGraph_t pg = nullptr;
         OC_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
         StepArgs pa = sa;
         pa.blocks = s->d_streamed_blocks;
         pa.use_cond = 0;
-        cudaError_t le = launch_cg_persist(pa, s->d_persist_ids, s->n_persist, s->n_streamed_blocks, s->persist_grid,
-                                           s->d_bar, s->d_perr, s->stream);
+        cudaError_t le = persist_cg(s, pa, s->n_streamed_blocks, s->persist_grid);
         cudaError_t ce = cudaStreamEndCapture(s->stream, &pg);
         if (le != cudaSuccess || ce != cudaSuccess) {
             if (pg) cudaGraphDestroy(pg);
             return fail_cuda(s, le != cudaSuccess ? le : ce, "capture of k_cg_persist");
         }
-        cudaError_t e = cudaGraphAddChildGraphNode(&n_pc, g, &n_bar, 1, pg);
+        cudaError_t e = cudaGraphAddChildGraphNode(&n_pc, g, &n_last, 1, pg);
         cudaGraphDestroy(pg);
         if (e != cudaSuccess) return fail_cuda(s, e, "cudaGraphAddChildGraphNode");
         updates.push_back(n_pc);
@@ -759,19 +767,38 @@ StepArgs gm_args(const oc_solver* s, float dt) {
     return a;
 }
 
-// One step in displacement mode: the assembly over every cloth, the CG of every cloth as
-// one cooperative launch without the update, then the displacement update.
+// The CG alone (no update) of every cloth, from the CG state set up in the planes and
+// the cloths' states: the resident cloths on chip (k_resident unfused, one launch per
+// bucket, beside) and the streamed ones in one cooperative launch of k_cg_persist over
+// the streamed block table.  A handle whose plan has no resident bucket runs every cloth
+// in k_cg_persist.
+oc_status solve_only(oc_solver* s, const StepArgs& a) {
+    StepArgs pa = a;
+    pa.cg_only = 1;
+    if (s->buckets.empty()) {
+        OC_TRY(persist_cg(s, pa, s->n_blocks, s->adj_persist_grid));
+        s->host_launches += 1;
+        return OC_OK;
+    }
+    if (oc_status r = launch_resident_all(s, pa, nullptr)) return r;
+    if (s->n_streamed_blocks > 0) {
+        pa.blocks = s->d_streamed_blocks;
+        const int grid = std::min(s->persist_per_sm * s->sm_count, std::max(1, s->n_streamed_blocks));
+        OC_TRY(persist_cg(s, pa, s->n_streamed_blocks, grid));
+        s->host_launches += 1;
+    }
+    return OC_OK;
+}
+
+// One step in displacement mode: the assembly over every cloth, the CG of every cloth
+// without the update, then the displacement update.
 oc_status gm_step(oc_solver* s, float dt) {
     const StepArgs a = gm_args(s, dt);
     OC_TRY(cudaMemsetAsync(a.unconverged, 0, sizeof(int32_t), s->stream));
     OC_TRY(launch_gm(1, a, s->n_blocks, s->stream));
-    OC_TRY(cudaMemsetAsync(s->d_bar, 0, sizeof(unsigned), s->stream));
-    StepArgs pa = a;
-    pa.cg_only = 1;
-    OC_TRY(launch_cg_persist(pa, s->d_adj_ids, s->n_inst, s->n_blocks, s->adj_persist_grid, s->d_bar, s->d_perr,
-                             s->stream));
+    if (oc_status r = solve_only(s, a)) return r;
     OC_TRY(launch_gm(2, a, s->n_blocks, s->stream));
-    s->host_launches += 3;
+    s->host_launches += 2;
     return OC_OK;
 }
 
@@ -998,28 +1025,20 @@ oc_status plan_execution(oc_solver* s) {
             s->aux_done.push_back(e);
         }
     }
-    // Persistent CG for the streamed REFERENCE cloths: few of them, no COUPLED cloth, a
-    // cooperative launch fits, and the configuration allows it.
-    std::vector<int32_t> ids;
-    bool any_coupled = false;
+    // Persistent CG for the streamed REFERENCE cloths, any number of them: no COUPLED
+    // cloth, a cooperative launch fits, and the configuration allows it.
+    bool any_streamed = false, any_coupled = false;
     for (int32_t k = 0; k < s->n_inst; ++k) {
         any_coupled |= s->inst_host[(size_t)k].coupled != 0;
-        if (!s->resident[(size_t)k] && !s->inst_host[(size_t)k].coupled) ids.push_back(k);
+        any_streamed |= !s->resident[(size_t)k] && !s->inst_host[(size_t)k].coupled;
     }
     s->persist = false;
-    if (cfg.persist && s->coop && s->persist_per_sm > 0 && !ids.empty() &&
-        (int)ids.size() <= persist_max_instances() && !any_coupled) {
+    const int pgrid = std::min(s->persist_per_sm * s->sm_count, std::max(1, s->n_streamed_blocks));
+    if (cfg.persist && s->coop && s->persist_per_sm > 0 && any_streamed && !any_coupled &&
+        (int64_t)s->n_streamed_blocks <= (int64_t)persist_max_entries_per_block() * pgrid) {
         s->persist = true;
-        s->n_persist = (int32_t)ids.size();
-        s->persist_grid = std::min(s->persist_per_sm * s->sm_count, std::max(1, s->n_streamed_blocks));
-        OC_TRY(reupload(s, &s->d_persist_ids, ids));
-        if (!s->d_bar) {
-            // arrival word at [0], generation at [32], the cloths' totals (16 doubles) at [64]
-            OC_TRY(dalloc(s, &s->d_bar, 128));
-            OC_TRY(cudaMemset(s->d_bar, 0, 128 * sizeof(unsigned)));
-            OC_TRY(dalloc(s, &s->d_perr, 1));
-            OC_TRY(cudaMemset(s->d_perr, 0, sizeof(int)));
-        }
+        s->persist_grid = pgrid;
+        if (oc_status r = alloc_persist_words(s)) return r;
     }
     drop_graphs(s);
     return OC_OK;
@@ -1399,20 +1418,14 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
         const int per_sm = allowed ? s->persist_per_sm : 0;
         const int n_sm = s->sm_count;
         const int coop = s->coop ? 1 : 0;
-        // The adjoint solve runs every cloth's CG: one cooperative launch without the
-        // update when the handle holds at most persist_max_instances() cloths.
-        if (allowed && coop && per_sm > 0 && P.n_inst <= persist_max_instances() && !P.any_coupled) {
+        // The adjoint solve runs every cloth's CG over the full block table: one
+        // cooperative launch without the update, any number of cloths.
+        const int adj_grid = std::min(per_sm * n_sm, std::max(1, s->n_blocks));
+        if (allowed && coop && per_sm > 0 && !P.any_coupled &&
+            (int64_t)s->n_blocks <= (int64_t)persist_max_entries_per_block() * adj_grid) {
             s->adj_persist = true;
-            std::vector<int32_t> all((size_t)P.n_inst);
-            for (int32_t k = 0; k < P.n_inst; ++k) all[(size_t)k] = k;
-            OC_CREATE_TRY(upload(s, &s->d_adj_ids, all));
-            s->adj_persist_grid = std::min(per_sm * n_sm, std::max(1, s->n_blocks));
-            if (!s->d_bar) {
-                OC_CREATE_TRY(dalloc(s, &s->d_bar, 128));
-                OC_CREATE_TRY(cudaMemset(s->d_bar, 0, 128 * sizeof(unsigned)));
-                OC_CREATE_TRY(dalloc(s, &s->d_perr, 1));
-                OC_CREATE_TRY(cudaMemset(s->d_perr, 0, sizeof(int)));
-            }
+            s->adj_persist_grid = adj_grid;
+            if (oc_status r = alloc_persist_words(s)) return bail(r);
         }
     }
     OC_CREATE_TRY(dalloc(s, &a.unconverged, 1));
@@ -1965,8 +1978,8 @@ oc_status oc_set_tape_mode(oc_solver* s, int32_t mode) {
     auto& T = s->tape;
     if (mode == OC_TAPE_DISPLACEMENT) {
         if (!s->adj_persist)
-            return fail(s, OC_ERR_UNSUPPORTED, "oc_set_tape_mode: the displacement mode runs every cloth's CG as one "
-                                               "cooperative launch (at most 16 cloths, no COUPLED cloth)");
+            return fail(s, OC_ERR_UNSUPPORTED, "oc_set_tape_mode: the displacement mode runs every cloth's CG through "
+                                               "the cooperative CG (no COUPLED cloth, cooperative launch available)");
         OC_TRY(cudaSetDevice(s->device));
         if (!T.Xbase) {
             OC_TRY(dalloc(s, &T.Xbase, (size_t)s->nv));
@@ -2096,13 +2109,9 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
                 for (int k = 0; k < 6; ++k) b.A[k] = slot + k * st;  // read in place
             else  // the WHILE graph's nodes read the handle's A planes
                 OC_TRY(cudaMemcpyAsync(live_Ax, slot, 6 * st * sizeof(float), cudaMemcpyDeviceToDevice, s->stream));
-            if (s->adj_persist) {  // lambda = A^-1 g_dV: seed, then one cooperative launch
+            if (s->adj_persist) {  // lambda = A^-1 g_dV: seed, then the CG alone
                 OC_TRY(launch_adjoint(0, b, jj, s->n_blocks, s->stream));
-                OC_TRY(cudaMemsetAsync(s->d_bar, 0, sizeof(unsigned), s->stream));
-                StepArgs pa = b;
-                pa.cg_only = 1;
-                OC_TRY(launch_cg_persist(pa, s->d_adj_ids, s->n_inst, s->n_blocks, s->adj_persist_grid, s->d_bar,
-                                         s->d_perr, s->stream));
+                if (oc_status r2 = solve_only(s, b)) return r2;
             } else {  // the WHILE-loop graph, its seed node pointed at this step
                 StepArgs bs = b;
                 bs.use_cond = 1;

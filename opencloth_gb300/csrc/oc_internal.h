@@ -104,7 +104,7 @@ struct StepArgs {
     unsigned long long cond; // cudaGraphConditionalHandle
     int32_t all_streamed;    // 1: every cloth's CG runs in the streamed loop (adjoint solves)
     int32_t cg_only;         // k_cg_persist: 1 = the CG alone, no update (adjoint solves)
-    // k_cg_persist's grid barrier: polls of the generation word before a wait gives up,
+    // k_cg_persist's waits: polls of a cloth's completion word before a wait gives up,
     // and a block that never arrives (-1: none; set only by oc_test_barrier_timeout).
     uint32_t barrier_polls;
     int32_t withhold_block;
@@ -206,14 +206,15 @@ enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3
                   K_ASSEMBLE_GRID = 11, K_CG_PERSIST = 12, K_ASSEMBLE_STRIP = 13, K_ASSEMBLE_REDUCE = 14,
                   K_ASSEMBLE_FINISH = 15, K_COUNT = 16 };
 
-// The whole CG loop of a few large streamed cloths in one cooperative launch
-// (oc_kernels.cu): block table a.blocks[0, n_entries), cloths inst_ids[0, n_inst);
-// bar: the arrival counter (zeroed before each launch) and, 128 bytes on, the generation;
-// err: bit 0 set if a grid barrier gave up.
-int persist_max_instances();
+// The whole CG loop of the cloths of block table a.blocks[0, n_entries) in one
+// cooperative launch of `grid` blocks (oc_kernels.cu), any number of cloths; a block
+// owns at most persist_max_entries_per_block() entries.  words: one completion word per
+// cloth of the handle, indexed by cloth, zeroed before each launch; the cloths' tickets
+// start at zero (the assembly epilogue leaves them so).  err: bit 0 set if a wait gave up.
+int persist_max_entries_per_block();
 int persist_blocks_per_sm();
-cudaError_t launch_cg_persist(const StepArgs& a, const int32_t* inst_ids, int32_t n_inst, int32_t n_entries,
-                              int grid, unsigned* bar, int* err, cudaStream_t stream);
+cudaError_t launch_cg_persist(const StepArgs& a, int32_t n_entries, int grid, unsigned* words, int* err,
+                              cudaStream_t stream);
 
 // Interaction kernels (oc_interact.cu).
 cudaError_t launch_pick(const float4* X, int64_t v0, int64_t nv, const float pt[3], double radius, int32_t* out,

@@ -8,8 +8,8 @@
 //   k_assemble_grid  the same for grid cloths, with the neighbours from a stencil
 //   k_cg_dir     [d = r + beta d]; alpha = delta_new / d.(A d)    (IMP:320-321, 327)
 //   k_cg_update  x += alpha d; r -= alpha A d; delta_new = r.r     (IMP:322-326)
-//   k_cg_persist the CG loop of up to 16 cloths and their update in one cooperative
-//                launch (the two passes above, grid barriers between them)
+//   k_cg_persist the CG loop of any number of cloths and their update in one
+//                cooperative launch (the two passes above, per-cloth completion words)
 //   k_integrate  V += dV dt; X += dt V; ground clamp               (IMP:790-797)
 //                [+ EllipsoidCollision, IMP:824-848]
 //   k_provot     ApplyProvotDynamicInverse as a per-vertex gather   (IMP:800-823)
@@ -632,24 +632,41 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
 }
 
 // ---- the whole CG loop in one cooperative launch ----------------------------------------
-// For a few large streamed cloths the loop's cost is the kernel boundaries, not the
-// bytes: each (k_cg_dir, k_cg_update) launch pays a launch, a tail and a serial
-// epilogue of about 12 us even on a small cloth.  k_cg_persist runs every iteration of
-// every streamed cloth in one launch, all its blocks co-resident (cooperative launch),
-// with two grid barriers per iteration.  Each block walks the streamed block table with
-// a stride of the grid and runs the same per-block passes as k_cg_dir / k_cg_update,
-// writing the same per-block partials.  The last block to reach a barrier sums each
-// cloth's partials with the same fixed-order sum the last-block epilogue uses and
-// publishes the totals before it releases the others; every block then applies the
-// same scalar rules to the same totals, so all blocks hold identical copies of the
-// scalars and the results are those of the two-kernel loop bit for bit.  The update is
-// fused at the end (it is per vertex).
+// For streamed cloths the loop's cost is the kernel boundaries, not the bytes: each
+// (k_cg_dir, k_cg_update) launch pays a launch, a tail and a serial epilogue of about
+// 12 us even on a small cloth.  k_cg_persist runs every iteration of every cloth of its
+// block table in one launch, all its blocks co-resident (cooperative launch).  Block b
+// owns the table entries b, b + grid, b + 2 grid, ... and runs on them the same
+// per-block passes as k_cg_dir / k_cg_update, writing the same per-block partials.
+//
+// The cloths are independent, so there is no grid barrier: each cloth has its own
+// completion word.  Phase q of a cloth is the direction pass (q even) or the update pass
+// (q odd) of iteration q / 2.  An entry's pass of phase q starts once its cloth's word
+// reads at least q (phase q - 1 complete).  Every entry then arrives at its cloth's
+// ticket; the block that makes the cloth's last arrival of the phase sums the cloth's
+// partials in the last-block epilogue's fixed order, applies the epilogue's scalar rule
+// to the cloth's state and publishes the word (q + 1, or kPhaseDone when the cloth's
+// loop has ended).  Totals, scalars and decisions are those of the two-kernel loop bit
+// for bit.  Progress: a pass of phase q waits only on phase q - 1 of its own cloths,
+// whose arrivals every block makes before any of its phase-q work, so by induction on q
+// every phase completes.  A wait gives up after a.barrier_polls polls (the default,
+// 2^22 polls with a 32 ns back-off, is about half a second) or when another block has
+// given up: it sets bit 0 of *err and the block returns without its update.  The block
+// a.withhold_block (a testing aid; normally -1) returns before its first arrival, so
+// the waits on its cloths run out.
 
-constexpr int kPersistMaxInst = 16;       // streamed cloths one launch handles
+constexpr int kPersistMaxOwn = kThreads;  // table entries one block owns (one waiting thread each)
+constexpr unsigned kPhaseDone = 0xffffffffu;
 
 __device__ __forceinline__ unsigned load_acquire(const unsigned* p) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ int load_relaxed(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
 
@@ -659,177 +676,129 @@ __device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned x) {
     return v;
 }
 
-__device__ __forceinline__ void red_add_release(unsigned* p, unsigned x) {
-    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(x) : "memory");
+__device__ __forceinline__ void store_release(unsigned* p, unsigned x) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(x) : "memory");
 }
 
-// A cloth's total over its blocks' partials: the last-block epilogue's order (finish).
-__device__ double instance_total(const StepArgs& a, const InstParams& ip) {
-    __shared__ double s_tot;
-    double acc = 0.0;
-#pragma unroll 8
-    for (int j = threadIdx.x; j < ip.nblk; j += blockDim.x) acc += __ldcg(a.partials + ip.blk0 + j);
-    const double total = block_sum(acc);
-    if (threadIdx.x == 0) s_tot = total;
-    __syncthreads();
-    const double t = s_tot;
-    __syncthreads();
-    return t;
-}
-
-struct PersistScalars {
-    double delta_new, delta0, dq;
-    float alpha, beta;
-    int32_t iter, active;
-    uint32_t flags;
-};
-
-// Grid barrier that also forms the cloths' totals, bounded.  bar[0] is the arrival word:
-// block 0 adds 2^31 - (n - 1), every other block 1, so the n-th arrival, whichever it
-// is, flips bit 31 and the low bits are back where they started (no reset).  That last
-// block sums the partials of every active cloth into totals[] and then bumps the
-// generation bar[32] with a release; the others poll the generation with acquire loads
-// and read the totals into tot[] (shared).  A wait gives up after a.barrier_polls polls
-// (the default, 2^22 polls with a 32 ns back-off, is about half a second): it sets bit 0
-// of *err and returns false, the kernel unwinds and the host reports the error.  The
-// block a.withhold_block (a testing aid; normally -1) returns false at its first barrier
-// without arriving, so every other block's wait runs out.
-__device__ bool barrier_totals(const StepArgs& a, const int32_t* inst_ids, int n_inst, const PersistScalars* sc,
-                               unsigned* bar, double* totals, int* err, double* tot) {
-    __shared__ int s_last, s_ok;
-    unsigned* gen = bar + 32;
-    __syncthreads();  // this block's partial (thread 0's store) precedes its arrival
-    if (threadIdx.x == 0 && (int)blockIdx.x == a.withhold_block) {
-        s_ok = 0;
-    } else if (threadIdx.x == 0) {
-        s_ok = 1;
-        const unsigned nb = gridDim.x;
-        const unsigned add = blockIdx.x == 0 ? 0x80000000u - (nb - 1) : 1u;
-        const unsigned g0 = load_acquire(gen);
-        const unsigned old = atom_add_acq_rel(bar, add);
-        s_last = ((old ^ (old + add)) & 0x80000000u) != 0;
-        if (!s_last) {
-            unsigned spins = 0;
-            while (load_acquire(gen) == g0) {
-                if (++spins > a.barrier_polls) {
-                    atomicOr(err, 1);
-                    s_ok = 0;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
+// Wait until *word >= q; false when the wait gave up (poll limit, or *err already set).
+__device__ bool wait_phase(const StepArgs& a, const unsigned* word, unsigned q, const int* err) {
+    unsigned spins = 0;
+    while (load_acquire(word) < q) {
+        if (++spins > a.barrier_polls || ((spins & 63u) == 0 && load_relaxed(err) != 0)) return false;
+        __nanosleep(32);
     }
-    __syncthreads();
-    if (!s_ok) return false;
-    if (s_last) {
-        for (int k = 0; k < n_inst; ++k) {
-            if (!sc[k].active) continue;
-            const double t = instance_total(a, a.inst[inst_ids[k]]);
-            if (threadIdx.x == 0) {
-                tot[k] = t;
-                totals[k] = t;
-            }
-        }
-        if (threadIdx.x == 0) red_add_release(gen, 1u);
-    } else if (threadIdx.x == 0) {
-        for (int k = 0; k < n_inst; ++k)
-            if (sc[k].active) tot[k] = __ldcg(totals + k);
-    }
-    __syncthreads();
     return true;
 }
 
-__global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, const int32_t* inst_ids, int32_t n_inst,
-                                                            int32_t n_entries, unsigned* bar, int* err) {
-    __shared__ PersistScalars sc[kPersistMaxInst];
-    __shared__ double tot[kPersistMaxInst];
-    __shared__ int s_any;
-    double* totals = reinterpret_cast<double*>(bar + 64);
-    for (int k = threadIdx.x; k < n_inst; k += blockDim.x) {
-        const InstState& st = a.state[inst_ids[k]];
-        sc[k].delta_new = st.delta_new;
-        sc[k].delta0 = st.delta0;
-        sc[k].dq = st.dq;
-        sc[k].alpha = st.alpha;
-        sc[k].beta = st.beta;
-        sc[k].iter = st.iter;
-        sc[k].active = st.active;
-        sc[k].flags = st.flags;
+// The scalar rules of finish<K_CG_DIR> / finish<K_CG_UPDATE> on one cloth's state.  The
+// state was last written by whichever block completed the previous phase, so it is read
+// from L2 (__ldcg): this SM's L1 may hold an older copy.  Returns whether the cloth's
+// loop goes on.
+__device__ bool apply_rule(InstState& st, const InstParams& ip, bool dir, double total) {
+    const double delta_new = __ldcg(&st.delta_new);
+    uint32_t flags = __ldcg(&st.flags);
+    if (dir) {
+        st.dq = total;
+        if (!(total > 0.0) || !isfinite(total)) {
+            st.flags = flags | (isfinite(total) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE);
+            st.active = 0;
+            return false;
+        }
+        st.alpha = (float)(delta_new / total);
+        return true;
     }
-    __syncthreads();
-    auto local = [&](int32_t inst) {
-        int li = 0;
-        while (li < n_inst - 1 && inst_ids[li] != inst) ++li;
-        return li;
-    };
-    bool ok = true;
-    for (;;) {
+    const double delta0 = __ldcg(&st.delta0);
+    const int32_t iter = __ldcg(&st.iter) + 1;
+    st.delta_new = total;
+    st.beta = (float)(total / delta_new);
+    st.iter = iter;
+    const bool more = iter < ip.imax && total > (double)ip.eps2 * delta0;
+    if (!isfinite(total)) flags |= OC_FLAG_NON_FINITE;
+    if (!more || !isfinite(total)) {
+        if (isfinite(total) && total > (double)ip.eps2 * delta0) flags |= OC_FLAG_NOT_CONVERGED;
+        st.active = 0;
+    }
+    st.flags = flags;
+    return more && isfinite(total);
+}
+
+__global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, int32_t n_entries, unsigned* words,
+                                                            int* err) {
+    __shared__ double s_part[kPersistMaxOwn];
+    __shared__ float s_scal[kPersistMaxOwn];      // beta (direction pass) or alpha (update pass)
+    __shared__ unsigned char s_run[kPersistMaxOwn];  // 0 idle, 1 runs, 2 runs its first direction pass
+    __shared__ short s_last[kPersistMaxOwn];      // owned entries whose arrival completed a phase
+    __shared__ int s_nlast, s_any, s_ok;
+    const int own = ((int)n_entries - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    if (threadIdx.x == 0) s_ok = 1;
+    for (unsigned q = 0;; ++q) {
+        const bool dir = (q & 1u) == 0u;
         if (threadIdx.x == 0) {
-            int any = 0;
-            for (int k = 0; k < n_inst; ++k) any |= sc[k].active;
-            s_any = any;
+            s_any = 0;
+            s_nlast = 0;
         }
         __syncthreads();
-        if (!s_any || !ok) break;
-        // Direction pass (k_cg_dir).
-        for (int32_t e = blockIdx.x; e < n_entries; e += gridDim.x) {
-            const BlockInfo bi = a.blocks[e];
-            const PersistScalars& c = sc[local(bi.inst)];
-            if (!c.active) continue;
-            const double bsum = block_sum_acc(cg_dir_block(a, bi, c.iter == 0, c.beta));
-            if (threadIdx.x == 0) a.partials[bi.gblk] = bsum;
+        // Each owned entry's cloth has completed phase q - 1: its state is final for q.
+        for (int j = threadIdx.x; j < own; j += blockDim.x) {
+            const int inst = a.blocks[blockIdx.x + j * gridDim.x].inst;
+            s_run[j] = 0;
+            if (!wait_phase(a, words + inst, q, err)) {
+                atomicOr(err, 1);
+                s_ok = 0;
+                continue;
+            }
+            const InstState& st = a.state[inst];
+            if (__ldcg(&st.active) == 0) continue;
+            s_run[j] = (dir && __ldcg(&st.iter) == 0) ? 2 : 1;
+            s_scal[j] = dir ? __ldcg(&st.beta) : __ldcg(&st.alpha);
+            s_any = 1;
         }
-        ok = barrier_totals(a, inst_ids, n_inst, sc, bar, totals, err, tot);
-        if (!ok) break;
-        if (threadIdx.x == 0) {
-            for (int k = 0; k < n_inst; ++k) {  // finish<K_CG_DIR>
-                PersistScalars& c = sc[k];
-                if (!c.active) continue;
-                const double total = tot[k];
-                c.dq = total;
-                if (!(total > 0.0) || !isfinite(total)) {
-                    c.flags |= isfinite(total) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
-                    c.active = 0;
-                } else {
-                    c.alpha = (float)(c.delta_new / total);
-                }
+        __syncthreads();
+        if (!s_ok || !s_any) break;
+        // The passes (k_cg_dir / k_cg_update) of the owned entries that run.
+        for (int j = 0; j < own; ++j) {
+            if (!s_run[j]) continue;
+            const BlockInfo bi = a.blocks[blockIdx.x + j * gridDim.x];
+            const double bsum = block_sum_acc(dir ? cg_dir_block(a, bi, s_run[j] == 2, s_scal[j])
+                                                  : cg_update_block(a, bi, s_scal[j]));
+            if (threadIdx.x == 0) s_part[j] = bsum;
+        }
+        __syncthreads();
+        if ((int)blockIdx.x == a.withhold_block) {
+            s_ok = 0;
+            break;
+        }
+        // Arrivals: thread j publishes entry j's partial and arrives at its cloth's ticket.
+        for (int j = threadIdx.x; j < own; j += blockDim.x) {
+            if (!s_run[j]) continue;
+            const BlockInfo bi = a.blocks[blockIdx.x + j * gridDim.x];
+            a.partials[bi.gblk] = s_part[j];
+            const unsigned t = atom_add_acq_rel(&a.state[bi.inst].ticket, 1u);
+            if (t == (unsigned)(a.inst[bi.inst].nblk - 1)) s_last[atomicAdd(&s_nlast, 1)] = (short)j;
+        }
+        __syncthreads();
+        // The cloths this block completed: totals in the epilogue's order, rule, publish.
+        const int n_last = s_nlast;
+        for (int l = 0; l < n_last; ++l) {
+            const int inst = a.blocks[blockIdx.x + s_last[l] * gridDim.x].inst;
+            const InstParams& ip = a.inst[inst];
+            __threadfence();
+            double acc = 0.0;
+#pragma unroll 8
+            for (int j = threadIdx.x; j < ip.nblk; j += blockDim.x) acc += __ldcg(a.partials + ip.blk0 + j);
+            const double total = block_sum(acc);
+            if (threadIdx.x == 0) {
+                InstState& st = a.state[inst];
+                st.ticket = 0;
+                const bool go_on = apply_rule(st, ip, dir, total);
+                store_release(words + inst, go_on ? q + 1u : kPhaseDone);
             }
         }
         __syncthreads();
-        // Update pass (k_cg_update).
-        for (int32_t e = blockIdx.x; e < n_entries; e += gridDim.x) {
-            const BlockInfo bi = a.blocks[e];
-            const PersistScalars& c = sc[local(bi.inst)];
-            if (!c.active) continue;
-            const double bsum = block_sum_acc(cg_update_block(a, bi, c.alpha));
-            if (threadIdx.x == 0) a.partials[bi.gblk] = bsum;
-        }
-        ok = barrier_totals(a, inst_ids, n_inst, sc, bar, totals, err, tot);
-        if (!ok) break;
-        if (threadIdx.x == 0) {
-            for (int k = 0; k < n_inst; ++k) {  // finish<K_CG_UPDATE>
-                PersistScalars& c = sc[k];
-                if (!c.active) continue;
-                const InstParams& ip = a.inst[inst_ids[k]];
-                const double total = tot[k];
-                const double old = c.delta_new;
-                c.delta_new = total;
-                c.beta = (float)(total / old);
-                c.iter += 1;
-                const bool more = c.iter < ip.imax && total > (double)ip.eps2 * c.delta0;
-                if (!isfinite(total)) c.flags |= OC_FLAG_NON_FINITE;
-                if (!more || !isfinite(total)) {
-                    if (isfinite(total) && total > (double)ip.eps2 * c.delta0) c.flags |= OC_FLAG_NOT_CONVERGED;
-                    c.active = 0;
-                }
-            }
-        }
-        __syncthreads();
     }
-    // The update of these cloths (k_integrate): per vertex, no barrier needed.  An
-    // adjoint solve (cg_only) stops at the solution.
-    if (ok && !a.cg_only) {
+    // The update of the owned entries (k_integrate): per vertex, after every owned cloth's
+    // loop has ended.  An adjoint solve (cg_only) stops at the solution.
+    if (s_ok && !a.cg_only) {
         for (int32_t e = blockIdx.x; e < n_entries; e += gridDim.x) {
             const BlockInfo bi = a.blocks[e];
             const InstParams& ip = a.inst[bi.inst];
@@ -839,19 +808,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, co
                 a.X[g] = Xg;
                 a.V[g] = Vg;
             }
-        }
-    }
-    if (blockIdx.x == 0) {
-        for (int k = threadIdx.x; k < n_inst; k += blockDim.x) {
-            InstState& st = a.state[inst_ids[k]];
-            const PersistScalars& c = sc[k];
-            st.delta_new = c.delta_new;
-            st.dq = c.dq;
-            st.alpha = c.alpha;
-            st.beta = c.beta;
-            st.iter = c.iter;
-            st.active = 0;
-            st.flags = c.flags;
         }
     }
 }
@@ -1177,7 +1133,7 @@ cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStre
     return cudaGetLastError();
 }
 
-int persist_max_instances() { return kPersistMaxInst; }
+int persist_max_entries_per_block() { return kPersistMaxOwn; }
 
 int persist_blocks_per_sm() {
     int n = 0;
@@ -1194,8 +1150,9 @@ cudaError_t launch_snapshot(const float4* X, const float4* V, float4* dX, float4
     return cudaGetLastError();
 }
 
-cudaError_t launch_cg_persist(const StepArgs& a, const int32_t* inst_ids, int32_t n_inst, int32_t n_entries,
-                              int grid, unsigned* bar, int* err, cudaStream_t stream) {
+cudaError_t launch_cg_persist(const StepArgs& a, int32_t n_entries, int grid, unsigned* words, int* err,
+                              cudaStream_t stream) {
+    if (grid <= 0 || (int64_t)n_entries > (int64_t)kPersistMaxOwn * grid) return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3((unsigned)kThreads);
@@ -1206,7 +1163,7 @@ cudaError_t launch_cg_persist(const StepArgs& a, const int32_t* inst_ids, int32_
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_cg_persist, a, inst_ids, n_inst, n_entries, bar, err);
+    return cudaLaunchKernelEx(&cfg, k_cg_persist, a, n_entries, words, err);
 }
 
 }  // namespace oc

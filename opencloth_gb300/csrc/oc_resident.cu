@@ -6,7 +6,8 @@
 // k_assemble_grid) straight into shared memory, so a small cloth's whole step is one
 // kernel whose HBM traffic is the state in and out; unfused, they load the state
 // k_assemble left in the planes.  The CG loop touches no HBM and needs no per-iteration
-// launch.
+// launch.  Unfused with a.cg_only, the kernel is the adjoint solve of a resident cloth:
+// the CG state k_adj_seed left in the planes in, the solution out, no update.
 // Dot products reduce per CTA (Acc pairs within warps, FP64 above), then in FP64 across
 // the cluster through distributed shared memory after a hardware cluster barrier, in
 // the same fixed order in every CTA, so all of them take identical decisions.  There
@@ -249,16 +250,20 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
         if (!s_go) break;
     }
     // V += dV dt; X += dt V; ground clamp (IMP:790-797), then the ellipsoid pass when
-    // enabled; dV stays as the warm start.
+    // enabled; dV stays as the warm start.  An adjoint solve (cg_only, unfused) stops at
+    // the solution.
     const float dt = a.dt;
+    const bool upd = !a.cg_only;
 #pragma unroll
     for (int u = 0; u < kResidentVpt; ++u) {
         if (!own[u]) continue;
         const int64_t g = base + threadIdx.x + u * T;
-        float4 Xg = a.X[g], Vg = a.V[g];
-        update_vertex(ip, dt, x[u][0], x[u][1], x[u][2], Xg, Vg);
-        a.X[g] = Xg;
-        a.V[g] = Vg;
+        if (upd) {
+            float4 Xg = a.X[g], Vg = a.V[g];
+            update_vertex(ip, dt, x[u][0], x[u][1], x[u][2], Xg, Vg);
+            a.X[g] = Xg;
+            a.V[g] = Vg;
+        }
         a.x[0][g] = x[u][0];
         a.x[1][g] = x[u][1];
         a.x[2][g] = x[u][2];

@@ -217,14 +217,53 @@ def test_displacement_mode_tracks_the_positions_forward_and_its_gradients(case, 
         assert np.linalg.norm(a - b) <= 1e-2 * np.linalg.norm(b), k_gpu
 
 
-def test_displacement_mode_needs_a_cooperative_adjoint():
-    from opencloth_gb300 import OcError, grid_cloth
+def test_displacement_mode_on_a_batch_equals_solo_handles():
+    """The displacement mode on a batch of 17 cloths, 16 small (resident) and one above
+    the resident cut-off (streamed, its CG in the cooperative launch): every small cloth's
+    displacement and gradients are those of a handle holding that cloth alone, bit for
+    bit; the streamed cloth's agree within 1e-5 relative (its vertex blocks, and so its
+    partial sums, are cut for the batch).  A COUPLED handle has no adjoint and refuses the
+    mode (status 7)."""
+    from opencloth_gb300 import JAC_COUPLED, OcError, grid_cloth
 
-    descs = []
-    for k in range(17):  # more cloths than one cooperative launch takes
-        X, sp = grid_cloth(5, 5, seed=k)
-        descs.append(ClothDesc(n_vertices=25, springs=sp, pinned=np.array([0, 4], np.int32)))
-    with ClothSolver(descs) as s:
+    rng = np.random.default_rng(11)
+    cloths = []
+    for k in range(17):
+        n = int(rng.integers(5, 12)) if k else 140  # one cloth above the resident cut-off
+        X, sp = grid_cloth(n, n, jitter=1e-2, seed=k)
+        V0 = rng.normal(0.0, 0.05, X.shape).astype(np.float32)
+        V0[[0, n - 1]] = 0.0
+        cloths.append((ClothDesc(n_vertices=n * n, springs=sp, pinned=np.array([0, n - 1], np.int32),
+                                 cg_max_iter=300, cg_tol=1e-6), X, V0))
+
+    def run(items):
+        with ClothSolver([d for d, _, _ in items]) as s:
+            s.set_tape_mode(True)
+            X = np.concatenate([x for _, x, _ in items])
+            s.set_state(X, np.concatenate([v for _, _, v in items]), np.zeros_like(X))
+            s.tape_forward(DT, 12, 4)
+            u = s.tape_displacement()
+            g = s.tape_backward(np.full_like(X, 1e-3))
+            return u, g
+
+    u, g = run(cloths)
+    off = np.cumsum([0] + [d.n_vertices for d, _, _ in cloths])
+    so = np.cumsum([0] + [len(d.springs) for d, _, _ in cloths])
+    def close(a, b):
+        return np.linalg.norm(a.astype(np.float64) - b) <= 1e-5 * np.linalg.norm(b.astype(np.float64))
+
+    for k, item in enumerate(cloths):
+        us, gs = run([item])
+        sl, ss = slice(off[k], off[k + 1]), slice(so[k], so[k + 1])
+        same = np.array_equal if k else close
+        assert same(u[sl], us), k
+        for key in ("dV0", "dext", "dX0"):
+            assert same(g[key][sl], gs[key]), (k, key)
+        for key in ("dKs", "dKd"):
+            assert same(g[key][ss], gs[key]), (k, key)
+    d, X, V0 = cloths[1]
+    desc = ClothDesc(n_vertices=d.n_vertices, springs=d.springs, pinned=d.pinned, jacobian_mode=JAC_COUPLED)
+    with ClothSolver(desc) as s:
         with pytest.raises(OcError) as e:
             s.set_tape_mode(True)
         assert e.value.status == 7
