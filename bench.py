@@ -558,7 +558,9 @@ def adjoint_workload(name: str, seed: int):
 
 
 def measure_adjoint(name: str, seed: int, local: int) -> dict:
-    """Forward, taped forward and reverse pass times of one gradient evaluation."""
+    """Forward, taped forward and reverse pass times of one gradient evaluation: the
+    reverse pass with the gradients left on the device (backward_ms) and with all of them
+    copied to host arrays (backward_e2e_ms); both upload dL/dX_T from a host array."""
     import torch
 
     from opencloth_gb300 import ClothSolver
@@ -613,14 +615,25 @@ def measure_adjoint(name: str, seed: int, local: int) -> dict:
         gX = loss_grad()
         t0 = time.perf_counter()
         g = s.tape_backward(gX)
-        bwd = time.perf_counter() - t0
+        bwd_e2e = time.perf_counter() - t0
         every_used, tape_bytes = s.tape_info()
+        kind, intervals = s.tape_layout()
+        # The same reverse pass with the gradients left on the device (every gradient is
+        # still computed; only the copies to host arrays are left out).
+        reset()
+        s.tape_forward(DT, steps, every, budget)
+        gX = loss_grad()
+        t0 = time.perf_counter()
+        s.tape_backward(gX, want=())
+        bwd = time.perf_counter() - t0
     torch.cuda.synchronize()
+    per_interval = {int(e): int((intervals == e).sum()) for e in np.unique(intervals)}
     return {"vertices": nv, "instances": len(descs), "steps": steps, "checkpoint_every": every_used,
-            "tape_mode": "displacement" if displacement else "positions",
-            "tape_bytes": tape_bytes, "forward_ms": 1e3 * fwd, "taped_forward_ms": 1e3 * tape,
+            "tape_mode": "displacement" if displacement else "positions", "tape": kind,
+            "cloths_per_interval": per_interval, "budget_bytes": budget, "tape_bytes": tape_bytes, "forward_ms": 1e3 * fwd, "taped_forward_ms": 1e3 * tape,
             "backward_ms": 1e3 * bwd, "backward_to_forward": bwd / fwd, "gradient_to_forward": (tape + bwd) / fwd,
-            "gradients_per_s": len(descs) / (tape + bwd),
+            "backward_e2e_ms": 1e3 * bwd_e2e, "gradient_to_forward_e2e": (tape + bwd_e2e) / fwd,
+            "gradients_per_s": len(descs) / (tape + bwd_e2e),
             "grad_norm_ks": float(np.linalg.norm(g["dKs"])), "finite": bool(np.isfinite(g["dKs"]).all())}
 
 

@@ -223,18 +223,43 @@ oc_status oc_set_spring_params(oc_solver* s, const float* ks, const float* kd);
 /* A constant per-vertex external force added to every unpinned vertex (host, 3 floats
  * per vertex), for cloths created without one too. */
 oc_status oc_set_ext_force(oc_solver* s, const float* ext);
-/* Run n_steps steps from the current state keeping a checkpoint of (X, V, dV) every
- * checkpoint_every steps (0: about sqrt(n_steps)); fails with OC_ERR_OUT_OF_MEMORY when
- * the checkpoints would exceed budget_bytes (0: no limit), with OC_ERR_UNSUPPORTED when a
- * cloth has passes after the update (the adjoint covers the implicit step only). */
+/* Run n_steps steps from the current state, taped for oc_tape_backward.  Two tapes:
+ *   OC_TAPE_REPLAY     the solution dV of every step (12 bytes per vertex and step) and,
+ *                      per cloth, its state (X, V) every `every` steps, the interval chosen
+ *                      per cloth.  Given dV the update is elementwise, so the reverse pass
+ *                      rebuilds every state by replaying it from the checkpoint before,
+ *                      bit for bit, without re-running the step's assembly and CG.
+ *   OC_TAPE_RECOMPUTE  every cloth's state every checkpoint_every steps; the reverse pass
+ *                      re-runs the steps of each segment from its checkpoint, except the
+ *                      last segments, which the budget's room keeps from the forward.
+ * Every cloth's interval is checkpoint_every (0: ceil(sqrt(n_steps)), which minimises a
+ * cloth's checkpoints plus segment buffer; the replay costs the same at any interval, so
+ * that is also the fastest); oc_tape_forward_intervals sets them cloth by cloth.  With
+ * budget_bytes > 0 the replay tape is used when it fits the budget, otherwise the
+ * recompute tape, or OC_ERR_OUT_OF_MEMORY when even its checkpoints would exceed the
+ * budget.  With budget_bytes <= 0: the replay tape, or the recompute tape (one segment
+ * buffer) when the replay tape's buffers cannot be allocated.  Both tapes give the same
+ * gradients bit for bit.  Fails with OC_ERR_UNSUPPORTED when a cloth has passes after the
+ * update (the adjoint covers the implicit step only). */
+#define OC_TAPE_REPLAY 0
+#define OC_TAPE_RECOMPUTE 1
 oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t checkpoint_every, int64_t budget_bytes);
+/* oc_tape_forward on the replay tape with the given interval of every cloth (every[i] >= 1,
+ * instance order; an interval above n_steps is taken as n_steps), no budget. */
+oc_status oc_tape_forward_intervals(oc_solver* s, float dt, int32_t n_steps, const int32_t* every);
+/* The last tape's kind (OC_TAPE_*) and every cloth's interval (instance order); either
+ * may be NULL.  OC_ERR_INVALID_ARGUMENT without a tape. */
+oc_status oc_tape_layout(const oc_solver* s, int32_t* kind, int32_t* every);
 /* Reverse pass of the last oc_tape_forward: given dL/dX and dL/dV (NULL = 0) of its final
  * state, returns dL/dX0, dL/dV0 (initial state), dL/dKs, dL/dKd (per spring) and dL/dext
- * (the constant external force); any output may be NULL.  Segments between checkpoints
- * are recomputed; each step's linear solve is back-propagated by one CG on the same
+ * (the constant external force); any output may be NULL.  Each step's state comes from the
+ * tape (replayed or recomputed), its system's diagonal blocks are rebuilt from spring i
+ * as the step formed them, and its linear solve is back-propagated by one CG on the same
  * symmetric system (exact-solve adjoint).  The handle's state is left at the final state. */
 oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV, float* dL_dX0, float* dL_dV0,
                            float* dL_dKs, float* dL_dKd, float* dL_dext);
+/* The default interval of the last tape and its device bytes (checkpoints, segment
+ * buffers, the replay tape's dV and the final state). */
 oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* tape_bytes);
 /* How the taped forward holds positions.  OC_TAPE_POSITIONS: as the step does (FP32
  * positions; the forward is the step itself).  OC_TAPE_DISPLACEMENT: as the start

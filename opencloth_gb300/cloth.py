@@ -303,21 +303,39 @@ class ClothSolver:
         """Constant per-vertex external force (3 floats per vertex)."""
         self._call(self._lib.oc_set_ext_force(self._h, ptr(self._vec(ext))))
 
-    def tape_forward(self, dt: float, n_steps: int, checkpoint_every: int = 0, budget_bytes: int = 0) -> None:
-        """Run n_steps keeping checkpoints for tape_backward."""
+    def tape_forward(self, dt: float, n_steps: int, checkpoint_every: int = 0, budget_bytes: int = 0,
+                     intervals=None) -> None:
+        """Run n_steps taped for tape_backward.  intervals: every cloth's checkpoint
+        interval on the replay tape (oc_tape_forward_intervals); otherwise the tape and
+        the intervals follow checkpoint_every and budget_bytes (oc_tape_forward)."""
+        if intervals is not None:
+            ev = np.ascontiguousarray(np.broadcast_to(np.asarray(intervals, np.int32), (self.n_instances,)))
+            self._call(self._lib.oc_tape_forward_intervals(self._h, float(dt), int(n_steps), ptr(ev)))
+            return
         self._call(self._lib.oc_tape_forward(self._h, float(dt), int(n_steps), int(checkpoint_every),
                                              int(budget_bytes)))
 
-    def tape_backward(self, dL_dX, dL_dV=None) -> dict:
+    def tape_layout(self):
+        """The last tape's kind ("replay" or "recompute") and every cloth's interval."""
+        kind = C.c_int32()
+        ev = np.zeros(self.n_instances, np.int32)
+        self._call(self._lib.oc_tape_layout(self._h, C.byref(kind), ptr(ev)))
+        return ("replay", "recompute")[kind.value], ev
+
+    GRADIENTS = ("dX0", "dV0", "dKs", "dKd", "dext")
+
+    def tape_backward(self, dL_dX, dL_dV=None, want=GRADIENTS) -> dict:
         """Gradients of a loss of the final state with respect to the initial state, the
-        per-spring Ks / Kd and the constant external force."""
+        per-spring Ks / Kd and the constant external force; `want` names the ones copied
+        out (the reverse pass computes all of them either way)."""
         gX = self._vec(dL_dX)
         gV = self._vec(dL_dV)
-        out = {k: np.zeros((self.n_vertices, 3), np.float32) for k in ("dX0", "dV0", "dext")}
-        out["dKs"] = np.zeros(self.n_springs, np.float32)
-        out["dKd"] = np.zeros(self.n_springs, np.float32)
-        self._call(self._lib.oc_tape_backward(self._h, ptr(gX), ptr(gV), ptr(out["dX0"]), ptr(out["dV0"]),
-                                              ptr(out["dKs"]), ptr(out["dKd"]), ptr(out["dext"])))
+        out = {}
+        for k in want:
+            out[k] = np.zeros(self.n_springs if k in ("dKs", "dKd") else (self.n_vertices, 3), np.float32)
+        p = {k: (ptr(out[k]) if k in out else None) for k in self.GRADIENTS}
+        self._call(self._lib.oc_tape_backward(self._h, ptr(gX), ptr(gV), p["dX0"], p["dV0"], p["dKs"], p["dKd"],
+                                              p["dext"]))
         return out
 
     def set_tape_mode(self, displacement: bool) -> None:

@@ -159,207 +159,246 @@ __device__ __forceinline__ void spring_jac_adj(const Geo& Gm, const float4 v1, c
     }
 }
 
-// Clamp, X' = X + dt V', V' = V + dt dV: the step's outputs' adjoints (gX, gV in the
-// planes) become gX, gV of X, V plus g_dV = dt gV'; then the adjoint CG is set up on
-// the system just assembled: x = 0, r = g_dV (pinned rows filtered), d = P^-1 r.
-__global__ void __launch_bounds__(kAdjThreads) k_adj_seed(const StepArgs a, const AdjArgs j) {
-    const int blk = blockIdx.x + a.blk_base;
-    const BlockInfo bi = a.blocks[blk];
-    const float dt = a.dt;
-    Acc part = acc_zero();
-    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
-        const float4 Xg = a.X[g], Vg = a.V[g];
-        const float dvy = j.dV[1][g];
-        const float vy = Vg.y + dvy * dt;
-        const float y = a.gm ? __ldg(a.Xbase + g).y + Xg.y : Xg.y;  // displacement mode: X holds u
-        const float ypre = y + dt * vy;
-        float gx0 = j.gX[0][g], gx1 = j.gX[1][g], gx2 = j.gX[2][g];
-        if (ypre < 0.0f) gx1 = 0.0f;  // clamped: X'.y does not depend on X, V
-        const float gv0 = j.gV[0][g] + dt * gx0, gv1 = j.gV[1][g] + dt * gx1, gv2 = j.gV[2][g] + dt * gx2;
-        j.gX[0][g] = gx0;
-        j.gX[1][g] = gx1;
-        j.gX[2][g] = gx2;
-        j.gV[0][g] = gv0;
-        j.gV[1][g] = gv1;
-        j.gV[2][g] = gv2;
-        const bool pinned = Vg.w != 0.0f;
-        const float r0 = pinned ? 0.0f : dt * gv0, r1 = pinned ? 0.0f : dt * gv1, r2 = pinned ? 0.0f : dt * gv2;
-        const float A0 = a.A[0][g], A3 = a.A[3][g], A5 = a.A[5][g];
-        a.x[0][g] = 0.0f;
-        a.x[1][g] = 0.0f;
-        a.x[2][g] = 0.0f;
-        a.r[0][g] = r0;
-        a.r[1][g] = r1;
-        a.r[2][g] = r2;
-        a.d[0][g] = (1.0f / A0) * r0;
-        a.d[1][g] = (1.0f / A3) * r1;
-        a.d[2][g] = (1.0f / A5) * r2;
-        acc_add(part, r0 * (A0 * r0) + r1 * (A3 * r1) + r2 * (A5 * r2));
-    }
-    finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
-}
-
 // Per vertex i: lambda -> g_F = h lambda, the terms of A_i and b_i: g_J = h^2 lambda (V +
 // dV)^T, g_Jv = h lambda dV^T, g_V += h^2 J lambda + damping g_F, g_ext += g_F; spring
 // i's Jacobian adjoint goes to the vertex's own-spring slots and to Ks_i, Kd_i.
-__global__ void __launch_bounds__(kAdjThreads) k_adj_vertex(const StepArgs a, const AdjArgs j) {
+// Variants (AdjArgs::vertex_variant): VPT vertices per thread with every load of a stage
+// in flight together (the vertex's own entries and spring i's ends and old gradient
+// entries, then the arithmetic), and CTAs per SM the register budget is set for.
+template <int VPT, int MINB>
+__global__ void __launch_bounds__(kAdjThreads, MINB) k_adj_vertex(const StepArgs a, const AdjArgs j) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstParams& ip = a.inst[bi.inst];
     const float h = a.dt;
-    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
-        const float4 Vg = a.V[g];
-        const bool pinned = Vg.w != 0.0f;
-        const float lam[3] = {a.x[0][g], a.x[1][g], a.x[2][g]};
-        const float dv[3] = {j.dV[0][g], j.dV[1][g], j.dV[2][g]};
-        const float v[3] = {Vg.x, Vg.y, Vg.z};
-        float gF[3];
+    const int64_t T = blockDim.x;
+    for (int64_t base = bi.v_begin + threadIdx.x; base < bi.v_end; base += VPT * T) {
+        float4 Vg[VPT];
+        float lam[VPT][3], dv[VPT][3], gv[VPT][3];
+        OwnSpring os[VPT];
+        int32_t sid[VPT];
+        float gk_old[VPT], gd_old[VPT];
+        bool ok[VPT];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) gF[k] = pinned ? 0.0f : h * lam[k];
-        float gv[3] = {j.gV[0][g], j.gV[1][g], j.gV[2][g]};
-        float gdP[3] = {0.f, 0.f, 0.f}, gdVs[3] = {0.f, 0.f, 0.f};
-        const OwnSpring os = load_own(a, g);
-        if (os.ends.x >= 0 && !pinned) {
-            const Geo geo = spring_geo(a, os.ends.x, os.ends.y, os.E1, os.E2, os.par.x, a.gm_own, g);
-            SpringEval e;
-            spring_eval(geo, os.W1, os.W2, e);
-            float J[6], Jv[6];
-            jac_element(e, os.par.y, os.par.z, 0, 0, J[0], Jv[0]);
-            jac_element(e, os.par.y, os.par.z, 0, 1, J[1], Jv[1]);
-            jac_element(e, os.par.y, os.par.z, 0, 2, J[2], Jv[2]);
-            jac_element(e, os.par.y, os.par.z, 1, 1, J[3], Jv[3]);
-            jac_element(e, os.par.y, os.par.z, 1, 2, J[4], Jv[4]);
-            jac_element(e, os.par.y, os.par.z, 2, 2, J[5], Jv[5]);
-            float jl0, jl1, jl2;
-            matvec(J, lam[0], lam[1], lam[2], jl0, jl1, jl2);
-            gv[0] += h * h * jl0;
-            gv[1] += h * h * jl1;
-            gv[2] += h * h * jl2;
-            float G[3][3], H[3][3];
+        for (int u = 0; u < VPT; ++u) {
+            const int64_t g = base + u * T;
+            ok[u] = g < bi.v_end;
+            const int64_t q = ok[u] ? g : base;
+            Vg[u] = a.V[q];
 #pragma unroll
-            for (int r = 0; r < 3; ++r)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    G[r][c] = h * h * lam[r] * (v[c] + dv[c]);
-                    H[r][c] = h * lam[r] * dv[c];
-                }
-            float gks, gkd;
-            spring_jac_adj(geo, os.W1, os.W2, os.par.y, os.par.z, G, H, gdP, gdVs, gks, gkd);
-            const int32_t sid = j.own_sid[g];
-            j.gKs[sid] += gks;
-            j.gKd[sid] += gkd;
+            for (int k = 0; k < 3; ++k) {
+                lam[u][k] = a.x[k][q];
+                dv[u][k] = j.dV[k][q];
+                gv[u][k] = j.gV[k][q];
+            }
+            os[u].ends = __ldg(a.own_ends + q);
+            sid[u] = __ldg(j.own_sid + q);
+            if (!ok[u]) os[u].ends.x = -1;
         }
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            gv[k] += ip.damping * gF[k];
-            j.gV[k][g] = gv[k];
-            j.gF[k][g] = gF[k];
-            j.gOwn[k][g] = gdP[k];
-            j.gOwn[3 + k][g] = gdVs[k];
-            if (!pinned) j.gExt[k][g] += gF[k];
+        for (int u = 0; u < VPT; ++u) {
+            os[u].par = make_float4(0.f, 0.f, 0.f, 0.f);
+            os[u].E1 = os[u].E2 = os[u].W1 = os[u].W2 = make_float4(0.f, 0.f, 0.f, 0.f);
+            gk_old[u] = gd_old[u] = 0.0f;
+            if (os[u].ends.x >= 0 && Vg[u].w == 0.0f) {
+                const int64_t g = base + u * T;
+                os[u].par = __ldg(a.own_par + g);
+                os[u].E1 = __ldg(a.X + os[u].ends.x);
+                os[u].E2 = __ldg(a.X + os[u].ends.y);
+                os[u].W1 = __ldg(a.V + os[u].ends.x);
+                os[u].W2 = __ldg(a.V + os[u].ends.y);
+                gk_old[u] = j.gKs[sid[u]];
+                gd_old[u] = j.gKd[sid[u]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < VPT; ++u) {
+            if (!ok[u]) continue;
+            const int64_t g = base + u * T;
+            const bool pinned = Vg[u].w != 0.0f;
+            const float v[3] = {Vg[u].x, Vg[u].y, Vg[u].z};
+            float gF[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) gF[k] = pinned ? 0.0f : h * lam[u][k];
+            float gdP[3] = {0.f, 0.f, 0.f}, gdVs[3] = {0.f, 0.f, 0.f};
+            if (os[u].ends.x >= 0 && !pinned) {
+                const Geo geo = spring_geo(a, os[u].ends.x, os[u].ends.y, os[u].E1, os[u].E2, os[u].par.x, a.gm_own, g);
+                SpringEval e;
+                spring_eval(geo, os[u].W1, os[u].W2, e);
+                float J[6], Jv[6];
+                jac_element(e, os[u].par.y, os[u].par.z, 0, 0, J[0], Jv[0]);
+                jac_element(e, os[u].par.y, os[u].par.z, 0, 1, J[1], Jv[1]);
+                jac_element(e, os[u].par.y, os[u].par.z, 0, 2, J[2], Jv[2]);
+                jac_element(e, os[u].par.y, os[u].par.z, 1, 1, J[3], Jv[3]);
+                jac_element(e, os[u].par.y, os[u].par.z, 1, 2, J[4], Jv[4]);
+                jac_element(e, os[u].par.y, os[u].par.z, 2, 2, J[5], Jv[5]);
+                float jl0, jl1, jl2;
+                matvec(J, lam[u][0], lam[u][1], lam[u][2], jl0, jl1, jl2);
+                gv[u][0] += h * h * jl0;
+                gv[u][1] += h * h * jl1;
+                gv[u][2] += h * h * jl2;
+                float G[3][3], H[3][3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        G[r][c] = h * h * lam[u][r] * (v[c] + dv[u][c]);
+                        H[r][c] = h * lam[u][r] * dv[u][c];
+                    }
+                float gks, gkd;
+                spring_jac_adj(geo, os[u].W1, os[u].W2, os[u].par.y, os[u].par.z, G, H, gdP, gdVs, gks, gkd);
+                j.gKs[sid[u]] = gk_old[u] + gks;
+                j.gKd[sid[u]] = gd_old[u] + gkd;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                gv[u][k] += ip.damping * gF[k];
+                j.gV[k][g] = gv[u][k];
+                j.gF[k][g] = gF[k];
+                j.gOwn[k][g] = gdP[k];
+                j.gOwn[3 + k][g] = gdVs[k];
+                if (!pinned) j.gExt[k][g] += gF[k];
+            }
         }
     }
 }
 
 // Per vertex v: every incident spring's force adjoint, in spring-id order (the spring's
 // p1 side also adds to Ks_s, Kd_s), then the own-spring Jacobian terms of the vertices
-// whose spring touches v.  The incidences are taken kAdjAhead at a time: their records,
-// then the neighbours' states and gradient entries, are all in flight before the first
-// is used (a serial walk waits on two dependent loads per incidence).  A spring's Ks / Kd
+// whose spring touches v.  The incidences are taken kAdjAhead at a time: their
+// neighbours' states and gradient entries are all in flight before the first is used.
+// An incidence comes from the vertex's record (neighbour | p2 flag, rest, Ks, Kd), or,
+// for a grid cloth whose parameters fit its stencil slots (the forward's stencil
+// condition), from its class's template entry: the neighbour offset and the parameter
+// slot, no record read (rest lengths that vary from rest_inc, as the forward reads them).
+// Both give the same incidences in the same order, so the same bits.  A spring's Ks / Kd
 // gradient is written only by its p1 vertex, so its old value can be fetched early.
-constexpr int kAdjAhead = 4;
+struct AdjInc {
+    int32_t o;      // the other end
+    bool p2;        // this vertex is the spring's p2
+    float rest, ks, kd;
+};
 
-__global__ void __launch_bounds__(kAdjThreads, 2) k_adj_springs(const StepArgs a, const AdjArgs j) {
-    const int blk = blockIdx.x + a.blk_base;
-    const BlockInfo bi = a.blocks[blk];
+template <bool STENCIL, int kAdjAhead>
+__device__ __forceinline__ void adj_springs_vertex(const StepArgs& a, const AdjArgs& j, const InstParams& ip,
+                                                   int64_t g) {
     const float4* __restrict__ X = a.X;
     const float4* __restrict__ V = a.V;
-    const int4* __restrict__ inc = a.inc;
-    const int32_t* __restrict__ isid = j.inc_sid;
     const float* __restrict__ gF0 = j.gF[0];
     const float* __restrict__ gF1 = j.gF[1];
     const float* __restrict__ gF2 = j.gF[2];
-    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
-        const float4 Xg = __ldg(X + g), Vg = __ldg(V + g);
-        const bool pin_g = Vg.w != 0.0f;
-        const float gFg[3] = {__ldg(gF0 + g), __ldg(gF1 + g), __ldg(gF2 + g)};
-        float gx[3] = {j.gX[0][g], j.gX[1][g], j.gX[2][g]};
-        float gv[3] = {j.gV[0][g], j.gV[1][g], j.gV[2][g]};
-        const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
-        for (int32_t kb = k0; kb < k1; kb += kAdjAhead) {
-            int4 rec[kAdjAhead];
-            int32_t sid[kAdjAhead];
+    const float4 Xg = __ldg(X + g), Vg = __ldg(V + g);
+    const float gFg[3] = {__ldg(gF0 + g), __ldg(gF1 + g), __ldg(gF2 + g)};
+    float gx[3] = {j.gX[0][g], j.gX[1][g], j.gX[2][g]};
+    float gv[3] = {j.gV[0][g], j.gV[1][g], j.gV[2][g]};
+    const int32_t k0 = __ldg(a.rowptr + g), k1 = __ldg(a.rowptr + g + 1);
+    const int32_t* st = nullptr;
+    const float4* par = nullptr;
+    int32_t ebase = 0;
+    const int32_t cols = ip.grid_cols;
+    if constexpr (STENCIL) {
+        const int32_t l = (int32_t)(g - ip.v_off);
+        const int32_t r = l / cols, c = l - r * cols;
+        st = a.st_data + ip.st_off;
+        par = a.st_param + ip.st_par;
+        ebase = __ldg(st + stencil_class_1d(r, ip.grid_rows) * 6 + stencil_class_1d(c, cols)) - k0;
+    }
+    for (int32_t kb = k0; kb < k1; kb += kAdjAhead) {
+        AdjInc in[kAdjAhead];
+        int32_t sid[kAdjAhead];
 #pragma unroll
-            for (int u = 0; u < kAdjAhead; ++u) {
-                const bool in = kb + u < k1;
-                rec[u] = in ? __ldg(inc + kb + u) : make_int4((int)g, 0, 0, 0);
-                sid[u] = in ? __ldg(isid + kb + u) : 0;
+        for (int u = 0; u < kAdjAhead; ++u) {
+            const int32_t k = kb + u;
+            if (k >= k1) {
+                in[u] = AdjInc{(int32_t)g, true, 0.0f, 0.0f, 0.0f};
+            } else if constexpr (STENCIL) {
+                const int32_t v = __ldg(st + ebase + k);
+                const int32_t di = (v & 7) - 2, dj = ((v >> 3) & 7) - 2;
+                const float4 p = __ldg(par + (v >> 7));
+                in[u] = AdjInc{(int32_t)(g + (int64_t)di * cols + dj), (v & 64) != 0,
+                               ip.st_rest ? __ldg(a.rest_inc + k) : p.x, p.y, p.z};
+            } else {
+                const int4 rec = __ldg(a.inc + k);
+                in[u] = AdjInc{rec.x & 0x7fffffff, rec.x < 0, __int_as_float(rec.y), __int_as_float(rec.z),
+                               __int_as_float(rec.w)};
             }
-            float4 Xo[kAdjAhead], Vo[kAdjAhead];
-            float gFo[kAdjAhead][3], gk_old[kAdjAhead], gd_old[kAdjAhead];
-#pragma unroll
-            for (int u = 0; u < kAdjAhead; ++u) {
-                const int32_t o = rec[u].x & 0x7fffffff;
-                Xo[u] = __ldg(X + o);
-                Vo[u] = __ldg(V + o);
-                gFo[u][0] = __ldg(gF0 + o);
-                gFo[u][1] = __ldg(gF1 + o);
-                gFo[u][2] = __ldg(gF2 + o);
-                const bool p1 = kb + u < k1 && rec[u].x >= 0;
-                gk_old[u] = p1 ? j.gKs[sid[u]] : 0.0f;
-                gd_old[u] = p1 ? j.gKd[sid[u]] : 0.0f;
-            }
-#pragma unroll
-            for (int u = 0; u < kAdjAhead; ++u) {
-                if (kb + u >= k1) break;
-                const bool as_p2 = rec[u].x < 0;
-                const bool pin_o = Vo[u].w != 0.0f;
-                // g_f = [p1 free] gF[p1] - [p2 free] gF[p2]
-                float gf[3];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float g1 = as_p2 ? (pin_o ? 0.0f : gFo[u][c]) : (pin_g ? 0.0f : gFg[c]);
-                    const float g2 = as_p2 ? (pin_g ? 0.0f : gFg[c]) : (pin_o ? 0.0f : gFo[u][c]);
-                    gf[c] = g1 - g2;
-                }
-                const float rest = __int_as_float(rec[u].y), ks = __int_as_float(rec[u].z),
-                            kd = __int_as_float(rec[u].w);
-                float gdP[3], gdV[3], gks, gkd;
-                const int32_t o = rec[u].x & 0x7fffffff;
-                if (as_p2)
-                    spring_force_adj(spring_geo(a, o, (int32_t)g, Xo[u], Xg, rest, a.gm_inc, kb + u), Vo[u], Vg, ks, kd,
-                                     gf, gdP, gdV, gks, gkd);
-                else
-                    spring_force_adj(spring_geo(a, (int32_t)g, o, Xg, Xo[u], rest, a.gm_inc, kb + u), Vg, Vo[u], ks, kd,
-                                     gf, gdP, gdV, gks, gkd);
-                const float sgn = as_p2 ? -1.0f : 1.0f;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    gx[c] += sgn * gdP[c];
-                    gv[c] += sgn * gdV[c];
-                }
-                if (!as_p2) {
-                    j.gKs[sid[u]] = gk_old[u] + gks;
-                    j.gKd[sid[u]] = gd_old[u] + gkd;
-                }
-            }
+            sid[u] = (k < k1 && !in[u].p2) ? __ldg(j.inc_sid + k) : 0;
         }
-        const int32_t o0 = __ldg(j.own_rowptr + g), o1 = __ldg(j.own_rowptr + g + 1);
-        for (int32_t k = o0; k < o1; ++k) {
-            const int32_t e = __ldg(j.own_ent + k);
-            const int32_t i = e & 0x7fffffff;
-            const float sgn = e < 0 ? -1.0f : 1.0f;
+        float4 Xo[kAdjAhead], Vo[kAdjAhead];
+        float gFo[kAdjAhead][3], gk_old[kAdjAhead], gd_old[kAdjAhead];
+#pragma unroll
+        for (int u = 0; u < kAdjAhead; ++u) {
+            const int32_t o = in[u].o;
+            Xo[u] = __ldg(X + o);
+            Vo[u] = __ldg(V + o);
+            gFo[u][0] = __ldg(gF0 + o);
+            gFo[u][1] = __ldg(gF1 + o);
+            gFo[u][2] = __ldg(gF2 + o);
+            const bool p1 = kb + u < k1 && !in[u].p2;
+            gk_old[u] = p1 ? j.gKs[sid[u]] : 0.0f;
+            gd_old[u] = p1 ? j.gKd[sid[u]] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < kAdjAhead; ++u) {
+            if (kb + u >= k1) break;
+            const bool as_p2 = in[u].p2;
+            // g_f = [p1 free] gF[p1] - [p2 free] gF[p2]; k_adj_vertex leaves gF = 0 at
+            // pinned vertices.
+            float gf[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) gf[c] = as_p2 ? gFo[u][c] - gFg[c] : gFg[c] - gFo[u][c];
+            float gdP[3], gdV[3], gks, gkd;
+            const int32_t o = in[u].o;
+            if (as_p2)
+                spring_force_adj(spring_geo(a, o, (int32_t)g, Xo[u], Xg, in[u].rest, a.gm_inc, kb + u), Vo[u], Vg,
+                                 in[u].ks, in[u].kd, gf, gdP, gdV, gks, gkd);
+            else
+                spring_force_adj(spring_geo(a, (int32_t)g, o, Xg, Xo[u], in[u].rest, a.gm_inc, kb + u), Vg, Vo[u],
+                                 in[u].ks, in[u].kd, gf, gdP, gdV, gks, gkd);
+            const float sgn = as_p2 ? -1.0f : 1.0f;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                gx[c] += sgn * j.gOwn[c][i];
-                gv[c] += sgn * j.gOwn[3 + c][i];
+                gx[c] += sgn * gdP[c];
+                gv[c] += sgn * gdV[c];
+            }
+            if (!as_p2) {
+                j.gKs[sid[u]] = gk_old[u] + gks;
+                j.gKd[sid[u]] = gd_old[u] + gkd;
             }
         }
+    }
+    const int32_t o0 = __ldg(j.own_rowptr + g), o1 = __ldg(j.own_rowptr + g + 1);
+    for (int32_t k = o0; k < o1; ++k) {
+        const int32_t e = __ldg(j.own_ent + k);
+        const int32_t i = e & 0x7fffffff;
+        const float sgn = e < 0 ? -1.0f : 1.0f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            j.gX[c][g] = gx[c];
-            j.gV[c][g] = gv[c];
+            gx[c] += sgn * j.gOwn[c][i];
+            gv[c] += sgn * j.gOwn[3 + c][i];
         }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        j.gX[c][g] = gx[c];
+        j.gV[c][g] = gv[c];
+    }
+}
+
+// Variants (AdjArgs::springs_variant): incidences in flight per batch and CTAs per SM
+// the register budget is set for.  The default, two incidences and three CTAs (80
+// registers), measured 0.3 ms faster per reverse step on 12M vertices than four and two.
+template <int AHEAD, int MINB>
+__global__ void __launch_bounds__(kAdjThreads, MINB) k_adj_springs(const StepArgs a, const AdjArgs j) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    const InstParams& ip = a.inst[bi.inst];
+    if (ip.grid_cols > 0) {
+        for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x)
+            adj_springs_vertex<true, AHEAD>(a, j, ip, g);
+    } else {
+        for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x)
+            adj_springs_vertex<false, AHEAD>(a, j, ip, g);
     }
 }
 
@@ -421,6 +460,31 @@ __device__ __forceinline__ float3 spring_force_geo(const Geo& G, const float4 v1
 
 // 1: the step's assembly in displacement mode (incidence-record gather in spring order,
 // spring i's Jacobians, A and b, the CG set-up), one thread per vertex.
+// Spring i's blocks of vertex g in the displacement mode (IMP:744-770 on geo_disp):
+// A = M - h (Jv + h J) and h J.  The assembly and the reverse pass's seed both form them
+// here.
+__device__ __forceinline__ void gm_own_blocks(const StepArgs& a, int64_t g, float mass, float h, float A[6],
+                                              float hJ[6]) {
+    const OwnSpring os = load_own(a, g);
+    float J[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, Jv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (os.ends.x >= 0) {
+        SpringEval e;
+        spring_eval(spring_geo(a, os.ends.x, os.ends.y, os.E1, os.E2, 0.0f, a.gm_own, g), os.W1, os.W2, e);
+        jac_element(e, os.par.y, os.par.z, 0, 0, J[0], Jv[0]);
+        jac_element(e, os.par.y, os.par.z, 0, 1, J[1], Jv[1]);
+        jac_element(e, os.par.y, os.par.z, 0, 2, J[2], Jv[2]);
+        jac_element(e, os.par.y, os.par.z, 1, 1, J[3], Jv[3]);
+        jac_element(e, os.par.y, os.par.z, 1, 2, J[4], Jv[4]);
+        jac_element(e, os.par.y, os.par.z, 2, 2, J[5], Jv[5]);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const float Mk = (k == 0 || k == 3 || k == 5) ? mass : 0.0f;
+        A[k] = Mk - h * (Jv[k] + h * J[k]);
+        hJ[k] = h * J[k];
+    }
+}
+
 __global__ void __launch_bounds__(kAdjThreads) k_gm_assemble(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
@@ -468,26 +532,9 @@ __global__ void __launch_bounds__(kAdjThreads) k_gm_assemble(const StepArgs a) {
             }
         }
         // Spring i's Jacobians (IMP:744-770) and the vertex's system.
-        const OwnSpring os = load_own(a, g);
-        float J[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, Jv[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if (os.ends.x >= 0) {
-            SpringEval e;
-            spring_eval(spring_geo(a, os.ends.x, os.ends.y, os.E1, os.E2, 0.0f, a.gm_own, g), os.W1, os.W2, e);
-            jac_element(e, os.par.y, os.par.z, 0, 0, J[0], Jv[0]);
-            jac_element(e, os.par.y, os.par.z, 0, 1, J[1], Jv[1]);
-            jac_element(e, os.par.y, os.par.z, 0, 2, J[2], Jv[2]);
-            jac_element(e, os.par.y, os.par.z, 1, 1, J[3], Jv[3]);
-            jac_element(e, os.par.y, os.par.z, 1, 2, J[4], Jv[4]);
-            jac_element(e, os.par.y, os.par.z, 2, 2, J[5], Jv[5]);
-        }
         VertexSystem sys;
         float hJ[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            const float Mk = (k == 0 || k == 3 || k == 5) ? Ug.w : 0.0f;
-            sys.A[k] = Mk - h * (Jv[k] + h * J[k]);
-            hJ[k] = h * J[k];
-        }
+        gm_own_blocks(a, g, Ug.w, h, sys.A, hJ);
         float wx, wy, wz;
         matvec(hJ, Vg.x, Vg.y, Vg.z, wx, wy, wz);
         sys.b[0] = h * (Fx + wx);
@@ -507,6 +554,23 @@ __global__ void __launch_bounds__(kAdjThreads) k_gm_assemble(const StepArgs a) {
     finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
 }
 
+// The reverse pass's seed in the displacement mode: spring i's blocks rebuilt as the
+// assembly formed them (A planes written), then adj_seed_vertex and the epilogue.
+__global__ void __launch_bounds__(kAdjThreads) k_gm_seed_own(const StepArgs a, const AdjArgs j) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    Acc part = acc_zero();
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Ug = a.X[g], Vg = a.V[g];
+        float A[6], hJ[6];
+        gm_own_blocks(a, g, Ug.w, a.dt, A, hJ);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.A[k][g] = A[k];
+        acc_add(part, adj_seed_vertex(a, j, g, Ug, Vg, A[0], A[3], A[5]));
+    }
+    finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
+}
+
 // 2: V += dV dt, u += dt V, ground clamp on the position (IMP:790-797).
 __global__ void __launch_bounds__(kAdjThreads) k_gm_update(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;
@@ -514,14 +578,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_gm_update(const StepArgs a) {
     const float dt = a.dt;
     for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
         float4 U = a.X[g], V = a.V[g];
-        V.x = V.x + a.x[0][g] * dt;
-        V.y = V.y + a.x[1][g] * dt;
-        V.z = V.z + a.x[2][g] * dt;
-        U.x = U.x + dt * V.x;
-        U.y = U.y + dt * V.y;
-        U.z = U.z + dt * V.z;
-        const float by = __ldg(a.Xbase + g).y;
-        if (by + U.y < 0.0f) U.y = -by;
+        gm_advance(dt, a.x[0][g], a.x[1][g], a.x[2][g], __ldg(a.Xbase + g).y, U, V);
         a.X[g] = U;
         a.V[g] = V;
     }
@@ -554,15 +611,27 @@ __global__ void k_set_spring_params(const StepArgs a, const AdjArgs j, const flo
 cudaError_t launch_adjoint(int which, const StepArgs& a, const AdjArgs& j, int nblocks, cudaStream_t stream) {
     if (nblocks <= 0) return cudaSuccess;
     switch (which) {
-        case 0: k_adj_seed<<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
-        case 1: k_adj_vertex<<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
-        case 2: k_adj_springs<<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+        case 0: k_gm_seed_own<<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+        case 1:
+            switch (j.vertex_variant) {
+                case 1: k_adj_vertex<1, 3><<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+                case 2: k_adj_vertex<2, 3><<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+                default: k_adj_vertex<2, 2><<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+            }
+            break;
+        case 2:
+            switch (j.springs_variant) {
+                case 1: k_adj_springs<4, 2><<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+                case 2: k_adj_springs<2, 2><<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+                case 3: k_adj_springs<1, 4><<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+                default: k_adj_springs<2, 3><<<nblocks, kAdjThreads, 0, stream>>>(a, j); break;
+            }
+            break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
 
-const void* adjoint_seed_fn() { return (const void*)k_adj_seed; }
 
 cudaError_t launch_gm(int which, const StepArgs& a, int n, cudaStream_t stream) {
     const int64_t nv = (int64_t)n;  // the per-vertex kernels (0, 3, 4) take the vertex count

@@ -106,21 +106,31 @@ struct oc_solver {
     float* d_kd = nullptr;
     size_t stride = 0;      // plane stride (vertices)
     struct Tape {
-        int32_t n_steps = 0, every = 0, n_ck = 0;
-        // Segment buffers (every step's X, V, A, dV of one segment): n_buf of them.  The
-        // last n_keep segments are kept from the taped forward and walked without a
-        // recompute; the others are recomputed into buffer 0 (absent when n_keep = n_ck).
-        int32_t n_buf = 0, n_keep = 0, cap_buf = 0, cap_every = 0;
+        int32_t n_steps = 0, every = 0;
         float dt = 0.0f;
+        // REPLAY (OC_TAPE_REPLAY): dV of every step (three planes of `stride` floats per
+        // step) and per cloth its state every tc[i].every steps plus a segment buffer, in
+        // one arena; the reverse pass rebuilds the states by replaying the update.
+        bool replay = false;
+        float* dvt = nullptr;
+        size_t dvt_cap = 0;  // floats
+        float4* arena = nullptr;
+        size_t arena_cap = 0;  // float4s
+        TapeCloth* d_tc = nullptr;
+        std::vector<TapeCloth> tc;
+        // RECOMPUTE (OC_TAPE_RECOMPUTE, when the dV of every step does not fit the
+        // budget): every cloth's state every `every` steps (n_ck checkpoints); segment
+        // buffers of every step's X, V and dV, n_buf of them: the last n_keep segments
+        // are kept from the taped forward, the others are recomputed with the step into
+        // buffer 0 (absent when n_keep = n_ck).
+        int32_t n_ck = 0, n_buf = 0, n_keep = 0, cap_ck = 0, cap_slots = 0;
         float4 *ckX = nullptr, *ckV = nullptr, *segX = nullptr, *segV = nullptr, *finX = nullptr, *finV = nullptr;
-        // segAx: per step of a segment, the system A (6 planes) and the solution dV (3
-        // planes) as the step left them (the A and x planes are contiguous).
-        float *ckx = nullptr, *segAx = nullptr, *finx = nullptr;
+        float *ckx = nullptr, *segx = nullptr, *finx = nullptr;
         float* planes = nullptr;  // gX 3, gV 3, gF 3, gOwn 6, gExt 3, dV 3
         float* gK = nullptr;      // gKs, gKd
         cudaGraph_t graph = nullptr;  // the adjoint solve as a WHILE loop (many cloths)
         cudaGraphExec_t exec = nullptr;
-        cudaGraphNode_t n_seed = nullptr;  // k_adj_seed: its arguments change every step
+        cudaGraphNode_t n_seed = nullptr;  // k_adj_seed_own: its arguments change every step
         cudaGraphConditionalHandle handle = 0;
         float graph_dt = 0.0f;
         bool valid = false;
@@ -802,8 +812,10 @@ oc_status gm_step(oc_solver* s, float dt) {
     return OC_OK;
 }
 
-// The adjoint solve of one step as a graph: reset the loop counter, set up the CG on
-// the adjoint right-hand side (k_adj_seed), iterate (WHILE node) over every cloth.
+// The adjoint solve of one step as a graph (positions mode, a handle without the
+// cooperative CG): reset the loop counter, rebuild the system's diagonal blocks and set
+// up the CG on the adjoint right-hand side (k_adj_seed_own), iterate (WHILE node) over
+// every cloth.
 oc_status build_adjoint_graph(oc_solver* s, float dt) {
     auto& T = s->tape;
     if (T.exec) {
@@ -838,7 +850,7 @@ oc_status build_adjoint_graph(oc_solver* s, float dt) {
     mp.pitch = sizeof(int32_t);
     OC_TRY(cudaGraphAddMemsetNode(&n_reset, g, nullptr, 0, &mp));
     cudaKernelNodeParams kp{};
-    kp.func = const_cast<void*>(adjoint_seed_fn());
+    kp.func = const_cast<void*>(adjoint_seed_own_fn());
     kp.gridDim = dim3((unsigned)s->n_blocks);
     kp.blockDim = dim3(256);
     kp.kernelParams = params_seed;
@@ -1303,6 +1315,8 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
         s->adj.own_sid = own_sid;
         s->adj.own_rowptr = own_rowptr;
         s->adj.own_ent = own_ent;
+        if (const char* e = std::getenv("OC_ADJ_SPRINGS_VARIANT")) s->adj.springs_variant = std::atoi(e);
+        if (const char* e = std::getenv("OC_ADJ_VERTEX_VARIANT")) s->adj.vertex_variant = std::atoi(e);
     }
     float* planes = nullptr;
     OC_CREATE_TRY(dalloc(s, &planes, 15 * stride));
@@ -1876,59 +1890,123 @@ oc_status oc_set_ext_force(oc_solver* s, const float* ext) {
     return OC_OK;
 }
 
-oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t checkpoint_every, int64_t budget_bytes) {
-    if (!valid_solver(s) || n_steps < 1 || checkpoint_every < 0 || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
-    if (s->any_passes)
-        return fail(s, OC_ERR_UNSUPPORTED, "oc_tape_forward: the adjoint covers the implicit step only, not the "
-                                           "passes after it");
-    if (s->any_coupled)
-        return fail(s, OC_ERR_UNSUPPORTED, "oc_tape_forward: the adjoint covers the REFERENCE Jacobian mode");
-    OC_TRY(cudaSetDevice(s->device));
+}  // extern "C"
+
+namespace {
+
+int32_t ceil_div(int32_t a, int32_t b) { return (a + b - 1) / b; }
+
+// Bytes of one state of every cloth as the recompute tape keeps it (X, V and three planes:
+// the warm start in a checkpoint, the step's dV in a segment slot); also the final state
+// both tapes keep.
+double tape_state_bytes(const oc_solver* s) {
+    return 2.0 * sizeof(float4) * (double)s->nv + 3.0 * (double)s->stride * sizeof(float);
+}
+
+// float4s of one cloth's replay arena for interval e over n steps: its checkpoints and, for
+// e > 1, a segment buffer.
+size_t replay_cloth_f4(int64_t nv, int32_t n, int32_t e) {
+    return 2 * (size_t)nv * ((size_t)ceil_div(n, e) + (e > 1 ? (size_t)e : 0));
+}
+
+double replay_bytes(const oc_solver* s, int32_t n, const std::vector<int32_t>& every) {
+    double b = tape_state_bytes(s) + (double)n * 3.0 * (double)s->stride * sizeof(float);
+    for (int32_t i = 0; i < s->n_inst; ++i)
+        b += (double)sizeof(float4) * (double)replay_cloth_f4(s->inst_host[(size_t)i].nv, n, every[(size_t)i]);
+    return b;
+}
+
+// Buffers both tapes use: the final state, the gradient planes and the spring gradients.
+oc_status alloc_tape_common(oc_solver* s) {
     auto& T = s->tape;
-    const size_t state_bytes = 2 * sizeof(float4) * (size_t)s->nv + 3 * s->stride * sizeof(float);
-    const size_t seg_bytes = 2 * sizeof(float4) * (size_t)s->nv + 9 * s->stride * sizeof(float);
-    int32_t every = checkpoint_every;
-    if (every == 0) every = std::max(1, (int32_t)std::ceil(std::sqrt((double)n_steps)));
-    every = std::min(every, n_steps);
-    const int32_t n_ck = (n_steps + every - 1) / every;
-    const double buf_bytes = (double)seg_bytes * (double)every;
-    const double need = (double)state_bytes * (double)(n_ck + 1) + buf_bytes;
-    if (budget_bytes > 0 && need > (double)budget_bytes)
-        return fail(s, OC_ERR_OUT_OF_MEMORY, "oc_tape_forward: checkpoints need " + std::to_string(need) +
-                                                 " bytes, above the budget");
-    // With a budget, the room left after the checkpoints keeps whole segments from this
-    // forward, the last ones first, so that the reverse pass need not recompute them.
-    int32_t n_buf = 1;
-    if (budget_bytes > 0)
-        n_buf = (int32_t)std::min<double>(n_ck, 1.0 + std::floor(((double)budget_bytes - need) / buf_bytes));
-    const int32_t n_keep = n_buf >= n_ck ? n_ck : n_buf - 1;
-    // (Re)allocate when the shape grew; buffers live until the handle is destroyed.
-    if (T.n_ck < n_ck || T.cap_every < every || T.cap_buf < n_buf || !T.ckX) {
-        float4* p4 = nullptr;
-        float* pf = nullptr;
-        OC_TRY(dalloc(s, &p4, (size_t)s->nv * n_ck)); T.ckX = p4;
-        OC_TRY(dalloc(s, &p4, (size_t)s->nv * n_ck)); T.ckV = p4;
-        OC_TRY(dalloc(s, &pf, 3 * s->stride * n_ck)); T.ckx = pf;
-        const size_t slots = (size_t)every * n_buf;
-        OC_TRY(dalloc(s, &p4, (size_t)s->nv * slots)); T.segX = p4;
-        OC_TRY(dalloc(s, &p4, (size_t)s->nv * slots)); T.segV = p4;
-        OC_TRY(dalloc(s, &pf, 9 * s->stride * slots)); T.segAx = pf;
-        T.cap_buf = n_buf;
-        T.cap_every = every;
-        if (!T.finX) {
-            OC_TRY(dalloc(s, &p4, (size_t)s->nv)); T.finX = p4;
-            OC_TRY(dalloc(s, &p4, (size_t)s->nv)); T.finV = p4;
-            OC_TRY(dalloc(s, &pf, 3 * s->stride)); T.finx = pf;
-            OC_TRY(dalloc(s, &pf, 21 * s->stride)); T.planes = pf;
-            OC_TRY(dalloc(s, &pf, 2 * (size_t)s->ns + 2)); T.gK = pf;
-        }
+    if (T.finX) return OC_OK;
+    OC_TRY(dalloc(s, &T.finX, (size_t)s->nv));
+    OC_TRY(dalloc(s, &T.finV, (size_t)s->nv));
+    OC_TRY(dalloc(s, &T.finx, 3 * s->stride));
+    OC_TRY(dalloc(s, &T.planes, 21 * s->stride));
+    OC_TRY(dalloc(s, &T.gK, 2 * (size_t)s->ns + 2));
+    return OC_OK;
+}
+
+void free_recompute(oc_solver* s) {
+    auto& T = s->tape;
+    dfree(s, &T.ckX);
+    dfree(s, &T.ckV);
+    dfree(s, &T.ckx);
+    dfree(s, &T.segX);
+    dfree(s, &T.segV);
+    dfree(s, &T.segx);
+    T.cap_ck = T.cap_slots = 0;
+}
+
+void free_replay(oc_solver* s) {
+    auto& T = s->tape;
+    dfree(s, &T.arena);
+    dfree(s, &T.dvt);
+    T.arena_cap = T.dvt_cap = 0;
+}
+
+// The replay tape's layout for per-cloth intervals every[i] (1 ... n): offsets, arena, dV.
+cudaError_t alloc_replay(oc_solver* s, int32_t n, const std::vector<int32_t>& every) {
+    auto& T = s->tape;
+    T.tc.assign((size_t)s->n_inst, TapeCloth{});
+    size_t off = 0;
+    for (int32_t i = 0; i < s->n_inst; ++i) {
+        const int64_t nv = s->inst_host[(size_t)i].nv;
+        TapeCloth& c = T.tc[(size_t)i];
+        c.every = every[(size_t)i];
+        c.ck = (int64_t)off;
+        off += 2 * (size_t)nv * (size_t)ceil_div(n, c.every);
+        c.buf = (int64_t)off;
+        if (c.every > 1) off += 2 * (size_t)nv * (size_t)c.every;
     }
-    T.n_steps = n_steps;
-    T.every = every;
-    T.n_ck = n_ck;
-    T.n_buf = n_buf;
-    T.n_keep = n_keep;
-    T.dt = dt;
+    const size_t nd = (size_t)n * 3 * s->stride;
+    cudaError_t e = cudaSuccess;
+    if (T.arena_cap < off) {
+        dfree(s, &T.arena);
+        T.arena_cap = 0;
+        if ((e = dalloc(s, &T.arena, off)) != cudaSuccess) return e;
+        T.arena_cap = off;
+    }
+    if (T.dvt_cap < nd) {
+        dfree(s, &T.dvt);
+        T.dvt_cap = 0;
+        if ((e = dalloc(s, &T.dvt, nd)) != cudaSuccess) return e;
+        T.dvt_cap = nd;
+    }
+    return reupload(s, &T.d_tc, T.tc);
+}
+
+cudaError_t alloc_recompute(oc_solver* s, int32_t n_ck, int32_t every, int32_t n_buf) {
+    auto& T = s->tape;
+    cudaError_t e = cudaSuccess;
+    if (T.cap_ck < n_ck) {
+        dfree(s, &T.ckX);
+        dfree(s, &T.ckV);
+        dfree(s, &T.ckx);
+        T.cap_ck = 0;
+        if ((e = dalloc(s, &T.ckX, (size_t)s->nv * n_ck)) != cudaSuccess) return e;
+        if ((e = dalloc(s, &T.ckV, (size_t)s->nv * n_ck)) != cudaSuccess) return e;
+        if ((e = dalloc(s, &T.ckx, 3 * s->stride * n_ck)) != cudaSuccess) return e;
+        T.cap_ck = n_ck;
+    }
+    const int32_t slots = every * n_buf;
+    if (T.cap_slots < slots) {
+        dfree(s, &T.segX);
+        dfree(s, &T.segV);
+        dfree(s, &T.segx);
+        T.cap_slots = 0;
+        if ((e = dalloc(s, &T.segX, (size_t)s->nv * slots)) != cudaSuccess) return e;
+        if ((e = dalloc(s, &T.segV, (size_t)s->nv * slots)) != cudaSuccess) return e;
+        if ((e = dalloc(s, &T.segx, 3 * s->stride * slots)) != cudaSuccess) return e;
+        T.cap_slots = slots;
+    }
+    return cudaSuccess;
+}
+
+// The taped forward of n steps from the handle's state (either tape).
+oc_status taped_forward(oc_solver* s, float dt) {
+    auto& T = s->tape;
     const bool gm = T.mode == OC_TAPE_DISPLACEMENT;
     T.gm_valid = false;
     if (gm) {  // the start positions and spring constants; the state becomes u = 0
@@ -1936,40 +2014,148 @@ oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t check
         OC_TRY(launch_gm(0, ga, (int)s->nv, s->stream));
         OC_TRY(launch_gm(4, ga, (int)s->nv, s->stream));
     }
-    const size_t nAx = 9 * s->stride;
-    for (int32_t t = 0; t < n_steps; ++t) {
-        const int32_t c = t / every, q = t - c * every;
-        const int32_t len = std::min(n_steps, (c + 1) * every) - c * every;
-        if (q == 0) {
-            oc_status st = copy_state(s, T.ckX + (size_t)c * s->nv, T.ckV + (size_t)c * s->nv,
-                                      T.ckx + 3 * s->stride * c, s->args.X, s->args.V, xplanes(s));
-            if (st != OC_OK) return st;
+    const size_t st = s->stride;
+    for (int32_t t = 0; t < T.n_steps; ++t) {
+        int32_t b = -1, q = 0, len = 0;
+        float4 *sX = nullptr, *sV = nullptr;
+        float* sx = nullptr;
+        if (T.replay) {
+            OC_TRY(launch_tape_save(s->args, T.d_tc, T.arena, t, s->n_blocks, s->stream));
+        } else {
+            const int32_t c = t / T.every;
+            q = t - c * T.every;
+            len = std::min(T.n_steps, (c + 1) * T.every) - c * T.every;
+            if (q == 0) {
+                oc_status st0 = copy_state(s, T.ckX + (size_t)c * s->nv, T.ckV + (size_t)c * s->nv,
+                                           T.ckx + 3 * st * c, s->args.X, s->args.V, xplanes(s));
+                if (st0 != OC_OK) return st0;
+            }
+            b = tape_buffer(T, c);  // a kept segment: its slots as the recompute would fill them
+            if (b >= 0) {
+                sX = T.segX + (size_t)b * T.every * s->nv;
+                sV = T.segV + (size_t)b * T.every * s->nv;
+                sx = T.segx + (size_t)b * T.every * 3 * st;
+                if (q == 0) OC_TRY(launch_snapshot(s->args.X, s->args.V, sX, sV, nullptr, nullptr, s->nv, 0, s->stream));
+            }
         }
-        const int32_t b = tape_buffer(T, c);  // a kept segment: snapshot as the recompute would
-        float4* sX = T.segX + (size_t)b * every * s->nv;
-        float4* sV = T.segV + (size_t)b * every * s->nv;
-        float* sAx = T.segAx + (size_t)b * every * nAx;
-        if (b >= 0 && q == 0)
-            OC_TRY(launch_snapshot(s->args.X, s->args.V, sX, sV, nullptr, nullptr, s->nv, 0, s->stream));
-        oc_status st = gm ? gm_step(s, dt) : oc_step(s, dt, 1);
-        if (st != OC_OK) return st;
-        if (b >= 0) {
+        oc_status r = gm ? gm_step(s, dt) : oc_step(s, dt, 1);
+        if (r != OC_OK) return r;
+        if (T.replay) {
+            OC_TRY(cudaMemcpyAsync(T.dvt + (size_t)t * 3 * st, xplanes(s), 3 * st * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, s->stream));
+        } else if (b >= 0) {
             const bool more = q + 1 < len;
             OC_TRY(launch_snapshot(s->args.X, s->args.V, more ? sX + (size_t)(q + 1) * s->nv : nullptr,
-                                   more ? sV + (size_t)(q + 1) * s->nv : nullptr, s->args.A[0], sAx + nAx * q,
-                                   s->nv, (int64_t)nAx, s->stream));
+                                   more ? sV + (size_t)(q + 1) * s->nv : nullptr, xplanes(s), sx + 3 * st * q,
+                                   s->nv, (int64_t)(3 * st), s->stream));
         }
     }
     if (gm) {  // keep the final displacement, then the state goes back to positions
         OC_TRY(cudaMemcpyAsync(T.finU, s->args.X, sizeof(float4) * (size_t)s->nv, cudaMemcpyDeviceToDevice, s->stream));
         OC_TRY(launch_gm(3, gm_args(s, dt), (int)s->nv, s->stream));
     }
-    oc_status st = copy_state(s, T.finX, T.finV, T.finx, s->args.X, s->args.V, xplanes(s));
-    if (st != OC_OK) return st;
+    oc_status r = copy_state(s, T.finX, T.finV, T.finx, s->args.X, s->args.V, xplanes(s));
+    if (r != OC_OK) return r;
     OC_TRY(cudaStreamSynchronize(s->stream));
-    if ((st = check_device_error(s)) != OC_OK) return st;
+    if ((r = check_device_error(s)) != OC_OK) return r;
     T.valid = true;
     T.gm_valid = gm;
+    return OC_OK;
+}
+
+// Chooses the tape and its intervals, allocates it and runs the taped forward.
+//   every_in != null: the replay tape with those per-cloth intervals.
+//   otherwise: every cloth at the interval `checkpoint_every` (0: ceil(sqrt(n)), which
+//   minimises each cloth's checkpoints plus segment buffer; the replay's cost does not
+//   depend on the interval, and interval 1 would move a copy of the state into every
+//   forward step).  The replay tape when it fits the budget (budget <= 0: when its
+//   buffers can be had); else the recompute tape, keeping as many segments as fit.
+oc_status tape_begin(oc_solver* s, float dt, int32_t n, int32_t checkpoint_every, int64_t budget,
+                     const int32_t* every_in) {
+    if (!valid_solver(s) || n < 1 || checkpoint_every < 0 || !std::isfinite(dt)) return OC_ERR_INVALID_ARGUMENT;
+    if (s->any_passes)
+        return fail(s, OC_ERR_UNSUPPORTED, "oc_tape_forward: the adjoint covers the implicit step only, not the "
+                                           "passes after it");
+    if (s->any_coupled)
+        return fail(s, OC_ERR_UNSUPPORTED, "oc_tape_forward: the adjoint covers the REFERENCE Jacobian mode");
+    OC_TRY(cudaSetDevice(s->device));
+    OC_TRY(cudaStreamSynchronize(s->stream));
+    auto& T = s->tape;
+    T.valid = false;
+    int32_t every = checkpoint_every;
+    if (every == 0) every = std::max(1, (int32_t)std::ceil(std::sqrt((double)n)));
+    every = std::min(every, n);
+    std::vector<int32_t> ev((size_t)s->n_inst, every);
+    bool replay = true;
+    if (every_in) {
+        for (int32_t i = 0; i < s->n_inst; ++i) {
+            if (every_in[i] < 1) return OC_ERR_INVALID_ARGUMENT;
+            ev[(size_t)i] = std::min(every_in[i], n);
+        }
+    } else if (budget > 0 && replay_bytes(s, n, ev) > (double)budget) {
+        replay = false;
+    }
+    if (replay) {
+        free_recompute(s);
+        cudaError_t e = alloc_replay(s, n, ev);
+        if (e == cudaErrorMemoryAllocation && !every_in && budget <= 0) {
+            cudaGetLastError();
+            free_replay(s);
+            replay = false;
+        } else if (e != cudaSuccess) {
+            free_replay(s);
+            return fail_cuda(s, e, "oc_tape_forward: the replay tape's buffers");
+        }
+    }
+    if (!replay) {
+        free_replay(s);
+        const int32_t n_ck = ceil_div(n, every);
+        const double state = tape_state_bytes(s), buf = state * (double)every;
+        const double need = state * (double)(n_ck + 1) + buf;
+        if (budget > 0 && need > (double)budget)
+            return fail(s, OC_ERR_OUT_OF_MEMORY, "oc_tape_forward: checkpoints need " + std::to_string(need) +
+                                                     " bytes, above the budget");
+        // The room left after the checkpoints keeps whole segments from this forward, the
+        // last ones first, so that the reverse pass need not recompute them.
+        int32_t n_buf = 1;
+        if (budget > 0) n_buf = (int32_t)std::min<double>(n_ck, 1.0 + std::floor(((double)budget - need) / buf));
+        T.n_ck = n_ck;
+        T.n_buf = n_buf;
+        T.n_keep = n_buf >= n_ck ? n_ck : n_buf - 1;
+        cudaError_t e = alloc_recompute(s, n_ck, every, n_buf);
+        if (e != cudaSuccess) {
+            free_recompute(s);
+            return fail_cuda(s, e, "oc_tape_forward: the recompute tape's buffers");
+        }
+    }
+    if (oc_status r = alloc_tape_common(s)) return r;
+    T.replay = replay;
+    T.n_steps = n;
+    T.every = every;
+    T.dt = dt;
+    return taped_forward(s, dt);
+}
+
+}  // namespace
+
+extern "C" {
+
+oc_status oc_tape_forward(oc_solver* s, float dt, int32_t n_steps, int32_t checkpoint_every, int64_t budget_bytes) {
+    return tape_begin(s, dt, n_steps, checkpoint_every, budget_bytes, nullptr);
+}
+
+oc_status oc_tape_forward_intervals(oc_solver* s, float dt, int32_t n_steps, const int32_t* every) {
+    if (!every) return OC_ERR_INVALID_ARGUMENT;
+    return tape_begin(s, dt, n_steps, 0, 0, every);
+}
+
+oc_status oc_tape_layout(const oc_solver* s, int32_t* kind, int32_t* every) {
+    if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
+    const auto& T = s->tape;
+    if (!T.valid) return OC_ERR_INVALID_ARGUMENT;
+    if (kind) *kind = T.replay ? OC_TAPE_REPLAY : OC_TAPE_RECOMPUTE;
+    if (every)
+        for (int32_t i = 0; i < s->n_inst; ++i) every[i] = T.replay ? T.tc[(size_t)i].every : T.every;
     return OC_OK;
 }
 
@@ -2048,85 +2234,73 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
     a.blk_base = 0;
     a.use_cond = 0;
     a.all_streamed = 1;
-    // A step's system A comes from the tape, where the recompute left it, unless a
-    // resident cloth assembles in shared memory only (the fused resident kernel): then the
-    // CSR assembly rebuilds every cloth's A.  The displacement mode always tapes its A.
-    const bool split_asm = !(s->resident_fused && !s->buckets.empty());
-    const bool taped_A = split_asm || gm;
-    auto assemble = [&](const StepArgs& b) -> cudaError_t {
-        cudaError_t e = cudaSuccess;
-        if (!split_asm) return launch_kernel(K_ASSEMBLE, b, s->n_blocks, s->stream);
-        StepArgs ba = b, bg = b;
-        ba.blocks = s->d_asm_blocks;
-        bg.blocks = s->d_grid_blocks;
-        if (s->n_asm_blocks > 0) e = launch_kernel(K_ASSEMBLE, ba, s->n_asm_blocks, s->stream);
-        if (e == cudaSuccess && s->n_grid_blocks > 0) e = launch_kernel(K_ASSEMBLE_GRID, bg, s->n_grid_blocks, s->stream);
-        if (e == cudaSuccess && b.n_strip_work > 0) {
-            StepArgs br = b;
-            br.blocks = s->d_sred_blocks;
-            e = launch_kernel(K_ASSEMBLE_STRIP, b, strip_blocks(b.n_strip_work), s->stream);
-            if (e == cudaSuccess) e = launch_kernel(K_ASSEMBLE_REDUCE, br, s->n_sred_blocks, s->stream);
-            if (e == cudaSuccess) e = launch_kernel(K_ASSEMBLE_FINISH, b, b.n_strip_ids, s->stream);
+    // One reverse step on the state b.X, b.V with the step's dV at dv (three planes): the
+    // system's diagonal blocks rebuilt from spring i as the step formed them, the adjoint
+    // seed, lambda = A^-1 g_dV, then the vertex and spring terms.
+    auto reverse_step = [&](const StepArgs& b, const float* dv) -> oc_status {
+        AdjArgs jj = j;
+        for (int k = 0; k < 3; ++k) jj.dV[k] = dv + k * st;
+        if (gm) {
+            OC_TRY(launch_adjoint(0, b, jj, s->n_blocks, s->stream));
+        } else if (s->adj_persist) {
+            OC_TRY(launch_adj_seed_own(b, jj, s->n_blocks, s->stream));
         }
-        return e;
+        if (s->adj_persist) {
+            if (oc_status r = solve_only(s, b)) return r;
+        } else {  // the WHILE-loop graph, its seed node pointed at this step
+            StepArgs bs = b;
+            bs.use_cond = 1;
+            bs.cond = (unsigned long long)T.handle;
+            void* params_seed[] = {&bs, &jj};
+            cudaKernelNodeParams kp{};
+            kp.func = const_cast<void*>(adjoint_seed_own_fn());
+            kp.gridDim = dim3((unsigned)s->n_blocks);
+            kp.blockDim = dim3(256);
+            kp.kernelParams = params_seed;
+            OC_TRY(cudaGraphExecKernelNodeSetParams(T.exec, T.n_seed, &kp));
+            OC_TRY(cudaGraphLaunch(T.exec, s->stream));
+        }
+        OC_TRY(launch_adjoint(1, b, jj, s->n_blocks, s->stream));
+        OC_TRY(launch_adjoint(2, b, jj, s->n_blocks, s->stream));
+        return OC_OK;
     };
-    const size_t nAx = 9 * st;
-    float* live_Ax = s->args.A[0];  // A (6 planes) then x (3 planes)
-    for (int32_t c = T.n_ck - 1; c >= 0; --c) {
-        const int32_t t0 = c * T.every, t1 = std::min(T.n_steps, t0 + T.every), len = t1 - t0;
-        const int32_t kept = tape_buffer(T, c);
-        const int32_t buf = kept >= 0 ? kept : 0;
-        float4* const segX = T.segX + (size_t)buf * T.every * s->nv;
-        float4* const segV = T.segV + (size_t)buf * T.every * s->nv;
-        float* const segAx = T.segAx + (size_t)buf * T.every * nAx;
-        oc_status r = OC_OK;
-        if (kept < 0) {
-            // Recompute the segment from its checkpoint, keeping every step's input state,
-            // system and solution.
-            r = copy_state(s, s->args.X, s->args.V, xplanes(s), T.ckX + (size_t)c * s->nv, T.ckV + (size_t)c * s->nv,
-                           T.ckx + 3 * st * c);
-            if (r != OC_OK) return r;
-            OC_TRY(launch_snapshot(s->args.X, s->args.V, segX, segV, nullptr, nullptr, s->nv, 0, s->stream));
-            for (int32_t q = 0; q < len; ++q) {
-                if ((r = gm ? gm_step(s, T.dt) : oc_step(s, T.dt, 1)) != OC_OK) return r;
-                const bool more = q + 1 < len;
-                OC_TRY(launch_snapshot(s->args.X, s->args.V, more ? segX + (size_t)(q + 1) * s->nv : nullptr,
-                                       more ? segV + (size_t)(q + 1) * s->nv : nullptr, live_Ax, segAx + nAx * q,
-                                       s->nv, (int64_t)nAx, s->stream));
-            }
+    if (T.replay) {
+        // Each step's state is rebuilt into the handle's X, V (the replay tape's view).
+        for (int32_t t = T.n_steps - 1; t >= 0; --t) {
+            OC_TRY(launch_tape_view(a, T.d_tc, T.arena, T.dvt, (int64_t)(3 * st), t, T.n_steps, s->n_blocks,
+                                    s->stream));
+            if (oc_status r = reverse_step(a, T.dvt + (size_t)t * 3 * st)) return r;
         }
-        // And walk it backwards: the kernels read the step's state in place in the tape.
-        for (int32_t q = len - 1; q >= 0; --q) {
-            StepArgs b = a;
-            b.X = segX + (size_t)q * s->nv;
-            b.V = segV + (size_t)q * s->nv;
-            AdjArgs jj = j;
-            float* slot = segAx + nAx * q;
-            for (int k = 0; k < 3; ++k) jj.dV[k] = slot + (6 + k) * st;
-            if (!taped_A)
-                OC_TRY(assemble(b));  // A of this step, rebuilt
-            else if (s->adj_persist)
-                for (int k = 0; k < 6; ++k) b.A[k] = slot + k * st;  // read in place
-            else  // the WHILE graph's nodes read the handle's A planes
-                OC_TRY(cudaMemcpyAsync(live_Ax, slot, 6 * st * sizeof(float), cudaMemcpyDeviceToDevice, s->stream));
-            if (s->adj_persist) {  // lambda = A^-1 g_dV: seed, then the CG alone
-                OC_TRY(launch_adjoint(0, b, jj, s->n_blocks, s->stream));
-                if (oc_status r2 = solve_only(s, b)) return r2;
-            } else {  // the WHILE-loop graph, its seed node pointed at this step
-                StepArgs bs = b;
-                bs.use_cond = 1;
-                bs.cond = (unsigned long long)T.handle;
-                void* params_seed[] = {&bs, &jj};
-                cudaKernelNodeParams kp{};
-                kp.func = const_cast<void*>(adjoint_seed_fn());
-                kp.gridDim = dim3((unsigned)s->n_blocks);
-                kp.blockDim = dim3(256);
-                kp.kernelParams = params_seed;
-                OC_TRY(cudaGraphExecKernelNodeSetParams(T.exec, T.n_seed, &kp));
-                OC_TRY(cudaGraphLaunch(T.exec, s->stream));
+    } else {
+        for (int32_t c = T.n_ck - 1; c >= 0; --c) {
+            const int32_t t0 = c * T.every, t1 = std::min(T.n_steps, t0 + T.every), len = t1 - t0;
+            const int32_t kept = tape_buffer(T, c);
+            const int32_t buf = kept >= 0 ? kept : 0;
+            float4* const segX = T.segX + (size_t)buf * T.every * s->nv;
+            float4* const segV = T.segV + (size_t)buf * T.every * s->nv;
+            float* const segx = T.segx + (size_t)buf * T.every * 3 * st;
+            if (kept < 0) {
+                // Recompute the segment from its checkpoint, keeping every step's input state
+                // and solution.
+                oc_status r = copy_state(s, s->args.X, s->args.V, xplanes(s), T.ckX + (size_t)c * s->nv,
+                                         T.ckV + (size_t)c * s->nv, T.ckx + 3 * st * c);
+                if (r != OC_OK) return r;
+                OC_TRY(launch_snapshot(s->args.X, s->args.V, segX, segV, nullptr, nullptr, s->nv, 0, s->stream));
+                for (int32_t q = 0; q < len; ++q) {
+                    if ((r = gm ? gm_step(s, T.dt) : oc_step(s, T.dt, 1)) != OC_OK) return r;
+                    const bool more = q + 1 < len;
+                    OC_TRY(launch_snapshot(s->args.X, s->args.V, more ? segX + (size_t)(q + 1) * s->nv : nullptr,
+                                           more ? segV + (size_t)(q + 1) * s->nv : nullptr, xplanes(s),
+                                           segx + 3 * st * q, s->nv, (int64_t)(3 * st), s->stream));
+                }
             }
-            OC_TRY(launch_adjoint(1, b, jj, s->n_blocks, s->stream));
-            OC_TRY(launch_adjoint(2, b, jj, s->n_blocks, s->stream));
+            // And walk it backwards: the kernels read the step's state in place in the tape.
+            for (int32_t q = len - 1; q >= 0; --q) {
+                StepArgs b = a;
+                b.X = segX + (size_t)q * s->nv;
+                b.V = segV + (size_t)q * s->nv;
+                if (oc_status r = reverse_step(b, segx + 3 * st * q)) return r;
+            }
         }
     }
     oc_status r = copy_state(s, s->args.X, s->args.V, xplanes(s), T.finX, T.finV, T.finx);
@@ -2444,11 +2618,17 @@ oc_status oc_test_barrier_timeout(oc_solver* s, int32_t withhold_block, uint32_t
 oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* tape_bytes) {
     if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
     const auto& T = s->tape;
-    const size_t state_bytes = 2 * sizeof(float4) * (size_t)s->nv + 3 * s->stride * sizeof(float);
     if (checkpoint_every) *checkpoint_every = T.every;
-    const size_t seg_bytes = 2 * sizeof(float4) * (size_t)s->nv + 9 * s->stride * sizeof(float);
-    if (tape_bytes)
-        *tape_bytes = (int64_t)(state_bytes * (size_t)(T.n_ck + 1) + seg_bytes * (size_t)T.every * (size_t)T.n_buf);
+    if (tape_bytes) {
+        if (T.replay) {
+            std::vector<int32_t> ev((size_t)s->n_inst);
+            for (int32_t i = 0; i < s->n_inst; ++i) ev[(size_t)i] = T.tc.empty() ? 1 : T.tc[(size_t)i].every;
+            *tape_bytes = (int64_t)replay_bytes(s, T.n_steps, ev);
+        } else {
+            const double state = tape_state_bytes(s);
+            *tape_bytes = (int64_t)(state * (double)(T.n_ck + 1) + state * (double)T.every * (double)T.n_buf);
+        }
+    }
     return OC_OK;
 }
 

@@ -174,9 +174,42 @@ struct AdjArgs {
     const int32_t* own_sid;  // vertex i -> id of spring i, or -1
     const int32_t* own_rowptr;  // vertex -> vertices whose spring touches it
     const int32_t* own_ent;     // that vertex | (1 << 31 when the vertex is the spring's p2)
+    int32_t springs_variant;    // k_adj_springs' launch variant (OC_ADJ_SPRINGS_VARIANT; 0 default)
+    int32_t vertex_variant;     // k_adj_vertex's launch variant (OC_ADJ_VERTEX_VARIANT; 0 default)
 };
 
+// Adjoint kernels (oc_adjoint.cu) over the blocks a.blocks[blk_base, blk_base + nblocks):
+//   0 the displacement mode's seed (spring i's blocks rebuilt, adj_seed_vertex);
+//   1 the vertex terms (k_adj_vertex); 2 the spring terms (k_adj_springs).
 cudaError_t launch_adjoint(int which, const StepArgs& a, const AdjArgs& j, int nblocks, cudaStream_t stream);
+
+// The replay tape of one cloth (oc_tape_forward).  The forward keeps the solution dV of
+// every step; the cloth's state (X then V, nv float4 each) is kept every `every` steps
+// (checkpoint c at arena + ck + 2 nv c) and the reverse pass rebuilds the states in
+// between by replaying the update, which given dV is elementwise and exact; segment
+// slot s lives at arena + buf + 2 nv s (every > 1 only).
+struct TapeCloth {
+    int32_t every;
+    int32_t pad;
+    int64_t ck;
+    int64_t buf;
+};
+
+// Replay tape kernels (oc_kernels.cu), over the full block table a.blocks[0, nblocks):
+//   save  the state of step t (before it) into the checkpoints that fall on t;
+//   view  the state of step t into a.X, a.V: from the checkpoint, the segment slot, or
+//         (at a segment's last step) by replaying the segment from its checkpoint with
+//         the taped dV (dvt + step * dv_stride, three planes of a.x's stride), filling
+//         the slots; a.gm selects the displacement mode's update;
+//   seed  the adjoint seed with the system's diagonal blocks rebuilt from spring i
+//         (own_blocks, as every assembly forms them): A planes written, then
+//         adj_seed_vertex and the assembly epilogue.
+cudaError_t launch_tape_save(const StepArgs& a, const TapeCloth* tc, float4* arena, int32_t t, int nblocks,
+                             cudaStream_t stream);
+cudaError_t launch_tape_view(const StepArgs& a, const TapeCloth* tc, float4* arena, const float* dvt,
+                             int64_t dv_stride, int32_t t, int32_t n_steps, int nblocks, cudaStream_t stream);
+cudaError_t launch_adj_seed_own(const StepArgs& a, const AdjArgs& j, int nblocks, cudaStream_t stream);
+const void* adjoint_seed_own_fn();
 // Displacement mode kernels (oc_adjoint.cu).  Per vertex (n = the vertex count):
 //   0 Xbase = X;  4 the spring constants gm_inc, gm_own from Xbase and X = (0, 0, 0, mass);
 //   3 X = Xbase + u.  Over the blocks a.blocks[blk_base, blk_base + n):
@@ -187,7 +220,6 @@ cudaError_t launch_gm(int which, const StepArgs& a, int n, cudaStream_t stream);
 // of x into dx (skipped when dx is null).
 cudaError_t launch_snapshot(const float4* X, const float4* V, float4* dX, float4* dV, const float* x, float* dx,
                             int64_t nv, int64_t nx, cudaStream_t stream);
-const void* adjoint_seed_fn();
 cudaError_t launch_set_spring_params(const StepArgs& a, const AdjArgs& j, const float* ks, const float* kd,
                                      int64_t n_rec, int64_t nv, cudaStream_t stream);
 

@@ -812,6 +812,82 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, in
     }
 }
 
+// ---- the replay tape ---------------------------------------------------------------
+// Given the step's solution dV, the update (IMP:790-797) is elementwise: the forward
+// keeps dV of every step and a cloth's (X, V) every `every` steps, and the reverse pass
+// rebuilds any step's state from the checkpoint before it with the same update function
+// the step used, bit for bit, instead of re-running the step's assembly and CG.
+
+__global__ void __launch_bounds__(kThreads) k_tape_save(const StepArgs a, const TapeCloth* tc, float4* arena,
+                                                        int32_t t) {
+    const BlockInfo bi = a.blocks[blockIdx.x];
+    const TapeCloth c = tc[bi.inst];
+    if (t % c.every != 0) return;
+    const InstParams& ip = a.inst[bi.inst];
+    float4* dst = arena + c.ck + (int64_t)(t / c.every) * 2 * ip.nv;
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const int64_t l = g - ip.v_off;
+        dst[l] = a.X[g];
+        dst[ip.nv + l] = a.V[g];
+    }
+}
+
+template <bool GM>
+__global__ void __launch_bounds__(kThreads) k_tape_view(const StepArgs a, const TapeCloth* tc, float4* arena,
+                                                        const float* dvt, int64_t dv_stride, int32_t t,
+                                                        int32_t n_steps) {
+    const BlockInfo bi = a.blocks[blockIdx.x];
+    const TapeCloth c = tc[bi.inst];
+    const InstParams& ip = a.inst[bi.inst];
+    const int64_t nv = ip.nv, ps = a.x[1] - a.x[0];  // plane stride
+    const int32_t seg = t / c.every, q = t - seg * c.every;
+    const int32_t len = min(n_steps, (seg + 1) * c.every) - seg * c.every;
+    const float4* ck = arena + c.ck + (int64_t)seg * 2 * nv;
+    float4* buf = arena + c.buf;
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const int64_t l = g - ip.v_off;
+        float4 X, V;
+        if (q == 0) {
+            X = ck[l];
+            V = ck[nv + l];
+        } else if (q < len - 1) {
+            X = buf[(int64_t)q * 2 * nv + l];
+            V = buf[(int64_t)q * 2 * nv + nv + l];
+        } else {  // the segment's last step: replay it from the checkpoint, filling the slots
+            X = ck[l];
+            V = ck[nv + l];
+            const float by = GM ? __ldg(a.Xbase + g).y : 0.0f;
+            for (int32_t k = 1; k <= q; ++k) {
+                const float* d = dvt + (int64_t)(seg * c.every + k - 1) * dv_stride;
+                if constexpr (GM)
+                    gm_advance(a.dt, d[g], d[ps + g], d[2 * ps + g], by, X, V);
+                else
+                    update_vertex(ip, a.dt, d[g], d[ps + g], d[2 * ps + g], X, V);
+                if (k < q) {
+                    buf[(int64_t)k * 2 * nv + l] = X;
+                    buf[(int64_t)k * 2 * nv + nv + l] = V;
+                }
+            }
+        }
+        a.X[g] = X;
+        a.V[g] = V;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_adj_seed_own(const StepArgs a, const AdjArgs j) {
+    const int blk = blockIdx.x + a.blk_base;
+    const BlockInfo bi = a.blocks[blk];
+    Acc part = acc_zero();
+    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
+        const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
+        const OwnBlocks ob = own_blocks(a.dt, Xg.w, load_own<true>(a, g));
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.A[k][g] = ob.A[k];
+        acc_add(part, adj_seed_vertex(a, j, g, Xg, Vg, ob.A[0], ob.A[3], ob.A[5]));
+    }
+    finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
+}
+
 __global__ void k_snapshot(const float4* X, const float4* V, float4* dX, float4* dV, const float* x, float* dx,
                            int64_t nv, int64_t nx) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -1149,6 +1225,31 @@ cudaError_t launch_snapshot(const float4* X, const float4* V, float4* dX, float4
     k_snapshot<<<blocks, kThreads, 0, stream>>>(X, V, dX, dV, x, dx, nv, nx);
     return cudaGetLastError();
 }
+
+cudaError_t launch_tape_save(const StepArgs& a, const TapeCloth* tc, float4* arena, int32_t t, int nblocks,
+                             cudaStream_t stream) {
+    if (nblocks <= 0) return cudaSuccess;
+    k_tape_save<<<nblocks, kThreads, 0, stream>>>(a, tc, arena, t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tape_view(const StepArgs& a, const TapeCloth* tc, float4* arena, const float* dvt,
+                             int64_t dv_stride, int32_t t, int32_t n_steps, int nblocks, cudaStream_t stream) {
+    if (nblocks <= 0) return cudaSuccess;
+    if (a.gm)
+        k_tape_view<true><<<nblocks, kThreads, 0, stream>>>(a, tc, arena, dvt, dv_stride, t, n_steps);
+    else
+        k_tape_view<false><<<nblocks, kThreads, 0, stream>>>(a, tc, arena, dvt, dv_stride, t, n_steps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adj_seed_own(const StepArgs& a, const AdjArgs& j, int nblocks, cudaStream_t stream) {
+    if (nblocks <= 0) return cudaSuccess;
+    k_adj_seed_own<<<nblocks, kThreads, 0, stream>>>(a, j);
+    return cudaGetLastError();
+}
+
+const void* adjoint_seed_own_fn() { return (const void*)k_adj_seed_own; }
 
 cudaError_t launch_cg_persist(const StepArgs& a, int32_t n_entries, int grid, unsigned* words, int* err,
                               cudaStream_t stream) {

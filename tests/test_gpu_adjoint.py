@@ -20,15 +20,17 @@ from opencloth_gb300 import ClothDesc, ClothSolver
 pytestmark = pytest.mark.gpu
 
 
-def gpu_grads(case, every=10, executor="auto", cg_tol=1e-6, budget=0, info=None):
+def gpu_grads(case, every=10, executor="auto", cg_tol=1e-6, budget=0, info=None, intervals=None, layout=None):
     desc = ClothDesc(n_vertices=len(case["X"]), springs=case["springs"], pinned=case["pins"], cg_max_iter=500,
                      cg_tol=cg_tol)
     with ClothSolver(desc, executor=executor) as s:
         s.set_ext_force(case["ext"])
         s.set_state(case["X"], case["V0"], np.zeros_like(case["X"]))
-        s.tape_forward(DT, case["steps"], every, budget)
+        s.tape_forward(DT, case["steps"], every, budget, intervals=intervals)
         if info is not None:
             info.append(s.tape_info())
+        if layout is not None:
+            layout.append(s.tape_layout())
         X, _, _ = s.get_state()
         gX = 2.0 * (X - case["target"]) / len(X)
         g = s.tape_backward(gX)
@@ -112,18 +114,66 @@ def test_checkpoint_interval_does_not_change_gradients(case):
         assert np.array_equal(ga[k], gb[k]) and np.array_equal(ga[k], gc[k]), k
 
 
-def test_kept_segments_do_not_change_gradients(case):
-    """With a byte budget the taped forward keeps its last segments' step states and the
-    reverse pass walks them without a recompute: the same gradients bit for bit, whether
-    no segment, some or all of them are kept."""
-    info = []
-    ga, _ = gpu_grads(case, every=10, info=info)
-    base = info[-1][1]
-    gb, _ = gpu_grads(case, every=10, budget=3 * base, info=info)
-    gc, _ = gpu_grads(case, every=10, budget=1 << 30, info=info)
-    assert base < info[1][1] < info[2][1]  # some segments kept, then all
-    for k in ga:
-        assert np.array_equal(ga[k], gb[k]) and np.array_equal(ga[k], gc[k]), k
+def state_bytes(nv):
+    """Bytes of one state of a cloth in the recompute tape: X and V (float4) and three
+    planes of the handle's plane stride (the vertex count rounded up to 64)."""
+    return 32 * nv + 12 * ((nv + 63) // 64 * 64)
+
+
+def test_tapes_and_intervals_give_the_same_gradients(case):
+    """The replay tape (the default interval, and intervals 1 and 7) and the recompute tape
+    (no segment kept from the forward, and some): the same gradients bit for bit.  The
+    replay tape rebuilds each state from its checkpoint with the step's own update; the
+    recompute tape re-runs the steps; either way the reverse pass sees the same states."""
+    st, every = state_bytes(len(case["X"])), 10
+    n_ck = -(-case["steps"] // every)
+    lay = []
+    g0, _ = gpu_grads(case, every=every, layout=lay)
+    runs = [gpu_grads(case, intervals=[1], layout=lay), gpu_grads(case, intervals=[7], layout=lay),
+            gpu_grads(case, every=every, budget=st * (n_ck + 1 + every), layout=lay),
+            gpu_grads(case, every=every, budget=st * (n_ck + 1 + 6 * every), layout=lay)]
+    assert [k for k, _ in lay] == ["replay"] * 3 + ["recompute"] * 2
+    assert [e.tolist() for _, e in lay[:3]] == [[every], [1], [7]]
+    for g, _ in runs:
+        for k in g0:
+            assert np.array_equal(g0[k], g[k]), k
+
+
+def test_per_cloth_intervals_give_the_same_gradients(case):
+    """A batch of three cloths on the replay tape with a different interval per cloth: the
+    same gradients bit for bit as one interval for all; under a byte budget that holds
+    the replay tape, every cloth gets the default interval ceil(sqrt(steps))."""
+    cases = [case, make_case(cols=9, rows=11, steps=case["steps"], seed=8),
+             make_case(cols=12, rows=6, steps=case["steps"], seed=9)]
+    descs = [ClothDesc(n_vertices=len(c["X"]), springs=c["springs"], pinned=c["pins"], cg_max_iter=500, cg_tol=1e-6)
+             for c in cases]
+
+    def grads(**kw):
+        with ClothSolver(descs) as s:
+            s.set_ext_force(np.concatenate([c["ext"] for c in cases]))
+            s.set_state(np.concatenate([c["X"] for c in cases]), np.concatenate([c["V0"] for c in cases]))
+            s.tape_forward(DT, case["steps"], 10, **kw)
+            layout, info = s.tape_layout(), s.tape_info()
+            X, _, _ = s.get_state()
+            off = s.offsets
+            gX = np.concatenate([2.0 * (X[off[k]:off[k + 1]] - c["target"]) / len(c["X"])
+                                 for k, c in enumerate(cases)])
+            return s.tape_backward(gX), layout, info
+
+    g0, lay0, info0 = grads()
+    assert lay0[0] == "replay" and lay0[1].tolist() == [10, 10, 10]
+    g1, lay1, _ = grads(intervals=[1, 13, 200])
+    assert lay1[1].tolist() == [1, 13, 200]
+    g2, lay2, info2 = grads(intervals=[7, 1, 3])
+    assert lay2[1].tolist() == [7, 1, 3]
+    with ClothSolver(descs) as s:
+        s.set_state(np.concatenate([c["X"] for c in cases]), np.concatenate([c["V0"] for c in cases]))
+        s.tape_forward(DT, case["steps"], 0, info0[1])
+        kind, ev = s.tape_layout()
+        assert kind == "replay" and ev.tolist() == [15, 15, 15] and s.tape_info()[1] <= info0[1]
+    for g in (g1, g2):
+        for k in g0:
+            assert np.array_equal(g0[k], g[k]), k
 
 
 def test_streamed_and_resident_forward_give_the_same_gradients(case):
