@@ -530,33 +530,6 @@ def tune_cache_path() -> str:
     return str(d / "tune.txt")
 
 
-def adjoint_workload(name: str, seed: int):
-    """The differentiable configurations: one 257 x 257 cloth (200 steps, checkpoint every
-    20) and 512 cloths with sides uniform in [16,256] (100 steps, checkpoints chosen
-    under a 40 GB budget).  Targets are final positions of a run whose per-spring Ks carry
-    log-normal(0, 0.1^2) factors; the loss is the mean squared distance to them."""
-    from opencloth_gb300 import ClothDesc, grid_cloth
-
-    rng = np.random.default_rng(seed)
-    if name == "grid257":
-        sides, steps, every = [257], 200, 20
-    else:
-        sides, steps, every = list(rng.integers(16, 257, 512)), 100, 0
-    descs, Xs, ks_t = [], [], []
-    for k, n in enumerate(sides):
-        n = int(n)
-        if name == "grid257":
-            ks, kd = (50.75, 50.75, 50.95), (-0.25, -0.25, -0.25)
-        else:
-            ks, kd = tuple(np.exp(rng.uniform(np.log(10.0), np.log(500.0), 3))), tuple(rng.uniform(-0.5, -0.05, 3))
-        X, sp = grid_cloth(n, n, ks=ks, kd=kd, jitter=1e-3, seed=seed * 7 + k)
-        descs.append(ClothDesc(n_vertices=n * n, springs=sp, pinned=np.array([0, n - 1], np.int32),
-                               cg_max_iter=200, cg_tol=1e-5))
-        Xs.append(X)
-        ks_t.append((sp["ks"] * np.exp(rng.normal(0.0, 0.1, len(sp)))).astype(np.float32))
-    return descs, np.concatenate(Xs), np.concatenate(ks_t), steps, every
-
-
 def measure_adjoint(name: str, seed: int, local: int) -> dict:
     """Forward, taped forward and reverse pass times of one gradient evaluation: the
     reverse pass with the gradients left on the device (backward_ms) and with all of them
@@ -564,6 +537,8 @@ def measure_adjoint(name: str, seed: int, local: int) -> dict:
     import torch
 
     from opencloth_gb300 import ClothSolver
+
+    from opencloth_gb300.profile_adjoint import adjoint_workload
 
     descs, X0, ks_target, steps, every = adjoint_workload(name, seed)
     nv = len(X0)
