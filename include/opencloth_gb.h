@@ -290,7 +290,7 @@ typedef struct oc_launch_config {
     int32_t resident_vcta;         /* vertices per resident CTA: 256, 512, 1024 or 2048 */
     int32_t resident_threads;      /* threads per resident CTA: 128, 256 or 512, with vcta <= 4 x threads */
     int32_t resident_fused;        /* 1: resident cloths assemble inside the resident kernel */
-    int32_t persist;               /* 1: the CG of up to 16 streamed cloths as one cooperative launch */
+    int32_t persist;               /* 1: the CG of the streamed cloths as one cooperative launch */
     int32_t gather_variant;        /* incidence-record force gather: 0 block-cooperative, 1..6 per vertex */
     int32_t strip;                 /* 1: grid cloths in the reference's spring order take the strip sweep */
     int32_t strip_rows;            /* rows per strip band (1 ... 64); 0: chosen from the work size */

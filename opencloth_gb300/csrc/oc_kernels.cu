@@ -642,8 +642,9 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
 // The cloths are independent, so there is no grid barrier: each cloth has its own
 // completion word.  Phase q of a cloth is the direction pass (q even) or the update pass
 // (q odd) of iteration q / 2.  An entry's pass of phase q starts once its cloth's word
-// reads at least q (phase q - 1 complete).  Every entry then arrives at its cloth's
-// ticket; the block that makes the cloth's last arrival of the phase sums the cloth's
+// reads at least q (phase q - 1 complete).  The entries then arrive at their cloth's
+// ticket (a block's consecutive entries of one cloth with one atomic add of their
+// count); the block that makes the cloth's last arrival of the phase sums the cloth's
 // partials in the last-block epilogue's fixed order, applies the epilogue's scalar rule
 // to the cloth's state and publishes the word (q + 1, or kPhaseDone when the cloth's
 // loop has ended).  Totals, scalars and decisions are those of the two-kernel loop bit
@@ -768,13 +769,22 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, in
             s_ok = 0;
             break;
         }
-        // Arrivals: thread j publishes entry j's partial and arrives at its cloth's ticket.
+        // Arrivals: the owned entries of one cloth are consecutive (the table is in cloth
+        // order), so the thread of a run's first entry publishes the run's partials and
+        // arrives once at the cloth's ticket with the run's length.
         for (int j = threadIdx.x; j < own; j += blockDim.x) {
             if (!s_run[j]) continue;
-            const BlockInfo bi = a.blocks[blockIdx.x + j * gridDim.x];
-            a.partials[bi.gblk] = s_part[j];
-            const unsigned t = atom_add_acq_rel(&a.state[bi.inst].ticket, 1u);
-            if (t == (unsigned)(a.inst[bi.inst].nblk - 1)) s_last[atomicAdd(&s_nlast, 1)] = (short)j;
+            const int inst = a.blocks[blockIdx.x + j * gridDim.x].inst;
+            if (j > 0 && a.blocks[blockIdx.x + (j - 1) * gridDim.x].inst == inst) continue;
+            unsigned n = 0;
+            for (int k = j; k < own; ++k) {
+                const BlockInfo bk = a.blocks[blockIdx.x + k * gridDim.x];
+                if (bk.inst != inst) break;
+                a.partials[bk.gblk] = s_part[k];
+                ++n;
+            }
+            const unsigned t = atom_add_acq_rel(&a.state[inst].ticket, n);
+            if (t + n == (unsigned)a.inst[inst].nblk) s_last[atomicAdd(&s_nlast, 1)] = (short)j;
         }
         __syncthreads();
         // The cloths this block completed: totals in the epilogue's order, rule, publish.
