@@ -8,10 +8,11 @@
 // k_assemble left in the planes.  The CG loop touches no HBM and needs no per-iteration
 // launch.  Unfused with a.cg_only, the kernel is the adjoint solve of a resident cloth:
 // the CG state k_adj_seed left in the planes in, the solution out, no update.
-// Dot products reduce per CTA (Acc pairs within warps, FP64 above), then in FP64 across
-// the cluster through distributed shared memory after a hardware cluster barrier, in
-// the same fixed order in every CTA, so all of them take identical decisions.  There
-// are no spin-waits.
+// Dot products reduce per CTA and then across the cluster through distributed shared
+// memory after a hardware cluster barrier, as error-free float pairs (about 48 bits, the
+// role FP64 plays in the streamed kernels), in the same fixed order in every CTA, so all
+// of them take identical decisions; alpha and beta are the pairs' quotients rounded to
+// float.  There are no spin-waits.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -25,8 +26,8 @@ namespace {
 
 // Sum over the CTA, then over the cluster (C CTAs), carried as error-free float pairs
 // (Acc: the running sum and its exact rounding errors, about 48 significant bits) up to
-// the cluster total, which thread 0 turns into one FP64 value.  FP64 is slow on this GPU
-// and these reductions are the serial part of every CG iteration, so no level uses it.
+// the cluster total.  FP64 is slow on this GPU and these reductions and the scalars after
+// them are the serial part of every CG iteration, so no level uses it.
 // The CTA's warps merge in a fixed tree in warp 0.  Each CTA then pushes its pair into
 // slot [rank] of every CTA of the cluster (lane r of warp 0 stores into CTA r's shared
 // memory), one cluster barrier makes the pushes visible, and every CTA merges its C local
@@ -40,7 +41,7 @@ __device__ __forceinline__ Acc shfl_acc(Acc v, int o) {
     return u;
 }
 
-__device__ double cluster_sum(Acc part, int C, Acc (*slots)[kResidentMaxCluster], int& phase) {
+__device__ Acc cluster_sum(Acc part, int C, Acc (*slots)[kResidentMaxCluster], int& phase) {
     __shared__ Acc warp_part[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
@@ -70,7 +71,37 @@ __device__ double cluster_sum(Acc part, int C, Acc (*slots)[kResidentMaxCluster]
         }
     }
     ++phase;
-    return (double)v.s + (double)v.c;
+    return v;
+}
+
+// The CG's scalar arithmetic on the pairs, with no FP64 (one FP64 division costs a
+// resident CTA about a tenth of its time on this GPU).  norm: the pair's value as
+// hi + lo with hi = fl(hi + lo) (TwoSum).  div: the quotient of two normalised pairs,
+// rounded to float: q0 = fl(a.hi / b.hi), the exact remainder a - q0 b (an FMA for the
+// head product, Sterbenz for the subtraction), then q0 + remainder / b.hi rounded once;
+// it is the correctly rounded quotient unless the exact one lies within about 2^-46 of a
+// rounding boundary.  gt: a > b for normalised pairs.
+__device__ __forceinline__ Acc pair_norm(Acc a) {
+    const float s = a.s + a.c;
+    const float bp = s - a.s;
+    return make_acc(s, (a.s - (s - bp)) + (a.c - bp));
+}
+
+__device__ __forceinline__ float pair_div(Acc a, Acc b) {
+    const float q0 = __fdiv_rn(a.s, b.s);
+    const float ph = __fmul_rn(q0, b.s);
+    const float pl = __fmaf_rn(q0, b.s, -ph);
+    const float r = (((a.s - ph) - pl) + a.c) - __fmul_rn(q0, b.c);
+    return __fadd_rn(q0, __fdiv_rn(r, b.s));
+}
+
+__device__ __forceinline__ bool pair_gt(Acc a, Acc b) { return a.s > b.s || (a.s == b.s && a.c > b.c); }
+
+__device__ __forceinline__ bool pair_finite(Acc a) { return isfinite(a.s) && isfinite(a.c); }
+
+__device__ __forceinline__ Acc pair_from(double x) {
+    const float h = (float)x;
+    return make_acc(h, (float)(x - (double)h));
 }
 
 // Resident CTAs per SM the register budget is set for: 128-thread CTAs hold up to 512
@@ -85,8 +116,8 @@ template <int T, bool FUSED>
 __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const StepArgs a, const ResidentLaunch L) {
     extern __shared__ __align__(16) float smem[];
     __shared__ Acc slots[2][kResidentMaxCluster];
-    // The CG scalars live in thread 0 (FP64 is slow on this GPU: one thread does the
-    // divisions and tests); the other threads get alpha, beta and the go / stop decision.
+    // The CG scalars live in thread 0 (one thread does the divisions and tests, on float
+    // pairs); the other threads get alpha, beta and the go / stop decision.
     __shared__ float s_alpha, s_beta;
     __shared__ int s_go;
     const int C = L.cluster;
@@ -111,7 +142,9 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
 
     int phase = 0;
     Acc part;
-    double delta0 = 0.0, delta = 0.0, thresh = 0.0;  // thread 0's
+    // Thread 0's: delta0 (FP64, set once), and the iteration's r.r and threshold as pairs.
+    double delta0 = 0.0;
+    Acc delta = acc_zero(), thresh = acc_zero();
     uint32_t flags = 0u;                             // thread 0's
     if constexpr (FUSED) {
         // The assembly of these vertices (k_assemble / k_assemble_grid); X and V are
@@ -141,8 +174,9 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
         // delta0 and the decision to iterate, as the assembly's last-block epilogue takes
         // them (finish<K_ASSEMBLE>).  The cluster reduction also orders every CTA's reads
         // of X and V before any CTA's writes below.
-        const double total = cluster_sum(part, C, slots, phase);
+        const Acc tp = pair_norm(cluster_sum(part, C, slots, phase));
         if (threadIdx.x == 0) {
+            const double total = (double)tp.s + (double)tp.c;
             delta0 = total;
             bool run = (0 < ip.imax) && (total > (double)ip.eps2 * total);
             if (!isfinite(total)) {
@@ -178,8 +212,8 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
     __syncthreads();
     bool run = s_go != 0;
     if (threadIdx.x == 0) {
-        delta = delta0;
-        thresh = (double)ip.eps2 * delta0;
+        delta = pair_from(delta0);
+        thresh = pair_from((double)ip.eps2 * delta0);
     }
     int it = 0;
     float beta = 0.0f;
@@ -200,13 +234,13 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
             matvec(A, d[u][0], d[u][1], d[u][2], q0, q1, q2);
             acc_add(part, d[u][0] * q0 + d[u][1] * q1 + d[u][2] * q2);
         }
-        const double dq = cluster_sum(part, C, slots, phase);
+        const Acc dq = pair_norm(cluster_sum(part, C, slots, phase));
         if (threadIdx.x == 0) {
-            if (!(dq > 0.0) || !isfinite(dq)) {
-                flags |= isfinite(dq) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
+            if (!(dq.s > 0.0f) || !pair_finite(dq)) {
+                flags |= pair_finite(dq) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
                 s_go = 0;
             } else {
-                s_alpha = (float)(delta / dq);
+                s_alpha = pair_div(delta, dq);
                 s_go = 1;
             }
         }
@@ -229,18 +263,18 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
             }
             acc_add(part, r[u][0] * r[u][0] + r[u][1] * r[u][1] + r[u][2] * r[u][2]);
         }
-        const double rr = cluster_sum(part, C, slots, phase);
+        const Acc rr = pair_norm(cluster_sum(part, C, slots, phase));
         ++it;
         if (threadIdx.x == 0) {
-            const double old = delta;
+            const Acc old = delta;
             delta = rr;
-            s_beta = (float)(delta / old);
+            s_beta = pair_div(delta, old);
             int go = 1;
-            if (!isfinite(delta)) {
+            if (!pair_finite(delta)) {
                 flags |= OC_FLAG_NON_FINITE;
                 go = 0;
-            } else if (!(it < ip.imax && delta > thresh)) {
-                if (delta > thresh) flags |= OC_FLAG_NOT_CONVERGED;
+            } else if (!(it < ip.imax && pair_gt(delta, thresh))) {
+                if (pair_gt(delta, thresh)) flags |= OC_FLAG_NOT_CONVERGED;
                 go = 0;
             }
             s_go = go;
@@ -271,7 +305,7 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
     if (rank == 0 && threadIdx.x == 0) {
         InstState& st = a.state[inst];
         st.delta0 = delta0;
-        st.delta_new = delta;
+        st.delta_new = (double)delta.s + (double)delta.c;
         st.dq = 0.0;
         st.iter = it;
         st.flags = flags;
