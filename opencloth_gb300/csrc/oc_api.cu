@@ -62,11 +62,9 @@ struct oc_solver {
     int32_t n_asm_blocks = 0;
     BlockInfo* d_grid_blocks = nullptr;  // REFERENCE grid cloths on the stencil gather
     int32_t n_grid_blocks = 0;
-    // Grid cloths on the strip sweep (k_assemble_strip, then k_assemble_reduce over their
-    // standard blocks and k_assemble_finish per cloth): the work items (in
-    // args.strip_work), each cloth's range of them and its index in args.strip_ids.
-    BlockInfo* d_sred_blocks = nullptr;
-    int32_t n_sred_blocks = 0;
+    // Grid cloths on the strip sweep (k_assemble_strip, then k_assemble_finish per cloth):
+    // the work items (in args.strip_work), each cloth's range of them and its index in
+    // args.strip_ids.
     std::vector<std::pair<int32_t, int32_t>> strip_range;
     std::vector<int32_t> strip_pos;
     // The launch configuration (oc_launch_config) and what re-planning needs: the full
@@ -305,10 +303,9 @@ void account_step_bytes(const oc_solver* s, KernelTimer* t) {
         // Assembled by k_resident (fused) or by the COUPLED kernels: no assembly bytes here.
         const bool fused = (s->resident[k] && s->resident_fused) || s->inst_host[k].coupled;
         if (!fused && s->inst_host[k].strip) {
-            // The strip sweep: k_assemble_grid's bytes plus the delta0 term written, rest
-            // lengths (when they vary) as six planes by anchor; k_assemble_reduce reads the terms.
-            t->bytes[K_ASSEMBLE_STRIP] += 120.0 * nv + (s->inst_host[k].st_rest ? 24.0 * nv : 0.0);
-            t->bytes[K_ASSEMBLE_REDUCE] += 4.0 * nv;
+            // The strip sweep: k_assemble_grid's bytes, rest lengths (when they vary) as six
+            // planes by anchor.
+            t->bytes[K_ASSEMBLE_STRIP] += 116.0 * nv + (s->inst_host[k].st_rest ? 24.0 * nv : 0.0);
         } else if (!fused && s->inst_host[k].grid_cols > 0)  // no incidence records, no row pointer
             t->bytes[K_ASSEMBLE_GRID] +=              // unless rest lengths are per incidence
                 116.0 * nv + (s->inst_host[k].st_rest ? 4.0 * nv + 8.0 * ns : 0.0);
@@ -433,12 +430,12 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
                 StepArgs w = a;
                 w.strip_work = s->args.strip_work + s->strip_range[(size_t)grp].first;
                 w.n_strip_work = s->strip_range[(size_t)grp].second;
+                w.strip_item0 = s->strip_range[(size_t)grp].first;
                 if ((st = launch_timed(s, K_ASSEMBLE_STRIP, w, strip_blocks(w.n_strip_work), t)) != OC_OK) return st;
-                if ((st = launch_timed(s, K_ASSEMBLE_REDUCE, a, nb, t)) != OC_OK) return st;
                 StepArgs fa = a;
                 fa.strip_ids = s->args.strip_ids + s->strip_pos[(size_t)grp];
                 if ((st = launch_timed(s, K_ASSEMBLE_FINISH, fa, 1, t)) != OC_OK) return st;
-                s->host_launches += 2;
+                s->host_launches += 1;
             } else {
                 const KernelKind ka =
                     cpl ? K_CPL_ASSEMBLE : (s->inst_host[grp].grid_cols > 0 ? K_ASSEMBLE_GRID : K_ASSEMBLE);
@@ -474,12 +471,9 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
             s->host_launches += 1;
         }
         if (s->args.n_strip_work > 0) {
-            StepArgs ra = a;
-            ra.blocks = s->d_sred_blocks;
             if ((st = launch_timed(s, K_ASSEMBLE_STRIP, a, strip_blocks(a.n_strip_work), t)) != OC_OK) return st;
-            if ((st = launch_timed(s, K_ASSEMBLE_REDUCE, ra, s->n_sred_blocks, t)) != OC_OK) return st;
             if ((st = launch_timed(s, K_ASSEMBLE_FINISH, a, a.n_strip_ids, t)) != OC_OK) return st;
-            s->host_launches += 3;
+            s->host_launches += 2;
         }
         if (s->n_cpl_blocks > 0) {
             if ((st = launch_timed(s, K_CPL_ASSEMBLE, ca, s->n_cpl_blocks, t)) != OC_OK) return st;
@@ -556,10 +550,9 @@ oc_status build_graph(oc_solver* s, float dt) {
     a.blk_base = 0;
     a.use_cond = loop ? 1 : 0;
     a.cond = (unsigned long long)handle;
-    StepArgs aa = a, ga = a, sa = a, ca = a, ua = a, ra = a;
+    StepArgs aa = a, ga = a, sa = a, ca = a, ua = a;
     aa.blocks = s->d_asm_blocks;       // REFERENCE cloths: k_assemble
     ga.blocks = s->d_grid_blocks;      // REFERENCE grid cloths: k_assemble_grid
-    ra.blocks = s->d_sred_blocks;      // grid cloths on the strip sweep: k_assemble_reduce
     sa.blocks = s->d_streamed_blocks;  // streamed REFERENCE cloths: CG loop
     ca.blocks = s->d_cpl_blocks;       // COUPLED cloths
     ua.blocks = s->d_upd_blocks;       // k_integrate
@@ -569,15 +562,13 @@ oc_status build_graph(oc_solver* s, float dt) {
     void* params_str[] = {&sa};
     void* params_cpl[] = {&ca};
     void* params_upd[] = {&ua};
-    void* params_sred[] = {&ra};
-    enum Table { T_ALL, T_ASM, T_STR, T_CPL, T_UPD, T_GRID, T_STRIP, T_SRED, T_SFIN };
+    enum Table { T_ALL, T_ASM, T_STR, T_CPL, T_UPD, T_GRID, T_STRIP, T_SFIN };
     auto kparams = [&](KernelKind k, Table tab) {
         cudaKernelNodeParams kp{};
         kp.func = const_cast<void*>(kernel_fn(k, a));
         const int n[] = {s->n_blocks, s->n_asm_blocks, s->n_streamed_blocks, s->n_cpl_blocks, s->n_upd_blocks,
-                         s->n_grid_blocks, strip_blocks(s->args.n_strip_work), s->n_sred_blocks, s->args.n_strip_ids};
-        void** pp[] = {params_all, params_asm, params_str, params_cpl, params_upd, params_grid, params_all, params_sred,
-                       params_all};
+                         s->n_grid_blocks, strip_blocks(s->args.n_strip_work), s->args.n_strip_ids};
+        void** pp[] = {params_all, params_asm, params_str, params_cpl, params_upd, params_grid, params_all, params_all};
         kp.gridDim = dim3((unsigned)n[tab]);
         kp.blockDim = dim3((unsigned)kernel_block_threads());
         kp.sharedMemBytes = (unsigned)kernel_smem_bytes(k, a);
@@ -606,12 +597,9 @@ oc_status build_graph(oc_solver* s, float dt) {
         kp = kparams(K_ASSEMBLE_GRID, T_GRID);
         OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &prev, 1, &kp));
     }
-    if (s->args.n_strip_work > 0) {  // the strip sweep, then its delta0 partials and totals
+    if (s->args.n_strip_work > 0) {  // the strip sweep, then its cloths' delta0 totals
         cudaGraphNode_t prev = n_asm;
         kp = kparams(K_ASSEMBLE_STRIP, T_STRIP);
-        OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &prev, 1, &kp));
-        prev = n_asm;
-        kp = kparams(K_ASSEMBLE_REDUCE, T_SRED);
         OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &prev, 1, &kp));
         prev = n_asm;
         kp = kparams(K_ASSEMBLE_FINISH, T_SFIN);
@@ -885,16 +873,28 @@ oc_status build_adjoint_graph(oc_solver* s, float dt) {
 oc_status build_strip_work(oc_solver* s) {
     std::vector<StripWork> work;
     s->strip_range.assign((size_t)s->n_inst, std::make_pair(0, 0));
-    const int64_t target = 64LL * std::max(1, s->sm_count);
-    int64_t area = 0;
-    for (int32_t k = 0; k < s->n_inst; ++k) {
-        const InstParams& ip = s->inst_host[(size_t)k];
-        if (ip.strip) area += (int64_t)((ip.grid_cols + kStripOwned - 1) / kStripOwned) * ip.grid_rows;
+    // Band height: a warp walks R + 2 rows for R owned ones, and the warps run in waves of
+    // (SMs x CTAs per SM x 8): take the R of 4 ... 64 that minimises waves x (R + 2).
+    const int64_t per_wave = (int64_t)std::max(1, s->sm_count) * s->cfg.strip_variant * (kStripThreads / 32);
+    int32_t R = 16;
+    double best = 0.0;
+    for (int32_t r = 4; r <= 64; ++r) {
+        int64_t items = 0;
+        for (int32_t k = 0; k < s->n_inst; ++k) {
+            const InstParams& ip = s->inst_host[(size_t)k];
+            if (ip.strip)
+                items += (int64_t)((ip.grid_cols + kStripOwned - 1) / kStripOwned) * ((ip.grid_rows + r - 1) / r);
+        }
+        const double cost = (double)((items + per_wave - 1) / per_wave) * (double)(r + 2);
+        if (items > 0 && (best == 0.0 || cost < best)) {
+            best = cost;
+            R = r;
+        }
     }
-    int32_t R = (int32_t)std::min<int64_t>(16, std::max<int64_t>(4, area / target));
     if (s->cfg.strip_rows > 0) R = s->cfg.strip_rows;
     for (int32_t k = 0; k < s->n_inst; ++k) {
-        const InstParams& ip = s->inst_host[(size_t)k];
+        InstParams& ip = s->inst_host[(size_t)k];
+        ip.strip_w0 = ip.strip_nw = 0;
         if (!ip.strip) continue;
         const int32_t first = (int32_t)work.size();
         const int32_t rows = ip.grid_rows, band = std::min(R, rows);
@@ -902,11 +902,16 @@ oc_status build_strip_work(oc_solver* s) {
             for (int32_t c0 = 0; c0 < ip.grid_cols; c0 += kStripOwned)
                 work.push_back(StripWork{k, c0, r0, std::min(rows, r0 + band)});
         s->strip_range[(size_t)k] = std::make_pair(first, (int32_t)work.size() - first);
+        ip.strip_w0 = first;
+        ip.strip_nw = (int32_t)work.size() - first;
     }
     StripWork* d = const_cast<StripWork*>(s->args.strip_work);
     OC_TRY(reupload(s, &d, work));
     s->args.strip_work = d;
     s->args.n_strip_work = (int32_t)work.size();
+    s->args.strip_item0 = 0;
+    dfree(s, &s->args.strip_part);
+    OC_TRY(dalloc(s, &s->args.strip_part, std::max<size_t>(work.size(), 1)));
     std::vector<int32_t> ids;
     s->strip_pos.assign((size_t)s->n_inst, -1);
     for (int32_t k = 0; k < s->n_inst; ++k)
@@ -957,7 +962,7 @@ oc_status plan_execution(oc_solver* s) {
     s->resident.assign((size_t)s->n_inst, 0);
     for (oc_solver::Bucket& b : s->buckets) dfree(s, &b.d_ids);
     s->buckets.clear();
-    std::vector<BlockInfo> streamed, asm_ref, cpl, upd, grid, sred;
+    std::vector<BlockInfo> streamed, asm_ref, cpl, upd, grid;
     std::map<std::tuple<int, int, int>, std::vector<int32_t>> groups;
     for (int32_t k = 0; k < s->n_inst; ++k) {
         InstParams& ip = s->inst_host[(size_t)k];
@@ -982,8 +987,10 @@ oc_status plan_execution(oc_solver* s) {
         }
         if (!(want && s->resident_fused)) {
             ip.strip = strip_wanted(cfg, ip) ? 1 : 0;
-            auto& tab = ip.grid_cols > 0 ? (ip.strip ? sred : grid) : asm_ref;
-            tab.insert(tab.end(), kb, kb + ip.nblk);
+            if (!ip.strip) {  // a cloth on the strip sweep is in no block table of the assembly
+                auto& tab = ip.grid_cols > 0 ? grid : asm_ref;
+                tab.insert(tab.end(), kb, kb + ip.nblk);
+            }
         }
         if (want) {
             s->resident[(size_t)k] = 1;
@@ -997,8 +1004,6 @@ oc_status plan_execution(oc_solver* s) {
     OC_TRY(reupload(s, &s->d_asm_blocks, asm_ref));
     s->n_grid_blocks = (int32_t)grid.size();
     OC_TRY(reupload(s, &s->d_grid_blocks, grid));
-    s->n_sred_blocks = (int32_t)sred.size();
-    OC_TRY(reupload(s, &s->d_sred_blocks, sred));
     s->n_cpl_blocks = (int32_t)cpl.size();
     OC_TRY(reupload(s, &s->d_cpl_blocks, cpl));
     s->n_upd_blocks = (int32_t)upd.size();
@@ -1296,9 +1301,6 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
                 OC_CREATE_TRY(upload(s, &d_sr, P.strip_rest));
                 a.strip_rest = d_sr;
             }
-            float* term = nullptr;  // delta0 terms of the swept vertices
-            OC_CREATE_TRY(dalloc(s, &term, (size_t)P.nv));
-            a.term = term;
         }
     }
     a.own_ends = own_ends;
@@ -1592,7 +1594,7 @@ oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
     // the resident launches and the Provot pass; the WHILE loop's launches are counted on
     // the device (loop_count).
     const int64_t per_step = (s->n_asm_blocks > 0 ? 1 : 0) + (s->n_grid_blocks > 0 ? 1 : 0) +
-                             (s->args.n_strip_work > 0 ? 3 : 0) + (s->n_cpl_blocks > 0 ? 1 : 0) +
+                             (s->args.n_strip_work > 0 ? 2 : 0) + (s->n_cpl_blocks > 0 ? 1 : 0) +
                              (s->persist ? 1 : (s->n_upd_blocks > 0 ? 1 : 0)) + (int64_t)s->buckets.size() +
                              (s->any_provot ? 1 : 0);
     s->host_launches += per_step * (int64_t)n_steps;
@@ -1800,8 +1802,8 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
     cudaEventDestroy(t.ev[0]);
     cudaEventDestroy(t.ev[1]);
     if (st != OC_OK) return st;
-    const KernelKind kinds[] = {K_ASSEMBLE, K_ASSEMBLE_GRID, K_ASSEMBLE_STRIP, K_ASSEMBLE_REDUCE, K_ASSEMBLE_FINISH,
-                                K_CG_DIR, K_CG_UPDATE, K_INTEGRATE, K_CG_PERSIST, K_RESIDENT, K_PROVOT,
+    const KernelKind kinds[] = {K_ASSEMBLE, K_ASSEMBLE_GRID, K_ASSEMBLE_STRIP, K_ASSEMBLE_FINISH, K_CG_DIR,
+                                K_CG_UPDATE, K_INTEGRATE, K_CG_PERSIST, K_RESIDENT, K_PROVOT,
                                 K_CPL_ASSEMBLE, K_CPL_DIR, K_CPL_UPDATE};
     int32_t n = 0;
     for (KernelKind k : kinds) {
@@ -1811,8 +1813,7 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
         if (k == K_ASSEMBLE_GRID && s->n_grid_blocks == 0) continue;
         if (k == K_CG_PERSIST && !s->persist) continue;
         if ((k == K_CG_DIR || k == K_CG_UPDATE || k == K_INTEGRATE) && s->persist) continue;
-        if ((k == K_ASSEMBLE_STRIP || k == K_ASSEMBLE_REDUCE || k == K_ASSEMBLE_FINISH) && s->args.n_strip_work == 0)
-            continue;
+        if ((k == K_ASSEMBLE_STRIP || k == K_ASSEMBLE_FINISH) && s->args.n_strip_work == 0) continue;
         if (k == K_ASSEMBLE && s->n_asm_blocks == 0 && (s->n_grid_blocks > 0 || s->args.n_strip_work > 0)) continue;
         if (names) {
             std::memset(names + 32 * n, 0, 32);

@@ -35,10 +35,13 @@ struct InstParams {
     // (36 words, one per anchor position class, six 4-bit parameter slots each: H, bR, V,
     // shA, shB, bC), strip_rest its first rest length in StepArgs::strip_rest (six planes of
     // nv floats, by kind and anchor vertex) or -1 when the slots hold the rest lengths;
-    // strip_ok 1 when the cloth may take the sweep (strip 1 when it does).
+    // strip_ok 1 when the cloth may take the sweep (strip 1 when it does); strip_w0 and
+    // strip_nw its range of StepArgs::strip_work (and of strip_part).
     int32_t strip;
     int32_t strip_ok;
     int32_t strip_slot;
+    int32_t strip_w0;
+    int32_t strip_nw;
     int64_t strip_rest;
     float provot_ratio;     // IMP:808
     float ellipsoid[16];    // object -> world, column-major (IMP:583-585)
@@ -129,14 +132,16 @@ struct StepArgs {
     const int32_t* st_data;
     const float4* st_param;
     const float* rest_inc;   // rest length of every incidence record (CSR order), or nullptr
-    // The strip sweep: its work items, parameter-slot words and rest planes (see
-    // InstParams), the per-vertex delta0 terms it leaves for k_assemble_reduce, and the
+    // The strip sweep: its work items (strip_item0: the first item's index in the handle's
+    // list, for a launch over a part of it), parameter-slot words and rest planes (see
+    // InstParams), one delta0 partial per item (a float pair in each 8-byte slot), and the
     // cloths on the sweep (k_assemble_finish: one CTA each).
     const StripWork* strip_work;
     int32_t n_strip_work;
+    int32_t strip_item0;
     const uint32_t* strip_slot;
     const float* strip_rest;
-    float* term;
+    double* strip_part;
     const int32_t* strip_ids;
     int32_t n_strip_ids;
     // Displacement mode of the adjoint tape (oc_set_tape_mode): X holds the displacement u
@@ -235,8 +240,8 @@ __host__ __device__ inline int stencil_class_1d(int32_t i, int32_t n) {
 
 enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3, K_FORCES = 4, K_RESIDENT = 5,
                   K_PROVOT = 6, K_ELLIPSOID = 7, K_CPL_ASSEMBLE = 8, K_CPL_DIR = 9, K_CPL_UPDATE = 10,
-                  K_ASSEMBLE_GRID = 11, K_CG_PERSIST = 12, K_ASSEMBLE_STRIP = 13, K_ASSEMBLE_REDUCE = 14,
-                  K_ASSEMBLE_FINISH = 15, K_COUNT = 16 };
+                  K_ASSEMBLE_GRID = 11, K_CG_PERSIST = 12, K_ASSEMBLE_STRIP = 13, K_ASSEMBLE_FINISH = 14,
+                  K_COUNT = 15 };
 
 // The whole CG loop of the cloths of block table a.blocks[0, n_entries) in one
 // cooperative launch of `grid` blocks (oc_kernels.cu), any number of cloths; a block

@@ -214,9 +214,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_assemble_grid(const StepArgs a)
 // originals' values again.  It adds them in spring-id order with the p1 / p2 signs, so F is
 // the stencil gather's bits, then forms its system and CG set-up as k_assemble_grid does.
 // The two lanes on each side own nothing, and a band starts two rows early to form the
-// springs that reach into it from above.  delta0's per-vertex terms go to a.term;
-// k_assemble_reduce and k_assemble_finish sum them over the standard block table in
-// k_assemble_grid's order (the same partials and totals, so the same CG).
+// springs that reach into it from above.  delta0: each warp sums its vertices' terms as
+// a float pair into its item's slot of strip_part, and k_assemble_finish sums a cloth's
+// items in item order and sets the CG scalars.  delta0 is then summed in the sweep's own
+// order, not k_assemble_grid's; F, A, b and the CG set-up are the stencil gather's bits.
 
 __device__ __forceinline__ float3 shfl_down3(const float4 v, int d) {
     return make_float3(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d),
@@ -255,6 +256,10 @@ __device__ __forceinline__ float4 strip_param(const StripParams& sp, bool has_re
     float4 p = sp.par[(w >> (4 * kind)) & 15u];
     if (has_rest) p.x = rs[kind];
     return p;
+}
+
+__device__ __forceinline__ Acc shfl_down_acc(Acc v, int o) {
+    return make_acc(__shfl_down_sync(0xffffffffu, v.s, o), __shfl_down_sync(0xffffffffu, v.c, o));
 }
 
 template <int MINB>
@@ -306,6 +311,7 @@ __global__ void __launch_bounds__(kStripThreads, MINB) k_assemble_strip(const St
         for (int k = 0; k < 6; ++k) rs[k] = __ldg(rest + (size_t)k * nvk + r * cols + c);
     // Springs anchored one and two rows up (this lane's column).
     float3 fV1 = zero3, fA1 = zero3, fB1 = zero3, fC1 = zero3, fC2 = zero3;
+    Acc part = acc_zero();
     for (; r < w.r1; ++r) {
         const bool band = r >= w.r0;
         const bool own = owner && band;
@@ -400,7 +406,7 @@ __global__ void __launch_bounds__(kStripThreads, MINB) k_assemble_strip(const St
         if (springs && r == rows - 3) add3(Fx, Fy, Fz, fC);
         if (springs && r == rows - 1) sub3(Fx, Fy, Fz, fC2);
         if (own)
-            a.term[g] = store_system(a, g, Va, system_from(own_blocks(h, Xa.w, os), h, Va, make_float3(Fx, Fy, Fz)));
+            acc_add(part, store_system(a, g, Va, system_from(own_blocks(h, Xa.w, os), h, Va, make_float3(Fx, Fy, Fz))));
         fC2 = fC1;
         fC1 = fC;
         fV1 = fV;
@@ -415,44 +421,45 @@ __global__ void __launch_bounds__(kStripThreads, MINB) k_assemble_strip(const St
 #pragma unroll
         for (int k = 0; k < 6; ++k) rs[k] = rn[k];
     }
+    // delta0: this item's pair (k_assemble_finish sums the cloth's items).
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part = acc_merge(part, shfl_down_acc(part, o));
+    if (lane == 0)
+        reinterpret_cast<float2*>(a.strip_part)[a.strip_item0 + wid] = make_float2(part.s, part.c);
 }
 
-// delta0 of the strip-swept cloths over the standard block table, in two launches so
-// that no blocks pile up on one atomic counter (they all finish together here, unlike
-// the assembly kernels whose epilogue this splits):
-//   k_assemble_reduce  each block sums its vertices' terms in k_assemble_grid's order into
-//                      its partial (loads eight per thread at a time; a block holds at most
-//                      2048 vertices);
-//   k_assemble_finish  one CTA per cloth sums the cloth's partials with the last-block
-//                      epilogue's tree and sets the CG scalars as finish<K_ASSEMBLE> does.
-// The same partials and the same totals, so the same CG as after k_assemble_grid.
-__global__ void __launch_bounds__(kThreads) k_assemble_reduce(const StepArgs a) {
-    const int blk = blockIdx.x + a.blk_base;
-    const BlockInfo bi = a.blocks[blk];
-    Acc part = acc_zero();
-    for (int64_t g0 = bi.v_begin + threadIdx.x; g0 < bi.v_end; g0 += 8 * (int64_t)blockDim.x) {
-        float t[8];
+// delta0 of a cloth on the strip sweep: one CTA per cloth sums its items' pairs in item
+// order (a fixed tree) and sets the CG scalars as finish<K_ASSEMBLE> does; the last CTA
+// sets the graph's WHILE condition.
+__global__ void __launch_bounds__(kThreads) k_assemble_finish(const StepArgs a) {
+    __shared__ Acc warp_part[kThreads / 32];
+    const int32_t inst = a.strip_ids[blockIdx.x];
+    const InstParams& ip = a.inst[inst];
+    const float2* item_part = reinterpret_cast<const float2*>(a.strip_part) + ip.strip_w0;
+    // Eight items in flight per thread, merged in item order.
+    Acc tot = acc_zero();
+    for (int j0 = threadIdx.x; j0 < ip.strip_nw; j0 += 8 * blockDim.x) {
+        float2 p[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-            const int64_t g = g0 + (int64_t)u * blockDim.x;
-            t[u] = g < bi.v_end ? __ldcg(a.term + g) : 0.0f;
+            const int j = j0 + u * blockDim.x;
+            p[u] = j < ip.strip_nw ? __ldcg(item_part + j) : make_float2(0.f, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u)
-            if (g0 + (int64_t)u * blockDim.x < bi.v_end) acc_add(part, t[u]);
+            if (j0 + u * (int)blockDim.x < ip.strip_nw) tot = acc_merge(tot, make_acc(p[u].x, p[u].y));
     }
-    const double bsum = block_sum_acc(part);
-    if (threadIdx.x == 0) a.partials[bi.gblk] = bsum;
-}
-
-__global__ void __launch_bounds__(kThreads) k_assemble_finish(const StepArgs a) {
-    const int32_t inst = a.strip_ids[blockIdx.x];
-    const InstParams& ip = a.inst[inst];
-    double acc = 0.0;
-#pragma unroll 8
-    for (int j = threadIdx.x; j < ip.nblk; j += blockDim.x) acc += __ldcg(a.partials + ip.blk0 + j);
-    const double total = block_sum(acc);
-    if (threadIdx.x == 0) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tot = acc_merge(tot, shfl_down_acc(tot, o));
+    if (lane == 0) warp_part[w] = tot;
+    __syncthreads();
+    if (w != 0) return;
+    tot = lane < (int)(blockDim.x >> 5) ? warp_part[lane] : acc_zero();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tot = acc_merge(tot, shfl_down_acc(tot, o));
+    if (lane == 0) {
+        const double total = (double)tot.s + (double)tot.c;
         InstState& st = a.state[inst];
         st.ticket = 0;
         st.delta0 = total;
@@ -1128,7 +1135,6 @@ const char* kernel_name(KernelKind k) {
         case K_ASSEMBLE_GRID: return "k_assemble_grid";
         case K_CG_PERSIST: return "k_cg_persist";
         case K_ASSEMBLE_STRIP: return "k_assemble_strip";
-        case K_ASSEMBLE_REDUCE: return "k_assemble_reduce";
         case K_ASSEMBLE_FINISH: return "k_assemble_finish";
         case K_CPL_DIR: return "k_cpl_dir";
         case K_CPL_UPDATE: return "k_cpl_update";
@@ -1150,7 +1156,6 @@ const void* kernel_fn(KernelKind k, const StepArgs& a) {
         case K_CPL_UPDATE: return coupled_fn(k);
         case K_ASSEMBLE_GRID: return (const void*)k_assemble_grid;
         case K_ASSEMBLE_STRIP: return strip_fn(a.strip_variant);
-        case K_ASSEMBLE_REDUCE: return (const void*)k_assemble_reduce;
         case K_ASSEMBLE_FINISH: return (const void*)k_assemble_finish;
         default: return nullptr;
     }
@@ -1212,7 +1217,6 @@ cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStre
             reinterpret_cast<void (*)(StepArgs)>(const_cast<void*>(strip_fn(a.strip_variant)))
                 <<<nblocks, kStripThreads, 0, stream>>>(a);
             break;
-        case K_ASSEMBLE_REDUCE: k_assemble_reduce<<<nblocks, kThreads, 0, stream>>>(a); break;
         case K_ASSEMBLE_FINISH: k_assemble_finish<<<nblocks, kThreads, 0, stream>>>(a); break;
         default: return cudaErrorInvalidValue;
     }

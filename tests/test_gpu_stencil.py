@@ -180,9 +180,10 @@ def strip_batch(seed: int):
 @pytest.mark.parametrize("rows_per_band", [0, 1, 2, 5, 16])
 @pytest.mark.parametrize("executor", ["streamed", "resident"])
 def test_strip_sweep_same_bits_as_stencil(rows_per_band, executor):
-    """k_assemble_strip (each spring force once, bands of rows, delta0 reduced over the
-    standard blocks) against k_assemble_grid (each spring at both ends): the same F, A, b
-    and delta0, so the same steps bit for bit, for any band height."""
+    """k_assemble_strip (each spring force once, bands of rows, delta0 summed in the
+    sweep's own order) against k_assemble_grid (each spring at both ends): the same F, A
+    and b; delta0's two orders agree to about 2^-48 relative, which leaves the float CG
+    scalars, and so every step, the same bits here, for any band height."""
     descs, X, V = strip_batch(11)
     env = {"OC_STRIP": 1}
     if rows_per_band:
@@ -217,5 +218,4 @@ def test_strip_sweep_profile_names_its_kernels():
         s.set_launch_config(strip=1)
         s.set_state(X, V)
         prof = s.profile(DT, 2)
-    assert prof["k_assemble_strip"]["launches"] == 2 and prof["k_assemble_reduce"]["launches"] == 2
-    assert prof["k_assemble_finish"]["launches"] == 2
+    assert prof["k_assemble_strip"]["launches"] == 2 and prof["k_assemble_finish"]["launches"] == 2
