@@ -345,6 +345,16 @@ oc_status oc_tune_cache_store(const char* path, const char* key, const oc_launch
  * persistent CG. */
 oc_status oc_test_barrier_timeout(oc_solver* s, int32_t withhold_block, uint32_t max_polls);
 
+/* No counterpart in the reference.  For tests: the step computes spring lengths, their
+ * reciprocals, the quotients of ComputeForces / CalcForceDerivatives (IMP:720-727) and the
+ * preconditioner's reciprocals (IMP:312-314) with branch-free correctly rounded sequences
+ * when the arguments lie in [2^-60, 2^60], and with the IEEE intrinsics otherwise.  This
+ * checks the sequences against the intrinsics on `device`: the reciprocal of every float
+ * of that range and its negation, the square root of every float of that range, and
+ * n_pairs random quotients (and their negations) from `seed`.  mismatches[3] receives the
+ * number of results whose bits differ (reciprocal, square root, quotient). */
+oc_status oc_test_cr_arith(int32_t device, uint64_t n_pairs, uint64_t seed, uint64_t* mismatches);
+
 /* ---- allocation-free solve -------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory
  * around a solve — an engine that manages a fixed device-memory budget itself, or a

@@ -132,6 +132,7 @@ SIGNATURES = {
     "oc_tape_forward_intervals": (C.c_int32, [_P, C.c_float, C.c_int32, C.c_void_p]),
     "oc_tape_layout": (C.c_int32, [_P, C.POINTER(C.c_int32), C.c_void_p]),
     "oc_test_barrier_timeout": (C.c_int32, [_P, C.c_int32, C.c_uint32]),
+    "oc_test_cr_arith": (C.c_int32, [C.c_int32, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)]),
     "oc_set_tape_mode": (C.c_int32, [_P, C.c_int32]),
     "oc_tape_displacement": (C.c_int32, [_P, _P]),
     "oc_get_launch_config": (C.c_int32, [_P, C.POINTER(LaunchConfigC)]),

@@ -2616,6 +2616,22 @@ oc_status oc_test_barrier_timeout(oc_solver* s, int32_t withhold_block, uint32_t
     return OC_OK;
 }
 
+oc_status oc_test_cr_arith(int32_t device, uint64_t n_pairs, uint64_t seed, uint64_t* mismatches) {
+    if (!mismatches || device < 0) return OC_ERR_INVALID_ARGUMENT;
+    oc_solver* s = nullptr;  // fail_cuda records the message without a handle
+    OC_TRY(cudaSetDevice(device));
+    unsigned long long* counts = nullptr;
+    OC_TRY(cudaMalloc(&counts, 3 * sizeof(unsigned long long)));
+    unsigned long long h[3] = {0, 0, 0};
+    cudaError_t e = cudaMemset(counts, 0, sizeof h);
+    if (e == cudaSuccess) e = launch_test_cr_arith(counts, n_pairs, seed, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(h, counts, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(counts);
+    if (e != cudaSuccess) return fail_cuda(s, e, "oc_test_cr_arith");
+    for (int k = 0; k < 3; ++k) mismatches[k] = h[k];
+    return OC_OK;
+}
+
 oc_status oc_tape_info(const oc_solver* s, int32_t* checkpoint_every, int64_t* tape_bytes) {
     if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
     const auto& T = s->tape;

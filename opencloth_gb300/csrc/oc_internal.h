@@ -250,6 +250,7 @@ enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3
 // start at zero (the assembly epilogue leaves them so).  err: bit 0 set if a wait gave up.
 int persist_max_entries_per_block();
 int persist_blocks_per_sm();
+cudaError_t launch_test_cr_arith(unsigned long long* counts, uint64_t n_pairs, uint64_t seed, cudaStream_t stream);
 cudaError_t launch_cg_persist(const StepArgs& a, int32_t n_entries, int grid, unsigned* words, int* err,
                               cudaStream_t stream);
 

@@ -1119,6 +1119,49 @@ const void* assemble_fn(int v) {
     }
 }
 
+// ---- check of the branch-free correctly rounded arithmetic (tests) --------------------
+// counts[0]: reciprocals, counts[1]: square roots, counts[2]: quotients that differ from
+// the IEEE intrinsics' bits.
+__global__ void k_test_cr_unary(unsigned long long* counts, uint32_t lo, uint32_t hi) {
+    unsigned long long br = 0, bs = 0;
+    for (uint64_t u = lo + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < hi; u += (uint64_t)gridDim.x * blockDim.x) {
+        const float x = __uint_as_float((uint32_t)u);
+        br += __float_as_uint(rcp_cr(x)) != __float_as_uint(__frcp_rn(x));
+        br += __float_as_uint(rcp_cr(-x)) != __float_as_uint(__frcp_rn(-x));
+        bs += __float_as_uint(sqrt_cr(x)) != __float_as_uint(__fsqrt_rn(x));
+    }
+    if (br) atomicAdd(counts, br);
+    if (bs) atomicAdd(counts + 1, bs);
+}
+
+__device__ __forceinline__ uint32_t mix32(uint64_t x) {  // splitmix64's finaliser
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return (uint32_t)x;
+}
+
+// Random a in +-[2^-60, 2^60] (or 0), b in [2^-30, 2^30] (the quotients of the springs'
+// arithmetic: dot / dist and dP / dist, dist the square root of an argument in range);
+// every 8th pair has a significand of b near all ones or near a power of two.
+__global__ void k_test_cr_div(unsigned long long* counts, uint64_t n, uint64_t seed) {
+    unsigned long long bad = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t h1 = mix32(seed + 3 * i), h2 = mix32(seed + 3 * i + 1), h3 = mix32(seed + 3 * i + 2);
+        uint32_t mb = h2 & 0x7fffffu;
+        if ((h3 & 7u) == 1u) mb = 0x7fffffu - ((h3 >> 20) & 15u);
+        if ((h3 & 7u) == 2u) mb = (h3 >> 20) & 15u;
+        const uint32_t ea = 67u + (h1 >> 23) % 121u, eb = 97u + (h3 >> 8) % 61u;
+        const float a = (h3 & 0x70u) == 0x70u ? 0.0f : __uint_as_float((h3 & 0x80000000u) | ea << 23 | (h1 & 0x7fffffu));
+        const float b = __uint_as_float(eb << 23 | mb);
+        bad += __float_as_uint(div_cr(a, b, __frcp_rn(b))) != __float_as_uint(__fdiv_rn(a, b));
+        bad += __float_as_uint(div_cr(-a, b, __frcp_rn(b))) != __float_as_uint(__fdiv_rn(-a, b));
+    }
+    if (bad) atomicAdd(counts + 2, bad);
+}
+
 }  // namespace
 
 const char* kernel_name(KernelKind k) {
@@ -1279,6 +1322,15 @@ cudaError_t launch_cg_persist(const StepArgs& a, int32_t n_entries, int grid, un
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, k_cg_persist, a, n_entries, words, err);
+}
+
+cudaError_t launch_test_cr_arith(unsigned long long* counts, uint64_t n_pairs, uint64_t seed, cudaStream_t stream) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_test_cr_unary<<<8 * std::max(sms, 1), kThreads, 0, stream>>>(counts, 0x21800000u /* 2^-60 */, 0x5d800001u /* past 2^60 */);
+    if (n_pairs > 0) k_test_cr_div<<<8 * std::max(sms, 1), kThreads, 0, stream>>>(counts, n_pairs, seed);
+    return cudaGetLastError();
 }
 
 }  // namespace oc
