@@ -107,10 +107,12 @@ __device__ __forceinline__ int64_t slot_pos(const BsrArgs& a, const BsrParams& s
     return (a.slice_ptr[s] + j) * 32 + (local & 31);
 }
 
-// One slot: the block and its column.
+// One slot: the block and its column.  The sliced planes are read once per pass and are
+// far larger than L2, so they are loaded evict-first (.cs): the direction and residual
+// records the rows gather stay in L2.
 __device__ __forceinline__ int32_t load_block(const BsrArgs& a, int64_t pos, float m[9]) {
-    const float4 u = __ldg(a.sb0 + pos), v = __ldg(a.sb1 + pos);
-    const float2 w = __ldg(a.sb2 + pos);
+    const float4 u = __ldcs(a.sb0 + pos), v = __ldcs(a.sb1 + pos);
+    const float2 w = __ldcs(a.sb2 + pos);
     m[0] = u.x; m[1] = u.y; m[2] = u.z; m[3] = u.w;
     m[4] = v.x; m[5] = v.y; m[6] = v.z; m[7] = v.w;
     m[8] = w.x;

@@ -45,13 +45,25 @@ __device__ __forceinline__ SpringBlock spring_block(const float4 p1, const float
                                                     float h, float hh) {
     SpringBlock c;
     const float dx = p1.x - p2.x, dy = p1.y - p2.y, dz = p1.z - p2.z;
-    const float l = sqrtf(dx * dx + dy * dy + dz * dz);
-    c.n0 = dx / l;
-    c.n1 = dy / l;
-    c.n2 = dz / l;
+    const float sqr = dx * dx + dy * dy + dz * dz;
+    float l, rl;
+    if (cr_arg(sqr) && cr_num(dx) && cr_num(dy) && cr_num(dz) && cr_num(rest)) {
+        l = sqrt_cr(sqr);
+        const float inv = rcp_cr(l);
+        c.n0 = div_cr(dx, l, inv);
+        c.n1 = div_cr(dy, l, inv);
+        c.n2 = div_cr(dz, l, inv);
+        rl = div_cr(rest, l, inv);
+    } else {
+        l = __fsqrt_rn(sqr);
+        c.n0 = __fdiv_rn(dx, l);
+        c.n1 = __fdiv_rn(dy, l);
+        c.n2 = __fdiv_rn(dz, l);
+        rl = __fdiv_rn(rest, l);
+    }
     const float ksn = ks > 0.0f ? ks : 0.0f;
     const float kdn = -kd > 0.0f ? -kd : 0.0f;
-    const float t = 1.0f - rest / l;
+    const float t = 1.0f - rl;
     const float kst = ksn * (t > 0.0f ? t : 0.0f);
     const float alpha = h * kdn + hh * ksn;
     c.beta = hh * kst;
@@ -239,9 +251,11 @@ __global__ void __launch_bounds__(kThreads) k_cpl_dir(const StepArgs a) {
                 q2 = mp * n2;
                 const int32_t deg = __ldg(a.rowptr + g + 1) - __ldg(a.rowptr + g);
                 const int64_t slot0 = __ldg(a.cpl_slice + (g >> 5)) + (g & 31);
+                // The per-incidence planes are read once per pass (evict-first, .cs), so
+                // the gathered z and d records stay in L2.
                 for (int32_t e = 0; e < deg; ++e) {
                     const int64_t k = slot0 + 32 * (int64_t)e;
-                    const int32_t o = __ldg(a.cpl_o + k);
+                    const int32_t o = __ldcs(a.cpl_o + k);
                     const float4 zo = Z[o];
                     float m0 = zo.x, m1 = zo.y, m2 = zo.z;
                     if (!first) {
@@ -250,7 +264,8 @@ __global__ void __launch_bounds__(kThreads) k_cpl_dir(const StepArgs a) {
                         m1 = m1 + dd.y * beta;
                         m2 = m2 + dd.z * beta;
                     }
-                    block_apply(C0[k], C1[k], C2[k], C3[k], C4[k], n0 - m0, n1 - m1, n2 - m2, q0, q1, q2);
+                    block_apply(__ldcs(C0 + k), __ldcs(C1 + k), __ldcs(C2 + k), __ldcs(C3 + k), __ldcs(C4 + k),
+                                n0 - m0, n1 - m1, n2 - m2, q0, q1, q2);
                 }
                 acc_add(part, n0 * q0 + n1 * q1 + n2 * q2);
             }
