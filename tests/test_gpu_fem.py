@@ -197,3 +197,22 @@ def test_resident_edge_systems_give_the_streamed_bits():
     for k in (0, 1, 3):
         Vo, _ = oracle.bsr_cg(systems[k], dot_fp64=True)
         assert rel_free(Va[off[k]:off[k + 1]], Vo, systems[k]) <= 1e-6, k
+
+
+@pytest.mark.parametrize("variant", ["1", "2", "3", "5", "6", "7"])
+def test_matrix_vector_variants_give_the_same_bits(variant, monkeypatch):
+    """Every launch shape of the streamed matrix-vector pass (OC_BSR_VARIANT, read at
+    create time: the unroll of the slot loop and the register cap) keeps each row's
+    products in slot order and the default's thread-to-row map, so it gives the default's
+    bits.  Systems of several slices and ragged last slices, batched, graph and
+    host-driven."""
+    rng = np.random.default_rng(11)
+    gens = [fem_system(12, 5, 4, V=rng.normal(0.0, 0.2, (13 * 6 * 5, 3))),
+            fem_system(7, 3, 9, V=rng.normal(0.0, 0.2, (8 * 4 * 10, 3)))]
+    systems = [oracle.BsrSystem(g["row_ptr"], g["col"], g["blocks"], g["b"], g["V"], g["fixed"], 20) for g in gens]
+    monkeypatch.delenv("OC_BSR_VARIANT", raising=False)
+    V0, r0 = solve(systems, executor=1)
+    monkeypatch.setenv("OC_BSR_VARIANT", variant)
+    for graph in (True, False):
+        V, r = solve(systems, use_graph=graph, executor=1)
+        assert np.array_equal(V, V0) and np.array_equal(r, r0)
