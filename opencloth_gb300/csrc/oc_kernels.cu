@@ -26,6 +26,7 @@
 // CUDA-graph WHILE condition to "some instance still iterating".  k_cg_persist forms
 // the same sums in the same order at its grid barriers.
 #include <algorithm>
+#include <cstdlib>
 
 #include <cuda_runtime.h>
 
@@ -185,7 +186,8 @@ __global__ void __launch_bounds__(kThreads, MINB) k_assemble_thread(const StepAr
 }
 
 // Assembly of grid cloths (one thread per vertex, no incidence records).
-__global__ void __launch_bounds__(kThreads, 4) k_assemble_grid(const StepArgs a) {
+template <int B, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_assemble_grid(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
     const InstParams& ip = a.inst[bi.inst];
@@ -193,10 +195,20 @@ __global__ void __launch_bounds__(kThreads, 4) k_assemble_grid(const StepArgs a)
     for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
         const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
         const OwnSpring os = load_own(a, g);
-        const float3 F = stencil_gather(a, ip, g, Xg, Vg);
+        const float3 F = B == 1 ? stencil_gather(a, ip, g, Xg, Vg) : stencil_gather_ahead<B>(a, ip, g, Xg, Vg);
         acc_add(part, assemble_vertex(a, g, Xg, Vg, F, os));
     }
     finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
+}
+
+// Two incidences fetched ahead at four CTAs per SM (the default), or one at a time
+// (OC_GRID_VARIANT=1).  Measured on GB300: 1.78 against 1.81 ms on the 4096-cloth batch and
+// 88 against 91.5 us on the 1M-vertex cloth; two or three ahead at three CTAs per SM and four
+// at two were 8-44% slower.  All give the same bits.
+typedef void (*GridAsmFn)(StepArgs);
+GridAsmFn grid_asm_fn() {
+    const char* e = std::getenv("OC_GRID_VARIANT");
+    return (e && std::atoi(e) == 1) ? k_assemble_grid<1, 4> : k_assemble_grid<2, 4>;
 }
 
 // ---- the strip sweep: every spring force of a grid cloth evaluated once ----------------
@@ -1197,7 +1209,7 @@ const void* kernel_fn(KernelKind k, const StepArgs& a) {
         case K_CPL_ASSEMBLE:
         case K_CPL_DIR:
         case K_CPL_UPDATE: return coupled_fn(k);
-        case K_ASSEMBLE_GRID: return (const void*)k_assemble_grid;
+        case K_ASSEMBLE_GRID: return (const void*)grid_asm_fn();
         case K_ASSEMBLE_STRIP: return strip_fn(a.strip_variant);
         case K_ASSEMBLE_FINISH: return (const void*)k_assemble_finish;
         default: return nullptr;
@@ -1255,7 +1267,7 @@ cudaError_t launch_kernel(KernelKind k, const StepArgs& a, int nblocks, cudaStre
         case K_CPL_ASSEMBLE:
         case K_CPL_DIR:
         case K_CPL_UPDATE: return launch_coupled(k, a, nblocks, stream);
-        case K_ASSEMBLE_GRID: k_assemble_grid<<<nblocks, kThreads, 0, stream>>>(a); break;
+        case K_ASSEMBLE_GRID: grid_asm_fn()<<<nblocks, kThreads, 0, stream>>>(a); break;
         case K_ASSEMBLE_STRIP:
             reinterpret_cast<void (*)(StepArgs)>(const_cast<void*>(strip_fn(a.strip_variant)))
                 <<<nblocks, kStripThreads, 0, stream>>>(a);
