@@ -160,6 +160,10 @@ struct oc_solver {
 
 namespace {
 
+// Floats between the staging planes of X, V and dV (three floats per vertex, rounded up
+// to 64 so that every plane is 256-byte aligned for the float4 check of k_state_check4).
+size_t stage_stride(int64_t nv) { return (3 * (size_t)nv + 63) / 64 * 64; }
+
 oc_status fail(oc_solver* s, oc_status code, const std::string& msg) {
     if (s) s->err = msg;
     return code;
@@ -1451,7 +1455,7 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
     OC_CREATE_TRY(cudaMallocHost(&s->h_loop, sizeof(unsigned long long)));
     OC_CREATE_TRY(cudaMemset(a.unconverged, 0, sizeof(int32_t)));
     OC_CREATE_TRY(cudaMemset(a.grid_ticket, 0, sizeof(uint32_t)));
-    OC_CREATE_TRY(dalloc(s, &s->stage, 9 * (size_t)P.nv));
+    OC_CREATE_TRY(dalloc(s, &s->stage, 3 * stage_stride(P.nv)));
     OC_CREATE_TRY(dalloc(s, &s->d_err, 1));
     OC_CREATE_TRY(cudaMallocHost(&s->h_state, sizeof(InstState) * P.n_inst));
     OC_CREATE_TRY(cudaMallocHost(&s->h_scalar, sizeof(int32_t)));
@@ -1509,9 +1513,10 @@ namespace {
 oc_status stage_checked(oc_solver* s, const float* X, const float* V, const float* dV, float** sx, float** sv,
                         float** sd, const char* who) {
     const size_t n3 = 3 * (size_t)s->nv;
+    const size_t ps = stage_stride(s->nv);
     *sx = X ? s->stage : nullptr;
-    *sv = V ? s->stage + n3 : nullptr;
-    *sd = dV ? s->stage + 2 * n3 : nullptr;
+    *sv = V ? s->stage + ps : nullptr;
+    *sd = dV ? s->stage + 2 * ps : nullptr;
     if (X) OC_TRY(cudaMemcpyAsync(*sx, X, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     if (V) OC_TRY(cudaMemcpyAsync(*sv, V, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     if (dV) OC_TRY(cudaMemcpyAsync(*sd, dV, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
@@ -1540,9 +1545,10 @@ oc_status oc_get_state(oc_solver* s, float* X, float* V, float* dV) {
     if (!valid_solver(s)) return OC_ERR_INVALID_ARGUMENT;
     OC_TRY(cudaSetDevice(s->device));
     const size_t n3 = 3 * (size_t)s->nv;
+    const size_t ps = stage_stride(s->nv);
     float* sx = X ? s->stage : nullptr;
-    float* sv = V ? s->stage + n3 : nullptr;
-    float* sd = dV ? s->stage + 2 * n3 : nullptr;
+    float* sv = V ? s->stage + ps : nullptr;
+    float* sd = dV ? s->stage + 2 * ps : nullptr;
     OC_TRY(launch_state_out(s->args, sx, sv, sd, s->nv, s->stream));
     if (X) OC_TRY(cudaMemcpyAsync(X, sx, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     if (V) OC_TRY(cudaMemcpyAsync(V, sv, n3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
@@ -2222,8 +2228,9 @@ oc_status oc_tape_backward(oc_solver* s, const float* dL_dX, const float* dL_dV,
     OC_TRY(launch_state_in(up, nullptr, nullptr, s->stage, s->nv, s->d_err, s->stream));
     if (dL_dV) {
         for (int k = 0; k < 3; ++k) up.x[k] = j.gV[k];
-        OC_TRY(cudaMemcpyAsync(s->stage + n3, dL_dV, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-        OC_TRY(launch_state_in(up, nullptr, nullptr, s->stage + n3, s->nv, s->d_err, s->stream));
+        float* sv = s->stage + stage_stride(s->nv);
+        OC_TRY(cudaMemcpyAsync(sv, dL_dV, n3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        OC_TRY(launch_state_in(up, nullptr, nullptr, sv, s->nv, s->d_err, s->stream));
     }
     if (!s->adj_persist && (!T.exec || T.graph_dt != T.dt)) {
         oc_status r = build_adjoint_graph(s, T.dt);

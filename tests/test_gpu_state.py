@@ -118,3 +118,40 @@ def test_set_state_rejects_non_finite_input_without_effect():
         assert e.value.status == 3
         for a, b in zip(before, s.get_state()):
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("cols,rows", [(33, 21), (16, 8), (5, 3)])
+def test_device_state_aligned_and_unaligned_give_the_same_bits(cols, rows):
+    """The device-pointer state functions take packed float triples at any 4-byte
+    alignment: 16-byte aligned and unaligned arrays round-trip the same bits, for vertex
+    counts that are and are not multiples of four, and agree with the host path."""
+    import torch
+
+    desc, _, X, V = seeded_cloth(cols, rows, seed=5, velocity=0.01)
+    dV = np.random.default_rng(7).normal(0.0, 1e-3, X.shape).astype(np.float32)
+    n3 = X.size
+    sp = (n3 + 8 + 3) // 4 * 4  # floats between the arrays: a multiple of four
+    res = {}
+    for off in (0, 1):  # floats of offset: 0 keeps 16-byte alignment, 1 breaks it
+        buf = torch.zeros(3 * sp, dtype=torch.float32, device="cuda")
+        ins = [buf[k * sp + off: k * sp + off + n3] for k in range(3)]
+        for t, a in zip(ins, (X, V, dV)):
+            t.copy_(torch.from_numpy(a.reshape(-1)))
+        assert all((t.data_ptr() % 16 == 0) == (off == 0) for t in ins)
+        with ClothSolver(desc) as s:
+            s.set_state_device(ins[0].data_ptr(), ins[1].data_ptr(), ins[2].data_ptr())
+            s.synchronize()
+            Xh, Vh, dVh = s.get_state()
+            assert np.array_equal(Xh, X) and np.array_equal(Vh, V) and np.array_equal(dVh, dV)
+            s.step(DT, 3)
+            out = torch.zeros(3 * sp, dtype=torch.float32, device="cuda")
+            outs = [out[k * sp + off: k * sp + off + n3] for k in range(3)]
+            s.get_state_device(outs[0].data_ptr(), outs[1].data_ptr(), outs[2].data_ptr())
+            s.synchronize()
+            got = [t.cpu().numpy().reshape(-1, 3) for t in outs]
+            ref = s.get_state()
+            for g, r in zip(got, ref):
+                assert np.array_equal(g.view(np.uint32), np.asarray(r).view(np.uint32))
+            res[off] = got
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
