@@ -89,7 +89,7 @@ struct oc_solver {
     // when there is no COUPLED cloth; otherwise the WHILE loop.
     bool persist = false;
     int persist_grid = 0;
-    unsigned* d_words = nullptr;  // k_cg_persist: one completion word per cloth
+    unsigned* d_words = nullptr;  // k_cg_persist: one arrival count per cloth
     int* d_perr = nullptr;        // bit 0: a wait of k_cg_persist gave up
     // The adjoint solve (every cloth iterates) as one cooperative launch of k_cg_persist
     // without the update, when the handle has no COUPLED cloth.
@@ -180,14 +180,14 @@ oc_status fail_cuda(oc_solver* s, cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return fail_cuda(s, e_, #call); \
     } while (0)
 
-// Polls of a cloth's completion word before a wait of k_cg_persist gives up (about half
+// Polls of a cloth's arrival count before a wait of k_cg_persist gives up (about half
 // a second with its 32 ns back-off).
 constexpr uint32_t kDefaultBarrierPolls = 1u << 22;
 
 // A wait of k_cg_persist that gave up (the stream is synchronised).  The error word is
-// cleared once reported and the cloths' CG state (whose tickets the abandoned launch
-// left part-counted) is zeroed: every step's assembly sets it up again, and the next
-// launch starts from zeroed completion words, so the handle steps on.
+// cleared once reported and the cloths' CG state (which the abandoned launch left part
+// updated) is zeroed: every step's assembly sets it up again, and the next launch starts
+// from zeroed arrival counts, so the handle steps on.
 oc_status check_device_error(oc_solver* s) {
     if (!s->d_perr) return OC_OK;
     int h = 0;
@@ -201,7 +201,7 @@ oc_status check_device_error(oc_solver* s) {
     return OC_OK;
 }
 
-// k_cg_persist over block table a.blocks[0, n): its cloths' completion words zeroed, then
+// k_cg_persist over block table a.blocks[0, n): its cloths' arrival counts zeroed, then
 // the cooperative launch.
 cudaError_t persist_cg(oc_solver* s, const StepArgs& a, int32_t n, int grid) {
     cudaError_t e = cudaMemsetAsync(s->d_words, 0, sizeof(unsigned) * (size_t)s->n_inst, s->stream);
@@ -1333,7 +1333,8 @@ oc_status oc_create(const oc_cloth_desc* descs, int32_t n_instances, const oc_op
         a.r[k] = planes + (9 + k) * stride;
         a.d[k] = planes + (12 + k) * stride;
     }
-    OC_CREATE_TRY(dalloc(s, &a.partials, P.blocks.size()));
+    OC_CREATE_TRY(dalloc(s, &a.partials, 2 * P.blocks.size()));
+    a.partials_b = a.partials + P.blocks.size();
     InstParams* inst = nullptr;
     OC_CREATE_TRY(upload(s, &inst, P.inst));
     a.inst = inst;

@@ -94,6 +94,7 @@ struct StepArgs {
     float* r[3];
     float* d[3];
     double* partials;        // one per streamed block
+    double* partials_b;      // a second set (the persistent CG's phases of odd parity)
     const InstParams* inst;
     InstState* state;
     const BlockInfo* blocks;
@@ -107,7 +108,7 @@ struct StepArgs {
     unsigned long long cond; // cudaGraphConditionalHandle
     int32_t all_streamed;    // 1: every cloth's CG runs in the streamed loop (adjoint solves)
     int32_t cg_only;         // k_cg_persist: 1 = the CG alone, no update (adjoint solves)
-    // k_cg_persist's waits: polls of a cloth's completion word before a wait gives up,
+    // k_cg_persist's waits: polls of a cloth's arrival count before a wait gives up,
     // and a block that never arrives (-1: none; set only by oc_test_barrier_timeout).
     uint32_t barrier_polls;
     int32_t withhold_block;
@@ -245,9 +246,10 @@ enum KernelKind { K_ASSEMBLE = 0, K_CG_DIR = 1, K_CG_UPDATE = 2, K_INTEGRATE = 3
 
 // The whole CG loop of the cloths of block table a.blocks[0, n_entries) in one
 // cooperative launch of `grid` blocks (oc_kernels.cu), any number of cloths; a block
-// owns at most persist_max_entries_per_block() entries.  words: one completion word per
-// cloth of the handle, indexed by cloth, zeroed before each launch; the cloths' tickets
-// start at zero (the assembly epilogue leaves them so).  err: bit 0 set if a wait gave up.
+// owns at most persist_max_entries_per_block() entries.  words: one arrival count per
+// cloth of the handle, indexed by cloth, zeroed before each launch.  The per-block
+// partials are double buffered (StepArgs::partials, partials_b).  err: bit 0 set if a
+// wait gave up.
 int persist_max_entries_per_block();
 int persist_blocks_per_sm();
 cudaError_t launch_test_cr_arith(unsigned long long* counts, uint64_t n_pairs, uint64_t seed, cudaStream_t stream);

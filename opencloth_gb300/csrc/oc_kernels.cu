@@ -9,7 +9,7 @@
 //   k_cg_dir     [d = r + beta d]; alpha = delta_new / d.(A d)    (IMP:320-321, 327)
 //   k_cg_update  x += alpha d; r -= alpha A d; delta_new = r.r     (IMP:322-326)
 //   k_cg_persist the CG loop of any number of cloths and their update in one
-//                cooperative launch (the two passes above, per-cloth completion words)
+//                cooperative launch (the two passes above, per-cloth arrival counts)
 //   k_integrate  V += dV dt; X += dt V; ground clamp               (IMP:790-797)
 //                [+ EllipsoidCollision, IMP:824-848]
 //   k_provot     ApplyProvotDynamicInverse as a per-vertex gather   (IMP:800-823)
@@ -659,25 +659,27 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(const StepArgs a) {
 // owns the table entries b, b + grid, b + 2 grid, ... and runs on them the same
 // per-block passes as k_cg_dir / k_cg_update, writing the same per-block partials.
 //
-// The cloths are independent, so there is no grid barrier: each cloth has its own
-// completion word.  Phase q of a cloth is the direction pass (q even) or the update pass
-// (q odd) of iteration q / 2.  An entry's pass of phase q starts once its cloth's word
-// reads at least q (phase q - 1 complete).  The entries then arrive at their cloth's
-// ticket (a block's consecutive entries of one cloth with one atomic add of their
-// count); the block that makes the cloth's last arrival of the phase sums the cloth's
-// partials in the last-block epilogue's fixed order, applies the epilogue's scalar rule
-// to the cloth's state and publishes the word (q + 1, or kPhaseDone when the cloth's
-// loop has ended).  Totals, scalars and decisions are those of the two-kernel loop bit
-// for bit.  Progress: a pass of phase q waits only on phase q - 1 of its own cloths,
-// whose arrivals every block makes before any of its phase-q work, so by induction on q
-// every phase completes.  A wait gives up after a.barrier_polls polls (the default,
+// The cloths are independent, so there is no grid barrier: each cloth has its own word,
+// which counts the arrivals of its entries (it is never reset within the launch).  Phase
+// q of a cloth is the direction pass (q even) or the update pass (q odd) of iteration
+// q / 2.  Phase q - 1 of cloth c is complete once c's word reaches q nblk(c).  Then every
+// block that owns entries of c sums c's partials of phase q - 1 itself, in the
+// last-block epilogue's fixed order, and applies the epilogue's scalar rule to its own
+// copy of c's scalars in shared memory: all blocks compute the same totals and take the
+// same decisions, with no last block that has to publish them first.  The partials are
+// double buffered by phase parity: a block writes phase q + 1's only after phase q is
+// complete, that is after every block has read phase q - 1's.  The block owning c's first
+// entry writes c's state for the host.  Totals, scalars and decisions are those of the
+// two-kernel loop bit for bit.  Progress: a block waits at phase q only for cloths it
+// still runs, every owner of a running cloth makes its phase q - 1 arrival (one release
+// add per run of its consecutive entries of that cloth) before its phase-q wait, and all
+// blocks are co-resident.  A wait gives up after a.barrier_polls polls (the default,
 // 2^22 polls with a 32 ns back-off, is about half a second) or when another block has
 // given up: it sets bit 0 of *err and the block returns without its update.  The block
-// a.withhold_block (a testing aid; normally -1) returns before its first arrival, so
-// the waits on its cloths run out.
+// a.withhold_block (a testing aid; normally -1) returns before its first arrival, so the
+// waits on its cloths run out.
 
 constexpr int kPersistMaxOwn = kThreads;  // table entries one block owns (one waiting thread each)
-constexpr unsigned kPhaseDone = 0xffffffffu;
 
 __device__ __forceinline__ unsigned load_acquire(const unsigned* p) {
     unsigned v;
@@ -697,86 +699,118 @@ __device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned x) {
     return v;
 }
 
-__device__ __forceinline__ void store_release(unsigned* p, unsigned x) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(x) : "memory");
-}
-
-// Wait until *word >= q; false when the wait gave up (poll limit, or *err already set).
-__device__ bool wait_phase(const StepArgs& a, const unsigned* word, unsigned q, const int* err) {
-    unsigned spins = 0;
-    while (load_acquire(word) < q) {
-        if (++spins > a.barrier_polls || ((spins & 63u) == 0 && load_relaxed(err) != 0)) return false;
-        __nanosleep(32);
-    }
-    return true;
-}
-
-// The scalar rules of finish<K_CG_DIR> / finish<K_CG_UPDATE> on one cloth's state.  The
-// state was last written by whichever block completed the previous phase, so it is read
-// from L2 (__ldcg): this SM's L1 may hold an older copy.  Returns whether the cloth's
-// loop goes on.
-__device__ bool apply_rule(InstState& st, const InstParams& ip, bool dir, double total) {
-    const double delta_new = __ldcg(&st.delta_new);
-    uint32_t flags = __ldcg(&st.flags);
-    if (dir) {
-        st.dq = total;
-        if (!(total > 0.0) || !isfinite(total)) {
-            st.flags = flags | (isfinite(total) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE);
-            st.active = 0;
-            return false;
-        }
-        st.alpha = (float)(delta_new / total);
-        return true;
-    }
-    const double delta0 = __ldcg(&st.delta0);
-    const int32_t iter = __ldcg(&st.iter) + 1;
-    st.delta_new = total;
-    st.beta = (float)(total / delta_new);
-    st.iter = iter;
-    const bool more = iter < ip.imax && total > (double)ip.eps2 * delta0;
-    if (!isfinite(total)) flags |= OC_FLAG_NON_FINITE;
-    if (!more || !isfinite(total)) {
-        if (isfinite(total) && total > (double)ip.eps2 * delta0) flags |= OC_FLAG_NOT_CONVERGED;
-        st.active = 0;
-    }
-    st.flags = flags;
-    return more && isfinite(total);
-}
-
 __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, int32_t n_entries, unsigned* words,
                                                             int* err) {
     __shared__ double s_part[kPersistMaxOwn];
-    __shared__ float s_scal[kPersistMaxOwn];      // beta (direction pass) or alpha (update pass)
-    __shared__ unsigned char s_run[kPersistMaxOwn];  // 0 idle, 1 runs, 2 runs its first direction pass
-    __shared__ short s_last[kPersistMaxOwn];      // owned entries whose arrival completed a phase
-    __shared__ int s_nlast, s_any, s_ok;
+    __shared__ double s_dn[kPersistMaxOwn], s_d0[kPersistMaxOwn];  // delta_new, delta0
+    __shared__ float s_scal[kPersistMaxOwn];                        // beta or alpha for the next pass
+    __shared__ int s_it[kPersistMaxOwn];
+    __shared__ uint32_t s_fl[kPersistMaxOwn];
+    __shared__ unsigned char s_run[kPersistMaxOwn];  // 0 stopped, 1 runs, 2 runs its first direction pass
+    __shared__ unsigned char s_head[kPersistMaxOwn];  // first owned entry of a run of one cloth
+    __shared__ int s_any, s_ok;
     const int own = ((int)n_entries - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
     if (threadIdx.x == 0) s_ok = 1;
+    for (int j = threadIdx.x; j < own; j += blockDim.x) {
+        const int inst = a.blocks[blockIdx.x + j * gridDim.x].inst;
+        const InstState& st = a.state[inst];
+        s_head[j] = (j == 0 || a.blocks[blockIdx.x + (j - 1) * gridDim.x].inst != inst) ? 1 : 0;
+        s_run[j] = __ldcg(&st.active) ? 2 : 0;
+        s_dn[j] = __ldcg(&st.delta_new);
+        s_d0[j] = __ldcg(&st.delta0);
+        s_it[j] = __ldcg(&st.iter);
+        s_fl[j] = __ldcg(&st.flags);
+        s_scal[j] = 0.0f;
+    }
+    __syncthreads();
     for (unsigned q = 0;; ++q) {
         const bool dir = (q & 1u) == 0u;
-        if (threadIdx.x == 0) {
-            s_any = 0;
-            s_nlast = 0;
-        }
-        __syncthreads();
-        // Each owned entry's cloth has completed phase q - 1: its state is final for q.
-        for (int j = threadIdx.x; j < own; j += blockDim.x) {
-            const int inst = a.blocks[blockIdx.x + j * gridDim.x].inst;
-            s_run[j] = 0;
-            if (!wait_phase(a, words + inst, q, err)) {
-                atomicOr(err, 1);
-                s_ok = 0;
-                continue;
+        if (q > 0) {
+            // Phase q - 1 of every running cloth: wait for its arrivals (one thread per run).
+            for (int j = threadIdx.x; j < own; j += blockDim.x) {
+                if (!s_run[j] || !s_head[j]) continue;
+                const BlockInfo bi = a.blocks[blockIdx.x + j * gridDim.x];
+                const unsigned need = q * (unsigned)a.inst[bi.inst].nblk;
+                unsigned spins = 0;
+                while ((int)(load_acquire(words + bi.inst) - need) < 0) {
+                    if (++spins > a.barrier_polls || ((spins & 63u) == 0 && load_relaxed(err) != 0)) {
+                        atomicOr(err, 1);
+                        s_ok = 0;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
             }
-            const InstState& st = a.state[inst];
-            if (__ldcg(&st.active) == 0) continue;
-            s_run[j] = (dir && __ldcg(&st.iter) == 0) ? 2 : 1;
-            s_scal[j] = dir ? __ldcg(&st.beta) : __ldcg(&st.alpha);
-            s_any = 1;
+            __syncthreads();
+            if (!s_ok) break;
+            // Totals and rule of phase q - 1, per run of one cloth, in every block.
+            const double* prev = (q & 1u) ? a.partials : a.partials_b;
+            for (int j = 0; j < own; ++j) {
+                if (!s_run[j] || !s_head[j]) continue;
+                const int inst = a.blocks[blockIdx.x + j * gridDim.x].inst;
+                const InstParams& ip = a.inst[inst];
+                double acc = 0.0;
+#pragma unroll 8
+                for (int k = threadIdx.x; k < ip.nblk; k += blockDim.x) acc += __ldcg(prev + ip.blk0 + k);
+                const double total = block_sum(acc);
+                if (threadIdx.x == 0) {
+                    uint32_t fl = s_fl[j];
+                    int it = s_it[j];
+                    double dn = s_dn[j];
+                    float scal = 0.0f;
+                    bool run = true;
+                    if (!dir) {  // phase q - 1 was a direction pass: d.(A d) -> alpha
+                        if (!(total > 0.0) || !isfinite(total)) {
+                            fl |= isfinite(total) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
+                            run = false;
+                        } else {
+                            scal = (float)(dn / total);
+                        }
+                    } else {  // an update pass: r.r -> beta, the stop test
+                        it += 1;
+                        scal = (float)(total / dn);
+                        dn = total;
+                        const bool more = it < ip.imax && total > (double)ip.eps2 * s_d0[j];
+                        if (!isfinite(total)) fl |= OC_FLAG_NON_FINITE;
+                        if (!more || !isfinite(total)) {
+                            if (isfinite(total) && total > (double)ip.eps2 * s_d0[j]) fl |= OC_FLAG_NOT_CONVERGED;
+                            run = false;
+                        }
+                    }
+                    // The run's entries share the cloth's copy.
+                    for (int k = j; k < own && (k == j || !s_head[k]); ++k) {
+                        s_fl[k] = fl;
+                        s_it[k] = it;
+                        s_dn[k] = dn;
+                        s_scal[k] = scal;
+                        s_run[k] = run ? 1 : 0;
+                    }
+                    if (a.blocks[blockIdx.x + j * gridDim.x].gblk == ip.blk0) {  // the cloth's first entry
+                        InstState& st = a.state[inst];
+                        if (!dir) {
+                            st.dq = total;
+                            if (run) st.alpha = scal;
+                        } else {
+                            st.delta_new = dn;
+                            st.beta = scal;
+                            st.iter = it;
+                        }
+                        st.flags = fl;
+                        if (!run) st.active = 0;
+                        st.ticket = 0;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        if (threadIdx.x == 0) {
+            int any = 0;
+            for (int j = 0; j < own; ++j) any |= s_run[j];
+            s_any = any;
         }
         __syncthreads();
-        if (!s_ok || !s_any) break;
-        // The passes (k_cg_dir / k_cg_update) of the owned entries that run.
+        if (!s_any) break;
+        // The passes of the owned entries that run, as k_cg_persist's.
         for (int j = 0; j < own; ++j) {
             if (!s_run[j]) continue;
             const BlockInfo bi = a.blocks[blockIdx.x + j * gridDim.x];
@@ -789,45 +823,27 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, in
             s_ok = 0;
             break;
         }
-        // Arrivals: the owned entries of one cloth are consecutive (the table is in cloth
-        // order), so the thread of a run's first entry publishes the run's partials and
-        // arrives once at the cloth's ticket with the run's length.
+        // Arrivals: the partials of phase q into the buffer of its parity, then one release
+        // add per run of one cloth.
+        double* cur = (q & 1u) ? a.partials_b : a.partials;
         for (int j = threadIdx.x; j < own; j += blockDim.x) {
-            if (!s_run[j]) continue;
+            if (!s_run[j] || !s_head[j]) continue;
             const int inst = a.blocks[blockIdx.x + j * gridDim.x].inst;
-            if (j > 0 && a.blocks[blockIdx.x + (j - 1) * gridDim.x].inst == inst) continue;
             unsigned n = 0;
             for (int k = j; k < own; ++k) {
                 const BlockInfo bk = a.blocks[blockIdx.x + k * gridDim.x];
                 if (bk.inst != inst) break;
-                a.partials[bk.gblk] = s_part[k];
+                cur[bk.gblk] = s_part[k];
                 ++n;
             }
-            const unsigned t = atom_add_acq_rel(&a.state[inst].ticket, n);
-            if (t + n == (unsigned)a.inst[inst].nblk) s_last[atomicAdd(&s_nlast, 1)] = (short)j;
+            atom_add_acq_rel(words + inst, n);
         }
         __syncthreads();
-        // The cloths this block completed: totals in the epilogue's order, rule, publish.
-        const int n_last = s_nlast;
-        for (int l = 0; l < n_last; ++l) {
-            const int inst = a.blocks[blockIdx.x + s_last[l] * gridDim.x].inst;
-            const InstParams& ip = a.inst[inst];
-            __threadfence();
-            double acc = 0.0;
-#pragma unroll 8
-            for (int j = threadIdx.x; j < ip.nblk; j += blockDim.x) acc += __ldcg(a.partials + ip.blk0 + j);
-            const double total = block_sum(acc);
-            if (threadIdx.x == 0) {
-                InstState& st = a.state[inst];
-                st.ticket = 0;
-                const bool go_on = apply_rule(st, ip, dir, total);
-                store_release(words + inst, go_on ? q + 1u : kPhaseDone);
-            }
-        }
+        if (threadIdx.x == 0)
+            for (int j = 0; j < own; ++j)
+                if (s_run[j] == 2) s_run[j] = 1;
         __syncthreads();
     }
-    // The update of the owned entries (k_integrate): per vertex, after every owned cloth's
-    // loop has ended.  An adjoint solve (cg_only) stops at the solution.
     if (s_ok && !a.cg_only) {
         for (int32_t e = blockIdx.x; e < n_entries; e += gridDim.x) {
             const BlockInfo bi = a.blocks[e];
