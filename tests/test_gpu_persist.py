@@ -7,7 +7,8 @@ import os
 import numpy as np
 import pytest
 
-from opencloth_gb300 import PASS_ELLIPSOID, PASS_PROVOT, ClothDesc, ClothSolver, grid_cloth, reference_ellipsoid
+from opencloth_gb300 import (FLAG_BREAKDOWN, FLAG_NON_FINITE, PASS_ELLIPSOID, PASS_PROVOT, ClothDesc, ClothSolver,
+                             grid_cloth, reference_ellipsoid)
 
 pytestmark = pytest.mark.gpu
 
@@ -152,3 +153,35 @@ def test_barrier_wait_runs_out_and_the_handle_steps_on():
         for a, b in zip(s.get_state(), t.get_state()):
             assert same_bits(a, b)
         assert np.array_equal(s.stats()[0], t.stats()[0])
+
+
+def test_stop_rules_per_cloth():
+    """Streamed cloths that end their loops for every reason the scalar rule has, in one
+    launch: converged, the iteration cap (OC_FLAG_NOT_CONVERGED after one iteration), no
+    iterations at all (cg_max_iter 0) and an indefinite system (a stiffness whose h^2 Ks
+    exceeds the mass, which breaks the CG down or ends it early).  Every block forms each
+    cloth's totals and decisions itself; they must be the two-kernel loop's bits, flags
+    and iteration counts."""
+    specs = [(70, 60, 200, 1e-5, 50.0), (64, 52, 1, 1e-9, 50.0), (58, 66, 0, 1e-5, 50.0), (61, 57, 50, 1e-9, 5e5),
+             (75, 40, 200, 1e-6, 20.0)]
+    descs, Xs, Vs = [], [], []
+    for k, (cols, rows, imax, tol, ks) in enumerate(specs):
+        rng = np.random.default_rng(300 + k)
+        X, sp = grid_cloth(cols, rows, ks=(ks, ks, ks), kd=(-0.25, -0.25, -0.25), jitter=1e-2, seed=300 + k)
+        V = rng.normal(0.0, 0.05, X.shape).astype(np.float32)
+        V[[0, cols - 1]] = 0.0
+        descs.append(ClothDesc(n_vertices=cols * rows, springs=sp, pinned=np.array([0, cols - 1], np.int32),
+                               cg_max_iter=imax, cg_tol=tol))
+        Xs.append(X)
+        Vs.append(V)
+    X, V = np.concatenate(Xs), np.concatenate(Vs)
+    a, sa = run(descs, X, V, 2, True, executor="streamed")
+    b, sb = run(descs, X, V, 2, False, executor="streamed")
+    for x, y in zip(a, b):
+        assert same_bits(x, y)
+    assert np.array_equal(sa[0], sb[0]) and np.array_equal(sa[2], sb[2])
+    it, _, fl = sa
+    assert it[1] == 1 and fl[1] & 1  # OC_FLAG_NOT_CONVERGED
+    assert it[2] == 0
+    assert fl[3] & (FLAG_BREAKDOWN | FLAG_NON_FINITE) or it[3] < 50
+    assert it[0] > 1 and fl[0] == 0 and it[4] > 1
