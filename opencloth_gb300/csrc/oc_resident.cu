@@ -120,6 +120,11 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
     // pairs); the other threads get alpha, beta and the go / stop decision.
     __shared__ float s_alpha, s_beta;
     __shared__ int s_go;
+    // Thread 0's scalars, in shared memory rather than in every thread's registers:
+    // delta0 (FP64, set once), the iteration's r.r and threshold as pairs, the flags.
+    __shared__ double s_delta0;
+    __shared__ Acc s_delta, s_thresh;
+    __shared__ uint32_t s_flags;
     const int C = L.cluster;
     const int rank = (C > 1) ? (int)cgx::this_cluster().block_rank() : 0;
     const int inst = L.inst_ids[blockIdx.x / C];
@@ -142,10 +147,10 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
 
     int phase = 0;
     Acc part;
-    // Thread 0's: delta0 (FP64, set once), and the iteration's r.r and threshold as pairs.
-    double delta0 = 0.0;
-    Acc delta = acc_zero(), thresh = acc_zero();
-    uint32_t flags = 0u;                             // thread 0's
+    if (threadIdx.x == 0) {
+        s_delta0 = 0.0;
+        s_flags = 0u;
+    }
     if constexpr (FUSED) {
         // The assembly of these vertices (k_assemble / k_assemble_grid); X and V are
         // written at the end of this kernel, so they are read with plain loads.
@@ -177,10 +182,10 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
         const Acc tp = pair_norm(cluster_sum(part, C, slots, phase));
         if (threadIdx.x == 0) {
             const double total = (double)tp.s + (double)tp.c;
-            delta0 = total;
+            s_delta0 = total;
             bool run = (0 < ip.imax) && (total > (double)ip.eps2 * total);
             if (!isfinite(total)) {
-                flags |= OC_FLAG_NON_FINITE;
+                s_flags |= OC_FLAG_NON_FINITE;
                 run = false;
             }
             s_go = run ? 1 : 0;
@@ -204,16 +209,16 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
         }
         if (threadIdx.x == 0) {
             const InstState& st0 = a.state[inst];
-            delta0 = st0.delta0;
-            flags = st0.flags;
+            s_delta0 = st0.delta0;
+            s_flags = st0.flags;
             s_go = st0.active != 0 ? 1 : 0;
         }
     }
     __syncthreads();
     bool run = s_go != 0;
     if (threadIdx.x == 0) {
-        delta = pair_from(delta0);
-        thresh = pair_from((double)ip.eps2 * delta0);
+        s_delta = pair_from(s_delta0);
+        s_thresh = pair_from((double)ip.eps2 * s_delta0);
     }
     int it = 0;
     float beta = 0.0f;
@@ -237,10 +242,10 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
         const Acc dq = pair_norm(cluster_sum(part, C, slots, phase));
         if (threadIdx.x == 0) {
             if (!(dq.s > 0.0f) || !pair_finite(dq)) {
-                flags |= pair_finite(dq) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
+                s_flags |= pair_finite(dq) ? OC_FLAG_BREAKDOWN : OC_FLAG_NON_FINITE;
                 s_go = 0;
             } else {
-                s_alpha = pair_div(delta, dq);
+                s_alpha = pair_div(s_delta, dq);
                 s_go = 1;
             }
         }
@@ -266,15 +271,16 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
         const Acc rr = pair_norm(cluster_sum(part, C, slots, phase));
         ++it;
         if (threadIdx.x == 0) {
-            const Acc old = delta;
-            delta = rr;
+            const Acc old = s_delta, thresh = s_thresh;
+            const Acc delta = rr;
+            s_delta = delta;
             s_beta = pair_div(delta, old);
             int go = 1;
             if (!pair_finite(delta)) {
-                flags |= OC_FLAG_NON_FINITE;
+                s_flags |= OC_FLAG_NON_FINITE;
                 go = 0;
             } else if (!(it < ip.imax && pair_gt(delta, thresh))) {
-                if (pair_gt(delta, thresh)) flags |= OC_FLAG_NOT_CONVERGED;
+                if (pair_gt(delta, thresh)) s_flags |= OC_FLAG_NOT_CONVERGED;
                 go = 0;
             }
             s_go = go;
@@ -304,11 +310,11 @@ __global__ void __launch_bounds__(T, resident_min_blocks<T>()) k_resident(const 
     }
     if (rank == 0 && threadIdx.x == 0) {
         InstState& st = a.state[inst];
-        st.delta0 = delta0;
-        st.delta_new = (double)delta.s + (double)delta.c;
+        st.delta0 = s_delta0;
+        st.delta_new = (double)s_delta.s + (double)s_delta.c;
         st.dq = 0.0;
         st.iter = it;
-        st.flags = flags;
+        st.flags = s_flags;
         st.active = 0;
         st.alpha = 0.0f;
         st.beta = beta;
