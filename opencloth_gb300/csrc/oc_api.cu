@@ -89,6 +89,9 @@ struct oc_solver {
     // when there is no COUPLED cloth; otherwise the WHILE loop.
     bool persist = false;
     int persist_grid = 0;
+    // k_assemble_finish runs when a strip-swept cloth is resident or the streamed CG is
+    // not the persistent one; otherwise k_cg_persist forms their delta0 itself.
+    bool strip_finish = true;
     unsigned* d_words = nullptr;  // k_cg_persist: one arrival count per cloth
     int* d_perr = nullptr;        // bit 0: a wait of k_cg_persist gave up
     // The adjoint solve (every cloth iterates) as one cooperative launch of k_cg_persist
@@ -476,8 +479,11 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
         }
         if (s->args.n_strip_work > 0) {
             if ((st = launch_timed(s, K_ASSEMBLE_STRIP, a, strip_blocks(a.n_strip_work), t)) != OC_OK) return st;
-            if ((st = launch_timed(s, K_ASSEMBLE_FINISH, a, a.n_strip_ids, t)) != OC_OK) return st;
-            s->host_launches += 2;
+            s->host_launches += 1;
+            if (s->strip_finish) {
+                if ((st = launch_timed(s, K_ASSEMBLE_FINISH, a, a.n_strip_ids, t)) != OC_OK) return st;
+                s->host_launches += 1;
+            }
         }
         if (s->n_cpl_blocks > 0) {
             if ((st = launch_timed(s, K_CPL_ASSEMBLE, ca, s->n_cpl_blocks, t)) != OC_OK) return st;
@@ -487,6 +493,7 @@ oc_status step_host_driven(oc_solver* s, float dt, bool per_cloth, KernelTimer* 
         const int nb = s->n_streamed_blocks, nc = s->n_cpl_blocks;
         if (s->persist) {
             if (t) OC_TRY(cudaEventRecord(t->ev[0], s->stream));
+            sa.persist_d0 = 1;
             OC_TRY(persist_cg(s, sa, nb, s->persist_grid));
             s->host_launches += 1;
             if (t) {
@@ -605,9 +612,11 @@ oc_status build_graph(oc_solver* s, float dt) {
         cudaGraphNode_t prev = n_asm;
         kp = kparams(K_ASSEMBLE_STRIP, T_STRIP);
         OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &prev, 1, &kp));
-        prev = n_asm;
-        kp = kparams(K_ASSEMBLE_FINISH, T_SFIN);
-        OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &prev, 1, &kp));
+        if (s->strip_finish) {
+            prev = n_asm;
+            kp = kparams(K_ASSEMBLE_FINISH, T_SFIN);
+            OC_TRY(cudaGraphAddKernelNode(&n_asm, g, &prev, 1, &kp));
+        }
     }
     cudaGraphNode_t n_last = n_asm;  // the loop waits for every assembly
     if (coupled) {
@@ -656,6 +665,7 @@ oc_status build_graph(oc_solver* s, float dt) {
         StepArgs pa = sa;
         pa.blocks = s->d_streamed_blocks;
         pa.use_cond = 0;
+        pa.persist_d0 = 1;
         cudaError_t le = persist_cg(s, pa, s->n_streamed_blocks, s->persist_grid);
         cudaError_t ce = cudaStreamEndCapture(s->stream, &pg);
         if (le != cudaSuccess || ce != cudaSuccess) {
@@ -1061,6 +1071,9 @@ oc_status plan_execution(oc_solver* s) {
         s->persist_grid = pgrid;
         if (oc_status r = alloc_persist_words(s)) return r;
     }
+    s->strip_finish = false;
+    for (int32_t k = 0; k < s->n_inst; ++k)
+        if (s->inst_host[(size_t)k].strip && (s->resident[(size_t)k] || !s->persist)) s->strip_finish = true;
     drop_graphs(s);
     return OC_OK;
 }
@@ -1601,7 +1614,7 @@ oc_status oc_step(oc_solver* s, float dt, int32_t n_steps) {
     // the resident launches and the Provot pass; the WHILE loop's launches are counted on
     // the device (loop_count).
     const int64_t per_step = (s->n_asm_blocks > 0 ? 1 : 0) + (s->n_grid_blocks > 0 ? 1 : 0) +
-                             (s->args.n_strip_work > 0 ? 2 : 0) + (s->n_cpl_blocks > 0 ? 1 : 0) +
+                             (s->args.n_strip_work > 0 ? (s->strip_finish ? 2 : 1) : 0) + (s->n_cpl_blocks > 0 ? 1 : 0) +
                              (s->persist ? 1 : (s->n_upd_blocks > 0 ? 1 : 0)) + (int64_t)s->buckets.size() +
                              (s->any_provot ? 1 : 0);
     s->host_launches += per_step * (int64_t)n_steps;
@@ -1821,6 +1834,7 @@ oc_status oc_profile_steps(oc_solver* s, float dt, int32_t n_steps, int32_t max_
         if (k == K_CG_PERSIST && !s->persist) continue;
         if ((k == K_CG_DIR || k == K_CG_UPDATE || k == K_INTEGRATE) && s->persist) continue;
         if ((k == K_ASSEMBLE_STRIP || k == K_ASSEMBLE_FINISH) && s->args.n_strip_work == 0) continue;
+        if (k == K_ASSEMBLE_FINISH && !s->strip_finish) continue;
         if (k == K_ASSEMBLE && s->n_asm_blocks == 0 && (s->n_grid_blocks > 0 || s->args.n_strip_work > 0)) continue;
         if (names) {
             std::memset(names + 32 * n, 0, 32);

@@ -108,6 +108,7 @@ struct StepArgs {
     unsigned long long cond; // cudaGraphConditionalHandle
     int32_t all_streamed;    // 1: every cloth's CG runs in the streamed loop (adjoint solves)
     int32_t cg_only;         // k_cg_persist: 1 = the CG alone, no update (adjoint solves)
+    int32_t persist_d0;      // k_cg_persist: 1 = it forms its strip-swept cloths' delta0 (the step's launch)
     // k_cg_persist's waits: polls of a cloth's arrival count before a wait gives up,
     // and a block that never arrives (-1: none; set only by oc_test_barrier_timeout).
     uint32_t barrier_polls;

@@ -443,12 +443,12 @@ __global__ void __launch_bounds__(kStripThreads, MINB) k_assemble_strip(const St
 // delta0 of a cloth on the strip sweep: one CTA per cloth sums its items' pairs in item
 // order (a fixed tree) and sets the CG scalars as finish<K_ASSEMBLE> does; the last CTA
 // sets the graph's WHILE condition.
-__global__ void __launch_bounds__(kThreads) k_assemble_finish(const StepArgs a) {
+// A strip-swept cloth's delta0: its work items' pairs merged in item order, eight in
+// flight per thread, then across the CTA in a fixed tree.  Every thread of the CTA must
+// call it; the result is valid in thread 0.
+__device__ double strip_delta0(const StepArgs& a, const InstParams& ip) {
     __shared__ Acc warp_part[kThreads / 32];
-    const int32_t inst = a.strip_ids[blockIdx.x];
-    const InstParams& ip = a.inst[inst];
     const float2* item_part = reinterpret_cast<const float2*>(a.strip_part) + ip.strip_w0;
-    // Eight items in flight per thread, merged in item order.
     Acc tot = acc_zero();
     for (int j0 = threadIdx.x; j0 < ip.strip_nw; j0 += 8 * blockDim.x) {
         float2 p[8];
@@ -466,12 +466,20 @@ __global__ void __launch_bounds__(kThreads) k_assemble_finish(const StepArgs a) 
     for (int o = 16; o > 0; o >>= 1) tot = acc_merge(tot, shfl_down_acc(tot, o));
     if (lane == 0) warp_part[w] = tot;
     __syncthreads();
-    if (w != 0) return;
-    tot = lane < (int)(blockDim.x >> 5) ? warp_part[lane] : acc_zero();
+    if (w == 0) {
+        tot = lane < (int)(blockDim.x >> 5) ? warp_part[lane] : acc_zero();
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) tot = acc_merge(tot, shfl_down_acc(tot, o));
-    if (lane == 0) {
-        const double total = (double)tot.s + (double)tot.c;
+        for (int o = 16; o > 0; o >>= 1) tot = acc_merge(tot, shfl_down_acc(tot, o));
+    }
+    __syncthreads();  // warp_part may be written again by a later call
+    return (double)tot.s + (double)tot.c;
+}
+
+__global__ void __launch_bounds__(kThreads) k_assemble_finish(const StepArgs a) {
+    const int32_t inst = a.strip_ids[blockIdx.x];
+    const InstParams& ip = a.inst[inst];
+    const double total = strip_delta0(a, ip);
+    if (threadIdx.x == 0) {
         InstState& st = a.state[inst];
         st.ticket = 0;
         st.delta0 = total;
@@ -722,6 +730,47 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, in
         s_scal[j] = 0.0f;
     }
     __syncthreads();
+    if (a.persist_d0) {
+        // The strip-swept cloths' delta0 and the decision to iterate, formed here as
+        // k_assemble_finish forms them (the step then launches that kernel only for the
+        // strip-swept cloths this launch does not run).
+        for (int j = 0; j < own; ++j) {
+            if (!s_head[j]) continue;
+            const BlockInfo bj = a.blocks[blockIdx.x + j * gridDim.x];
+            const InstParams& ip = a.inst[bj.inst];
+            if (!ip.strip) continue;
+            const double total = strip_delta0(a, ip);
+            if (threadIdx.x == 0) {
+                uint32_t fl = 0u;
+                bool run = (0 < ip.imax) && (total > (double)ip.eps2 * total);
+                if (!isfinite(total)) {
+                    fl |= OC_FLAG_NON_FINITE;
+                    run = false;
+                }
+                for (int k = j; k < own && (k == j || !s_head[k]); ++k) {
+                    s_run[k] = run ? 2 : 0;
+                    s_dn[k] = total;
+                    s_d0[k] = total;
+                    s_it[k] = 0;
+                    s_fl[k] = fl;
+                    s_scal[k] = 0.0f;
+                }
+                if (bj.gblk == ip.blk0) {
+                    InstState& st = a.state[bj.inst];
+                    st.ticket = 0;
+                    st.delta0 = total;
+                    st.delta_new = total;
+                    st.dq = 0.0;
+                    st.alpha = 0.0f;
+                    st.beta = 0.0f;
+                    st.iter = 0;
+                    st.flags = fl;
+                    st.active = run ? 1 : 0;
+                }
+            }
+            __syncthreads();
+        }
+    }
     for (unsigned q = 0;; ++q) {
         const bool dir = (q & 1u) == 0u;
         if (q > 0) {

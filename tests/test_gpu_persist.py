@@ -119,8 +119,8 @@ def test_launch_count_is_per_step():
         s.set_launch_config(strip=1)
         l0 = s.launch_count()
         s.step(DT, 5)
-        # with the strip sweep, its delta0 totals and the persistent CG
-        assert s.launch_count() - l0 == 15
+        # with the strip sweep and the persistent CG, which forms the sweep's delta0 itself
+        assert s.launch_count() - l0 == 10
 
 
 def test_barrier_wait_runs_out_and_the_handle_steps_on():

@@ -213,9 +213,16 @@ def test_strip_sweep_exact_spacing_and_passes():
 
 
 def test_strip_sweep_profile_names_its_kernels():
+    """Streamed cloths on the strip sweep: the persistent CG forms their delta0 itself, so
+    k_assemble_finish does not run; with the WHILE-loop CG (persist 0) it does."""
     descs, X, V = strip_batch(3)
     with ClothSolver(descs, executor="streamed") as s:
         s.set_launch_config(strip=1)
         s.set_state(X, V)
         prof = s.profile(DT, 2)
-    assert prof["k_assemble_strip"]["launches"] == 2 and prof["k_assemble_finish"]["launches"] == 2
+        assert prof["k_assemble_strip"]["launches"] == 2 and prof["k_cg_persist"]["launches"] == 2
+        assert "k_assemble_finish" not in prof
+        s.set_launch_config(persist=0)
+        s.set_state(X, V)
+        prof = s.profile(DT, 2)
+        assert prof["k_assemble_strip"]["launches"] == 2 and prof["k_assemble_finish"]["launches"] == 2
