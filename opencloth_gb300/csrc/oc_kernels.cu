@@ -528,6 +528,33 @@ __global__ void __launch_bounds__(kThreads) k_assemble_coop(const StepArgs a) {
     finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
 }
 
+// The update (IMP:790-797) over vertices [v0, v1) of one block, two vertices per thread:
+// both vertices' loads are issued before either is updated and stored.
+__device__ __forceinline__ void update_range(const StepArgs& a, const InstParams& ip, int64_t v0, int64_t v1) {
+    float4* __restrict__ X = a.X;
+    float4* __restrict__ V = a.V;
+    const float* __restrict__ D0 = a.x[0];
+    const float* __restrict__ D1 = a.x[1];
+    const float* __restrict__ D2 = a.x[2];
+    const int64_t T = blockDim.x;
+    for (int64_t g = v0 + threadIdx.x; g < v1; g += 2 * T) {
+        const int64_t h = g + T;
+        const bool ok = h < v1;
+        const int64_t hq = ok ? h : g;
+        float4 Xg = X[g], Vg = V[g], Xh = X[hq], Vh = V[hq];
+        const float g0 = D0[g], g1 = D1[g], g2 = D2[g];
+        const float h0 = D0[hq], h1 = D1[hq], h2 = D2[hq];
+        update_vertex(ip, a.dt, g0, g1, g2, Xg, Vg);
+        X[g] = Xg;
+        V[g] = Vg;
+        if (ok) {
+            update_vertex(ip, a.dt, h0, h1, h2, Xh, Vh);
+            X[h] = Xh;
+            V[h] = Vh;
+        }
+    }
+}
+
 // The CG passes stream fifteen FP32 planes.  Each thread keeps two vertices' loads in
 // flight (g and g + blockDim) before computing; __restrict__ lets the loads of the
 // next pair be issued ahead of this pair's stores.  The per-thread FP64 partial still
@@ -800,7 +827,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, in
                 double acc = 0.0;
 #pragma unroll 8
                 for (int k = threadIdx.x; k < ip.nblk; k += blockDim.x) acc += __ldcg(prev + ip.blk0 + k);
-                const double total = block_sum(acc);
+                const double total = block_sum_packed(acc);  // block_sum's bits (kThreads = 256)
                 if (threadIdx.x == 0) {
                     uint32_t fl = s_fl[j];
                     int it = s_it[j];
@@ -895,13 +922,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_cg_persist(const StepArgs a, in
     if (s_ok && !a.cg_only) {
         for (int32_t e = blockIdx.x; e < n_entries; e += gridDim.x) {
             const BlockInfo bi = a.blocks[e];
-            const InstParams& ip = a.inst[bi.inst];
-            for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
-                float4 Xg = a.X[g], Vg = a.V[g];
-                update_vertex(ip, a.dt, a.x[0][g], a.x[1][g], a.x[2][g], Xg, Vg);
-                a.X[g] = Xg;
-                a.V[g] = Vg;
-            }
+            update_range(a, a.inst[bi.inst], bi.v_begin, bi.v_end);
         }
     }
 }
@@ -998,14 +1019,7 @@ __global__ void k_snapshot(const float4* X, const float4* V, float4* dX, float4*
 __global__ void __launch_bounds__(kThreads) k_integrate(const StepArgs a) {
     const int blk = blockIdx.x + a.blk_base;
     const BlockInfo bi = a.blocks[blk];
-    const float dt = a.dt;
-    const InstParams& ip = a.inst[bi.inst];
-    for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
-        float4 Xg = a.X[g], Vg = a.V[g];
-        update_vertex(ip, dt, a.x[0][g], a.x[1][g], a.x[2][g], Xg, Vg);
-        a.X[g] = Xg;
-        a.V[g] = Vg;
-    }
+    update_range(a, a.inst[bi.inst], bi.v_begin, bi.v_end);
 }
 
 // ApplyProvotDynamicInverse (IMP:800-823) as a per-vertex gather.  The reference walks
