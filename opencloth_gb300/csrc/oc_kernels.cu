@@ -197,8 +197,10 @@ __global__ void __launch_bounds__(kThreads, MINB) k_assemble_grid(const StepArgs
     Acc part = acc_zero();
     for (int64_t g = bi.v_begin + threadIdx.x; g < bi.v_end; g += blockDim.x) {
         const float4 Xg = __ldg(a.X + g), Vg = __ldg(a.V + g);
+        const int2 ends = __ldg(a.own_ends + g);
+        prefetch_own(a, g, ends);  // into L1 while the forces are gathered
         const float3 F = B == 1 ? stencil_gather(a, ip, g, Xg, Vg) : stencil_gather_ahead<B>(a, ip, g, Xg, Vg);
-        acc_add(part, assemble_vertex(a, g, Xg, Vg, F, load_own(a, g)));
+        acc_add(part, assemble_vertex(a, g, Xg, Vg, F, load_own_at(a, g, ends)));
     }
     finish<K_ASSEMBLE>(a, bi.gblk, bi.inst, true, part);
 }
@@ -319,6 +321,9 @@ __global__ void __launch_bounds__(kStripThreads, MINB) k_assemble_strip(const St
             Vc = __ldg(Vcol + (int64_t)(r + 2) * cols);
         }
     }
+    // Spring i's ends of this row's vertex (own_ends, fetched a row ahead); its record and
+    // end states are prefetched into L1 at the start of the row and loaded after the forces.
+    int2 ends = colok ? __ldg(a.own_ends + vo + (int64_t)r * cols + c) : make_int2(-1, -1);
     float rs[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (has_rest && colok)
 #pragma unroll
@@ -336,6 +341,8 @@ __global__ void __launch_bounds__(kStripThreads, MINB) k_assemble_strip(const St
         if (has_rest && colok && r + 1 < w.r1)
 #pragma unroll
             for (int k = 0; k < 6; ++k) rn[k] = __ldg(rest + (size_t)k * nvk + (r + 1) * cols + c);
+        const int2 ends_next = (colok && r + 1 < w.r1) ? __ldg(a.own_ends + g + cols) : make_int2(-1, -1);
+        if (own) prefetch_own(a, g, ends);
         float4 Xd = zero4, Vd = zero4;
         if (colok && r + 3 < rows && r + 1 < w.r1) {
             Xd = __ldg(Xcol + (int64_t)(r + 3) * cols);
@@ -418,7 +425,7 @@ __global__ void __launch_bounds__(kStripThreads, MINB) k_assemble_strip(const St
         if (springs && r == rows - 1) sub3(Fx, Fy, Fz, fC2);
         if (own)  // spring i's record and end states, loaded here: held across the forces they spill
             acc_add(part, store_system(a, g, Va,
-                                       system_from(own_blocks(h, Xa.w, load_own(a, g)), h, Va, make_float3(Fx, Fy, Fz))));
+                                       system_from(own_blocks(h, Xa.w, load_own_at(a, g, ends)), h, Va, make_float3(Fx, Fy, Fz))));
         fC2 = fC1;
         fC1 = fC;
         fV1 = fV;
@@ -430,6 +437,7 @@ __global__ void __launch_bounds__(kStripThreads, MINB) k_assemble_strip(const St
         Vb = Vc;
         Xc = Xd;
         Vc = Vd;
+        ends = ends_next;
 #pragma unroll
         for (int k = 0; k < 6; ++k) rs[k] = rn[k];
     }
