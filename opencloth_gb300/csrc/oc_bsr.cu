@@ -343,8 +343,8 @@ constexpr int kResSlots = 4;    // slots of a row multiplied together in the res
 constexpr int kResMaxDeg = 64;  // blocks of a resident system's longest row (bounds the offset table)
 
 // The first half of block_sum_acc: each warp's pair, reduced by the same shuffle tree,
-// becomes one FP64 value in wacc[warp] (read after a barrier).
-__device__ __forceinline__ void warp_partial(Acc v, double* wacc) {
+// is stored in wacc[warp] (read after a barrier).
+__device__ __forceinline__ void warp_partial(Acc v, Acc* wacc) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         Acc u;
@@ -352,18 +352,23 @@ __device__ __forceinline__ void warp_partial(Acc v, double* wacc) {
         u.c = __shfl_down_sync(0xffffffffu, v.c, o);
         v = acc_merge(v, u);
     }
-    if ((threadIdx.x & 31) == 0) wacc[threadIdx.x >> 5] = (double)v.s + (double)v.c;
+    if ((threadIdx.x & 31) == 0) wacc[threadIdx.x >> 5] = v;
 }
 
-// The second half, by one thread: block_sum_acc's shuffle tree over at most 8 warp
-// values.  The tree's first two levels add zeros (lanes 8-31), which leaves each value
-// unchanged (a warp value is never -0: its pair starts at +0), so lane 0's result is
-// ((w0 + w4) + (w2 + w6)) + ((w1 + w5) + (w3 + w7)): the same bits.
-__device__ __forceinline__ double sum_warp_partials(const double* wacc, int nw) {
-    double w[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) w[i] = i < nw ? wacc[i] : 0.0;
-    return ((w[0] + w[4]) + (w[2] + w[6])) + ((w[1] + w[5]) + (w[3] + w[7]));
+// The second half, by warp 0 (every lane calls it; the result is valid in lane 0): lane i
+// turns warp i's pair into s + c in FP64, then block_sum_acc's shuffle tree over at most 8
+// warp values.  The tree's first two levels add zeros (lanes 8-31), which leaves each value
+// unchanged (a warp value is never -0: its pair starts at +0), so its result is
+// ((w0 + w4) + (w2 + w6)) + ((w1 + w5) + (w3 + w7)), formed here by three shuffle levels:
+// the same bits, with one FP64 warp instruction per conversion or level rather than one
+// per warp and a serial sum in one thread.
+__device__ __forceinline__ double sum_warp_pairs(const Acc* wacc, int nw) {
+    const int lane = threadIdx.x & 31;
+    double v = lane < nw ? (double)wacc[lane].s + (double)wacc[lane].c : 0.0;
+    v += __shfl_down_sync(0xffffffffu, v, 4);
+    v += __shfl_down_sync(0xffffffffu, v, 2);
+    v += __shfl_down_sync(0xffffffffu, v, 1);
+    return v;
 }
 
 // The whole solve of one small system in one CTA: the system's blocks are read once
@@ -384,8 +389,8 @@ __global__ void __launch_bounds__(kThreads) k_bsr_resident(const BsrArgs a, cons
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ float s_d3, s_d4;
     __shared__ int s_wcount[kThreads / 32];
-    __shared__ double s_w0[kThreads / 32], s_w1[kThreads / 32], s_w2[kThreads / 32];
-    static_assert(kThreads / 32 <= 8, "sum_warp_partials takes at most 8 warps");
+    __shared__ Acc s_w0[kThreads / 32], s_w1[kThreads / 32], s_w2[kThreads / 32];
+    static_assert(kThreads / 32 <= 8, "sum_warp_pairs takes at most 8 warps");
     float4* s_n4 = reinterpret_cast<float4*>(smem);
     float4* s_b0 = s_n4 + blockDim.x;
     float4* s_b1 = s_b0 + nnzb_max;
@@ -529,14 +534,16 @@ __global__ void __launch_bounds__(kThreads) k_bsr_resident(const BsrArgs a, cons
         if (first) warp_partial(pd, s_w0);
         warp_partial(pd2, s_w1);
         __syncthreads();
-        if (t == 0) {  // bsr_scalars<0>
-            const double t0 = first ? sum_warp_partials(s_w0, nw) : d1;
-            const double t1 = sum_warp_partials(s_w1, nw);
-            d = t0;
-            d2 = t1;
-            double dd2 = d2;
-            if (fabs(dd2) < tiny) dd2 = tiny;  // FEM:885-886
-            s_d3 = (float)(t0 / dd2);
+        if (w == 0) {  // bsr_scalars<0>, in thread 0
+            const double t0 = first ? sum_warp_pairs(s_w0, nw) : d1;
+            const double t1 = sum_warp_pairs(s_w1, nw);
+            if (t == 0) {
+                d = t0;
+                d2 = t1;
+                double dd2 = d2;
+                if (fabs(dd2) < tiny) dd2 = tiny;  // FEM:885-886
+                s_d3 = (float)(t0 / dd2);
+            }
         }
         __syncthreads();  // d3, and every row's reads of r and p are done
         d3 = s_d3;
@@ -556,12 +563,14 @@ __global__ void __launch_bounds__(kThreads) k_bsr_resident(const BsrArgs a, cons
         }
         warp_partial(pd1, s_w2);
         __syncthreads();
-        if (t == 0) {  // bsr_scalars<1>
-            const double t2 = sum_warp_partials(s_w2, nw);
-            d1 = t2;
-            double dd = d;
-            if (fabs(dd) < tiny) dd = tiny;  // FEM:908-909
-            s_d4 = (float)(t2 / dd);
+        if (w == 0) {  // bsr_scalars<1>, in thread 0
+            const double t2 = sum_warp_pairs(s_w2, nw);
+            if (t == 0) {
+                d1 = t2;
+                double dd = d;
+                if (fabs(dd) < tiny) dd = tiny;  // FEM:908-909
+                s_d4 = (float)(t2 / dd);
+            }
         }
         __syncthreads();
         d4 = s_d4;
